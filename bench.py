@@ -1,0 +1,357 @@
+"""Ghost-fill benchmark: GB/s of the fused fill on the sphere mesh, one GB300.
+
+Workload (the default): 3-D, 8^3 periodic roots, N = 16, G = 3, cell-centred,
+4 Float64 variables, point-value operators of order 4, three levels nested
+around the sphere |x - 1/2| = 0.25 (14,736 blocks, 5.0 GB of field data).
+A step is one whole ghost fill.  ``value`` counts the reference's algorithmic
+bytes (one read plus one write per ghost point-variable written,
+``bench/copies.jl:17-21``) per second with the field data resident in HBM;
+``e2e`` is the same through ``fill_ghosts`` with the field data copied from
+pinned host memory and back every step.  The field data (5 GB) are far larger
+than L2 (129 MB), so no flush is needed between steps.
+
+``--impl reference`` times the CPU restatement of the reference's threaded
+fill (the oracle, ``oracle/fill_oracle.c``) on this machine's host cores:
+the reference itself is Julia, which this machine does not have.
+
+Launch: ``python bench.py [--gpus N] [--steps K] [--warmup W]``; N > 1 under
+torchrun runs N independent replicas (the path does not shard on one GPU machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "treeamr.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ghost-fill GB/s (batched fused fill, algorithmic bytes)"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--method", choices=["fused", "plain"], default="fused")
+    ap.add_argument("--roots", type=int, default=8)
+    ap.add_argument("--levels", type=int, default=3)
+    ap.add_argument("--nvars", type=int, default=4)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(args, f, sched):
+    return {
+        "workload": "sphere: 3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, PV(4,4), "
+                    "3 levels nested around |x-1/2|=0.25" if (args.roots, args.levels, args.nvars) == (8, 3, 4)
+                    else f"sphere: {args.roots}^3 roots, {args.levels} levels, {args.nvars} vars",
+        "blocks": f.nleaves(),
+        "groups": len(sched.groups),
+        "ghost_points_per_var": int(sched.ghost_items(1)),
+        "nvars": args.nvars,
+        "field_bytes": None,
+        "l2": "inputs larger than L2 (5 GB field data vs 129 MB L2); no flush",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_fill_rate(sched, fs_host_work, nvars, factors, bytes_per_fill, budget_s=15.0,
+                  max_runs=5):
+    """The oracle's threaded fill on every host core: (GB/s, seconds per
+    fill, runs, threads)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    work = fs_host_work
+    oracle.fill(sched, work, nvars, factors, nthreads=threads)          # warm-up
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_runs and (time.perf_counter() - t_all) < budget_s:
+        t0 = time.perf_counter()
+        oracle.fill(sched, work, nvars, factors, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    best = min(times)
+    return bytes_per_fill / best / 1e9, best, len(times), threads
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+    from treeamr.ghosts import device_schedule
+    from treeamr import _native
+
+    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
+    fs = FieldSet(f, args.nvars, G=3, T=np.float64, device=dev)
+    ops = Operators(prolongation=4, restriction=4)
+    sched = GhostSchedule(fs, ops)
+    g = torch.Generator(device=dev).manual_seed(1 + rank)
+    fs.work.uniform_(-1.0, 1.0, generator=g)
+    cfg = workload_config(args, f, sched)
+    field_bytes = fs.work.numel() * fs.work.element_size()
+    cfg["field_bytes"] = field_bytes
+    nvars = args.nvars
+    points = sched.ghost_items(nvars)
+    bytes_per_fill = 2 * points * 8                     # one read + one write per point-variable
+    ds = device_schedule(sched, dev.index)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(fn, steps):
+        torch.cuda.synchronize(dev)
+        barrier()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        ms = a.elapsed_time(b)
+        if world > 1:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+    method = args.method
+    for _ in range(args.warmup):
+        fill_ghosts(fs, sched, method=method)
+    with ClockSampler(dev.index) as clk:
+        ms = timed(lambda: fill_ghosts(fs, sched, method=method), args.steps)
+    clocks = clk.summary()
+    value = world * bytes_per_fill / (ms * 1e-3) / 1e9
+
+    # the plain one-launch-per-group fill on the same data
+    for _ in range(max(1, args.warmup // 2)):
+        fill_ghosts(fs, sched, method="plain")
+    ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(3, args.steps // 2))
+    plain_value = world * bytes_per_fill / (ms_plain * 1e-3) / 1e9
+
+    # per-stage launches of the fused kernel, CUDA events on the launching stream
+    stage_ms = {}
+    stage_bytes = {}
+    tags = sorted({gr.stage for gr in sched.groups})
+    for tag in tags:
+        stage_bytes[tag] = 2 * 8 * nvars * sum(int(np.prod(gr.boxsize())) * gr.ntransfers()
+                                               for gr in sched.groups if gr.stage == tag)
+    reps = max(3, args.steps // 2)
+    evs = []
+    torch.cuda.synchronize(dev)
+    for _ in range(reps):
+        for tag in tags:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ds.run(fs, tag, tag, "fused")
+            b.record(stream)
+            evs.append((tag, a, b))
+    torch.cuda.synchronize(dev)
+    for tag, a, b in evs:
+        stage_ms.setdefault(tag, []).append(a.elapsed_time(b))
+    kern_ms = sum(statistics.mean(v) for v in stage_ms.values())
+    achieved = sum(stage_bytes.values()) / (kern_ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "fused_stage_traffic.json")))
+        traffic = prof.get("traffic_bytes_per_fill")
+    except Exception:
+        pass
+
+    # end to end through the public call, host buffers, copies inside the timing
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty_like(fs.work, device="cpu").pin_memory()
+        host_in.copy_(fs.work)
+        host_out = torch.empty_like(host_in).pin_memory()
+
+        def e2e_step():
+            fs.work.copy_(host_in, non_blocking=True)
+            fill_ghosts(fs, sched, method=method)
+            host_out.copy_(fs.work, non_blocking=True)
+        e2e_step()
+        e2e_steps = max(3, min(args.steps, 10))
+        ms_e2e = timed(e2e_step, e2e_steps)
+        e2e = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+               "ms_per_step": ms_e2e, "h2d_bytes_per_step": field_bytes,
+               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps}
+        del host_in, host_out
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        host = fs.work.cpu().numpy().copy()
+        gbs, best, runs, threads = cpu_fill_rate(sched, host, nvars, fs.factors_host,
+                                                 bytes_per_fill)
+        cpu = {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"whole fills of the same mesh and data, best of {runs} after one "
+                         f"warm-up ({best:.3f} s a fill), oracle/fill_oracle.c with "
+                         f"{threads} OpenMP threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded uniform [-1,1] field data on the sphere mesh)",
+            "config": dict(cfg, method=method, parallelism=f"replicas{world}"),
+            "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
+                      "speedup_fused_vs_plain": ms_plain / ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_src,
+                         "kernel": "fused_stage_kernel",
+                         "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
+                         "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": args.steps * ds.nstages if method == "fused" else
+            args.steps * ds.ngroups,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference(args):
+    """The CPU restatement of the reference's threaded fill on the host cores."""
+    import torch
+    from treeamr import FieldSet, GhostSchedule, Operators, meshes
+    import oracle
+    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
+    fs = FieldSet(f, args.nvars, G=3, T=np.float64, device="cpu")
+    meshes.random_fill(fs, seed=1)
+    sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    cfg = workload_config(args, f, sched)
+    cfg["field_bytes"] = fs.work.numel() * 8
+    points = sched.ghost_items(args.nvars)
+    bytes_per_fill = 2 * points * 8
+    host = fs.work.numpy()
+    threads = os.cpu_count() or 1
+    oracle.build()
+    # every step is one whole fill; the count is capped so the run stays
+    # within about two minutes
+    t0 = time.perf_counter()
+    oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+    one = time.perf_counter() - t0
+    warm = max(0, min(args.warmup - 1, int(20 / max(one, 1e-3))))
+    for _ in range(warm):
+        oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+    steps = max(1, min(args.steps, int(90 / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+    sec = (time.perf_counter() - t0) / steps
+    value = bytes_per_fill / sec / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform [-1,1] field data on the sphere mesh)",
+        "config": dict(cfg, method="cpu threaded fill", parallelism="host threads"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} whole fills after {warm + 1} warm-up, "
+                                   "oracle/fill_oracle.c (the reference is Julia, absent here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,154 @@
+/*
+ * treeamr_cuda.h -- C ABI of libtreeamr_cuda.so, the GB300 ghost-fill engine.
+ *
+ * The reference (TreeAMR.jl) replays a precomputed GhostSchedule of
+ * TransferGroups with one KernelAbstractions launch per group
+ * (src/ghosts.jl:372-402 transfer_kernel!, :420-521 run_group!,
+ * :563-593 run_phase!, :1099-1160 exchange_ghosts!).  This library takes the
+ * same schedule, flattened once into the plain arrays below by the host that
+ * built it (src/schedule.jl:3075-3292 GhostSchedule, :2970 local_groups), and
+ * replays it on one GPU.
+ *
+ * Conventions, all the reference's own so a Julia caller passes its arrays
+ * unchanged:
+ *   - work is column-major (S_1, ..., S_D, nvars, nblocks), index 1 fastest
+ *     (src/storage.jl:364-472); S_d = N + 2 G_d + c_d.
+ *   - block indices and stored indices are 1-based.
+ *   - a stencil column i holds `order` weights, weights[w + order*i + m].
+ *   - the factor table is nvars x ncols column-major (src/storage.jl:536-551).
+ *   - pointers to field data (work, factors) are device pointers owned by the
+ *     caller; the library borrows them for the call only.
+ *   - every entry point returns TAM_OK (0) or a negative tam_status, never
+ *     aborts and never traps; tam_last_error() says why.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ */
+#ifndef TREEAMR_CUDA_H
+#define TREEAMR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TAM_ABI_VERSION 1
+#define TAM_MAX_DIM 3
+
+enum tam_status {
+  TAM_OK = 0,
+  TAM_EINVAL = -1,        /* an argument or descriptor is malformed        */
+  TAM_ECUDA = -2,         /* a CUDA call failed                            */
+  TAM_ENOMEM = -3,        /* device allocation failed                      */
+  TAM_ELAYOUT = -4,       /* field set does not match the schedule layout  */
+  TAM_ETIMEOUT = -5,      /* a bounded device wait gave up                 */
+  TAM_EUNSUPPORTED = -6   /* a feature the schedule asks for is not built  */
+};
+
+enum tam_dtype { TAM_F32 = 1, TAM_F64 = 2 };
+enum tam_kind { TAM_COPY = 1, TAM_RESTRICT = 2, TAM_PROLONG = 3 };
+
+/* Stage tags, ascending in the order a fill runs them
+ * (src/schedule.jl:640-642, src/ghosts.jl:1099-1160). */
+#define TAM_STAGE_SELFIMAGE (-1) /* stage P: wall-plane projection   */
+#define TAM_STAGE_UNIFY 0        /* stage 0: secondaries <- primary  */
+#define TAM_STAGE_PHASE1 1       /* copies and restrictions          */
+#define TAM_STAGE_PROLONG(l) (2 + (l)) /* prolongations onto level l */
+#define TAM_STAGE_ALL_FIRST (-1)
+#define TAM_STAGE_ALL_LAST 0x7fffffff
+
+/* One dimension of a transfer: Stencil1D (src/schedule.jl:64-93). */
+typedef struct tam_stencil {
+  int32_t targetfirst; /* 1-based stored index of the first target row   */
+  int32_t ntarget;     /* target rows                                    */
+  int32_t order;       /* weights per column                             */
+  int32_t unit;        /* 1: one point of weight exactly one (a copy)    */
+  int64_t srcstart;    /* offset into srcstart pool: ntarget entries     */
+  int64_t weights;     /* offset into weight pool: order*ntarget entries */
+} tam_stencil;
+
+/* One TransferGroup (src/schedule.jl:150-197): the transfers
+ * (targetblocks[first+t], sourceblocks[first+t]), t < ntransfers. */
+typedef struct tam_group {
+  int32_t kind;      /* tam_kind                                          */
+  int32_t stage;     /* stage tag (transfer_stage, src/schedule.jl:656)   */
+  int32_t factorcol; /* 0, or the 1-based factor-table column             */
+  int32_t bounded;   /* must be 0: bounded operators are not built        */
+  int64_t first;     /* offset into the block lists                        */
+  int64_t ntransfers;
+  tam_stencil stencil[TAM_MAX_DIM]; /* dimensions >= ndim are ignored      */
+} tam_group;
+
+/* A whole schedule, as host arrays (read during the call only). */
+typedef struct tam_schedule_desc {
+  int32_t abi_version;        /* TAM_ABI_VERSION                           */
+  int32_t ndim;               /* D in 1..3                                 */
+  int32_t dtype;              /* tam_dtype of the weights and of work      */
+  int32_t stored[TAM_MAX_DIM];/* S_d                                       */
+  int64_t nblocks;
+  int32_t ngroups;
+  int32_t nfactorcols;        /* 3^D, the factor table's columns           */
+  const tam_group *groups;
+  int64_t ntransfers;         /* length of both block lists                */
+  const int32_t *targetblocks;/* 1-based                                   */
+  const int32_t *sourceblocks;/* 1-based                                   */
+  int64_t nsrcstart;
+  const int32_t *srcstart;    /* 1-based stored indices                    */
+  int64_t nweights;
+  const void *weights;        /* float or double per dtype                 */
+} tam_schedule_desc;
+
+typedef struct tam_ctx tam_ctx;
+typedef struct tam_sched tam_sched;
+
+/* Library version: TAM_ABI_VERSION. */
+int tam_abi_version(void);
+
+/* Open the library on a CUDA device.  Replaces the reference's backend
+ * selection (src/device.jl:1-34 todevice / get_backend). */
+int tam_init(int device, tam_ctx **out);
+void tam_free(tam_ctx *ctx);
+
+/* The last error message of this context (or of the library when ctx is
+ * NULL), NUL-terminated into buf. */
+int tam_last_error(const tam_ctx *ctx, char *buf, size_t n);
+
+/* Validate a flattened schedule and upload it once.  Replaces
+ * todevice(backend, ::TransferGroup) and local_groups
+ * (src/schedule.jl:184-188, 2970-2992).  Every stencil window and block
+ * index is checked against the layout here, so no fill can read or write
+ * outside `work`. */
+int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *desc, tam_sched **out);
+void tam_schedule_free(tam_sched *s);
+
+/* Counts of the uploaded schedule: groups, transfers, point-variables per
+ * variable written (sum ntransfers * prod ntarget), stages. */
+int tam_schedule_info(const tam_sched *s, int64_t *ngroups, int64_t *ntransfers,
+                      int64_t *points, int32_t *nstages);
+
+/* The fused fill: every stage tag in [first_stage, last_stage], in order,
+ * each stage one batched launch over all its groups' transfers, grouped by
+ * target block.  Replaces exchange_ghosts! / run_stages! / run_phase! for a
+ * serial forest (src/ghosts.jl:1099-1160, 988-1007, 563-570).  A boundary
+ * hook runs between two calls: [-1, 1] then [2, TAM_STAGE_ALL_LAST]
+ * (src/ghosts.jl:1134-1136).  `factors` may be NULL when no group has a
+ * factor column.  Asynchronous on `stream`. */
+int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
+             const void *factors, int32_t first_stage, int32_t last_stage,
+             void *stream);
+
+/* The plain fill: one launch per TransferGroup, one thread per
+ * point-variable, as the reference's device path launches transfer_kernel!
+ * (src/ghosts.jl:420-521).  Same arguments and results as tam_fill. */
+int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
+                   const void *factors, int32_t first_stage, int32_t last_stage,
+                   void *stream);
+
+/* Read (and clear) the device error word of the schedule's last fills:
+ * 0, or a tam_status a kernel recorded.  Synchronizes `stream`. */
+int tam_device_status(tam_sched *s, void *stream, int32_t *code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TREEAMR_CUDA_H */

@@ -1,0 +1,114 @@
+"""The oracle: a CPU restatement of the reference's ghost fill.
+
+TEST INFRASTRUCTURE ONLY -- imported by tests/, by __graft_entry__.smoke() as
+the checker, and by bench.py's cpu_baseline leg.  The product never calls it.
+
+``fill(schedule, work, ...)`` and ``fill_adjoint(...)`` run ``fill_oracle.c``
+(compiled by ``build()`` into ``oracle/_build``) over the same flattened
+schedule the CUDA library uploads; ``exact_weights`` and friends are in the
+host package's ``operators`` module and are pinned by the reference's
+known-answer tests in ``tests/test_operators.py``.
+
+Parity status: pinned by the reference's known-answer and property tests
+(restated in tests/).  No golden vectors exist in the reference and the
+reference (Julia) cannot run in this environment.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libtam_oracle.so")
+SRC = os.path.join(HERE, "fill_oracle.c")
+HDR = os.path.join(ROOT, "include", "treeamr_cuda.h")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """gcc -O2 -fopenmp -ffp-contract=off: no fused multiply-add on any host."""
+    with _lock:
+        os.makedirs(BUILD_DIR, exist_ok=True)
+        newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
+        if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+            return LIB_PATH
+        tmp = LIB_PATH + ".tmp"
+        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+               "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), SRC, "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+        os.replace(tmp, LIB_PATH)
+        return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        l = C.CDLL(LIB_PATH)
+        l.oracle_fill.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                  C.c_int32, C.c_int]
+        l.oracle_fill.restype = C.c_int
+        l.oracle_fill_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                          C.c_int32, C.c_int32]
+        l.oracle_fill_adjoint.restype = C.c_int
+        _lib = l
+    return _lib
+
+
+def _descriptor(schedule):
+    import treeamr._native as nat
+    cache = schedule.__dict__.setdefault("_oracle_desc", None)
+    if cache is None:
+        cache = nat.Descriptor(schedule)
+        schedule._oracle_desc = cache
+    return cache
+
+
+ALL_FIRST, ALL_LAST = -1, 0x7FFFFFFF
+
+
+def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
+         last=ALL_LAST, nthreads: int = 1) -> np.ndarray:
+    """In place on ``work`` (shape (nblocks, nvars, S_D..S_1), C order)."""
+    assert work.flags.c_contiguous and work.dtype == np.dtype(schedule.T)
+    d = _descriptor(schedule)
+    f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=work.dtype)
+    rc = lib().oracle_fill(C.addressof(d.desc), work.ctypes.data, nvars, f.ctypes.data, first,
+                           last, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle_fill failed")
+    return work
+
+
+def fill_adjoint(schedule, y: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
+                 last=ALL_LAST) -> np.ndarray:
+    assert y.flags.c_contiguous and y.dtype == np.dtype(schedule.T)
+    d = _descriptor(schedule)
+    f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=y.dtype)
+    rc = lib().oracle_fill_adjoint(C.addressof(d.desc), y.ctypes.data, nvars, f.ctypes.data,
+                                   first, last)
+    if rc != 0:
+        raise RuntimeError("oracle_fill_adjoint failed")
+    return y
+
+
+def fill_fieldset(fs, schedule, *, boundary_values=None, nthreads: int = 1) -> np.ndarray:
+    """The oracle's fill of a field set's current contents, returned as a new
+    host array; ``boundary_values(host, fs, regions)`` fills the outer-face
+    regions between phase 1 and the prolongations."""
+    host = fs.work.detach().cpu().numpy().copy()
+    if boundary_values is None or not schedule.boundaries:
+        return fill(schedule, host, fs.nvars, fs.factors_host, nthreads=nthreads)
+    fill(schedule, host, fs.nvars, fs.factors_host, last=1, nthreads=nthreads)
+    boundary_values(host, fs, schedule.boundaries)
+    return fill(schedule, host, fs.nvars, fs.factors_host, first=2, nthreads=nthreads)

@@ -1,0 +1,262 @@
+/*
+ * fill_oracle.c -- CPU restatement of the reference's ghost fill.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA engine is checked
+ * against and the CPU baseline bench.py times; nothing in the product calls
+ * it.  Parity is pinned by the reference's own known-answer and property
+ * tests restated in tests/ (exact weights, polynomial exactness, every ghost
+ * written once, periodic = tiling bit for bit, interiors untouched, parity
+ * at reflecting faces, outflow = nearest owned point).  The reference itself
+ * (Julia) cannot run here, and it stores no golden vectors.
+ *
+ * What it restates, over a schedule already flattened into the
+ * tam_schedule_desc arrays (include/treeamr_cuda.h):
+ *   - stencil_sum            src/ghosts.jl:75-118  (m_1 innermost, weight
+ *                            product ((w_1*w_2)*w_3), acc from +0, no FMA)
+ *   - copy_load              src/ghosts.jl:127-128 (+0 + x)
+ *   - scaled                 src/ghosts.jl:369-370 (x*f + 0)
+ *   - transfer_kernel!       src/ghosts.jl:372-402
+ *   - run_phase! (CPU form)  src/ghosts.jl:572-593: the owned blocks split
+ *                            into contiguous chunks, one per thread
+ *                            (src/threading.jl:50-70 equalsplit), each thread
+ *                            running its share of every group of the stage
+ *   - exchange_ghosts!       src/ghosts.jl:1099-1160: stages in tag order
+ *   - the adjoint (transpose) of the same linear map, stage by stage in
+ *     reverse, in scatter form: a new capability with no reference
+ *     counterpart, so its oracle is the linear algebra of the forward.
+ *
+ * Build: see oracle/build.py.  Compiled with -ffp-contract=off so that no
+ * multiply-add is fused on any host architecture.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "treeamr_cuda.h"
+
+/* contiguous chunk c of n blocks split k ways (src/threading.jl:58-70) */
+static void equalsplit(int64_t n, int k, int c, int64_t *lo, int64_t *hi) {
+  int64_t q = n / k, r = n % k;
+  *lo = c * q + (c < r ? c : r);
+  *hi = *lo + q + (c < r ? 1 : 0);
+}
+
+/* first index in [lo, hi) of the non-decreasing list with list[i] >= x */
+static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t x) {
+  while (lo < hi) {
+    int64_t mid = lo + (hi - lo) / 2;
+    if (list[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+#define DEFINE_ORACLE(T, SUFFIX)                                                                \
+  static void run_transfers_##SUFFIX(const tam_schedule_desc *d, const tam_group *g,            \
+                                     int64_t t0, int64_t t1, T *work, int32_t nvars,           \
+                                     const T *factors) {                                        \
+    const int D = d->ndim;                                                                      \
+    int n[3] = {1, 1, 1}, o[3] = {1, 1, 1}, tf[3] = {0, 0, 0};                                  \
+    int64_t S[3] = {1, 1, 1};                                                                   \
+    int unit = 1;                                                                               \
+    for (int k = 0; k < D; ++k) {                                                               \
+      n[k] = g->stencil[k].ntarget;                                                             \
+      o[k] = g->stencil[k].order;                                                               \
+      tf[k] = g->stencil[k].targetfirst - 1;                                                    \
+      S[k] = d->stored[k];                                                                      \
+      unit = unit && g->stencil[k].unit;                                                        \
+    }                                                                                           \
+    const T *W = (const T *)d->weights;                                                         \
+    const int64_t s2 = S[0], s3 = S[0] * S[1], vs = S[0] * S[1] * S[2];                         \
+    const int64_t bs = vs * nvars;                                                              \
+    for (int64_t t = t0; t < t1; ++t) {                                                         \
+      const int64_t tb = d->targetblocks[g->first + t] - 1;                                     \
+      const int64_t sb = d->sourceblocks[g->first + t] - 1;                                     \
+      for (int v = 0; v < nvars; ++v)                                                           \
+        for (int i3 = 0; i3 < n[2]; ++i3)                                                       \
+          for (int i2 = 0; i2 < n[1]; ++i2)                                                     \
+            for (int i1 = 0; i1 < n[0]; ++i1) {                                                 \
+              int idx[3] = {i1, i2, i3};                                                        \
+              int64_t base[3] = {0, 0, 0};                                                      \
+              const T *wc[3] = {0, 0, 0};                                                       \
+              for (int k = 0; k < D; ++k) {                                                     \
+                base[k] = d->srcstart[g->stencil[k].srcstart + idx[k]] - 1;                     \
+                wc[k] = W + g->stencil[k].weights + (int64_t)o[k] * idx[k];                     \
+              }                                                                                 \
+              const T *src = work + sb * bs + v * vs + base[0] + base[1] * s2 + base[2] * s3;   \
+              T acc = (T)0;                                                                     \
+              if (unit) {                                                                       \
+                acc = (T)0 + src[0];                                                            \
+              } else {                                                                          \
+                for (int m3 = 0; m3 < o[2]; ++m3)                                               \
+                  for (int m2 = 0; m2 < o[1]; ++m2)                                             \
+                    for (int m1 = 0; m1 < o[0]; ++m1) {                                         \
+                      T wp = wc[0][m1];                                                         \
+                      if (D >= 2) wp = wp * wc[1][m2];                                          \
+                      if (D >= 3) wp = wp * wc[2][m3];                                          \
+                      T term = wp * src[m1 + m2 * s2 + m3 * s3];                                \
+                      acc = acc + term;                                                         \
+                    }                                                                           \
+              }                                                                                 \
+              T x = acc;                                                                        \
+              if (g->factorcol) {                                                               \
+                T f = factors[v + (int64_t)nvars * (g->factorcol - 1)];                         \
+                x = x * f + (T)0;                                                               \
+              }                                                                                 \
+              work[tb * bs + v * vs + (tf[0] + i1) + (int64_t)(tf[1] + i2) * s2 +               \
+                   (int64_t)(tf[2] + i3) * s3] = x;                                             \
+            }                                                                                   \
+    }                                                                                           \
+  }                                                                                             \
+                                                                                                \
+  static void run_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *work,             \
+                                 int32_t nvars, const T *factors, int nthreads) {               \
+    _Pragma("omp parallel num_threads(nthreads)") {                                             \
+      int c = 0, k = 1;                                                                         \
+      ORACLE_THREAD_IDS(c, k);                                                                  \
+      int64_t lo, hi;                                                                           \
+      equalsplit(d->nblocks, k, c, &lo, &hi);                                                   \
+      for (int32_t gi = 0; gi < d->ngroups; ++gi) {                                             \
+        const tam_group *g = &d->groups[gi];                                                    \
+        if (g->stage != tag) continue;                                                          \
+        const int32_t *owners = d->targetblocks + g->first;                                     \
+        int64_t a = lower_bound(owners, 0, g->ntransfers, lo + 1);                              \
+        int64_t b = lower_bound(owners, 0, g->ntransfers, hi + 1);                              \
+        if (a < b) run_transfers_##SUFFIX(d, g, a, b, work, nvars, factors);                    \
+      }                                                                                         \
+    }                                                                                           \
+  }
+
+#ifdef _OPENMP
+#define ORACLE_THREAD_IDS(c, k) \
+  do {                          \
+    c = omp_get_thread_num();   \
+    k = omp_get_num_threads();  \
+  } while (0)
+#else
+#define ORACLE_THREAD_IDS(c, k) \
+  do {                          \
+    c = 0;                      \
+    k = 1;                      \
+  } while (0)
+#endif
+
+DEFINE_ORACLE(double, f64)
+DEFINE_ORACLE(float, f32)
+
+static int collect_tags(const tam_schedule_desc *d, int32_t *tags, int cap) {
+  int n = 0;
+  for (int32_t gi = 0; gi < d->ngroups; ++gi) {
+    int32_t t = d->groups[gi].stage, seen = 0;
+    for (int j = 0; j < n; ++j) seen |= tags[j] == t;
+    if (!seen && n < cap) tags[n++] = t;
+  }
+  for (int i = 1; i < n; ++i)
+    for (int j = i; j > 0 && tags[j - 1] > tags[j]; --j) {
+      int32_t x = tags[j];
+      tags[j] = tags[j - 1];
+      tags[j - 1] = x;
+    }
+  return n;
+}
+
+/* The serial-forest fill: every stage tag in [first, last], in order. */
+int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const void *factors,
+                int32_t first, int32_t last, int nthreads) {
+  if (!d || !work || nvars < 1) return -1;
+  if (nthreads < 1) nthreads = 1;
+  int32_t tags[128];
+  int nt = collect_tags(d, tags, 128);
+  for (int i = 0; i < nt; ++i) {
+    if (tags[i] < first || tags[i] > last) continue;
+    if (d->dtype == TAM_F64)
+      run_stage_f64(d, tags[i], (double *)work, nvars, (const double *)factors, nthreads);
+    else
+      run_stage_f32(d, tags[i], (float *)work, nvars, (const float *)factors, nthreads);
+  }
+  return 0;
+}
+
+/* The transpose of the fill, in scatter form, serial.  Stage s is
+ * x <- (I - E_s) x + E_s A_s x, with E_s the projection on its targets and
+ * A_s reading only points that are not its targets; its transpose is
+ * y <- (I - E_s) y + A_s^T E_s y: every target's adjoint is scattered onto
+ * its sources with the transfer's weights, then the targets are zeroed.
+ * Stages run in reverse tag order. */
+#define DEFINE_ADJOINT(T, SUFFIX)                                                               \
+  static void adjoint_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *y,            \
+                                     int32_t nvars, const T *factors) {                         \
+    const int D = d->ndim;                                                                      \
+    int64_t S[3] = {1, 1, 1};                                                                   \
+    for (int k = 0; k < D; ++k) S[k] = d->stored[k];                                            \
+    const int64_t s2 = S[0], s3 = S[0] * S[1], vs = S[0] * S[1] * S[2], bs = vs * nvars;        \
+    const T *W = (const T *)d->weights;                                                         \
+    for (int pass = 0; pass < 2; ++pass)                                                        \
+      for (int32_t gi = 0; gi < d->ngroups; ++gi) {                                             \
+        const tam_group *g = &d->groups[gi];                                                    \
+        if (g->stage != tag) continue;                                                          \
+        int n[3] = {1, 1, 1}, o[3] = {1, 1, 1}, tf[3] = {0, 0, 0};                              \
+        for (int k = 0; k < D; ++k) {                                                           \
+          n[k] = g->stencil[k].ntarget;                                                         \
+          o[k] = g->stencil[k].order;                                                           \
+          tf[k] = g->stencil[k].targetfirst - 1;                                                \
+        }                                                                                       \
+        for (int64_t t = 0; t < g->ntransfers; ++t) {                                           \
+          const int64_t tb = d->targetblocks[g->first + t] - 1;                                 \
+          const int64_t sb = d->sourceblocks[g->first + t] - 1;                                 \
+          for (int v = 0; v < nvars; ++v)                                                       \
+            for (int i3 = 0; i3 < n[2]; ++i3)                                                   \
+              for (int i2 = 0; i2 < n[1]; ++i2)                                                 \
+                for (int i1 = 0; i1 < n[0]; ++i1) {                                             \
+                  T *yt = y + tb * bs + v * vs + (tf[0] + i1) + (int64_t)(tf[1] + i2) * s2 +    \
+                          (int64_t)(tf[2] + i3) * s3;                                           \
+                  if (pass == 1) {                                                              \
+                    *yt = (T)0;                                                                 \
+                    continue;                                                                   \
+                  }                                                                             \
+                  T a = *yt;                                                                    \
+                  if (g->factorcol) a = a * factors[v + (int64_t)nvars * (g->factorcol - 1)];   \
+                  int idx[3] = {i1, i2, i3};                                                    \
+                  int64_t base[3] = {0, 0, 0};                                                  \
+                  const T *wc[3] = {0, 0, 0};                                                   \
+                  for (int k = 0; k < D; ++k) {                                                 \
+                    base[k] = d->srcstart[g->stencil[k].srcstart + idx[k]] - 1;                 \
+                    wc[k] = W + g->stencil[k].weights + (int64_t)o[k] * idx[k];                 \
+                  }                                                                             \
+                  T *ys = y + sb * bs + v * vs + base[0] + base[1] * s2 + base[2] * s3;         \
+                  for (int m3 = 0; m3 < o[2]; ++m3)                                             \
+                    for (int m2 = 0; m2 < o[1]; ++m2)                                           \
+                      for (int m1 = 0; m1 < o[0]; ++m1) {                                       \
+                        T wp = wc[0][m1];                                                       \
+                        if (D >= 2) wp = wp * wc[1][m2];                                        \
+                        if (D >= 3) wp = wp * wc[2][m3];                                        \
+                        ys[m1 + m2 * s2 + m3 * s3] += wp * a;                                   \
+                      }                                                                         \
+                }                                                                               \
+        }                                                                                       \
+      }                                                                                         \
+  }
+
+DEFINE_ADJOINT(double, f64)
+DEFINE_ADJOINT(float, f32)
+
+int oracle_fill_adjoint(const tam_schedule_desc *d, void *y, int32_t nvars, const void *factors,
+                        int32_t first, int32_t last) {
+  if (!d || !y || nvars < 1) return -1;
+  int32_t tags[128];
+  int nt = collect_tags(d, tags, 128);
+  for (int i = nt - 1; i >= 0; --i) {
+    if (tags[i] < first || tags[i] > last) continue;
+    if (d->dtype == TAM_F64)
+      adjoint_stage_f64(d, tags[i], (double *)y, nvars, (const double *)factors);
+    else
+      adjoint_stage_f32(d, tags[i], (float *)y, nvars, (const float *)factors);
+  }
+  return 0;
+}

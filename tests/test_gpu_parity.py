@@ -1,0 +1,171 @@
+"""Parity of the CUDA engine with the oracle, through the C ABI.
+
+Every fill is compared with the oracle's fill of the same data bit for bit:
+the kernels evaluate the reference's expression in the reference's order
+with no fused multiply-add, so there is no tolerance to state (the north
+star's bound of 2 ulp in Float64 and 4 in Float32 for restriction and
+prolongation is met with 0).  NaN is compared as one pattern
+(``test/helpers/ghost.jl:191-219``)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from _helpers import (awkward_fill, exact_values, ghost_mask, makepoly, nanbits, nested_forest)
+from treeamr import (EvenParity, FieldSet, Forest, GhostSchedule, OddParity, Operators,
+                     fill_ghosts)
+from treeamr import meshes
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["fused", "plain"]
+
+
+def _gpu_vs_oracle(fs_host, ops, method, *, host=None, boundary=False, exact=None):
+    """Fill a copy of ``fs_host``'s data on the GPU and with the oracle."""
+    s = GhostSchedule(fs_host, ops)
+    if host is None:
+        host = fs_host.work.numpy().copy()
+    fs_host.work.copy_(torch.from_numpy(host))
+    bv = None
+    if boundary:
+        def bv(h, fs_, regions):
+            for r in regions:
+                sl = tuple(slice(a - 1, z) for a, z in reversed(r.region))
+                h[(r.block, slice(None)) + sl] = exact[(r.block, slice(None)) + sl]
+    expect = oracle.fill_fieldset(fs_host, s, boundary_values=bv)
+    fs = fs_host
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fs.factors = fs.factors.cuda()
+
+    hook = None
+    if boundary:
+        def hook(fsd, regions):
+            h = fsd.work.cpu().numpy()
+            bv(h, fsd, regions)
+            fsd.work.copy_(torch.from_numpy(h).cuda())
+    fill_ghosts(fs, s, boundary=hook, method=method)
+    torch.cuda.synchronize()
+    got = fs.work.cpu().numpy()
+    return got, expect
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_quadrant_bit_exact(cuda_lib, method):
+    f, fs, ops = meshes.quadrant_setup()
+    meshes.random_fill(fs, seed=11)
+    got, expect = _gpu_vs_oracle(fs, ops, method)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("D", [1, 2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+@pytest.mark.parametrize("p,G,N", [(2, 1, 4), (4, 2, 8), (6, 3, 8)])
+def test_nested_bit_exact(cuda_lib, method, D, T, p, G, N):
+    if D == 3 and p == 6:
+        pytest.skip("order 6 runs in 1-D and 2-D, as the reference's test does")
+    f = nested_forest(D, N=N)
+    fs = FieldSet(f, 3, G=G, T=T)
+    exact = exact_values(fs, makepoly(D, 2))
+    rng = np.random.default_rng(D * 100 + p)
+    host = exact.copy()
+    host[:, :, ghost_mask(fs)] = rng.uniform(-9, 9, size=host[:, :, ghost_mask(fs)].shape)
+    got, expect = _gpu_vs_oracle(fs, Operators(prolongation=p, restriction=p), method,
+                                 host=host, boundary=True, exact=exact)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("D", [1, 2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_awkward_data_bit_exact(cuda_lib, method, D, T):
+    """+-0, NaN, +-Inf and subnormals through copies, restrictions and
+    prolongations (``test/ghost_tests.jl:507-560``)."""
+    N = 6 if D == 3 else 8
+    f = Forest((2,) * D, N=N, periodic=(True,) * D)
+    f.refine(f.leaves[0])
+    f.balance()
+    fs = FieldSet(f, 3, G=2, T=T)
+    host = awkward_fill(tuple(fs.work.shape), T, seed=D)
+    got, expect = _gpu_vs_oracle(fs, Operators(prolongation=4, restriction=4), method, host=host)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("D", [2, 3])
+def test_reflecting_outflow_bit_exact(cuda_lib, method, D):
+    refl = tuple((True, False) for _ in range(D))
+    outf = tuple((False, True) for _ in range(D))
+    f = Forest((2,) * D, N=8, reflecting=refl, outflow=outf, extents=[(0.0, 2.0)] * D)
+    f.refine(f.leaves[0])
+    f.balance()
+    parity = [(EvenParity,) * D] * 2 + [tuple(OddParity if e == d else EvenParity
+                                              for e in range(D)) for d in range(D)]
+    fs = FieldSet(f, len(parity), G=2, parity=parity)
+    host = awkward_fill(tuple(fs.work.shape), np.float64, seed=5)
+    got, expect = _gpu_vs_oracle(fs, Operators(prolongation=4, restriction=4), method, host=host)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_sphere_small_bit_exact(cuda_lib, T):
+    """The sphere mesh at a reduced root count (4^3 roots, 2 levels)."""
+    f, fs, ops = meshes.sphere_setup(nvars=2, T=T, roots=4, levels=2)
+    meshes.random_fill(fs, seed=3)
+    for method in METHODS:
+        got, expect = _gpu_vs_oracle(fs, ops, method)
+        assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+def test_fused_equals_plain_and_is_idempotent(cuda_lib):
+    f, fs, ops = meshes.sphere_setup(nvars=2, roots=4, levels=2, device="cuda")
+    meshes.random_fill(fs, seed=9)
+    s = GhostSchedule(fs, ops)
+    a = fs.work.clone()
+    fill_ghosts(fs, s, method="plain")
+    plain = fs.work.clone()
+    fs.work.copy_(a)
+    fill_ghosts(fs, s, method="fused")
+    fused = fs.work.clone()
+    assert torch.equal(plain.view(torch.int64), fused.view(torch.int64))
+    fill_ghosts(fs, s, method="fused")
+    assert torch.equal(fs.work.view(torch.int64), fused.view(torch.int64))
+
+
+def test_interiors_untouched_on_gpu(cuda_lib):
+    f, fs, ops = meshes.sphere_setup(nvars=1, roots=4, levels=2, device="cuda")
+    meshes.random_fill(fs, seed=2)
+    before = fs.work.clone()
+    fill_ghosts(fs, GhostSchedule(fs, ops))
+    inter = (slice(None), slice(None)) + fs.interior()
+    assert torch.equal(fs.work[inter], before[inter])
+    assert not torch.equal(fs.work, before)
+
+
+def test_layout_mismatch_refused(cuda_lib):
+    f = Forest((2, 2), N=8, periodic=(True, True))
+    fs1 = FieldSet(f, 1, G=2, device="cuda")
+    fs2 = FieldSet(f, 1, G=3, device="cuda")
+    s = GhostSchedule(fs1, Operators(prolongation=4, restriction=4))
+    with pytest.raises(ValueError, match="G="):
+        fill_ghosts(fs2, s)
+
+
+def test_bad_descriptor_rejected_before_launch(cuda_lib):
+    """A stencil window outside the stored extent is refused at upload."""
+    import ctypes as C
+    from treeamr import _native
+    f = Forest((2, 2), N=8, periodic=(True, True))
+    fs = FieldSet(f, 1, G=2)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    d = _native.Descriptor(s)
+    d.srcstart[0] = 100
+    ctx = _native.context(0)
+    h = C.c_void_p()
+    rc = cuda_lib.tam_schedule_upload(ctx, d.ref(), C.byref(h))
+    assert rc == -1
+    assert "outside" in _native.last_error(ctx)
+    d.srcstart[0] = 1
+    d.targetblocks[0] = 99
+    assert cuda_lib.tam_schedule_upload(ctx, d.ref(), C.byref(h)) == -1

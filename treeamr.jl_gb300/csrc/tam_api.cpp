@@ -1,0 +1,401 @@
+// Host side of libtreeamr_cuda.so: descriptor validation, upload, tiling
+// and the stage loop of a fill.  See include/treeamr_cuda.h for the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tam_internal.h"
+#include "treeamr_cuda.h"
+
+namespace {
+
+std::mutex g_err_mutex;
+std::string g_err;  // errors with no context
+
+int fail(tam_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) {
+    ctx->err = msg;
+  } else {
+    std::lock_guard<std::mutex> lock(g_err_mutex);
+    g_err = msg;
+  }
+  return code;
+}
+
+int cuda_fail(tam_ctx *ctx, cudaError_t e, const char *what) {
+  cudaGetLastError();  // clear a sticky-free error so the next call starts clean
+  return fail(ctx, TAM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Runs the body with the context's device current and puts the caller's
+// device back afterwards.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    ok_ = cudaGetDevice(&prev_) == cudaSuccess;
+    if (ok_ && prev_ != device) ok_ = cudaSetDevice(device) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != prev_) cudaSetDevice(prev_);
+  }
+  bool ok() const { return ok_; }
+
+ private:
+  int prev_ = 0;
+  bool ok_ = false;
+};
+
+template <typename T>
+cudaError_t upload(T **dst, const T *src, size_t n) {
+  *dst = nullptr;
+  if (n == 0) n = 1;  // a valid pointer even for an empty pool
+  cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (src) return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+  return cudaMemset(*dst, 0, n * sizeof(T));
+}
+
+void free_sched_device(tam_sched *s) {
+  cudaFree(s->d_groups);
+  cudaFree(s->d_tb);
+  cudaFree(s->d_sb);
+  cudaFree(s->d_srcstart);
+  cudaFree(s->d_weights);
+  cudaFree(s->d_tiles);
+  cudaFree(s->d_err);
+  s->d_groups = nullptr;
+  s->d_tb = s->d_sb = s->d_srcstart = nullptr;
+  s->d_weights = nullptr;
+  s->d_tiles = nullptr;
+  s->d_err = nullptr;
+}
+
+// Every check that makes a fill memory-safe: indices into the pools, block
+// indices, and each stencil's target rows and source windows inside the
+// stored extent.
+int validate(tam_ctx *ctx, const tam_schedule_desc *d) {
+  char buf[256];
+  if (!d) return fail(ctx, TAM_EINVAL, "schedule descriptor is NULL");
+  if (d->abi_version != TAM_ABI_VERSION) {
+    snprintf(buf, sizeof buf, "descriptor ABI version %d, library %d", d->abi_version,
+             TAM_ABI_VERSION);
+    return fail(ctx, TAM_EINVAL, buf);
+  }
+  if (d->ndim < 1 || d->ndim > 3) return fail(ctx, TAM_EINVAL, "ndim must be 1, 2 or 3");
+  if (d->dtype != TAM_F32 && d->dtype != TAM_F64)
+    return fail(ctx, TAM_EINVAL, "dtype must be TAM_F32 or TAM_F64");
+  if (d->nblocks < 0 || d->nblocks > INT32_MAX) return fail(ctx, TAM_EINVAL, "bad nblocks");
+  if (d->ngroups < 0) return fail(ctx, TAM_EINVAL, "bad ngroups");
+  if (d->ngroups > 0 && !d->groups) return fail(ctx, TAM_EINVAL, "groups is NULL");
+  if (d->ntransfers < 0 || d->ntransfers > INT32_MAX)
+    return fail(ctx, TAM_EINVAL, "bad ntransfers");
+  if (d->ntransfers > 0 && (!d->targetblocks || !d->sourceblocks))
+    return fail(ctx, TAM_EINVAL, "block lists are NULL");
+  if (d->nsrcstart < 0 || (d->nsrcstart > 0 && !d->srcstart))
+    return fail(ctx, TAM_EINVAL, "bad srcstart pool");
+  if (d->nweights < 0 || (d->nweights > 0 && !d->weights))
+    return fail(ctx, TAM_EINVAL, "bad weight pool");
+  int64_t maxcols = 1;
+  for (int k = 0; k < d->ndim; ++k) maxcols *= 3;
+  for (int k = 0; k < d->ndim; ++k)
+    if (d->stored[k] < 1) return fail(ctx, TAM_EINVAL, "stored extents must be positive");
+  for (int64_t t = 0; t < d->ntransfers; ++t) {
+    if (d->targetblocks[t] < 1 || d->targetblocks[t] > d->nblocks ||
+        d->sourceblocks[t] < 1 || d->sourceblocks[t] > d->nblocks) {
+      snprintf(buf, sizeof buf, "transfer %lld names a block outside 1:%lld", (long long)t,
+               (long long)d->nblocks);
+      return fail(ctx, TAM_EINVAL, buf);
+    }
+  }
+  for (int32_t gi = 0; gi < d->ngroups; ++gi) {
+    const tam_group &g = d->groups[gi];
+    if (g.kind < TAM_COPY || g.kind > TAM_PROLONG) return fail(ctx, TAM_EINVAL, "bad group kind");
+    if (g.bounded != 0)
+      return fail(ctx, TAM_EUNSUPPORTED, "bounded operators are not part of this engine");
+    if (g.factorcol < 0 || g.factorcol > maxcols)
+      return fail(ctx, TAM_EINVAL, "factor column outside the table");
+    if (g.first < 0 || g.ntransfers < 0 || g.first + g.ntransfers > d->ntransfers)
+      return fail(ctx, TAM_EINVAL, "group block range outside the block lists");
+    if (g.stage < TAM_STAGE_SELFIMAGE || g.stage > 2 + 64)
+      return fail(ctx, TAM_EINVAL, "bad stage tag");
+    for (int k = 0; k < d->ndim; ++k) {
+      const tam_stencil &s = g.stencil[k];
+      const int S = d->stored[k];
+      if (s.ntarget < 1 || s.order < 1 || s.order > 16) {
+        snprintf(buf, sizeof buf, "group %d dim %d: ntarget %d order %d", gi, k + 1, s.ntarget,
+                 s.order);
+        return fail(ctx, TAM_EINVAL, buf);
+      }
+      if (s.targetfirst < 1 || s.targetfirst + s.ntarget - 1 > S)
+        return fail(ctx, TAM_EINVAL, "target rows outside the stored extent");
+      if (s.srcstart < 0 || s.srcstart + s.ntarget > d->nsrcstart)
+        return fail(ctx, TAM_EINVAL, "srcstart offset outside the pool");
+      if (s.weights < 0 || s.weights + (int64_t)s.order * s.ntarget > d->nweights)
+        return fail(ctx, TAM_EINVAL, "weight offset outside the pool");
+      for (int i = 0; i < s.ntarget; ++i) {
+        const int32_t b = d->srcstart[s.srcstart + i];
+        if (b < 1 || b + s.order - 1 > S) {
+          snprintf(buf, sizeof buf,
+                   "group %d dim %d row %d: source window %d:%d outside 1:%d", gi, k + 1, i + 1,
+                   b, b + s.order - 1, S);
+          return fail(ctx, TAM_EINVAL, buf);
+        }
+      }
+    }
+  }
+  return TAM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tam_abi_version(void) { return TAM_ABI_VERSION; }
+
+int tam_init(int device, tam_ctx **out) {
+  if (!out) return fail(nullptr, TAM_EINVAL, "tam_init: out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+  if (device < 0 || device >= n) return fail(nullptr, TAM_EINVAL, "no such CUDA device");
+  tam_ctx *ctx = new (std::nothrow) tam_ctx;
+  if (!ctx) return fail(nullptr, TAM_ENOMEM, "out of host memory");
+  ctx->device = device;
+  e = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
+  }
+  *out = ctx;
+  return TAM_OK;
+}
+
+void tam_free(tam_ctx *ctx) { delete ctx; }
+
+int tam_last_error(const tam_ctx *ctx, char *buf, size_t n) {
+  if (!buf || n == 0) return TAM_EINVAL;
+  std::string msg;
+  if (ctx) {
+    msg = ctx->err;
+  } else {
+    std::lock_guard<std::mutex> lock(g_err_mutex);
+    msg = g_err;
+  }
+  size_t k = std::min(n - 1, msg.size());
+  memcpy(buf, msg.data(), k);
+  buf[k] = 0;
+  return TAM_OK;
+}
+
+int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **out) {
+  if (!ctx || !out) return fail(ctx, TAM_EINVAL, "tam_schedule_upload: NULL argument");
+  *out = nullptr;
+  int rc = validate(ctx, d);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(ctx->device);
+  if (!guard.ok()) return fail(ctx, TAM_ECUDA, "cannot make the context's device current");
+
+  tam_sched *s = new (std::nothrow) tam_sched;
+  if (!s) return fail(ctx, TAM_ENOMEM, "out of host memory");
+  s->ctx = ctx;
+  s->D = d->ndim;
+  s->dtype = d->dtype;
+  for (int k = 0; k < 3; ++k) s->S[k] = k < d->ndim ? d->stored[k] : 1;
+  s->nblocks = d->nblocks;
+  s->nfactorcols = d->nfactorcols;
+  s->ntransfers = d->ntransfers;
+  s->host_groups.assign(d->groups, d->groups + d->ngroups);
+
+  // Device groups, with a unit pad entry (srcstart 1, weight 1) for the
+  // dimensions beyond D.
+  std::vector<int32_t> srcstart(d->srcstart, d->srcstart + d->nsrcstart);
+  const int64_t pad_ss = (int64_t)srcstart.size();
+  srcstart.push_back(1);
+  const size_t esz = d->dtype == TAM_F64 ? 8 : 4;
+  std::vector<unsigned char> weights((size_t)(d->nweights + 1) * esz);
+  if (d->nweights) memcpy(weights.data(), d->weights, (size_t)d->nweights * esz);
+  const int64_t pad_w = d->nweights;
+  if (d->dtype == TAM_F64) {
+    double one = 1.0;
+    memcpy(weights.data() + pad_w * esz, &one, esz);
+  } else {
+    float one = 1.0f;
+    memcpy(weights.data() + pad_w * esz, &one, esz);
+  }
+
+  s->groups.resize(d->ngroups);
+  for (int32_t gi = 0; gi < d->ngroups; ++gi) {
+    const tam_group &h = d->groups[gi];
+    tam::DevGroup &g = s->groups[gi];
+    memset(&g, 0, sizeof g);
+    bool unit = true, uniform = true;
+    int p0 = h.stencil[0].order;
+    for (int k = 0; k < 3; ++k) {
+      if (k < d->ndim) {
+        const tam_stencil &st = h.stencil[k];
+        g.n[k] = st.ntarget;
+        g.tf[k] = st.targetfirst - 1;
+        g.order[k] = st.order;
+        g.ss[k] = st.srcstart;
+        g.w[k] = st.weights;
+        unit = unit && st.unit;
+        uniform = uniform && st.order == p0;
+      } else {
+        g.n[k] = 1;
+        g.tf[k] = 0;
+        g.order[k] = 1;
+        g.ss[k] = pad_ss;
+        g.w[k] = pad_w;
+      }
+    }
+    g.unit = unit ? 1 : 0;
+    g.factorcol = h.factorcol;
+    g.pclass = unit ? 0 : (uniform && (p0 == 2 || p0 == 3 || p0 == 4 || p0 == 6)) ? p0 : -1;
+    g.first = h.first;
+    g.ntransfers = h.ntransfers;
+    if (h.factorcol != 0) s->needs_factors = true;
+    s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
+  }
+
+  // Stages in tag order, and the fused tiles of each: ordered by target
+  // block, then group, then box position.
+  std::map<int32_t, std::vector<int32_t>> bytag;
+  for (int32_t gi = 0; gi < d->ngroups; ++gi) bytag[d->groups[gi].stage].push_back(gi);
+  std::vector<tam::Tile> tiles;
+  const int ti = s->shape.tile_items;
+  for (auto &kv : bytag) {
+    tam::Stage st;
+    st.tag = kv.first;
+    st.groups = kv.second;
+    st.tile0 = (int64_t)tiles.size();
+    struct Entry {
+      int32_t tblock, group, transfer;
+    };
+    std::vector<Entry> entries;
+    for (int32_t gi : st.groups) {
+      const tam::DevGroup &g = s->groups[gi];
+      for (int64_t t = 0; t < g.ntransfers; ++t)
+        entries.push_back({d->targetblocks[g.first + t], gi, (int32_t)(g.first + t)});
+    }
+    std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
+      return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
+    });
+    for (const Entry &e : entries) {
+      const tam::DevGroup &g = s->groups[e.group];
+      const int box = g.n[0] * g.n[1] * g.n[2];
+      for (int i0 = 0; i0 < box; i0 += ti)
+        tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+    }
+    st.ntiles = (int64_t)tiles.size() - st.tile0;
+    s->stages.push_back(st);
+  }
+
+  cudaError_t e;
+  if ((e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
+      (e = upload(&s->d_tb, d->targetblocks, (size_t)d->ntransfers)) != cudaSuccess ||
+      (e = upload(&s->d_sb, d->sourceblocks, (size_t)d->ntransfers)) != cudaSuccess ||
+      (e = upload(&s->d_srcstart, srcstart.data(), srcstart.size())) != cudaSuccess ||
+      (e = upload((unsigned char **)&s->d_weights, weights.data(), weights.size())) !=
+          cudaSuccess ||
+      (e = upload(&s->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
+      (e = upload(&s->d_err, (const int32_t *)nullptr, 1)) != cudaSuccess) {
+    free_sched_device(s);
+    delete s;
+    return e == cudaErrorMemoryAllocation ? fail(ctx, TAM_ENOMEM, "device allocation failed")
+                                          : cuda_fail(ctx, e, "schedule upload");
+  }
+  *out = s;
+  return TAM_OK;
+}
+
+void tam_schedule_free(tam_sched *s) {
+  if (!s) return;
+  DeviceGuard guard(s->ctx->device);
+  free_sched_device(s);
+  delete s;
+}
+
+int tam_schedule_info(const tam_sched *s, int64_t *ngroups, int64_t *ntransfers, int64_t *points,
+                      int32_t *nstages) {
+  if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_info: NULL schedule");
+  if (ngroups) *ngroups = (int64_t)s->groups.size();
+  if (ntransfers) *ntransfers = s->ntransfers;
+  if (points) *points = s->points;
+  if (nstages) *nstages = (int32_t)s->stages.size();
+  return TAM_OK;
+}
+
+static int check_fill_args(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
+                           const void *factors) {
+  if (!s) return fail(nullptr, TAM_EINVAL, "fill: NULL schedule");
+  tam_ctx *ctx = s->ctx;
+  if (!work) return fail(ctx, TAM_EINVAL, "fill: work is NULL");
+  if (nvars < 1) return fail(ctx, TAM_EINVAL, "fill: nvars must be positive");
+  if (nblocks != s->nblocks)
+    return fail(ctx, TAM_ELAYOUT, "fill: the field set's block count differs from the schedule's");
+  if (s->needs_factors && !factors)
+    return fail(ctx, TAM_EINVAL,
+                "this schedule mirrors ghosts across a reflecting face, but no factor table "
+                "was given (src/ghosts.jl:426-429)");
+  return TAM_OK;
+}
+
+int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
+             int32_t first_stage, int32_t last_stage, void *stream) {
+  int rc = check_fill_args(s, work, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  cudaStream_t st = (cudaStream_t)stream;
+  for (const tam::Stage &stage : s->stages) {
+    if (stage.tag < first_stage || stage.tag > last_stage) continue;
+    cudaError_t e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles + stage.tile0,
+                                            stage.ntiles, s->d_groups, s->d_tb, s->d_sb,
+                                            s->d_srcstart, s->d_weights, work, factors, nvars, s->S,
+                                            s->shape.threads, st);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
+  }
+  return TAM_OK;
+}
+
+int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
+                   int32_t first_stage, int32_t last_stage, void *stream) {
+  int rc = check_fill_args(s, work, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  cudaStream_t st = (cudaStream_t)stream;
+  for (const tam::Stage &stage : s->stages) {
+    if (stage.tag < first_stage || stage.tag > last_stage) continue;
+    for (int32_t gi : stage.groups) {
+      cudaError_t e = tam::launch_plain_group(s->dtype, s->D, s->groups[gi], s->d_groups + gi,
+                                              s->d_tb, s->d_sb, s->d_srcstart, s->d_weights, work,
+                                              factors, nvars, s->S, st);
+      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "plain group launch");
+    }
+  }
+  return TAM_OK;
+}
+
+int tam_device_status(tam_sched *s, void *stream, int32_t *code) {
+  if (!s || !code) return fail(nullptr, TAM_EINVAL, "tam_device_status: NULL argument");
+  DeviceGuard guard(s->ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, s->d_err, sizeof h, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "tam_device_status");
+  *code = h;
+  return TAM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,100 @@
+// Internal types of libtreeamr_cuda.so shared by the host API and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "treeamr_cuda.h"
+
+namespace tam {
+
+// A TransferGroup as the kernels read it: the host descriptor with the
+// stored-index offsets made 0-based and unused dimensions padded to one
+// row of one unit weight, so a kernel for D < 3 is the D = 3 kernel with
+// trip counts of one.
+struct DevGroup {
+  int32_t n[3];      // target rows per dimension
+  int32_t tf[3];     // targetfirst - 1
+  int32_t order[3];  // weights per column
+  int32_t unit;      // every dimension is a unit copy
+  int32_t factorcol; // 0 or the 1-based factor column
+  int32_t pclass;    // 0: copy, P > 0: uniform order P, -1: mixed orders
+  int64_t ss[3];     // srcstart pool offsets (0-based entries)
+  int64_t w[3];      // weight pool offsets
+  int64_t first;     // block-list offset
+  int64_t ntransfers;
+};
+
+// A warp's share of one transfer: box points [item0, item0 + nitems) of
+// transfer `transfer` (an index into the block lists) of group `group`.
+// Every variable of those points is the same warp's.
+struct Tile {
+  int32_t group;
+  int32_t transfer;
+  int32_t item0;
+  int32_t nitems;
+};
+
+struct Stage {
+  int32_t tag;
+  std::vector<int32_t> groups;  // indices into the schedule's groups
+  int64_t tile0 = 0;            // first tile in the schedule's tile array
+  int64_t ntiles = 0;
+};
+
+struct LaunchShape {
+  int tile_items = 128;     // box points per tile
+  int threads = 256;        // threads per CTA of the fused kernel
+};
+
+}  // namespace tam
+
+struct tam_ctx {
+  int device = 0;
+  int nsm = 0;
+  std::string err;
+};
+
+struct tam_sched {
+  tam_ctx *ctx = nullptr;
+  int D = 0;
+  int dtype = 0;
+  int S[3] = {1, 1, 1};
+  int64_t nblocks = 0;
+  int32_t nfactorcols = 0;
+  bool needs_factors = false;
+  std::vector<tam_group> host_groups;
+  std::vector<tam::DevGroup> groups;
+  std::vector<tam::Stage> stages;
+  int64_t ntransfers = 0;
+  int64_t points = 0;
+  tam::LaunchShape shape;
+  // device arrays
+  tam::DevGroup *d_groups = nullptr;
+  int32_t *d_tb = nullptr;
+  int32_t *d_sb = nullptr;
+  int32_t *d_srcstart = nullptr;
+  void *d_weights = nullptr;
+  tam::Tile *d_tiles = nullptr;
+  int32_t *d_err = nullptr;
+};
+
+namespace tam {
+
+// Kernel launchers (tam_kernels.cu).  All asynchronous on `stream`.
+cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
+                               const int32_t *tb, const int32_t *sb, const int32_t *srcstart,
+                               const void *weights, void *work, const void *factors,
+                               int nvars, const int S[3], cudaStream_t stream);
+
+cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntiles,
+                               const DevGroup *groups, const int32_t *tb, const int32_t *sb,
+                               const int32_t *srcstart, const void *weights, void *work,
+                               const void *factors, int nvars, const int S[3], int threads,
+                               cudaStream_t stream);
+
+}  // namespace tam

@@ -1,0 +1,132 @@
+"""``fill_ghosts``: replay a GhostSchedule on the GPU through libtreeamr_cuda.so.
+
+Mirrors the reference's entry point ``fill_ghosts!(fs, schedule; boundary)``
+(``src/ghosts.jl:1783-1794``) with its checks (``check_fill``,
+``src/ghosts.jl:2058-2101``) and stage order (``exchange_ghosts!``,
+``src/ghosts.jl:1099-1160``): stage P, stage 0, phase 1, the boundary hook,
+then the prolongations coarsest target level first.  The stages run on the
+device; only the hook, when one is given, runs between two library calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Optional
+
+import numpy as np
+import torch
+
+from . import _native
+from .schedule import GhostSchedule, PHASE1_TAG
+from .storage import FieldSet
+
+METHODS = ("fused", "plain")
+
+
+class DeviceSchedule:
+    """A schedule uploaded to one device (``tam_schedule_upload``).  Freed
+    with the object."""
+
+    def __init__(self, schedule: GhostSchedule, device: int):
+        self.lib = _native.lib()
+        self.ctx = _native.context(device)
+        self.desc = _native.Descriptor(schedule)
+        handle = C.c_void_p()
+        _native.check(self.lib.tam_schedule_upload(self.ctx, self.desc.ref(), C.byref(handle)),
+                      self.ctx, "tam_schedule_upload")
+        self.handle = handle
+        self.device = device
+        ng, nt, pts = C.c_int64(), C.c_int64(), C.c_int64()
+        ns = C.c_int32()
+        self.lib.tam_schedule_info(handle, C.byref(ng), C.byref(nt), C.byref(pts), C.byref(ns))
+        self.ngroups, self.ntransfers, self.points, self.nstages = ng.value, nt.value, pts.value, ns.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.tam_schedule_free(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def run(self, fs: FieldSet, first: int, last: int, method: str = "fused",
+            stream: Optional[torch.cuda.Stream] = None):
+        fn = {"fused": self.lib.tam_fill, "plain": self.lib.tam_fill_plain}[method]
+        s = stream if stream is not None else torch.cuda.current_stream(fs.work.device)
+        rc = fn(self.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars, fs.nblocks(),
+                C.c_void_p(fs.factors.data_ptr()), first, last, C.c_void_p(s.cuda_stream))
+        _native.check(rc, self.ctx, f"tam_fill ({method})")
+
+    def status(self, fs: FieldSet) -> int:
+        code = C.c_int32()
+        s = torch.cuda.current_stream(fs.work.device)
+        _native.check(self.lib.tam_device_status(self.handle, C.c_void_p(s.cuda_stream),
+                                                 C.byref(code)), self.ctx, "tam_device_status")
+        return code.value
+
+
+def device_schedule(schedule: GhostSchedule, device: int) -> DeviceSchedule:
+    """The schedule's upload to ``device``, made once and cached on it."""
+    cache = schedule.__dict__.setdefault("_device", {})
+    if device not in cache:
+        cache[device] = DeviceSchedule(schedule, device)
+    return cache[device]
+
+
+def check_fill(fs: FieldSet, schedule: GhostSchedule):
+    """The reference's refusals before any launch (``src/ghosts.jl:2058-2101``)."""
+    if fs.forest is not schedule.forest:
+        raise ValueError("the field set and the schedule are over different forests")
+    if schedule.isstale():
+        raise ValueError("the schedule is stale: the forest changed since it was built; "
+                         "rebuild it (GhostSchedule(fs, ops))")
+    if fs.generation != schedule.forest.generation:
+        raise ValueError("the field set is stale: the forest changed since it was allocated")
+    if fs.G != schedule.G:
+        raise ValueError(f"the schedule was built for G={schedule.G}, the field set has G={fs.G}")
+    if fs.centering != schedule.centering:
+        raise ValueError(f"the schedule was built for centering {schedule.centering}, "
+                         f"the field set has {fs.centering}")
+    if fs.T != schedule.T:
+        raise ValueError(f"the schedule was built for {schedule.T}, the field set holds {fs.T}")
+    if fs.work.device.type != "cuda":
+        raise ValueError("fill_ghosts runs on the GPU: the field set must live on a CUDA device")
+
+
+def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Callable] = None,
+                method: str = "fused", stream: Optional[torch.cuda.Stream] = None) -> FieldSet:
+    """Fill every ghost of ``fs`` from its neighbours (``fill_ghosts!``).
+
+    ``boundary(fs, regions)`` fills the regions facing out through outer faces;
+    it runs after phase 1 and before the prolongations, as the reference's
+    hook does (``src/ghosts.jl:1129-1136``).  ``method`` picks the fused
+    batched launch (default) or the plain one-launch-per-group replay."""
+    if method not in METHODS:
+        raise ValueError(f"method must be one of {METHODS}")
+    check_fill(fs, schedule)
+    ds = device_schedule(schedule, fs.work.device.index or 0)
+    if boundary is None or not schedule.boundaries:
+        ds.run(fs, _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST, method, stream)
+        return fs
+    ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
+    boundary(fs, schedule.boundaries)
+    ds.run(fs, PHASE1_TAG + 1, _native.TAM_STAGE_ALL_LAST, method, stream)
+    return fs
+
+
+def boundary_by_coordinates(fn: Callable):
+    """A hook that sets every outer-face ghost to ``fn(x, v)`` at its position
+    (``src/ghosts.jl:1400-1440``, the form the reference's tests use)."""
+    def hook(fs: FieldSet, regions):
+        host = fs.work.detach().cpu().numpy()
+        for r in regions:
+            pos = fs.positions(r.block)
+            axes = [pos[d][a - 1:z] for d, (a, z) in enumerate(r.region)]
+            grids = np.meshgrid(*axes, indexing="ij")
+            sl = tuple(slice(a - 1, z) for a, z in reversed(r.region))
+            for v in range(fs.nvars):
+                vals = np.broadcast_to(np.asarray(fn(tuple(grids), v), dtype=np.float64),
+                                       grids[0].shape)
+                host[(r.block, v) + sl] = vals.astype(fs.T).transpose()
+        fs.work.copy_(torch.from_numpy(host).to(fs.work.device))
+    return hook

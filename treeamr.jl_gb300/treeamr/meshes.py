@@ -1,0 +1,109 @@
+"""Seeded synthetic meshes and data of the ghost-fill workloads.
+
+The reference measures on synthetic meshes only (``bench/*.jl``); these are
+the meshes the engine is tested and benchmarked on, each built the way the
+reference's tests build theirs (``refine!`` then ``balance!``,
+``test/ghost_oracles.jl:275-343``).
+"""
+from __future__ import annotations
+
+import math
+from typing import Tuple
+
+import numpy as np
+
+from .forest import Forest
+from .operators import Operators
+from .storage import FieldSet
+
+
+def _box_meets_sphere(ext, center, r) -> bool:
+    lo2 = hi2 = 0.0
+    for (a, b), c in zip(ext, center):
+        near = min(max(c, a), b)
+        lo2 += (near - c) ** 2
+        hi2 += max((a - c) ** 2, (b - c) ** 2)
+    return lo2 <= r * r <= hi2
+
+
+def refine_where(forest: Forest, pred, levels):
+    """For each level in ``levels``: refine every leaf of that level where
+    ``pred(extent)`` holds, then balance."""
+    for lvl in levels:
+        targets = [k for k in forest.leaves if k.level == lvl and pred(forest.block_extent(k))]
+        if not targets:
+            continue
+        forest.refine(targets)
+        forest.balance()
+    return forest
+
+
+def quadrant_forest(seed: int = 0) -> Forest:
+    """2-D, 4x4 periodic roots, N = 8; a seeded quarter of the roots refined
+    once, then balanced (the CPU-sized correctness mesh)."""
+    rng = np.random.default_rng(seed)
+    f = Forest((4, 4), N=8, periodic=(True, True), extents=((0.0, 4.0), (0.0, 4.0)))
+    roots = list(f.leaves)
+    pick = rng.choice(len(roots), size=len(roots) // 4, replace=False)
+    f.refine([roots[i] for i in sorted(pick)])
+    f.balance()
+    return f
+
+
+def sphere_forest(roots: int = 8, N: int = 16, levels: int = 3, radius: float = 0.25) -> Forest:
+    """3-D, ``roots^3`` periodic roots over the unit cube; ``levels`` nested
+    refinements of every leaf whose box meets the sphere ``|x - 1/2| = radius``,
+    each followed by balance."""
+    f = Forest((roots,) * 3, N=N, periodic=(True,) * 3, extents=((0.0, 1.0),) * 3)
+    c = (0.5, 0.5, 0.5)
+    return refine_where(f, lambda ext: _box_meets_sphere(ext, c, radius), range(levels))
+
+
+def sphere_data(seed: int = 1, noise: float = 1e-3):
+    """``sin(2 pi x) sin(2 pi y) sin(2 pi z)`` plus seeded uniform noise."""
+    rng = np.random.default_rng(seed)
+
+    def fn(x, v):
+        base = np.sin(2 * math.pi * x[0]) * np.sin(2 * math.pi * x[1]) * np.sin(2 * math.pi * x[2])
+        return base + noise * rng.uniform(-1.0, 1.0, size=np.shape(x[0]))
+    return fn
+
+
+def uniform_data(seed: int = 1):
+    rng = np.random.default_rng(seed)
+
+    def fn(x, v):
+        return rng.uniform(-1.0, 1.0, size=np.shape(x[0]))
+    return fn
+
+
+def random_fill(fs: FieldSet, seed: int = 1, lo=-1.0, hi=1.0) -> FieldSet:
+    """Every stored point of ``fs`` seeded uniform in ``[lo, hi]`` (fast: no
+    positions)."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    host = torch.empty(tuple(fs.work.shape), dtype=fs.work.dtype).uniform_(lo, hi, generator=g)
+    fs.work.copy_(host)
+    return fs
+
+
+WORKLOADS = {
+    "quadrant": dict(desc="2-D 4x4 periodic roots, N=8, G=2, cell, 1 var F64, 25% of roots "
+                          "refined once, PV(4,4)"),
+    "sphere": dict(desc="3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, 3 levels nested "
+                        "around the sphere |x-1/2|=0.25, PV(4,4)"),
+}
+
+
+def quadrant_setup(device="cpu", seed=0):
+    f = quadrant_forest(seed)
+    fs = FieldSet(f, 1, G=2, T=np.float64, device=device)
+    ops = Operators(prolongation=4, restriction=4)
+    return f, fs, ops
+
+
+def sphere_setup(device="cpu", nvars=4, T=np.float64, roots=8, N=16, G=3, levels=3, p=4):
+    f = sphere_forest(roots=roots, N=N, levels=levels)
+    fs = FieldSet(f, nvars, G=G, T=T, device=device)
+    ops = Operators(prolongation=p, restriction=p)
+    return f, fs, ops
