@@ -201,6 +201,11 @@ def main():
         return ms / steps
 
     method = args.method
+    tuned = None
+    if method == "fused":
+        from treeamr.autotune import autotune
+        tuned = autotune(fs, sched)
+        cfg["tuned"] = tuned
     for _ in range(args.warmup):
         fill_ghosts(fs, sched, method=method)
     with ClockSampler(dev.index) as clk:

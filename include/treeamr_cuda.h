@@ -144,9 +144,27 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
                    const void *factors, int32_t first_stage, int32_t last_stage,
                    void *stream);
 
+/* Launch options of the fused fill, per schedule (no reference counterpart:
+ * the reference has no tuning; these are what the autotuner sets).  Changing
+ * one changes speed only, never a result. */
+#define TAM_OPT_TILE_ITEMS 1 /* box points per warp tile, 16..4096           */
+#define TAM_OPT_THREADS 2    /* threads per CTA, 64..512, a multiple of 32    */
+#define TAM_OPT_INT_MUL 3    /* 1: Float64 short-weight multiplies on the     */
+                             /* integer pipe (see tam_selftest), 0: FP64 pipe  */
+int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
+int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
+
 /* Read (and clear) the device error word of the schedule's last fills:
  * 0, or a tam_status a kernel recorded.  Synchronizes `stream`. */
 int tam_device_status(tam_sched *s, void *stream, int32_t *code);
+
+/* Built-in self-test, no reference counterpart: which = 1 compares the
+ * integer-pipe Float64 multiply the fills use for short weight products
+ * with the hardware multiply on n pseudo-random pairs (all bit patterns of
+ * the data, specials included) and returns the number of results that
+ * differ in any bit (NaNs compared as one pattern).  Synchronous. */
+#define TAM_SELFTEST_MUL 1
+int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches);
 
 #ifdef __cplusplus
 }

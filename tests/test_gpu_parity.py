@@ -25,8 +25,9 @@ def _gpu_vs_oracle(fs_host, ops, method, *, host=None, boundary=False, exact=Non
     """Fill a copy of ``fs_host``'s data on the GPU and with the oracle."""
     s = GhostSchedule(fs_host, ops)
     if host is None:
-        host = fs_host.work.numpy().copy()
-    fs_host.work.copy_(torch.from_numpy(host))
+        host = fs_host.work.cpu().numpy().copy()
+    fs_host.work = torch.from_numpy(host.copy())
+    fs_host.factors = fs_host.factors.cpu()
     bv = None
     if boundary:
         def bv(h, fs_, regions):
@@ -169,3 +170,57 @@ def test_bad_descriptor_rejected_before_launch(cuda_lib):
     d.srcstart[0] = 1
     d.targetblocks[0] = 99
     assert cuda_lib.tam_schedule_upload(ctx, d.ref(), C.byref(h)) == -1
+
+
+def test_integer_pipe_multiply_matches_hardware(cuda_lib):
+    """The Float64 multiply the fused fill runs on the integer pipe equals the
+    hardware multiply in every bit, over 2^26 pairs of every data pattern."""
+    import ctypes as C
+    from treeamr import _native
+    ctx = _native.context(0)
+    bad = C.c_int64(-1)
+    for seed in (1, 2, 3):
+        _native.check(cuda_lib.tam_selftest(ctx, 1, 1 << 26, seed, C.byref(bad)), ctx,
+                      "tam_selftest")
+        assert bad.value == 0
+
+
+def test_launch_options_change_no_bit(cuda_lib):
+    """Every launch option of the fused fill gives the same bits."""
+    from treeamr.ghosts import device_schedule
+    f, fs, ops = meshes.sphere_setup(nvars=3, roots=4, levels=2)
+    meshes.random_fill(fs, seed=21)
+    host = fs.work.numpy().copy()
+    s = GhostSchedule(fs, ops)
+    expect = oracle.fill_fieldset(fs, s)
+    fs.work = torch.from_numpy(host).cuda()
+    fs.factors = fs.factors.cuda()
+    ds = device_schedule(s, 0)
+    for ti, th, im in ((16, 64, 0), (37, 96, 1), (512, 512, 1), (4096, 128, 0)):
+        ds.set_option("tile_items", ti)
+        ds.set_option("threads", th)
+        ds.set_option("int_mul", im)
+        assert ds.options() == {"tile_items": ti, "threads": th, "int_mul": im}
+        fs.work.copy_(torch.from_numpy(host))
+        fill_ghosts(fs, s)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))
+    with pytest.raises(Exception):
+        ds.set_option("threads", 100)
+
+
+def test_autotune_keeps_results(cuda_lib):
+    from treeamr.autotune import autotune
+    f, fs, ops = meshes.sphere_setup(nvars=2, roots=4, levels=2)
+    meshes.random_fill(fs, seed=5)
+    host = fs.work.numpy().copy()
+    s = GhostSchedule(fs, ops)
+    expect = oracle.fill_fieldset(fs, s)
+    fs.work = torch.from_numpy(host).cuda()
+    fs.factors = fs.factors.cuda()
+    best = autotune(fs, s, reps=1, tile_items=(64, 256), threads=(128, 256))
+    assert set(best) == {"tile_items", "threads", "int_mul"}
+    fs.work.copy_(torch.from_numpy(host))
+    fill_ghosts(fs, s)
+    torch.cuda.synchronize()
+    assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))

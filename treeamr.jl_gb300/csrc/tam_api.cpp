@@ -69,11 +69,15 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_srcstart);
   cudaFree(s->d_weights);
   cudaFree(s->d_tiles);
+  cudaFree(s->d_cls);
+  cudaFree(s->d_wtab);
   cudaFree(s->d_err);
   s->d_groups = nullptr;
   s->d_tb = s->d_sb = s->d_srcstart = nullptr;
   s->d_weights = nullptr;
   s->d_tiles = nullptr;
+  s->d_cls = nullptr;
+  s->d_wtab = nullptr;
   s->d_err = nullptr;
 }
 
@@ -151,6 +155,115 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d) {
     }
   }
   return TAM_OK;
+}
+
+// The weight products of a uniform-order group: per dimension the distinct
+// weight columns ("classes") and each row's class, then for every class
+// combination the P^D products ((w_1*w_2)*w_3) rounded in T in that order
+// (src/ghosts.jl:58-74), which is what the reference forms per tap.  Only the
+// operand order matters for the bits: each product is one IEEE multiply.
+template <typename T>
+void build_product_table(const tam_schedule_desc *d, const tam_group &h, tam::DevGroup &g,
+                         std::vector<int32_t> &cls, std::vector<unsigned char> &wtab) {
+  const T *W = (const T *)d->weights;
+  const int P = h.stencil[0].order;
+  std::vector<std::vector<const T *>> columns(3);
+  for (int k = 0; k < 3; ++k) {
+    g.cls[k] = (int64_t)cls.size();
+    if (k >= d->ndim) {
+      g.C[k] = 1;
+      cls.push_back(0);
+      continue;
+    }
+    const tam_stencil &st = h.stencil[k];
+    for (int i = 0; i < st.ntarget; ++i) {
+      const T *col = W + st.weights + (int64_t)P * i;
+      int found = -1;
+      for (size_t c = 0; c < columns[k].size(); ++c)
+        if (memcmp(columns[k][c], col, sizeof(T) * P) == 0) {
+          found = (int)c;
+          break;
+        }
+      if (found < 0) {
+        found = (int)columns[k].size();
+        columns[k].push_back(col);
+      }
+      cls.push_back(found);
+    }
+    g.C[k] = (int32_t)columns[k].size();
+  }
+  const int P2 = d->ndim >= 2 ? P : 1, P3 = d->ndim >= 3 ? P : 1;
+  size_t off = wtab.size();
+  // element-aligned start
+  while (off % sizeof(T)) ++off;
+  g.wtab = (int64_t)(off / sizeof(T));
+  const int64_t count = (int64_t)g.C[0] * g.C[1] * g.C[2] * P * P2 * P3;
+  wtab.resize(off + count * sizeof(T));
+  T *out = (T *)(wtab.data() + off);
+  int64_t n = 0;
+  const T one = T(1);
+  for (int c3 = 0; c3 < g.C[2]; ++c3)
+    for (int c2 = 0; c2 < g.C[1]; ++c2)
+      for (int c1 = 0; c1 < g.C[0]; ++c1)
+        for (int m3 = 0; m3 < P3; ++m3)
+          for (int m2 = 0; m2 < P2; ++m2)
+            for (int m1 = 0; m1 < P; ++m1) {
+              const T w1 = columns[0][c1][m1];
+              const T w2 = d->ndim >= 2 ? columns[1][c2][m2] : one;
+              const T w3 = d->ndim >= 3 ? columns[2][c3][m3] : one;
+              volatile T p = w1;  // one rounding per multiply, in T, left to right
+              if (d->ndim >= 2) p = p * w2;
+              if (d->ndim >= 3) p = p * w3;
+              out[n++] = p;
+            }
+  // Float64 products whose significands fit 24 bits take the integer-pipe
+  // multiply (mul_short in tam_kernels.cu); it needs normal nonzero weights.
+  g.shortw = 0;
+  if (sizeof(T) == 8) {
+    bool ok = true;
+    for (int64_t i = 0; i < count && ok; ++i) {
+      uint64_t b;
+      memcpy(&b, &out[i], 8);
+      const uint64_t e = (b >> 52) & 0x7FF;
+      ok = e >= 1 && e <= 2046 && (b & ((1ull << 29) - 1)) == 0;
+    }
+    g.shortw = ok ? 1 : 0;
+  }
+}
+
+tam::SchedArgs sched_args(const tam_sched *s) {
+  return tam::SchedArgs{s->d_groups, s->d_tb, s->d_sb, s->d_srcstart, s->d_weights, s->d_cls,
+                        s->d_wtab, s->shape.int_mul};
+}
+
+// The fused tiles of every stage: each stage's transfers ordered by target
+// block, then group, each cut into runs of `tile_items` box points.
+std::vector<tam::Tile> build_tiles(tam_sched *s) {
+  std::vector<tam::Tile> tiles;
+  const int ti = s->shape.tile_items;
+  for (tam::Stage &st : s->stages) {
+    st.tile0 = (int64_t)tiles.size();
+    struct Entry {
+      int32_t tblock, group, transfer;
+    };
+    std::vector<Entry> entries;
+    for (int32_t gi : st.groups) {
+      const tam::DevGroup &g = s->groups[gi];
+      for (int64_t t = 0; t < g.ntransfers; ++t)
+        entries.push_back({s->h_tb[g.first + t], gi, (int32_t)(g.first + t)});
+    }
+    std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
+      return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
+    });
+    for (const Entry &e : entries) {
+      const tam::DevGroup &g = s->groups[e.group];
+      const int box = g.n[0] * g.n[1] * g.n[2];
+      for (int i0 = 0; i0 < box; i0 += ti)
+        tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+    }
+    st.ntiles = (int64_t)tiles.size() - st.tile0;
+  }
+  return tiles;
 }
 
 }  // namespace
@@ -232,6 +345,8 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
   }
 
   s->groups.resize(d->ngroups);
+  std::vector<int32_t> cls;
+  std::vector<unsigned char> wtab;
   for (int32_t gi = 0; gi < d->ngroups; ++gi) {
     const tam_group &h = d->groups[gi];
     tam::DevGroup &g = s->groups[gi];
@@ -263,40 +378,27 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
     g.ntransfers = h.ntransfers;
     if (h.factorcol != 0) s->needs_factors = true;
     s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
+    for (int k = 0; k < 3; ++k) g.C[k] = 1;
+    if (g.pclass > 1) {
+      if (d->dtype == TAM_F64)
+        build_product_table<double>(d, h, g, cls, wtab);
+      else
+        build_product_table<float>(d, h, g, cls, wtab);
+    }
   }
 
   // Stages in tag order, and the fused tiles of each: ordered by target
   // block, then group, then box position.
   std::map<int32_t, std::vector<int32_t>> bytag;
   for (int32_t gi = 0; gi < d->ngroups; ++gi) bytag[d->groups[gi].stage].push_back(gi);
-  std::vector<tam::Tile> tiles;
-  const int ti = s->shape.tile_items;
   for (auto &kv : bytag) {
     tam::Stage st;
     st.tag = kv.first;
     st.groups = kv.second;
-    st.tile0 = (int64_t)tiles.size();
-    struct Entry {
-      int32_t tblock, group, transfer;
-    };
-    std::vector<Entry> entries;
-    for (int32_t gi : st.groups) {
-      const tam::DevGroup &g = s->groups[gi];
-      for (int64_t t = 0; t < g.ntransfers; ++t)
-        entries.push_back({d->targetblocks[g.first + t], gi, (int32_t)(g.first + t)});
-    }
-    std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
-      return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
-    });
-    for (const Entry &e : entries) {
-      const tam::DevGroup &g = s->groups[e.group];
-      const int box = g.n[0] * g.n[1] * g.n[2];
-      for (int i0 = 0; i0 < box; i0 += ti)
-        tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
-    }
-    st.ntiles = (int64_t)tiles.size() - st.tile0;
     s->stages.push_back(st);
   }
+  s->h_tb.assign(d->targetblocks, d->targetblocks + d->ntransfers);
+  std::vector<tam::Tile> tiles = build_tiles(s);
 
   cudaError_t e;
   if ((e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
@@ -306,6 +408,8 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
       (e = upload((unsigned char **)&s->d_weights, weights.data(), weights.size())) !=
           cudaSuccess ||
       (e = upload(&s->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
+      (e = upload(&s->d_cls, cls.data(), cls.size())) != cudaSuccess ||
+      (e = upload((unsigned char **)&s->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
       (e = upload(&s->d_err, (const int32_t *)nullptr, 1)) != cudaSuccess) {
     free_sched_device(s);
     delete s;
@@ -358,9 +462,8 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
   for (const tam::Stage &stage : s->stages) {
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
     cudaError_t e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles + stage.tile0,
-                                            stage.ntiles, s->d_groups, s->d_tb, s->d_sb,
-                                            s->d_srcstart, s->d_weights, work, factors, nvars, s->S,
-                                            s->shape.threads, st);
+                                            stage.ntiles, sched_args(s), work, factors, nvars,
+                                            s->S, s->shape.threads, st);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
   }
   return TAM_OK;
@@ -377,11 +480,73 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, con
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
     for (int32_t gi : stage.groups) {
       cudaError_t e = tam::launch_plain_group(s->dtype, s->D, s->groups[gi], s->d_groups + gi,
-                                              s->d_tb, s->d_sb, s->d_srcstart, s->d_weights, work,
-                                              factors, nvars, s->S, st);
+                                              sched_args(s), work, factors, nvars, s->S, st);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "plain group launch");
     }
   }
+  return TAM_OK;
+}
+
+int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
+  if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_set_option: NULL schedule");
+  switch (option) {
+    case TAM_OPT_TILE_ITEMS: {
+      if (value < 16 || value > 4096)
+        return fail(s->ctx, TAM_EINVAL, "tile items must be in 16..4096");
+      if (value == s->shape.tile_items) return TAM_OK;
+      DeviceGuard guard(s->ctx->device);
+      const int old = s->shape.tile_items;
+      s->shape.tile_items = (int)value;
+      std::vector<tam::Tile> tiles = build_tiles(s);
+      tam::Tile *d = nullptr;
+      cudaError_t e = upload(&d, tiles.data(), tiles.size());
+      if (e != cudaSuccess) {
+        s->shape.tile_items = old;
+        build_tiles(s);
+        return cuda_fail(s->ctx, e, "re-tiling");
+      }
+      cudaDeviceSynchronize();  // no fill may still read the old tiles
+      cudaFree(s->d_tiles);
+      s->d_tiles = d;
+      return TAM_OK;
+    }
+    case TAM_OPT_THREADS:
+      if (value < 64 || value > 512 || value % 32)
+        return fail(s->ctx, TAM_EINVAL, "threads must be a multiple of 32 in 64..512");
+      s->shape.threads = (int)value;
+      return TAM_OK;
+    case TAM_OPT_INT_MUL:
+      if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "int_mul is 0 or 1");
+      s->shape.int_mul = (int)value;
+      return TAM_OK;
+    default:
+      return fail(s->ctx, TAM_EINVAL, "unknown option");
+  }
+}
+
+int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) {
+  if (!s || !value) return fail(nullptr, TAM_EINVAL, "tam_schedule_get_option: NULL argument");
+  switch (option) {
+    case TAM_OPT_TILE_ITEMS: *value = s->shape.tile_items; return TAM_OK;
+    case TAM_OPT_THREADS: *value = s->shape.threads; return TAM_OK;
+    case TAM_OPT_INT_MUL: *value = s->shape.int_mul; return TAM_OK;
+    default: return fail(s->ctx, TAM_EINVAL, "unknown option");
+  }
+}
+
+int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches) {
+  if (!ctx || !mismatches || n < 0) return fail(ctx, TAM_EINVAL, "tam_selftest: bad argument");
+  if (which != TAM_SELFTEST_MUL) return fail(ctx, TAM_EINVAL, "tam_selftest: unknown test");
+  DeviceGuard guard(ctx->device);
+  if (!guard.ok()) return fail(ctx, TAM_ECUDA, "cannot make the context's device current");
+  unsigned long long *d = nullptr, h = 0;
+  cudaError_t e = cudaMalloc((void **)&d, sizeof h);
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof h);
+  if (e == cudaSuccess) e = tam::launch_selftest_mul(n, seed, d, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tam_selftest");
+  *mismatches = (int64_t)h;
   return TAM_OK;
 }
 

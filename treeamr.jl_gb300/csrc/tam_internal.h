@@ -27,6 +27,16 @@ struct DevGroup {
   int64_t w[3];      // weight pool offsets
   int64_t first;     // block-list offset
   int64_t ntransfers;
+  // Uniform-order groups only: the weight products ((w_1*w_2)*w_3) of every
+  // combination of distinct weight columns, rounded in the element type in
+  // that order, so a tap costs one multiply and one add and the result is
+  // bit-identical to forming the product per tap.  Row i of dimension d has
+  // column class cls[d][i]; the products of classes (c1, c2, c3) start at
+  // wtab + ((c3 * C2 + c2) * C1 + c1) * P^D, taps m_1 fastest.
+  int32_t C[3];      // distinct columns per dimension
+  int32_t shortw;    // every product is normal with a significand of <= 24 bits
+  int64_t cls[3];    // class-index pool offsets (one int32 per target row)
+  int64_t wtab;      // product-table pool offset
 };
 
 // A warp's share of one transfer: box points [item0, item0 + nitems) of
@@ -49,6 +59,7 @@ struct Stage {
 struct LaunchShape {
   int tile_items = 128;     // box points per tile
   int threads = 256;        // threads per CTA of the fused kernel
+  int int_mul = 0;          // Float64 short-weight multiplies on the integer pipe
 };
 
 }  // namespace tam
@@ -68,6 +79,7 @@ struct tam_sched {
   int32_t nfactorcols = 0;
   bool needs_factors = false;
   std::vector<tam_group> host_groups;
+  std::vector<int32_t> h_tb;  // target blocks, for re-tiling
   std::vector<tam::DevGroup> groups;
   std::vector<tam::Stage> stages;
   int64_t ntransfers = 0;
@@ -79,6 +91,8 @@ struct tam_sched {
   int32_t *d_sb = nullptr;
   int32_t *d_srcstart = nullptr;
   void *d_weights = nullptr;
+  int32_t *d_cls = nullptr;
+  void *d_wtab = nullptr;
   tam::Tile *d_tiles = nullptr;
   int32_t *d_err = nullptr;
 };
@@ -86,15 +100,27 @@ struct tam_sched {
 namespace tam {
 
 // Kernel launchers (tam_kernels.cu).  All asynchronous on `stream`.
+// The read-only schedule arrays every kernel gets.
+struct SchedArgs {
+  const DevGroup *groups;
+  const int32_t *tb;
+  const int32_t *sb;
+  const int32_t *srcstart;
+  const void *weights;
+  const int32_t *cls;
+  const void *wtab;
+  int int_mul;
+};
+
 cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
-                               const int32_t *tb, const int32_t *sb, const int32_t *srcstart,
-                               const void *weights, void *work, const void *factors,
-                               int nvars, const int S[3], cudaStream_t stream);
+                               const SchedArgs &a, void *work, const void *factors, int nvars,
+                               const int S[3], cudaStream_t stream);
 
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntiles,
-                               const DevGroup *groups, const int32_t *tb, const int32_t *sb,
-                               const int32_t *srcstart, const void *weights, void *work,
-                               const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream);
+                               const SchedArgs &a, void *work, const void *factors, int nvars,
+                               const int S[3], int threads, cudaStream_t stream);
+
+cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                cudaStream_t stream);
 
 }  // namespace tam

@@ -82,92 +82,301 @@ __device__ __forceinline__ T scaled(T acc, const T *__restrict__ factors, int v,
   return A::add(A::mul(acc, __ldg(factors + v + (int64_t)nvars * (fcol - 1))), T(0));
 }
 
-// Everything one item needs from its group and transfer.
-struct ItemGeom {
-  int64_t tbase;  // element offset of (tidx, v = 0) in work
-  int64_t sbase;  // element offset of (base, v = 0) in work
-  int wcol[3];    // target row per dimension (weight column)
+// The item at box point (i1, i2, i3) of transfer (tblock, sblock), every
+// variable in [v0, v1).
+template <typename T>
+struct Args {
+  const DevGroup *__restrict__ groups;
+  const int32_t *__restrict__ tb;
+  const int32_t *__restrict__ sb;
+  const int32_t *__restrict__ srcstart;
+  const T *__restrict__ weights;
+  const int32_t *__restrict__ cls;
+  const T *__restrict__ wtab;
+  int int_mul;
 };
 
-// The body shared by both launch forms: the item at box point (i1, i2, i3)
-// of transfer (tblock, sblock), every variable in [v0, v1).
-template <typename T, int D, int P>
-__device__ __forceinline__ void do_point(const DevGroup &g, int i1, int i2, int i3,
+template <typename T>
+__host__ __device__ inline Args<T> typed(const SchedArgs &a) {
+  return Args<T>{a.groups, a.tb, a.sb, a.srcstart, (const T *)a.weights, a.cls,
+                 (const T *)a.wtab, a.int_mul};
+}
+
+struct Geom {
+  int64_t toff;     // element offset of the target point, variable 0
+  int64_t soff;     // element offset of the source window's first point, variable 0
+  int64_t vstride;  // elements between variables
+  int64_t s2, s3;   // strides of dimensions 2 and 3
+};
+
+template <int D>
+__device__ __forceinline__ Geom geometry(const DevGroup &g, int i1, int i2, int i3,
                                          int64_t tblock, int64_t sblock,
-                                         const int32_t *__restrict__ srcstart,
-                                         const T *__restrict__ weights, T *work,
-                                         const T *__restrict__ factors, int nvars, int v0, int v1,
-                                         int S1, int S2, int S3) {
-  using A = Arith<T>;
-  const int64_t s2 = S1, s3 = (int64_t)S1 * S2;
-  const int64_t vstride = s3 * S3;
-  const int64_t bstride = vstride * nvars;
+                                         const int32_t *__restrict__ srcstart, int nvars, int S1,
+                                         int S2, int S3) {
+  Geom o;
+  o.s2 = S1;
+  o.s3 = (int64_t)S1 * S2;
+  o.vstride = o.s3 * S3;
+  const int64_t bstride = o.vstride * nvars;
   const int b1 = __ldg(srcstart + g.ss[0] + i1) - 1;
   const int b2 = D >= 2 ? __ldg(srcstart + g.ss[1] + i2) - 1 : 0;
   const int b3 = D >= 3 ? __ldg(srcstart + g.ss[2] + i3) - 1 : 0;
-  const int64_t toff = tblock * bstride + (int64_t)(g.tf[0] + i1) +
-                       (D >= 2 ? (int64_t)(g.tf[1] + i2) * s2 : 0) +
-                       (D >= 3 ? (int64_t)(g.tf[2] + i3) * s3 : 0);
-  const int64_t soff = sblock * bstride + b1 + (int64_t)b2 * s2 + (int64_t)b3 * s3;
-  if (P == 1) {  // a unit copy: +0 + x (src/ghosts.jl:127-128)
-    for (int v = v0; v < v1; ++v) {
-      T x = A::add(T(0), work[soff + v * vstride]);
-      work[toff + v * vstride] = scaled(x, factors, v, nvars, g.factorcol);
-    }
-    return;
+  o.toff = tblock * bstride + (int64_t)(g.tf[0] + i1) +
+           (D >= 2 ? (int64_t)(g.tf[1] + i2) * o.s2 : 0) +
+           (D >= 3 ? (int64_t)(g.tf[2] + i3) * o.s3 : 0);
+  o.soff = sblock * bstride + b1 + (int64_t)b2 * o.s2 + (int64_t)b3 * o.s3;
+  return o;
+}
+
+// +0 + x without the floating-point pipe: x itself, except that -0 becomes
+// +0 (IEEE round-to-nearest gives +0 for +0 + -0).  A NaN stays a NaN (its
+// payload kept rather than made canonical; NaNs compare as one pattern).
+// Used for the F64 copies, which would otherwise queue on the GB300's narrow
+// FP64 pipe.
+__device__ __forceinline__ double plus_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return b == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+__device__ __forceinline__ float plus_zero(float x) { return __fadd_rn(0.0f, x); }
+
+// RN(w * u) on the integer pipe, for a weight w whose significand has at
+// most 24 significant bits: wm is that significand as an integer in
+// [2^23, 2^24), we its unbiased exponent and wsign its sign bit (bit 31).
+// The exact product of the 53-bit and 24-bit significands (at most 77 bits)
+// is formed from two 32x32 multiplies, rounded to nearest-even at bit
+// 23 or 24, and packed; a zero, subnormal, infinite or NaN u, and a result
+// outside the normal range, take the hardware multiply instead.  Bit-identical
+// to __dmul_rn(w, u) on every input (checked by tam_selftest).
+__device__ __forceinline__ double mul_short(double w, uint32_t wm, int we, uint32_t wsign,
+                                            double u) {
+  const uint32_t uhi = (uint32_t)__double2hiint(u);
+  const uint32_t ulo = (uint32_t)__double2loint(u);
+  const int eu = (int)((uhi >> 20) & 0x7FF);
+  const uint32_t mh = (uhi & 0xFFFFFu) | 0x100000u;
+  const uint64_t t0 = (uint64_t)ulo * wm;                    // < 2^56
+  const uint64_t t1 = (uint64_t)mh * wm;                     // < 2^45
+  const uint32_t p0 = (uint32_t)t0;
+  const uint64_t mid = (t0 >> 32) + (uint32_t)t1;
+  const uint32_t p1 = (uint32_t)mid;
+  const uint32_t p2 = (uint32_t)(t1 >> 32) + (uint32_t)(mid >> 32);  // < 2^13
+  const uint32_t top = p2 >> 12;                             // the product has 77 bits
+  const uint32_t s = 23u + top;
+  const uint32_t lo = __funnelshift_r(p0, p1, s);
+  const uint32_t hi = __funnelshift_r(p1, p2, s);            // < 2^21
+  const uint32_t guard = (p0 >> (s - 1u)) & 1u;
+  const uint32_t sticky = (p0 & ((1u << (s - 1u)) - 1u)) != 0u;
+  const uint32_t inc = guard & (sticky | (lo & 1u));
+  uint64_t m = (((uint64_t)hi << 32) | lo) + inc;
+  int E = eu + we + (int)top;
+  if (m >> 53) {  // rounded up to 2^53
+    m >>= 1;
+    E += 1;
   }
-  const T *w1 = weights + g.w[0] + (int64_t)g.order[0] * i1;
-  const T *w2 = weights + g.w[1] + (int64_t)g.order[1] * i2;
-  const T *w3 = weights + g.w[2] + (int64_t)g.order[2] * i3;
-  for (int v = v0; v < v1; ++v) {
-    T acc = stencil_sum<T, D, (P > 1 ? P : 0)>(work + soff + v * vstride, s2, s3, w1, w2, w3,
-                                                g.order);
-    work[toff + v * vstride] = scaled(acc, factors, v, nvars, g.factorcol);
+  if ((unsigned)(eu - 1) >= 2046u || (unsigned)(E - 1) >= 2046u) return __dmul_rn(w, u);
+  const uint32_t rhi = ((uhi & 0x80000000u) ^ wsign) | ((uint32_t)E << 20) |
+                       ((uint32_t)(m >> 32) & 0xFFFFFu);
+  return __hiloint2double((int)rhi, (int)(uint32_t)m);
+}
+
+// The same multiply without the branch: `bad` is set where the fast path
+// does not apply, and the caller recomputes those points on the FP64 pipe.
+__device__ __forceinline__ double mul_short_flag(uint32_t wm, int we, uint32_t wsign, double u,
+                                                 bool &bad) {
+  const uint32_t uhi = (uint32_t)__double2hiint(u);
+  const uint32_t ulo = (uint32_t)__double2loint(u);
+  const int eu = (int)((uhi >> 20) & 0x7FF);
+  const uint32_t mh = (uhi & 0xFFFFFu) | 0x100000u;
+  const uint64_t t0 = (uint64_t)ulo * wm;
+  const uint64_t t1 = (uint64_t)mh * wm;
+  const uint32_t p0 = (uint32_t)t0;
+  const uint64_t mid = (t0 >> 32) + (uint32_t)t1;
+  const uint32_t p1 = (uint32_t)mid;
+  const uint32_t p2 = (uint32_t)(t1 >> 32) + (uint32_t)(mid >> 32);
+  const uint32_t top = p2 >> 12;
+  const uint32_t s = 23u + top;
+  const uint32_t lo = __funnelshift_r(p0, p1, s);
+  const uint32_t hi = __funnelshift_r(p1, p2, s);
+  const uint32_t guard = (p0 >> (s - 1u)) & 1u;
+  const uint32_t sticky = (p0 & ((1u << (s - 1u)) - 1u)) != 0u;
+  const uint32_t inc = guard & (sticky | (lo & 1u));
+  const uint64_t m0 = (((uint64_t)hi << 32) | lo) + inc;
+  const uint32_t carry = (uint32_t)(m0 >> 53);
+  const uint64_t m = m0 >> carry;
+  const int E = eu + we + (int)top + (int)carry;
+  bad |= ((unsigned)(eu - 1) >= 2046u) | ((unsigned)(E - 1) >= 2046u);
+  const uint32_t rhi = ((uhi & 0x80000000u) ^ wsign) | ((uint32_t)E << 20) |
+                       ((uint32_t)(m >> 32) & 0xFFFFFu);
+  return __hiloint2double((int)rhi, (int)(uint32_t)m);
+}
+
+// The parts of a weight mul_short takes.
+struct ShortW {
+  double w;
+  uint32_t wm, wsign;
+  int we;
+};
+__device__ __forceinline__ ShortW short_weight(double w) {
+  const uint32_t whi = (uint32_t)__double2hiint(w);
+  const uint32_t wlo = (uint32_t)__double2loint(w);
+  ShortW r;
+  r.w = w;
+  r.wm = (((whi & 0xFFFFFu) | 0x100000u) << 3) | (wlo >> 29);
+  r.we = (int)((whi >> 20) & 0x7FF) - 1023;
+  r.wsign = whi & 0x80000000u;
+  return r;
+}
+
+// A unit copy of every variable: +0 + x (src/ghosts.jl:127-128).
+template <typename T>
+__device__ __forceinline__ void copy_point(const DevGroup &g, const Geom &o, T *work,
+                                           const T *__restrict__ factors, int nvars) {
+  for (int v = 0; v < nvars; ++v) {
+    T x = plus_zero(work[o.soff + v * o.vstride]);
+    work[o.toff + v * o.vstride] = scaled(x, factors, v, nvars, g.factorcol);
   }
 }
 
+// A uniform order-P stencil through the group's product table: per tap one
+// multiply and one add per variable, the weight product loaded once for
+// VC variables at a time.
+template <typename T, int D, int P, int VC>
+__device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, int i3,
+                                            const Geom &o, const Args<T> &a, T *work,
+                                            const T *__restrict__ factors, int nvars) {
+  using A = Arith<T>;
+  constexpr int P2 = D >= 2 ? P : 1;
+  constexpr int P3 = D >= 3 ? P : 1;
+  constexpr int PD = P * P2 * P3;
+  const int c1 = __ldg(a.cls + g.cls[0] + i1);
+  const int c2 = D >= 2 ? __ldg(a.cls + g.cls[1] + i2) : 0;
+  const int c3 = D >= 3 ? __ldg(a.cls + g.cls[2] + i3) : 0;
+  const T *__restrict__ W = a.wtab + g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * PD;
+  if constexpr (sizeof(T) == 8) {
+    if (g.shortw && a.int_mul) {
+      // F64 with short weight products: the multiplies on the integer pipe,
+      // only the adds on the FP64 pipe.
+      for (int v0 = 0; v0 < nvars; v0 += VC) {
+        double acc[VC];
+#pragma unroll
+        for (int j = 0; j < VC; ++j) acc[j] = 0.0;
+        const double *src = work + o.soff + v0 * o.vstride;
+        bool bad = false;
+#pragma unroll 1
+        for (int m3 = 0; m3 < P3; ++m3) {
+#pragma unroll
+          for (int m2 = 0; m2 < P2; ++m2) {
+#pragma unroll
+            for (int m1 = 0; m1 < P; ++m1) {
+              const ShortW sw = short_weight(__ldg(W + (m3 * P2 + m2) * P + m1));
+              const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+              for (int j = 0; j < VC; ++j)
+                if (v0 + j < nvars) {
+                  const double p = mul_short_flag(sw.wm, sw.we, sw.wsign,
+                                                  src[off + j * o.vstride], bad);
+                  acc[j] = __dadd_rn(acc[j], p);
+                }
+            }
+          }
+        }
+        if (bad) {  // a zero, subnormal or special datum, or an out-of-range product
+#pragma unroll
+          for (int j = 0; j < VC; ++j) acc[j] = 0.0;
+#pragma unroll 1
+          for (int k = 0; k < PD; ++k) {
+            const int m1 = k % P, m2 = (k / P) % P2, m3 = k / (P * P2);
+            const double w = __ldg(W + k);
+            const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+            for (int j = 0; j < VC; ++j)
+              if (v0 + j < nvars) acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.vstride]));
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < VC; ++j)
+          if (v0 + j < nvars)
+            work[o.toff + (v0 + j) * o.vstride] =
+                scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
+      }
+      return;
+    }
+  }
+  for (int v0 = 0; v0 < nvars; v0 += VC) {
+    T acc[VC];
+#pragma unroll
+    for (int j = 0; j < VC; ++j) acc[j] = T(0);
+    const T *src = work + o.soff + v0 * o.vstride;
+#pragma unroll
+    for (int m3 = 0; m3 < P3; ++m3) {
+#pragma unroll
+      for (int m2 = 0; m2 < P2; ++m2) {
+#pragma unroll
+        for (int m1 = 0; m1 < P; ++m1) {
+          const T w = __ldg(W + (m3 * P2 + m2) * P + m1);
+          const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+          for (int j = 0; j < VC; ++j)
+            if (v0 + j < nvars) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.vstride]));
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < VC; ++j)
+      if (v0 + j < nvars)
+        work[o.toff + (v0 + j) * o.vstride] = scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
+  }
+}
+
+// Mixed orders: the reference's nest with the product formed per tap.
 template <typename T, int D>
-__device__ __forceinline__ void dispatch_point(const DevGroup &g, int i1, int i2, int i3,
-                                               int64_t tblock, int64_t sblock,
-                                               const int32_t *__restrict__ srcstart,
-                                               const T *__restrict__ weights, T *work,
-                                               const T *__restrict__ factors, int nvars, int v0,
-                                               int v1, int S1, int S2, int S3) {
+__device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2, int i3,
+                                              const Geom &o, const Args<T> &a, T *work,
+                                              const T *__restrict__ factors, int nvars) {
+  const T *w1 = a.weights + g.w[0] + (int64_t)g.order[0] * i1;
+  const T *w2 = a.weights + g.w[1] + (int64_t)g.order[1] * i2;
+  const T *w3 = a.weights + g.w[2] + (int64_t)g.order[2] * i3;
+  for (int v = 0; v < nvars; ++v) {
+    T acc = stencil_sum<T, D, 0>(work + o.soff + v * o.vstride, o.s2, o.s3, w1, w2, w3, g.order);
+    work[o.toff + v * o.vstride] = scaled(acc, factors, v, nvars, g.factorcol);
+  }
+}
+
+// Every variable of one box point of one transfer, by the group's class.
+template <typename T, int D>
+__device__ __forceinline__ void do_point(const DevGroup &g, int i1, int i2, int i3,
+                                         int64_t tblock, int64_t sblock, const Args<T> &a,
+                                         T *work, const T *__restrict__ factors, int nvars,
+                                         int S1, int S2, int S3) {
+  const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
   switch (g.pclass) {
     case 0:
-      do_point<T, D, 1>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      copy_point<T>(g, o, work, factors, nvars);
       break;
     case 2:
-      do_point<T, D, 2>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      table_point<T, D, 2, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
       break;
     case 3:
-      do_point<T, D, 3>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      table_point<T, D, 3, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
       break;
     case 4:
-      do_point<T, D, 4>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      table_point<T, D, 4, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
       break;
     case 6:
-      do_point<T, D, 6>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      table_point<T, D, 6, 2>(g, i1, i2, i3, o, a, work, factors, nvars);
       break;
     default:
-      do_point<T, D, 0>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                        v0, v1, S1, S2, S3);
+      generic_point<T, D>(g, i1, i2, i3, o, a, work, factors, nvars);
       break;
   }
 }
 
 // ---- plain: one launch per group, one thread per (point, variable) ---------
 template <typename T, int D>
-__global__ void __launch_bounds__(256) plain_group_kernel(
-    const DevGroup *__restrict__ gp, const int32_t *__restrict__ tb,
-    const int32_t *__restrict__ sb, const int32_t *__restrict__ srcstart,
-    const T *__restrict__ weights, T *work, const T *__restrict__ factors, int nvars, int S1,
-    int S2, int S3) {
+__global__ void __launch_bounds__(256) plain_group_kernel(const DevGroup *__restrict__ gp,
+                                                          Args<T> a, T *work,
+                                                          const T *__restrict__ factors,
+                                                          int nvars, int S1, int S2, int S3) {
   const DevGroup g = *gp;
   const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
   const int64_t items = box * nvars * g.ntransfers;
@@ -182,28 +391,46 @@ __global__ void __launch_bounds__(256) plain_group_kernel(
     r /= g.n[2];
     const int v = (int)(r % nvars);
     const int64_t t = r / nvars + g.first;
-    const int64_t tblock = __ldg(tb + t) - 1;
-    const int64_t sblock = __ldg(sb + t) - 1;
-    dispatch_point<T, D>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                         v, v + 1, S1, S2, S3);
+    const int64_t tblock = __ldg(a.tb + t) - 1;
+    const int64_t sblock = __ldg(a.sb + t) - 1;
+    // one variable: the point as a one-variable field at variable v's offset
+    const int64_t vs = (int64_t)S1 * S2 * S3;
+    Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
+    o.toff += v * vs;
+    o.soff += v * vs;
+    if (g.pclass == 0) {
+      using A = Arith<T>;
+      T x = A::add(T(0), work[o.soff]);
+      work[o.toff] = scaled(x, factors, v, nvars, g.factorcol);
+    } else {
+      const T *w1 = a.weights + g.w[0] + (int64_t)g.order[0] * i1;
+      const T *w2 = a.weights + g.w[1] + (int64_t)g.order[1] * i2;
+      const T *w3 = a.weights + g.w[2] + (int64_t)g.order[2] * i3;
+      T acc;
+      switch (g.pclass) {
+        case 2: acc = stencil_sum<T, D, 2>(work + o.soff, o.s2, o.s3, w1, w2, w3, g.order); break;
+        case 4: acc = stencil_sum<T, D, 4>(work + o.soff, o.s2, o.s3, w1, w2, w3, g.order); break;
+        default: acc = stencil_sum<T, D, 0>(work + o.soff, o.s2, o.s3, w1, w2, w3, g.order); break;
+      }
+      work[o.toff] = scaled(acc, factors, v, nvars, g.factorcol);
+    }
   }
 }
 
 // ---- fused: one launch per stage, one warp per tile ---------------------------
 template <typename T, int D>
-__global__ void __launch_bounds__(256) fused_stage_kernel(
-    const Tile *__restrict__ tiles, int64_t ntiles, const DevGroup *__restrict__ groups,
-    const int32_t *__restrict__ tb, const int32_t *__restrict__ sb,
-    const int32_t *__restrict__ srcstart, const T *__restrict__ weights, T *work,
-    const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
+__global__ void __launch_bounds__(512) fused_stage_kernel(const Tile *__restrict__ tiles,
+                                                          int64_t ntiles, Args<T> a, T *work,
+                                                          const T *__restrict__ factors,
+                                                          int nvars, int S1, int S2, int S3) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
        w += warps) {
     const Tile tile = tiles[w];
-    const DevGroup &g = groups[tile.group];
-    const int64_t tblock = __ldg(tb + tile.transfer) - 1;
-    const int64_t sblock = __ldg(sb + tile.transfer) - 1;
+    const DevGroup &g = a.groups[tile.group];
+    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
+    const int64_t sblock = __ldg(a.sb + tile.transfer) - 1;
     const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
     for (int k = lane; k < tile.nitems; k += 32) {
       const int item = tile.item0 + k;
@@ -211,16 +438,15 @@ __global__ void __launch_bounds__(256) fused_stage_kernel(
       const int rem = item - i3 * n12;
       const int i2 = rem / n1;
       const int i1 = rem - i2 * n1;
-      dispatch_point<T, D>(g, i1, i2, i3, tblock, sblock, srcstart, weights, work, factors, nvars,
-                           0, nvars, S1, S2, S3);
+      do_point<T, D>(g, i1, i2, i3, tblock, sblock, a, work, factors, nvars, S1, S2, S3);
     }
   }
 }
 
 template <typename T>
-cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const int32_t *tb,
-                           const int32_t *sb, const int32_t *srcstart, const T *weights, T *work,
-                           const T *factors, int nvars, const int S[3], cudaStream_t stream) {
+cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const Args<T> &a,
+                           T *work, const T *factors, int nvars, const int S[3],
+                           cudaStream_t stream) {
   const int64_t items = (int64_t)g.n[0] * g.n[1] * g.n[2] * nvars * g.ntransfers;
   if (items == 0) return cudaSuccess;
   const int threads = 256;
@@ -228,26 +454,25 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
   if (blocks > (int64_t)1 << 30) blocks = (int64_t)1 << 30;
   switch (D) {
     case 1:
-      plain_group_kernel<T, 1><<<(unsigned)blocks, threads, 0, stream>>>(
-          d_g, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+      plain_group_kernel<T, 1><<<(unsigned)blocks, threads, 0, stream>>>(d_g, a, work, factors,
+                                                                          nvars, S[0], S[1], S[2]);
       break;
     case 2:
-      plain_group_kernel<T, 2><<<(unsigned)blocks, threads, 0, stream>>>(
-          d_g, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+      plain_group_kernel<T, 2><<<(unsigned)blocks, threads, 0, stream>>>(d_g, a, work, factors,
+                                                                          nvars, S[0], S[1], S[2]);
       break;
     default:
-      plain_group_kernel<T, 3><<<(unsigned)blocks, threads, 0, stream>>>(
-          d_g, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+      plain_group_kernel<T, 3><<<(unsigned)blocks, threads, 0, stream>>>(d_g, a, work, factors,
+                                                                          nvars, S[0], S[1], S[2]);
       break;
   }
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ntiles, const DevGroup *groups,
-                           const int32_t *tb, const int32_t *sb, const int32_t *srcstart,
-                           const T *weights, T *work, const T *factors, int nvars, const int S[3],
-                           int threads, cudaStream_t stream) {
+cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ntiles, const Args<T> &a, T *work,
+                           const T *factors, int nvars, const int S[3], int threads,
+                           cudaStream_t stream) {
   if (ntiles == 0) return cudaSuccess;
   const int wpb = threads / 32;
   int64_t blocks = (ntiles + wpb - 1) / wpb;
@@ -255,15 +480,15 @@ cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ntiles, const DevGr
   switch (D) {
     case 1:
       fused_stage_kernel<T, 1><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, groups, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
       break;
     case 2:
       fused_stage_kernel<T, 2><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, groups, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
       break;
     default:
       fused_stage_kernel<T, 3><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, groups, tb, sb, srcstart, weights, work, factors, nvars, S[0], S[1], S[2]);
+          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
       break;
   }
   return cudaGetLastError();
@@ -272,27 +497,76 @@ cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ntiles, const DevGr
 }  // namespace
 
 cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
-                               const int32_t *tb, const int32_t *sb, const int32_t *srcstart,
-                               const void *weights, void *work, const void *factors, int nvars,
+                               const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], cudaStream_t stream) {
   if (dtype == TAM_F64)
-    return plain_dispatch<double>(D, g, d_g, tb, sb, srcstart, (const double *)weights,
-                                  (double *)work, (const double *)factors, nvars, S, stream);
-  return plain_dispatch<float>(D, g, d_g, tb, sb, srcstart, (const float *)weights, (float *)work,
-                               (const float *)factors, nvars, S, stream);
+    return plain_dispatch<double>(D, g, d_g, typed<double>(a), (double *)work,
+                                  (const double *)factors, nvars, S, stream);
+  return plain_dispatch<float>(D, g, d_g, typed<float>(a), (float *)work, (const float *)factors,
+                               nvars, S, stream);
 }
 
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntiles,
-                               const DevGroup *groups, const int32_t *tb, const int32_t *sb,
-                               const int32_t *srcstart, const void *weights, void *work,
-                               const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream) {
+                               const SchedArgs &a, void *work, const void *factors, int nvars,
+                               const int S[3], int threads, cudaStream_t stream) {
   if (dtype == TAM_F64)
-    return fused_dispatch<double>(D, tiles, ntiles, groups, tb, sb, srcstart,
-                                  (const double *)weights, (double *)work, (const double *)factors,
-                                  nvars, S, threads, stream);
-  return fused_dispatch<float>(D, tiles, ntiles, groups, tb, sb, srcstart, (const float *)weights,
-                               (float *)work, (const float *)factors, nvars, S, threads, stream);
+    return fused_dispatch<double>(D, tiles, ntiles, typed<double>(a), (double *)work,
+                                  (const double *)factors, nvars, S, threads, stream);
+  return fused_dispatch<float>(D, tiles, ntiles, typed<float>(a), (float *)work,
+                               (const float *)factors, nvars, S, threads, stream);
+}
+
+}  // namespace tam
+
+// ---- self-test of the integer-pipe multiply ----------------------------------
+namespace tam {
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// Compares mul_short with __dmul_rn on n pseudo-random pairs: weights with
+// random 24-bit significands, signs and exponents in [-40, 40]; data drawn
+// from every bit pattern (specials, subnormals, extreme exponents) or, for
+// half the pairs, near the weights' scale.  Counts bitwise differences, every
+// NaN one pattern.
+__global__ void selftest_mul_kernel(int64_t n, uint64_t seed,
+                                    unsigned long long *__restrict__ mismatches) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r1 = splitmix(seed ^ (uint64_t)(2 * i));
+    const uint64_t r2 = splitmix(seed ^ (uint64_t)(2 * i + 1));
+    // weight: sign, exponent in [-40, 40], 24-bit significand
+    const uint64_t wexp = (uint64_t)(1023 - 40 + (int)(r1 % 81));
+    const uint64_t wsig = (r1 >> 8) & 0x7FFFFFull;  // 23 fraction bits
+    const uint64_t wbits = ((r1 >> 63) << 63) | (wexp << 52) | (wsig << 29);
+    uint64_t ubits = r2;
+    if (r1 & 0x100) {  // near the normal range's middle, and at its edges
+      const uint64_t e = (r1 & 0x200) ? (uint64_t)(1 + (int)((r1 >> 10) % 60))
+                                      : (uint64_t)(900 + (int)((r1 >> 10) % 250));
+      ubits = (r2 & 0x800FFFFFFFFFFFFFull) | (e << 52);
+    }
+    const double w = __longlong_as_double((long long)wbits);
+    const double u = __longlong_as_double((long long)ubits);
+    const ShortW sw = short_weight(w);
+    const double a = mul_short(sw.w, sw.wm, sw.we, sw.wsign, u);
+    const double b = __dmul_rn(w, u);
+    const bool same = (__double_as_longlong(a) == __double_as_longlong(b)) ||
+                      (a != a && b != b);
+    if (!same) atomicAdd(mismatches, 1ull);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                cudaStream_t stream) {
+  selftest_mul_kernel<<<1216, 256, 0, stream>>>(n, seed, mismatches);
+  return cudaGetLastError();
 }
 
 }  // namespace tam

@@ -207,8 +207,12 @@ def _declare(lib: C.CDLL):
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
     lib.tam_device_status.argtypes = [vp, vp, C.POINTER(i32)]
+    lib.tam_selftest.argtypes = [vp, i32, i64, C.c_uint64, C.POINTER(i64)]
+    lib.tam_schedule_set_option.argtypes = [vp, i32, i64]
+    lib.tam_schedule_get_option.argtypes = [vp, i32, C.POINTER(i64)]
     for name in ("tam_init", "tam_last_error", "tam_schedule_upload", "tam_schedule_info",
-                 "tam_device_status"):
+                 "tam_device_status", "tam_selftest", "tam_schedule_set_option",
+                 "tam_schedule_get_option"):
         getattr(lib, name).restype = C.c_int
 
 

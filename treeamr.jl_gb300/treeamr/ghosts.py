@@ -57,6 +57,22 @@ class DeviceSchedule:
                 C.c_void_p(fs.factors.data_ptr()), first, last, C.c_void_p(s.cuda_stream))
         _native.check(rc, self.ctx, f"tam_fill ({method})")
 
+    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3}
+
+    def set_option(self, name: str, value: int):
+        _native.check(self.lib.tam_schedule_set_option(self.handle, self.OPTIONS[name], int(value)),
+                      self.ctx, f"tam_schedule_set_option({name})")
+
+    def get_option(self, name: str) -> int:
+        v = C.c_int64()
+        _native.check(self.lib.tam_schedule_get_option(self.handle, self.OPTIONS[name],
+                                                       C.byref(v)), self.ctx,
+                      f"tam_schedule_get_option({name})")
+        return v.value
+
+    def options(self):
+        return {k: self.get_option(k) for k in self.OPTIONS}
+
     def status(self, fs: FieldSet) -> int:
         code = C.c_int32()
         s = torch.cuda.current_stream(fs.work.device)
