@@ -219,6 +219,15 @@ def main():
     ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(3, args.steps // 2))
     plain_value = world * bytes_per_fill / (ms_plain * 1e-3) / 1e9
 
+    # the adjoint fill (transpose, gather form) on the same mesh
+    from treeamr.adjoint import fill_ghosts_adjoint
+    yadj = fs.work.clone()
+    fill_ghosts_adjoint(fs, sched, yadj)                  # prepares the transpose, scratch
+    ms_adj = timed(lambda: fill_ghosts_adjoint(fs, sched, yadj), max(3, args.steps // 2))
+    adjoint = {"value": world * bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
+               "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms}
+    del yadj
+
     # per-stage launches of the fused kernel, CUDA events on the launching stream
     stage_ms = {}
     stage_bytes = {}
@@ -294,6 +303,7 @@ def main():
             "config": dict(cfg, method=method, parallelism=f"replicas{world}"),
             "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
                       "speedup_fused_vs_plain": ms_plain / ms},
+            "adjoint": adjoint,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_src,

@@ -144,6 +144,29 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
                    const void *factors, int32_t first_stage, int32_t last_stage,
                    void *stream);
 
+/* The adjoint (transpose) of the fill: y <- A^T y, stages in reverse, in
+ * gather form (deterministic, no atomics).  No reference counterpart: the
+ * reference has no adjoint; this is the kernel a ChainRulesCore rrule of
+ * fill_ghosts! (src/ghosts.jl:1783) would call for its pullback.  For each
+ * stage s, y <- (I - E_s) y + A_s^T E_s y with E_s the stage's targets: the
+ * ghosts' adjoints are pushed onto the points their values came from, and
+ * the ghosts' own adjoints are zeroed.  Same arguments as tam_fill; `y`
+ * has the layout of `work`.  The library allocates its scratch on the
+ * first call with a given nvars (so make that call before any stream
+ * capture). */
+int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                     const void *factors, int32_t first_stage, int32_t last_stage,
+                     void *stream);
+
+/* Scratch bytes tam_fill_adjoint_scratch needs for `nvars` variables. */
+int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes);
+
+/* tam_fill_adjoint with caller-owned device scratch of at least
+ * tam_adjoint_scratch_bytes; allocates nothing per call. */
+int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                             const void *factors, int32_t first_stage, int32_t last_stage,
+                             void *scratch, size_t scratch_bytes, void *stream);
+
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing
  * one changes speed only, never a result. */

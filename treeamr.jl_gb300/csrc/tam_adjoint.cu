@@ -1,0 +1,425 @@
+// The adjoint (transpose) of the ghost fill, in gather form.
+//
+// No reference counterpart: TreeAMR.jl has no adjoint (its only "adjoint" is
+// an element restriction, src/operators.jl:72-75).  The fill is linear, and
+// stage s of it (src/ghosts.jl:1099-1160) is
+//
+//   x <- (I - E_s) x + E_s A_s x,
+//
+// E_s the projection onto the stage's target points and A_s reading only
+// points that are not the stage's targets (ghosts are written from owned
+// points, or a coarser block's ghosts written by an earlier stage).  Its
+// transpose is
+//
+//   y <- (I - E_s) y + A_s^T E_s y,
+//
+// applied stage by stage in reverse.  A_s^T is formed in gather form, with
+// no atomics and a fixed order of summation, so the adjoint is deterministic:
+//
+//   pass 1  every transfer gathers, for each point of its source footprint,
+//           sum over its target points reading that point of
+//           w * (f * y[target]) into a scratch box of its own, through the
+//           per-dimension transposed stencils (CSR: source row -> (target
+//           row, tap)) and the forward fill's weight-product tables;
+//   pass 2  one CTA per source block adds the boxes of the transfers reading
+//           it, in transfer order, one transfer at a time;
+//   zero    the stage's target points are set to zero.
+//
+// The scratch is Sum over a stage's transfers of footprint x nvars elements
+// (tam_adjoint_scratch_bytes); the library owns one, or the caller passes
+// its own (tam_fill_adjoint_scratch).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "tam_internal.h"
+
+namespace tam {
+namespace {
+
+template <typename T>
+struct AArith;
+template <>
+struct AArith<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+};
+template <>
+struct AArith<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+};
+
+template <typename T>
+struct AdjArgs {
+  const DevGroup *__restrict__ groups;
+  const AdjGroup *__restrict__ ag;
+  const int32_t *__restrict__ tb;
+  const int32_t *__restrict__ sb;
+  const T *__restrict__ weights;
+  const int32_t *__restrict__ cls;
+  const T *__restrict__ wtab;
+  const int32_t *__restrict__ off;
+  const int32_t *__restrict__ ent;
+  const int64_t *__restrict__ scr;
+};
+
+// The weight of tap (m1, m2, m3) of target point (i1, i2, i3): exactly the
+// factor the forward fill multiplies that source value by.
+template <typename T, int D>
+__device__ __forceinline__ T tap_weight(const DevGroup &g, const AdjArgs<T> &a, int i1, int i2,
+                                        int i3, int m1, int m2, int m3) {
+  if (g.pclass == 0) return T(1);
+  if (g.pclass > 1) {
+    const int P = g.order[0];
+    const int P2 = D >= 2 ? P : 1, P3 = D >= 3 ? P : 1;
+    const int c1 = __ldg(a.cls + g.cls[0] + i1);
+    const int c2 = D >= 2 ? __ldg(a.cls + g.cls[1] + i2) : 0;
+    const int c3 = D >= 3 ? __ldg(a.cls + g.cls[2] + i3) : 0;
+    const int64_t base = g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * P * P2 * P3;
+    return __ldg(a.wtab + base + (m3 * P2 + m2) * P + m1);
+  }
+  using A = AArith<T>;
+  T w = __ldg(a.weights + g.w[0] + (int64_t)g.order[0] * i1 + m1);
+  if (D >= 2) w = A::mul(w, __ldg(a.weights + g.w[1] + (int64_t)g.order[1] * i2 + m2));
+  if (D >= 3) w = A::mul(w, __ldg(a.weights + g.w[2] + (int64_t)g.order[2] * i3 + m3));
+  return w;
+}
+
+// Pass 1: one warp per tile of one transfer's footprint points.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) adjoint_gather_kernel(
+    const Tile *__restrict__ tiles, int64_t ntiles, AdjArgs<T> a, const T *y, T *scratch,
+    const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
+  using A = AArith<T>;
+  const int lane = threadIdx.x & 31;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
+       w += warps) {
+    const Tile tile = tiles[w];
+    const DevGroup &g = a.groups[tile.group];
+    const AdjGroup &h = a.ag[tile.group];
+    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
+    T *out = scratch + __ldg(a.scr + tile.transfer) * nvars;
+    const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
+    for (int k = lane; k < tile.nitems; k += 32) {
+      const int p = tile.item0 + k;
+      const int j3 = p / f01;
+      const int r = p - j3 * f01;
+      const int j2 = r / f0;
+      const int j1 = r - j2 * f0;
+      const int e1a = __ldg(a.off + h.off[0] + j1), e1b = __ldg(a.off + h.off[0] + j1 + 1);
+      const int e2a = D >= 2 ? __ldg(a.off + h.off[1] + j2) : 0;
+      const int e2b = D >= 2 ? __ldg(a.off + h.off[1] + j2 + 1) : 1;
+      const int e3a = D >= 3 ? __ldg(a.off + h.off[2] + j3) : 0;
+      const int e3b = D >= 3 ? __ldg(a.off + h.off[2] + j3 + 1) : 1;
+      for (int v = 0; v < nvars; ++v) {
+        const T *yv = y + tblock * bs + v * vs;
+        T acc = T(0);
+        for (int e3 = e3a; e3 < e3b; ++e3) {
+          const int q3 = D >= 3 ? __ldg(a.ent + e3) : 0;
+          const int i3 = q3 >> 8, m3 = q3 & 0xFF;
+          for (int e2 = e2a; e2 < e2b; ++e2) {
+            const int q2 = D >= 2 ? __ldg(a.ent + e2) : 0;
+            const int i2 = q2 >> 8, m2 = q2 & 0xFF;
+            for (int e1 = e1a; e1 < e1b; ++e1) {
+              const int q1 = __ldg(a.ent + e1);
+              const int i1 = q1 >> 8, m1 = q1 & 0xFF;
+              const T wt = tap_weight<T, D>(g, a, i1, i2, i3, m1, m2, m3);
+              const T yt = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 +
+                              (int64_t)(g.tf[2] + i3) * s3];
+              acc = A::add(acc, A::mul(wt, yt));
+            }
+          }
+        }
+        // a factor of -1, 0 or 1 commutes with the rounded sum
+        if (g.factorcol) acc = A::mul(acc, __ldg(factors + v + (int64_t)nvars * (g.factorcol - 1)));
+        out[(int64_t)v * h.fsize + p] = acc;
+      }
+    }
+  }
+}
+
+// Pass 2: one CTA per source block, its transfers' boxes added in order.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) adjoint_reduce_kernel(
+    const AdjReduce *__restrict__ red, int64_t nred, const int2 *__restrict__ list,
+    AdjArgs<T> a, T *y, const T *scratch, int nvars, int S1, int S2, int S3) {
+  using A = AArith<T>;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
+  for (int64_t b = blockIdx.x; b < nred; b += gridDim.x) {
+    const AdjReduce r = red[b];
+    T *yb = y + (int64_t)r.sblock * bs;
+    for (int q = 0; q < r.count; ++q) {
+      const int2 tg = list[r.first + q];  // (transfer, group)
+      const AdjGroup &h = a.ag[tg.y];
+      const T *src = scratch + __ldg(a.scr + tg.x) * nvars;
+      const int64_t n = h.fsize * nvars;
+      const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
+      for (int64_t p = threadIdx.x; p < n; p += blockDim.x) {
+        const int v = (int)(p / h.fsize);
+        const int pt = (int)(p - (int64_t)v * h.fsize);
+        const int j3 = pt / f01;
+        const int rr = pt - j3 * f01;
+        const int j2 = rr / f0;
+        const int j1 = rr - j2 * f0;
+        T *dst = yb + v * vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * s2 +
+                 (int64_t)(h.flo[2] + j3) * s3;
+        *dst = A::add(*dst, src[p]);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Zero the targets of a stage: the forward tiles of the stage.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restrict__ tiles,
+                                                           int64_t ntiles,
+                                                           const DevGroup *__restrict__ groups,
+                                                           const int32_t *__restrict__ tb, T *y,
+                                                           int nvars, int S1, int S2, int S3) {
+  const int lane = threadIdx.x & 31;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
+       w += warps) {
+    const Tile tile = tiles[w];
+    const DevGroup &g = groups[tile.group];
+    const int64_t tblock = __ldg(tb + tile.transfer) - 1;
+    const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
+    for (int k = lane; k < tile.nitems; k += 32) {
+      const int item = tile.item0 + k;
+      const int i3 = item / n12;
+      const int rem = item - i3 * n12;
+      const int i2 = rem / n1;
+      const int i1 = rem - i2 * n1;
+      const int64_t o = tblock * bs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 +
+                        (int64_t)(g.tf[2] + i3) * s3;
+      for (int v = 0; v < nvars; ++v) y[o + v * vs] = T(0);
+    }
+  }
+}
+
+template <typename T>
+AdjArgs<T> adj_args(const tam_sched *s) {
+  return AdjArgs<T>{s->d_groups,       s->d_adj_groups, s->d_tb,        s->d_sb,
+                    (const T *)s->d_weights, s->d_cls,  (const T *)s->d_wtab, s->d_adj_off,
+                    s->d_adj_ent,      s->d_adj_scr};
+}
+
+template <typename T, int D>
+cudaError_t run_typed(tam_sched *s, T *y, int nvars, const T *factors, int32_t first,
+                      int32_t last, T *scratch, cudaStream_t stream) {
+  const AdjArgs<T> a = adj_args<T>(s);
+  const int threads = 256, wpb = threads / 32;
+  // stages in reverse order
+  for (int k = (int)s->adj_stages.size() - 1; k >= 0; --k) {
+    const AdjStage &st = s->adj_stages[k];
+    if (st.tag < first || st.tag > last) continue;
+    const Stage &fw = s->stages[k];
+    if (st.ntiles > 0) {
+      const int64_t blocks = std::min<int64_t>((st.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
+      adjoint_gather_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
+          s->d_adj_tiles + st.tile0, st.ntiles, a, y, scratch, factors, nvars, s->S[0], s->S[1],
+          s->S[2]);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (st.nred > 0) {
+      const int64_t blocks = std::min<int64_t>(st.nred, (int64_t)1 << 30);
+      adjoint_reduce_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
+          s->d_adj_red + st.red0, st.nred, (const int2 *)s->d_adj_list, a, y, scratch, nvars,
+          s->S[0], s->S[1], s->S[2]);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (fw.ntiles > 0) {
+      const int64_t blocks = std::min<int64_t>((fw.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
+      adjoint_zero_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
+          s->d_tiles + fw.tile0, fw.ntiles, s->d_groups, s->d_tb, y, nvars, s->S[0], s->S[1],
+          s->S[2]);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t up(T **dst, const std::vector<T> &v) {
+  *dst = nullptr;
+  size_t n = std::max<size_t>(v.size(), 1);
+  cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (!v.empty()) return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+// Build the transposed stencils, the pass-1 tiles and the pass-2 lists.
+int adjoint_prepare(tam_sched *s, std::string &err) {
+  if (s->adj_ready) return TAM_OK;
+  const int D = s->D;
+  std::vector<AdjGroup> ag(s->groups.size());
+  std::vector<int32_t> off, ent;
+  for (size_t gi = 0; gi < s->groups.size(); ++gi) {
+    const tam_group &h = s->host_groups[gi];
+    AdjGroup &a = ag[gi];
+    a.fsize = 1;
+    for (int d = 0; d < 3; ++d) {
+      if (d >= D) {
+        a.flo[d] = 0;
+        a.fn[d] = 1;
+        a.off[d] = (int64_t)off.size();
+        off.push_back((int32_t)ent.size());
+        ent.push_back(0);  // (i = 0, m = 0)
+        off.push_back((int32_t)ent.size());
+        continue;
+      }
+      const tam_stencil &st = h.stencil[d];
+      int lo = INT32_MAX, hi = INT32_MIN;
+      for (int i = 0; i < st.ntarget; ++i) {
+        const int b = s->h_srcstart[st.srcstart + i] - 1;
+        lo = std::min(lo, b);
+        hi = std::max(hi, b + st.order - 1);
+      }
+      if (st.ntarget >= (1 << 23) || st.order > 255) {
+        err = "a stencil too large for the adjoint's packed entries";
+        return TAM_EUNSUPPORTED;
+      }
+      a.flo[d] = lo;
+      a.fn[d] = hi - lo + 1;
+      a.off[d] = (int64_t)off.size();
+      for (int r = lo; r <= hi; ++r) {
+        off.push_back((int32_t)ent.size());
+        for (int i = 0; i < st.ntarget; ++i) {
+          const int b = s->h_srcstart[st.srcstart + i] - 1;
+          const int m = r - b;
+          if (m >= 0 && m < st.order) ent.push_back((i << 8) | m);
+        }
+      }
+      off.push_back((int32_t)ent.size());
+      a.fsize *= a.fn[d];
+    }
+    if (ent.size() > (size_t)INT32_MAX) {
+      err = "the adjoint's transposed stencils exceed 2^31 entries";
+      return TAM_EUNSUPPORTED;
+    }
+  }
+  // per stage: scratch offsets, tiles by target block, reduction lists by
+  // source block
+  std::vector<int64_t> scr(s->ntransfers, 0);
+  std::vector<Tile> tiles;
+  std::vector<AdjReduce> red;
+  std::vector<int2> list;
+  std::vector<AdjStage> stages;
+  int64_t maxpts = 0;
+  const int ti = s->shape.tile_items;
+  for (const Stage &fw : s->stages) {
+    AdjStage st;
+    st.tag = fw.tag;
+    st.tile0 = (int64_t)tiles.size();
+    st.red0 = (int64_t)red.size();
+    struct E {
+      int32_t tblock, sblock, group, transfer;
+    };
+    std::vector<E> es;
+    for (int32_t gi : fw.groups) {
+      const DevGroup &g = s->groups[gi];
+      for (int64_t t = 0; t < g.ntransfers; ++t)
+        es.push_back({s->h_tb[g.first + t], s->h_sb[g.first + t], gi, (int32_t)(g.first + t)});
+    }
+    // scratch in transfer order
+    std::vector<E> byt = es;
+    std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) { return x.transfer < y.transfer; });
+    int64_t pts = 0;
+    for (const E &e : byt) {
+      scr[e.transfer] = pts;
+      pts += ag[e.group].fsize;
+    }
+    st.scratch_points = pts;
+    maxpts = std::max(maxpts, pts);
+    // pass-1 tiles by target block
+    std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
+      return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
+    });
+    for (const E &e : es) {
+      const int64_t n = ag[e.group].fsize;
+      for (int64_t i0 = 0; i0 < n; i0 += ti)
+        tiles.push_back({e.group, e.transfer, (int32_t)i0, (int32_t)std::min<int64_t>(ti, n - i0)});
+    }
+    st.ntiles = (int64_t)tiles.size() - st.tile0;
+    // pass-2 lists by source block, transfers in transfer order
+    std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) {
+      return x.sblock != y.sblock ? x.sblock < y.sblock : x.transfer < y.transfer;
+    });
+    for (size_t i = 0; i < byt.size();) {
+      size_t j = i;
+      while (j < byt.size() && byt[j].sblock == byt[i].sblock) ++j;
+      red.push_back({byt[i].sblock - 1, (int32_t)(j - i), (int64_t)list.size()});
+      for (size_t k = i; k < j; ++k) list.push_back(make_int2(byt[k].transfer, byt[k].group));
+      i = j;
+    }
+    st.nred = (int64_t)red.size() - st.red0;
+    stages.push_back(st);
+  }
+  cudaError_t e;
+  if ((e = up(&s->d_adj_groups, ag)) != cudaSuccess || (e = up(&s->d_adj_off, off)) != cudaSuccess ||
+      (e = up(&s->d_adj_ent, ent)) != cudaSuccess || (e = up(&s->d_adj_scr, scr)) != cudaSuccess ||
+      (e = up(&s->d_adj_tiles, tiles)) != cudaSuccess || (e = up(&s->d_adj_red, red)) != cudaSuccess ||
+      (e = up((int2 **)&s->d_adj_list, list)) != cudaSuccess) {
+    adjoint_free(s);
+    err = std::string("adjoint upload: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA;
+  }
+  s->adj_groups = std::move(ag);
+  s->adj_stages = std::move(stages);
+  s->adj_scratch_points = maxpts;
+  s->adj_ready = true;
+  return TAM_OK;
+}
+
+void adjoint_free(tam_sched *s) {
+  cudaFree(s->d_adj_groups);
+  cudaFree(s->d_adj_off);
+  cudaFree(s->d_adj_ent);
+  cudaFree(s->d_adj_scr);
+  cudaFree(s->d_adj_tiles);
+  cudaFree(s->d_adj_red);
+  cudaFree(s->d_adj_list);
+  cudaFree(s->adj_scratch);
+  s->d_adj_groups = nullptr;
+  s->d_adj_off = s->d_adj_ent = nullptr;
+  s->d_adj_scr = nullptr;
+  s->d_adj_tiles = nullptr;
+  s->d_adj_red = nullptr;
+  s->d_adj_list = nullptr;
+  s->adj_scratch = nullptr;
+  s->adj_scratch_bytes = 0;
+  s->adj_ready = false;
+}
+
+cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
+                        int32_t last, void *scratch, cudaStream_t stream) {
+  if (s->dtype == TAM_F64) {
+    switch (s->D) {
+      case 1: return run_typed<double, 1>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
+      case 2: return run_typed<double, 2>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
+      default: return run_typed<double, 3>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
+    }
+  }
+  switch (s->D) {
+    case 1: return run_typed<float, 1>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
+    case 2: return run_typed<float, 2>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
+    default: return run_typed<float, 3>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
+  }
+}
+
+}  // namespace tam

@@ -398,6 +398,8 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
     s->stages.push_back(st);
   }
   s->h_tb.assign(d->targetblocks, d->targetblocks + d->ntransfers);
+  s->h_sb.assign(d->sourceblocks, d->sourceblocks + d->ntransfers);
+  s->h_srcstart.assign(d->srcstart, d->srcstart + d->nsrcstart);
   std::vector<tam::Tile> tiles = build_tiles(s);
 
   cudaError_t e;
@@ -423,8 +425,72 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
 void tam_schedule_free(tam_sched *s) {
   if (!s) return;
   DeviceGuard guard(s->ctx->device);
+  tam::adjoint_free(s);
   free_sched_device(s);
   delete s;
+}
+
+static int adjoint_ready(tam_sched *s) {
+  if (s->adj_ready) return TAM_OK;
+  std::string err;
+  int rc = tam::adjoint_prepare(s, err);
+  if (rc != TAM_OK) return fail(s->ctx, rc, err);
+  return TAM_OK;
+}
+
+int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes) {
+  if (!s || !bytes || nvars < 1) return fail(s ? s->ctx : nullptr, TAM_EINVAL,
+                                             "tam_adjoint_scratch_bytes: bad argument");
+  DeviceGuard guard(s->ctx->device);
+  int rc = adjoint_ready(s);
+  if (rc != TAM_OK) return rc;
+  *bytes = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  return TAM_OK;
+}
+
+static int check_fill_args(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
+                           const void *factors);
+
+int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                             const void *factors, int32_t first_stage, int32_t last_stage,
+                             void *scratch, size_t scratch_bytes, void *stream) {
+  int rc = check_fill_args(s, y, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  rc = adjoint_ready(s);
+  if (rc != TAM_OK) return rc;
+  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  if (need > 0 && (!scratch || scratch_bytes < need))
+    return fail(s->ctx, TAM_EINVAL, "adjoint scratch smaller than tam_adjoint_scratch_bytes");
+  cudaError_t e =
+      tam::adjoint_run(s, y, nvars, factors, first_stage, last_stage, scratch, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "adjoint launch");
+  return TAM_OK;
+}
+
+int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, const void *factors,
+                     int32_t first_stage, int32_t last_stage, void *stream) {
+  int rc = check_fill_args(s, y, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  rc = adjoint_ready(s);
+  if (rc != TAM_OK) return rc;
+  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  if (need > s->adj_scratch_bytes) {
+    // grown only between fills: wait for any fill still using the old one
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "adjoint scratch");
+    cudaFree(s->adj_scratch);
+    s->adj_scratch = nullptr;
+    s->adj_scratch_bytes = 0;
+    e = cudaMalloc(&s->adj_scratch, need);
+    if (e != cudaSuccess) return fail(s->ctx, TAM_ENOMEM, "adjoint scratch allocation failed");
+    s->adj_scratch_bytes = need;
+  }
+  return tam_fill_adjoint_scratch(s, y, nvars, nblocks, factors, first_stage, last_stage,
+                                  s->adj_scratch, s->adj_scratch_bytes, stream);
 }
 
 int tam_schedule_info(const tam_sched *s, int64_t *ngroups, int64_t *ntransfers, int64_t *points,

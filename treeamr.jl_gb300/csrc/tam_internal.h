@@ -56,6 +56,35 @@ struct Stage {
   int64_t ntiles = 0;
 };
 
+// The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
+// dimension the footprint, the source rows the group's windows cover
+// (flo .. flo + fn - 1, 0-based stored indices), and for each footprint row
+// the (target row, tap) pairs that read it, in CSR form: entries
+// [off[r], off[r+1]) of the entry pool, each packed (i << 8) | m.
+struct AdjGroup {
+  int32_t flo[3];
+  int32_t fn[3];
+  int64_t off[3];    // offset into the row-offset pool (fn + 1 entries)
+  int64_t fsize;     // footprint points: fn[0] * fn[1] * fn[2]
+};
+
+// One stage of the adjoint: pass-1 tiles over the footprints of its
+// transfers, and the source blocks pass 2 reduces into.
+struct AdjStage {
+  int32_t tag;
+  int64_t tile0 = 0, ntiles = 0;  // into the adjoint tile array
+  int64_t red0 = 0, nred = 0;     // into the reduction block list
+  int64_t scratch_points = 0;     // footprint points of the stage (per variable)
+};
+
+// Pass 2's work for one source block: the transfers reading it,
+// list[first .. first + count), in transfer order.
+struct AdjReduce {
+  int32_t sblock;  // 0-based
+  int32_t count;
+  int64_t first;
+};
+
 struct LaunchShape {
   int tile_items = 128;     // box points per tile
   int threads = 256;        // threads per CTA of the fused kernel
@@ -80,6 +109,8 @@ struct tam_sched {
   bool needs_factors = false;
   std::vector<tam_group> host_groups;
   std::vector<int32_t> h_tb;  // target blocks, for re-tiling
+  std::vector<int32_t> h_sb;  // source blocks, for the adjoint's lists
+  std::vector<int32_t> h_srcstart;
   std::vector<tam::DevGroup> groups;
   std::vector<tam::Stage> stages;
   int64_t ntransfers = 0;
@@ -95,6 +126,20 @@ struct tam_sched {
   void *d_wtab = nullptr;
   tam::Tile *d_tiles = nullptr;
   int32_t *d_err = nullptr;
+  // the adjoint, prepared on first use (tam_adjoint.cu)
+  bool adj_ready = false;
+  std::vector<tam::AdjGroup> adj_groups;
+  std::vector<tam::AdjStage> adj_stages;
+  int64_t adj_scratch_points = 0;       // max over stages, per variable
+  tam::AdjGroup *d_adj_groups = nullptr;
+  int32_t *d_adj_off = nullptr;         // CSR row offsets
+  int32_t *d_adj_ent = nullptr;         // CSR entries
+  int64_t *d_adj_scr = nullptr;         // per transfer: scratch offset in points
+  tam::Tile *d_adj_tiles = nullptr;
+  tam::AdjReduce *d_adj_red = nullptr;
+  int32_t *d_adj_list = nullptr;        // transfers of each reduction block
+  void *adj_scratch = nullptr;          // owned scratch, grown on demand
+  size_t adj_scratch_bytes = 0;
 };
 
 namespace tam {
@@ -122,5 +167,11 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntil
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);
+
+// The adjoint (tam_adjoint.cu).
+int adjoint_prepare(tam_sched *s, std::string &err);
+void adjoint_free(tam_sched *s);
+cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
+                        int32_t last, void *scratch, cudaStream_t stream);
 
 }  // namespace tam

@@ -30,7 +30,7 @@ TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["tam_kernels.cu", "tam_api.cpp"]
+SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu"]
 
 
 class tam_stencil(C.Structure):
@@ -208,6 +208,10 @@ def _declare(lib: C.CDLL):
         f.restype = C.c_int
     lib.tam_device_status.argtypes = [vp, vp, C.POINTER(i32)]
     lib.tam_selftest.argtypes = [vp, i32, i64, C.c_uint64, C.POINTER(i64)]
+    lib.tam_adjoint_scratch_bytes.argtypes = [vp, i32, C.POINTER(C.c_size_t)]
+    lib.tam_adjoint_scratch_bytes.restype = C.c_int
+    lib.tam_fill_adjoint_scratch.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp, C.c_size_t, vp]
+    lib.tam_fill_adjoint_scratch.restype = C.c_int
     lib.tam_schedule_set_option.argtypes = [vp, i32, i64]
     lib.tam_schedule_get_option.argtypes = [vp, i32, C.POINTER(i64)]
     for name in ("tam_init", "tam_last_error", "tam_schedule_upload", "tam_schedule_info",

@@ -57,6 +57,29 @@ class DeviceSchedule:
                 C.c_void_p(fs.factors.data_ptr()), first, last, C.c_void_p(s.cuda_stream))
         _native.check(rc, self.ctx, f"tam_fill ({method})")
 
+    def run_adjoint(self, y: torch.Tensor, nvars: int, factors: torch.Tensor, first: int,
+                    last: int, stream: Optional[torch.cuda.Stream] = None,
+                    scratch: Optional[torch.Tensor] = None):
+        """``y <- A^T y`` in place (``tam_fill_adjoint``), or with the caller's
+        scratch tensor (``tam_fill_adjoint_scratch``)."""
+        s = stream if stream is not None else torch.cuda.current_stream(y.device)
+        if scratch is None:
+            rc = self.lib.tam_fill_adjoint(self.handle, C.c_void_p(y.data_ptr()), nvars,
+                                           y.shape[0], C.c_void_p(factors.data_ptr()), first,
+                                           last, C.c_void_p(s.cuda_stream))
+        else:
+            rc = self.lib.tam_fill_adjoint_scratch(
+                self.handle, C.c_void_p(y.data_ptr()), nvars, y.shape[0],
+                C.c_void_p(factors.data_ptr()), first, last, C.c_void_p(scratch.data_ptr()),
+                scratch.numel() * scratch.element_size(), C.c_void_p(s.cuda_stream))
+        _native.check(rc, self.ctx, "tam_fill_adjoint")
+
+    def adjoint_scratch_bytes(self, nvars: int) -> int:
+        b = C.c_size_t()
+        _native.check(self.lib.tam_adjoint_scratch_bytes(self.handle, nvars, C.byref(b)),
+                      self.ctx, "tam_adjoint_scratch_bytes")
+        return b.value
+
     OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3}
 
     def set_option(self, name: str, value: int):
