@@ -1,0 +1,212 @@
+# TreeAMRCUDA.jl -- the ccall side of libtreeamr_cuda.so for TreeAMR.jl.
+#
+# A package extension a TreeAMR.jl maintainer adds (it loads with CUDA.jl):
+# it flattens each GhostSchedule once into the struct-of-arrays descriptor
+# of include/treeamr_cuda.h, uploads it, and routes fill_ghosts! of a
+# CuArray field set through tam_fill, with the boundary hook between phase 1
+# and the prolongations exactly where exchange_ghosts! runs it
+# (src/ghosts.jl:1099-1160).  The adjoint is exposed as a ChainRulesCore
+# rrule.  Written against the reference's own types (src/schedule.jl:64-197,
+# 820-864; src/storage.jl:364-472); not executed in this repository, which
+# has no Julia toolchain.
+module TreeAMRCUDA
+
+using TreeAMR
+using TreeAMR: GhostSchedule, TransferGroup, Stencil1D, FieldSet, CellBoundary
+using CUDA
+import ChainRulesCore
+
+const LIB = get(ENV, "TREEAMR_CUDA_LIB", joinpath(@__DIR__, "..", "csrc", "_build",
+                                                  "libtreeamr_cuda.so"))
+
+const TAM_ABI_VERSION = Int32(1)
+const TAM_F32, TAM_F64 = Int32(1), Int32(2)
+const TAM_COPY, TAM_RESTRICT, TAM_PROLONG = Int32(1), Int32(2), Int32(3)
+const STAGE_FIRST, STAGE_LAST = Int32(-1), typemax(Int32)
+
+# include/treeamr_cuda.h: tam_stencil, tam_group, tam_schedule_desc
+struct TamStencil
+    targetfirst::Int32
+    ntarget::Int32
+    order::Int32
+    unit::Int32
+    srcstart::Int64
+    weights::Int64
+end
+
+struct TamGroup
+    kind::Int32
+    stage::Int32
+    factorcol::Int32
+    bounded::Int32
+    first::Int64
+    ntransfers::Int64
+    stencil::NTuple{3,TamStencil}
+end
+
+struct TamScheduleDesc
+    abi_version::Int32
+    ndim::Int32
+    dtype::Int32
+    stored::NTuple{3,Int32}
+    nblocks::Int64
+    ngroups::Int32
+    nfactorcols::Int32
+    groups::Ptr{TamGroup}
+    ntransfers::Int64
+    targetblocks::Ptr{Int32}
+    sourceblocks::Ptr{Int32}
+    nsrcstart::Int64
+    srcstart::Ptr{Int32}
+    nweights::Int64
+    weights::Ptr{Cvoid}
+end
+
+function check(rc, ctx, what)
+    rc == 0 && return nothing
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:tam_last_error, LIB), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), ctx, buf, length(buf))
+    msg = unsafe_string(pointer(buf))
+    rc == -1 ? throw(ArgumentError("$what: $msg")) : error("$what failed ($rc): $msg")
+end
+
+const CONTEXTS = Dict{Int,Ptr{Cvoid}}()
+function context(dev::Int)
+    get!(CONTEXTS, dev) do
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:tam_init, LIB), Cint, (Cint, Ref{Ptr{Cvoid}}), dev, out), C_NULL,
+              "tam_init")
+        out[]
+    end
+end
+
+kindcode(k::Symbol) = k === :copy ? TAM_COPY : k === :restrict ? TAM_RESTRICT : TAM_PROLONG
+
+# The stage of a group: the stage tag its key had (src/schedule.jl:656-658),
+# recovered from where the schedule filed it.
+function stage_groups(s::GhostSchedule)
+    out = Tuple{Int32,Any}[]
+    foreach(g -> push!(out, (Int32(-1), g)), s.selfimage)
+    foreach(g -> push!(out, (Int32(0), g)), s.unify)
+    foreach(g -> push!(out, (Int32(1), g)), s.phase1)
+    for (l, gs) in zip(s.levels, s.phase2)
+        foreach(g -> push!(out, (Int32(2 + l), g)), gs)
+    end
+    return out
+end
+
+# Flatten a host-built schedule (the stencils on the CPU backend) into the
+# descriptor's pools, upload it, and keep the handle.
+mutable struct DeviceSchedule
+    handle::Ptr{Cvoid}
+    ctx::Ptr{Cvoid}
+    generation::Int
+end
+
+function upload(s::GhostSchedule{T,D}, dev::Int=CUDA.device().handle) where {T,D}
+    groups = TamGroup[]
+    tb, sb, ss = Int32[], Int32[], Int32[]
+    ws = T[]
+    memo = IdDict{Any,Tuple{Int64,Int64}}()
+    for (stage, g) in stage_groups(s)
+        sts = ntuple(3) do d
+            d > D && return TamStencil(1, 1, 1, 1, 0, 0)
+            st = g.stencils[d]
+            off = get!(memo, st) do
+                o = (Int64(length(ss)), Int64(length(ws)))
+                append!(ss, Array(st.srcstart))
+                append!(ws, vec(Array(st.weights)))
+                o
+            end
+            TamStencil(st.targetfirst, length(st.srcstart), size(st.weights, 1), st.unit,
+                       off[1], off[2])
+        end
+        push!(groups, TamGroup(kindcode(g.kind), stage, g.factorcol, g.bounded,
+                               length(tb), length(g.targetblocks), sts))
+        append!(tb, Array(g.targetblocks))
+        append!(sb, Array(g.sourceblocks))
+    end
+    c = map(x -> x === :vertex ? 1 : 0, s.centering)
+    stored = ntuple(d -> d <= D ? Int32(s.forest.N + 2s.G[d] + c[d]) : Int32(1), 3)
+    ctx = context(dev)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve groups tb sb ss ws begin
+        desc = TamScheduleDesc(TAM_ABI_VERSION, D, T === Float64 ? TAM_F64 : TAM_F32, stored,
+                               nleaves(s.forest), length(groups), 3^D, pointer(groups),
+                               length(tb), pointer(tb), pointer(sb), length(ss), pointer(ss),
+                               length(ws), pointer(ws))
+        check(ccall((:tam_schedule_upload, LIB), Cint,
+                    (Ptr{Cvoid}, Ref{TamScheduleDesc}, Ref{Ptr{Cvoid}}), ctx, desc, out),
+              ctx, "tam_schedule_upload")
+    end
+    ds = DeviceSchedule(out[], ctx, s.generation)
+    finalizer(d -> ccall((:tam_schedule_free, LIB), Cvoid, (Ptr{Cvoid},), d.handle), ds)
+    return ds
+end
+
+const UPLOADS = WeakKeyDict{GhostSchedule,DeviceSchedule}()
+device_schedule(s::GhostSchedule) = get!(() -> upload(s), UPLOADS, s)
+
+function tam_fill!(fs::FieldSet, ds::DeviceSchedule, first::Int32, last::Int32;
+                   plain::Bool=false)
+    f = plain ? :tam_fill_plain : :tam_fill
+    stream = CUDA.stream().handle
+    factors = fs.factors === nothing ? CU_NULL : pointer(fs.factors)
+    rc = ccall((f, LIB), Cint,
+               (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Int32, Ptr{Cvoid}),
+               ds.handle, pointer(fs.work), fs.nvars, size(fs.work, ndims(fs.work)), factors,
+               first, last, stream)
+    check(rc, ds.ctx, String(f))
+end
+
+# The drop-in: fill_ghosts! of a CuArray field set (src/ghosts.jl:1783),
+# after the reference's own checks.
+function TreeAMR.exchange_ghosts!(fs::FieldSet{T,D,R,<:CuArray}, schedule::GhostSchedule,
+                                  boundary, backend) where {T,D,R}
+    ds = device_schedule(schedule)
+    if boundary === nothing
+        tam_fill!(fs, ds, STAGE_FIRST, STAGE_LAST)
+    else
+        tam_fill!(fs, ds, STAGE_FIRST, Int32(1))
+        TreeAMR.apply_boundary!(fs, boundary, schedule, backend)
+        tam_fill!(fs, ds, Int32(2), STAGE_LAST)
+    end
+    return fs
+end
+
+# y <- A^T y (tam_fill_adjoint): the pullback of the fill.
+function fill_ghosts_adjoint!(y::CuArray, fs::FieldSet, schedule::GhostSchedule)
+    ds = device_schedule(schedule)
+    factors = fs.factors === nothing ? CU_NULL : pointer(fs.factors)
+    rc = ccall((:tam_fill_adjoint, LIB), Cint,
+               (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Int32, Ptr{Cvoid}),
+               ds.handle, pointer(y), fs.nvars, size(y, ndims(y)), factors, STAGE_FIRST,
+               STAGE_LAST, CUDA.stream().handle)
+    check(rc, ds.ctx, "tam_fill_adjoint")
+    return y
+end
+
+# A functional form for differentiation: the filled copy of `x`.
+function ghost_filled(x::CuArray, fs::FieldSet, schedule::GhostSchedule)
+    y = copy(x)
+    saved = fs.work
+    try
+        fs.work .= y
+        fill_ghosts!(fs, schedule)
+        copyto!(y, fs.work)
+    finally
+        copyto!(fs.work, saved)
+    end
+    return y
+end
+
+function ChainRulesCore.rrule(::typeof(ghost_filled), x::CuArray, fs::FieldSet,
+                              schedule::GhostSchedule)
+    y = ghost_filled(x, fs, schedule)
+    pullback(ȳ) = (ChainRulesCore.NoTangent(),
+                   fill_ghosts_adjoint!(copy(ChainRulesCore.unthunk(ȳ)), fs, schedule),
+                   ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    return y, pullback
+end
+
+end # module
