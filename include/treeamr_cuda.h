@@ -167,6 +167,28 @@ int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nbloc
                              const void *factors, int32_t first_stage, int32_t last_stage,
                              void *scratch, size_t scratch_bytes, void *stream);
 
+/* tam_fill_adjoint for callers that must not allocate device memory while
+ * they run -- a solver inside someone else's memory pool or arena, a code
+ * path that must never trigger the synchronisation cudaMalloc/cudaFree
+ * imply, or an allocator-free real-time loop.  It has no counterpart in the
+ * reference.  Its scratch is a fixed array compiled into the library,
+ * TAM_STATIC_SCRATCH_BYTES (64 MiB) on every GPU that loads the library,
+ * held until the process exits; a schedule whose adjoint needs more for
+ * `nvars` variables (tam_adjoint_scratch_bytes) is refused with
+ * TAM_EUNSUPPORTED.  Set-up that does allocate must come first: the
+ * schedule's transposed stencils are built by tam_adjoint_scratch_bytes (or
+ * a first tam_fill_adjoint), and a schedule without them is refused with
+ * TAM_EINVAL.  The first call on each device looks up the array's device
+ * address once (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array and leave their results in
+ * it, so calls that overlap on the GPU (two streams, two threads) race and
+ * must be serialised by the caller.  Nothing in the array needs to start
+ * at zero: each call writes every scratch element before reading it. */
+#define TAM_STATIC_SCRATCH_BYTES ((size_t)64 << 20)
+int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                            const void *factors, int32_t first_stage, int32_t last_stage,
+                            void *stream);
+
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing
  * one changes speed only, never a result. */

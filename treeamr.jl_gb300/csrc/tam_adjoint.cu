@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -405,6 +406,97 @@ void adjoint_free(tam_sched *s) {
   s->adj_scratch_bytes = 0;
   s->adj_ready = false;
 }
+
+}  // namespace tam
+
+// ---- the adjoint without allocation -----------------------------------------
+//
+// Scratch for tam_fill_adjoint_static: one fixed array per GPU that loads the
+// library, held until the process exits.  In host code the name is only a
+// host-side handle, never a device address, so each device's address is
+// looked up once with that device current and kept below.
+static __device__ __align__(256) unsigned char g_adjoint_static_scratch[TAM_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+void *g_static_ptr[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                                       const void *factors, int32_t first_stage,
+                                       int32_t last_stage, void *stream) {
+  if (!s) return TAM_EINVAL;
+  tam_ctx *ctx = s->ctx;
+  if (!y || nvars < 1) {
+    ctx->err = "tam_fill_adjoint_static: NULL vector or no variables";
+    return TAM_EINVAL;
+  }
+  if (nblocks != s->nblocks) {
+    ctx->err = "tam_fill_adjoint_static: the block count differs from the schedule's";
+    return TAM_ELAYOUT;
+  }
+  if (s->needs_factors && !factors) {
+    ctx->err = "tam_fill_adjoint_static: this schedule mirrors ghosts and needs the factor table";
+    return TAM_EINVAL;
+  }
+  if (!s->adj_ready) {
+    ctx->err = "tam_fill_adjoint_static: the schedule's transposed stencils are not built; "
+               "call tam_adjoint_scratch_bytes once first (it allocates)";
+    return TAM_EINVAL;
+  }
+  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  if (need > TAM_STATIC_SCRATCH_BYTES) {
+    ctx->err = "tam_fill_adjoint_static: this schedule's adjoint needs " + std::to_string(need) +
+               " bytes of scratch for " + std::to_string(nvars) +
+               " variables, more than the built-in " +
+               std::to_string((size_t)TAM_STATIC_SCRATCH_BYTES) +
+               "; use tam_fill_adjoint or tam_fill_adjoint_scratch";
+    return TAM_EUNSUPPORTED;
+  }
+  if (ctx->device < 0 || ctx->device >= kMaxDevices) {
+    ctx->err = "tam_fill_adjoint_static: device index beyond the library's table";
+    return TAM_EUNSUPPORTED;
+  }
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    ctx->err = "tam_fill_adjoint_static: cudaGetDevice failed";
+    return TAM_ECUDA;
+  }
+  if (prev != ctx->device && cudaSetDevice(ctx->device) != cudaSuccess) {
+    ctx->err = "tam_fill_adjoint_static: cannot make the schedule's device current";
+    return TAM_ECUDA;
+  }
+  void *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_ptr[ctx->device]) {
+      // once per device, with that device current
+      cudaError_t e = cudaGetSymbolAddress(&g_static_ptr[ctx->device], g_adjoint_static_scratch);
+      if (e != cudaSuccess) {
+        g_static_ptr[ctx->device] = nullptr;
+        if (prev != ctx->device) cudaSetDevice(prev);
+        ctx->err = std::string("tam_fill_adjoint_static: cudaGetSymbolAddress: ") +
+                   cudaGetErrorString(e);
+        return TAM_ECUDA;
+      }
+    }
+    scratch = g_static_ptr[ctx->device];
+  }
+  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, first_stage, last_stage, scratch,
+                                   (cudaStream_t)stream);
+  if (prev != ctx->device) cudaSetDevice(prev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->err = std::string("tam_fill_adjoint_static: ") + cudaGetErrorString(e);
+    return TAM_ECUDA;
+  }
+  return TAM_OK;
+}
+
+namespace tam {
 
 cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
                         int32_t last, void *scratch, cudaStream_t stream) {

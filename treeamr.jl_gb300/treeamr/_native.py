@@ -200,7 +200,7 @@ def _declare(lib: C.CDLL):
     lib.tam_schedule_free.restype = None
     lib.tam_schedule_info.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                                       C.POINTER(i32)]
-    for name in ("tam_fill", "tam_fill_plain", "tam_fill_adjoint"):
+    for name in ("tam_fill", "tam_fill_plain", "tam_fill_adjoint", "tam_fill_adjoint_static"):
         if not hasattr(lib, name):
             continue
         f = getattr(lib, name)
