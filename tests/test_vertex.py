@@ -1,0 +1,187 @@
+"""Vertex-centred layouts: closed blocks, stage 0 and stage P.
+
+Restates the reference's closed-block properties (``test/closed_tests.jl``,
+``test/ghost_oracles.jl:420-470`` ``closed_values``, ``test/reflect_tests.jl``,
+``test/outflow_tests.jl``) on the oracle, then checks the CUDA engine against
+the oracle bit for bit."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from _helpers import (awkward_fill, boundary_from, exact_values, ghost_mask, makepoly, nanbits,
+                      nested_forest)
+from treeamr import (EvenParity, FieldSet, Forest, GhostSchedule, OddParity, Operators,
+                     fill_ghosts, vertexcentered)
+from treeamr.schedule import SELFIMAGE_TAG, UNIFY_TAG
+
+
+def _own_copies_consistent(fs, out, periodic):
+    """Every stored copy of every point of any block's closed range holds one
+    value: the primary's (stage 0; ``closed_values``)."""
+    f = fs.forest
+    D, N = f.D, f.N
+    G = fs.G
+    L = f.maxlevel()
+    vals, bad = {}, 0
+    for b, k in enumerate(f.leaves):
+        B = f.block_base(k)
+        sc = 1 << (L - k.level)
+        for idx in np.ndindex(*([N + 1] * D)):
+            pos = tuple((B[d] + idx[d]) * sc for d in range(D))
+            if periodic:
+                pos = tuple(p % ((f.roots[d] * N) << L) for d, p in enumerate(pos))
+            v = out[(b, slice(None)) + tuple(reversed([G[d] + idx[d] for d in range(D)]))]
+            v = v.view(np.uint64)
+            if pos in vals:
+                bad += int(not np.array_equal(vals[pos], v))
+            else:
+                vals[pos] = v.copy()
+    return bad, len(vals)
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+def test_vertex_partition(D):
+    f = nested_forest(D, N=8)
+    fs = FieldSet(f, 1, G=2, centering=vertexcentered(D))
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    counts = s.write_counts()
+    m = ghost_mask(fs)
+    for b in range(f.nleaves()):
+        assert (counts[b][m] == 1).all()
+        assert (counts[b][~m] == 0).all()
+    assert s.unify and UNIFY_TAG in s.stage_tags
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+@pytest.mark.parametrize("p", [2, 4])
+def test_vertex_exact_for_polynomials(D, p):
+    f = nested_forest(D, N=8)
+    fs = FieldSet(f, 2, G=2, centering=vertexcentered(D))
+    ops = Operators(prolongation=p, restriction=p)
+    s = GhostSchedule(fs, ops)
+    for deg, exact_expected in ((p - 1, True), (p, False)):
+        exact = exact_values(fs, makepoly(D, deg))
+        host = exact.copy()
+        host[:, :, ghost_mask(fs)] = np.nan
+        fs.work.copy_(torch.from_numpy(host))
+        out = oracle.fill_fieldset(fs, s, boundary_values=boundary_from(exact))
+        assert not np.isnan(out).any()
+        err = np.max(np.abs(out - exact))
+        if exact_expected:
+            assert err < 1e-10
+        else:
+            assert err > 1e-9
+
+
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_every_copy_of_a_shared_point_agrees(D, periodic):
+    f = nested_forest(D, N=8, periodic=(periodic,) * D)
+    fs = FieldSet(f, 2, G=2, centering=vertexcentered(D))
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    rng = np.random.default_rng(D)
+    host = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    fs.work.copy_(torch.from_numpy(host))
+    exact = host.copy()
+    out = oracle.fill_fieldset(fs, s, boundary_values=boundary_from(exact))
+    bad, n = _own_copies_consistent(fs, out, periodic)
+    assert n > 0 and bad == 0
+
+
+def _walls_forest(D, N=8, levels=2):
+    refl = tuple((True, False) for _ in range(D))
+    outf = tuple((False, True) for _ in range(D))
+    f = Forest((2,) * D, N=N, reflecting=refl, outflow=outf, extents=[(0.0, 2.0)] * D)
+    for _ in range(levels):
+        f.refine(f.leaves[0])
+        f.balance()
+    return f
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+def test_vertex_reflecting_parity_and_stage_p(D):
+    f = _walls_forest(D)
+    par = [(EvenParity,) * D, tuple(OddParity if d == 0 else EvenParity for d in range(D))]
+    fs = FieldSet(f, 2, G=2, centering=vertexcentered(D), parity=par)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    assert s.selfimage and SELFIMAGE_TAG in s.stage_tags
+
+    def fn(x, v):
+        if v == 0:
+            return sum((x[d] ** 2) * (0.5 + d) for d in range(D)) + 1.0
+        return x[0] * (1.0 + sum(x[d] ** 2 for d in range(1, D)))
+    exact = exact_values(fs, fn)
+    host = exact.copy()
+    host[:, :, ghost_mask(fs)] = np.nan
+    fs.work.copy_(torch.from_numpy(host))
+    out = oracle.fill_fieldset(fs, s)
+    assert not np.isnan(out).any()
+    G, N = 2, 8
+    low = np.ones(out.shape[2:], bool)
+    for a in np.indices(out.shape[2:]):
+        low &= a < G + N + 1                       # leave out the outflow (high) ghosts
+    assert np.max(np.abs(out - exact)[:, :, low]) < 1e-12
+    # random data: stage P zeroes the odd variable on the reflecting wall plane
+    rng = np.random.default_rng(3)
+    fs.work.copy_(torch.from_numpy(rng.uniform(-1, 1, size=host.shape)))
+    out = oracle.fill_fieldset(fs, s)
+    for b, k in enumerate(f.leaves):
+        if k.coords[0] == 0 and f.root_position(k.root)[0] == 0:
+            assert not np.any(out[b, 1][..., G])
+            assert np.any(out[b, 0][..., G])
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+def test_vertex_outflow_ghost_is_the_wall_row(D):
+    f = Forest((1,) * D, N=8, outflow=tuple((True, True) for _ in range(D)))
+    fs = FieldSet(f, 1, G=2, centering=vertexcentered(D))
+    rng = np.random.default_rng(7)
+    fs.work.copy_(torch.from_numpy(rng.uniform(-1, 1, size=tuple(fs.work.shape))))
+    out = oracle.fill_fieldset(fs, GhostSchedule(fs, Operators(prolongation=2, restriction=2)))
+    G, N = 2, 8
+    idx = np.indices(tuple(reversed(fs.stored)))
+    near = [np.clip(idx[k], G, G + N) for k in range(D)]
+    assert np.array_equal(out[0, 0], out[0, 0][tuple(near)])
+
+
+# --- the CUDA engine against the oracle --------------------------------------
+
+def _gpu_fill(fs, s, host, method):
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fs.factors = fs.factors.cuda()
+    fill_ghosts(fs, s, method=method)
+    torch.cuda.synchronize()
+    return fs.work.cpu().numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["fused", "plain"])
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_vertex_walls_bit_exact(cuda_lib, method, D, T):
+    f = _walls_forest(D)
+    par = [(EvenParity,) * D] * 2 + [tuple(OddParity if e == d else EvenParity
+                                           for e in range(D)) for d in range(D)]
+    fs = FieldSet(f, len(par), G=2, centering=vertexcentered(D), parity=par, T=T)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    host = awkward_fill(tuple(fs.work.shape), T, seed=D)
+    fs.work.copy_(torch.from_numpy(host))
+    expect = oracle.fill_fieldset(fs, s)
+    got = _gpu_fill(fs, s, host, method)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_gpu_vertex_nested_bit_exact(cuda_lib, D, periodic):
+    f = nested_forest(D, N=8, periodic=(periodic,) * D)
+    fs = FieldSet(f, 3, G=2, centering=vertexcentered(D))
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    rng = np.random.default_rng(11)
+    host = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    fs.work.copy_(torch.from_numpy(host))
+    expect = oracle.fill_fieldset(fs, s)
+    got = _gpu_fill(fs, s, host, "fused")
+    assert np.array_equal(nanbits(got), nanbits(expect))

@@ -128,6 +128,9 @@ def check_fill(fs: FieldSet, schedule: GhostSchedule):
                          f"the field set has {fs.centering}")
     if fs.T != schedule.T:
         raise ValueError(f"the schedule was built for {schedule.T}, the field set holds {fs.T}")
+    if schedule.selfimage and schedule.parities and fs.parities != schedule.parities:
+        raise ValueError("the schedule's stage P was built for other variable parities than "
+                         "the field set's; build the schedule from this field set")
     if fs.work.device.type != "cuda":
         raise ValueError("fill_ghosts runs on the GPU: the field set must live on a CUDA device")
 

@@ -87,6 +87,58 @@ def random_fill(fs: FieldSet, seed: int = 1, lo=-1.0, hi=1.0) -> FieldSet:
     return fs
 
 
+def walls_points(seed: int = 2, n: int = 2):
+    """The seeded refinement centres of the walls mesh, inside (0.1, 0.9)^3."""
+    rng = np.random.default_rng(seed)
+    return [tuple(float(x) for x in rng.uniform(0.1, 0.9, size=3)) for _ in range(n)]
+
+
+def walls_forest(roots: int = 8, N: int = 32, levels: int = 5, seed: int = 2) -> Forest:
+    """3-D over the unit cube, ``roots^3`` roots, low faces reflecting and high
+    faces outflow; ``levels`` passes that refine every leaf of the pass's
+    level containing or adjacent to one of two seeded points, each followed by
+    balance."""
+    f = Forest((roots,) * 3, N=N, reflecting=((True, False),) * 3,
+               outflow=((False, True),) * 3, extents=((0.0, 1.0),) * 3)
+    pts = walls_points(seed)
+
+    def near(ext):
+        w = ext[0][1] - ext[0][0]
+        return any(all(a - w <= p[d] <= b + w for d, (a, b) in enumerate(ext)) for p in pts)
+    return refine_where(f, near, range(levels))
+
+
+def walls_data(seed: int = 3, width: float = 0.05):
+    """Gaussian bumps of width ``width`` at the two refinement centres plus
+    seeded uniform noise in [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    pts = walls_points()
+
+    def fn(x, v):
+        bump = sum(np.exp(-sum((x[d] - p[d]) ** 2 for d in range(3)) / (2 * width ** 2))
+                   for p in pts)
+        return bump + rng.uniform(-1.0, 1.0, size=np.shape(x[0]))
+    return fn
+
+
+def walls_parities():
+    """Five even variables and a vector's three components, each odd in its
+    own dimension."""
+    from .storage import EvenParity, OddParity
+    even = (EvenParity,) * 3
+    vec = [tuple(OddParity if e == d else EvenParity for e in range(3)) for d in range(3)]
+    return [even] * 5 + vec
+
+
+def walls_setup(device="cpu", T=np.float64, roots=8, N=32, levels=5, G=2):
+    from .storage import vertexcentered
+    f = walls_forest(roots=roots, N=N, levels=levels)
+    fs = FieldSet(f, 8, G=G, centering=vertexcentered(3), parity=walls_parities(), T=T,
+                  device=device)
+    ops = Operators(prolongation=4, restriction=4)
+    return f, fs, ops
+
+
 WORKLOADS = {
     "quadrant": dict(desc="2-D 4x4 periodic roots, N=8, G=2, cell, 1 var F64, 25% of roots "
                           "refined once, PV(4,4)"),

@@ -22,6 +22,7 @@ struct-of-arrays descriptors the CUDA library uploads once.
 from __future__ import annotations
 
 from fractions import Fraction
+import itertools
 from typing import Dict, List, NamedTuple, Optional, Sequence, Tuple
 
 import numpy as np
@@ -156,8 +157,8 @@ def target_range(N: int, G: int, c: int, dd: int, od: int, halved: bool) -> rang
     return range(G + 1, G + N + c + 1)
 
 
-def copy_stencil(T, N, G, c, dd) -> Stencil1D:
-    rng = target_range(N, G, c, dd, 0, False)
+def copy_stencil(T, N, G, c, dd, span: int = -1) -> Stencil1D:
+    rng = piece_range(N, G, c, span) if span >= 0 else target_range(N, G, c, dd, 0, False)
     return Stencil1D(rng.start, [j - N * dd for j in rng], [(Fraction(1),)] * len(rng), T)
 
 
@@ -220,10 +221,14 @@ def conservative_prolong_stencil(T, N, G, c, dd, od, p) -> Stencil1D:
     return Stencil1D(rng.start, ss, ws, T)
 
 
-def kind_stencil(T, N, G, c, kind, dd, od, ops: Operators) -> Stencil1D:
-    """``src/schedule.jl:1183-1195`` (no element sets)."""
+def kind_stencil(T, N, G, c, kind, dd, od, ops: Operators, span: int = -1) -> Stencil1D:
+    """``src/schedule.jl:1183-1195`` (no element sets); ``span`` a sub-piece
+    span along a tangential vertex-like dimension (``prolongation_stencil``)."""
     if kind == COPY:
-        return copy_stencil(T, N, G, c, dd)
+        return copy_stencil(T, N, G, c, dd, span)
+    if kind == PROLONG and span >= 0:
+        return prolong_stencil_over(T, piece_range(N, G, c, span), N, G, c, dd, od,
+                                    ops.vertex_order())
     if kind == RESTRICT:
         return restrict_stencil_over(T, target_range(N, G, c, dd, od, True), N, G, c, dd, od,
                                      ops.restriction)
@@ -271,11 +276,16 @@ def mirror_restriction(T, N, G, od, p) -> Stencil1D:
 
 # --- the neighbour search ---------------------------------------------------
 
-NOSPAN = None
-
-
 def _nospan(D):
     return (-1,) * D
+
+
+def _record(pairs, key, b, s):
+    lst = pairs.get(key)
+    if lst is None:
+        lst = pairs[key] = ([], [])
+    lst[0].append(b + 1)
+    lst[1].append(s + 1)
 
 
 def boundary_region(forest: Forest, k: MortonKey, b: int, delta, region) -> BoundaryRegion:
@@ -283,22 +293,23 @@ def boundary_region(forest: Forest, k: MortonKey, b: int, delta, region) -> Boun
 
 
 def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
-                  boundaries: List[BoundaryRegion], forest: Forest, G, c, b: int, dirs):
-    """Every transfer block ``b``'s ghosts need (``src/schedule.jl:1525-1610``).
-    ``b`` is 0-based; recorded block indices are 1-based."""
+                  boundaries: List[BoundaryRegion], forest: Forest, G, c, b: int, dirs,
+                  table: Optional["NeighbourTable"] = None):
+    """Every transfer block ``b``'s ghosts need (``src/schedule.jl:1525-1610``),
+    and for a layout with a vertex-like dimension its stage-0 transfers
+    (``unify_sources!``).  ``b`` is 0-based; recorded block indices are 1-based.
+    Returns the block's primary bits (0 for a cell-centred layout)."""
     k = forest.leaves[b]
     N, D = forest.N, forest.D
     zero = (0,) * D
     nomirror = (0,) * D
     nospan = _nospan(D)
+    closed = any(cd == 1 for cd in c)
+    if closed and table is None:
+        table = NeighbourTable(forest, b)
 
-    def record(kind, offset, lvl, s, delta):
-        key = GroupKey(kind, delta, offset, lvl, nomirror, nospan)
-        lst = pairs.get(key)
-        if lst is None:
-            lst = pairs[key] = ([], [])
-        lst[0].append(b + 1)
-        lst[1].append(s + 1)
+    def record(kind, offset, lvl, s, delta, span=nospan):
+        _record(pairs, GroupKey(kind, tuple(delta), offset, lvl, nomirror, span), b, s)
 
     for delta in dirs:
         region = [target_range(N, G[d], c[d], delta[d], 0, False) for d in range(D)]
@@ -309,6 +320,8 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
             mirror_sources(pairs, boundaries, forest, G, c, b, delta, dprime, faces, region)
             continue
         nbrs = forest.oriented_neighbors(k, delta)
+        if table is not None:
+            table.remember(delta, nbrs)
         if not nbrs:
             boundaries.append(boundary_region(forest, k, b, delta, region))
             continue
@@ -316,10 +329,22 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
         if nbl == k.level:
             record(COPY, zero, 0, forest.find_leaf(nbrs[0]), delta)
         elif nbl < k.level:
-            record(PROLONG, childoffset(k), k.level, forest.find_leaf(nbrs[0]), delta)
+            src = forest.find_leaf(nbrs[0])
+            parts = ghost_plane_parts(forest, k, delta, delta, c, src) if closed else None
+            if parts is None:
+                record(PROLONG, childoffset(k), k.level, src, delta)
+            else:
+                for kind, dirn, span, s in parts:
+                    if kind == PROLONG:
+                        record(PROLONG, childoffset(k), k.level, s, delta, span)
+                    else:
+                        record(COPY, zero, 0, s, dirn, span)
         else:
             for nbr in nbrs:
                 record(RESTRICT, childoffset(nbr), 0, forest.find_leaf(nbr), delta)
+    if closed:
+        return unify_sources(pairs, forest, c, b, table)
+    return 0
 
 
 def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, walls, region):
@@ -331,14 +356,10 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
     mask = [w != OUTER for w in walls]
     state = tuple(0 if not mask[d] else 3 if walls[d] == OUTFLOW else 1 for d in range(D))
     nospan = _nospan(D)
+    closed = any(cd == 1 for cd in c)
 
-    def record(kind, offset, lvl, s):
-        key = GroupKey(kind, tuple(delta), offset, lvl, state, nospan)
-        lst = pairs.get(key)
-        if lst is None:
-            lst = pairs[key] = ([], [])
-        lst[0].append(b + 1)
-        lst[1].append(s + 1)
+    def record(kind, offset, lvl, s, dirn=tuple(delta), span=nospan):
+        _record(pairs, GroupKey(kind, tuple(dirn), offset, lvl, state, span), b, s)
 
     if dprime == zero:
         record(COPY, zero, 0, b)
@@ -351,13 +372,400 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
     if nbl == k.level:
         record(COPY, zero, 0, forest.find_leaf(nbrs[0]))
     elif nbl < k.level:
-        record(PROLONG, childoffset(k), k.level, forest.find_leaf(nbrs[0]))
+        src = forest.find_leaf(nbrs[0])
+        parts = ghost_plane_parts(forest, k, tuple(delta), dprime, c, src) if closed else None
+        if parts is None:
+            record(PROLONG, childoffset(k), k.level, src)
+        else:
+            for kind, dirn, span, s in parts:
+                if kind == PROLONG:
+                    record(PROLONG, childoffset(k), k.level, s, tuple(delta), span)
+                else:
+                    record(COPY, zero, 0, s, dirn, span)
     else:
         wallside = [0 if delta[d] < 0 else 1 for d in range(D)]
         for nbr in nbrs:
             o = childoffset(nbr)
             if all((not mask[d]) or o[d] == wallside[d] for d in range(D)):
                 record(RESTRICT, o, 0, forest.find_leaf(nbr))
+
+
+# --- closed blocks: the primary of a shared point (vertex-like layouts) ---
+#
+# A point on a block face of a vertex-like dimension is held by every block
+# whose closed box contains it; one copy is the primary and stage 0 gives
+# the others its value (src/schedule.jl:1612-1990).  A block's closed box
+# falls into pieces by class per dimension (0 low face plane, 1 open
+# interior, 2 high face plane; 1 along a cell-like dimension) and finer into
+# sub-pieces (0 low plane, 1 lower open half, 2 mid-plane, 3 upper open
+# half, 4 high plane; 1 and 3 along a cell-like dimension).  The primary is
+# the copy on the finest level holding the point, and among those the one
+# with the greatest class tuple, dimension 1 first.
+
+def span_code(lo: int, hi: int) -> int:
+    return 8 * lo + hi
+
+
+def span_classes(code: int) -> Tuple[int, int]:
+    return code >> 3, code & 7
+
+
+def piece_range(N: int, G: int, c: int, code: int) -> range:
+    """Stored range of a span of sub-pieces (``src/schedule.jl:942-950``)."""
+    lo, hi = span_classes(code)
+    h = N // 2
+    if c == 0:
+        first = G + 1 if lo == 1 else G + h + 1
+        last = G + h if hi == 1 else G + N
+        return range(first, last + 1)
+    first = (G + 1, G + 2, G + h + 1, G + h + 2, G + N + 1)[lo]
+    last = (G + 1, G + h, G + h + 1, G + N, G + N + 1)[hi]
+    return range(first, last + 1)
+
+
+def piece_index(cls) -> int:
+    return sum(x * 3 ** d for d, x in enumerate(cls))
+
+
+def _product_dim1_fastest(values):
+    for rev in itertools.product(*reversed(values)):
+        yield tuple(reversed(rev))
+
+
+def closed_pieces(c):
+    return list(_product_dim1_fastest([(0, 1, 2) if cd == 1 else (1,) for cd in c]))
+
+
+def subpiece_values(c, N):
+    return [(1, 3) if cd == 0 else (0, 2, 4) if N == 2 else (0, 1, 2, 3, 4) for cd in c]
+
+
+def subpiece_list(c, N):
+    return list(_product_dim1_fastest(subpiece_values(c, N)))
+
+
+def piece_class(sub: int) -> int:
+    return 0 if sub == 0 else 2 if sub == 4 else 1
+
+
+def piece_of(sub):
+    return tuple(piece_class(x) for x in sub)
+
+
+def piece_representative(cls, c):
+    return tuple(1 if cd == 0 else 2 * x for x, cd in zip(cls, c))
+
+
+def piece_span(cls: int) -> int:
+    return span_code(0, 0) if cls == 0 else span_code(4, 4) if cls == 2 else span_code(1, 3)
+
+
+class NeighbourTable:
+    """The neighbours of one block per direction, looked up once
+    (``src/schedule.jl:1733-1782``): ``(level or -1, [(leaf, offset)])``."""
+
+    def __init__(self, forest: Forest, j: int):
+        self.forest = forest
+        self.j = j
+        self.level = forest.leaves[j].level
+        self.entries = {}
+
+    def remember(self, delta, nbrs):
+        if not nbrs:
+            e = (-1, [])
+        else:
+            e = (nbrs[0].level, [(self.forest.find_leaf(n), childoffset(n)) for n in nbrs])
+        self.entries[tuple(delta)] = e
+        return e
+
+    def neighbours(self, delta):
+        delta = tuple(delta)
+        e = self.entries.get(delta)
+        if e is None:
+            e = self.remember(delta, self.forest.oriented_neighbors(self.forest.leaves[self.j],
+                                                                   delta))
+        return e
+
+
+def piece_copies(t: NeighbourTable, sub, c):
+    """Every copy of sub-piece ``sub`` of ``t``'s block on its level or a finer
+    one, as ``(level, leaf, class, direction, offset)``, its own first
+    (``src/schedule.jl:1794-1854``; one brick, no seams or glue, so every copy
+    lies at the same position)."""
+    D = len(c)
+    zero = (0,) * D
+    cls = piece_of(sub)
+    copies = [(t.level, t.j, cls, zero, zero)]
+    side = tuple((-1 if cls[d] == 0 else 1) if (c[d] == 1 and cls[d] != 1) else 0
+                 for d in range(D))
+    for m in range(1, 1 << D):
+        if any((m >> d) & 1 and side[d] == 0 for d in range(D)):
+            continue
+        delta = tuple(side[d] if (m >> d) & 1 else 0 for d in range(D))
+        lvl, nbrs = t.neighbours(delta)
+        if lvl < 0 or lvl < t.level:
+            continue
+        across = tuple(cls[d] if delta[d] == 0 else 2 - cls[d] for d in range(D))
+        if lvl == t.level:
+            leaf, _ = nbrs[0]
+            copies.append((lvl, leaf, across, delta, zero))
+            continue
+        for leaf, o in nbrs:
+            holds = all(delta[d] != 0 or
+                        (o[d] == (1 if sub[d] == 3 else 0) if c[d] == 0 else
+                         (sub[d] == 2 or o[d] == (1 if sub[d] >= 3 else 0)))
+                        for d in range(D))
+            if not holds:
+                continue
+            fcls = []
+            for d in range(D):
+                if delta[d] != 0:
+                    fcls.append(across[d])
+                elif c[d] == 0:
+                    fcls.append(1)
+                elif sub[d] == 2:
+                    fcls.append(2 if o[d] == 0 else 0)
+                else:
+                    fcls.append(cls[d] if sub[d] in (0, 4) else 1)
+            copies.append((lvl, leaf, tuple(fcls), delta, o))
+    return copies
+
+
+def piece_primary(copies):
+    """The finest level, then the greatest class tuple; the first on a tie
+    (``src/schedule.jl:1921``)."""
+    best, bkey = None, None
+    for x in copies:
+        key = (-x[0], tuple(-v for v in x[2]))
+        if bkey is None or key < bkey:
+            best, bkey = x, key
+    return best
+
+
+def box_spans(subs, allowed):
+    D = len(allowed)
+    lo = tuple(min(p[d] for p in subs) for d in range(D))
+    hi = tuple(max(p[d] for p in subs) for d in range(D))
+    box = 1
+    for d in range(D):
+        box *= sum(1 for x in allowed[d] if lo[d] <= x <= hi[d])
+    return tuple(span_code(lo[d], hi[d]) for d in range(D)) if box == len(subs) else None
+
+
+def merged_transfers(entries, allowed):
+    """Stage 0's merging (``src/schedule.jl:2093-2125``): one transfer per
+    source, direction and offset over the bounding box of its sub-pieces where
+    they fill it; restrictions merged within one piece of the target only."""
+    bysource = {}
+    for sub, kind, s, delta, o in entries:
+        bysource.setdefault((KINDRANK[kind], s, delta, o), []).append(sub)
+    out = []
+    for key in sorted(bysource):
+        rank, s, delta, o = key
+        kind = COPY if rank == KINDRANK[COPY] else RESTRICT
+        subs = list(dict.fromkeys(bysource[key]))
+        spans = box_spans(subs, allowed) if kind == COPY else None
+        if spans is None:
+            for piece in sorted(set(piece_of(p) for p in subs)):
+                part = [p for p in subs if piece_of(p) == piece]
+                spans = box_spans(part, allowed)
+                if spans is None:
+                    for p in part:
+                        out.append((kind, s, delta, o, tuple(span_code(x, x) for x in p)))
+                else:
+                    out.append((kind, s, delta, o, spans))
+        else:
+            out.append((kind, s, delta, o, spans))
+    return out
+
+
+def unify_transfers(t: NeighbourTable, c):
+    """Stage 0's transfers into ``t``'s block and its primary bits
+    (``src/schedule.jl:1990-2040``)."""
+    forest = t.forest
+    b = t.j
+    D = len(c)
+    entries = []
+    lvl = t.level
+    npieces = 3 ** D
+    shared = [0] * npieces
+    primaries = [None] * npieces
+    bits = 0
+    for sub in subpiece_list(c, forest.N):
+        cls = piece_of(sub)
+        i = piece_index(cls)
+        if shared[i] == 0:
+            copies = piece_copies(t, piece_representative(cls, c), c)
+            primaries[i] = piece_primary(copies)
+            shared[i] = 1 if all(x[0] == lvl for x in copies) else 2
+            _, s, scls, _, _ = primaries[i]
+            if s == b and scls == cls:
+                bits |= 1 << i
+        if all(x == 1 for x in cls):
+            continue
+        slvl, s, scls, delta, o = primaries[i] if shared[i] == 1 else \
+            piece_primary(piece_copies(t, sub, c))
+        if s == b and scls == cls:
+            continue
+        entries.append((sub, COPY if slvl == lvl else RESTRICT, s, delta, o))
+    return merged_transfers(entries, subpiece_values(c, forest.N)), bits
+
+
+def unify_sources(pairs, forest: Forest, c, b: int, table: NeighbourTable) -> int:
+    """Stage 0's transfers into block ``b`` (``src/schedule.jl:1948-1988``)."""
+    D = len(c)
+    out, bits = unify_transfers(table, c)
+    for kind, s, delta, o, spans in out:
+        _record(pairs, GroupKey(kind, delta, o, 0, (0,) * D, spans), b, s)
+    return bits
+
+
+def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int):
+    """The ghosts of ``k`` in ``delta`` next to a coarser neighbour ``coarse``,
+    split where a block of ``k``'s level holds a face-plane row along a
+    tangential vertex-like dimension (``src/schedule.jl:1432-1507``).
+    ``None`` where nothing splits; otherwise parts ``(kind, direction, span,
+    source)`` (0-based source)."""
+    D = forest.D
+    tdims = [d for d in range(D) if delta[d] == 0 and c[d] == 1]
+    if not tdims:
+        return None
+    l = k.level
+    found = {}
+
+    def holder(dirn):
+        if dirn not in found:
+            nbrs = forest.oriented_neighbors(k, dirn)
+            if not nbrs:
+                found[dirn] = None
+            else:
+                lv = nbrs[0].level
+                if lv > l:
+                    raise RuntimeError(f"the ghost of {k} in direction {delta} has a face-plane "
+                                       f"row held by a finer block across {dirn}; 2:1 balance "
+                                       "forbids that, so this is a bug")
+                found[dirn] = (lv, forest.find_leaf(nbrs[0]))
+        return found[dirn]
+
+    pieces = list(_product_dim1_fastest([(0, 1, 2)] * len(tdims)))
+    sources = []
+    for cls in pieces:
+        plane = [(tdims[i], -1 if cls[i] == 0 else 1) for i in range(len(tdims)) if cls[i] != 1]
+        best = None
+        subsets = sorted(range(1, 2 ** len(plane)), key=lambda m: (bin(m).count("1"), m))
+        for m in subsets:
+            dirn = list(dlook)
+            for i, (d, s) in enumerate(plane):
+                if (m >> i) & 1:
+                    dirn[d] = s
+            h = holder(tuple(dirn))
+            if h is None:
+                continue
+            lv, j = h
+            if j == coarse:
+                continue
+            if lv == l and best is None:
+                best = (m, j)
+        if best is None:
+            sources.append(None)
+            continue
+        m, j = best
+        dirn = list(delta)
+        for i, (d, s) in enumerate(plane):
+            if (m >> i) & 1:
+                dirn[d] = s
+        sources.append((tuple(dirn), j))
+    if all(s is None for s in sources):
+        return None
+
+    def code(x):
+        return span_code(0, 0) if x == 0 else span_code(1, 3) if x == 1 else span_code(4, 4)
+
+    def spanof(cls):
+        return tuple(code(cls[tdims.index(d)]) if d in tdims else -1 for d in range(D))
+
+    parts = []
+    rest = [cls for cls, s in zip(pieces, sources) if s is None]
+    if rest:
+        n = len(tdims)
+        lo = tuple(min(p[i] for p in rest) for i in range(n))
+        hi = tuple(max(p[i] for p in rest) for i in range(n))
+        vol = 1
+        for i in range(n):
+            vol *= hi[i] - lo[i] + 1
+        if vol == len(rest):
+            fs = {0: 0, 1: 1, 2: 4}
+            ls = {0: 0, 1: 3, 2: 4}
+            span = tuple(span_code(fs[lo[tdims.index(d)]], ls[hi[tdims.index(d)]])
+                         if d in tdims else -1 for d in range(D))
+            parts.append((PROLONG, tuple(delta), span, coarse))
+        else:
+            for cls in rest:
+                parts.append((PROLONG, tuple(delta), spanof(cls), coarse))
+    for cls, s in zip(pieces, sources):
+        if s is None:
+            continue
+        parts.append((COPY, s[0], spanof(cls), s[1]))
+    return parts
+
+
+def selfimage_sources(pairs, forest: Forest, c, b: int, parities, bits: int):
+    """Stage P's transfers of block ``b``: every primary piece on a reflecting
+    wall plane of a vertex-like dimension, keyed by mirror state 2 there
+    (``src/schedule.jl:2605-2634``)."""
+    D = forest.D
+    if not any(cd == 1 for cd in c):
+        return
+    k = forest.leaves[b]
+
+    def face(d, s):
+        step = tuple(s if e == d else 0 for e in range(D))
+        return forest.wall_direction(k, step)[1][d]
+
+    refl = [((face(d, -1) == REFLECTING), (face(d, 1) == REFLECTING)) if c[d] == 1
+            else (False, False) for d in range(D)]
+    if not any(r[0] or r[1] for r in refl):
+        return
+    bystate = {}
+    for cls in closed_pieces(c):
+        if not (bits >> piece_index(cls)) & 1:
+            continue
+        state = tuple(2 if (cls[d] == 0 and refl[d][0]) or (cls[d] == 2 and refl[d][1]) else 0
+                      for d in range(D))
+        if not any(state):
+            continue
+        if parities and not any(any(state[d] == 2 and p[d] == "OddParity" for d in range(D))
+                                for p in parities):
+            continue
+        bystate.setdefault(state, []).append(cls)
+    zero = (0,) * D
+    for state in sorted(bystate):
+        for spans in piece_box_spans(bystate[state], c):
+            _record(pairs, GroupKey(COPY, zero, zero, 0, state, spans), b, b)
+
+
+def piece_box_spans(pieces, c):
+    D = len(c)
+    fs = {0: 0, 1: 1, 2: 4}
+    ls = {0: 0, 1: 3, 2: 4}
+    uniq = list(dict.fromkeys(pieces))
+    lo = tuple(min(p[d] for p in uniq) for d in range(D))
+    hi = tuple(max(p[d] for p in uniq) for d in range(D))
+    vol = 1
+    for d in range(D):
+        vol *= hi[d] - lo[d] + 1
+    if vol == len(uniq):
+        return [tuple(span_code(fs[lo[d]], ls[hi[d]]) for d in range(D))]
+    return [tuple(span_code(fs[p[d]], ls[p[d]]) for d in range(D)) for p in uniq]
+
+
+def unify_stencil(T, N, G, c, key: GroupKey, d: int, p: int) -> Stencil1D:
+    """One dimension of a stage-0 (or stage-P) transfer (``src/schedule.jl:973-984``)."""
+    dd, code = key.direction[d], key.span[d]
+    if key.kind == COPY:
+        return copy_stencil(T, N, G, c, dd, span=code)
+    rng = piece_range(N, G, c, code)
+    return restrict_stencil_over(T, rng, N, G, c, dd, key.offset[d], p)
 
 
 # --- the schedule -------------------------------------------------------------
@@ -386,10 +794,6 @@ class GhostSchedule:
         c = staggers(centering)
         storedsize(N, G, c)
         check_operators(N, G, c, operators)
-        if any(cd == 1 for cd in c):
-            raise NotImplementedError(
-                "vertex-like layouts need the closed-block stages 0 and P, which this "
-                "schedule builder does not provide yet")
         T = np.dtype(T)
         self.forest = forest
         self.generation = forest.generation
@@ -400,23 +804,32 @@ class GhostSchedule:
         self.operators = operators
         self.parities = parity
         self.stored = tuple(N + 2 * g + cd for g, cd in zip(G, c))
+        closed = any(cd == 1 for cd in c)
 
         dirs = alldirections(D)
         pairs: Dict[GroupKey, Tuple[List[int], List[int]]] = {}
+        ppairs: Dict[GroupKey, Tuple[List[int], List[int]]] = {}
         boundaries: List[BoundaryRegion] = []
+        bits = [0] * forest.nleaves()
         for b in range(forest.nleaves()):
-            block_sources(pairs, boundaries, forest, G, c, b, dirs)
+            bits[b] = block_sources(pairs, boundaries, forest, G, c, b, dirs)
+        if closed:
+            for b in range(forest.nleaves()):
+                selfimage_sources(ppairs, forest, c, b, parity or [], bits[b])
         self.boundaries = boundaries
+        self.primary_bits = bits
 
         built = {}
 
         def build1(key: GroupKey, d: int) -> Stencil1D:
+            if isunify(key):
+                return unify_stencil(T, N, G[d], c[d], key, d, operators.restriction)
             dd, od, state = key.direction[d], key.offset[d], key.mirror[d]
             ds = dd if state == 0 else 0
             if state != 0 and key.kind == RESTRICT and c[d] == 1:
                 s = mirror_restriction(T, N, G[d], od, operators.restriction)
             else:
-                s = kind_stencil(T, N, G[d], c[d], key.kind, ds, od, operators)
+                s = kind_stencil(T, N, G[d], c[d], key.kind, ds, od, operators, key.span[d])
             if state == 0:
                 return s
             if state == 3:
@@ -437,14 +850,18 @@ class GhostSchedule:
             tb, sb = pairs[key]
             groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
                                         transfer_stage(key)))
+        for key in sorted(ppairs, key=GroupKey.order):
+            tb, sb = ppairs[key]
+            groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
+                                        SELFIMAGE_TAG))
         self.groups = groups
+        self.selfimage = [g for g in groups if g.stage == SELFIMAGE_TAG]
         self.unify = [g for g in groups if g.stage == UNIFY_TAG]
         self.phase1 = [g for g in groups if g.stage == PHASE1_TAG]
         levels = sorted({g.key.level for g in groups if g.stage >= 2})
         self.levels = levels
         self.phase2 = [[g for g in groups if g.stage == prolongation_tag(l)] for l in levels]
-        self.selfimage: List[TransferGroup] = []
-        # every group in the order the fill runs them: stage P, stage 0,
+        # the stage tags in the order the fill runs them: stage P, stage 0,
         # phase 1, then the prolongations coarsest target level first
         self.stage_tags = sorted({g.stage for g in groups})
 
@@ -478,6 +895,8 @@ class GhostSchedule:
         D = self.forest.D
         counts = np.zeros((self.forest.nleaves(),) + tuple(reversed(self.stored)), dtype=np.int64)
         for g in self.groups:
+            if g.stage < PHASE1_TAG:        # stages P and 0 write owned points
+                continue
             sl = tuple(slice(s.targetfirst - 1, s.targetfirst - 1 + s.ntarget)
                        for s in reversed(g.stencils))
             for tb in g.targetblocks:
