@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-walls", action="store_true")
+    ap.add_argument("--workload", choices=["sphere", "walls"], default="sphere",
+                    help="walls: time only the walls mesh (for profiling)")
+    ap.add_argument("--dtype", choices=["float32", "float64"], default="float32",
+                    help="element type of --workload walls")
     return ap.parse_args()
 
 
@@ -67,7 +71,7 @@ def measure_walls(T, dev, timed, args, peak):
     from treeamr import GhostSchedule, fill_ghosts, meshes
     from treeamr.autotune import autotune
     from treeamr.ghosts import device_schedule
-    f, fs, ops = meshes.walls_setup(device=dev, T=T)
+    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots)
     sched = GhostSchedule(fs, ops)
     g = torch.Generator(device=dev).manual_seed(7)
     fs.work.uniform_(-1.0, 1.0, generator=g)
@@ -222,6 +226,28 @@ def main():
     from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
     from treeamr.ghosts import device_schedule
     from treeamr import _native
+
+    if args.workload == "walls":
+        stream = torch.cuda.current_stream(dev)
+
+        def timed_walls(fn, steps):
+            torch.cuda.synchronize(dev)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(steps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            return a.elapsed_time(b) / steps
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        out = measure_walls(np.dtype(args.dtype).type, dev, timed_walls, args,
+                            float(peaks.get("hbm_gbs", 6800.0)))
+        print(json.dumps(out), flush=True)
+        return 0
 
     f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
     fs = FieldSet(f, args.nvars, G=3, T=np.float64, device=dev)

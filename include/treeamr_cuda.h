@@ -189,6 +189,51 @@ int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int64_t nblock
                             const void *factors, int32_t first_stage, int32_t last_stage,
                             void *stream);
 
+/* A batch: several independent forests filled together, one launch per
+ * stage for all of them.  No reference counterpart (the reference fills one
+ * field set per call, src/ghosts.jl:1783); this is the multi-forest form of
+ * tam_fill for field data laid out in one arena, each member's `work`
+ * (column-major, its own S_d and nblocks, `nvars` shared) starting at
+ * work_offsets[m] elements and its factor table at factor_offsets[m]
+ * (NULL when no member mirrors).  Members share dimension and element type;
+ * they stay owned by the caller and must outlive the batch. */
+typedef struct tam_batch tam_batch;
+int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
+                     const int64_t *work_offsets, const int64_t *factor_offsets,
+                     tam_batch **out);
+void tam_batch_free(tam_batch *b);
+/* Every stage tag in [first_stage, last_stage] of every member; the arena
+ * holds arena_elems elements (checked against every member's extent). */
+int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                   const void *factor_arena, int64_t factor_elems, int32_t first_stage,
+                   int32_t last_stage, void *stream);
+/* The adjoint of tam_batch_fill, member by member (tam_fill_adjoint). */
+int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                           const void *factor_arena, int64_t factor_elems,
+                           int32_t first_stage, int32_t last_stage, void *stream);
+/* tam_schedule_set_option for a batch. */
+int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value);
+
+/* The second-order wave equation's right-hand side, u_t = v, v_t = lap(u)
+ * with the 7-point Laplacian, over every owned point of every listed block
+ * (the RHS of the reference's wave test, test/wave.jl:49-110; the
+ * application step around the fill, `map_blocks!`, src/state.jl:393).
+ * Cell-centred blocks with G >= 1; u is variable 1 of a block and v
+ * variable 2.  adjoint = 0: out = f(in) at owned points (out's ghosts are
+ * left alone).  adjoint = 1: out = f^T(in) at every stored point.  `blocks`
+ * is a device array. */
+typedef struct tam_wave_block {
+  int64_t off;     /* element offset of the block's variable u            */
+  int32_t S[3];    /* stored extents                                      */
+  int32_t G;       /* ghost width                                         */
+  int32_t N;       /* owned cells per dimension                           */
+  int32_t pad;
+  double inv_h2;   /* 1 / h^2 of the block's level                        */
+} tam_wave_block;
+int tam_wave_rhs(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
+                 int32_t max_points_per_block, const void *in, void *out, int32_t adjoint,
+                 void *stream);
+
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing
  * one changes speed only, never a result. */

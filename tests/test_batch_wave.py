@@ -1,0 +1,150 @@
+"""Many forests in one launch, and RK4 for the wave equation over them.
+
+The batch is a new capability (the reference fills one field set per call);
+its oracle is the per-member fill, which must agree bit for bit.  The RK4
+solver restates the reference's wave test (``test/wave.jl:49-110``) on the
+batch; its adjoint is checked by the dot-product test of the whole multi-step
+map and against central differences, with checkpointed recomputation."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from treeamr import GhostSchedule, fill_ghosts, meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_batch(T=np.float32, n=5, seed=7):
+    return meshes.forest_batch_setup(n=n, seed=seed, T=T, max_roots=3, max_levels=2)
+
+
+def test_batch_fill_equals_member_fills(cuda_lib):
+    fss, scheds, batch = _small_batch(np.float32)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    batch.arena.uniform_(-1, 1, generator=g)
+    start = batch.arena.clone()
+    # oracle: each member filled alone, on the CPU
+    expect = []
+    for m, (fs, s) in enumerate(zip(fss, scheds)):
+        host = batch.member_view(start, m).cpu().numpy().copy()
+        expect.append(oracle.fill(s, host, fs.nvars, fs.factors_host))
+    batch.fill()
+    torch.cuda.synchronize()
+    for m in range(len(fss)):
+        got = batch.member_view(batch.arena, m).cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), expect[m].view(np.uint32)), m
+    # and each member through its own fill gives the same
+    alone = start.clone()
+    for m, (fs, s) in enumerate(zip(fss, scheds)):
+        fs.work = batch.member_view(alone, m)
+        fill_ghosts(fs, s)
+    assert torch.equal(alone.view(torch.int32), batch.arena.view(torch.int32))
+
+
+def test_batch_rejects_a_short_arena(cuda_lib):
+    import ctypes as C
+    from treeamr import _native
+    fss, scheds, batch = _small_batch(np.float32, n=2)
+    short = batch.arena[: batch.arena.numel() // 2]
+    with pytest.raises(_native.TamError, match="outside the arena"):
+        batch.fill(short.contiguous())
+
+
+def test_wave_rhs_matches_torch(cuda_lib):
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = _small_batch(np.float64, n=3)
+    solver = WaveSolver(batch)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    x = torch.rand(batch.arena.shape, dtype=torch.float64, device="cuda", generator=g)
+    out = torch.zeros_like(x)
+    solver.rhs(x, out)
+    for m, fs in enumerate(fss):
+        xv = batch.member_view(x, m)
+        ov = batch.member_view(out, m)
+        G, N = fs.G[0], fs.forest.N
+        o = slice(G, G + N)
+        u = xv[:, 0]
+        lap = (u[:, G + 1:G + N + 1, o, o] + u[:, G - 1:G + N - 1, o, o] +
+               u[:, o, G + 1:G + N + 1, o] + u[:, o, G - 1:G + N - 1, o] +
+               u[:, o, o, G + 1:G + N + 1] + u[:, o, o, G - 1:G + N - 1] - 6 * u[:, o, o, o])
+        h2 = torch.tensor([float(fs.forest.spacing(k.level)) ** 2 for k in fs.forest.leaves],
+                          dtype=torch.float64, device="cuda").view(-1, 1, 1, 1)
+        assert torch.allclose(ov[:, 1, o, o, o], lap / h2, rtol=1e-12, atol=1e-9)
+        assert torch.equal(ov[:, 0, o, o, o], xv[:, 1, o, o, o])
+
+
+def test_wave_graph_equals_eager(cuda_lib):
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = _small_batch(np.float32)
+    meshes.wave_initial(batch)
+    solver = WaveSolver(batch)
+    y0 = batch.arena.clone()
+    eager = y0.clone()
+    for _ in range(4):
+        solver.step(eager)
+    y = y0.clone()
+    graph = solver.capture(y, steps=2)
+    y.copy_(y0)
+    graph.replay()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(y.view(torch.int32), eager.view(torch.int32))
+    assert torch.isfinite(y).all()
+
+
+def test_wave_adjoint_dot_product(cuda_lib):
+    """<M^n x, y> = <x, (M^T)^n y> for n = 10 RK4 steps, Float64."""
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = _small_batch(np.float64)
+    solver = WaveSolver(batch)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.rand(batch.arena.shape, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    yv = torch.rand(batch.arena.shape, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    mx = x.clone()
+    for _ in range(10):
+        solver.step(mx)
+    mty = yv.clone()
+    for _ in range(10):
+        solver.step_adjoint(mty)
+    lhs = torch.dot(mx, yv).item()
+    rhs = torch.dot(x, mty).item()
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))
+
+
+def test_wave_gradient_checkpointed(cuda_lib):
+    """The gradient of L = sum_n sum(w * y_n^2) over 10 steps: checkpoints every
+    2 steps give the same as every step, and central differences agree."""
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = _small_batch(np.float64, n=3)
+    solver = WaveSolver(batch)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    y0 = torch.rand(batch.arena.shape, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    w = torch.rand(batch.arena.shape, dtype=torch.float64, device="cuda", generator=g)
+
+    def loss(y):
+        y = y.clone()
+        total = 0.0
+        for _ in range(10):
+            solver.step(y)
+            total += torch.sum(w * y * y).item()
+        return total
+
+    grad2 = solver.gradient(y0, 10, lambda y: 2 * w * y, checkpoint=2)
+    grad1 = solver.gradient(y0, 10, lambda y: 2 * w * y, checkpoint=1)
+    assert torch.equal(grad1, grad2)
+    rng = np.random.default_rng(0)
+    # owned points of the first member, where the gradient is not trivially 0
+    fs = fss[0]
+    G, N = fs.G[0], fs.forest.N
+    view = batch.member_view(torch.arange(y0.numel(), device="cuda"), 0)
+    idx = view[:, :, G:G + N, G:G + N, G:G + N].reshape(-1)
+    h = 1e-6
+    for k in rng.choice(idx.cpu().numpy(), size=8, replace=False):
+        yp = y0.clone()
+        ym = y0.clone()
+        yp[k] += h
+        ym[k] -= h
+        fd = (loss(yp) - loss(ym)) / (2 * h)
+        gk = grad2[k].item()
+        assert abs(fd - gk) <= 1e-5 * max(1.0, abs(gk)), (k, fd, gk)

@@ -233,7 +233,7 @@ void build_product_table(const tam_schedule_desc *d, const tam_group &h, tam::De
 
 tam::SchedArgs sched_args(const tam_sched *s) {
   return tam::SchedArgs{s->d_groups, s->d_tb, s->d_sb, s->d_srcstart, s->d_weights, s->d_cls,
-                        s->d_wtab, s->shape.int_mul};
+                        s->d_wtab, s->shape.int_mul, nullptr};
 }
 
 // The fused tiles of every stage: each stage's transfers ordered by target
@@ -255,11 +255,16 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
     std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
       return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
     });
-    for (const Entry &e : entries) {
-      const tam::DevGroup &g = s->groups[e.group];
-      const int box = g.n[0] * g.n[1] * g.n[2];
-      for (int i0 = 0; i0 < box; i0 += ti)
-        tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+    // unit copies first (the light kernel), then the stencils
+    for (int pass = 0; pass < 2; ++pass) {
+      for (const Entry &e : entries) {
+        const tam::DevGroup &g = s->groups[e.group];
+        if ((g.pclass == 0) != (pass == 0)) continue;
+        const int box = g.n[0] * g.n[1] * g.n[2];
+        for (int i0 = 0; i0 < box; i0 += ti)
+          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+      }
+      if (pass == 0) st.ncopy = (int64_t)tiles.size() - st.tile0;
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
@@ -418,6 +423,11 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
     return e == cudaErrorMemoryAllocation ? fail(ctx, TAM_ENOMEM, "device allocation failed")
                                           : cuda_fail(ctx, e, "schedule upload");
   }
+  // host copies of the pools, for a batch of forests (tam_batch_create)
+  s->h_pool_srcstart = std::move(srcstart);
+  s->h_pool_weights = std::move(weights);
+  s->h_pool_cls = std::move(cls);
+  s->h_pool_wtab = std::move(wtab);
   *out = s;
   return TAM_OK;
 }
@@ -528,7 +538,8 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
   for (const tam::Stage &stage : s->stages) {
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
     cudaError_t e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles + stage.tile0,
-                                            stage.ntiles, sched_args(s), work, factors, nvars,
+                                            stage.ncopy, stage.ntiles, sched_args(s), work,
+                                            factors, nvars,
                                             s->S, s->shape.threads, st);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
   }

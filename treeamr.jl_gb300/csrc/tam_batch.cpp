@@ -1,0 +1,333 @@
+// Many forests in one launch: the batch of tam_batch_create / tam_batch_fill.
+//
+// The reference fills one field set at a time (src/ghosts.jl:1783).  A batch
+// takes the uploaded schedules of several independent forests -- of any
+// sizes and block extents, one element type -- whose field data live at
+// given offsets of one arena, concatenates their groups, pools and block
+// lists into one schedule-shaped set of device arrays with every group
+// tagged with its member, and tiles each stage tag across all members, so
+// that a whole stage of every forest is one copy launch and one stencil
+// launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tam_internal.h"
+#include "treeamr_cuda.h"
+
+struct tam_batch {
+  tam_ctx *ctx = nullptr;
+  int D = 0, dtype = 0;
+  std::vector<tam_sched *> members;
+  std::vector<tam::Member> layout;     // per member
+  std::vector<int64_t> member_points;  // nblocks * prod(S) per member (one variable)
+  bool needs_factors = false;
+  std::vector<tam::DevGroup> groups;
+  std::vector<int32_t> h_tb;
+  std::vector<tam::Stage> stages;
+  tam::LaunchShape shape;
+  tam::DevGroup *d_groups = nullptr;
+  int32_t *d_tb = nullptr, *d_sb = nullptr, *d_srcstart = nullptr, *d_cls = nullptr;
+  void *d_weights = nullptr, *d_wtab = nullptr;
+  tam::Tile *d_tiles = nullptr;
+  tam::Member *d_members = nullptr;
+};
+
+namespace {
+
+int bfail(tam_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+struct Guard {
+  int prev = 0;
+  bool ok = false;
+  explicit Guard(int device) {
+    ok = cudaGetDevice(&prev) == cudaSuccess;
+    if (ok && prev != device) ok = cudaSetDevice(device) == cudaSuccess;
+  }
+  ~Guard() {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+template <typename T>
+cudaError_t up(T **dst, const T *src, size_t n) {
+  *dst = nullptr;
+  const size_t m = std::max<size_t>(n, 1);
+  cudaError_t e = cudaMalloc((void **)dst, m * sizeof(T));
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_batch_device(tam_batch *b) {
+  cudaFree(b->d_groups);
+  cudaFree(b->d_tb);
+  cudaFree(b->d_sb);
+  cudaFree(b->d_srcstart);
+  cudaFree(b->d_cls);
+  cudaFree(b->d_weights);
+  cudaFree(b->d_wtab);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_members);
+  b->d_groups = nullptr;
+  b->d_tb = b->d_sb = b->d_srcstart = b->d_cls = nullptr;
+  b->d_weights = b->d_wtab = nullptr;
+  b->d_tiles = nullptr;
+  b->d_members = nullptr;
+}
+
+// Every stage tag's tiles across all members: per member the transfers by
+// target block, unit copies of every member first, then the stencils.
+std::vector<tam::Tile> batch_tiles(tam_batch *b) {
+  std::vector<tam::Tile> tiles;
+  const int ti = b->shape.tile_items;
+  for (tam::Stage &st : b->stages) {
+    st.tile0 = (int64_t)tiles.size();
+    struct Entry {
+      int32_t member, tblock, group, transfer;
+    };
+    std::vector<Entry> entries;
+    for (int32_t gi : st.groups) {
+      const tam::DevGroup &g = b->groups[gi];
+      for (int64_t t = 0; t < g.ntransfers; ++t)
+        entries.push_back({g.member, b->h_tb[g.first + t], gi, (int32_t)(g.first + t)});
+    }
+    std::stable_sort(entries.begin(), entries.end(), [](const Entry &x, const Entry &y) {
+      if (x.member != y.member) return x.member < y.member;
+      return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
+    });
+    for (int pass = 0; pass < 2; ++pass) {
+      for (const Entry &e : entries) {
+        const tam::DevGroup &g = b->groups[e.group];
+        if ((g.pclass == 0) != (pass == 0)) continue;
+        const int box = g.n[0] * g.n[1] * g.n[2];
+        for (int i0 = 0; i0 < box; i0 += ti)
+          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+      }
+      if (pass == 0) st.ncopy = (int64_t)tiles.size() - st.tile0;
+    }
+    st.ntiles = (int64_t)tiles.size() - st.tile0;
+  }
+  return tiles;
+}
+
+int check_arena(tam_batch *b, int64_t arena_elems, int32_t nvars, const void *factor_arena,
+                int64_t factor_elems) {
+  if (nvars < 1) return bfail(b->ctx, TAM_EINVAL, "batch fill: nvars must be positive");
+  int64_t cols = 1;
+  for (int k = 0; k < b->D; ++k) cols *= 3;
+  for (size_t m = 0; m < b->members.size(); ++m) {
+    const tam::Member &L = b->layout[m];
+    if (L.work_off < 0 || L.work_off + b->member_points[m] * nvars > arena_elems)
+      return bfail(b->ctx, TAM_EINVAL,
+                   "batch fill: member " + std::to_string(m) + " lies outside the arena");
+    if (b->members[m]->needs_factors &&
+        (!factor_arena || L.fac_off < 0 || L.fac_off + cols * nvars > factor_elems))
+      return bfail(b->ctx, TAM_EINVAL,
+                   "batch fill: member " + std::to_string(m) +
+                       " mirrors ghosts and its factor table lies outside the factor arena");
+  }
+  return TAM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
+                     const int64_t *work_offsets, const int64_t *factor_offsets,
+                     tam_batch **out) {
+  if (!ctx || !members || !work_offsets || !out || n < 1)
+    return bfail(ctx, TAM_EINVAL, "tam_batch_create: bad argument");
+  *out = nullptr;
+  const tam_sched *first = members[0];
+  if (!first) return bfail(ctx, TAM_EINVAL, "tam_batch_create: NULL member");
+  for (int32_t m = 0; m < n; ++m) {
+    if (!members[m]) return bfail(ctx, TAM_EINVAL, "tam_batch_create: NULL member");
+    if (members[m]->ctx != ctx)
+      return bfail(ctx, TAM_EINVAL, "tam_batch_create: a member was uploaded by another context");
+    if (members[m]->D != first->D || members[m]->dtype != first->dtype)
+      return bfail(ctx, TAM_EINVAL,
+                   "tam_batch_create: members differ in dimension or element type");
+  }
+  Guard guard(ctx->device);
+  if (!guard.ok) return bfail(ctx, TAM_ECUDA, "cannot make the context's device current");
+  tam_batch *b = new (std::nothrow) tam_batch;
+  if (!b) return bfail(ctx, TAM_ENOMEM, "out of host memory");
+  b->ctx = ctx;
+  b->D = first->D;
+  b->dtype = first->dtype;
+  const size_t esz = b->dtype == TAM_F64 ? 8 : 4;
+  std::vector<int32_t> tb, sb, srcstart, cls;
+  std::vector<unsigned char> weights, wtab;
+  std::map<int32_t, std::vector<int32_t>> bytag;
+  for (int32_t m = 0; m < n; ++m) {
+    tam_sched *s = members[m];
+    b->members.push_back(s);
+    tam::Member L;
+    memset(&L, 0, sizeof L);
+    L.work_off = work_offsets[m];
+    L.fac_off = factor_offsets ? factor_offsets[m] : 0;
+    for (int k = 0; k < 3; ++k) L.S[k] = s->S[k];
+    b->layout.push_back(L);
+    b->member_points.push_back(s->nblocks * (int64_t)s->S[0] * s->S[1] * s->S[2]);
+    b->needs_factors = b->needs_factors || s->needs_factors;
+    const int64_t g0 = (int64_t)b->groups.size(), t0 = (int64_t)tb.size();
+    const int64_t ss0 = (int64_t)srcstart.size(), c0 = (int64_t)cls.size();
+    const int64_t w0 = (int64_t)(weights.size() / esz), wt0 = (int64_t)(wtab.size() / esz);
+    for (const tam::DevGroup &h : s->groups) {
+      tam::DevGroup g = h;
+      for (int k = 0; k < 3; ++k) {
+        g.ss[k] += ss0;
+        g.w[k] += w0;
+        g.cls[k] += c0;
+      }
+      g.wtab += wt0;
+      g.first += t0;
+      g.member = m;
+      b->groups.push_back(g);
+    }
+    for (const tam::Stage &st : s->stages)
+      for (int32_t gi : st.groups) bytag[st.tag].push_back((int32_t)(g0 + gi));
+    tb.insert(tb.end(), s->h_tb.begin(), s->h_tb.end());
+    sb.insert(sb.end(), s->h_sb.begin(), s->h_sb.end());
+    srcstart.insert(srcstart.end(), s->h_pool_srcstart.begin(), s->h_pool_srcstart.end());
+    cls.insert(cls.end(), s->h_pool_cls.begin(), s->h_pool_cls.end());
+    weights.insert(weights.end(), s->h_pool_weights.begin(), s->h_pool_weights.end());
+    // element-aligned: each member's product table starts on an element
+    wtab.resize((wtab.size() + esz - 1) / esz * esz);
+    const int64_t wt0b = (int64_t)(wtab.size() / esz);
+    if (wt0b != wt0) {
+      for (int64_t gi = g0; gi < (int64_t)b->groups.size(); ++gi)
+        b->groups[gi].wtab += wt0b - wt0;
+    }
+    wtab.insert(wtab.end(), s->h_pool_wtab.begin(), s->h_pool_wtab.end());
+  }
+  if (tb.size() > (size_t)INT32_MAX || b->groups.size() > (size_t)INT32_MAX) {
+    delete b;
+    return bfail(ctx, TAM_EUNSUPPORTED, "tam_batch_create: more than 2^31 transfers or groups");
+  }
+  for (auto &kv : bytag) {
+    tam::Stage st;
+    st.tag = kv.first;
+    st.groups = kv.second;
+    b->stages.push_back(st);
+  }
+  b->h_tb = tb;
+  std::vector<tam::Tile> tiles = batch_tiles(b);
+  cudaError_t e;
+  if ((e = up(&b->d_groups, b->groups.data(), b->groups.size())) != cudaSuccess ||
+      (e = up(&b->d_tb, tb.data(), tb.size())) != cudaSuccess ||
+      (e = up(&b->d_sb, sb.data(), sb.size())) != cudaSuccess ||
+      (e = up(&b->d_srcstart, srcstart.data(), srcstart.size())) != cudaSuccess ||
+      (e = up(&b->d_cls, cls.data(), cls.size())) != cudaSuccess ||
+      (e = up((unsigned char **)&b->d_weights, weights.data(), weights.size())) != cudaSuccess ||
+      (e = up((unsigned char **)&b->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
+      (e = up(&b->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
+      (e = up(&b->d_members, b->layout.data(), b->layout.size())) != cudaSuccess) {
+    free_batch_device(b);
+    delete b;
+    return bfail(ctx, e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA,
+                 std::string("tam_batch_create: ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return TAM_OK;
+}
+
+void tam_batch_free(tam_batch *b) {
+  if (!b) return;
+  Guard guard(b->ctx->device);
+  free_batch_device(b);
+  delete b;
+}
+
+int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                   const void *factor_arena, int64_t factor_elems, int32_t first_stage,
+                   int32_t last_stage, void *stream) {
+  if (!b || !arena) return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_fill: NULL argument");
+  int rc = check_arena(b, arena_elems, nvars, factor_arena, factor_elems);
+  if (rc != TAM_OK) return rc;
+  Guard guard(b->ctx->device);
+  if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
+  const tam::SchedArgs args{b->d_groups, b->d_tb,   b->d_sb,          b->d_srcstart, b->d_weights,
+                            b->d_cls,    b->d_wtab, b->shape.int_mul, b->d_members};
+  const int S[3] = {1, 1, 1};  // each member's own, from the member table
+  for (const tam::Stage &st : b->stages) {
+    if (st.tag < first_stage || st.tag > last_stage) continue;
+    cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles + st.tile0, st.ncopy,
+                                            st.ntiles, args, arena, factor_arena, nvars, S,
+                                            b->shape.threads, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b->ctx, TAM_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));
+    }
+  }
+  return TAM_OK;
+}
+
+int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                           const void *factor_arena, int64_t factor_elems, int32_t first_stage,
+                           int32_t last_stage, void *stream) {
+  if (!b || !arena)
+    return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_fill_adjoint: NULL argument");
+  int rc = check_arena(b, arena_elems, nvars, factor_arena, factor_elems);
+  if (rc != TAM_OK) return rc;
+  const size_t esz = b->dtype == TAM_F64 ? 8 : 4;
+  for (size_t m = 0; m < b->members.size(); ++m) {
+    tam_sched *s = b->members[m];
+    unsigned char *y = (unsigned char *)arena + (size_t)b->layout[m].work_off * esz;
+    const unsigned char *f =
+        factor_arena ? (const unsigned char *)factor_arena + (size_t)b->layout[m].fac_off * esz
+                     : nullptr;
+    rc = tam_fill_adjoint(s, y, nvars, s->nblocks, f, first_stage, last_stage, stream);
+    if (rc != TAM_OK) {
+      b->ctx->err = "member " + std::to_string(m) + ": " + s->ctx->err;
+      return rc;
+    }
+  }
+  return TAM_OK;
+}
+
+int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
+  if (!b) return TAM_EINVAL;
+  if (option == TAM_OPT_TILE_ITEMS) {
+    if (value < 16 || value > 4096) return bfail(b->ctx, TAM_EINVAL, "tile items must be in 16..4096");
+    Guard guard(b->ctx->device);
+    const int old = b->shape.tile_items;
+    b->shape.tile_items = (int)value;
+    std::vector<tam::Tile> tiles = batch_tiles(b);
+    tam::Tile *d = nullptr;
+    cudaError_t e = up(&d, tiles.data(), tiles.size());
+    if (e != cudaSuccess) {
+      b->shape.tile_items = old;
+      batch_tiles(b);
+      return bfail(b->ctx, TAM_ECUDA, "re-tiling the batch failed");
+    }
+    cudaDeviceSynchronize();
+    cudaFree(b->d_tiles);
+    b->d_tiles = d;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_THREADS) {
+    if (value < 64 || value > 512 || value % 32)
+      return bfail(b->ctx, TAM_EINVAL, "threads must be a multiple of 32 in 64..512");
+    b->shape.threads = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_INT_MUL) {
+    if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "int_mul is 0 or 1");
+    b->shape.int_mul = (int)value;
+    return TAM_OK;
+  }
+  return bfail(b->ctx, TAM_EINVAL, "unknown option");
+}
+
+}  // extern "C"

@@ -37,6 +37,17 @@ struct DevGroup {
   int32_t shortw;    // every product is normal with a significand of <= 24 bits
   int64_t cls[3];    // class-index pool offsets (one int32 per target row)
   int64_t wtab;      // product-table pool offset
+  int32_t member;    // the forest of a batch this group belongs to (0 alone)
+  int32_t pad3;
+};
+
+// One forest of a batch (tam_batch_fill): where its field data and factor
+// table start in the batch's arenas, in elements, and its stored extents.
+struct Member {
+  int64_t work_off;
+  int64_t fac_off;
+  int32_t S[3];
+  int32_t pad;
 };
 
 // A warp's share of one transfer: box points [item0, item0 + nitems) of
@@ -53,7 +64,8 @@ struct Stage {
   int32_t tag;
   std::vector<int32_t> groups;  // indices into the schedule's groups
   int64_t tile0 = 0;            // first tile in the schedule's tile array
-  int64_t ntiles = 0;
+  int64_t ntiles = 0;           // copy tiles first, then stencil tiles
+  int64_t ncopy = 0;            // the stage's unit-copy tiles
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -111,6 +123,11 @@ struct tam_sched {
   std::vector<int32_t> h_tb;  // target blocks, for re-tiling
   std::vector<int32_t> h_sb;  // source blocks, for the adjoint's lists
   std::vector<int32_t> h_srcstart;
+  // the uploaded pools as the device holds them (with the pad entries)
+  std::vector<int32_t> h_pool_srcstart;
+  std::vector<unsigned char> h_pool_weights;
+  std::vector<int32_t> h_pool_cls;
+  std::vector<unsigned char> h_pool_wtab;
   std::vector<tam::DevGroup> groups;
   std::vector<tam::Stage> stages;
   int64_t ntransfers = 0;
@@ -155,13 +172,14 @@ struct SchedArgs {
   const int32_t *cls;
   const void *wtab;
   int int_mul;
+  const Member *members;  // a batch's member table, or null for one schedule
 };
 
 cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
                                const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], cudaStream_t stream);
 
-cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntiles,
+cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ncopy, int64_t ntiles,
                                const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], int threads, cudaStream_t stream);
 

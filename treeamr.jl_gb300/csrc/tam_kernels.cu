@@ -94,12 +94,13 @@ struct Args {
   const int32_t *__restrict__ cls;
   const T *__restrict__ wtab;
   int int_mul;
+  const Member *__restrict__ members;
 };
 
 template <typename T>
 __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
   return Args<T>{a.groups, a.tb, a.sb, a.srcstart, (const T *)a.weights, a.cls,
-                 (const T *)a.wtab, a.int_mul};
+                 (const T *)a.wtab, a.int_mul, a.members};
 }
 
 struct Geom {
@@ -227,13 +228,33 @@ __device__ __forceinline__ ShortW short_weight(double w) {
   return r;
 }
 
-// A unit copy of every variable: +0 + x (src/ghosts.jl:127-128).
-template <typename T>
-__device__ __forceinline__ void copy_point(const DevGroup &g, const Geom &o, T *work,
-                                           const T *__restrict__ factors, int nvars) {
-  for (int v = 0; v < nvars; ++v) {
-    T x = plus_zero(work[o.soff + v * o.vstride]);
-    work[o.toff + v * o.vstride] = scaled(x, factors, v, nvars, g.factorcol);
+// Within one stage no point is both read and written (targets are ghosts or
+// secondaries, sources points the stage does not write), so the kernels read
+// `work` through `src` and write it through `dst`, both restrict-qualified:
+// the loads of several points and variables can be in flight together.
+
+// Unit copies of every variable of one or two points: +0 + x
+// (src/ghosts.jl:127-128), all loads of a chunk issued before its stores.
+template <typename T, int NP>
+__device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[NP],
+                                            const bool (&on)[NP], const T *__restrict__ src,
+                                            T *__restrict__ dst, const T *__restrict__ factors,
+                                            int nvars) {
+  constexpr int VC = 8;
+  for (int v0 = 0; v0 < nvars; v0 += VC) {
+    T x[NP][VC];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int j = 0; j < VC; ++j)
+        if (on[p] && v0 + j < nvars) x[p][j] = src[o[p].soff + (v0 + j) * o[p].vstride];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int j = 0; j < VC; ++j)
+        if (on[p] && v0 + j < nvars)
+          dst[o[p].toff + (v0 + j) * o[p].vstride] =
+              scaled(plus_zero(x[p][j]), factors, v0 + j, nvars, g.factorcol);
   }
 }
 
@@ -242,7 +263,8 @@ __device__ __forceinline__ void copy_point(const DevGroup &g, const Geom &o, T *
 // VC variables at a time.
 template <typename T, int D, int P, int VC>
 __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, int i3,
-                                            const Geom &o, const Args<T> &a, T *work,
+                                            const Geom &o, const Args<T> &a,
+                                            const T *__restrict__ work, T *__restrict__ dst,
                                             const T *__restrict__ factors, int nvars) {
   using A = Arith<T>;
   constexpr int P2 = D >= 2 ? P : 1;
@@ -296,7 +318,7 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
 #pragma unroll
         for (int j = 0; j < VC; ++j)
           if (v0 + j < nvars)
-            work[o.toff + (v0 + j) * o.vstride] =
+            dst[o.toff + (v0 + j) * o.vstride] =
                 scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
       }
       return;
@@ -324,49 +346,48 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
 #pragma unroll
     for (int j = 0; j < VC; ++j)
       if (v0 + j < nvars)
-        work[o.toff + (v0 + j) * o.vstride] = scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
+        dst[o.toff + (v0 + j) * o.vstride] = scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
   }
 }
 
 // Mixed orders: the reference's nest with the product formed per tap.
 template <typename T, int D>
 __device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2, int i3,
-                                              const Geom &o, const Args<T> &a, T *work,
+                                              const Geom &o, const Args<T> &a,
+                                              const T *__restrict__ work, T *__restrict__ dst,
                                               const T *__restrict__ factors, int nvars) {
   const T *w1 = a.weights + g.w[0] + (int64_t)g.order[0] * i1;
   const T *w2 = a.weights + g.w[1] + (int64_t)g.order[1] * i2;
   const T *w3 = a.weights + g.w[2] + (int64_t)g.order[2] * i3;
   for (int v = 0; v < nvars; ++v) {
     T acc = stencil_sum<T, D, 0>(work + o.soff + v * o.vstride, o.s2, o.s3, w1, w2, w3, g.order);
-    work[o.toff + v * o.vstride] = scaled(acc, factors, v, nvars, g.factorcol);
+    dst[o.toff + v * o.vstride] = scaled(acc, factors, v, nvars, g.factorcol);
   }
 }
 
-// Every variable of one box point of one transfer, by the group's class.
+// Every variable of one box point of one stencil transfer, by the group's class.
 template <typename T, int D>
-__device__ __forceinline__ void do_point(const DevGroup &g, int i1, int i2, int i3,
-                                         int64_t tblock, int64_t sblock, const Args<T> &a,
-                                         T *work, const T *__restrict__ factors, int nvars,
-                                         int S1, int S2, int S3) {
+__device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2, int i3,
+                                              int64_t tblock, int64_t sblock, const Args<T> &a,
+                                              const T *__restrict__ src, T *__restrict__ dst,
+                                              const T *__restrict__ factors, int nvars, int S1,
+                                              int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
   switch (g.pclass) {
-    case 0:
-      copy_point<T>(g, o, work, factors, nvars);
-      break;
     case 2:
-      table_point<T, D, 2, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
+      table_point<T, D, 2, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
       break;
     case 3:
-      table_point<T, D, 3, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
+      table_point<T, D, 3, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
       break;
     case 4:
-      table_point<T, D, 4, 4>(g, i1, i2, i3, o, a, work, factors, nvars);
+      table_point<T, D, 4, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
       break;
     case 6:
-      table_point<T, D, 6, 2>(g, i1, i2, i3, o, a, work, factors, nvars);
+      table_point<T, D, 6, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
       break;
     default:
-      generic_point<T, D>(g, i1, i2, i3, o, a, work, factors, nvars);
+      generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
       break;
   }
 }
@@ -418,27 +439,95 @@ __global__ void __launch_bounds__(256) plain_group_kernel(const DevGroup *__rest
 }
 
 // ---- fused: one launch per stage, one warp per tile ---------------------------
-template <typename T, int D>
-__global__ void __launch_bounds__(512) fused_stage_kernel(const Tile *__restrict__ tiles,
-                                                          int64_t ntiles, Args<T> a, T *work,
-                                                          const T *__restrict__ factors,
-                                                          int nvars, int S1, int S2, int S3) {
+__device__ __forceinline__ void box_point(int item, int n1, int n12, int &i1, int &i2, int &i3) {
+  i3 = item / n12;
+  const int rem = item - i3 * n12;
+  i2 = rem / n1;
+  i1 = rem - i2 * n1;
+}
+
+// The layout a tile works in: the kernel's own for one schedule, or its
+// member's (base offsets and stored extents) in a batch of forests.
+template <typename T, bool BATCH>
+struct TileLayout {
+  const T *src;
+  T *dst;
+  const T *factors;
+  int S1, S2, S3;
+  __device__ __forceinline__ TileLayout(const DevGroup &g, const Args<T> &a,
+                                        const T *__restrict__ s, T *__restrict__ d,
+                                        const T *__restrict__ f, int s1, int s2, int s3)
+      : src(s), dst(d), factors(f), S1(s1), S2(s2), S3(s3) {
+    if (BATCH) {
+      const Member &m = a.members[g.member];
+      src += m.work_off;
+      dst += m.work_off;
+      factors += m.fac_off;
+      S1 = m.S[0];
+      S2 = m.S[1];
+      S3 = m.S[2];
+    }
+  }
+};
+
+// The unit-copy tiles of a stage: a light kernel, every variable's load of a
+// point in flight together, and the next tile's descriptor fetched while this
+// one runs.
+template <typename T, int D, bool BATCH>
+__global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict__ tiles,
+                                                         int64_t ntiles, Args<T> a,
+                                                         const T *__restrict__ src,
+                                                         T *__restrict__ dst,
+                                                         const T *__restrict__ factors,
+                                                         int nvars, int S1, int S2, int S3) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
-       w += warps) {
-    const Tile tile = tiles[w];
+  int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  Tile next = w < ntiles ? tiles[w] : Tile{0, 0, 0, 0};
+  for (; w < ntiles; w += warps) {
+    const Tile tile = next;
+    if (w + warps < ntiles) next = tiles[w + warps];
     const DevGroup &g = a.groups[tile.group];
+    const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
     const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
     const int64_t sblock = __ldg(a.sb + tile.transfer) - 1;
     const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
     for (int k = lane; k < tile.nitems; k += 32) {
-      const int item = tile.item0 + k;
-      const int i3 = item / n12;
-      const int rem = item - i3 * n12;
-      const int i2 = rem / n1;
-      const int i1 = rem - i2 * n1;
-      do_point<T, D>(g, i1, i2, i3, tblock, sblock, a, work, factors, nvars, S1, S2, S3);
+      Geom o[1];
+      const bool on[1] = {true};
+      int i1, i2, i3;
+      box_point(tile.item0 + k, n1, n12, i1, i2, i3);
+      o[0] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
+      copy_points<T, 1>(g, o, on, L.src, L.dst, L.factors, nvars);
+    }
+  }
+}
+
+// The stencil tiles of a stage: one point a lane, every variable.
+template <typename T, int D, bool BATCH>
+__global__ void __launch_bounds__(512) fused_stage_kernel(const Tile *__restrict__ tiles,
+                                                          int64_t ntiles, Args<T> a,
+                                                          const T *__restrict__ src,
+                                                          T *__restrict__ dst,
+                                                          const T *__restrict__ factors,
+                                                          int nvars, int S1, int S2, int S3) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  Tile next = w < ntiles ? tiles[w] : Tile{0, 0, 0, 0};
+  for (; w < ntiles; w += warps) {
+    const Tile tile = next;
+    if (w + warps < ntiles) next = tiles[w + warps];
+    const DevGroup &g = a.groups[tile.group];
+    const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
+    const int64_t sblock = __ldg(a.sb + tile.transfer) - 1;
+    const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
+    for (int k = lane; k < tile.nitems; k += 32) {
+      int i1, i2, i3;
+      box_point(tile.item0 + k, n1, n12, i1, i2, i3);
+      stencil_point<T, D>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars, L.S1,
+                          L.S2, L.S3);
     }
   }
 }
@@ -469,26 +558,49 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ntiles, const Args<T> &a, T *work,
-                           const T *factors, int nvars, const int S[3], int threads,
-                           cudaStream_t stream) {
-  if (ntiles == 0) return cudaSuccess;
+template <typename T, int D>
+void launch_both(const Tile *tiles, int64_t ncopy, int64_t ntiles, const Args<T> &a, T *work,
+                 const T *factors, int nvars, const int S[3], int threads, cudaStream_t stream) {
   const int wpb = threads / 32;
-  int64_t blocks = (ntiles + wpb - 1) / wpb;
-  if (blocks > (int64_t)1 << 30) blocks = (int64_t)1 << 30;
+  const bool batch = a.members != nullptr;
+  if (ncopy > 0) {
+    const int64_t blocks = std::min<int64_t>((ncopy + wpb - 1) / wpb, (int64_t)1 << 30);
+    if (batch)
+      fused_copy_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles, ncopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+    else
+      fused_copy_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles, ncopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  }
+  const int64_t nst = ntiles - ncopy;
+  if (nst > 0) {
+    const int64_t blocks = std::min<int64_t>((nst + wpb - 1) / wpb, (int64_t)1 << 30);
+    if (batch)
+      fused_stage_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles + ncopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+    else
+      fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles + ncopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  }
+}
+
+// A stage: its unit copies and its stencils, two launches with no
+// dependency between them (their targets are disjoint and neither reads a
+// point of the stage's targets).
+template <typename T>
+cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ncopy, int64_t ntiles,
+                           const Args<T> &a, T *work, const T *factors, int nvars, const int S[3],
+                           int threads, cudaStream_t stream) {
+  if (ntiles == 0) return cudaSuccess;
   switch (D) {
     case 1:
-      fused_stage_kernel<T, 1><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
+      launch_both<T, 1>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
       break;
     case 2:
-      fused_stage_kernel<T, 2><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
+      launch_both<T, 2>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
       break;
     default:
-      fused_stage_kernel<T, 3><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ntiles, a, work, factors, nvars, S[0], S[1], S[2]);
+      launch_both<T, 3>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
       break;
   }
   return cudaGetLastError();
@@ -506,13 +618,14 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
                                nvars, S, stream);
 }
 
-cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ntiles,
-                               const SchedArgs &a, void *work, const void *factors, int nvars,
-                               const int S[3], int threads, cudaStream_t stream) {
+cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ncopy,
+                               int64_t ntiles, const SchedArgs &a, void *work,
+                               const void *factors, int nvars, const int S[3], int threads,
+                               cudaStream_t stream) {
   if (dtype == TAM_F64)
-    return fused_dispatch<double>(D, tiles, ntiles, typed<double>(a), (double *)work,
+    return fused_dispatch<double>(D, tiles, ncopy, ntiles, typed<double>(a), (double *)work,
                                   (const double *)factors, nvars, S, threads, stream);
-  return fused_dispatch<float>(D, tiles, ntiles, typed<float>(a), (float *)work,
+  return fused_dispatch<float>(D, tiles, ncopy, ntiles, typed<float>(a), (float *)work,
                                (const float *)factors, nvars, S, threads, stream);
 }
 

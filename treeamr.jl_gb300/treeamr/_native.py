@@ -30,7 +30,7 @@ TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu"]
+SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu"]
 
 
 class tam_stencil(C.Structure):
@@ -212,6 +212,17 @@ def _declare(lib: C.CDLL):
     lib.tam_adjoint_scratch_bytes.restype = C.c_int
     lib.tam_fill_adjoint_scratch.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp, C.c_size_t, vp]
     lib.tam_fill_adjoint_scratch.restype = C.c_int
+    lib.tam_batch_create.argtypes = [vp, C.POINTER(vp), i32, C.POINTER(i64), C.POINTER(i64),
+                                     C.POINTER(vp)]
+    lib.tam_batch_create.restype = C.c_int
+    lib.tam_batch_free.argtypes = [vp]
+    lib.tam_batch_free.restype = None
+    for name in ("tam_batch_fill", "tam_batch_fill_adjoint"):
+        f = getattr(lib, name)
+        f.argtypes = [vp, vp, i64, i32, vp, i64, i32, i32, vp]
+        f.restype = C.c_int
+    lib.tam_batch_set_option.argtypes = [vp, i32, i64]
+    lib.tam_batch_set_option.restype = C.c_int
     lib.tam_schedule_set_option.argtypes = [vp, i32, i64]
     lib.tam_schedule_get_option.argtypes = [vp, i32, C.POINTER(i64)]
     for name in ("tam_init", "tam_last_error", "tam_schedule_upload", "tam_schedule_info",

@@ -139,6 +139,65 @@ def walls_setup(device="cpu", T=np.float64, roots=8, N=32, levels=5, G=2):
     return f, fs, ops
 
 
+def forest_batch_specs(n: int = 64, seed: int = 4, max_roots: int = 6, max_levels: int = 4):
+    """The uneven batch: ``n`` forests with roots per side drawn from
+    {2,...,6}^3, N from {8, 16} and 1-4 refinement levels around two seeded
+    points each (cell-centred, periodic)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        roots = tuple(int(x) for x in rng.integers(2, max_roots + 1, size=3))
+        N = int(rng.choice([8, 16]))
+        levels = int(rng.integers(1, max_levels + 1))
+        pts = [tuple(float(rng.uniform(0, r)) for r in roots) for _ in range(2)]
+        specs.append((roots, N, levels, pts))
+    return specs
+
+
+def batch_forest(roots, N, levels, pts) -> Forest:
+    f = Forest(roots, N=N, periodic=(True,) * 3, extents=tuple((0.0, float(r)) for r in roots))
+
+    def near(ext):
+        w = ext[0][1] - ext[0][0]
+        return any(all(a - w <= p[d] <= b + w for d, (a, b) in enumerate(ext)) for p in pts)
+    return refine_where(f, near, range(levels))
+
+
+def forest_batch_setup(n: int = 64, seed: int = 4, T=np.float32, device="cuda", G: int = 2,
+                       max_roots: int = 6, max_levels: int = 4):
+    """The fields sets, schedules and batch of the uneven multi-forest
+    workload: 2 variables (u, v), G = 2, PV(4,4)."""
+    from .batch import ForestBatch
+    from .schedule import GhostSchedule
+    ops = Operators(prolongation=4, restriction=4)
+    fss, scheds = [], []
+    for roots, N, levels, pts in forest_batch_specs(n, seed, max_roots, max_levels):
+        f = batch_forest(roots, N, levels, pts)
+        fs = FieldSet(f, 2, G=G, T=T)
+        fss.append(fs)
+        scheds.append(GhostSchedule(fs, ops))
+    return fss, scheds, ForestBatch(fss, scheds, device=device)
+
+
+def wave_initial(batch, seed: int = 5):
+    """A smooth pulse in u and zero v, per forest, plus small seeded noise."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    for fs in batch.fieldsets:
+        f = fs.forest
+        ext = f.extents
+        centre = [(a + b) / 2 for a, b in ext]
+        host = np.zeros(tuple(fs.work.shape), dtype=fs.T)
+        for b in range(fs.nblocks()):
+            pos = fs.positions(b)
+            X = np.meshgrid(*pos, indexing="ij")
+            r2 = sum((X[d] - centre[d]) ** 2 for d in range(3))
+            host[b, 0] = np.exp(-r2 / 0.5).astype(fs.T).transpose()
+        noise = torch.empty(host.shape, dtype=torch.float64).uniform_(-1e-3, 1e-3, generator=g)
+        fs.work.copy_(torch.from_numpy(host) + noise.to(fs.work.dtype))
+    return batch
+
+
 WORKLOADS = {
     "quadrant": dict(desc="2-D 4x4 periodic roots, N=8, G=2, cell, 1 var F64, 25% of roots "
                           "refined once, PV(4,4)"),

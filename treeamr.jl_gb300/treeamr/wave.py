@@ -1,0 +1,176 @@
+"""RK4 for the wave equation over a batch of forests, forward and adjoint.
+
+The reference's wave test (``test/wave.jl:49-110,178-200``) advances
+``u_t = v, v_t = lap(u)`` with classical RK4, each stage a ghost fill and the
+7-point Laplacian on owned points.  ``WaveSolver`` does that for every forest
+of a ``ForestBatch`` at once:
+
+* every stage is one batched fill (``tam_batch_fill``) and one batched
+  right-hand side (``tam_wave_rhs``), and a whole step can be captured in a
+  CUDA graph and replayed;
+* the backward pass is the discrete adjoint of the same steps, each stage's
+  transpose being the right-hand side's transpose and then the fill's
+  (``tam_batch_fill_adjoint``).  The dynamics are linear, so states are needed
+  only for a loss that reads every step; they are recomputed from
+  checkpoints every ``checkpoint`` steps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _native
+from .batch import ForestBatch
+
+_WAVE_BLOCK = np.dtype([("off", np.int64), ("S", np.int32, (3,)), ("G", np.int32),
+                        ("N", np.int32), ("pad", np.int32), ("inv_h2", np.float64)])
+assert _WAVE_BLOCK.itemsize == 40
+
+
+class WaveSolver:
+    """The state is the batch's arena layout with variables (u, v)."""
+
+    def __init__(self, batch: ForestBatch, dt: Optional[float] = None, cfl: float = 0.25):
+        if batch.nvars != 2 or batch.D != 3:
+            raise ValueError("the wave solver needs 3-D field sets with two variables (u, v)")
+        rows = []
+        hmin = np.inf
+        for m, fs in enumerate(batch.fieldsets):
+            if any(cd != 0 for cd in fs.c) or min(fs.G) < 1:
+                raise ValueError("the wave right-hand side is for cell-centred sets with G >= 1")
+            f = fs.forest
+            S = fs.stored
+            per_block = fs.nvars * S[0] * S[1] * S[2]
+            for b, k in enumerate(f.leaves):
+                h = float(f.spacing(k.level, np.float64))
+                hmin = min(hmin, h)
+                rows.append((batch.offsets[m] + b * per_block, S, fs.G[0], f.N, 0, 1.0 / (h * h)))
+        table = np.zeros(len(rows), dtype=_WAVE_BLOCK)
+        for i, r in enumerate(rows):
+            table[i] = r
+        self.nblocks = len(rows)
+        self.max_points = int(max(np.prod(fs.stored) for fs in batch.fieldsets))
+        self.table = torch.from_numpy(table.view(np.uint8).copy()).to(batch.device)
+        self.batch = batch
+        self.lib = _native.lib()
+        self.lib.tam_wave_rhs.argtypes = [C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
+                                          C.c_void_p, C.c_int32, C.c_void_p]
+        self.lib.tam_wave_rhs.restype = C.c_int
+        self.dtype_code = _native.TAM_F64 if batch.T == np.float64 else _native.TAM_F32
+        self.dt = float(dt) if dt is not None else cfl * hmin
+        like = batch.arena
+        self.k = [torch.zeros_like(like) for _ in range(4)]
+        self.tmp = torch.zeros_like(like)
+        self.adj = [torch.zeros_like(like) for _ in range(3)]
+
+    # -- the pieces ------------------------------------------------------------
+    def rhs(self, x: torch.Tensor, out: torch.Tensor, adjoint: bool = False):
+        s = torch.cuda.current_stream(x.device)
+        rc = self.lib.tam_wave_rhs(self.dtype_code, C.c_void_p(self.table.data_ptr()),
+                                   self.nblocks, self.max_points, C.c_void_p(x.data_ptr()),
+                                   C.c_void_p(out.data_ptr()), 1 if adjoint else 0,
+                                   C.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise _native.TamError(f"tam_wave_rhs failed ({rc})")
+        return out
+
+    def F(self, x: torch.Tensor, out: torch.Tensor):
+        """``out = R(A x)``; ``x``'s ghosts are filled in place."""
+        self.batch.fill(x)
+        return self.rhs(x, out)
+
+    def FT(self, kbar: torch.Tensor, out: torch.Tensor):
+        """``out = A^T R^T kbar``."""
+        self.rhs(kbar, out, adjoint=True)
+        self.batch.fill_adjoint(out)
+        return out
+
+    # -- forward ---------------------------------------------------------------
+    def step(self, y: torch.Tensor):
+        """One RK4 step of ``y`` in place."""
+        dt, k, t = self.dt, self.k, self.tmp
+        self.F(y, k[0])
+        t.copy_(y).add_(k[0], alpha=dt / 2)
+        self.F(t, k[1])
+        t.copy_(y).add_(k[1], alpha=dt / 2)
+        self.F(t, k[2])
+        t.copy_(y).add_(k[2], alpha=dt)
+        self.F(t, k[3])
+        y.add_(k[0], alpha=dt / 6).add_(k[1], alpha=dt / 3).add_(k[2], alpha=dt / 3) \
+         .add_(k[3], alpha=dt / 6)
+        return y
+
+    def capture(self, y: torch.Tensor, steps: int = 1) -> torch.cuda.CUDAGraph:
+        """A CUDA graph of ``steps`` RK4 steps of ``y`` (warmed up first: the
+        fills and right-hand sides allocate nothing)."""
+        side = torch.cuda.Stream(device=y.device)
+        side.wait_stream(torch.cuda.current_stream(y.device))
+        with torch.cuda.stream(side):
+            probe = y.clone()
+            self.step(probe)
+        torch.cuda.current_stream(y.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(steps):
+                self.step(y)
+        return g
+
+    # -- the adjoint -------------------------------------------------------------
+    #
+    # One step as the forward runs it, with P the fill (applied in place) and
+    # R the right-hand side:  z = P y;  k1 = R z;  x2 = z + dt/2 k1, k2 = R P x2;
+    # x3 = z + dt/2 k2, k3 = R P x3;  x4 = z + dt k3, k4 = R P x4;
+    # y' = z + dt/6 k1 + dt/3 k2 + dt/3 k3 + dt/6 k4.  Its transpose, from g = y'bar:
+    # zbar = g; each k_ibar starts at its weight times g; x4bar = P^T R^T k4bar
+    # adds to zbar and (times dt) to k3bar; x3bar and x2bar likewise (times
+    # dt/2) to k2bar and k1bar; R^T k1bar adds to zbar; ybar = P^T zbar.
+    def step_adjoint(self, ybar: torch.Tensor):
+        """``ybar <- M^T ybar`` for one RK4 step ``M``, in place."""
+        dt = self.dt
+        g, kb, xb = self.adj
+        g.copy_(ybar)
+        kb.copy_(g).mul_(dt / 6)
+        self.FT(kb, xb)
+        ybar.add_(xb)
+        kb.copy_(g).mul_(dt / 3).add_(xb, alpha=dt)
+        self.FT(kb, xb)
+        ybar.add_(xb)
+        kb.copy_(g).mul_(dt / 3).add_(xb, alpha=dt / 2)
+        self.FT(kb, xb)
+        ybar.add_(xb)
+        kb.copy_(g).mul_(dt / 6).add_(xb, alpha=dt / 2)
+        self.rhs(kb, xb, adjoint=True)
+        ybar.add_(xb)
+        self.batch.fill_adjoint(ybar)
+        return ybar
+
+    def run(self, y: torch.Tensor, steps: int, checkpoint: int = 0):
+        """``steps`` forward steps of ``y`` in place; with ``checkpoint`` > 0, the
+        states at every ``checkpoint``-th step (from step 0) are kept."""
+        saved = {}
+        for n in range(steps):
+            if checkpoint and n % checkpoint == 0:
+                saved[n] = y.clone()
+            self.step(y)
+        return saved
+
+    def gradient(self, y0: torch.Tensor, steps: int, dloss: Callable, checkpoint: int = 2):
+        """The gradient with respect to ``y0`` of ``L = sum_n l(y_n)``, n = 1..steps,
+        given ``dloss(y) = dl/dy``: the states are recomputed from checkpoints
+        every ``checkpoint`` steps during the backward sweep."""
+        y = y0.clone()
+        saved = self.run(y, steps, checkpoint)
+        ybar = torch.zeros_like(y0)
+        cur, cur_n = None, None
+        for n in range(steps, 0, -1):
+            # y_n: from the latest checkpoint at or below n-1, stepped forward
+            c = ((n - 1) // checkpoint) * checkpoint
+            cur = saved[c].clone()
+            for _ in range(n - c):
+                self.step(cur)
+            ybar.add_(dloss(cur))
+            self.step_adjoint(ybar)
+        return ybar
