@@ -60,6 +60,63 @@ def parse():
     return ap.parse_args()
 
 
+def measure_batch(dev, timed, args, peak):
+    """The uneven batch: 64 independent periodic cell-centred forests (roots per
+    side from {2..6}^3, N from {8, 16}, 1-4 levels around seeded points), G=2,
+    2 Float32 variables (u, v), PV(4,4).  The batched fill (one launch per stage
+    for all forests) against 64 separate fills; 10 RK4 steps of the wave
+    equation replayed from one CUDA graph against the same steps launched
+    eagerly; and the adjoint sweep through the 10 steps with checkpoints every
+    2 steps."""
+    import torch
+    from treeamr import fill_ghosts, meshes
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = meshes.forest_batch_setup(device=dev)
+    g = torch.Generator(device=dev).manual_seed(9)
+    batch.arena.uniform_(-1.0, 1.0, generator=g)
+    esize = 4
+    bytes_per_fill = 2 * batch.ghost_points() * esize
+    for _ in range(args.warmup):
+        batch.fill()
+    steps = max(3, args.steps // 2)
+    ms = timed(batch.fill, steps)
+
+    def separate():
+        for fs, s in zip(fss, scheds):
+            fill_ghosts(fs, s)
+    separate()
+    ms_sep = timed(separate, max(2, steps // 2))
+    solver = WaveSolver(batch)
+    y = batch.arena
+    y.mul_(1e-3)
+    eager_ms = timed(lambda: [solver.step(y) for _ in range(10)], 1)
+    graph = solver.capture(y, steps=10)
+    graph.replay()
+    graph_ms = timed(graph.replay, 2)
+    y0 = y.clone()
+    w = torch.rand(y.shape, dtype=y.dtype, device=dev, generator=g)
+    solver.gradient(y0, 2, lambda v: 2 * w * v, checkpoint=2)      # prepares the adjoints
+    bwd_ms = timed(lambda: solver.gradient(y0, 10, lambda v: 2 * w * v, checkpoint=2), 1)
+    out = {
+        "workload": "batch64: 64 periodic cell-centred forests, roots per side from {2..6}^3, "
+                    "N from {8,16}, 1-4 levels, G=2, 2 vars F32 (u, v), PV(4,4)",
+        "dtype": "float32", "forests": len(fss),
+        "blocks": sum(fs.forest.nleaves() for fs in fss),
+        "field_bytes": batch.arena.numel() * esize,
+        "value": bytes_per_fill / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_fill": ms,
+        "separate_fills": {"ms_per_fill": ms_sep, "speedup_batched": ms_sep / ms},
+        "rk4_10_steps": {"graph_ms": graph_ms, "eager_ms": eager_ms,
+                         "fills": 40, "dt": solver.dt},
+        "adjoint_10_steps_checkpoint_2_ms": bwd_ms,
+        "roofline": {"bound": "hbm", "achieved": bytes_per_fill / (ms * 1e-3) / 1e9,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": bytes_per_fill / (ms * 1e-3) / 1e9 / peak},
+    }
+    del graph, solver, batch
+    torch.cuda.empty_cache()
+    return out
+
+
 def measure_walls(T, dev, timed, args, peak):
     """The walls mesh: 3-D vertex-centred, 8^3 roots over the unit cube, N=32, G=2,
     low faces reflecting and high faces outflow, five levels nested around two
@@ -356,6 +413,7 @@ def main():
     if not args.no_walls:
         for T in (np.float32, np.float64):
             walls["walls_" + np.dtype(T).name] = measure_walls(T, dev, timed, args, peak)
+        walls["batch64_float32"] = measure_batch(dev, timed, args, peak)
 
     # end to end through the public call, host buffers, copies inside the timing
     e2e = None

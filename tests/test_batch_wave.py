@@ -139,7 +139,10 @@ def test_wave_gradient_checkpointed(cuda_lib):
     G, N = fs.G[0], fs.forest.N
     view = batch.member_view(torch.arange(y0.numel(), device="cuda"), 0)
     idx = view[:, :, G:G + N, G:G + N, G:G + N].reshape(-1)
-    h = 1e-6
+    # L is exactly quadratic in y0 (linear dynamics), so central differences
+    # have no truncation error at any h; h = 1e-3 keeps the cancellation
+    # error of a ~1e10 sum below 1e-6 of the gradient
+    h = 1e-3
     for k in rng.choice(idx.cpu().numpy(), size=8, replace=False):
         yp = y0.clone()
         ym = y0.clone()
