@@ -241,6 +241,13 @@ int tam_wave_rhs(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
 #define TAM_OPT_THREADS 2    /* threads per CTA, 64..512, a multiple of 32    */
 #define TAM_OPT_INT_MUL 3    /* 1: Float64 short-weight multiplies on the     */
                              /* integer pipe (see tam_selftest), 0: FP64 pipe  */
+/* The form of the stencil sum (src/ghosts.jl:28-56): 1 (the default) is the
+ * reference's CPU form, a dimension whose weight column has one nonzero
+ * weight takes that one tap; 0 is its device form, every tap.  The two give
+ * the same bits for finite data; they differ only where a NaN or an infinity
+ * sits under a zero weight, which the full sum carries into the result.
+ * tam_fill_plain always takes the device form. */
+#define TAM_OPT_ONE_TAP 4
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 

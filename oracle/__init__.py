@@ -56,7 +56,7 @@ def lib():
         build()
         l = C.CDLL(LIB_PATH)
         l.oracle_fill.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
-                                  C.c_int32, C.c_int]
+                                  C.c_int32, C.c_int, C.c_int]
         l.oracle_fill.restype = C.c_int
         l.oracle_fill_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                           C.c_int32, C.c_int32]
@@ -78,13 +78,19 @@ ALL_FIRST, ALL_LAST = -1, 0x7FFFFFFF
 
 
 def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
-         last=ALL_LAST, nthreads: int = 1) -> np.ndarray:
-    """In place on ``work`` (shape (nblocks, nvars, S_D..S_1), C order)."""
+         last=ALL_LAST, nthreads: int = 1, one_tap: bool = True) -> np.ndarray:
+    """In place on ``work`` (shape (nblocks, nvars, S_D..S_1), C order).
+
+    ``one_tap`` picks the form of the stencil sum (src/ghosts.jl:28-56): the
+    reference's CPU form, where a dimension whose weight column has a single
+    nonzero weight takes only that tap, or (False) its device form, the full
+    sum.  They differ only where a NaN or an infinity sits under a zero
+    weight."""
     assert work.flags.c_contiguous and work.dtype == np.dtype(schedule.T)
     d = _descriptor(schedule)
     f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=work.dtype)
     rc = lib().oracle_fill(C.addressof(d.desc), work.ctypes.data, nvars, f.ctypes.data, first,
-                           last, nthreads)
+                           last, nthreads, 1 if one_tap else 0)
     if rc != 0:
         raise RuntimeError("oracle_fill failed")
     return work
@@ -102,13 +108,16 @@ def fill_adjoint(schedule, y: np.ndarray, nvars: int, factors: np.ndarray, *, fi
     return y
 
 
-def fill_fieldset(fs, schedule, *, boundary_values=None, nthreads: int = 1) -> np.ndarray:
+def fill_fieldset(fs, schedule, *, boundary_values=None, nthreads: int = 1,
+                  one_tap: bool = True) -> np.ndarray:
     """The oracle's fill of a field set's current contents, returned as a new
     host array; ``boundary_values(host, fs, regions)`` fills the outer-face
     regions between phase 1 and the prolongations."""
     host = fs.work.detach().cpu().numpy().copy()
     if boundary_values is None or not schedule.boundaries:
-        return fill(schedule, host, fs.nvars, fs.factors_host, nthreads=nthreads)
-    fill(schedule, host, fs.nvars, fs.factors_host, last=1, nthreads=nthreads)
+        return fill(schedule, host, fs.nvars, fs.factors_host, nthreads=nthreads,
+                    one_tap=one_tap)
+    fill(schedule, host, fs.nvars, fs.factors_host, last=1, nthreads=nthreads, one_tap=one_tap)
     boundary_values(host, fs, schedule.boundaries)
-    return fill(schedule, host, fs.nvars, fs.factors_host, first=2, nthreads=nthreads)
+    return fill(schedule, host, fs.nvars, fs.factors_host, first=2, nthreads=nthreads,
+                one_tap=one_tap)

@@ -12,7 +12,11 @@
  * What it restates, over a schedule already flattened into the
  * tam_schedule_desc arrays (include/treeamr_cuda.h):
  *   - stencil_sum            src/ghosts.jl:75-118  (m_1 innermost, weight
- *                            product ((w_1*w_2)*w_3), acc from +0, no FMA)
+ *                            product ((w_1*w_2)*w_3), acc from +0, no FMA),
+ *                            in both of its forms (src/ghosts.jl:28-56): the
+ *                            CPU's, where a dimension whose weight column has
+ *                            a single nonzero weight (src/schedule.jl:83-86)
+ *                            takes that one tap, and the device's full sum
  *   - copy_load              src/ghosts.jl:127-128 (+0 + x)
  *   - scaled                 src/ghosts.jl:369-370 (x*f + 0)
  *   - transfer_kernel!       src/ghosts.jl:372-402
@@ -60,7 +64,7 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
 #define DEFINE_ORACLE(T, SUFFIX)                                                                \
   static void run_transfers_##SUFFIX(const tam_schedule_desc *d, const tam_group *g,            \
                                      int64_t t0, int64_t t1, T *work, int32_t nvars,           \
-                                     const T *factors) {                                        \
+                                     const T *factors, int one_tap) {                           \
     const int D = d->ndim;                                                                      \
     int n[3] = {1, 1, 1}, o[3] = {1, 1, 1}, tf[3] = {0, 0, 0};                                  \
     int64_t S[3] = {1, 1, 1};                                                                   \
@@ -85,18 +89,30 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
               int idx[3] = {i1, i2, i3};                                                        \
               int64_t base[3] = {0, 0, 0};                                                      \
               const T *wc[3] = {0, 0, 0};                                                       \
+              int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};                                         \
               for (int k = 0; k < D; ++k) {                                                     \
                 base[k] = d->srcstart[g->stencil[k].srcstart + idx[k]] - 1;                     \
                 wc[k] = W + g->stencil[k].weights + (int64_t)o[k] * idx[k];                     \
+                hi[k] = o[k];                                                                   \
+                int nonzero = 0, row = 0;                                                       \
+                for (int m = 0; m < o[k]; ++m)                                                  \
+                  if (wc[k][m] != (T)0) {                                                       \
+                    ++nonzero;                                                                  \
+                    row = m;                                                                    \
+                  }                                                                             \
+                if (one_tap && nonzero == 1) {                                                  \
+                  lo[k] = row;                                                                  \
+                  hi[k] = row + 1;                                                              \
+                }                                                                               \
               }                                                                                 \
               const T *src = work + sb * bs + v * vs + base[0] + base[1] * s2 + base[2] * s3;   \
               T acc = (T)0;                                                                     \
               if (unit) {                                                                       \
                 acc = (T)0 + src[0];                                                            \
               } else {                                                                          \
-                for (int m3 = 0; m3 < o[2]; ++m3)                                               \
-                  for (int m2 = 0; m2 < o[1]; ++m2)                                             \
-                    for (int m1 = 0; m1 < o[0]; ++m1) {                                         \
+                for (int m3 = lo[2]; m3 < hi[2]; ++m3)                                          \
+                  for (int m2 = lo[1]; m2 < hi[1]; ++m2)                                        \
+                    for (int m1 = lo[0]; m1 < hi[0]; ++m1) {                                    \
                       T wp = wc[0][m1];                                                         \
                       if (D >= 2) wp = wp * wc[1][m2];                                          \
                       if (D >= 3) wp = wp * wc[2][m3];                                          \
@@ -116,7 +132,8 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
   }                                                                                             \
                                                                                                 \
   static void run_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *work,             \
-                                 int32_t nvars, const T *factors, int nthreads) {               \
+                                 int32_t nvars, const T *factors, int nthreads,                 \
+                                 int one_tap) {                                                 \
     _Pragma("omp parallel num_threads(nthreads)") {                                             \
       int c = 0, k = 1;                                                                         \
       ORACLE_THREAD_IDS(c, k);                                                                  \
@@ -128,7 +145,7 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
         const int32_t *owners = d->targetblocks + g->first;                                     \
         int64_t a = lower_bound(owners, 0, g->ntransfers, lo + 1);                              \
         int64_t b = lower_bound(owners, 0, g->ntransfers, hi + 1);                              \
-        if (a < b) run_transfers_##SUFFIX(d, g, a, b, work, nvars, factors);                    \
+        if (a < b) run_transfers_##SUFFIX(d, g, a, b, work, nvars, factors, one_tap);           \
       }                                                                                         \
     }                                                                                           \
   }
@@ -166,9 +183,10 @@ static int collect_tags(const tam_schedule_desc *d, int32_t *tags, int cap) {
   return n;
 }
 
-/* The serial-forest fill: every stage tag in [first, last], in order. */
+/* The serial-forest fill: every stage tag in [first, last], in order.
+ * one_tap = 1: the CPU form of the sum, 0: the device form. */
 int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const void *factors,
-                int32_t first, int32_t last, int nthreads) {
+                int32_t first, int32_t last, int nthreads, int one_tap) {
   if (!d || !work || nvars < 1) return -1;
   if (nthreads < 1) nthreads = 1;
   int32_t tags[128];
@@ -176,9 +194,11 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
   for (int i = 0; i < nt; ++i) {
     if (tags[i] < first || tags[i] > last) continue;
     if (d->dtype == TAM_F64)
-      run_stage_f64(d, tags[i], (double *)work, nvars, (const double *)factors, nthreads);
+      run_stage_f64(d, tags[i], (double *)work, nvars, (const double *)factors, nthreads,
+                    one_tap);
     else
-      run_stage_f32(d, tags[i], (float *)work, nvars, (const float *)factors, nthreads);
+      run_stage_f32(d, tags[i], (float *)work, nvars, (const float *)factors, nthreads,
+                    one_tap);
   }
   return 0;
 }

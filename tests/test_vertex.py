@@ -167,7 +167,9 @@ def test_gpu_vertex_walls_bit_exact(cuda_lib, method, D, T):
     s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
     host = awkward_fill(tuple(fs.work.shape), T, seed=D)
     fs.work.copy_(torch.from_numpy(host))
-    expect = oracle.fill_fieldset(fs, s)
+    # NaNs and infinities under zero weights: the fused kernels take the
+    # reference's CPU form of the sum, the plain kernel its device form
+    expect = oracle.fill_fieldset(fs, s, one_tap=method == "fused")
     got = _gpu_fill(fs, s, host, method)
     assert np.array_equal(nanbits(got), nanbits(expect))
 
@@ -185,3 +187,58 @@ def test_gpu_vertex_nested_bit_exact(cuda_lib, D, periodic):
     expect = oracle.fill_fieldset(fs, s)
     got = _gpu_fill(fs, s, host, "fused")
     assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+# --- the two forms of the stencil sum ----------------------------------------
+
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_one_tap_form_equals_full_sum_on_finite_data(D, T):
+    """The reference's CPU form (one tap along a dimension whose column has a
+    single nonzero weight) and its device form (every tap) give the same bits
+    for finite data, ±0 and subnormals included (src/ghosts.jl:46-56); they
+    part only where a NaN or an infinity sits under a zero weight."""
+    f = _walls_forest(D)
+    par = [(EvenParity,) * D, tuple(OddParity if d == 0 else EvenParity for d in range(D))]
+    fs = FieldSet(f, len(par), G=2, centering=vertexcentered(D), parity=par, T=T)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    host = awkward_fill(tuple(fs.work.shape), T, seed=5 + D)
+    finite = np.where(np.isfinite(host), host, T(0.25)).astype(T)
+    fs.work.copy_(torch.from_numpy(finite))
+    skip = oracle.fill_fieldset(fs, s, one_tap=True)
+    full = oracle.fill_fieldset(fs, s, one_tap=False)
+    assert np.array_equal(skip.view(np.uint8), full.view(np.uint8))
+    # a vertex prolongation has columns with one nonzero weight
+    singles = [st for g in s.all_groups() for st in g.stencils
+               if st.order > 1 and any(np.count_nonzero(st.weights[:, i]) == 1
+                                       for i in range(st.weights.shape[1]))]
+    assert singles
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("one_tap", [0, 1])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_one_tap_option_selects_the_form(cuda_lib, one_tap, T):
+    """The fused fill's one_tap option: 1 is the oracle's CPU form, 0 its
+    device form, bit for bit on data with NaNs and infinities."""
+    from treeamr.ghosts import device_schedule
+    D = 3
+    f = _walls_forest(D)
+    par = [(EvenParity,) * D, tuple(OddParity if d == 1 else EvenParity for d in range(D))]
+    fs = FieldSet(f, len(par), G=2, centering=vertexcentered(D), parity=par, T=T)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    host = awkward_fill(tuple(fs.work.shape), T, seed=17)
+    fs.work.copy_(torch.from_numpy(host))
+    expect = oracle.fill_fieldset(fs, s, one_tap=bool(one_tap))
+    other = oracle.fill_fieldset(fs, s, one_tap=not one_tap)
+    assert not np.array_equal(nanbits(expect), nanbits(other))  # the data tell them apart
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fs.factors = fs.factors.cuda()
+    ds = device_schedule(s, 0)
+    ds.set_option("one_tap", one_tap)
+    try:
+        fill_ghosts(fs, s)
+        torch.cuda.synchronize()
+    finally:
+        ds.set_option("one_tap", 1)
+    assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))

@@ -69,15 +69,21 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_srcstart);
   cudaFree(s->d_weights);
   cudaFree(s->d_tiles);
+  cudaFree(s->d_ptiles);
   cudaFree(s->d_cls);
   cudaFree(s->d_wtab);
+  cudaFree(s->d_csingle);
+  cudaFree(s->d_perm);
   cudaFree(s->d_err);
+  tam::side_destroy(s->side);
+  s->d_ptiles = nullptr;
   s->d_groups = nullptr;
   s->d_tb = s->d_sb = s->d_srcstart = nullptr;
   s->d_weights = nullptr;
   s->d_tiles = nullptr;
   s->d_cls = nullptr;
   s->d_wtab = nullptr;
+  s->d_csingle = s->d_perm = nullptr;
   s->d_err = nullptr;
 }
 
@@ -231,9 +237,61 @@ void build_product_table(const tam_schedule_desc *d, const tam_group &h, tam::De
   }
 }
 
+// The one-tap skip of the reference's CPU fill (src/ghosts.jl:28-56,
+// src/schedule.jl:83-86 single_rows): per dimension and target row, the row
+// of the column's only nonzero weight, or -1.  Where any row of the group has
+// one, `perm` lists the box points ordered (stably) by the set of dimensions
+// that skip, so that the lanes of a warp mostly share their trip counts.
+template <typename T>
+void build_singles(const tam_schedule_desc *d, const tam_group &h, tam::DevGroup &g,
+                   std::vector<int32_t> &csingle, std::vector<int32_t> &perm) {
+  const T *W = (const T *)d->weights;
+  bool any = false;
+  for (int k = 0; k < 3; ++k) {
+    g.csingle[k] = (int64_t)csingle.size();
+    if (k >= d->ndim) {
+      csingle.push_back(-1);
+      continue;
+    }
+    const tam_stencil &st = h.stencil[k];
+    for (int i = 0; i < st.ntarget; ++i) {
+      const T *col = W + st.weights + (int64_t)st.order * i;
+      int row = -1, nonzero = 0;
+      for (int m = 0; m < st.order; ++m)
+        if (col[m] != T(0)) {
+          ++nonzero;
+          row = m;
+        }
+      const int single = nonzero == 1 ? row : -1;
+      any = any || (single >= 0 && st.order > 1);
+      csingle.push_back(single);
+    }
+  }
+  g.perm = -1;
+  if (!any) return;
+  g.perm = (int64_t)perm.size();
+  std::vector<std::pair<int, int>> order;
+  order.reserve((size_t)g.n[0] * g.n[1] * g.n[2]);
+  for (int i3 = 0; i3 < g.n[2]; ++i3)
+    for (int i2 = 0; i2 < g.n[1]; ++i2)
+      for (int i1 = 0; i1 < g.n[0]; ++i1) {
+        const int idx[3] = {i1, i2, i3};
+        int mask = 0;
+        for (int k = 0; k < d->ndim; ++k)
+          if (csingle[g.csingle[k] + idx[k]] >= 0) mask |= 1 << k;
+        order.push_back({mask, i1 + g.n[0] * (i2 + g.n[1] * i3)});
+      }
+  std::stable_sort(order.begin(), order.end(),
+                   [](const std::pair<int, int> &a, const std::pair<int, int> &b) {
+                     return a.first < b.first;
+                   });
+  for (const auto &o : order) perm.push_back(o.second);
+}
+
 tam::SchedArgs sched_args(const tam_sched *s) {
-  return tam::SchedArgs{s->d_groups, s->d_tb, s->d_sb, s->d_srcstart, s->d_weights, s->d_cls,
-                        s->d_wtab, s->shape.int_mul, nullptr};
+  return tam::SchedArgs{s->d_groups, s->d_tb,     s->d_sb,        s->d_srcstart,
+                        s->d_weights, s->d_cls,   s->d_wtab,      s->shape.int_mul,
+                        nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap};
 }
 
 // The fused tiles of every stage: each stage's transfers ordered by target
@@ -352,6 +410,7 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
   s->groups.resize(d->ngroups);
   std::vector<int32_t> cls;
   std::vector<unsigned char> wtab;
+  std::vector<int32_t> csingle(1, -1), perm(1, 0);  // a valid pool even when unused
   for (int32_t gi = 0; gi < d->ngroups; ++gi) {
     const tam_group &h = d->groups[gi];
     tam::DevGroup &g = s->groups[gi];
@@ -384,11 +443,19 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
     if (h.factorcol != 0) s->needs_factors = true;
     s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
     for (int k = 0; k < 3; ++k) g.C[k] = 1;
+    for (int k = 0; k < 3; ++k) g.csingle[k] = 0;
+    g.perm = -1;
     if (g.pclass > 1) {
       if (d->dtype == TAM_F64)
         build_product_table<double>(d, h, g, cls, wtab);
       else
         build_product_table<float>(d, h, g, cls, wtab);
+    }
+    if (g.pclass != 0) {
+      if (d->dtype == TAM_F64)
+        build_singles<double>(d, h, g, csingle, perm);
+      else
+        build_singles<float>(d, h, g, csingle, perm);
     }
   }
 
@@ -406,9 +473,12 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
   s->h_sb.assign(d->sourceblocks, d->sourceblocks + d->ntransfers);
   s->h_srcstart.assign(d->srcstart, d->srcstart + d->nsrcstart);
   std::vector<tam::Tile> tiles = build_tiles(s);
+  std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
 
   cudaError_t e;
-  if ((e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
+  if ((e = tam::side_create(s->side)) != cudaSuccess ||
+      (e = upload(&s->d_ptiles, ptiles.data(), ptiles.size())) != cudaSuccess ||
+      (e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
       (e = upload(&s->d_tb, d->targetblocks, (size_t)d->ntransfers)) != cudaSuccess ||
       (e = upload(&s->d_sb, d->sourceblocks, (size_t)d->ntransfers)) != cudaSuccess ||
       (e = upload(&s->d_srcstart, srcstart.data(), srcstart.size())) != cudaSuccess ||
@@ -417,6 +487,8 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
       (e = upload(&s->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
       (e = upload(&s->d_cls, cls.data(), cls.size())) != cudaSuccess ||
       (e = upload((unsigned char **)&s->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
+      (e = upload(&s->d_csingle, csingle.data(), csingle.size())) != cudaSuccess ||
+      (e = upload(&s->d_perm, perm.data(), perm.size())) != cudaSuccess ||
       (e = upload(&s->d_err, (const int32_t *)nullptr, 1)) != cudaSuccess) {
     free_sched_device(s);
     delete s;
@@ -428,6 +500,8 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
   s->h_pool_weights = std::move(weights);
   s->h_pool_cls = std::move(cls);
   s->h_pool_wtab = std::move(wtab);
+  s->h_pool_csingle = std::move(csingle);
+  s->h_pool_perm = std::move(perm);
   *out = s;
   return TAM_OK;
 }
@@ -537,10 +611,9 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
   cudaStream_t st = (cudaStream_t)stream;
   for (const tam::Stage &stage : s->stages) {
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
-    cudaError_t e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles + stage.tile0,
-                                            stage.ncopy, stage.ntiles, sched_args(s), work,
-                                            factors, nvars,
-                                            s->S, s->shape.threads, st);
+    cudaError_t e = tam::launch_fused_stage(
+        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy, stage.nptiles,
+        sched_args(s), work, factors, nvars, s->S, s->shape.threads, st, &s->side);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
   }
   return TAM_OK;
@@ -575,16 +648,24 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
       const int old = s->shape.tile_items;
       s->shape.tile_items = (int)value;
       std::vector<tam::Tile> tiles = build_tiles(s);
+      std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
       tam::Tile *d = nullptr;
+      tam::PTile *dp = nullptr;
       cudaError_t e = upload(&d, tiles.data(), tiles.size());
+      if (e == cudaSuccess) e = upload(&dp, ptiles.data(), ptiles.size());
       if (e != cudaSuccess) {
+        cudaFree(d);
+        cudaFree(dp);
         s->shape.tile_items = old;
-        build_tiles(s);
+        std::vector<tam::Tile> back = build_tiles(s);
+        tam::pack_stages(s->stages, back, old);
         return cuda_fail(s->ctx, e, "re-tiling");
       }
       cudaDeviceSynchronize();  // no fill may still read the old tiles
       cudaFree(s->d_tiles);
+      cudaFree(s->d_ptiles);
       s->d_tiles = d;
+      s->d_ptiles = dp;
       return TAM_OK;
     }
     case TAM_OPT_THREADS:
@@ -595,6 +676,10 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
     case TAM_OPT_INT_MUL:
       if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "int_mul is 0 or 1");
       s->shape.int_mul = (int)value;
+      return TAM_OK;
+    case TAM_OPT_ONE_TAP:
+      if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "one_tap is 0 or 1");
+      s->shape.one_tap = (int)value;
       return TAM_OK;
     default:
       return fail(s->ctx, TAM_EINVAL, "unknown option");
@@ -607,6 +692,7 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_TILE_ITEMS: *value = s->shape.tile_items; return TAM_OK;
     case TAM_OPT_THREADS: *value = s->shape.threads; return TAM_OK;
     case TAM_OPT_INT_MUL: *value = s->shape.int_mul; return TAM_OK;
+    case TAM_OPT_ONE_TAP: *value = s->shape.one_tap; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
 }

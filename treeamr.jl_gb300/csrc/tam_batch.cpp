@@ -33,9 +33,12 @@ struct tam_batch {
   tam::LaunchShape shape;
   tam::DevGroup *d_groups = nullptr;
   int32_t *d_tb = nullptr, *d_sb = nullptr, *d_srcstart = nullptr, *d_cls = nullptr;
+  int32_t *d_csingle = nullptr, *d_perm = nullptr;
   void *d_weights = nullptr, *d_wtab = nullptr;
   tam::Tile *d_tiles = nullptr;
+  tam::PTile *d_ptiles = nullptr;
   tam::Member *d_members = nullptr;
+  tam::SideStream side;
 };
 
 namespace {
@@ -76,12 +79,18 @@ void free_batch_device(tam_batch *b) {
   cudaFree(b->d_weights);
   cudaFree(b->d_wtab);
   cudaFree(b->d_tiles);
+  cudaFree(b->d_ptiles);
   cudaFree(b->d_members);
+  cudaFree(b->d_csingle);
+  cudaFree(b->d_perm);
+  tam::side_destroy(b->side);
+  b->d_ptiles = nullptr;
   b->d_groups = nullptr;
   b->d_tb = b->d_sb = b->d_srcstart = b->d_cls = nullptr;
   b->d_weights = b->d_wtab = nullptr;
   b->d_tiles = nullptr;
   b->d_members = nullptr;
+  b->d_csingle = b->d_perm = nullptr;
 }
 
 // Every stage tag's tiles across all members: per member the transfers by
@@ -166,7 +175,7 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
   b->D = first->D;
   b->dtype = first->dtype;
   const size_t esz = b->dtype == TAM_F64 ? 8 : 4;
-  std::vector<int32_t> tb, sb, srcstart, cls;
+  std::vector<int32_t> tb, sb, srcstart, cls, csingle, perm;
   std::vector<unsigned char> weights, wtab;
   std::map<int32_t, std::vector<int32_t>> bytag;
   for (int32_t m = 0; m < n; ++m) {
@@ -182,6 +191,7 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     b->needs_factors = b->needs_factors || s->needs_factors;
     const int64_t g0 = (int64_t)b->groups.size(), t0 = (int64_t)tb.size();
     const int64_t ss0 = (int64_t)srcstart.size(), c0 = (int64_t)cls.size();
+    const int64_t cs0 = (int64_t)csingle.size(), p0 = (int64_t)perm.size();
     const int64_t w0 = (int64_t)(weights.size() / esz), wt0 = (int64_t)(wtab.size() / esz);
     for (const tam::DevGroup &h : s->groups) {
       tam::DevGroup g = h;
@@ -189,7 +199,9 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
         g.ss[k] += ss0;
         g.w[k] += w0;
         g.cls[k] += c0;
+        g.csingle[k] += cs0;
       }
+      if (g.perm >= 0) g.perm += p0;
       g.wtab += wt0;
       g.first += t0;
       g.member = m;
@@ -201,6 +213,8 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     sb.insert(sb.end(), s->h_sb.begin(), s->h_sb.end());
     srcstart.insert(srcstart.end(), s->h_pool_srcstart.begin(), s->h_pool_srcstart.end());
     cls.insert(cls.end(), s->h_pool_cls.begin(), s->h_pool_cls.end());
+    csingle.insert(csingle.end(), s->h_pool_csingle.begin(), s->h_pool_csingle.end());
+    perm.insert(perm.end(), s->h_pool_perm.begin(), s->h_pool_perm.end());
     weights.insert(weights.end(), s->h_pool_weights.begin(), s->h_pool_weights.end());
     // element-aligned: each member's product table starts on an element
     wtab.resize((wtab.size() + esz - 1) / esz * esz);
@@ -223,12 +237,17 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
   }
   b->h_tb = tb;
   std::vector<tam::Tile> tiles = batch_tiles(b);
+  std::vector<tam::PTile> ptiles = tam::pack_stages(b->stages, tiles, b->shape.tile_items);
   cudaError_t e;
-  if ((e = up(&b->d_groups, b->groups.data(), b->groups.size())) != cudaSuccess ||
+  if ((e = tam::side_create(b->side)) != cudaSuccess ||
+      (e = up(&b->d_ptiles, ptiles.data(), ptiles.size())) != cudaSuccess ||
+      (e = up(&b->d_groups, b->groups.data(), b->groups.size())) != cudaSuccess ||
       (e = up(&b->d_tb, tb.data(), tb.size())) != cudaSuccess ||
       (e = up(&b->d_sb, sb.data(), sb.size())) != cudaSuccess ||
       (e = up(&b->d_srcstart, srcstart.data(), srcstart.size())) != cudaSuccess ||
       (e = up(&b->d_cls, cls.data(), cls.size())) != cudaSuccess ||
+      (e = up(&b->d_csingle, csingle.data(), csingle.size())) != cudaSuccess ||
+      (e = up(&b->d_perm, perm.data(), perm.size())) != cudaSuccess ||
       (e = up((unsigned char **)&b->d_weights, weights.data(), weights.size())) != cudaSuccess ||
       (e = up((unsigned char **)&b->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
       (e = up(&b->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
@@ -257,14 +276,16 @@ int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars
   if (rc != TAM_OK) return rc;
   Guard guard(b->ctx->device);
   if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
-  const tam::SchedArgs args{b->d_groups, b->d_tb,   b->d_sb,          b->d_srcstart, b->d_weights,
-                            b->d_cls,    b->d_wtab, b->shape.int_mul, b->d_members};
+  const tam::SchedArgs args{b->d_groups,  b->d_tb,      b->d_sb,          b->d_srcstart,
+                            b->d_weights, b->d_cls,     b->d_wtab,        b->shape.int_mul,
+                            b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap};
   const int S[3] = {1, 1, 1};  // each member's own, from the member table
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
-    cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles + st.tile0, st.ncopy,
-                                            st.ntiles, args, arena, factor_arena, nvars, S,
-                                            b->shape.threads, (cudaStream_t)stream);
+    cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles + st.ptile0,
+                                            st.npcopy, st.nptiles, args, arena, factor_arena,
+                                            nvars, S, b->shape.threads, (cudaStream_t)stream,
+                                            &b->side);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return bfail(b->ctx, TAM_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));
@@ -304,16 +325,24 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
     const int old = b->shape.tile_items;
     b->shape.tile_items = (int)value;
     std::vector<tam::Tile> tiles = batch_tiles(b);
+    std::vector<tam::PTile> ptiles = tam::pack_stages(b->stages, tiles, b->shape.tile_items);
     tam::Tile *d = nullptr;
+    tam::PTile *dp = nullptr;
     cudaError_t e = up(&d, tiles.data(), tiles.size());
+    if (e == cudaSuccess) e = up(&dp, ptiles.data(), ptiles.size());
     if (e != cudaSuccess) {
+      cudaFree(d);
+      cudaFree(dp);
       b->shape.tile_items = old;
-      batch_tiles(b);
+      std::vector<tam::Tile> back = batch_tiles(b);
+      tam::pack_stages(b->stages, back, old);
       return bfail(b->ctx, TAM_ECUDA, "re-tiling the batch failed");
     }
     cudaDeviceSynchronize();
     cudaFree(b->d_tiles);
+    cudaFree(b->d_ptiles);
     b->d_tiles = d;
+    b->d_ptiles = dp;
     return TAM_OK;
   }
   if (option == TAM_OPT_THREADS) {
@@ -325,6 +354,11 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (option == TAM_OPT_INT_MUL) {
     if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "int_mul is 0 or 1");
     b->shape.int_mul = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_ONE_TAP) {
+    if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "one_tap is 0 or 1");
+    b->shape.one_tap = (int)value;
     return TAM_OK;
   }
   return bfail(b->ctx, TAM_EINVAL, "unknown option");

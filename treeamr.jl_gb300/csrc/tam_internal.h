@@ -39,6 +39,13 @@ struct DevGroup {
   int64_t wtab;      // product-table pool offset
   int32_t member;    // the forest of a batch this group belongs to (0 alone)
   int32_t pad3;
+  // The one-tap skip of the reference's CPU fill (src/ghosts.jl:28-56): per
+  // dimension, for each column class, the row of its only nonzero weight, or
+  // -1 (int32 pool entries at csingle[d] + class).  `perm` (or -1) orders the
+  // box points by which dimensions skip, so that a warp's lanes share their
+  // trip counts: point `perm[item]` is the item-th a tile takes.
+  int64_t csingle[3];
+  int64_t perm;
 };
 
 // One forest of a batch (tam_batch_fill): where its field data and factor
@@ -60,12 +67,46 @@ struct Tile {
   int32_t nitems;
 };
 
+// What a warp of the fused kernels takes: up to 32 consecutive tiles
+// (tiles[seg0 .. seg0 + nseg)), nitems box points in all, so that small
+// transfers -- an 8-point corner, a 2-point edge of a vertex set -- share a
+// warp instead of leaving most of its lanes idle.
+struct PTile {
+  int32_t seg0;
+  int32_t nseg;
+  int32_t nitems;
+  int32_t pad;
+};
+
+// The packing: consecutive tiles of [begin, end) joined while they fit in
+// `target` points and 32 segments.
+void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
+                std::vector<PTile> &out);
+
+struct Stage;
+// Every stage's packed tiles (sets the stages' ptile0, npcopy, nptiles).
+std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
+                               int target);
+
+// A second stream and two events, so a stage's copy and stencil launches run
+// side by side (fork and join on the caller's stream; capturable).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  bool ok() const { return stream && fork && join; }
+};
+cudaError_t side_create(SideStream &s);
+void side_destroy(SideStream &s);
+
 struct Stage {
   int32_t tag;
   std::vector<int32_t> groups;  // indices into the schedule's groups
   int64_t tile0 = 0;            // first tile in the schedule's tile array
   int64_t ntiles = 0;           // copy tiles first, then stencil tiles
   int64_t ncopy = 0;            // the stage's unit-copy tiles
+  int64_t ptile0 = 0;           // first packed tile of the stage
+  int64_t npcopy = 0;           // packed tiles of the copies, then
+  int64_t nptiles = 0;          // all packed tiles of the stage
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -101,6 +142,7 @@ struct LaunchShape {
   int tile_items = 128;     // box points per tile
   int threads = 256;        // threads per CTA of the fused kernel
   int int_mul = 0;          // Float64 short-weight multiplies on the integer pipe
+  int one_tap = 1;          // the CPU form of the sum (TAM_OPT_ONE_TAP)
 };
 
 }  // namespace tam
@@ -128,6 +170,8 @@ struct tam_sched {
   std::vector<unsigned char> h_pool_weights;
   std::vector<int32_t> h_pool_cls;
   std::vector<unsigned char> h_pool_wtab;
+  std::vector<int32_t> h_pool_csingle;
+  std::vector<int32_t> h_pool_perm;
   std::vector<tam::DevGroup> groups;
   std::vector<tam::Stage> stages;
   int64_t ntransfers = 0;
@@ -141,7 +185,11 @@ struct tam_sched {
   void *d_weights = nullptr;
   int32_t *d_cls = nullptr;
   void *d_wtab = nullptr;
+  int32_t *d_csingle = nullptr;
+  int32_t *d_perm = nullptr;
   tam::Tile *d_tiles = nullptr;
+  tam::PTile *d_ptiles = nullptr;
+  tam::SideStream side;
   int32_t *d_err = nullptr;
   // the adjoint, prepared on first use (tam_adjoint.cu)
   bool adj_ready = false;
@@ -173,15 +221,22 @@ struct SchedArgs {
   const void *wtab;
   int int_mul;
   const Member *members;  // a batch's member table, or null for one schedule
+  const int32_t *csingle;  // per group, dimension and target row: the single row or -1
+  const int32_t *perm;     // per group with singles: the box points in tile order
+  int one_tap;             // take the single rows (the CPU form) in the fused kernels
 };
 
 cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
                                const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], cudaStream_t stream);
 
-cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ncopy, int64_t ntiles,
-                               const SchedArgs &a, void *work, const void *factors, int nvars,
-                               const int S[3], int threads, cudaStream_t stream);
+// One stage: the packed tiles [0, npcopy) run the copy kernel and
+// [npcopy, nptiles) the stencil kernel, on `stream` and, when `side` is
+// given and both are present, the stencils on the side stream alongside.
+cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
+                               int64_t npcopy, int64_t nptiles, const SchedArgs &a, void *work,
+                               const void *factors, int nvars, const int S[3], int threads,
+                               cudaStream_t stream, SideStream *side);
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);

@@ -95,12 +95,16 @@ struct Args {
   const T *__restrict__ wtab;
   int int_mul;
   const Member *__restrict__ members;
+  const int32_t *__restrict__ csingle;
+  const int32_t *__restrict__ perm;
+  int one_tap;
 };
 
 template <typename T>
 __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
-  return Args<T>{a.groups, a.tb, a.sb, a.srcstart, (const T *)a.weights, a.cls,
-                 (const T *)a.wtab, a.int_mul, a.members};
+  return Args<T>{a.groups,  a.tb,      a.sb,   a.srcstart, (const T *)a.weights,
+                 a.cls,     (const T *)a.wtab, a.int_mul, a.members, a.csingle,
+                 a.perm,    a.one_tap};
 }
 
 struct Geom {
@@ -258,10 +262,22 @@ __device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[N
   }
 }
 
+// The taps of dimension d a point takes: every row [0, P), or in the CPU
+// form of the sum (src/ghosts.jl:28-56) only the row of the column's single
+// nonzero weight.
+__device__ __forceinline__ void tap_rows(const int32_t *__restrict__ single, int P, int &lo,
+                                         int &hi) {
+  const int k = __ldg(single);
+  lo = k >= 0 ? k : 0;
+  hi = k >= 0 ? k + 1 : P;
+}
+
 // A uniform order-P stencil through the group's product table: per tap one
 // multiply and one add per variable, the weight product loaded once for
-// VC variables at a time.
-template <typename T, int D, int P, int VC>
+// VC variables at a time.  SKIP: the one-tap rows of `tap_rows`, which
+// leave out only terms 0 * u, so the remaining products are summed in the
+// same order (m_1 fastest) as the full nest.
+template <typename T, int D, int P, int VC, bool SKIP>
 __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, int i3,
                                             const Geom &o, const Args<T> &a,
                                             const T *__restrict__ work, T *__restrict__ dst,
@@ -274,6 +290,12 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
   const int c2 = D >= 2 ? __ldg(a.cls + g.cls[1] + i2) : 0;
   const int c3 = D >= 3 ? __ldg(a.cls + g.cls[2] + i3) : 0;
   const T *__restrict__ W = a.wtab + g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * PD;
+  int lo1 = 0, hi1 = P, lo2 = 0, hi2 = P2, lo3 = 0, hi3 = P3;
+  if (SKIP) {
+    tap_rows(a.csingle + g.csingle[0] + i1, P, lo1, hi1);
+    if (D >= 2) tap_rows(a.csingle + g.csingle[1] + i2, P, lo2, hi2);
+    if (D >= 3) tap_rows(a.csingle + g.csingle[2] + i3, P, lo3, hi3);
+  }
   if constexpr (sizeof(T) == 8) {
     if (g.shortw && a.int_mul) {
       // F64 with short weight products: the multiplies on the integer pipe,
@@ -284,21 +306,25 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
         for (int j = 0; j < VC; ++j) acc[j] = 0.0;
         const double *src = work + o.soff + v0 * o.vstride;
         bool bad = false;
+        auto tap = [&](int m1, int m2, int m3) {
+          const ShortW sw = short_weight(__ldg(W + (m3 * P2 + m2) * P + m1));
+          const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+          for (int j = 0; j < VC; ++j)
+            if (v0 + j < nvars) {
+              const double p = mul_short_flag(sw.wm, sw.we, sw.wsign, src[off + j * o.vstride], bad);
+              acc[j] = __dadd_rn(acc[j], p);
+            }
+        };
 #pragma unroll 1
-        for (int m3 = 0; m3 < P3; ++m3) {
+        for (int m3 = lo3; m3 < hi3; ++m3) {
+#pragma unroll(SKIP ? 1 : P2)
+          for (int m2 = lo2; m2 < hi2; ++m2) {
+            if (SKIP && hi1 - lo1 == 1) {
+              tap(lo1, m2, m3);
+            } else {
 #pragma unroll
-          for (int m2 = 0; m2 < P2; ++m2) {
-#pragma unroll
-            for (int m1 = 0; m1 < P; ++m1) {
-              const ShortW sw = short_weight(__ldg(W + (m3 * P2 + m2) * P + m1));
-              const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
-#pragma unroll
-              for (int j = 0; j < VC; ++j)
-                if (v0 + j < nvars) {
-                  const double p = mul_short_flag(sw.wm, sw.we, sw.wsign,
-                                                  src[off + j * o.vstride], bad);
-                  acc[j] = __dadd_rn(acc[j], p);
-                }
+              for (int m1 = 0; m1 < P; ++m1) tap(m1, m2, m3);
             }
           }
         }
@@ -306,14 +332,18 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
 #pragma unroll
           for (int j = 0; j < VC; ++j) acc[j] = 0.0;
 #pragma unroll 1
-          for (int k = 0; k < PD; ++k) {
-            const int m1 = k % P, m2 = (k / P) % P2, m3 = k / (P * P2);
-            const double w = __ldg(W + k);
-            const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+          for (int m3 = lo3; m3 < hi3; ++m3)
+#pragma unroll 1
+            for (int m2 = lo2; m2 < hi2; ++m2)
+#pragma unroll 1
+              for (int m1 = lo1; m1 < hi1; ++m1) {
+                const double w = __ldg(W + (m3 * P2 + m2) * P + m1);
+                const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
-            for (int j = 0; j < VC; ++j)
-              if (v0 + j < nvars) acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.vstride]));
-          }
+                for (int j = 0; j < VC; ++j)
+                  if (v0 + j < nvars)
+                    acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.vstride]));
+              }
         }
 #pragma unroll
         for (int j = 0; j < VC; ++j)
@@ -329,17 +359,22 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
 #pragma unroll
     for (int j = 0; j < VC; ++j) acc[j] = T(0);
     const T *src = work + o.soff + v0 * o.vstride;
+    auto tap = [&](int m1, int m2, int m3) {
+      const T w = __ldg(W + (m3 * P2 + m2) * P + m1);
+      const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
-    for (int m3 = 0; m3 < P3; ++m3) {
+      for (int j = 0; j < VC; ++j)
+        if (v0 + j < nvars) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.vstride]));
+    };
+#pragma unroll(SKIP ? 1 : P3)
+    for (int m3 = lo3; m3 < hi3; ++m3) {
+#pragma unroll(SKIP ? 1 : P2)
+      for (int m2 = lo2; m2 < hi2; ++m2) {
+        if (SKIP && hi1 - lo1 == 1) {
+          tap(lo1, m2, m3);
+        } else {
 #pragma unroll
-      for (int m2 = 0; m2 < P2; ++m2) {
-#pragma unroll
-        for (int m1 = 0; m1 < P; ++m1) {
-          const T w = __ldg(W + (m3 * P2 + m2) * P + m1);
-          const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
-#pragma unroll
-          for (int j = 0; j < VC; ++j)
-            if (v0 + j < nvars) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.vstride]));
+          for (int m1 = 0; m1 < P; ++m1) tap(m1, m2, m3);
         }
       }
     }
@@ -350,19 +385,52 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
   }
 }
 
-// Mixed orders: the reference's nest with the product formed per tap.
+// Mixed orders: the reference's nest with the product formed per tap; a
+// dimension that takes one tap (SKIP) is the order-1 nest at that row.
 template <typename T, int D>
 __device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2, int i3,
                                               const Geom &o, const Args<T> &a,
                                               const T *__restrict__ work, T *__restrict__ dst,
-                                              const T *__restrict__ factors, int nvars) {
+                                              const T *__restrict__ factors, int nvars,
+                                              bool skip) {
   const T *w1 = a.weights + g.w[0] + (int64_t)g.order[0] * i1;
   const T *w2 = a.weights + g.w[1] + (int64_t)g.order[1] * i2;
   const T *w3 = a.weights + g.w[2] + (int64_t)g.order[2] * i3;
+  int ord[3] = {g.order[0], g.order[1], g.order[2]};
+  int64_t soff = o.soff;
+  if (skip) {
+    const int idx[3] = {i1, i2, i3};
+    const T *w[3] = {w1, w2, w3};
+    const int64_t stride[3] = {1, o.s2, o.s3};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const int k = __ldg(a.csingle + g.csingle[d] + idx[d]);
+      if (k >= 0) {
+        w[d] += k;
+        ord[d] = 1;
+        soff += k * stride[d];
+      }
+    }
+    w1 = w[0];
+    w2 = w[1];
+    w3 = w[2];
+  }
   for (int v = 0; v < nvars; ++v) {
-    T acc = stencil_sum<T, D, 0>(work + o.soff + v * o.vstride, o.s2, o.s3, w1, w2, w3, g.order);
+    T acc = stencil_sum<T, D, 0>(work + soff + v * o.vstride, o.s2, o.s3, w1, w2, w3, ord);
     dst[o.toff + v * o.vstride] = scaled(acc, factors, v, nvars, g.factorcol);
   }
+}
+
+template <typename T, int D, int P, int VC>
+__device__ __forceinline__ void table_dispatch(const DevGroup &g, int i1, int i2, int i3,
+                                               const Geom &o, const Args<T> &a,
+                                               const T *__restrict__ work, T *__restrict__ dst,
+                                               const T *__restrict__ factors, int nvars,
+                                               bool skip) {
+  if (skip)
+    table_point<T, D, P, VC, true>(g, i1, i2, i3, o, a, work, dst, factors, nvars);
+  else
+    table_point<T, D, P, VC, false>(g, i1, i2, i3, o, a, work, dst, factors, nvars);
 }
 
 // Every variable of one box point of one stencil transfer, by the group's class.
@@ -373,21 +441,22 @@ __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2,
                                               const T *__restrict__ factors, int nvars, int S1,
                                               int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
+  const bool skip = a.one_tap && g.perm >= 0;
   switch (g.pclass) {
     case 2:
-      table_point<T, D, 2, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
+      table_dispatch<T, D, 2, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 3:
-      table_point<T, D, 3, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
+      table_dispatch<T, D, 3, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 4:
-      table_point<T, D, 4, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
+      table_dispatch<T, D, 4, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 6:
-      table_point<T, D, 6, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
+      table_dispatch<T, D, 6, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     default:
-      generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars);
+      generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
   }
 }
@@ -470,33 +539,69 @@ struct TileLayout {
   }
 };
 
+// A warp's packed tile: lane l holds segment l; every lane then finds, for
+// each of its points, the segment holding it.  All shuffles run with the full
+// warp: the rounds loop to the tile's size, uniform across lanes.
+struct SegPoint {
+  int group, transfer, item;
+  bool on;
+};
+
+__device__ __forceinline__ void load_segments(const Tile *__restrict__ tiles, const PTile &pt,
+                                              int lane, Tile &seg, int &pref) {
+  seg = Tile{0, 0, 0, 0};
+  if (lane < pt.nseg) seg = tiles[pt.seg0 + lane];
+  int incl = seg.nitems;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  pref = incl - seg.nitems;
+}
+
+__device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int k) {
+  int mine = 0;
+  for (int s = 1; s < nseg; ++s)
+    if (k >= __shfl_sync(0xffffffffu, pref, s)) mine = s;
+  SegPoint p;
+  p.group = __shfl_sync(0xffffffffu, seg.group, mine);
+  p.transfer = __shfl_sync(0xffffffffu, seg.transfer, mine);
+  p.item = __shfl_sync(0xffffffffu, seg.item0, mine) + k - __shfl_sync(0xffffffffu, pref, mine);
+  p.on = true;
+  return p;
+}
+
 // The unit-copy tiles of a stage: a light kernel, every variable's load of a
-// point in flight together, and the next tile's descriptor fetched while this
-// one runs.
+// point in flight together.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict__ tiles,
-                                                         int64_t ntiles, Args<T> a,
+                                                         const PTile *__restrict__ ptiles,
+                                                         int64_t nptiles, Args<T> a,
                                                          const T *__restrict__ src,
                                                          T *__restrict__ dst,
                                                          const T *__restrict__ factors,
                                                          int nvars, int S1, int S2, int S3) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  Tile next = w < ntiles ? tiles[w] : Tile{0, 0, 0, 0};
-  for (; w < ntiles; w += warps) {
-    const Tile tile = next;
-    if (w + warps < ntiles) next = tiles[w + warps];
-    const DevGroup &g = a.groups[tile.group];
-    const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
-    const int64_t sblock = __ldg(a.sb + tile.transfer) - 1;
-    const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
-    for (int k = lane; k < tile.nitems; k += 32) {
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nptiles;
+       w += warps) {
+    const PTile pt = ptiles[w];
+    Tile seg;
+    int pref;
+    load_segments(tiles, pt, lane, seg, pref);
+    for (int base = 0; base < pt.nitems; base += 32) {
+      const int k = base + lane;
+      SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
+      if (k >= pt.nitems) continue;
+      const DevGroup &g = a.groups[q.group];
+      const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+      const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+      const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
+      int i1, i2, i3;
+      box_point(q.item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
       Geom o[1];
       const bool on[1] = {true};
-      int i1, i2, i3;
-      box_point(tile.item0 + k, n1, n12, i1, i2, i3);
       o[0] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
       copy_points<T, 1>(g, o, on, L.src, L.dst, L.factors, nvars);
     }
@@ -506,26 +611,31 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
 // The stencil tiles of a stage: one point a lane, every variable.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(512) fused_stage_kernel(const Tile *__restrict__ tiles,
-                                                          int64_t ntiles, Args<T> a,
+                                                          const PTile *__restrict__ ptiles,
+                                                          int64_t nptiles, Args<T> a,
                                                           const T *__restrict__ src,
                                                           T *__restrict__ dst,
                                                           const T *__restrict__ factors,
                                                           int nvars, int S1, int S2, int S3) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  Tile next = w < ntiles ? tiles[w] : Tile{0, 0, 0, 0};
-  for (; w < ntiles; w += warps) {
-    const Tile tile = next;
-    if (w + warps < ntiles) next = tiles[w + warps];
-    const DevGroup &g = a.groups[tile.group];
-    const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
-    const int64_t sblock = __ldg(a.sb + tile.transfer) - 1;
-    const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
-    for (int k = lane; k < tile.nitems; k += 32) {
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nptiles;
+       w += warps) {
+    const PTile pt = ptiles[w];
+    Tile seg;
+    int pref;
+    load_segments(tiles, pt, lane, seg, pref);
+    for (int base = 0; base < pt.nitems; base += 32) {
+      const int k = base + lane;
+      SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
+      if (k >= pt.nitems) continue;
+      const DevGroup &g = a.groups[q.group];
+      const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+      const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+      const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
+      const int item = g.perm >= 0 ? __ldg(a.perm + g.perm + q.item) : q.item;
       int i1, i2, i3;
-      box_point(tile.item0 + k, n1, n12, i1, i2, i3);
+      box_point(item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
       stencil_point<T, D>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars, L.S1,
                           L.S2, L.S3);
     }
@@ -559,51 +669,66 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
 }
 
 template <typename T, int D>
-void launch_both(const Tile *tiles, int64_t ncopy, int64_t ntiles, const Args<T> &a, T *work,
-                 const T *factors, int nvars, const int S[3], int threads, cudaStream_t stream) {
+cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy, int64_t nptiles,
+                        const Args<T> &a, T *work, const T *factors, int nvars, const int S[3],
+                        int threads, cudaStream_t stream, SideStream *side) {
   const int wpb = threads / 32;
   const bool batch = a.members != nullptr;
-  if (ncopy > 0) {
-    const int64_t blocks = std::min<int64_t>((ncopy + wpb - 1) / wpb, (int64_t)1 << 30);
-    if (batch)
-      fused_copy_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ncopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
-    else
-      fused_copy_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ncopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  const int64_t nst = nptiles - npcopy;
+  // both present: the stencils on the side stream, alongside the copies
+  const bool fork = side && side->ok() && npcopy > 0 && nst > 0;
+  cudaStream_t sst = stream;
+  if (fork) {
+    cudaError_t e = cudaEventRecord(side->fork, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
+    if (e != cudaSuccess) return e;
+    sst = side->stream;
   }
-  const int64_t nst = ntiles - ncopy;
   if (nst > 0) {
     const int64_t blocks = std::min<int64_t>((nst + wpb - 1) / wpb, (int64_t)1 << 30);
     if (batch)
-      fused_stage_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles + ncopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+      fused_stage_kernel<T, D, true><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, ptiles + npcopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
     else
-      fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles + ncopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+      fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, ptiles + npcopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
   }
+  if (npcopy > 0) {
+    const int64_t blocks = std::min<int64_t>((npcopy + wpb - 1) / wpb, (int64_t)1 << 30);
+    if (batch)
+      fused_copy_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles, ptiles, npcopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+    else
+      fused_copy_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
+          tiles, ptiles, npcopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  }
+  if (fork) {
+    cudaError_t e = cudaEventRecord(side->join, side->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, side->join, 0);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
 }
 
 // A stage: its unit copies and its stencils, two launches with no
 // dependency between them (their targets are disjoint and neither reads a
 // point of the stage's targets).
 template <typename T>
-cudaError_t fused_dispatch(int D, const Tile *tiles, int64_t ncopy, int64_t ntiles,
-                           const Args<T> &a, T *work, const T *factors, int nvars, const int S[3],
-                           int threads, cudaStream_t stream) {
-  if (ntiles == 0) return cudaSuccess;
+cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy,
+                           int64_t nptiles, const Args<T> &a, T *work, const T *factors, int nvars,
+                           const int S[3], int threads, cudaStream_t stream, SideStream *side) {
+  if (nptiles == 0) return cudaSuccess;
   switch (D) {
     case 1:
-      launch_both<T, 1>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
-      break;
+      return launch_both<T, 1>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+                               threads, stream, side);
     case 2:
-      launch_both<T, 2>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
-      break;
+      return launch_both<T, 2>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+                               threads, stream, side);
     default:
-      launch_both<T, 3>(tiles, ncopy, ntiles, a, work, factors, nvars, S, threads, stream);
-      break;
+      return launch_both<T, 3>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+                               threads, stream, side);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace
@@ -618,15 +743,58 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
                                nvars, S, stream);
 }
 
-cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, int64_t ncopy,
-                               int64_t ntiles, const SchedArgs &a, void *work,
+cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
+                               int64_t npcopy, int64_t nptiles, const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, SideStream *side) {
   if (dtype == TAM_F64)
-    return fused_dispatch<double>(D, tiles, ncopy, ntiles, typed<double>(a), (double *)work,
-                                  (const double *)factors, nvars, S, threads, stream);
-  return fused_dispatch<float>(D, tiles, ncopy, ntiles, typed<float>(a), (float *)work,
-                               (const float *)factors, nvars, S, threads, stream);
+    return fused_dispatch<double>(D, tiles, ptiles, npcopy, nptiles, typed<double>(a),
+                                  (double *)work, (const double *)factors, nvars, S, threads,
+                                  stream, side);
+  return fused_dispatch<float>(D, tiles, ptiles, npcopy, nptiles, typed<float>(a), (float *)work,
+                               (const float *)factors, nvars, S, threads, stream, side);
+}
+
+void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
+                std::vector<PTile> &out) {
+  int64_t i = begin;
+  while (i < end) {
+    PTile p{(int32_t)i, 0, 0, 0};
+    while (i < end && p.nseg < 32 && (p.nseg == 0 || p.nitems + tiles[i].nitems <= target)) {
+      p.nitems += tiles[i].nitems;
+      ++p.nseg;
+      ++i;
+    }
+    out.push_back(p);
+  }
+}
+
+std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
+                               int target) {
+  std::vector<PTile> out;
+  for (Stage &st : stages) {
+    st.ptile0 = (int64_t)out.size();
+    pack_tiles(tiles, st.tile0, st.tile0 + st.ncopy, target, out);
+    st.npcopy = (int64_t)out.size() - st.ptile0;
+    pack_tiles(tiles, st.tile0 + st.ncopy, st.tile0 + st.ntiles, target, out);
+    st.nptiles = (int64_t)out.size() - st.ptile0;
+  }
+  return out;
+}
+
+cudaError_t side_create(SideStream &s) {
+  cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
+  if (e != cudaSuccess) side_destroy(s);
+  return e;
+}
+
+void side_destroy(SideStream &s) {
+  if (s.fork) cudaEventDestroy(s.fork);
+  if (s.join) cudaEventDestroy(s.join);
+  if (s.stream) cudaStreamDestroy(s.stream);
+  s = SideStream{};
 }
 
 }  // namespace tam

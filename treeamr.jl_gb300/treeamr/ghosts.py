@@ -80,7 +80,9 @@ class DeviceSchedule:
                       self.ctx, "tam_adjoint_scratch_bytes")
         return b.value
 
-    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3}
+    # one_tap picks the form of the sum (1: the reference's CPU form, 0: its
+    # device form; the same bits for finite data), the others speed only.
+    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4}
 
     def set_option(self, name: str, value: int):
         _native.check(self.lib.tam_schedule_set_option(self.handle, self.OPTIONS[name], int(value)),
