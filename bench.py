@@ -53,11 +53,83 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-walls", action="store_true")
+    ap.add_argument("--no-fp64-peak", action="store_true",
+                    help="skip the DGEMM measurement of the FP64 rate (the fp64 roofline)")
+    ap.add_argument("--options", default=None,
+                    help="fixed launch options instead of the autotuner's, e.g. "
+                         "tile_items=64,threads=128,int_mul=1")
     ap.add_argument("--workload", choices=["sphere", "walls"], default="sphere",
                     help="walls: time only the walls mesh (for profiling)")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32",
                     help="element type of --workload walls")
     return ap.parse_args()
+
+
+def stencil_flops(sched, nvars, one_tap=True):
+    """Algorithmic FP64/FP32 operations of each stage's stencil transfers: per
+    target point-variable one multiply and one add per tap the reference's
+    sum takes (src/ghosts.jl:75-118), with the CPU form's one tap along a
+    dimension whose weight column has a single nonzero weight.  Copies have
+    none."""
+    out = {}
+    for gr in sched.groups:
+        if gr.unit():
+            continue
+        taps = 1
+        for st in gr.stencils:
+            nz = np.count_nonzero(st.weights, axis=0)
+            eff = np.where((nz == 1) & one_tap, 1, st.order)
+            taps *= int(eff.sum())               # a tensor-product box: product of sums
+        out[gr.stage] = out.get(gr.stage, 0) + 2 * taps * gr.ntransfers() * nvars
+    return out
+
+
+def fused_launches(sched):
+    """Kernel launches of one fused fill: per stage a copy launch when it has
+    unit copies and a stencil launch when it has stencils."""
+    n = 0
+    for tag in sorted({gr.stage for gr in sched.groups}):
+        grs = [gr for gr in sched.groups if gr.stage == tag]
+        n += any(gr.unit() for gr in grs) + any(not gr.unit() for gr in grs)
+    return n
+
+
+def fp64_peak_tflops(dev):
+    """cuBLAS DGEMM, 4096^3, best of 5 (CUDA events): the FP64 rate the
+    stencil stages are compared with."""
+    import torch
+    n = 4096
+    a = torch.rand(n, n, dtype=torch.float64, device=dev)
+    b = torch.rand(n, n, dtype=torch.float64, device=dev)
+    c = a @ b
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b, c
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def fp64_roofline(flops, stage_ms, peak_tf):
+    """The FP64-pipe view of the stencil stages: algorithmic operations (a
+    multiply and an add per tap, no fused multiply-add, as the reference's
+    rounding requires) per second against the measured DGEMM rate, which
+    counts a fused multiply-add as two.  Stages without stencils are left
+    out."""
+    ms = {k: statistics.mean(v) for k, v in stage_ms.items() if k in flops}
+    tot_ms = sum(ms.values())
+    tot = sum(flops[k] for k in ms)
+    ach = tot / (tot_ms * 1e-3) / 1e12 if tot_ms else 0.0
+    return {"bound": "fp64", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": ach / peak_tf if peak_tf else None,
+            "peak_source": "measured here: cuBLAS DGEMM 4096^3, best of 5",
+            "stage_tflops": {str(k): flops[k] / (ms[k] * 1e-3) / 1e12 for k in ms},
+            "stage_flops": {str(k): flops[k] for k in ms}}
 
 
 def measure_batch(dev, timed, args, peak):
@@ -158,6 +230,9 @@ def measure_walls(T, dev, timed, args, peak):
         stage_ms.setdefault(tag, []).append(a.elapsed_time(b))
     kern_ms = sum(statistics.mean(v) for v in stage_ms.values())
     achieved = bytes_per_fill / (kern_ms * 1e-3) / 1e9
+    fp = None
+    if T == np.float64 and getattr(args, "fp64_peak", None):
+        fp = fp64_roofline(stencil_flops(sched, fs.nvars), stage_ms, args.fp64_peak)
     out = {
         "workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
                     "faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd), PV(4,4)",
@@ -169,7 +244,9 @@ def measure_walls(T, dev, timed, args, peak):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()}},
+        "fp64": fp,
         "tuned": tuned,
+        "gpu_launches_per_fill": fused_launches(sched),
     }
     del fs, sched
     torch.cuda.empty_cache()
@@ -345,7 +422,12 @@ def main():
 
     method = args.method
     tuned = None
-    if method == "fused":
+    if method == "fused" and args.options:
+        for kv in args.options.split(","):
+            k, v = kv.split("=")
+            ds.set_option(k.strip(), int(v))
+        cfg["options"] = ds.options()
+    elif method == "fused":
         from treeamr.autotune import autotune
         tuned = autotune(fs, sched)
         cfg["tuned"] = tuned
@@ -400,6 +482,9 @@ def main():
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    args.fp64_peak = None if args.no_fp64_peak else fp64_peak_tflops(dev)
+    fp64 = fp64_roofline(stencil_flops(sched, nvars), stage_ms, args.fp64_peak) \
+        if args.fp64_peak else None
 
     traffic = None
     try:
@@ -418,21 +503,37 @@ def main():
     # end to end through the public call, host buffers, copies inside the timing
     e2e = None
     if not args.no_e2e:
+        from treeamr.host import HostPipeline
         host_in = torch.empty_like(fs.work, device="cpu").pin_memory()
         host_in.copy_(fs.work)
-        host_out = torch.empty_like(host_in).pin_memory()
+        host_out = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
+        # one step in isolation: upload, fill, download on one stream
+        pipe1 = HostPipeline(fs, sched, depth=1)
+        pipe1.submit(host_in, host_out[0])
+        pipe1.synchronize()
+        ms_single = timed(lambda: (pipe1.submit(host_in, host_out[0]), pipe1.join(stream)), 3)
+        del pipe1
+        torch.cuda.empty_cache()
+        # steps in flight together: each state's upload, fill and download on
+        # its own stream and device buffer, three states at a time
+        pipe = HostPipeline(fs, sched, depth=3)
 
-        def e2e_step():
-            fs.work.copy_(host_in, non_blocking=True)
-            fill_ghosts(fs, sched, method=method)
-            host_out.copy_(fs.work, non_blocking=True)
-        e2e_step()
-        e2e_steps = max(3, min(args.steps, 10))
-        ms_e2e = timed(e2e_step, e2e_steps)
+        def e2e_run(n):
+            pipe.wait_on(stream)                 # after the timing's start event
+            for i in range(n):
+                pipe.submit(host_in, host_out[i % 2])
+            pipe.join(stream)                    # before its end event
+        e2e_run(3)
+        e2e_steps = max(6, min(args.steps, 12))
+        ms_e2e = timed(lambda: e2e_run(e2e_steps), 1) / e2e_steps
         e2e = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
                "ms_per_step": ms_e2e, "h2d_bytes_per_step": field_bytes,
-               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps}
-        del host_in, host_out
+               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps,
+               "api": "tam_fill_host (C ABI, host buffers) through treeamr.host.HostPipeline, "
+                      "3 streams and device buffers",
+               "single_step_ms": ms_single}
+        del pipe, host_in, host_out
+        torch.cuda.empty_cache()
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -461,10 +562,11 @@ def main():
                          "kernel": "fused_stage_kernel",
                          "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
                          "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
+            "fp64": fp64,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": args.steps * ds.nstages if method == "fused" else
+            "gpu_launches": args.steps * fused_launches(sched) if method == "fused" else
             args.steps * ds.ngroups,
         }
         print(json.dumps(line), flush=True)

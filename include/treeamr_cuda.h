@@ -137,6 +137,21 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
              const void *factors, int32_t first_stage, int32_t last_stage,
              void *stream);
 
+/* The fill of a field set whose data live in host memory (the reference's
+ * fill_ghosts!, src/ghosts.jl:1783, on host arrays): asynchronous on
+ * `stream`, host_in (nblocks * nvars * S1*S2*S3 elements in the layout of
+ * tam_fill) is copied into device_work, the stages [first_stage, last_stage]
+ * are filled there as tam_fill fills them, and device_work is copied back
+ * into host_out (which may be host_in).  Page-locked host buffers let the
+ * copies run on the copy engines beside other streams' work: a caller that
+ * fills a sequence of field states round-robin over two or three streams,
+ * each with its own device buffer, keeps one state's upload, another's fill
+ * and a third's download in flight together.  factors is a device pointer,
+ * as for tam_fill. */
+int tam_fill_host(tam_sched *s, const void *host_in, void *host_out, void *device_work,
+                  int32_t nvars, int64_t nblocks, const void *factors, int32_t first_stage,
+                  int32_t last_stage, void *stream);
+
 /* The plain fill: one launch per TransferGroup, one thread per
  * point-variable, as the reference's device path launches transfer_kernel!
  * (src/ghosts.jl:420-521).  Same arguments and results as tam_fill. */

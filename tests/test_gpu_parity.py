@@ -226,3 +226,37 @@ def test_autotune_keeps_results(cuda_lib):
     fill_ghosts(fs, s)
     torch.cuda.synchronize()
     assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))
+
+
+def test_host_pipeline_equals_device_fill(cuda_lib):
+    """tam_fill_host through HostPipeline: states held in page-locked host
+    memory, filled three at a time on three streams, equal the device fill
+    bit for bit; in place and into a separate output."""
+    from treeamr.host import HostPipeline
+    f, fs, ops = meshes.sphere_setup(nvars=2, roots=4, levels=2)
+    s = GhostSchedule(fs, ops)
+    fs.work = fs.work.cuda()
+    fs.factors = fs.factors.cuda()
+    states = []
+    for k in range(5):
+        g = torch.Generator(device="cuda").manual_seed(40 + k)
+        states.append(torch.rand(fs.work.shape, dtype=fs.work.dtype, device="cuda", generator=g))
+    expect = []
+    for x in states:
+        fs.work.copy_(x)
+        fill_ghosts(fs, s)
+        expect.append(fs.work.clone())
+    pipe = HostPipeline(fs, s, depth=3)
+    ins = [x.cpu().pin_memory() for x in states]
+    outs = [torch.empty_like(h).pin_memory() for h in ins]
+    for k in range(5):
+        if k % 2:
+            pipe.submit(ins[k])                  # in place
+        else:
+            pipe.submit(ins[k], outs[k])
+    pipe.synchronize()
+    for k in range(5):
+        got = ins[k] if k % 2 else outs[k]
+        assert torch.equal(got.view(torch.int64), expect[k].cpu().view(torch.int64))
+    with pytest.raises(ValueError):
+        pipe.submit(ins[0][:1])

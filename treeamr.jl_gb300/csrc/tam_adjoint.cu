@@ -48,11 +48,17 @@ template <>
 struct AArith<double> {
   static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double fma(double a, double b, double c) {
+    return __fma_rn(a, b, c);
+  }
 };
 template <>
 struct AArith<float> {
   static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
   static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float fma(float a, float b, float c) {
+    return __fmaf_rn(a, b, c);
+  }
 };
 
 template <typename T>
@@ -65,46 +71,32 @@ struct AdjArgs {
   const int32_t *__restrict__ cls;
   const T *__restrict__ wtab;
   const int32_t *__restrict__ off;
-  const int32_t *__restrict__ ent;
+  const int2 *__restrict__ ent;
   const int64_t *__restrict__ scr;
 };
 
-// The weight of tap (m1, m2, m3) of target point (i1, i2, i3): exactly the
-// factor the forward fill multiplies that source value by.
-template <typename T, int D>
-__device__ __forceinline__ T tap_weight(const DevGroup &g, const AdjArgs<T> &a, int i1, int i2,
-                                        int i3, int m1, int m2, int m3) {
-  if (g.pclass == 0) return T(1);
-  if (g.pclass > 1) {
-    const int P = g.order[0];
-    const int P2 = D >= 2 ? P : 1, P3 = D >= 3 ? P : 1;
-    const int c1 = __ldg(a.cls + g.cls[0] + i1);
-    const int c2 = D >= 2 ? __ldg(a.cls + g.cls[1] + i2) : 0;
-    const int c3 = D >= 3 ? __ldg(a.cls + g.cls[2] + i3) : 0;
-    const int64_t base = g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * P * P2 * P3;
-    return __ldg(a.wtab + base + (m3 * P2 + m2) * P + m1);
-  }
-  using A = AArith<T>;
-  T w = __ldg(a.weights + g.w[0] + (int64_t)g.order[0] * i1 + m1);
-  if (D >= 2) w = A::mul(w, __ldg(a.weights + g.w[1] + (int64_t)g.order[1] * i2 + m2));
-  if (D >= 3) w = A::mul(w, __ldg(a.weights + g.w[2] + (int64_t)g.order[2] * i3 + m3));
-  return w;
-}
-
-// Pass 1: one warp per tile of one transfer's footprint points.
-template <typename T, int D>
+// Pass 1: one warp per tile of one transfer's footprint points.  Entry e of
+// dimension d's transposed stencil is (x, y): y the target row's element
+// offset along d, and x the weight's part -- for a product-table group the
+// row's class and the tap's offset in the table, so the table index of a
+// tap is the sum of its three x; otherwise the weight's index in the weight
+// pool, the three weights multiplied as ((w_1*w_2)*w_3), the factor the
+// forward fill applies.  A copy's weight is one.
+template <typename T, int D, int VC>
 __global__ void __launch_bounds__(256) adjoint_gather_kernel(
     const Tile *__restrict__ tiles, int64_t ntiles, AdjArgs<T> a, const T *y, T *scratch,
     const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
   const int lane = threadIdx.x & 31;
-  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
+  const int64_t vs = (int64_t)S1 * S2 * S3, bs = vs * nvars;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
        w += warps) {
     const Tile tile = tiles[w];
     const DevGroup &g = a.groups[tile.group];
     const AdjGroup &h = a.ag[tile.group];
+    const int pclass = g.pclass;
+    const T *__restrict__ W = pclass > 1 ? a.wtab + g.wtab : a.weights;
     const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
     T *out = scratch + __ldg(a.scr + tile.transfer) * nvars;
     const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
@@ -119,28 +111,51 @@ __global__ void __launch_bounds__(256) adjoint_gather_kernel(
       const int e2b = D >= 2 ? __ldg(a.off + h.off[1] + j2 + 1) : 1;
       const int e3a = D >= 3 ? __ldg(a.off + h.off[2] + j3) : 0;
       const int e3b = D >= 3 ? __ldg(a.off + h.off[2] + j3 + 1) : 1;
-      for (int v = 0; v < nvars; ++v) {
-        const T *yv = y + tblock * bs + v * vs;
-        T acc = T(0);
+      // VC variables at a time; the adjoint has no reference rounding to
+      // follow, so a tap is one fused multiply-add.
+      for (int v0 = 0; v0 < nvars; v0 += VC) {
+        const T *yv = y + tblock * bs + v0 * vs;
+        T acc[VC];
+#pragma unroll
+        for (int j = 0; j < VC; ++j) acc[j] = T(0);
         for (int e3 = e3a; e3 < e3b; ++e3) {
-          const int q3 = D >= 3 ? __ldg(a.ent + e3) : 0;
-          const int i3 = q3 >> 8, m3 = q3 & 0xFF;
+          const int2 q3 = D >= 3 ? __ldg(a.ent + e3) : make_int2(0, 0);
           for (int e2 = e2a; e2 < e2b; ++e2) {
-            const int q2 = D >= 2 ? __ldg(a.ent + e2) : 0;
-            const int i2 = q2 >> 8, m2 = q2 & 0xFF;
+            const int2 q2 = D >= 2 ? __ldg(a.ent + e2) : make_int2(0, 0);
+            const int x23 = q2.x + q3.x, t23 = q2.y + q3.y;
+            T w23 = T(1), w3 = T(1);
+            if (pclass < 0) {
+              w23 = D >= 2 ? __ldg(W + q2.x) : T(1);
+              w3 = D >= 3 ? __ldg(W + q3.x) : T(1);
+            }
             for (int e1 = e1a; e1 < e1b; ++e1) {
-              const int q1 = __ldg(a.ent + e1);
-              const int i1 = q1 >> 8, m1 = q1 & 0xFF;
-              const T wt = tap_weight<T, D>(g, a, i1, i2, i3, m1, m2, m3);
-              const T yt = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 +
-                              (int64_t)(g.tf[2] + i3) * s3];
-              acc = A::add(acc, A::mul(wt, yt));
+              const int2 q1 = __ldg(a.ent + e1);
+              T wt;
+              if (pclass > 1) {
+                wt = __ldg(W + q1.x + x23);
+              } else if (pclass == 0) {
+                wt = T(1);
+              } else {
+                wt = __ldg(W + q1.x);
+                if (D >= 2) wt = A::mul(wt, w23);
+                if (D >= 3) wt = A::mul(wt, w3);
+              }
+              const int t = q1.y + t23;
+#pragma unroll
+              for (int j = 0; j < VC; ++j)
+                if (v0 + j < nvars) acc[j] = A::fma(wt, yv[t + j * vs], acc[j]);
             }
           }
         }
-        // a factor of -1, 0 or 1 commutes with the rounded sum
-        if (g.factorcol) acc = A::mul(acc, __ldg(factors + v + (int64_t)nvars * (g.factorcol - 1)));
-        out[(int64_t)v * h.fsize + p] = acc;
+#pragma unroll
+        for (int j = 0; j < VC; ++j)
+          if (v0 + j < nvars) {
+            T r = acc[j];
+            // a factor of -1, 0 or 1 commutes with the rounded sum
+            if (g.factorcol)
+              r = A::mul(r, __ldg(factors + v0 + j + (int64_t)nvars * (g.factorcol - 1)));
+            out[(int64_t)(v0 + j) * h.fsize + p] = r;
+          }
       }
     }
   }
@@ -211,7 +226,7 @@ template <typename T>
 AdjArgs<T> adj_args(const tam_sched *s) {
   return AdjArgs<T>{s->d_groups,       s->d_adj_groups, s->d_tb,        s->d_sb,
                     (const T *)s->d_weights, s->d_cls,  (const T *)s->d_wtab, s->d_adj_off,
-                    s->d_adj_ent,      s->d_adj_scr};
+                    (const int2 *)s->d_adj_ent, s->d_adj_scr};
 }
 
 template <typename T, int D>
@@ -226,7 +241,7 @@ cudaError_t run_typed(tam_sched *s, T *y, int nvars, const T *factors, int32_t f
     const Stage &fw = s->stages[k];
     if (st.ntiles > 0) {
       const int64_t blocks = std::min<int64_t>((st.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
-      adjoint_gather_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
+      adjoint_gather_kernel<T, D, sizeof(T) == 8 ? 2 : 4><<<(unsigned)blocks, threads, 0, stream>>>(
           s->d_adj_tiles + st.tile0, st.ntiles, a, y, scratch, factors, nvars, s->S[0], s->S[1],
           s->S[2]);
       cudaError_t e = cudaGetLastError();
@@ -269,18 +284,27 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
   if (s->adj_ready) return TAM_OK;
   const int D = s->D;
   std::vector<AdjGroup> ag(s->groups.size());
-  std::vector<int32_t> off, ent;
+  std::vector<int32_t> off;
+  std::vector<int2> ent;
+  const int64_t stride[3] = {1, (int64_t)s->S[0], (int64_t)s->S[0] * s->S[1]};
   for (size_t gi = 0; gi < s->groups.size(); ++gi) {
     const tam_group &h = s->host_groups[gi];
+    const DevGroup &g = s->groups[gi];
     AdjGroup &a = ag[gi];
     a.fsize = 1;
+    // a product-table group: class and tap strides of the table per dimension
+    const int P = g.order[0];
+    const int64_t PD = (int64_t)P * (D >= 2 ? P : 1) * (D >= 3 ? P : 1);
+    const int64_t cstride[3] = {PD, PD * g.C[0], PD * g.C[0] * g.C[1]};
+    const int64_t mstride[3] = {1, P, (int64_t)P * P};
     for (int d = 0; d < 3; ++d) {
       if (d >= D) {
         a.flo[d] = 0;
         a.fn[d] = 1;
         a.off[d] = (int64_t)off.size();
         off.push_back((int32_t)ent.size());
-        ent.push_back(0);  // (i = 0, m = 0)
+        // one tap of weight one: class 0, tap 0, or the weight pool's pad one
+        ent.push_back(make_int2(g.pclass > 1 ? 0 : (int32_t)g.w[d], 0));
         off.push_back((int32_t)ent.size());
         continue;
       }
@@ -291,10 +315,6 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
         lo = std::min(lo, b);
         hi = std::max(hi, b + st.order - 1);
       }
-      if (st.ntarget >= (1 << 23) || st.order > 255) {
-        err = "a stencil too large for the adjoint's packed entries";
-        return TAM_EUNSUPPORTED;
-      }
       a.flo[d] = lo;
       a.fn[d] = hi - lo + 1;
       a.off[d] = (int64_t)off.size();
@@ -303,7 +323,16 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
         for (int i = 0; i < st.ntarget; ++i) {
           const int b = s->h_srcstart[st.srcstart + i] - 1;
           const int m = r - b;
-          if (m >= 0 && m < st.order) ent.push_back((i << 8) | m);
+          if (m < 0 || m >= st.order) continue;
+          const int64_t x = g.pclass > 1
+                                ? s->h_pool_cls[g.cls[d] + i] * cstride[d] + m * mstride[d]
+                                : g.w[d] + (int64_t)st.order * i + m;
+          const int64_t t = (int64_t)(g.tf[d] + i) * stride[d];
+          if (x > INT32_MAX || t > INT32_MAX) {
+            err = "a weight table or block too large for the adjoint's entries";
+            return TAM_EUNSUPPORTED;
+          }
+          ent.push_back(make_int2((int32_t)x, (int32_t)t));
         }
       }
       off.push_back((int32_t)ent.size());
@@ -373,7 +402,7 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
   }
   cudaError_t e;
   if ((e = up(&s->d_adj_groups, ag)) != cudaSuccess || (e = up(&s->d_adj_off, off)) != cudaSuccess ||
-      (e = up(&s->d_adj_ent, ent)) != cudaSuccess || (e = up(&s->d_adj_scr, scr)) != cudaSuccess ||
+      (e = up((int2 **)&s->d_adj_ent, ent)) != cudaSuccess || (e = up(&s->d_adj_scr, scr)) != cudaSuccess ||
       (e = up(&s->d_adj_tiles, tiles)) != cudaSuccess || (e = up(&s->d_adj_red, red)) != cudaSuccess ||
       (e = up((int2 **)&s->d_adj_list, list)) != cudaSuccess) {
     adjoint_free(s);
@@ -397,7 +426,8 @@ void adjoint_free(tam_sched *s) {
   cudaFree(s->d_adj_list);
   cudaFree(s->adj_scratch);
   s->d_adj_groups = nullptr;
-  s->d_adj_off = s->d_adj_ent = nullptr;
+  s->d_adj_off = nullptr;
+  s->d_adj_ent = nullptr;
   s->d_adj_scr = nullptr;
   s->d_adj_tiles = nullptr;
   s->d_adj_red = nullptr;

@@ -619,6 +619,27 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
   return TAM_OK;
 }
 
+int tam_fill_host(tam_sched *s, const void *host_in, void *host_out, void *device_work,
+                  int32_t nvars, int64_t nblocks, const void *factors, int32_t first_stage,
+                  int32_t last_stage, void *stream) {
+  if (!host_in || !host_out)
+    return fail(s ? s->ctx : nullptr, TAM_EINVAL, "tam_fill_host: NULL host buffer");
+  int rc = check_fill_args(s, device_work, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  const size_t bytes = (size_t)nblocks * nvars * s->S[0] * s->S[1] * s->S[2] *
+                       (s->dtype == TAM_F64 ? 8 : 4);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(device_work, host_in, bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "tam_fill_host upload");
+  rc = tam_fill(s, device_work, nvars, nblocks, factors, first_stage, last_stage, stream);
+  if (rc != TAM_OK) return rc;
+  e = cudaMemcpyAsync(host_out, device_work, bytes, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "tam_fill_host download");
+  return TAM_OK;
+}
+
 int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
                    int32_t first_stage, int32_t last_stage, void *stream) {
   int rc = check_fill_args(s, work, nvars, nblocks, factors);

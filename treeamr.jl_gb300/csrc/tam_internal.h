@@ -198,7 +198,7 @@ struct tam_sched {
   int64_t adj_scratch_points = 0;       // max over stages, per variable
   tam::AdjGroup *d_adj_groups = nullptr;
   int32_t *d_adj_off = nullptr;         // CSR row offsets
-  int32_t *d_adj_ent = nullptr;         // CSR entries
+  void *d_adj_ent = nullptr;            // CSR entries (int2: weight part, target offset)
   int64_t *d_adj_scr = nullptr;         // per transfer: scratch offset in points
   tam::Tile *d_adj_tiles = nullptr;
   tam::AdjReduce *d_adj_red = nullptr;

@@ -139,9 +139,16 @@ __device__ __forceinline__ Geom geometry(const DevGroup &g, int i1, int i2, int 
 // payload kept rather than made canonical; NaNs compare as one pattern).
 // Used for the F64 copies, which would otherwise queue on the GB300's narrow
 // FP64 pipe.
+// The halves are taken by an opaque move: a test of the bit pattern for +-0
+// is the same predicate as x == 0.0, which the compiler may otherwise turn
+// into a floating-point compare on the FP64 pipe.
 __device__ __forceinline__ double plus_zero(double x) {
-  const long long b = __double_as_longlong(x);
-  return b == (long long)0x8000000000000000ull ? 0.0 : x;
+  uint32_t lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+  const uint32_t zero = ((hi << 1) | lo) == 0u;  // +0 or -0
+  double r;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(r) : "r"(lo), "r"(hi & ~(zero << 31)));
+  return r;
 }
 __device__ __forceinline__ float plus_zero(float x) { return __fadd_rn(0.0f, x); }
 
@@ -318,7 +325,7 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
         };
 #pragma unroll 1
         for (int m3 = lo3; m3 < hi3; ++m3) {
-#pragma unroll(SKIP ? 1 : P2)
+#pragma unroll 1
           for (int m2 = lo2; m2 < hi2; ++m2) {
             if (SKIP && hi1 - lo1 == 1) {
               tap(lo1, m2, m3);
@@ -442,18 +449,22 @@ __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2,
                                               int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
   const bool skip = a.one_tap && g.perm >= 0;
+  // Float64 one variable at a time: the FP64 pipe binds, and the fewer
+  // registers a lane holds the more warps hide the loads' latency.
+  constexpr int VC = sizeof(T) == 8 ? 1 : 4;
   switch (g.pclass) {
     case 2:
-      table_dispatch<T, D, 2, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
+      table_dispatch<T, D, 2, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 3:
-      table_dispatch<T, D, 3, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
+      table_dispatch<T, D, 3, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 4:
-      table_dispatch<T, D, 4, 4>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
+      table_dispatch<T, D, 4, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
       break;
     case 6:
-      table_dispatch<T, D, 6, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
+      table_dispatch<T, D, 6, sizeof(T) == 8 ? 1 : 2>(g, i1, i2, i3, o, a, src, dst, factors,
+                                                      nvars, skip);
       break;
     default:
       generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
@@ -610,7 +621,7 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
 
 // The stencil tiles of a stage: one point a lane, every variable.
 template <typename T, int D, bool BATCH>
-__global__ void __launch_bounds__(512) fused_stage_kernel(const Tile *__restrict__ tiles,
+__global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tiles,
                                                           const PTile *__restrict__ ptiles,
                                                           int64_t nptiles, Args<T> a,
                                                           const T *__restrict__ src,

@@ -153,7 +153,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         os.makedirs(BUILD_DIR, exist_ok=True)
         srcs = [os.path.join(CSRC_DIR, s) for s in SOURCES]
         hdrs = [os.path.join(CSRC_DIR, "tam_internal.h"), os.path.join(INCLUDE_DIR, "treeamr_cuda.h")]
-        newest = max(os.path.getmtime(p) for p in srcs + hdrs)
+        newest = max(os.path.getmtime(p) for p in srcs + hdrs + [__file__])
         if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
             return LIB_PATH
         nvcc = _nvcc()
@@ -175,7 +175,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
             objs = list(ex.map(compile_one, srcs))
         tmp = LIB_PATH + ".tmp"
-        cmd = [nvcc, "-shared"] + ARCH_FLAGS + objs + ["-o", tmp]
+        # the shared CUDA runtime: the one the host process (torch) has loaded,
+        # so page-locked buffers it allocated are known to the library's copies
+        cmd = [nvcc, "-shared", "-cudart", "shared"] + ARCH_FLAGS + objs + ["-o", tmp]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
@@ -206,6 +208,8 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_fill_host.argtypes = [vp, vp, vp, vp, i32, i64, vp, i32, i32, vp]
+    lib.tam_fill_host.restype = C.c_int
     lib.tam_device_status.argtypes = [vp, vp, C.POINTER(i32)]
     lib.tam_selftest.argtypes = [vp, i32, i64, C.c_uint64, C.POINTER(i64)]
     lib.tam_adjoint_scratch_bytes.argtypes = [vp, i32, C.POINTER(C.c_size_t)]
