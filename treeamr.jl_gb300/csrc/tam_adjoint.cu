@@ -16,14 +16,24 @@
 // applied stage by stage in reverse.  A_s^T is formed in gather form, with
 // no atomics and a fixed order of summation, so the adjoint is deterministic:
 //
-//   pass 1  every transfer gathers, for each point of its source footprint,
-//           sum over its target points reading that point of
-//           w * (f * y[target]) into a scratch box of its own, through the
-//           per-dimension transposed stencils (CSR: source row -> (target
-//           row, tap)) and the forward fill's weight-product tables;
+//   pass 1  one CTA per transfer takes the transfer's target box of
+//           f * y[target] into shared memory and applies the transposed
+//           one-dimensional stencils one dimension at a time (CSR: source
+//           row -> (target row, weight)), leaving the box of its source
+//           footprint in a scratch box of its own.  The forward fill must
+//           sum the P^D taps of a point in the reference's order; its
+//           transpose has no reference rounding to follow, so the tensor
+//           product is applied as D passes of P taps each (3P multiply-adds
+//           a point instead of P^3 on the narrow FP64 pipe);
 //   pass 2  one CTA per source block adds the boxes of the transfers reading
 //           it, in transfer order, one transfer at a time;
 //   zero    the stage's target points are set to zero.
+//
+// The transpose differs from the exact transpose of the rounded forward
+// weights ((w_1*w_2)*w_3) by the rounding of the products, a few units in
+// the last place of each weight: the dot-product identity holds to the
+// sums' rounding.  A single weight (a unit vector y) comes out as
+// ((w_1*w_2)*w_3) exactly.
 //
 // The scratch is Sum over a stage's transfers of footprint x nvars elements
 // (tam_adjoint_scratch_bytes); the library owns one, or the caller passes
@@ -75,88 +85,77 @@ struct AdjArgs {
   const int64_t *__restrict__ scr;
 };
 
-// Pass 1: one warp per tile of one transfer's footprint points.  Entry e of
-// dimension d's transposed stencil is (x, y): y the target row's element
-// offset along d, and x the weight's part -- for a product-table group the
-// row's class and the tap's offset in the table, so the table index of a
-// tap is the sum of its three x; otherwise the weight's index in the weight
-// pool, the three weights multiplied as ((w_1*w_2)*w_3), the factor the
-// forward fill applies.  A copy's weight is one.
-template <typename T, int D, int VC>
-__global__ void __launch_bounds__(256) adjoint_gather_kernel(
-    const Tile *__restrict__ tiles, int64_t ntiles, AdjArgs<T> a, const T *y, T *scratch,
+// Pass 1: one CTA per transfer, the box passes in shared memory.  Entries of
+// dimension d's transposed stencil are (i, w): target row i, weight index w
+// into the weight pool; a dimension beyond D has one entry of weight one.
+// Per variable: A = f * y over the target box (n1 x n2 x n3, row 1 fastest),
+// B = T1 A (fn1 x n2 x n3), C = T2 B (fn1 x fn2 x n3), box = T3 C.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) adjoint_box_kernel(
+    const int2 *__restrict__ xfers, int64_t nxfers, AdjArgs<T> a, const T *y, T *scratch,
     const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
-  const int lane = threadIdx.x & 31;
-  const int64_t vs = (int64_t)S1 * S2 * S3, bs = vs * nvars;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
-       w += warps) {
-    const Tile tile = tiles[w];
-    const DevGroup &g = a.groups[tile.group];
-    const AdjGroup &h = a.ag[tile.group];
-    const int pclass = g.pclass;
-    const T *__restrict__ W = pclass > 1 ? a.wtab + g.wtab : a.weights;
-    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
-    T *out = scratch + __ldg(a.scr + tile.transfer) * nvars;
-    const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
-    for (int k = lane; k < tile.nitems; k += 32) {
-      const int p = tile.item0 + k;
-      const int j3 = p / f01;
-      const int r = p - j3 * f01;
-      const int j2 = r / f0;
-      const int j1 = r - j2 * f0;
-      const int e1a = __ldg(a.off + h.off[0] + j1), e1b = __ldg(a.off + h.off[0] + j1 + 1);
-      const int e2a = D >= 2 ? __ldg(a.off + h.off[1] + j2) : 0;
-      const int e2b = D >= 2 ? __ldg(a.off + h.off[1] + j2 + 1) : 1;
-      const int e3a = D >= 3 ? __ldg(a.off + h.off[2] + j3) : 0;
-      const int e3b = D >= 3 ? __ldg(a.off + h.off[2] + j3 + 1) : 1;
-      // VC variables at a time; the adjoint has no reference rounding to
-      // follow, so a tap is one fused multiply-add.
-      for (int v0 = 0; v0 < nvars; v0 += VC) {
-        const T *yv = y + tblock * bs + v0 * vs;
-        T acc[VC];
-#pragma unroll
-        for (int j = 0; j < VC; ++j) acc[j] = T(0);
-        for (int e3 = e3a; e3 < e3b; ++e3) {
-          const int2 q3 = D >= 3 ? __ldg(a.ent + e3) : make_int2(0, 0);
-          for (int e2 = e2a; e2 < e2b; ++e2) {
-            const int2 q2 = D >= 2 ? __ldg(a.ent + e2) : make_int2(0, 0);
-            const int x23 = q2.x + q3.x, t23 = q2.y + q3.y;
-            T w23 = T(1), w3 = T(1);
-            if (pclass < 0) {
-              w23 = D >= 2 ? __ldg(W + q2.x) : T(1);
-              w3 = D >= 3 ? __ldg(W + q3.x) : T(1);
-            }
-            for (int e1 = e1a; e1 < e1b; ++e1) {
-              const int2 q1 = __ldg(a.ent + e1);
-              T wt;
-              if (pclass > 1) {
-                wt = __ldg(W + q1.x + x23);
-              } else if (pclass == 0) {
-                wt = T(1);
-              } else {
-                wt = __ldg(W + q1.x);
-                if (D >= 2) wt = A::mul(wt, w23);
-                if (D >= 3) wt = A::mul(wt, w3);
-              }
-              const int t = q1.y + t23;
-#pragma unroll
-              for (int j = 0; j < VC; ++j)
-                if (v0 + j < nvars) acc[j] = A::fma(wt, yv[t + j * vs], acc[j]);
-            }
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < VC; ++j)
-          if (v0 + j < nvars) {
-            T r = acc[j];
-            // a factor of -1, 0 or 1 commutes with the rounded sum
-            if (g.factorcol)
-              r = A::mul(r, __ldg(factors + v0 + j + (int64_t)nvars * (g.factorcol - 1)));
-            out[(int64_t)(v0 + j) * h.fsize + p] = r;
-          }
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  T *SA = (T *)adj_smem;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int64_t q = blockIdx.x; q < nxfers; q += gridDim.x) {
+    const int2 tg = xfers[q];  // (transfer, group)
+    const DevGroup &g = a.groups[tg.y];
+    const AdjGroup &h = a.ag[tg.y];
+    const int n1 = g.n[0], n2 = g.n[1], n3 = g.n[2];
+    const int f1 = h.fn[0], f2 = h.fn[1], f3 = h.fn[2];
+    T *SB = SA + n1 * n2 * n3;
+    T *SC = SB + f1 * n2 * n3;
+    const int32_t *o1 = a.off + h.off[0], *o2 = a.off + h.off[1], *o3 = a.off + h.off[2];
+    const int64_t tblock = __ldg(a.tb + tg.x) - 1;
+    T *out = scratch + __ldg(a.scr + tg.x) * nvars;
+    const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
+    for (int v = 0; v < nvars; ++v) {
+      const T *yv = y + tblock * bs + v * vs;
+      const T f = g.factorcol ? __ldg(factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
+      for (int k = tid; k < nA; k += nt) {
+        const int i3 = k / (n1 * n2), r = k - i3 * (n1 * n2), i2 = r / n1, i1 = r - i2 * n1;
+        T x = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 + (int64_t)(g.tf[2] + i3) * s3];
+        // a factor of -1, 0 or 1 is exact here and commutes with the sums
+        if (g.factorcol) x = A::mul(x, f);
+        SA[k] = x;
       }
+      __syncthreads();
+      for (int k = tid; k < nB; k += nt) {  // B[(i3 n2 + i2) f1 + j1]
+        const int row = k / f1, j1 = k - row * f1;
+        const T *src = SA + row * n1;
+        T acc = T(0);
+        for (int e = __ldg(o1 + j1), e1 = __ldg(o1 + j1 + 1); e < e1; ++e) {
+          const int2 q1 = __ldg(a.ent + e);
+          acc = A::fma(__ldg(a.weights + q1.y), src[q1.x], acc);
+        }
+        SB[k] = acc;
+      }
+      __syncthreads();
+      for (int k = tid; k < nC; k += nt) {  // C[(i3 f2 + j2) f1 + j1]
+        const int i3 = k / (f1 * f2), r = k - i3 * (f1 * f2), j2 = r / f1, j1 = r - j2 * f1;
+        const T *src = SB + i3 * n2 * f1 + j1;
+        T acc = T(0);
+        for (int e = __ldg(o2 + j2), e1 = __ldg(o2 + j2 + 1); e < e1; ++e) {
+          const int2 q2 = __ldg(a.ent + e);
+          acc = A::fma(__ldg(a.weights + q2.y), src[q2.x * f1], acc);
+        }
+        SC[k] = acc;
+      }
+      __syncthreads();
+      T *ov = out + (int64_t)v * h.fsize;
+      for (int k = tid; k < nO; k += nt) {  // box[(j3 f2 + j2) f1 + j1]
+        const int j3 = k / (f1 * f2), r = k - j3 * (f1 * f2);
+        const T *src = SC + r;
+        T acc = T(0);
+        for (int e = __ldg(o3 + j3), e1 = __ldg(o3 + j3 + 1); e < e1; ++e) {
+          const int2 q3 = __ldg(a.ent + e);
+          acc = A::fma(__ldg(a.weights + q3.y), src[q3.x * f1 * f2], acc);
+        }
+        ov[k] = acc;
+      }
+      __syncthreads();
     }
   }
 }
@@ -240,10 +239,17 @@ cudaError_t run_typed(tam_sched *s, T *y, int nvars, const T *factors, int32_t f
     if (st.tag < first || st.tag > last) continue;
     const Stage &fw = s->stages[k];
     if (st.ntiles > 0) {
-      const int64_t blocks = std::min<int64_t>((st.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
-      adjoint_gather_kernel<T, D, sizeof(T) == 8 ? 2 : 4><<<(unsigned)blocks, threads, 0, stream>>>(
-          s->d_adj_tiles + st.tile0, st.ntiles, a, y, scratch, factors, nvars, s->S[0], s->S[1],
-          s->S[2]);
+      const size_t smem = (size_t)st.smem_elems * sizeof(T);
+      if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(adjoint_box_kernel<T, D>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+      }
+      const int64_t blocks = std::min<int64_t>(st.ntiles, (int64_t)1 << 30);
+      adjoint_box_kernel<T, D><<<(unsigned)blocks, 128, smem, stream>>>(
+          (const int2 *)s->d_adj_tiles + st.tile0, st.ntiles, a, y, scratch, factors, nvars,
+          s->S[0], s->S[1], s->S[2]);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -279,32 +285,25 @@ cudaError_t up(T **dst, const std::vector<T> &v) {
 
 }  // namespace
 
-// Build the transposed stencils, the pass-1 tiles and the pass-2 lists.
+// Build the transposed stencils, the pass-1 transfer lists and the pass-2 lists.
 int adjoint_prepare(tam_sched *s, std::string &err) {
   if (s->adj_ready) return TAM_OK;
   const int D = s->D;
   std::vector<AdjGroup> ag(s->groups.size());
   std::vector<int32_t> off;
   std::vector<int2> ent;
-  const int64_t stride[3] = {1, (int64_t)s->S[0], (int64_t)s->S[0] * s->S[1]};
   for (size_t gi = 0; gi < s->groups.size(); ++gi) {
     const tam_group &h = s->host_groups[gi];
     const DevGroup &g = s->groups[gi];
     AdjGroup &a = ag[gi];
     a.fsize = 1;
-    // a product-table group: class and tap strides of the table per dimension
-    const int P = g.order[0];
-    const int64_t PD = (int64_t)P * (D >= 2 ? P : 1) * (D >= 3 ? P : 1);
-    const int64_t cstride[3] = {PD, PD * g.C[0], PD * g.C[0] * g.C[1]};
-    const int64_t mstride[3] = {1, P, (int64_t)P * P};
     for (int d = 0; d < 3; ++d) {
       if (d >= D) {
         a.flo[d] = 0;
         a.fn[d] = 1;
         a.off[d] = (int64_t)off.size();
         off.push_back((int32_t)ent.size());
-        // one tap of weight one: class 0, tap 0, or the weight pool's pad one
-        ent.push_back(make_int2(g.pclass > 1 ? 0 : (int32_t)g.w[d], 0));
+        ent.push_back(make_int2(0, (int32_t)g.w[d]));  // the weight pool's pad one
         off.push_back((int32_t)ent.size());
         continue;
       }
@@ -324,15 +323,12 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
           const int b = s->h_srcstart[st.srcstart + i] - 1;
           const int m = r - b;
           if (m < 0 || m >= st.order) continue;
-          const int64_t x = g.pclass > 1
-                                ? s->h_pool_cls[g.cls[d] + i] * cstride[d] + m * mstride[d]
-                                : g.w[d] + (int64_t)st.order * i + m;
-          const int64_t t = (int64_t)(g.tf[d] + i) * stride[d];
-          if (x > INT32_MAX || t > INT32_MAX) {
-            err = "a weight table or block too large for the adjoint's entries";
+          const int64_t w = g.w[d] + (int64_t)st.order * i + m;
+          if (w > INT32_MAX) {
+            err = "a weight pool too large for the adjoint's entries";
             return TAM_EUNSUPPORTED;
           }
-          ent.push_back(make_int2((int32_t)x, (int32_t)t));
+          ent.push_back(make_int2(i, (int32_t)w));
         }
       }
       off.push_back((int32_t)ent.size());
@@ -346,16 +342,19 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
   // per stage: scratch offsets, tiles by target block, reduction lists by
   // source block
   std::vector<int64_t> scr(s->ntransfers, 0);
-  std::vector<Tile> tiles;
+  std::vector<int2> xfers;
   std::vector<AdjReduce> red;
   std::vector<int2> list;
   std::vector<AdjStage> stages;
   int64_t maxpts = 0;
-  const int ti = s->shape.tile_items;
+  int dev = 0, optin = 48 * 1024;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t smem_limit = (size_t)optin;
   for (const Stage &fw : s->stages) {
     AdjStage st;
     st.tag = fw.tag;
-    st.tile0 = (int64_t)tiles.size();
+    st.tile0 = (int64_t)xfers.size();
     st.red0 = (int64_t)red.size();
     struct E {
       int32_t tblock, sblock, group, transfer;
@@ -376,16 +375,24 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
     }
     st.scratch_points = pts;
     maxpts = std::max(maxpts, pts);
-    // pass-1 tiles by target block
+    // pass-1 transfers by target block; the shared memory of the largest box
     std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
       return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
     });
-    for (const E &e : es) {
-      const int64_t n = ag[e.group].fsize;
-      for (int64_t i0 = 0; i0 < n; i0 += ti)
-        tiles.push_back({e.group, e.transfer, (int32_t)i0, (int32_t)std::min<int64_t>(ti, n - i0)});
+    for (const E &e : es) xfers.push_back(make_int2(e.transfer, e.group));
+    st.ntiles = (int64_t)xfers.size() - st.tile0;
+    for (int32_t gi : fw.groups) {
+      const DevGroup &g = s->groups[gi];
+      const AdjGroup &a = ag[gi];
+      const int64_t n = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
+                        (int64_t)a.fn[0] * a.fn[1] * g.n[2];
+      st.smem_elems = std::max(st.smem_elems, n);
     }
-    st.ntiles = (int64_t)tiles.size() - st.tile0;
+    const size_t esz = s->dtype == TAM_F64 ? 8 : 4;
+    if ((size_t)st.smem_elems * esz > smem_limit) {
+      err = "a transfer box too large for the adjoint's shared memory";
+      return TAM_EUNSUPPORTED;
+    }
     // pass-2 lists by source block, transfers in transfer order
     std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) {
       return x.sblock != y.sblock ? x.sblock < y.sblock : x.transfer < y.transfer;
@@ -403,7 +410,7 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
   cudaError_t e;
   if ((e = up(&s->d_adj_groups, ag)) != cudaSuccess || (e = up(&s->d_adj_off, off)) != cudaSuccess ||
       (e = up((int2 **)&s->d_adj_ent, ent)) != cudaSuccess || (e = up(&s->d_adj_scr, scr)) != cudaSuccess ||
-      (e = up(&s->d_adj_tiles, tiles)) != cudaSuccess || (e = up(&s->d_adj_red, red)) != cudaSuccess ||
+      (e = up((int2 **)&s->d_adj_tiles, xfers)) != cudaSuccess || (e = up(&s->d_adj_red, red)) != cudaSuccess ||
       (e = up((int2 **)&s->d_adj_list, list)) != cudaSuccess) {
     adjoint_free(s);
     err = std::string("adjoint upload: ") + cudaGetErrorString(e);

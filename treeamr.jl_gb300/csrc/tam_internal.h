@@ -112,8 +112,8 @@ struct Stage {
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
 // dimension the footprint, the source rows the group's windows cover
 // (flo .. flo + fn - 1, 0-based stored indices), and for each footprint row
-// the (target row, tap) pairs that read it, in CSR form: entries
-// [off[r], off[r+1]) of the entry pool, each packed (i << 8) | m.
+// the target rows that read it with their weights, in CSR form: entries
+// [off[r], off[r+1]) of the entry pool, each (target row, weight index).
 struct AdjGroup {
   int32_t flo[3];
   int32_t fn[3];
@@ -121,11 +121,12 @@ struct AdjGroup {
   int64_t fsize;     // footprint points: fn[0] * fn[1] * fn[2]
 };
 
-// One stage of the adjoint: pass-1 tiles over the footprints of its
-// transfers, and the source blocks pass 2 reduces into.
+// One stage of the adjoint: its transfers for pass 1 (a CTA each), and the
+// source blocks pass 2 reduces into.
 struct AdjStage {
   int32_t tag;
-  int64_t tile0 = 0, ntiles = 0;  // into the adjoint tile array
+  int64_t tile0 = 0, ntiles = 0;  // into the pass-1 transfer list ((transfer, group) pairs)
+  int64_t smem_elems = 0;         // shared memory of pass 1, in elements
   int64_t red0 = 0, nred = 0;     // into the reduction block list
   int64_t scratch_points = 0;     // footprint points of the stage (per variable)
 };
@@ -200,7 +201,7 @@ struct tam_sched {
   int32_t *d_adj_off = nullptr;         // CSR row offsets
   void *d_adj_ent = nullptr;            // CSR entries (int2: weight part, target offset)
   int64_t *d_adj_scr = nullptr;         // per transfer: scratch offset in points
-  tam::Tile *d_adj_tiles = nullptr;
+  void *d_adj_tiles = nullptr;          // pass-1 transfers: (transfer, group) pairs
   tam::AdjReduce *d_adj_red = nullptr;
   int32_t *d_adj_list = nullptr;        // transfers of each reduction block
   void *adj_scratch = nullptr;          // owned scratch, grown on demand
