@@ -42,6 +42,35 @@ def test_batch_fill_equals_member_fills(cuda_lib):
     assert torch.equal(alone.view(torch.int32), batch.arena.view(torch.int32))
 
 
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+def test_batch_adjoint_equals_member_adjoints(cuda_lib, T):
+    """The batched adjoint (one launch per pass and stage for every forest)
+    equals each member's own adjoint bit for bit, and its transpose identity
+    holds against the oracle's forward fill of each member."""
+    from treeamr.adjoint import fill_ghosts_adjoint
+    fss, scheds, batch = _small_batch(T, n=5, seed=3)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    y = torch.rand(batch.arena.shape, dtype=batch.arena.dtype, device="cuda", generator=g)
+    got = y.clone()
+    batch.fill_adjoint(got)
+    alone = y.clone()
+    for m, (fs, s) in enumerate(zip(fss, scheds)):
+        view = batch.member_view(alone, m)
+        fill_ghosts_adjoint(fs, s, view)
+    torch.cuda.synchronize()
+    bits = torch.int64 if T == np.float64 else torch.int32
+    assert torch.equal(got.view(bits), alone.view(bits))
+    if T == np.float64:
+        rng = np.random.default_rng(2)
+        for m, (fs, s) in enumerate(zip(fss, scheds)):
+            x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+            ax = oracle.fill(s, x.copy(), fs.nvars, fs.factors_host)
+            ym = batch.member_view(y, m).cpu().numpy()
+            aty = batch.member_view(got, m).cpu().numpy()
+            lhs, rhs = float(np.dot(ax.ravel(), ym.ravel())), float(np.dot(x.ravel(), aty.ravel()))
+            assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+
+
 def test_batch_rejects_a_short_arena(cuda_lib):
     import ctypes as C
     from treeamr import _native

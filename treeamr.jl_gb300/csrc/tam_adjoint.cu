@@ -76,13 +76,36 @@ struct AdjArgs {
   const DevGroup *__restrict__ groups;
   const AdjGroup *__restrict__ ag;
   const int32_t *__restrict__ tb;
-  const int32_t *__restrict__ sb;
   const T *__restrict__ weights;
-  const int32_t *__restrict__ cls;
-  const T *__restrict__ wtab;
   const int32_t *__restrict__ off;
   const int2 *__restrict__ ent;
   const int64_t *__restrict__ scr;
+  const Member *__restrict__ members;  // a batch's, or null
+};
+
+// Where a transfer's field data and factors are: the kernel's own layout for
+// one schedule, or its member's in a batch of forests.
+template <typename T, bool BATCH>
+struct AdjLayout {
+  T *y;
+  const T *factors;
+  int64_t s2, s3, vs, bs;
+  __device__ __forceinline__ AdjLayout(const AdjArgs<T> &a, int member, T *y0, const T *f0,
+                                       int nvars, int S1, int S2, int S3)
+      : y(y0), factors(f0) {
+    if (BATCH) {
+      const Member &m = a.members[member];
+      y += m.work_off;
+      factors += m.fac_off;
+      S1 = m.S[0];
+      S2 = m.S[1];
+      S3 = m.S[2];
+    }
+    s2 = S1;
+    s3 = (int64_t)S1 * S2;
+    vs = s3 * S3;
+    bs = vs * nvars;
+  }
 };
 
 // Pass 1: one CTA per transfer, the box passes in shared memory.  Entries of
@@ -90,19 +113,19 @@ struct AdjArgs {
 // into the weight pool; a dimension beyond D has one entry of weight one.
 // Per variable: A = f * y over the target box (n1 x n2 x n3, row 1 fastest),
 // B = T1 A (fn1 x n2 x n3), C = T2 B (fn1 x fn2 x n3), box = T3 C.
-template <typename T, int D>
+template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_box_kernel(
-    const int2 *__restrict__ xfers, int64_t nxfers, AdjArgs<T> a, const T *y, T *scratch,
+    const int2 *__restrict__ xfers, int64_t nxfers, AdjArgs<T> a, T *y, T *scratch,
     const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
   extern __shared__ __align__(16) unsigned char adj_smem[];
   T *SA = (T *)adj_smem;
-  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int64_t q = blockIdx.x; q < nxfers; q += gridDim.x) {
     const int2 tg = xfers[q];  // (transfer, group)
     const DevGroup &g = a.groups[tg.y];
     const AdjGroup &h = a.ag[tg.y];
+    const AdjLayout<T, BATCH> L(a, g.member, y, factors, nvars, S1, S2, S3);
     const int n1 = g.n[0], n2 = g.n[1], n3 = g.n[2];
     const int f1 = h.fn[0], f2 = h.fn[1], f3 = h.fn[2];
     T *SB = SA + n1 * n2 * n3;
@@ -112,11 +135,12 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
     const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
     for (int v = 0; v < nvars; ++v) {
-      const T *yv = y + tblock * bs + v * vs;
-      const T f = g.factorcol ? __ldg(factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
+      const T *yv = L.y + tblock * L.bs + v * L.vs;
+      const T f =
+          g.factorcol ? __ldg(L.factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
       for (int k = tid; k < nA; k += nt) {
         const int i3 = k / (n1 * n2), r = k - i3 * (n1 * n2), i2 = r / n1, i1 = r - i2 * n1;
-        T x = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 + (int64_t)(g.tf[2] + i3) * s3];
+        T x = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 + (int64_t)(g.tf[2] + i3) * L.s3];
         // a factor of -1, 0 or 1 is exact here and commutes with the sums
         if (g.factorcol) x = A::mul(x, f);
         SA[k] = x;
@@ -161,15 +185,17 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
 }
 
 // Pass 2: one CTA per source block, its transfers' boxes added in order.
-template <typename T, int D>
+template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
     const AdjReduce *__restrict__ red, int64_t nred, const int2 *__restrict__ list,
     AdjArgs<T> a, T *y, const T *scratch, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
-  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
   for (int64_t b = blockIdx.x; b < nred; b += gridDim.x) {
     const AdjReduce r = red[b];
-    T *yb = y + (int64_t)r.sblock * bs;
+    // the transfers reading one block all belong to its forest
+    const int member = a.groups[list[r.first].y].member;
+    const AdjLayout<T, BATCH> L(a, member, y, nullptr, nvars, S1, S2, S3);
+    T *yb = L.y + (int64_t)r.sblock * L.bs;
     for (int q = 0; q < r.count; ++q) {
       const int2 tg = list[r.first + q];  // (transfer, group)
       const AdjGroup &h = a.ag[tg.y];
@@ -183,8 +209,8 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
         const int rr = pt - j3 * f01;
         const int j2 = rr / f0;
         const int j1 = rr - j2 * f0;
-        T *dst = yb + v * vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * s2 +
-                 (int64_t)(h.flo[2] + j3) * s3;
+        T *dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
+                 (int64_t)(h.flo[2] + j3) * L.s3;
         *dst = A::add(*dst, src[p]);
       }
       __syncthreads();
@@ -193,20 +219,18 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
 }
 
 // Zero the targets of a stage: the forward tiles of the stage.
-template <typename T, int D>
+template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restrict__ tiles,
-                                                           int64_t ntiles,
-                                                           const DevGroup *__restrict__ groups,
-                                                           const int32_t *__restrict__ tb, T *y,
+                                                           int64_t ntiles, AdjArgs<T> a, T *y,
                                                            int nvars, int S1, int S2, int S3) {
   const int lane = threadIdx.x & 31;
-  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3, bs = vs * nvars;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
        w += warps) {
     const Tile tile = tiles[w];
-    const DevGroup &g = groups[tile.group];
-    const int64_t tblock = __ldg(tb + tile.transfer) - 1;
+    const DevGroup &g = a.groups[tile.group];
+    const AdjLayout<T, BATCH> L(a, g.member, y, nullptr, nvars, S1, S2, S3);
+    const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
     const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
     for (int k = lane; k < tile.nitems; k += 32) {
       const int item = tile.item0 + k;
@@ -214,63 +238,72 @@ __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restric
       const int rem = item - i3 * n12;
       const int i2 = rem / n1;
       const int i1 = rem - i2 * n1;
-      const int64_t o = tblock * bs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 +
-                        (int64_t)(g.tf[2] + i3) * s3;
-      for (int v = 0; v < nvars; ++v) y[o + v * vs] = T(0);
+      const int64_t o = tblock * L.bs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
+                        (int64_t)(g.tf[2] + i3) * L.s3;
+      for (int v = 0; v < nvars; ++v) L.y[o + v * L.vs] = T(0);
     }
   }
 }
 
-template <typename T>
-AdjArgs<T> adj_args(const tam_sched *s) {
-  return AdjArgs<T>{s->d_groups,       s->d_adj_groups, s->d_tb,        s->d_sb,
-                    (const T *)s->d_weights, s->d_cls,  (const T *)s->d_wtab, s->d_adj_off,
-                    (const int2 *)s->d_adj_ent, s->d_adj_scr};
-}
-
-template <typename T, int D>
-cudaError_t run_typed(tam_sched *s, T *y, int nvars, const T *factors, int32_t first,
-                      int32_t last, T *scratch, cudaStream_t stream) {
-  const AdjArgs<T> a = adj_args<T>(s);
+template <typename T, int D, bool BATCH>
+cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const T *factors,
+                      int32_t first, int32_t last, T *scratch, cudaStream_t stream) {
+  const AdjArgs<T> a{r.groups, p.groups, r.tb, (const T *)r.weights,
+                     p.off,    (const int2 *)p.ent, p.scr, r.members};
+  const int S1 = r.S[0], S2 = r.S[1], S3 = r.S[2];
   const int threads = 256, wpb = threads / 32;
   // stages in reverse order
-  for (int k = (int)s->adj_stages.size() - 1; k >= 0; --k) {
-    const AdjStage &st = s->adj_stages[k];
+  for (int k = (int)p.stages.size() - 1; k >= 0; --k) {
+    const AdjStage &st = p.stages[k];
     if (st.tag < first || st.tag > last) continue;
-    const Stage &fw = s->stages[k];
+    const Stage &fw = (*r.fwd_stages)[k];
     if (st.ntiles > 0) {
       const size_t smem = (size_t)st.smem_elems * sizeof(T);
       if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(adjoint_box_kernel<T, D>,
+        cudaError_t e = cudaFuncSetAttribute(adjoint_box_kernel<T, D, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
       }
       const int64_t blocks = std::min<int64_t>(st.ntiles, (int64_t)1 << 30);
-      adjoint_box_kernel<T, D><<<(unsigned)blocks, 128, smem, stream>>>(
-          (const int2 *)s->d_adj_tiles + st.tile0, st.ntiles, a, y, scratch, factors, nvars,
-          s->S[0], s->S[1], s->S[2]);
+      adjoint_box_kernel<T, D, BATCH><<<(unsigned)blocks, 128, smem, stream>>>(
+          (const int2 *)p.xfers + st.tile0, st.ntiles, a, y, scratch, factors, nvars, S1, S2,
+          S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
     if (st.nred > 0) {
       const int64_t blocks = std::min<int64_t>(st.nred, (int64_t)1 << 30);
-      adjoint_reduce_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
-          s->d_adj_red + st.red0, st.nred, (const int2 *)s->d_adj_list, a, y, scratch, nvars,
-          s->S[0], s->S[1], s->S[2]);
+      adjoint_reduce_kernel<T, D, BATCH><<<(unsigned)blocks, threads, 0, stream>>>(
+          p.red + st.red0, st.nred, (const int2 *)p.list, a, y, scratch, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
     if (fw.ntiles > 0) {
       const int64_t blocks = std::min<int64_t>((fw.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
-      adjoint_zero_kernel<T, D><<<(unsigned)blocks, threads, 0, stream>>>(
-          s->d_tiles + fw.tile0, fw.ntiles, s->d_groups, s->d_tb, y, nvars, s->S[0], s->S[1],
-          s->S[2]);
+      adjoint_zero_kernel<T, D, BATCH><<<(unsigned)blocks, threads, 0, stream>>>(
+          r.fwd_tiles + fw.tile0, fw.ntiles, a, y, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
   }
   return cudaSuccess;
+}
+
+template <typename T, bool BATCH>
+cudaError_t run_dim(const AdjPlan &p, const AdjRun &r, void *y, int nvars, const void *factors,
+                    int32_t first, int32_t last, void *scratch, cudaStream_t stream) {
+  switch (r.D) {
+    case 1:
+      return run_typed<T, 1, BATCH>(p, r, (T *)y, nvars, (const T *)factors, first, last,
+                                    (T *)scratch, stream);
+    case 2:
+      return run_typed<T, 2, BATCH>(p, r, (T *)y, nvars, (const T *)factors, first, last,
+                                    (T *)scratch, stream);
+    default:
+      return run_typed<T, 3, BATCH>(p, r, (T *)y, nvars, (const T *)factors, first, last,
+                                    (T *)scratch, stream);
+  }
 }
 
 template <typename T>
@@ -283,28 +316,44 @@ cudaError_t up(T **dst, const std::vector<T> &v) {
   return cudaSuccess;
 }
 
-}  // namespace
-
-// Build the transposed stencils, the pass-1 transfer lists and the pass-2 lists.
-int adjoint_prepare(tam_sched *s, std::string &err) {
-  if (s->adj_ready) return TAM_OK;
-  const int D = s->D;
-  std::vector<AdjGroup> ag(s->groups.size());
+// The plan of one schedule on the host.
+struct AdjHost {
+  std::vector<AdjGroup> ag;
   std::vector<int32_t> off;
   std::vector<int2> ent;
+  std::vector<int64_t> scr;      // per transfer
+  std::vector<int2> xfers;       // per stage, by target block
+  std::vector<AdjReduce> red;
+  std::vector<int2> list;
+  std::vector<AdjStage> stages;  // one per forward stage
+  int64_t maxpts = 0;
+};
+
+size_t smem_limit() {
+  int dev = 0, optin = 48 * 1024;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return (size_t)optin;
+}
+
+// The transposed stencils, the pass-1 transfer lists and the pass-2 lists of
+// one schedule.
+int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
+  const int D = s->D;
+  o.ag.assign(s->groups.size(), AdjGroup{});
   for (size_t gi = 0; gi < s->groups.size(); ++gi) {
     const tam_group &h = s->host_groups[gi];
     const DevGroup &g = s->groups[gi];
-    AdjGroup &a = ag[gi];
+    AdjGroup &a = o.ag[gi];
     a.fsize = 1;
     for (int d = 0; d < 3; ++d) {
       if (d >= D) {
         a.flo[d] = 0;
         a.fn[d] = 1;
-        a.off[d] = (int64_t)off.size();
-        off.push_back((int32_t)ent.size());
-        ent.push_back(make_int2(0, (int32_t)g.w[d]));  // the weight pool's pad one
-        off.push_back((int32_t)ent.size());
+        a.off[d] = (int64_t)o.off.size();
+        o.off.push_back((int32_t)o.ent.size());
+        o.ent.push_back(make_int2(0, (int32_t)g.w[d]));  // the weight pool's pad one
+        o.off.push_back((int32_t)o.ent.size());
         continue;
       }
       const tam_stencil &st = h.stencil[d];
@@ -316,9 +365,9 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
       }
       a.flo[d] = lo;
       a.fn[d] = hi - lo + 1;
-      a.off[d] = (int64_t)off.size();
+      a.off[d] = (int64_t)o.off.size();
       for (int r = lo; r <= hi; ++r) {
-        off.push_back((int32_t)ent.size());
+        o.off.push_back((int32_t)o.ent.size());
         for (int i = 0; i < st.ntarget; ++i) {
           const int b = s->h_srcstart[st.srcstart + i] - 1;
           const int m = r - b;
@@ -328,34 +377,23 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
             err = "a weight pool too large for the adjoint's entries";
             return TAM_EUNSUPPORTED;
           }
-          ent.push_back(make_int2(i, (int32_t)w));
+          o.ent.push_back(make_int2(i, (int32_t)w));
         }
       }
-      off.push_back((int32_t)ent.size());
+      o.off.push_back((int32_t)o.ent.size());
       a.fsize *= a.fn[d];
     }
-    if (ent.size() > (size_t)INT32_MAX) {
+    if (o.ent.size() > (size_t)INT32_MAX) {
       err = "the adjoint's transposed stencils exceed 2^31 entries";
       return TAM_EUNSUPPORTED;
     }
   }
-  // per stage: scratch offsets, tiles by target block, reduction lists by
-  // source block
-  std::vector<int64_t> scr(s->ntransfers, 0);
-  std::vector<int2> xfers;
-  std::vector<AdjReduce> red;
-  std::vector<int2> list;
-  std::vector<AdjStage> stages;
-  int64_t maxpts = 0;
-  int dev = 0, optin = 48 * 1024;
-  if (cudaGetDevice(&dev) == cudaSuccess)
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t smem_limit = (size_t)optin;
+  o.scr.assign(s->ntransfers, 0);
   for (const Stage &fw : s->stages) {
     AdjStage st;
     st.tag = fw.tag;
-    st.tile0 = (int64_t)xfers.size();
-    st.red0 = (int64_t)red.size();
+    st.tile0 = (int64_t)o.xfers.size();
+    st.red0 = (int64_t)o.red.size();
     struct E {
       int32_t tblock, sblock, group, transfer;
     };
@@ -370,28 +408,23 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
     std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) { return x.transfer < y.transfer; });
     int64_t pts = 0;
     for (const E &e : byt) {
-      scr[e.transfer] = pts;
-      pts += ag[e.group].fsize;
+      o.scr[e.transfer] = pts;
+      pts += o.ag[e.group].fsize;
     }
     st.scratch_points = pts;
-    maxpts = std::max(maxpts, pts);
+    o.maxpts = std::max(o.maxpts, pts);
     // pass-1 transfers by target block; the shared memory of the largest box
     std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
       return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
     });
-    for (const E &e : es) xfers.push_back(make_int2(e.transfer, e.group));
-    st.ntiles = (int64_t)xfers.size() - st.tile0;
+    for (const E &e : es) o.xfers.push_back(make_int2(e.transfer, e.group));
+    st.ntiles = (int64_t)o.xfers.size() - st.tile0;
     for (int32_t gi : fw.groups) {
       const DevGroup &g = s->groups[gi];
-      const AdjGroup &a = ag[gi];
+      const AdjGroup &a = o.ag[gi];
       const int64_t n = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
                         (int64_t)a.fn[0] * a.fn[1] * g.n[2];
       st.smem_elems = std::max(st.smem_elems, n);
-    }
-    const size_t esz = s->dtype == TAM_F64 ? 8 : 4;
-    if ((size_t)st.smem_elems * esz > smem_limit) {
-      err = "a transfer box too large for the adjoint's shared memory";
-      return TAM_EUNSUPPORTED;
     }
     // pass-2 lists by source block, transfers in transfer order
     std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) {
@@ -400,48 +433,164 @@ int adjoint_prepare(tam_sched *s, std::string &err) {
     for (size_t i = 0; i < byt.size();) {
       size_t j = i;
       while (j < byt.size() && byt[j].sblock == byt[i].sblock) ++j;
-      red.push_back({byt[i].sblock - 1, (int32_t)(j - i), (int64_t)list.size()});
-      for (size_t k = i; k < j; ++k) list.push_back(make_int2(byt[k].transfer, byt[k].group));
+      o.red.push_back({byt[i].sblock - 1, (int32_t)(j - i), (int64_t)o.list.size()});
+      for (size_t k = i; k < j; ++k) o.list.push_back(make_int2(byt[k].transfer, byt[k].group));
       i = j;
     }
-    st.nred = (int64_t)red.size() - st.red0;
-    stages.push_back(st);
+    st.nred = (int64_t)o.red.size() - st.red0;
+    o.stages.push_back(st);
   }
-  cudaError_t e;
-  if ((e = up(&s->d_adj_groups, ag)) != cudaSuccess || (e = up(&s->d_adj_off, off)) != cudaSuccess ||
-      (e = up((int2 **)&s->d_adj_ent, ent)) != cudaSuccess || (e = up(&s->d_adj_scr, scr)) != cudaSuccess ||
-      (e = up((int2 **)&s->d_adj_tiles, xfers)) != cudaSuccess || (e = up(&s->d_adj_red, red)) != cudaSuccess ||
-      (e = up((int2 **)&s->d_adj_list, list)) != cudaSuccess) {
-    adjoint_free(s);
-    err = std::string("adjoint upload: ") + cudaGetErrorString(e);
-    return e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA;
-  }
-  s->adj_groups = std::move(ag);
-  s->adj_stages = std::move(stages);
-  s->adj_scratch_points = maxpts;
-  s->adj_ready = true;
   return TAM_OK;
 }
 
+int upload_plan(AdjPlan &p, const AdjHost &o, int dtype, std::string &err) {
+  const size_t esz = dtype == TAM_F64 ? 8 : 4, limit = smem_limit();
+  for (const AdjStage &st : o.stages)
+    if ((size_t)st.smem_elems * esz > limit) {
+      err = "a transfer box too large for the adjoint's shared memory";
+      return TAM_EUNSUPPORTED;
+    }
+  cudaError_t e;
+  if ((e = up(&p.groups, o.ag)) != cudaSuccess || (e = up(&p.off, o.off)) != cudaSuccess ||
+      (e = up((int2 **)&p.ent, o.ent)) != cudaSuccess || (e = up(&p.scr, o.scr)) != cudaSuccess ||
+      (e = up((int2 **)&p.xfers, o.xfers)) != cudaSuccess || (e = up(&p.red, o.red)) != cudaSuccess ||
+      (e = up((int2 **)&p.list, o.list)) != cudaSuccess) {
+    adjoint_plan_free(p);
+    err = std::string("adjoint upload: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA;
+  }
+  p.stages = o.stages;
+  p.scratch_points = o.maxpts;
+  p.ready = true;
+  return TAM_OK;
+}
+
+}  // namespace
+
+void adjoint_plan_free(AdjPlan &p) {
+  cudaFree(p.groups);
+  cudaFree(p.off);
+  cudaFree(p.ent);
+  cudaFree(p.scr);
+  cudaFree(p.xfers);
+  cudaFree(p.red);
+  cudaFree(p.list);
+  p = AdjPlan{};
+}
+
+int adjoint_prepare(tam_sched *s, std::string &err) {
+  if (s->adj.ready) return TAM_OK;
+  AdjHost o;
+  int rc = adjoint_build(s, o, err);
+  if (rc != TAM_OK) return rc;
+  return upload_plan(s->adj, o, s->dtype, err);
+}
+
+// Concatenate the members' plans: indices into groups, transfers, weights,
+// CSR rows and entries and the reduction lists move by each member's bases;
+// per stage tag the members' transfers follow one another, and so do their
+// scratch boxes.
+int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members,
+                          const std::vector<int64_t> &group_base,
+                          const std::vector<int64_t> &transfer_base,
+                          const std::vector<int64_t> &weight_base,
+                          const std::vector<Stage> &stages, std::string &err) {
+  if (plan.ready) return TAM_OK;
+  const int dtype = members.empty() ? TAM_F64 : members[0]->dtype;
+  std::vector<AdjHost> hs(members.size());
+  AdjHost o;
+  std::vector<int64_t> list_base(members.size());
+  for (size_t m = 0; m < members.size(); ++m) {
+    int rc = adjoint_build(members[m], hs[m], err);
+    if (rc != TAM_OK) return rc;
+    const AdjHost &h = hs[m];
+    const int64_t off0 = (int64_t)o.off.size(), ent0 = (int64_t)o.ent.size();
+    for (AdjGroup a : h.ag) {
+      for (int d = 0; d < 3; ++d) a.off[d] += off0;
+      o.ag.push_back(a);
+    }
+    for (int32_t v : h.off) o.off.push_back((int32_t)(v + ent0));
+    for (int2 e : h.ent) {
+      const int64_t w = e.y + weight_base[m];
+      if (w > INT32_MAX) {
+        err = "the batch's weight pool is too large for the adjoint's entries";
+        return TAM_EUNSUPPORTED;
+      }
+      o.ent.push_back(make_int2(e.x, (int32_t)w));
+    }
+    if (o.ent.size() > (size_t)INT32_MAX || o.off.size() > (size_t)INT32_MAX) {
+      err = "the batch's transposed stencils exceed 2^31 entries";
+      return TAM_EUNSUPPORTED;
+    }
+  }
+  int64_t ntransfers = 0;
+  for (size_t m = 0; m < members.size(); ++m)
+    ntransfers = std::max<int64_t>(ntransfers, transfer_base[m] + members[m]->ntransfers);
+  o.scr.assign(ntransfers, 0);
+  for (const Stage &fw : stages) {
+    AdjStage st;
+    st.tag = fw.tag;
+    st.tile0 = (int64_t)o.xfers.size();
+    st.red0 = (int64_t)o.red.size();
+    int64_t base = 0;
+    for (size_t m = 0; m < members.size(); ++m) {
+      const AdjHost &h = hs[m];
+      const tam_sched *s = members[m];
+      size_t k = 0;
+      while (k < s->stages.size() && s->stages[k].tag != fw.tag) ++k;
+      if (k == s->stages.size()) continue;
+      const AdjStage &ms = h.stages[k];
+      const int32_t G0 = (int32_t)group_base[m], T0 = (int32_t)transfer_base[m];
+      for (int64_t i = ms.tile0; i < ms.tile0 + ms.ntiles; ++i) {
+        const int2 x = h.xfers[i];
+        o.xfers.push_back(make_int2(x.x + T0, x.y + G0));
+        o.scr[x.x + T0] = base + h.scr[x.x];
+      }
+      for (int64_t i = ms.red0; i < ms.red0 + ms.nred; ++i) {
+        AdjReduce r = h.red[i];
+        const int64_t first = (int64_t)o.list.size();
+        for (int32_t q = 0; q < r.count; ++q) {
+          const int2 x = h.list[r.first + q];
+          o.list.push_back(make_int2(x.x + T0, x.y + G0));
+        }
+        r.first = first;
+        o.red.push_back(r);
+      }
+      base += ms.scratch_points;
+      st.smem_elems = std::max(st.smem_elems, ms.smem_elems);
+    }
+    st.ntiles = (int64_t)o.xfers.size() - st.tile0;
+    st.nred = (int64_t)o.red.size() - st.red0;
+    st.scratch_points = base;
+    o.maxpts = std::max(o.maxpts, base);
+    o.stages.push_back(st);
+  }
+  return upload_plan(plan, o, dtype, err);
+}
+
 void adjoint_free(tam_sched *s) {
-  cudaFree(s->d_adj_groups);
-  cudaFree(s->d_adj_off);
-  cudaFree(s->d_adj_ent);
-  cudaFree(s->d_adj_scr);
-  cudaFree(s->d_adj_tiles);
-  cudaFree(s->d_adj_red);
-  cudaFree(s->d_adj_list);
+  adjoint_plan_free(s->adj);
   cudaFree(s->adj_scratch);
-  s->d_adj_groups = nullptr;
-  s->d_adj_off = nullptr;
-  s->d_adj_ent = nullptr;
-  s->d_adj_scr = nullptr;
-  s->d_adj_tiles = nullptr;
-  s->d_adj_red = nullptr;
-  s->d_adj_list = nullptr;
   s->adj_scratch = nullptr;
   s->adj_scratch_bytes = 0;
-  s->adj_ready = false;
+}
+
+cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,
+                             const void *factors, int32_t first, int32_t last, void *scratch,
+                             cudaStream_t stream) {
+  const bool batch = r.members != nullptr;
+  if (r.dtype == TAM_F64)
+    return batch ? run_dim<double, true>(plan, r, y, nvars, factors, first, last, scratch, stream)
+                 : run_dim<double, false>(plan, r, y, nvars, factors, first, last, scratch, stream);
+  return batch ? run_dim<float, true>(plan, r, y, nvars, factors, first, last, scratch, stream)
+               : run_dim<float, false>(plan, r, y, nvars, factors, first, last, scratch, stream);
+}
+
+cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
+                        int32_t last, void *scratch, cudaStream_t stream) {
+  AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
+           &s->stages, {s->S[0], s->S[1], s->S[2]}};
+  return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
 }
 
 }  // namespace tam
@@ -479,12 +628,12 @@ extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int
     ctx->err = "tam_fill_adjoint_static: this schedule mirrors ghosts and needs the factor table";
     return TAM_EINVAL;
   }
-  if (!s->adj_ready) {
+  if (!s->adj.ready) {
     ctx->err = "tam_fill_adjoint_static: the schedule's transposed stencils are not built; "
                "call tam_adjoint_scratch_bytes once first (it allocates)";
     return TAM_EINVAL;
   }
-  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > TAM_STATIC_SCRATCH_BYTES) {
     ctx->err = "tam_fill_adjoint_static: this schedule's adjoint needs " + std::to_string(need) +
                " bytes of scratch for " + std::to_string(nvars) +
@@ -532,23 +681,3 @@ extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int
   }
   return TAM_OK;
 }
-
-namespace tam {
-
-cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
-                        int32_t last, void *scratch, cudaStream_t stream) {
-  if (s->dtype == TAM_F64) {
-    switch (s->D) {
-      case 1: return run_typed<double, 1>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
-      case 2: return run_typed<double, 2>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
-      default: return run_typed<double, 3>(s, (double *)y, nvars, (const double *)factors, first, last, (double *)scratch, stream);
-    }
-  }
-  switch (s->D) {
-    case 1: return run_typed<float, 1>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
-    case 2: return run_typed<float, 2>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
-    default: return run_typed<float, 3>(s, (float *)y, nvars, (const float *)factors, first, last, (float *)scratch, stream);
-  }
-}
-
-}  // namespace tam

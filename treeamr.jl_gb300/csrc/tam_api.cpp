@@ -515,7 +515,7 @@ void tam_schedule_free(tam_sched *s) {
 }
 
 static int adjoint_ready(tam_sched *s) {
-  if (s->adj_ready) return TAM_OK;
+  if (s->adj.ready) return TAM_OK;
   std::string err;
   int rc = tam::adjoint_prepare(s, err);
   if (rc != TAM_OK) return fail(s->ctx, rc, err);
@@ -528,7 +528,7 @@ int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes) {
   DeviceGuard guard(s->ctx->device);
   int rc = adjoint_ready(s);
   if (rc != TAM_OK) return rc;
-  *bytes = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  *bytes = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   return TAM_OK;
 }
 
@@ -544,7 +544,7 @@ int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nbloc
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
   rc = adjoint_ready(s);
   if (rc != TAM_OK) return rc;
-  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > 0 && (!scratch || scratch_bytes < need))
     return fail(s->ctx, TAM_EINVAL, "adjoint scratch smaller than tam_adjoint_scratch_bytes");
   cudaError_t e =
@@ -561,7 +561,7 @@ int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, cons
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
   rc = adjoint_ready(s);
   if (rc != TAM_OK) return rc;
-  const size_t need = (size_t)s->adj_scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
+  const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > s->adj_scratch_bytes) {
     // grown only between fills: wait for any fill still using the old one
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);

@@ -39,6 +39,12 @@ struct tam_batch {
   tam::PTile *d_ptiles = nullptr;
   tam::Member *d_members = nullptr;
   tam::SideStream side;
+  // each member's first group, transfer and weight in the concatenated arrays
+  std::vector<int64_t> group_base, transfer_base, weight_base;
+  // the batched adjoint, prepared on first use
+  tam::AdjPlan adj;
+  void *adj_scratch = nullptr;
+  size_t adj_scratch_bytes = 0;
 };
 
 namespace {
@@ -83,6 +89,10 @@ void free_batch_device(tam_batch *b) {
   cudaFree(b->d_members);
   cudaFree(b->d_csingle);
   cudaFree(b->d_perm);
+  tam::adjoint_plan_free(b->adj);
+  cudaFree(b->adj_scratch);
+  b->adj_scratch = nullptr;
+  b->adj_scratch_bytes = 0;
   tam::side_destroy(b->side);
   b->d_ptiles = nullptr;
   b->d_groups = nullptr;
@@ -193,6 +203,9 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     const int64_t ss0 = (int64_t)srcstart.size(), c0 = (int64_t)cls.size();
     const int64_t cs0 = (int64_t)csingle.size(), p0 = (int64_t)perm.size();
     const int64_t w0 = (int64_t)(weights.size() / esz), wt0 = (int64_t)(wtab.size() / esz);
+    b->group_base.push_back(g0);
+    b->transfer_base.push_back(t0);
+    b->weight_base.push_back(w0);
     for (const tam::DevGroup &h : s->groups) {
       tam::DevGroup g = h;
       for (int k = 0; k < 3; ++k) {
@@ -301,18 +314,36 @@ int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32
     return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_fill_adjoint: NULL argument");
   int rc = check_arena(b, arena_elems, nvars, factor_arena, factor_elems);
   if (rc != TAM_OK) return rc;
-  const size_t esz = b->dtype == TAM_F64 ? 8 : 4;
-  for (size_t m = 0; m < b->members.size(); ++m) {
-    tam_sched *s = b->members[m];
-    unsigned char *y = (unsigned char *)arena + (size_t)b->layout[m].work_off * esz;
-    const unsigned char *f =
-        factor_arena ? (const unsigned char *)factor_arena + (size_t)b->layout[m].fac_off * esz
-                     : nullptr;
-    rc = tam_fill_adjoint(s, y, nvars, s->nblocks, f, first_stage, last_stage, stream);
-    if (rc != TAM_OK) {
-      b->ctx->err = "member " + std::to_string(m) + ": " + s->ctx->err;
-      return rc;
+  Guard guard(b->ctx->device);
+  if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
+  if (!b->adj.ready) {
+    std::string err;
+    rc = tam::adjoint_prepare_batch(b->adj, b->members, b->group_base, b->transfer_base,
+                                    b->weight_base, b->stages, err);
+    if (rc != TAM_OK) return bfail(b->ctx, rc, "tam_batch_fill_adjoint: " + err);
+  }
+  const size_t need = (size_t)b->adj.scratch_points * nvars * (b->dtype == TAM_F64 ? 8 : 4);
+  if (need > b->adj_scratch_bytes) {
+    // grown only between fills: wait for any fill still using the old one
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+      return bfail(b->ctx, TAM_ECUDA, std::string("batch adjoint: ") + cudaGetErrorString(e));
+    cudaFree(b->adj_scratch);
+    b->adj_scratch = nullptr;
+    b->adj_scratch_bytes = 0;
+    if (cudaMalloc(&b->adj_scratch, need) != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b->ctx, TAM_ENOMEM, "batch adjoint: scratch allocation failed");
     }
+    b->adj_scratch_bytes = need;
+  }
+  const tam::AdjRun r{b->dtype, b->D, b->d_groups, b->d_tb, b->d_weights, b->d_members,
+                      b->d_tiles, &b->stages, {1, 1, 1}};
+  cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena, first_stage,
+                                        last_stage, b->adj_scratch, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b->ctx, TAM_ECUDA, std::string("batch adjoint launch: ") + cudaGetErrorString(e));
   }
   return TAM_OK;
 }

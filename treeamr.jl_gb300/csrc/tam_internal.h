@@ -139,6 +139,22 @@ struct AdjReduce {
   int64_t first;
 };
 
+// The adjoint's arrays on the device (tam_adjoint.cu), for one schedule or a
+// batch of forests: transposed stencils per group, per stage the pass-1
+// transfers and the pass-2 reduction blocks, and each transfer's scratch box.
+struct AdjPlan {
+  AdjGroup *groups = nullptr;
+  int32_t *off = nullptr;        // CSR row offsets
+  void *ent = nullptr;           // CSR entries, int2 (target row, weight index)
+  int64_t *scr = nullptr;        // per transfer: scratch offset in points
+  void *xfers = nullptr;         // pass-1 transfers, int2 (transfer, group)
+  AdjReduce *red = nullptr;      // pass-2 reduction blocks
+  void *list = nullptr;          // their transfers, int2 (transfer, group)
+  std::vector<AdjStage> stages;  // one per forward stage, in the same order
+  int64_t scratch_points = 0;    // max over stages, per variable
+  bool ready = false;
+};
+
 struct LaunchShape {
   int tile_items = 128;     // box points per tile
   int threads = 256;        // threads per CTA of the fused kernel
@@ -193,17 +209,7 @@ struct tam_sched {
   tam::SideStream side;
   int32_t *d_err = nullptr;
   // the adjoint, prepared on first use (tam_adjoint.cu)
-  bool adj_ready = false;
-  std::vector<tam::AdjGroup> adj_groups;
-  std::vector<tam::AdjStage> adj_stages;
-  int64_t adj_scratch_points = 0;       // max over stages, per variable
-  tam::AdjGroup *d_adj_groups = nullptr;
-  int32_t *d_adj_off = nullptr;         // CSR row offsets
-  void *d_adj_ent = nullptr;            // CSR entries (int2: weight part, target offset)
-  int64_t *d_adj_scr = nullptr;         // per transfer: scratch offset in points
-  void *d_adj_tiles = nullptr;          // pass-1 transfers: (transfer, group) pairs
-  tam::AdjReduce *d_adj_red = nullptr;
-  int32_t *d_adj_list = nullptr;        // transfers of each reduction block
+  tam::AdjPlan adj;
   void *adj_scratch = nullptr;          // owned scratch, grown on demand
   size_t adj_scratch_bytes = 0;
 };
@@ -247,5 +253,30 @@ int adjoint_prepare(tam_sched *s, std::string &err);
 void adjoint_free(tam_sched *s);
 cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
                         int32_t last, void *scratch, cudaStream_t stream);
+
+// A batch's plan from its members' (each member's groups, transfers and
+// weights at the given bases of the batch's concatenated arrays; `stages`
+// the batch's stages, whose tags the plan's stages follow).
+int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members,
+                          const std::vector<int64_t> &group_base,
+                          const std::vector<int64_t> &transfer_base,
+                          const std::vector<int64_t> &weight_base,
+                          const std::vector<Stage> &stages, std::string &err);
+void adjoint_plan_free(AdjPlan &plan);
+
+// The arrays a run of a plan reads beside it.
+struct AdjRun {
+  int dtype, D;
+  const DevGroup *groups;
+  const int32_t *tb;
+  const void *weights;
+  const Member *members;           // a batch's member table, or null
+  const Tile *fwd_tiles;           // the forward fill's tiles (the zero pass)
+  const std::vector<Stage> *fwd_stages;
+  int S[3];                        // stored extents (a batch: each member's own)
+};
+cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,
+                             const void *factors, int32_t first, int32_t last, void *scratch,
+                             cudaStream_t stream);
 
 }  // namespace tam
