@@ -186,6 +186,30 @@ function fill_ghosts_adjoint!(y::CuArray, fs::FieldSet, schedule::GhostSchedule)
     return y
 end
 
+# A field set held in host memory, filled on the GPU (tam_fill_host): the
+# state is uploaded into a device buffer kept per schedule, filled there and
+# downloaded into fs.work, all on the task's stream.  Page-locked host memory
+# (CUDA.Mem.pin(fs.work)) lets the copies overlap other streams' work.
+const HOST_BUFFERS = WeakKeyDict{GhostSchedule,Any}()
+function fill_ghosts_on_gpu!(fs::FieldSet{T,D,R,<:Array}, schedule::GhostSchedule;
+                             factors::Union{Nothing,CuArray}=nothing) where {T,D,R}
+    TreeAMR.check_fill(fs, schedule)
+    ds = device_schedule(schedule)
+    buf = get!(() -> CuArray{T}(undef, size(fs.work)), HOST_BUFFERS, schedule)
+    fdev = factors === nothing && fs.factors !== nothing ? CuArray(fs.factors) : factors
+    GC.@preserve fdev buf begin
+        rc = ccall((:tam_fill_host, LIB), Cint,
+                   (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid},
+                    Int32, Int32, Ptr{Cvoid}),
+                   ds.handle, pointer(fs.work), pointer(fs.work), pointer(buf), fs.nvars,
+                   size(fs.work, ndims(fs.work)), fdev === nothing ? CU_NULL : pointer(fdev),
+                   STAGE_FIRST, STAGE_LAST, CUDA.stream().handle)
+        check(rc, ds.ctx, "tam_fill_host")
+        CUDA.synchronize()
+    end
+    return fs
+end
+
 # A functional form for differentiation: the filled copy of `x`.
 function ghost_filled(x::CuArray, fs::FieldSet, schedule::GhostSchedule)
     y = copy(x)
