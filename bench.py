@@ -206,7 +206,14 @@ def measure_walls(T, dev, timed, args, peak):
     fs.work.uniform_(-1.0, 1.0, generator=g)
     esize = np.dtype(T).itemsize
     bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * esize
-    tuned = autotune(fs, sched)
+    if args.options:
+        ds0 = device_schedule(sched, dev.index)
+        for kv in args.options.split(","):
+            k, v = kv.split("=")
+            ds0.set_option(k.strip(), int(v))
+        tuned = ds0.options()
+    else:
+        tuned = autotune(fs, sched)
     for _ in range(args.warmup):
         fill_ghosts(fs, sched)
     steps = max(3, args.steps // 2)

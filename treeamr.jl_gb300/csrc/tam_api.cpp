@@ -313,16 +313,18 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
     std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
       return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
     });
-    // unit copies first (the light kernel), then the stencils
-    for (int pass = 0; pass < 2; ++pass) {
+    // unit copies first (the light kernel; those without a factor column
+    // first of all), then the stencils
+    for (int pass = 0; pass < 3; ++pass) {
       for (const Entry &e : entries) {
         const tam::DevGroup &g = s->groups[e.group];
-        if ((g.pclass == 0) != (pass == 0)) continue;
+        if (tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
         for (int i0 = 0; i0 < box; i0 += ti)
           tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
       }
-      if (pass == 0) st.ncopy = (int64_t)tiles.size() - st.tile0;
+      if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
+      if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
@@ -612,7 +614,8 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
   for (const tam::Stage &stage : s->stages) {
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
     cudaError_t e = tam::launch_fused_stage(
-        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy, stage.nptiles,
+        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
+        stage.nptiles,
         sched_args(s), work, factors, nvars, s->S, s->shape.threads, st, &s->side);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
   }

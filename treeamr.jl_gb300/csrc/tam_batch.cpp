@@ -123,15 +123,16 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b) {
       if (x.member != y.member) return x.member < y.member;
       return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
     });
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < 3; ++pass) {
       for (const Entry &e : entries) {
         const tam::DevGroup &g = b->groups[e.group];
-        if ((g.pclass == 0) != (pass == 0)) continue;
+        if (tam::tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
         for (int i0 = 0; i0 < box; i0 += ti)
           tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
       }
-      if (pass == 0) st.ncopy = (int64_t)tiles.size() - st.tile0;
+      if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
+      if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
@@ -296,7 +297,7 @@ int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
     cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles + st.ptile0,
-                                            st.npcopy, st.nptiles, args, arena, factor_arena,
+                                            st.npcopy0, st.npcopy, st.nptiles, args, arena, factor_arena,
                                             nvars, S, b->shape.threads, (cudaStream_t)stream,
                                             &b->side);
     if (e != cudaSuccess) {

@@ -78,6 +78,12 @@ struct PTile {
   int32_t pad;
 };
 
+// Which of a stage's three runs of tiles a group's transfers go to: unit
+// copies without a factor column, unit copies with one, stencils.
+inline int tile_pass(const DevGroup &g) {
+  return g.pclass != 0 ? 2 : g.factorcol != 0 ? 1 : 0;
+}
+
 // The packing: consecutive tiles of [begin, end) joined while they fit in
 // `target` points and 32 segments.
 void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
@@ -103,9 +109,11 @@ struct Stage {
   std::vector<int32_t> groups;  // indices into the schedule's groups
   int64_t tile0 = 0;            // first tile in the schedule's tile array
   int64_t ntiles = 0;           // copy tiles first, then stencil tiles
-  int64_t ncopy = 0;            // the stage's unit-copy tiles
+  int64_t ncopy0 = 0;           // the stage's unit-copy tiles without a factor column,
+  int64_t ncopy = 0;            // then all its unit-copy tiles
   int64_t ptile0 = 0;           // first packed tile of the stage
-  int64_t npcopy = 0;           // packed tiles of the copies, then
+  int64_t npcopy0 = 0;          // packed tiles of the copies without a factor, of
+  int64_t npcopy = 0;           // all the copies, then
   int64_t nptiles = 0;          // all packed tiles of the stage
 };
 
@@ -237,11 +245,13 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
                                const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], cudaStream_t stream);
 
-// One stage: the packed tiles [0, npcopy) run the copy kernel and
-// [npcopy, nptiles) the stencil kernel, on `stream` and, when `side` is
-// given and both are present, the stencils on the side stream alongside.
+// One stage: the packed tiles [0, npcopy) run the copy kernel (those from
+// npcopy0 on with their factor column) and [npcopy, nptiles) the stencil
+// kernel, on `stream` and, when `side` is given and both are present, the
+// stencils on the side stream alongside.
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
-                               int64_t npcopy, int64_t nptiles, const SchedArgs &a, void *work,
+                               int64_t npcopy0, int64_t npcopy, int64_t nptiles,
+                               const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side);
 

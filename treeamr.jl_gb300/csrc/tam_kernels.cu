@@ -246,7 +246,7 @@ __device__ __forceinline__ ShortW short_weight(double w) {
 
 // Unit copies of every variable of one or two points: +0 + x
 // (src/ghosts.jl:127-128), all loads of a chunk issued before its stores.
-template <typename T, int NP>
+template <typename T, int NP, bool FACTOR>
 __device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[NP],
                                             const bool (&on)[NP], const T *__restrict__ src,
                                             T *__restrict__ dst, const T *__restrict__ factors,
@@ -265,7 +265,8 @@ __device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[N
       for (int j = 0; j < VC; ++j)
         if (on[p] && v0 + j < nvars)
           dst[o[p].toff + (v0 + j) * o[p].vstride] =
-              scaled(plus_zero(x[p][j]), factors, v0 + j, nvars, g.factorcol);
+              FACTOR ? scaled(plus_zero(x[p][j]), factors, v0 + j, nvars, g.factorcol)
+                     : plus_zero(x[p][j]);
   }
 }
 
@@ -584,8 +585,11 @@ __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int ns
 }
 
 // The unit-copy tiles of a stage: a light kernel, every variable's load of a
-// point in flight together.
-template <typename T, int D, bool BATCH>
+// point in flight together.  Copies without a factor column run the FACTOR =
+// false form, which holds no floating-point operation at all: with the
+// factor's multiply in the same code the compiler issues it predicated, and
+// on GB300's narrow FP64 pipe that competes with the stencils alongside.
+template <typename T, int D, bool BATCH, bool FACTOR>
 __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict__ tiles,
                                                          const PTile *__restrict__ ptiles,
                                                          int64_t nptiles, Args<T> a,
@@ -614,7 +618,7 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
       Geom o[1];
       const bool on[1] = {true};
       o[0] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
-      copy_points<T, 1>(g, o, on, L.src, L.dst, L.factors, nvars);
+      copy_points<T, 1, FACTOR>(g, o, on, L.src, L.dst, L.factors, nvars);
     }
   }
 }
@@ -679,10 +683,22 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
   return cudaGetLastError();
 }
 
+template <typename T, int D, bool BATCH, bool FACTOR>
+cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, const Args<T> &a,
+                          T *work, const T *factors, int nvars, const int S[3], int threads,
+                          cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int wpb = threads / 32;
+  const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
+  fused_copy_kernel<T, D, BATCH, FACTOR><<<(unsigned)blocks, threads, 0, stream>>>(
+      tiles, ptiles, n, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  return cudaSuccess;
+}
+
 template <typename T, int D>
-cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy, int64_t nptiles,
-                        const Args<T> &a, T *work, const T *factors, int nvars, const int S[3],
-                        int threads, cudaStream_t stream, SideStream *side) {
+cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
+                        int64_t nptiles, const Args<T> &a, T *work, const T *factors, int nvars,
+                        const int S[3], int threads, cudaStream_t stream, SideStream *side) {
   const int wpb = threads / 32;
   const bool batch = a.members != nullptr;
   const int64_t nst = nptiles - npcopy;
@@ -704,14 +720,16 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy, 
       fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, sst>>>(
           tiles, ptiles + npcopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
   }
-  if (npcopy > 0) {
-    const int64_t blocks = std::min<int64_t>((npcopy + wpb - 1) / wpb, (int64_t)1 << 30);
-    if (batch)
-      fused_copy_kernel<T, D, true><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ptiles, npcopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
-    else
-      fused_copy_kernel<T, D, false><<<(unsigned)blocks, threads, 0, stream>>>(
-          tiles, ptiles, npcopy, a, work, work, factors, nvars, S[0], S[1], S[2]);
+  if (batch) {
+    launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, work, factors, nvars, S,
+                                     threads, stream);
+    launch_copies<T, D, true, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, work,
+                                    factors, nvars, S, threads, stream);
+  } else {
+    launch_copies<T, D, false, false>(tiles, ptiles, npcopy0, a, work, factors, nvars, S,
+                                      threads, stream);
+    launch_copies<T, D, false, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, work,
+                                     factors, nvars, S, threads, stream);
   }
   if (fork) {
     cudaError_t e = cudaEventRecord(side->join, side->stream);
@@ -725,19 +743,19 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy, 
 // dependency between them (their targets are disjoint and neither reads a
 // point of the stage's targets).
 template <typename T>
-cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy,
+cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
                            int64_t nptiles, const Args<T> &a, T *work, const T *factors, int nvars,
                            const int S[3], int threads, cudaStream_t stream, SideStream *side) {
   if (nptiles == 0) return cudaSuccess;
   switch (D) {
     case 1:
-      return launch_both<T, 1>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 1>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
                                threads, stream, side);
     case 2:
-      return launch_both<T, 2>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 2>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
                                threads, stream, side);
     default:
-      return launch_both<T, 3>(tiles, ptiles, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 3>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
                                threads, stream, side);
   }
 }
@@ -755,14 +773,15 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
 }
 
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
-                               int64_t npcopy, int64_t nptiles, const SchedArgs &a, void *work,
+                               int64_t npcopy0, int64_t npcopy, int64_t nptiles,
+                               const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side) {
   if (dtype == TAM_F64)
-    return fused_dispatch<double>(D, tiles, ptiles, npcopy, nptiles, typed<double>(a),
+    return fused_dispatch<double>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<double>(a),
                                   (double *)work, (const double *)factors, nvars, S, threads,
                                   stream, side);
-  return fused_dispatch<float>(D, tiles, ptiles, npcopy, nptiles, typed<float>(a), (float *)work,
+  return fused_dispatch<float>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<float>(a), (float *)work,
                                (const float *)factors, nvars, S, threads, stream, side);
 }
 
@@ -785,7 +804,9 @@ std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Til
   std::vector<PTile> out;
   for (Stage &st : stages) {
     st.ptile0 = (int64_t)out.size();
-    pack_tiles(tiles, st.tile0, st.tile0 + st.ncopy, target, out);
+    pack_tiles(tiles, st.tile0, st.tile0 + st.ncopy0, target, out);
+    st.npcopy0 = (int64_t)out.size() - st.ptile0;
+    pack_tiles(tiles, st.tile0 + st.ncopy0, st.tile0 + st.ncopy, target, out);
     st.npcopy = (int64_t)out.size() - st.ptile0;
     pack_tiles(tiles, st.tile0 + st.ncopy, st.tile0 + st.ntiles, target, out);
     st.nptiles = (int64_t)out.size() - st.ptile0;

@@ -54,24 +54,16 @@ def autotune(fs: FieldSet, sched: GhostSchedule, *, reps: int = 3,
         return dict(cache[key])
     if int_mul is None:
         int_mul = (0, 1) if fs.T.itemsize == 8 else (0,)
+    # every combination: the best tile and CTA size differ between the two
+    # multiply paths, so neither is chosen before the other
     results = []
-    # threads and tiles first with the FP64 multiply, then the multiply path
-    for ti, th in itertools.product(tile_items, threads):
+    for im, ti, th in itertools.product(int_mul, tile_items, threads):
         ds.set_option("tile_items", ti)
         ds.set_option("threads", th)
-        ds.set_option("int_mul", 0)
-        results.append((_time_fill(fs, sched, reps), {"tile_items": ti, "threads": th,
-                                                      "int_mul": 0}))
-    best_t, best = min(results, key=lambda r: r[0])
-    for im in int_mul:
-        if im == 0:
-            continue
-        ds.set_option("tile_items", best["tile_items"])
-        ds.set_option("threads", best["threads"])
         ds.set_option("int_mul", im)
-        t = _time_fill(fs, sched, reps)
-        if t < best_t:
-            best_t, best = t, dict(best, int_mul=im)
+        results.append((_time_fill(fs, sched, reps), {"tile_items": ti, "threads": th,
+                                                      "int_mul": im}))
+    best_t, best = min(results, key=lambda r: r[0])
     for k, v in best.items():
         ds.set_option(k, v)
     cache[key] = dict(best)
