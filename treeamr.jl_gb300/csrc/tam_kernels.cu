@@ -244,14 +244,13 @@ __device__ __forceinline__ ShortW short_weight(double w) {
 // `work` through `src` and write it through `dst`, both restrict-qualified:
 // the loads of several points and variables can be in flight together.
 
-// Unit copies of every variable of one or two points: +0 + x
-// (src/ghosts.jl:127-128), all loads of a chunk issued before its stores.
-template <typename T, int NP, bool FACTOR>
-__device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[NP],
+// Unit copies of every variable of NP points: +0 + x (src/ghosts.jl:127-128),
+// all loads of a chunk issued before its stores; fac[p] is point p's factor
+// column (FACTOR only), x * f + 0 (src/ghosts.jl:369-370).
+template <typename T, int NP, int VC, bool FACTOR>
+__device__ __forceinline__ void copy_points(const T *const (&fac)[NP], const Geom (&o)[NP],
                                             const bool (&on)[NP], const T *__restrict__ src,
-                                            T *__restrict__ dst, const T *__restrict__ factors,
-                                            int nvars) {
-  constexpr int VC = 8;
+                                            T *__restrict__ dst, int nvars) {
   for (int v0 = 0; v0 < nvars; v0 += VC) {
     T x[NP][VC];
 #pragma unroll
@@ -265,7 +264,8 @@ __device__ __forceinline__ void copy_points(const DevGroup &g, const Geom (&o)[N
       for (int j = 0; j < VC; ++j)
         if (on[p] && v0 + j < nvars)
           dst[o[p].toff + (v0 + j) * o[p].vstride] =
-              FACTOR ? scaled(plus_zero(x[p][j]), factors, v0 + j, nvars, g.factorcol)
+              FACTOR ? Arith<T>::add(Arith<T>::mul(plus_zero(x[p][j]), __ldg(fac[p] + v0 + j)),
+                                     T(0))
                      : plus_zero(x[p][j]);
   }
 }
@@ -584,6 +584,10 @@ __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int ns
   return p;
 }
 
+// Points a lane of the copy kernel takes at once, and variables per chunk.
+constexpr int kCopyPoints = 1;
+constexpr int kCopyVars = 8;
+
 // The unit-copy tiles of a stage: a light kernel, every variable's load of a
 // point in flight together.  Copies without a factor column run the FACTOR =
 // false form, which holds no floating-point operation at all: with the
@@ -605,20 +609,31 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
     Tile seg;
     int pref;
     load_segments(tiles, pt, lane, seg, pref);
-    for (int base = 0; base < pt.nitems; base += 32) {
-      const int k = base + lane;
-      SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
-      if (k >= pt.nitems) continue;
-      const DevGroup &g = a.groups[q.group];
-      const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-      const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
-      const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
-      int i1, i2, i3;
-      box_point(q.item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
-      Geom o[1];
-      const bool on[1] = {true};
-      o[0] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
-      copy_points<T, 1, FACTOR>(g, o, on, L.src, L.dst, L.factors, nvars);
+    // kCopyPoints points a lane: their loads in flight together
+    for (int base = 0; base < pt.nitems; base += 32 * kCopyPoints) {
+      Geom o[kCopyPoints];
+      bool on[kCopyPoints];
+      const T *fac[kCopyPoints];
+#pragma unroll
+      for (int p = 0; p < kCopyPoints; ++p) {
+        const int k = base + 32 * p + lane;
+        SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
+        on[p] = k < pt.nitems;
+        const DevGroup &g = a.groups[q.group];
+        const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+        const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+        const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
+        int i1, i2, i3;
+        box_point(q.item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
+        o[p] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
+        // a batch member's offsets folded into the point's own
+        if (BATCH) {
+          o[p].soff += L.src - src;
+          o[p].toff += L.dst - dst;
+        }
+        fac[p] = FACTOR ? L.factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
+      }
+      copy_points<T, kCopyPoints, kCopyVars, FACTOR>(fac, o, on, src, dst, nvars);
     }
   }
 }
