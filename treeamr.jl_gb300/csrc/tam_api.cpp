@@ -444,6 +444,33 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
     g.ntransfers = h.ntransfers;
     if (h.factorcol != 0) s->needs_factors = true;
     s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
+    // the division-free box decomposition
+    {
+      const uint64_t n1 = (uint64_t)g.n[0], n12 = n1 * (uint64_t)g.n[1];
+      const uint64_t box = n12 * (uint64_t)g.n[2];
+      g.mag1 = g.mag12 = 0;
+      if (box * n1 < (1ull << 32) && box * n12 < (1ull << 32)) {
+        g.mag1 = (uint32_t)(((1ull << 32) + n1 - 1) / n1);
+        g.mag12 = (uint32_t)(((1ull << 32) + n12 - 1) / n12);
+        if (n1 == 1) g.mag1 = 0;    // 2^32 does not fit: divide
+        if (n12 == 1) g.mag12 = 0;
+      }
+    }
+    // affine unit copies
+    g.affine = 0;
+    if (g.pclass == 0) {
+      bool aff = true;
+      for (int k = 0; k < 3; ++k) {
+        const int32_t *ssk = srcstart.data() + g.ss[k];
+        const int n = g.n[k];
+        const int32_t step = n > 1 ? ssk[1] - ssk[0] : 0;
+        aff = aff && step >= -1 && step <= 1;
+        for (int i = 1; i < n && aff; ++i) aff = ssk[i] - ssk[0] == step * i;
+        g.cs0[k] = ssk[0] - 1;
+        g.cstep[k] = step;
+      }
+      g.affine = aff ? 1 : 0;
+    }
     for (int k = 0; k < 3; ++k) g.C[k] = 1;
     for (int k = 0; k < 3; ++k) g.csingle[k] = 0;
     g.perm = -1;

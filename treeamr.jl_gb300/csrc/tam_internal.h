@@ -46,6 +46,15 @@ struct DevGroup {
   // trip counts: point `perm[item]` is the item-th a tile takes.
   int64_t csingle[3];
   int64_t perm;
+  // Box points to rows without a division: i3 = umulhi(item, mag12),
+  // i2 = umulhi(rest, mag1), exact because box * n1 < 2^32 (0: divide).
+  uint32_t mag1, mag12;
+  // A unit copy whose source rows advance by -1, 0 or +1 a target row in
+  // every dimension (a translation, a mirror, a clamp): the source row of
+  // target row i is cs0[d] + cstep[d] * i (0-based), no srcstart load.
+  int32_t affine;
+  int32_t cs0[3];
+  int32_t cstep[3];
 };
 
 // One forest of a batch (tam_batch_fill): where its field data and factor

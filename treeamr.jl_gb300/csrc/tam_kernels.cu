@@ -134,6 +134,27 @@ __device__ __forceinline__ Geom geometry(const DevGroup &g, int i1, int i2, int 
   return o;
 }
 
+// The geometry of an affine unit copy: its source rows from the group's
+// first row and step, no srcstart load.
+template <int D>
+__device__ __forceinline__ Geom copy_geometry(const DevGroup &g, int i1, int i2, int i3,
+                                              int64_t tblock, int64_t sblock, int nvars, int S1,
+                                              int S2, int S3) {
+  Geom o;
+  o.s2 = S1;
+  o.s3 = (int64_t)S1 * S2;
+  o.vstride = o.s3 * S3;
+  const int64_t bstride = o.vstride * nvars;
+  const int b1 = g.cs0[0] + g.cstep[0] * i1;
+  const int b2 = D >= 2 ? g.cs0[1] + g.cstep[1] * i2 : 0;
+  const int b3 = D >= 3 ? g.cs0[2] + g.cstep[2] * i3 : 0;
+  o.toff = tblock * bstride + (int64_t)(g.tf[0] + i1) +
+           (D >= 2 ? (int64_t)(g.tf[1] + i2) * o.s2 : 0) +
+           (D >= 3 ? (int64_t)(g.tf[2] + i3) * o.s3 : 0);
+  o.soff = sblock * bstride + b1 + (int64_t)b2 * o.s2 + (int64_t)b3 * o.s3;
+  return o;
+}
+
 // +0 + x without the floating-point pipe: x itself, except that -0 becomes
 // +0 (IEEE round-to-nearest gives +0 for +0 + -0).  A NaN stays a NaN (its
 // payload kept rather than made canonical; NaNs compare as one pattern).
@@ -520,10 +541,13 @@ __global__ void __launch_bounds__(256) plain_group_kernel(const DevGroup *__rest
 }
 
 // ---- fused: one launch per stage, one warp per tile ---------------------------
-__device__ __forceinline__ void box_point(int item, int n1, int n12, int &i1, int &i2, int &i3) {
-  i3 = item / n12;
+__device__ __forceinline__ void box_point(const DevGroup &g, int item, int &i1, int &i2,
+                                          int &i3) {
+  const int n1 = g.n[0], n12 = g.n[0] * g.n[1];
+  const uint32_t m1 = g.mag1, m12 = g.mag12;
+  i3 = m12 ? (int)__umulhi((uint32_t)item, m12) : item / n12;
   const int rem = item - i3 * n12;
-  i2 = rem / n1;
+  i2 = m1 ? (int)__umulhi((uint32_t)rem, m1) : rem / n1;
   i1 = rem - i2 * n1;
 }
 
@@ -624,8 +648,10 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
         const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
         const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
         int i1, i2, i3;
-        box_point(q.item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
-        o[p] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2, L.S3);
+        box_point(g, q.item, i1, i2, i3);
+        o[p] = g.affine ? copy_geometry<D>(g, i1, i2, i3, tblock, sblock, nvars, L.S1, L.S2, L.S3)
+                        : geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1,
+                                      L.S2, L.S3);
         // a batch member's offsets folded into the point's own
         if (BATCH) {
           o[p].soff += L.src - src;
@@ -665,7 +691,7 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
       const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
       const int item = g.perm >= 0 ? __ldg(a.perm + g.perm + q.item) : q.item;
       int i1, i2, i3;
-      box_point(item, g.n[0], g.n[0] * g.n[1], i1, i2, i3);
+      box_point(g, item, i1, i2, i3);
       stencil_point<T, D>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars, L.S1,
                           L.S2, L.S3);
     }
