@@ -65,6 +65,19 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time: every rank's replica is timed alone, and the
+    job's time is the maximum (an all-reduce on ``device``, which is a CUDA
+    device under NCCL and the CPU under gloo)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def stencil_flops(sched, nvars, one_tap=True):
     """Algorithmic FP64/FP32 operations of each stage's stencil transfers: per
     target point-variable one multiply and one add per tap the reference's
@@ -420,12 +433,7 @@ def main():
         b.record(stream)
         torch.cuda.synchronize(dev)
         barrier()
-        ms = a.elapsed_time(b)
-        if world > 1:
-            t = torch.tensor([ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms / steps
+        return max_over_ranks(a.elapsed_time(b), world, dev) / steps
 
     method = args.method
     tuned = None
@@ -613,7 +621,8 @@ def run_reference(args):
     sec = (time.perf_counter() - t0) / steps
     value = bytes_per_fill / sec / 1e9
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus,
         "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",

@@ -1,0 +1,71 @@
+"""The bench's N > 1 path on the CPU: replicas only, timed alone and joined by
+the maximum over ranks, with the reference arm printed by rank 0 alone.
+Two gloo ranks stand in for two GPUs."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _rank(rank, world, port, out):
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        got = bench.max_over_ranks(10.0 + 5.0 * rank, world, torch.device("cpu"))
+        out.put((rank, got))
+    finally:
+        dist.destroy_process_group()
+
+
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_max_over_ranks_with_gloo():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    got = dict(q.get(timeout=10) for _ in range(2))
+    assert got == {0: 15.0, 1: 15.0}
+
+
+def test_max_over_ranks_single_rank_is_identity():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(3.5, 1, "cpu") == 3.5
+
+
+@pytest.mark.parametrize("rank", [0, 1])
+def test_reference_arm_prints_on_rank_zero_only(rank):
+    env = dict(os.environ, RANK=str(rank), WORLD_SIZE="2", LOCAL_RANK=str(rank),
+               MASTER_ADDR="127.0.0.1", MASTER_PORT="29555")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--gpus", "2", "--roots", "2", "--levels", "1", "--nvars", "1",
+                        "--steps", "1", "--warmup", "1"],
+                       cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    if rank:
+        assert lines == []
+    else:
+        line = json.loads(lines[-1])
+        assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+        assert line["cpu_baseline"]["kind"] == "port"
