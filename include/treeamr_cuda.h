@@ -248,6 +248,23 @@ typedef struct tam_wave_block {
 int tam_wave_rhs(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
                  int32_t max_points_per_block, const void *in, void *out, int32_t adjoint,
                  void *stream);
+/* One stage of classical RK4 around that right-hand side, at every stored
+ * point: k = R(x) (zero at ghosts), t_out = y + ct*k (when t_out is not
+ * NULL) and acc_out = (acc_in, or y when NULL) + ca*k, so a step's stage
+ * states and weighted sum need no stored k.  x's ghosts must be filled; x
+ * may not be t_out or acc_out; acc_out may be acc_in. */
+int tam_wave_rk4_stage(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
+                       int32_t max_points_per_block, const void *x, const void *y,
+                       void *t_out, const void *acc_in, void *acc_out, double ct, double ca,
+                       void *stream);
+/* The transpose of a stage's right-hand side with its cotangent formed on
+ * the fly: out = R^T (c1*g + c2*xprev) (xprev may be NULL), and when ybar is
+ * not NULL, ybar += xprev at every stored point.  out may alias none of g,
+ * xprev, ybar; ybar may not alias xprev. */
+int tam_wave_rk4_adjoint_stage(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
+                               int32_t max_points_per_block, const void *g, double c1,
+                               const void *xprev, double c2, void *out, void *ybar,
+                               void *stream);
 
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing

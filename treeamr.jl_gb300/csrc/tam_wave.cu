@@ -84,7 +84,141 @@ __global__ void __launch_bounds__(256) wave_rhs_adjoint_kernel(
   }
 }
 
+// One stage of classical RK4 around the right-hand side, at every stored
+// point of every block: k = R(x) (zero at a ghost, as the plain right-hand
+// side leaves a zeroed k there), then
+//   t_out = y + ct * k            (when t_out is given)
+//   acc_out = (acc_in or y) + ca * k
+// so a step's stage states and its weighted sum are formed without storing
+// k.  x's ghosts must be filled.  acc_out may be acc_in; neither aliases x.
+template <typename T>
+__global__ void __launch_bounds__(256) wave_rk4_stage_kernel(
+    const tam_wave_block *__restrict__ blocks, int32_t nblocks, const T *__restrict__ x,
+    const T *y, T *t_out, const T *acc_in, T *acc_out, T ct, T ca) {
+  const int b = blockIdx.x;
+  if (b >= nblocks) return;
+  const tam_wave_block B = blocks[b];
+  const int N = B.N, G = B.G;
+  const int S1 = B.S[0], S2 = B.S[1], S3 = B.S[2];
+  const int total = S1 * S2 * S3;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3;
+  const T ih2 = (T)B.inv_h2;
+  for (int p = blockIdx.y * blockDim.x + threadIdx.x; p < total; p += gridDim.y * blockDim.x) {
+    const int k = p / (S1 * S2), r = p - k * S1 * S2, j = r / S1, i = r - j * S1;
+    const bool own = i >= G && i < G + N && j >= G && j < G + N && k >= G && k < G + N;
+    const int64_t c = B.off + p;
+    T ku = T(0), kv = T(0);
+    if (own) {
+      const T u = ldg_t(x + c);
+      const T sum = ((ldg_t(x + c - 1) + ldg_t(x + c + 1)) + (ldg_t(x + c - s2) + ldg_t(x + c + s2))) +
+                    (ldg_t(x + c - s3) + ldg_t(x + c + s3));
+      ku = ldg_t(x + c + vs);
+      kv = (sum - T(6) * u) * ih2;
+    }
+    const T yu = y[c], yv = y[c + vs];
+    if (t_out) {
+      t_out[c] = yu + ct * ku;
+      t_out[c + vs] = yv + ct * kv;
+    }
+    const T au = acc_in ? acc_in[c] : yu, av = acc_in ? acc_in[c + vs] : yv;
+    acc_out[c] = au + ca * ku;
+    acc_out[c + vs] = av + ca * kv;
+  }
+}
+
+// The transpose of one RK4 stage's right-hand side with its cotangent
+// formed on the fly: out = R^T kb, kb = c1 * g + c2 * xprev (xprev may be
+// NULL), and, when ybar is given, ybar += xprev at every stored point (the
+// previous stage's contribution, added in stage order).  out may alias
+// neither g nor xprev.
+template <typename T>
+__global__ void __launch_bounds__(256) wave_rk4_adjoint_stage_kernel(
+    const tam_wave_block *__restrict__ blocks, int32_t nblocks, const T *__restrict__ g, T c1,
+    const T *__restrict__ xprev, T c2, T *__restrict__ out, T *ybar) {
+  const int b = blockIdx.x;
+  if (b >= nblocks) return;
+  const tam_wave_block B = blocks[b];
+  const int N = B.N, G = B.G;
+  const int S1 = B.S[0], S2 = B.S[1], S3 = B.S[2];
+  const int total = S1 * S2 * S3;
+  const int64_t s2 = S1, s3 = (int64_t)S1 * S2, vs = s3 * S3;
+  const T ih2 = (T)B.inv_h2;
+  auto kb = [&](int64_t q) {
+    return xprev ? c1 * ldg_t(g + q) + c2 * ldg_t(xprev + q) : c1 * ldg_t(g + q);
+  };
+  for (int p = blockIdx.y * blockDim.x + threadIdx.x; p < total; p += gridDim.y * blockDim.x) {
+    const int k = p / (S1 * S2), r = p - k * S1 * S2, j = r / S1, i = r - j * S1;
+    auto owned = [&](int x, int y, int z) {
+      return x >= G && x < G + N && y >= G && y < G + N && z >= G && z < G + N;
+    };
+    const int64_t c = B.off + p;
+    T acc = T(0);
+    if (owned(i - 1, j, k)) acc += kb(vs + c - 1);
+    if (owned(i + 1, j, k)) acc += kb(vs + c + 1);
+    if (owned(i, j - 1, k)) acc += kb(vs + c - s2);
+    if (owned(i, j + 1, k)) acc += kb(vs + c + s2);
+    if (owned(i, j, k - 1)) acc += kb(vs + c - s3);
+    if (owned(i, j, k + 1)) acc += kb(vs + c + s3);
+    const bool me = owned(i, j, k);
+    out[c] = acc * ih2 - (me ? T(6) * ih2 * kb(vs + c) : T(0));
+    out[c + vs] = me ? kb(c) : T(0);
+    if (ybar && xprev) {
+      ybar[c] += ldg_t(xprev + c);
+      ybar[c + vs] += ldg_t(xprev + c + vs);
+    }
+  }
+}
+
 }  // namespace
+
+extern "C" int tam_wave_rk4_adjoint_stage(int32_t dtype, const tam_wave_block *blocks,
+                                          int32_t nblocks, int32_t max_points_per_block,
+                                          const void *g, double c1, const void *xprev,
+                                          double c2, void *out, void *ybar, void *stream) {
+  if (!blocks || !g || !out || nblocks < 0 || max_points_per_block < 0) return TAM_EINVAL;
+  if (out == g || out == xprev || (ybar && (ybar == out || ybar == xprev))) return TAM_EINVAL;
+  if (nblocks == 0) return TAM_OK;
+  const int threads = 256;
+  const int chunks = std::max(1, std::min(64, (max_points_per_block + threads - 1) / threads));
+  const dim3 grid(nblocks, chunks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == TAM_F64)
+    wave_rk4_adjoint_stage_kernel<double><<<grid, threads, 0, s>>>(
+        blocks, nblocks, (const double *)g, c1, (const double *)xprev, c2, (double *)out,
+        (double *)ybar);
+  else if (dtype == TAM_F32)
+    wave_rk4_adjoint_stage_kernel<float><<<grid, threads, 0, s>>>(
+        blocks, nblocks, (const float *)g, (float)c1, (const float *)xprev, (float)c2,
+        (float *)out, (float *)ybar);
+  else
+    return TAM_EINVAL;
+  return cudaGetLastError() == cudaSuccess ? TAM_OK : TAM_ECUDA;
+}
+
+extern "C" int tam_wave_rk4_stage(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
+                                  int32_t max_points_per_block, const void *x, const void *y,
+                                  void *t_out, const void *acc_in, void *acc_out, double ct,
+                                  double ca, void *stream) {
+  if (!blocks || !x || !y || !acc_out || nblocks < 0 || max_points_per_block < 0)
+    return TAM_EINVAL;
+  if (x == acc_out || x == t_out) return TAM_EINVAL;
+  if (nblocks == 0) return TAM_OK;
+  const int threads = 256;
+  const int chunks = std::max(1, std::min(64, (max_points_per_block + threads - 1) / threads));
+  const dim3 grid(nblocks, chunks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == TAM_F64)
+    wave_rk4_stage_kernel<double><<<grid, threads, 0, s>>>(
+        blocks, nblocks, (const double *)x, (const double *)y, (double *)t_out,
+        (const double *)acc_in, (double *)acc_out, ct, ca);
+  else if (dtype == TAM_F32)
+    wave_rk4_stage_kernel<float><<<grid, threads, 0, s>>>(
+        blocks, nblocks, (const float *)x, (const float *)y, (float *)t_out,
+        (const float *)acc_in, (float *)acc_out, (float)ct, (float)ca);
+  else
+    return TAM_EINVAL;
+  return cudaGetLastError() == cudaSuccess ? TAM_OK : TAM_ECUDA;
+}
 
 extern "C" int tam_wave_rhs(int32_t dtype, const tam_wave_block *blocks, int32_t nblocks,
                             int32_t max_points_per_block, const void *in, void *out,

@@ -59,6 +59,15 @@ class WaveSolver:
         self.lib.tam_wave_rhs.argtypes = [C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
                                           C.c_void_p, C.c_int32, C.c_void_p]
         self.lib.tam_wave_rhs.restype = C.c_int
+        self.lib.tam_wave_rk4_stage.argtypes = [C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+        self.lib.tam_wave_rk4_stage.restype = C.c_int
+        self.lib.tam_wave_rk4_adjoint_stage.argtypes = [C.c_int32, C.c_void_p, C.c_int32,
+                                                        C.c_int32, C.c_void_p, C.c_double,
+                                                        C.c_void_p, C.c_double, C.c_void_p,
+                                                        C.c_void_p, C.c_void_p]
+        self.lib.tam_wave_rk4_adjoint_stage.restype = C.c_int
         self.dtype_code = _native.TAM_F64 if batch.T == np.float64 else _native.TAM_F32
         self.dt = float(dt) if dt is not None else cfl * hmin
         like = batch.arena
@@ -77,6 +86,32 @@ class WaveSolver:
             raise _native.TamError(f"tam_wave_rhs failed ({rc})")
         return out
 
+    def stage(self, x: torch.Tensor, y: torch.Tensor, t_out: Optional[torch.Tensor],
+              acc_in: Optional[torch.Tensor], acc_out: torch.Tensor, ct: float, ca: float):
+        """One fused RK4 stage (``tam_wave_rk4_stage``): with k = R(x),
+        ``t_out = y + ct k`` and ``acc_out = (acc_in or y) + ca k``."""
+        s = torch.cuda.current_stream(x.device)
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        rc = self.lib.tam_wave_rk4_stage(self.dtype_code, C.c_void_p(self.table.data_ptr()),
+                                         self.nblocks, self.max_points, ptr(x), ptr(y),
+                                         ptr(t_out), ptr(acc_in), ptr(acc_out), float(ct),
+                                         float(ca), C.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise _native.TamError(f"tam_wave_rk4_stage failed ({rc})")
+
+    def stage_adjoint(self, g: torch.Tensor, c1: float, xprev: Optional[torch.Tensor],
+                      c2: float, out: torch.Tensor, ybar: Optional[torch.Tensor]):
+        """``out = R^T (c1 g + c2 xprev)`` and ``ybar += xprev``
+        (``tam_wave_rk4_adjoint_stage``)."""
+        s = torch.cuda.current_stream(g.device)
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        rc = self.lib.tam_wave_rk4_adjoint_stage(
+            self.dtype_code, C.c_void_p(self.table.data_ptr()), self.nblocks, self.max_points,
+            ptr(g), float(c1), ptr(xprev), float(c2), ptr(out), ptr(ybar),
+            C.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise _native.TamError(f"tam_wave_rk4_adjoint_stage failed ({rc})")
+
     def F(self, x: torch.Tensor, out: torch.Tensor):
         """``out = R(A x)``; ``x``'s ghosts are filled in place."""
         self.batch.fill(x)
@@ -90,17 +125,19 @@ class WaveSolver:
 
     # -- forward ---------------------------------------------------------------
     def step(self, y: torch.Tensor):
-        """One RK4 step of ``y`` in place."""
-        dt, k, t = self.dt, self.k, self.tmp
-        self.F(y, k[0])
-        t.copy_(y).add_(k[0], alpha=dt / 2)
-        self.F(t, k[1])
-        t.copy_(y).add_(k[1], alpha=dt / 2)
-        self.F(t, k[2])
-        t.copy_(y).add_(k[2], alpha=dt)
-        self.F(t, k[3])
-        y.add_(k[0], alpha=dt / 6).add_(k[1], alpha=dt / 3).add_(k[2], alpha=dt / 3) \
-         .add_(k[3], alpha=dt / 6)
+        """One RK4 step of ``y`` in place: four fills, each followed by one
+        fused stage that forms the next stage state and adds the stage's
+        share of the step, k1/6 + k2/3 + k3/3 + k4/6 times dt, in that order."""
+        dt = self.dt
+        ta, tb, acc = self.k[0], self.k[1], self.k[2]
+        self.batch.fill(y)
+        self.stage(y, y, ta, None, acc, dt / 2, dt / 6)
+        self.batch.fill(ta)
+        self.stage(ta, y, tb, acc, acc, dt / 2, dt / 3)
+        self.batch.fill(tb)
+        self.stage(tb, y, ta, acc, acc, dt, dt / 3)
+        self.batch.fill(ta)
+        self.stage(ta, y, None, acc, y, 0.0, dt / 6)
         return y
 
     def capture(self, y: torch.Tensor, steps: int = 1) -> torch.cuda.CUDAGraph:
@@ -128,21 +165,20 @@ class WaveSolver:
     # adds to zbar and (times dt) to k3bar; x3bar and x2bar likewise (times
     # dt/2) to k2bar and k1bar; R^T k1bar adds to zbar; ybar = P^T zbar.
     def step_adjoint(self, ybar: torch.Tensor):
-        """``ybar <- M^T ybar`` for one RK4 step ``M``, in place."""
+        """``ybar <- M^T ybar`` for one RK4 step ``M``, in place.  Each stage's
+        cotangent k_ibar = w_i g + c x_(i+1)bar is formed inside the transposed
+        right-hand side, which also adds the previous stage's x bar to
+        ``ybar``."""
         dt = self.dt
-        g, kb, xb = self.adj
+        g, xa, xb = self.adj
         g.copy_(ybar)
-        kb.copy_(g).mul_(dt / 6)
-        self.FT(kb, xb)
-        ybar.add_(xb)
-        kb.copy_(g).mul_(dt / 3).add_(xb, alpha=dt)
-        self.FT(kb, xb)
-        ybar.add_(xb)
-        kb.copy_(g).mul_(dt / 3).add_(xb, alpha=dt / 2)
-        self.FT(kb, xb)
-        ybar.add_(xb)
-        kb.copy_(g).mul_(dt / 6).add_(xb, alpha=dt / 2)
-        self.rhs(kb, xb, adjoint=True)
+        self.stage_adjoint(g, dt / 6, None, 0.0, xa, None)         # x4bar = P^T R^T k4bar
+        self.batch.fill_adjoint(xa)
+        self.stage_adjoint(g, dt / 3, xa, dt, xb, ybar)            # x3bar; ybar += x4bar
+        self.batch.fill_adjoint(xb)
+        self.stage_adjoint(g, dt / 3, xb, dt / 2, xa, ybar)        # x2bar; ybar += x3bar
+        self.batch.fill_adjoint(xa)
+        self.stage_adjoint(g, dt / 6, xa, dt / 2, xb, ybar)        # R^T k1bar; ybar += x2bar
         ybar.add_(xb)
         self.batch.fill_adjoint(ybar)
         return ybar
