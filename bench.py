@@ -468,6 +468,29 @@ def main():
                "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms}
     del yadj
 
+    # the state vector's copies (scatter!/gather!) and one right-hand side's
+    # scatter + fill, on the same mesh
+    from treeamr.state import gather, scatter, scatter_fill, statelength, statevector
+    u = statevector(fs)
+    gather(u, fs)
+    state_bytes = 2 * u.numel() * u.element_size()         # one read + one write per entry
+    ms_scatter = timed(lambda: scatter(fs, u), max(3, args.steps // 2))
+    ms_gather = timed(lambda: gather(u, fs), max(3, args.steps // 2))
+    ms_sf = timed(lambda: scatter_fill(fs, sched, u), max(3, args.steps // 2))
+    peaks0 = {}
+    try:
+        peaks0 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks0.get("hbm_gbs", 6800.0))
+    state = {"entries": u.numel(), "bytes_per_copy": state_bytes,
+             "scatter_ms": ms_scatter, "gather_ms": ms_gather,
+             "scatter_gbs": state_bytes / (ms_scatter * 1e-3) / 1e9,
+             "gather_gbs": state_bytes / (ms_gather * 1e-3) / 1e9,
+             "scatter_frac_of_hbm": state_bytes / (ms_scatter * 1e-3) / 1e9 / hbm,
+             "scatter_fill_ms": ms_sf}
+    del u
+
     # per-stage launches of the fused kernel, CUDA events on the launching stream
     stage_ms = {}
     stage_bytes = {}
@@ -570,6 +593,7 @@ def main():
             "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
                       "speedup_fused_vs_plain": ms_plain / ms},
             "adjoint": adjoint,
+            "state": state,
             "workloads": walls,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,

@@ -266,6 +266,26 @@ int tam_wave_rk4_adjoint_stage(int32_t dtype, const tam_wave_block *blocks, int3
                                const void *xprev, double c2, void *out, void *ybar,
                                void *stream);
 
+/* The state vector and the working array (src/state.jl:101-160): the
+ * state holds every block's own points only, shape (own_1, own_2, own_3,
+ * nvars, nblocks) column-major with own_d = N + c_d; own point i_d is stored
+ * index ghosts_d + i_d (0-based) of the working array (stored_1, stored_2,
+ * stored_3, nvars, nblocks).  Unused dimensions: own = stored = 1, ghosts = 0. */
+typedef struct tam_state_layout {
+  int32_t dtype;       /* TAM_F32 or TAM_F64                                */
+  int32_t ndim;
+  int32_t own[3];
+  int32_t stored[3];
+  int32_t ghosts[3];
+  int32_t nvars;
+  int64_t nblocks;
+} tam_state_layout;
+/* scatter!: state -> the working array's own points; ghosts untouched.
+ * gather!: the working array's own points -> state.  Device pointers,
+ * asynchronous on `stream`; bits are copied, NaN payloads and -0 kept. */
+int tam_scatter(const tam_state_layout *layout, const void *state, void *work, void *stream);
+int tam_gather(const tam_state_layout *layout, const void *work, void *state, void *stream);
+
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing
  * one changes speed only, never a result. */

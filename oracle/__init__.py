@@ -121,3 +121,27 @@ def fill_fieldset(fs, schedule, *, boundary_values=None, nthreads: int = 1,
     boundary_values(host, fs, schedule.boundaries)
     return fill(schedule, host, fs.nvars, fs.factors_host, first=2, nthreads=nthreads,
                 one_tap=one_tap)
+
+
+def _own_slices(fs):
+    """Own range ``G_d+1 : G_d+N+c_d`` per dimension, in the host array's
+    reversed index order."""
+    N = fs.forest.N
+    return tuple(slice(g, g + N + cd) for g, cd in reversed(list(zip(fs.G, fs.c))))
+
+
+def scatter(fs, work: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """``scatter!`` (src/state.jl:101-106, 130-141): the state vector's
+    entries, in the working array's order without ghosts, into the own
+    points of ``work`` (shape (nblocks, nvars, S_D..S_1)); ghosts untouched."""
+    own = _own_slices(fs)
+    shape = work[(slice(None), slice(None)) + own].shape
+    work[(slice(None), slice(None)) + own] = u.reshape(shape)
+    return work
+
+
+def gather(fs, work: np.ndarray) -> np.ndarray:
+    """``gather!`` (src/state.jl:108-113, 143-160): the own points of ``work``
+    as a flat state vector."""
+    own = _own_slices(fs)
+    return np.ascontiguousarray(work[(slice(None), slice(None)) + own]).ravel()

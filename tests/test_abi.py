@@ -42,6 +42,9 @@ def test_struct_layout_matches_header():
     assert C.sizeof(_native.tam_stencil) == 32
     assert C.sizeof(_native.tam_group) == 16 + 16 + 3 * 32
     assert _native.tam_schedule_desc.groups.offset == 40
+    assert C.sizeof(_native.tam_state_layout) == 56
+    assert _native.tam_state_layout.nblocks.offset == 48
+    assert _native.tam_state_layout.ghosts.offset == 32
 
 
 def test_calls_fail_cleanly_without_arguments():
@@ -52,6 +55,8 @@ def test_calls_fail_cleanly_without_arguments():
     assert b"NULL" in buf.value
     assert lib.tam_fill(None, None, 1, 1, None, -1, 1, None) != 0
     assert lib.tam_schedule_upload(None, None, None) != 0
+    assert lib.tam_scatter(None, None, None, None) != 0
+    assert lib.tam_gather(None, None, None, None) != 0
 
 
 def test_no_gpu_init_reports_an_error():

@@ -1,0 +1,103 @@
+// The copies between a state vector and the working array: scatter! and
+// gather! (src/state.jl:101-160).
+//
+// The state vector holds every block's own points only, in the working
+// array's index order minus the ghosts: shape (O_1, O_2, O_3, nvars, nblocks)
+// with O_d = N + c_d, against (S_1, S_2, S_3, nvars, nblocks) for the
+// working array, own point i_d at stored index G_d + i_d (0-based).  Both
+// are column-major, so a row of O_1 state entries is a contiguous run of the
+// working array too.  A CTA takes whole rows (blockDim / O_1 of them at a
+// time, a thread per entry), so the state side is read or written in one
+// linear sweep and the working side in runs of O_1; a row's position is two
+// divisions per thread, none per entry.  Bits are moved, not arithmetic:
+// NaN payloads and -0 survive.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "tam_internal.h"
+#include "treeamr_cuda.h"
+
+namespace {
+
+template <typename T, bool TO_WORK>
+__global__ void __launch_bounds__(256) state_copy_kernel(T *__restrict__ work,
+                                                         T *__restrict__ state, int64_t nrows,
+                                                         int O1, int O2, int O3, int S1, int S2,
+                                                         int S3, int G1, int G2, int G3) {
+  const int rpi = blockDim.x / O1;  // rows a CTA takes at a time
+  const int lr = threadIdx.x / O1, e = threadIdx.x - lr * O1;
+  if (lr >= rpi) return;
+  for (int64_t r0 = (int64_t)blockIdx.x * rpi; r0 < nrows; r0 += (int64_t)gridDim.x * rpi) {
+    const int64_t r = r0 + lr;
+    if (r >= nrows) continue;
+    const int64_t q = r / O2;
+    const int i2 = (int)(r - q * O2);
+    const int64_t vb = q / O3;
+    const int i3 = (int)(q - vb * O3);
+    const int64_t w = ((vb * S3 + i3 + G3) * S2 + i2 + G2) * (int64_t)S1 + G1 + e;
+    const int64_t s = r * O1 + e;
+    if (TO_WORK)
+      work[w] = state[s];
+    else
+      state[s] = work[w];
+  }
+}
+
+template <typename T>
+cudaError_t launch(bool to_work, T *work, T *state, int64_t nrows, const int O[3],
+                   const int S[3], const int G[3], cudaStream_t stream) {
+  const int threads = O[0] <= 256 ? 256 : 1024;
+  const int rpi = threads / O[0];
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (nrows + rpi - 1) / rpi;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)nsm * 32));
+  if (to_work)
+    state_copy_kernel<T, true><<<(unsigned)blocks, threads, 0, stream>>>(
+        work, state, nrows, O[0], O[1], O[2], S[0], S[1], S[2], G[0], G[1], G[2]);
+  else
+    state_copy_kernel<T, false><<<(unsigned)blocks, threads, 0, stream>>>(
+        work, state, nrows, O[0], O[1], O[2], S[0], S[1], S[2], G[0], G[1], G[2]);
+  return cudaGetLastError();
+}
+
+int state_copy(bool to_work, const tam_state_layout *L, void *work, void *state,
+               void *stream) {
+  if (!L || !work || !state) return TAM_EINVAL;
+  if (L->ndim < 1 || L->ndim > 3 || L->nvars < 1 || L->nblocks < 0) return TAM_EINVAL;
+  int O[3] = {1, 1, 1}, S[3] = {1, 1, 1}, G[3] = {0, 0, 0};
+  for (int d = 0; d < L->ndim; ++d) {
+    O[d] = L->own[d];
+    S[d] = L->stored[d];
+    G[d] = L->ghosts[d];
+    if (O[d] < 1 || G[d] < 0 || G[d] + O[d] > S[d]) return TAM_ELAYOUT;
+  }
+  if (O[0] > 1024) return TAM_EUNSUPPORTED;
+  const int64_t nrows = (int64_t)O[1] * O[2] * L->nvars * L->nblocks;
+  if (nrows == 0) return TAM_OK;
+  cudaError_t e;
+  if (L->dtype == TAM_F64)
+    e = launch<double>(to_work, (double *)work, (double *)state, nrows, O, S, G,
+                       (cudaStream_t)stream);
+  else if (L->dtype == TAM_F32)
+    e = launch<float>(to_work, (float *)work, (float *)state, nrows, O, S, G,
+                      (cudaStream_t)stream);
+  else
+    return TAM_EINVAL;
+  return e == cudaSuccess ? TAM_OK : TAM_ECUDA;
+}
+
+}  // namespace
+
+extern "C" int tam_scatter(const tam_state_layout *layout, const void *state, void *work,
+                           void *stream) {
+  return state_copy(true, layout, work, const_cast<void *>(state), stream);
+}
+
+extern "C" int tam_gather(const tam_state_layout *layout, const void *work, void *state,
+                          void *stream) {
+  return state_copy(false, layout, const_cast<void *>(work), state, stream);
+}

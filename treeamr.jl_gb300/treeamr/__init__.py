@@ -11,6 +11,7 @@ from .storage import (EvenParity, FieldSet, NoParity, OddParity, cellcentered, c
                       staggers, vertexcentered)
 from .schedule import GhostSchedule, TransferGroup, Stencil1D, GroupKey
 from .ghosts import boundary_by_coordinates, fill_ghosts
+from .state import gather, scatter, scatter_fill, statearray, statelength, statevector
 
 __all__ = [
     "Forest", "MortonKey", "alldirections", "childoffset", "curve_key", "parentkey",
@@ -20,4 +21,5 @@ __all__ = [
     "staggers", "coordinates",
     "GhostSchedule", "TransferGroup", "Stencil1D", "GroupKey",
     "fill_ghosts", "boundary_by_coordinates",
+    "statelength", "statevector", "statearray", "scatter", "gather", "scatter_fill",
 ]

@@ -30,7 +30,8 @@ TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu"]
+SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu",
+           "tam_state.cu"]
 
 
 class tam_stencil(C.Structure):
@@ -52,6 +53,12 @@ class tam_schedule_desc(C.Structure):
                 ("sourceblocks", C.POINTER(C.c_int32)), ("nsrcstart", C.c_int64),
                 ("srcstart", C.POINTER(C.c_int32)), ("nweights", C.c_int64),
                 ("weights", C.c_void_p)]
+
+
+class tam_state_layout(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("ndim", C.c_int32), ("own", C.c_int32 * 3),
+                ("stored", C.c_int32 * 3), ("ghosts", C.c_int32 * 3), ("nvars", C.c_int32),
+                ("nblocks", C.c_int64)]
 
 
 def _ptr(a: np.ndarray, ctype):
@@ -208,6 +215,10 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_scatter.argtypes = [C.POINTER(tam_state_layout), vp, vp, vp]
+    lib.tam_scatter.restype = C.c_int
+    lib.tam_gather.argtypes = [C.POINTER(tam_state_layout), vp, vp, vp]
+    lib.tam_gather.restype = C.c_int
     lib.tam_fill_host.argtypes = [vp, vp, vp, vp, i32, i64, vp, i32, i32, vp]
     lib.tam_fill_host.restype = C.c_int
     lib.tam_device_status.argtypes = [vp, vp, C.POINTER(i32)]
