@@ -233,6 +233,13 @@ def measure_walls(T, dev, timed, args, peak):
     ms = timed(lambda: fill_ghosts(fs, sched), steps)
     fill_ghosts(fs, sched, method="plain")
     ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(2, steps // 2))
+    # unify! of the set (stages P and 0 alone: every secondary copy of a
+    # shared point takes its primary's value)
+    from treeamr.unify import unify
+    unify(fs, sched)
+    ms_unify = timed(lambda: unify(fs, sched), max(2, steps // 2))
+    unify_bytes = 2 * esize * fs.nvars * sum(int(np.prod(g.boxsize())) * g.ntransfers()
+                                             for g in sched.groups if g.stage <= 0)
     ds = device_schedule(sched, dev.index)
     stream = torch.cuda.current_stream(dev)
     tags = sorted({gr.stage for gr in sched.groups})
@@ -265,6 +272,8 @@ def measure_walls(T, dev, timed, args, peak):
                      "frac": achieved / peak,
                      "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()}},
         "fp64": fp,
+        "unify": {"ms": ms_unify, "bytes": unify_bytes,
+                  "gbs": unify_bytes / (ms_unify * 1e-3) / 1e9},
         "tuned": tuned,
         "gpu_launches_per_fill": fused_launches(sched),
     }

@@ -33,6 +33,18 @@ def vertexcentered(D: int) -> Tuple[str, ...]:
     return ("vertex",) * D
 
 
+def facecentered(D: int, d: int) -> Tuple[str, ...]:
+    """Vertex-like along dimension ``d`` (1-based), cell-like along the others:
+    a flux through the faces normal to ``d``."""
+    return tuple("vertex" if e == d - 1 else "cell" for e in range(D))
+
+
+def edgecentered(D: int, d: int) -> Tuple[str, ...]:
+    """Cell-like along dimension ``d`` (1-based), vertex-like along the others:
+    a quantity on the edges that run along ``d``."""
+    return tuple("cell" if e == d - 1 else "vertex" for e in range(D))
+
+
 def staggers(centering: Sequence[str]) -> Tuple[int, ...]:
     """``c_d = 1`` along a vertex-like dimension, 0 along a cell-like one."""
     for c in centering:
