@@ -282,6 +282,38 @@ def measure_walls(T, dev, timed, args, peak):
     return out
 
 
+def measure_hook(dev, timed, args):
+    """The device boundary hook (CellBoundary with a built-in quadratic
+    polynomial): the sphere mesh without periodic faces, 4^3 roots, N=16,
+    G=3, 3 levels, 4 Float64 variables; the fill with the hook against the
+    same stages without it."""
+    import torch
+    from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+    from treeamr.boundary import CellBoundary, Polynomial
+    from treeamr.ghosts import device_schedule
+    from treeamr import _native
+    f = meshes.sphere_forest(roots=4, N=16, levels=3, periodic=False)
+    fs = FieldSet(f, args.nvars, G=3, T=np.float64, device=dev)
+    sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    fs.work.uniform_(-1.0, 1.0)
+    terms = {(0, 0, 0): [1.0] * args.nvars, (1, 0, 0): [0.5] * args.nvars,
+             (0, 1, 0): [-0.25] * args.nvars, (0, 0, 2): [0.125] * args.nvars}
+    hook = CellBoundary(Polynomial(terms))
+    fill_ghosts(fs, sched, boundary=hook)
+    steps = max(3, args.steps // 2)
+    ms_hook = timed(lambda: fill_ghosts(fs, sched, boundary=hook), steps)
+    ms_plain = timed(lambda: fill_ghosts(fs, sched), steps)
+    pts = sum(int(np.prod([z - a + 1 for a, z in r.region])) for r in sched.boundaries)
+    out = {"workload": "sphere without periodic faces: 4^3 roots, N=16, G=3, 3 levels, "
+                       f"{args.nvars} vars F64, PV(4,4), quadratic polynomial boundary",
+           "blocks": f.nleaves(), "regions": len(sched.boundaries),
+           "hook_points_per_var": pts, "fill_with_hook_ms": ms_hook,
+           "fill_without_hook_ms": ms_plain, "hook_ms": ms_hook - ms_plain}
+    del fs, sched
+    torch.cuda.empty_cache()
+    return out
+
+
 def workload_config(args, f, sched):
     return {
         "workload": "sphere: 3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, PV(4,4), "
@@ -546,6 +578,7 @@ def main():
         for T in (np.float32, np.float64):
             walls["walls_" + np.dtype(T).name] = measure_walls(T, dev, timed, args, peak)
         walls["batch64_float32"] = measure_batch(dev, timed, args, peak)
+        walls["boundary_hook"] = measure_hook(dev, timed, args)
 
     # end to end through the public call, host buffers, copies inside the timing
     e2e = None

@@ -266,6 +266,38 @@ int tam_wave_rk4_adjoint_stage(int32_t dtype, const tam_wave_block *blocks, int3
                                const void *xprev, double c2, void *out, void *ybar,
                                void *stream);
 
+/* The cell-wise boundary hook on the device (CellBoundary,
+ * src/ghosts.jl:1166-1318) with a built-in function of position: every ghost
+ * of every region beyond an outer face gets g(x, v), x formed as
+ * nodeposition forms it (fma(T(m), s, lo), src/storage.jl:1008-1017).
+ * TAM_BC_CONSTANT: g = coef[v].  TAM_BC_POLYNOMIAL: g = sum over the terms q
+ * of ((coef[v*nterms+q] * x1^a) * x2^b) * x3^c, (a, b, c) = exps[q], powers
+ * by repeated multiplication, summed in term order from +0, every operation
+ * rounded once.  Regions and coef are device arrays; regions' blocks are
+ * 0-based, first 1-based stored indices.  Asynchronous on stream. */
+#define TAM_BC_CONSTANT 1
+#define TAM_BC_POLYNOMIAL 2
+#define TAM_BC_MAX_TERMS 20
+typedef struct tam_boundary_region {
+  int32_t block;       /* 0-based                                            */
+  int32_t first[3];    /* 1-based stored index of the region's first point  */
+  int32_t n[3];        /* extent per dimension (1 beyond ndim)              */
+  int32_t ghosts[3];   /* the layout's ghost widths G_d                      */
+  int32_t stagger[3];  /* c_d: 1 vertex-like, 0 cell-like                    */
+  int32_t pad;
+  int64_t base[3];     /* the block's integer base B_d (nodeposition)        */
+  double lo[3];        /* the domain's low corner along d, in T              */
+  double h;            /* the block's spacing, in T                          */
+} tam_boundary_region;
+typedef struct tam_boundary_fn {
+  int32_t kind;
+  int32_t nterms;
+  int32_t exps[TAM_BC_MAX_TERMS][3];
+} tam_boundary_fn;
+int tam_boundary_apply(int32_t dtype, const tam_boundary_region *regions, int32_t nregions,
+                       tam_boundary_fn fn, const void *coef, void *work, int32_t nvars,
+                       const int32_t stored[3], void *stream);
+
 /* The state vector and the working array (src/state.jl:101-160): the
  * state holds every block's own points only, shape (own_1, own_2, own_3,
  * nvars, nblocks) column-major with own_d = N + c_d; own point i_d is stored

@@ -145,3 +145,34 @@ def gather(fs, work: np.ndarray) -> np.ndarray:
     as a flat state vector."""
     own = _own_slices(fs)
     return np.ascontiguousarray(work[(slice(None), slice(None)) + own]).ravel()
+
+
+def cell_boundary(fs, host: np.ndarray, regions, g) -> np.ndarray:
+    """The device hook's built-in functions evaluated on the host, in place on
+    ``host``: every point of every region gets ``g(x, v)``, ``x`` the exactly
+    rounded ``nodeposition`` (``src/storage.jl:1008-1017``, through
+    ``FieldSet.positions``), a polynomial's terms ``((c * x1^a) * x2^b) *
+    x3^c`` with powers by repeated multiplication, summed in order from +0,
+    every operation rounded once in the element type."""
+    from treeamr.boundary import Constant
+    T = np.dtype(fs.T).type
+    D = fs.D
+    for r in regions:
+        pos = fs.positions(r.block)
+        idxs = [range(a, z + 1) for a, z in r.region]
+        for I in np.ndindex(*[len(i) for i in idxs]):
+            idx = tuple(idxs[d][I[d]] for d in range(D))
+            x = [T(pos[d][idx[d] - 1]) for d in range(D)]
+            for v in range(fs.nvars):
+                if isinstance(g, Constant):
+                    val = T(g.values[v])
+                else:
+                    val = T(0)
+                    for exps, coefs in g.terms:
+                        term = T(coefs[v])
+                        for d, e in enumerate(exps):
+                            for _ in range(e):
+                                term = T(term * x[d])
+                        val = T(val + term)
+                host[(r.block, v) + tuple(i - 1 for i in reversed(idx))] = val
+    return host

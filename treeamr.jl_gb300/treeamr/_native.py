@@ -31,7 +31,7 @@ TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu",
-           "tam_state.cu"]
+           "tam_state.cu", "tam_boundary.cu"]
 
 
 class tam_stencil(C.Structure):
@@ -53,6 +53,20 @@ class tam_schedule_desc(C.Structure):
                 ("sourceblocks", C.POINTER(C.c_int32)), ("nsrcstart", C.c_int64),
                 ("srcstart", C.POINTER(C.c_int32)), ("nweights", C.c_int64),
                 ("weights", C.c_void_p)]
+
+
+TAM_BC_CONSTANT, TAM_BC_POLYNOMIAL, TAM_BC_MAX_TERMS = 1, 2, 20
+
+
+class tam_boundary_region(C.Structure):
+    _fields_ = [("block", C.c_int32), ("first", C.c_int32 * 3), ("n", C.c_int32 * 3),
+                ("ghosts", C.c_int32 * 3), ("stagger", C.c_int32 * 3), ("pad", C.c_int32),
+                ("base", C.c_int64 * 3), ("lo", C.c_double * 3), ("h", C.c_double)]
+
+
+class tam_boundary_fn(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nterms", C.c_int32),
+                ("exps", (C.c_int32 * 3) * TAM_BC_MAX_TERMS)]
 
 
 class tam_state_layout(C.Structure):
@@ -215,6 +229,9 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_boundary_apply.argtypes = [i32, vp, i32, tam_boundary_fn, vp, vp, i32,
+                                       C.POINTER(C.c_int32), vp]
+    lib.tam_boundary_apply.restype = C.c_int
     lib.tam_scatter.argtypes = [C.POINTER(tam_state_layout), vp, vp, vp]
     lib.tam_scatter.restype = C.c_int
     lib.tam_gather.argtypes = [C.POINTER(tam_state_layout), vp, vp, vp]

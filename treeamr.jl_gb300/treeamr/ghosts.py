@@ -153,7 +153,11 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
         ds.run(fs, _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST, method, stream)
         return fs
     ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
-    boundary(fs, schedule.boundaries)
+    from .boundary import CellBoundary
+    if isinstance(boundary, CellBoundary):
+        boundary.apply(fs, schedule, stream)        # the device hook
+    else:
+        boundary(fs, schedule.boundaries)           # the region form, on the host
     ds.run(fs, PHASE1_TAG + 1, _native.TAM_STAGE_ALL_LAST, method, stream)
     return fs
 

@@ -50,11 +50,13 @@ def quadrant_forest(seed: int = 0) -> Forest:
     return f
 
 
-def sphere_forest(roots: int = 8, N: int = 16, levels: int = 3, radius: float = 0.25) -> Forest:
-    """3-D, ``roots^3`` periodic roots over the unit cube; ``levels`` nested
-    refinements of every leaf whose box meets the sphere ``|x - 1/2| = radius``,
-    each followed by balance."""
-    f = Forest((roots,) * 3, N=N, periodic=(True,) * 3, extents=((0.0, 1.0),) * 3)
+def sphere_forest(roots: int = 8, N: int = 16, levels: int = 3, radius: float = 0.25,
+                  periodic: bool = True) -> Forest:
+    """3-D, ``roots^3`` roots over the unit cube, periodic unless asked not to
+    be (then every face is an outer face, filled by the boundary hook);
+    ``levels`` nested refinements of every leaf whose box meets the sphere
+    ``|x - 1/2| = radius``, each followed by balance."""
+    f = Forest((roots,) * 3, N=N, periodic=(periodic,) * 3, extents=((0.0, 1.0),) * 3)
     c = (0.5, 0.5, 0.5)
     return refine_where(f, lambda ext: _box_meets_sphere(ext, c, radius), range(levels))
 
