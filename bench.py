@@ -314,6 +314,44 @@ def measure_hook(dev, timed, args):
     return out
 
 
+def measure_regrid(dev, timed, args):
+    """The regrid transfer (``regrid!``'s move of the own points) on the
+    sphere mesh: every level-0 leaf with x < 0.25 refined and a tenth of the
+    finest families coarsened, then balanced; 4 Float64 variables, PV(4,4).
+    Algorithmic bytes: one read and one write per new own point-variable."""
+    import torch
+    from treeamr import Operators, meshes
+    from treeamr.forest import parentkey, sortedchildkeys
+    from treeamr.regrid import RegridTransfer
+    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
+    old = list(f.leaves)
+    refine = [k for k in old if k.level == 0 and f.block_extent(k)[0][1] <= 0.25]
+    top = max(k.level for k in old)
+    index = set(old)
+    fams = sorted({parentkey(k) for k in old if k.level == top})
+    fams = [p for p in fams if all(c in index for c in sortedchildkeys(p))][::10]
+    f.refine(refine)
+    f.coarsen(fams)
+    f.balance()
+    t = RegridTransfer(f, old, 3, ("cell",) * 3, np.float64,
+                       Operators(prolongation=4, restriction=4))
+    S = t.stored
+    a = torch.empty((len(old), args.nvars) + tuple(reversed(S)), dtype=torch.float64, device=dev)
+    a.uniform_(-1.0, 1.0)
+    b = torch.zeros((f.nleaves(), args.nvars) + tuple(reversed(S)), dtype=torch.float64,
+                    device=dev)
+    t.run(a, b, args.nvars)
+    ms = timed(lambda: t.run(a, b, args.nvars), max(3, args.steps // 2))
+    pts = f.nleaves() * 16 ** 3 * args.nvars
+    out = {"workload": f"sphere {args.roots}^3 roots, {args.levels} levels: {len(refine)} "
+                       f"level-0 leaves refined, {len(fams)} finest families coarsened",
+           "old_blocks": len(old), "new_blocks": f.nleaves(), "transfers": t.counts(),
+           "ms": ms, "gbs": 2 * 8 * pts / (ms * 1e-3) / 1e9}
+    del a, b, t
+    torch.cuda.empty_cache()
+    return out
+
+
 def workload_config(args, f, sched):
     return {
         "workload": "sphere: 3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, PV(4,4), "
@@ -579,6 +617,7 @@ def main():
             walls["walls_" + np.dtype(T).name] = measure_walls(T, dev, timed, args, peak)
         walls["batch64_float32"] = measure_batch(dev, timed, args, peak)
         walls["boundary_hook"] = measure_hook(dev, timed, args)
+        walls["regrid"] = measure_regrid(dev, timed, args)
 
     # end to end through the public call, host buffers, copies inside the timing
     e2e = None

@@ -152,6 +152,20 @@ int tam_fill_host(tam_sched *s, const void *host_in, void *host_out, void *devic
                   int32_t nvars, int64_t nblocks, const void *factors, int32_t first_stage,
                   int32_t last_stage, void *stream);
 
+/* The regrid transfer (src/regrid.jl:585-756, 942-955): the serial transfer
+ * groups from the leaves before a refinement or coarsening (sources, blocks
+ * of the old array) to the leaves after (targets, blocks of the new array),
+ * every target the new block's own range: a copy of a kept leaf, a
+ * prolongation from the parent of a created one, a restriction from each
+ * child of a coarsened one.  tam_regrid_upload takes the descriptor with
+ * nblocks the new count and the old count beside it; tam_regrid_transfer
+ * reads old_work and writes new_work (distinct arrays of one layout),
+ * asynchronous on stream.  The ghosts are left to the next fill. */
+int tam_regrid_upload(tam_ctx *ctx, const tam_schedule_desc *desc, int64_t old_nblocks,
+                      tam_sched **out);
+int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
+                        void *new_work, int64_t new_nblocks, int32_t nvars, void *stream);
+
 /* The plain fill: one launch per TransferGroup, one thread per
  * point-variable, as the reference's device path launches transfer_kernel!
  * (src/ghosts.jl:420-521).  Same arguments and results as tam_fill. */

@@ -90,7 +90,7 @@ void free_sched_device(tam_sched *s) {
 // Every check that makes a fill memory-safe: indices into the pools, block
 // indices, and each stencil's target rows and source windows inside the
 // stored extent.
-int validate(tam_ctx *ctx, const tam_schedule_desc *d) {
+int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
   char buf[256];
   if (!d) return fail(ctx, TAM_EINVAL, "schedule descriptor is NULL");
   if (d->abi_version != TAM_ABI_VERSION) {
@@ -116,11 +116,13 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d) {
   for (int k = 0; k < d->ndim; ++k) maxcols *= 3;
   for (int k = 0; k < d->ndim; ++k)
     if (d->stored[k] < 1) return fail(ctx, TAM_EINVAL, "stored extents must be positive");
+  if (nsource < 0 || nsource > INT32_MAX) return fail(ctx, TAM_EINVAL, "bad source block count");
   for (int64_t t = 0; t < d->ntransfers; ++t) {
     if (d->targetblocks[t] < 1 || d->targetblocks[t] > d->nblocks ||
-        d->sourceblocks[t] < 1 || d->sourceblocks[t] > d->nblocks) {
-      snprintf(buf, sizeof buf, "transfer %lld names a block outside 1:%lld", (long long)t,
-               (long long)d->nblocks);
+        d->sourceblocks[t] < 1 || d->sourceblocks[t] > nsource) {
+      snprintf(buf, sizeof buf,
+               "transfer %lld names a block outside 1:%lld (targets) or 1:%lld (sources)",
+               (long long)t, (long long)d->nblocks, (long long)nsource);
       return fail(ctx, TAM_EINVAL, buf);
     }
   }
@@ -373,10 +375,24 @@ int tam_last_error(const tam_ctx *ctx, char *buf, size_t n) {
   return TAM_OK;
 }
 
+static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource,
+                           tam_sched **out);
+
 int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **out) {
-  if (!ctx || !out) return fail(ctx, TAM_EINVAL, "tam_schedule_upload: NULL argument");
+  if (!ctx || !out || !d) return fail(ctx, TAM_EINVAL, "tam_schedule_upload: NULL argument");
+  return schedule_upload(ctx, d, d->nblocks, out);
+}
+
+int tam_regrid_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t old_nblocks,
+                      tam_sched **out) {
+  if (!ctx || !out || !d) return fail(ctx, TAM_EINVAL, "tam_regrid_upload: NULL argument");
+  return schedule_upload(ctx, d, old_nblocks, out);
+}
+
+static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource,
+                           tam_sched **out) {
   *out = nullptr;
-  int rc = validate(ctx, d);
+  int rc = validate(ctx, d, nsource);
   if (rc != TAM_OK) return rc;
   DeviceGuard guard(ctx->device);
   if (!guard.ok()) return fail(ctx, TAM_ECUDA, "cannot make the context's device current");
@@ -388,6 +404,7 @@ int tam_schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, tam_sched **ou
   s->dtype = d->dtype;
   for (int k = 0; k < 3; ++k) s->S[k] = k < d->ndim ? d->stored[k] : 1;
   s->nblocks = d->nblocks;
+  s->nsource = nsource;
   s->nfactorcols = d->nfactorcols;
   s->ntransfers = d->ntransfers;
   s->host_groups.assign(d->groups, d->groups + d->ngroups);
@@ -643,7 +660,7 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const voi
     cudaError_t e = tam::launch_fused_stage(
         s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
         stage.nptiles,
-        sched_args(s), work, factors, nvars, s->S, s->shape.threads, st, &s->side);
+        sched_args(s), work, factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
   }
   return TAM_OK;
@@ -667,6 +684,31 @@ int tam_fill_host(tam_sched *s, const void *host_in, void *host_out, void *devic
   if (rc != TAM_OK) return rc;
   e = cudaMemcpyAsync(host_out, device_work, bytes, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "tam_fill_host download");
+  return TAM_OK;
+}
+
+int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
+                        void *new_work, int64_t new_nblocks, int32_t nvars, void *stream) {
+  if (!s || !old_work || !new_work)
+    return fail(s ? s->ctx : nullptr, TAM_EINVAL, "tam_regrid_transfer: NULL argument");
+  if (nvars < 1) return fail(s->ctx, TAM_EINVAL, "tam_regrid_transfer: nvars must be positive");
+  if (new_nblocks != s->nblocks || old_nblocks != s->nsource)
+    return fail(s->ctx, TAM_ELAYOUT,
+                "tam_regrid_transfer: the block counts differ from the transfer's");
+  if (s->needs_factors)
+    return fail(s->ctx, TAM_EUNSUPPORTED, "a regrid transfer takes no factor column");
+  if (old_work == new_work)
+    return fail(s->ctx, TAM_EINVAL, "tam_regrid_transfer: the old and new arrays must differ");
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  cudaStream_t st = (cudaStream_t)stream;
+  for (const tam::Stage &stage : s->stages) {
+    cudaError_t e = tam::launch_fused_stage(
+        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
+        stage.nptiles, sched_args(s), new_work, nullptr, nvars, s->S, s->shape.threads, st,
+        &s->side, old_work);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "regrid transfer launch");
+  }
   return TAM_OK;
 }
 

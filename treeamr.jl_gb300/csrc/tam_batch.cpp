@@ -299,7 +299,7 @@ int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars
     cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles + st.ptile0,
                                             st.npcopy0, st.npcopy, st.nptiles, args, arena, factor_arena,
                                             nvars, S, b->shape.threads, (cudaStream_t)stream,
-                                            &b->side);
+                                            &b->side, nullptr);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return bfail(b->ctx, TAM_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));

@@ -193,6 +193,7 @@ struct tam_sched {
   int dtype = 0;
   int S[3] = {1, 1, 1};
   int64_t nblocks = 0;
+  int64_t nsource = 0;        // source blocks: nblocks, or a regrid's old count
   int32_t nfactorcols = 0;
   bool needs_factors = false;
   std::vector<tam_group> host_groups;
@@ -257,12 +258,13 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
 // One stage: the packed tiles [0, npcopy) run the copy kernel (those from
 // npcopy0 on with their factor column) and [npcopy, nptiles) the stencil
 // kernel, on `stream` and, when `side` is given and both are present, the
-// stencils on the side stream alongside.
+// stencils on the side stream alongside.  Sources are read from `src` when
+// given (a regrid's old array), else from `work`.
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
                                int64_t npcopy0, int64_t npcopy, int64_t nptiles,
                                const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream, SideStream *side);
+                               cudaStream_t stream, SideStream *side, const void *src);
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);

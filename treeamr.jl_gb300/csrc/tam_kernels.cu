@@ -726,20 +726,21 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
 
 template <typename T, int D, bool BATCH, bool FACTOR>
 cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, const Args<T> &a,
-                          T *work, const T *factors, int nvars, const int S[3], int threads,
-                          cudaStream_t stream) {
+                          const T *src, T *work, const T *factors, int nvars, const int S[3],
+                          int threads, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   const int wpb = threads / 32;
   const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
   fused_copy_kernel<T, D, BATCH, FACTOR><<<(unsigned)blocks, threads, 0, stream>>>(
-      tiles, ptiles, n, a, work, work, factors, nvars, S[0], S[1], S[2]);
+      tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
   return cudaSuccess;
 }
 
 template <typename T, int D>
 cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
-                        int64_t nptiles, const Args<T> &a, T *work, const T *factors, int nvars,
-                        const int S[3], int threads, cudaStream_t stream, SideStream *side) {
+                        int64_t nptiles, const Args<T> &a, const T *src, T *work,
+                        const T *factors, int nvars, const int S[3], int threads,
+                        cudaStream_t stream, SideStream *side) {
   const int wpb = threads / 32;
   const bool batch = a.members != nullptr;
   const int64_t nst = nptiles - npcopy;
@@ -756,20 +757,20 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
     const int64_t blocks = std::min<int64_t>((nst + wpb - 1) / wpb, (int64_t)1 << 30);
     if (batch)
       fused_stage_kernel<T, D, true><<<(unsigned)blocks, threads, 0, sst>>>(
-          tiles, ptiles + npcopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+          tiles, ptiles + npcopy, nst, a, src, work, factors, nvars, S[0], S[1], S[2]);
     else
       fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, sst>>>(
-          tiles, ptiles + npcopy, nst, a, work, work, factors, nvars, S[0], S[1], S[2]);
+          tiles, ptiles + npcopy, nst, a, src, work, factors, nvars, S[0], S[1], S[2]);
   }
   if (batch) {
-    launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, work, factors, nvars, S,
+    launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
                                      threads, stream);
-    launch_copies<T, D, true, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, work,
+    launch_copies<T, D, true, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
                                     factors, nvars, S, threads, stream);
   } else {
-    launch_copies<T, D, false, false>(tiles, ptiles, npcopy0, a, work, factors, nvars, S,
+    launch_copies<T, D, false, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
                                       threads, stream);
-    launch_copies<T, D, false, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, work,
+    launch_copies<T, D, false, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
                                      factors, nvars, S, threads, stream);
   }
   if (fork) {
@@ -785,18 +786,18 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
 // point of the stage's targets).
 template <typename T>
 cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
-                           int64_t nptiles, const Args<T> &a, T *work, const T *factors, int nvars,
+                           int64_t nptiles, const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
                            const int S[3], int threads, cudaStream_t stream, SideStream *side) {
   if (nptiles == 0) return cudaSuccess;
   switch (D) {
     case 1:
-      return launch_both<T, 1>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 1>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
                                threads, stream, side);
     case 2:
-      return launch_both<T, 2>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 2>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
                                threads, stream, side);
     default:
-      return launch_both<T, 3>(tiles, ptiles, npcopy0, npcopy, nptiles, a, work, factors, nvars, S,
+      return launch_both<T, 3>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
                                threads, stream, side);
   }
 }
@@ -817,13 +818,15 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                int64_t npcopy0, int64_t npcopy, int64_t nptiles,
                                const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream, SideStream *side) {
+                               cudaStream_t stream, SideStream *side, const void *src) {
+  if (!src) src = work;
   if (dtype == TAM_F64)
     return fused_dispatch<double>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<double>(a),
-                                  (double *)work, (const double *)factors, nvars, S, threads,
-                                  stream, side);
-  return fused_dispatch<float>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<float>(a), (float *)work,
-                               (const float *)factors, nvars, S, threads, stream, side);
+                                  (const double *)src, (double *)work, (const double *)factors,
+                                  nvars, S, threads, stream, side);
+  return fused_dispatch<float>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<float>(a),
+                               (const float *)src, (float *)work, (const float *)factors, nvars,
+                               S, threads, stream, side);
 }
 
 void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,

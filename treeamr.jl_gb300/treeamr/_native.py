@@ -229,6 +229,10 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_regrid_upload.argtypes = [vp, C.POINTER(tam_schedule_desc), i64, C.POINTER(vp)]
+    lib.tam_regrid_upload.restype = C.c_int
+    lib.tam_regrid_transfer.argtypes = [vp, vp, i64, vp, i64, i32, vp]
+    lib.tam_regrid_transfer.restype = C.c_int
     lib.tam_boundary_apply.argtypes = [i32, vp, i32, tam_boundary_fn, vp, vp, i32,
                                        C.POINTER(C.c_int32), vp]
     lib.tam_boundary_apply.restype = C.c_int
