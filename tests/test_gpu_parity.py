@@ -2,9 +2,9 @@
 
 Every fill is compared with the oracle's fill of the same data bit for bit:
 the kernels evaluate the reference's expression in the reference's order
-with no fused multiply-add, so there is no tolerance to state (the north
-star's bound of 2 ulp in Float64 and 4 in Float32 for restriction and
-prolongation is met with 0).  NaN is compared as one pattern
+with no fused multiply-add, so there is no tolerance to state (a bound of
+2 ulp in Float64 and 4 in Float32 for restriction and prolongation would
+be met with 0).  NaN is compared as one pattern
 (``test/helpers/ghost.jl:191-219``)."""
 import numpy as np
 import pytest

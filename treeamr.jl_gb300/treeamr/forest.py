@@ -15,7 +15,7 @@ walks once per regrid (never on the per-fill path):
 * ``wall_direction`` -- ``src/forest.jl:1617-1630``.
 * ``refine`` / ``coarsen`` / ``balance`` -- ``src/forest.jl:1761-1890``.
 
-Rotating seams, half turns and glued patches are not part of this build
+Rotating seams, half turns and glued patches are not implemented here
 (no workload of the ghost-fill engine uses them).
 """
 from __future__ import annotations
