@@ -134,6 +134,31 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int64_t tblock = __ldg(a.tb + tg.x) - 1;
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
     const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
+    // A unit copy whose source rows step by +-1 (a translation or a mirror):
+    // its transpose is the same permutation read backwards, so the box is
+    // the target values in place, +0 + f * y as the weight-one passes give.
+    const bool direct = g.pclass == 0 && g.affine &&
+                        (n1 == 1 || g.cstep[0] != 0) && (n2 == 1 || g.cstep[1] != 0) &&
+                        (n3 == 1 || g.cstep[2] != 0);
+    if (direct) {
+      for (int v = 0; v < nvars; ++v) {
+        const T *yv = L.y + tblock * L.bs + v * L.vs;
+        const T f =
+            g.factorcol ? __ldg(L.factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
+        T *ov = out + (int64_t)v * h.fsize;
+        for (int k = tid; k < nO; k += nt) {
+          const int j3 = k / (f1 * f2), r = k - j3 * (f1 * f2), j2 = r / f1, j1 = r - j2 * f1;
+          const int i1 = g.cstep[0] < 0 ? n1 - 1 - j1 : j1;
+          const int i2 = g.cstep[1] < 0 ? n2 - 1 - j2 : j2;
+          const int i3 = g.cstep[2] < 0 ? n3 - 1 - j3 : j3;
+          T x = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
+                   (int64_t)(g.tf[2] + i3) * L.s3];
+          if (g.factorcol) x = A::mul(x, f);
+          ov[k] = A::add(x, T(0));
+        }
+      }
+      continue;
+    }
     for (int v = 0; v < nvars; ++v) {
       const T *yv = L.y + tblock * L.bs + v * L.vs;
       const T f =
