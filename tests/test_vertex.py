@@ -237,8 +237,14 @@ def test_gpu_one_tap_option_selects_the_form(cuda_lib, one_tap, T):
     ds = device_schedule(s, 0)
     ds.set_option("one_tap", one_tap)
     try:
-        fill_ghosts(fs, s)
-        torch.cuda.synchronize()
+        # both multiply paths: the integer pipe's meets the tables' zero
+        # products in the full sum and must hand those points to the FP64 pipe
+        for im in ((0, 1) if T == np.float64 else (0,)):
+            ds.set_option("int_mul", im)
+            fs.work.copy_(torch.from_numpy(host))
+            fill_ghosts(fs, s)
+            torch.cuda.synchronize()
+            assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), im
     finally:
         ds.set_option("one_tap", 1)
-    assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))
+        ds.set_option("int_mul", 0)

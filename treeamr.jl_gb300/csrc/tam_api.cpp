@@ -233,7 +233,9 @@ void build_product_table(const tam_schedule_desc *d, const tam_group &h, tam::De
       uint64_t b;
       memcpy(&b, &out[i], 8);
       const uint64_t e = (b >> 52) & 0x7FF;
-      ok = e >= 1 && e <= 2046 && (b & ((1ull << 29) - 1)) == 0;
+      // a zero product is allowed: the multiply flags it and the point takes
+      // the FP64 pipe, and the one-tap form never reaches it
+      ok = (b << 1) == 0 || (e >= 1 && e <= 2046 && (b & ((1ull << 29) - 1)) == 0);
     }
     g.shortw = ok ? 1 : 0;
   }

@@ -255,7 +255,10 @@ __device__ __forceinline__ ShortW short_weight(double w) {
   ShortW r;
   r.w = w;
   r.wm = (((whi & 0xFFFFFu) | 0x100000u) << 3) | (wlo >> 29);
-  r.we = (int)((whi >> 20) & 0x7FF) - 1023;
+  // a zero weight gets an exponent no datum can bring into range, so the
+  // multiply flags it and the point is recomputed on the FP64 pipe
+  const int ew = (int)((whi >> 20) & 0x7FF);
+  r.we = ew == 0 ? -4096 : ew - 1023;
   r.wsign = whi & 0x80000000u;
   return r;
 }
