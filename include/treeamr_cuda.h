@@ -287,8 +287,11 @@ int tam_wave_rk4_adjoint_stage(int32_t dtype, const tam_wave_block *blocks, int3
  * TAM_BC_CONSTANT: g = coef[v].  TAM_BC_POLYNOMIAL: g = sum over the terms q
  * of ((coef[v*nterms+q] * x1^a) * x2^b) * x3^c, (a, b, c) = exps[q], powers
  * by repeated multiplication, summed in term order from +0, every operation
- * rounded once.  Regions and coef are device arrays; regions' blocks are
- * 0-based, first 1-based stored indices.  Asynchronous on stream. */
+ * rounded once.  With fn.relative, the relative form (Relative,
+ * src/ghosts.jl:1431-1475): g(x_g) + (u(r) - g(x_r)), r the ghost's index
+ * with clamps[d] in place of it where clamps[d] != 0, read from work.
+ * Regions and coef are device arrays; regions' blocks are 0-based, first
+ * 1-based stored indices.  Asynchronous on stream. */
 #define TAM_BC_CONSTANT 1
 #define TAM_BC_POLYNOMIAL 2
 #define TAM_BC_MAX_TERMS 20
@@ -298,6 +301,8 @@ typedef struct tam_boundary_region {
   int32_t n[3];        /* extent per dimension (1 beyond ndim)              */
   int32_t ghosts[3];   /* the layout's ghost widths G_d                      */
   int32_t stagger[3];  /* c_d: 1 vertex-like, 0 cell-like                    */
+  int32_t clamps[3];   /* relative form: the nearest evolved point's stored */
+                       /* index along d, or 0 (the ghost's own index)        */
   int32_t pad;
   int64_t base[3];     /* the block's integer base B_d (nodeposition)        */
   double lo[3];        /* the domain's low corner along d, in T              */
@@ -306,6 +311,7 @@ typedef struct tam_boundary_region {
 typedef struct tam_boundary_fn {
   int32_t kind;
   int32_t nterms;
+  int32_t relative;    /* 1: Relative(g), the ghost is g(x_g) + (u(r) - g(x_r)) */
   int32_t exps[TAM_BC_MAX_TERMS][3];
 } tam_boundary_fn;
 int tam_boundary_apply(int32_t dtype, const tam_boundary_region *regions, int32_t nregions,

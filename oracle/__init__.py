@@ -153,26 +153,39 @@ def cell_boundary(fs, host: np.ndarray, regions, g) -> np.ndarray:
     rounded ``nodeposition`` (``src/storage.jl:1008-1017``, through
     ``FieldSet.positions``), a polynomial's terms ``((c * x1^a) * x2^b) *
     x3^c`` with powers by repeated multiplication, summed in order from +0,
-    every operation rounded once in the element type."""
-    from treeamr.boundary import Constant
+    every operation rounded once in the element type.  ``Relative(f)``
+    (``src/ghosts.jl:1431-1475``): ``f(x_g) + (u(r) - f(x_r))`` with ``r`` the
+    region's clamped index, read from ``host``."""
+    from treeamr.boundary import Constant, Relative
     T = np.dtype(fs.T).type
     D = fs.D
+    relative = isinstance(g, Relative)
+    f = g.f if relative else g
+
+    def ev(x, v):
+        if isinstance(f, Constant):
+            return T(f.values[v])
+        val = T(0)
+        for exps, coefs in f.terms:
+            term = T(coefs[v])
+            for d, e in enumerate(exps):
+                for _ in range(e):
+                    term = T(term * x[d])
+            val = T(val + term)
+        return val
+
     for r in regions:
         pos = fs.positions(r.block)
         idxs = [range(a, z + 1) for a, z in r.region]
         for I in np.ndindex(*[len(i) for i in idxs]):
             idx = tuple(idxs[d][I[d]] for d in range(D))
             x = [T(pos[d][idx[d] - 1]) for d in range(D)]
+            rr = tuple((r.clamps[d] if r.clamps and r.clamps[d] else idx[d]) for d in range(D))
+            xr = [T(pos[d][rr[d] - 1]) for d in range(D)]
             for v in range(fs.nvars):
-                if isinstance(g, Constant):
-                    val = T(g.values[v])
-                else:
-                    val = T(0)
-                    for exps, coefs in g.terms:
-                        term = T(coefs[v])
-                        for d, e in enumerate(exps):
-                            for _ in range(e):
-                                term = T(term * x[d])
-                        val = T(val + term)
+                val = ev(x, v)
+                if relative:
+                    ur = T(host[(r.block, v) + tuple(i - 1 for i in reversed(rr))])
+                    val = T(val + T(ur - ev(xr, v)))
                 host[(r.block, v) + tuple(i - 1 for i in reversed(idx))] = val
     return host

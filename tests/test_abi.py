@@ -43,9 +43,9 @@ def test_struct_layout_matches_header():
     assert C.sizeof(_native.tam_group) == 16 + 16 + 3 * 32
     assert _native.tam_schedule_desc.groups.offset == 40
     assert C.sizeof(_native.tam_state_layout) == 56
-    assert C.sizeof(_native.tam_boundary_region) == 112
-    assert _native.tam_boundary_region.base.offset == 56
-    assert C.sizeof(_native.tam_boundary_fn) == 8 + 12 * _native.TAM_BC_MAX_TERMS
+    assert C.sizeof(_native.tam_boundary_region) == 128
+    assert _native.tam_boundary_region.base.offset == 72
+    assert C.sizeof(_native.tam_boundary_fn) == 12 + 12 * _native.TAM_BC_MAX_TERMS
     assert _native.tam_state_layout.nblocks.offset == 48
     assert _native.tam_state_layout.ghosts.offset == 32
 

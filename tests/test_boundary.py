@@ -101,3 +101,60 @@ def test_gpu_polynomial_hook_keeps_the_fill_exact(cuda_lib):
     got = fs.work.cpu().numpy()
     assert not np.isnan(got).any()
     assert np.max(np.abs(got - host)) < 1e-10
+
+
+# --- the relative form ---------------------------------------------------------
+
+def _oracle_relative_fill(fs, s, g, host):
+    """The fill with the relative hook in parts: phase 1, the slot-1
+    regions, then each later stage followed by its slot's regions."""
+    from treeamr.schedule import PHASE1_TAG
+    out = oracle.fill(s, host, fs.nvars, fs.factors_host, last=PHASE1_TAG)
+    by = {}
+    for r in s.boundaries:
+        by.setdefault(r.slot, []).append(r)
+    oracle.cell_boundary(fs, out, by.get(PHASE1_TAG, []), g)
+    for tag in [t for t in s.stage_tags if t > PHASE1_TAG]:
+        oracle.fill(s, out, fs.nvars, fs.factors_host, first=tag, last=tag)
+        oracle.cell_boundary(fs, out, by.get(tag, []), g)
+    return out
+
+
+def test_relative_zero_is_a_zero_gradient_outflow():
+    """``Relative(0)``: every outer ghost equals the nearest evolved point
+    (``src/ghosts.jl:1445``), and a later slot exists on this mesh."""
+    from treeamr.boundary import Relative
+    D = 2
+    f = nested_forest(D, N=8)
+    fs = FieldSet(f, 2, G=2)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    rng = np.random.default_rng(2)
+    host = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    out = _oracle_relative_fill(fs, s, Relative(Constant([0.0, 0.0])), host.copy())
+    for r in s.boundaries:
+        idxs = [range(a, z + 1) for a, z in r.region]
+        for I in np.ndindex(*[len(i) for i in idxs]):
+            idx = tuple(idxs[d][I[d]] for d in range(D))
+            rr = tuple(r.clamps[d] or idx[d] for d in range(D))
+            for v in range(2):
+                assert out[(r.block, v) + tuple(i - 1 for i in reversed(idx))] == \
+                    out[(r.block, v) + tuple(i - 1 for i in reversed(rr))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_relative_hook_bit_exact(cuda_lib, D, T):
+    from treeamr.boundary import Relative
+    f = nested_forest(D, N=8)
+    fs = FieldSet(f, 2, G=2, T=T)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    g = Relative(_poly(D, 2))
+    rng = np.random.default_rng(7 + D)
+    host = rng.uniform(-1, 1, size=tuple(fs.work.shape)).astype(T)
+    expect = _oracle_relative_fill(fs, s, g, host.copy())
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fs.factors = fs.factors.cuda()
+    fill_ghosts(fs, s, boundary=CellBoundary(g))
+    torch.cuda.synchronize()
+    assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))

@@ -41,6 +41,26 @@ struct BArith<float> {
   }
 };
 
+// The built-in function at x for variable v.
+template <typename T>
+__device__ __forceinline__ T eval_fn(const tam_boundary_fn &fn, const T *__restrict__ coef, int v,
+                                     const T (&x)[3]) {
+  using A = BArith<T>;
+  if (fn.kind == TAM_BC_CONSTANT) return coef[v];
+  // sum over monomials in table order: ((c * x1^a) * x2^b) * x3^c, each
+  // power by repeated multiplication left to right, from +0
+  const T *cv = coef + (int64_t)v * fn.nterms;
+  T val = T(0);
+  for (int q = 0; q < fn.nterms; ++q) {
+    T term = cv[q];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      for (int e = 0; e < fn.exps[q][d]; ++e) term = A::mul(term, x[d]);
+    val = A::add(val, term);
+  }
+  return val;
+}
+
 // One CTA per region, a thread per (point, variable).
 template <typename T>
 __global__ void __launch_bounds__(256) boundary_kernel(const tam_boundary_region *__restrict__ regions,
@@ -67,20 +87,24 @@ __global__ void __launch_bounds__(256) boundary_kernel(const tam_boundary_region
         const T s = vertex ? (T)R.h : (T)R.h * T(0.5);
         x[d] = A::fma(m, s, (T)R.lo[d]);
       }
-      T val = T(0);
-      if (fn.kind == TAM_BC_CONSTANT) {
-        val = coef[v];
-      } else {
-        // sum over monomials in table order: ((c * x1^a) * x2^b) * x3^c,
-        // each power by repeated multiplication left to right, from +0
-        const T *cv = coef + (int64_t)v * fn.nterms;
-        for (int q = 0; q < fn.nterms; ++q) {
-          T term = cv[q];
+      T val = eval_fn(fn, coef, v, x);
+      if (fn.relative) {
+        // the nearest evolved point: the clamped index along components
+        // that leave the domain, the ghost's own along the others
+        int r[3];
+        T xr[3];
 #pragma unroll
-          for (int d = 0; d < 3; ++d)
-            for (int e = 0; e < fn.exps[q][d]; ++e) term = A::mul(term, x[d]);
-          val = A::add(val, term);
+        for (int d = 0; d < 3; ++d) {
+          r[d] = R.clamps[d] != 0 ? R.clamps[d] : idx[d];
+          const int64_t k = (int64_t)R.base[d] + r[d] - 1 - R.ghosts[d];
+          const bool vertex = R.stagger[d] == 1;
+          const T m = vertex ? (T)k : (T)(2 * k + 1);
+          const T s = vertex ? (T)R.h : (T)R.h * T(0.5);
+          xr[d] = A::fma(m, s, (T)R.lo[d]);
         }
+        const T ur = work[(int64_t)R.block * bs + v * vs + (r[0] - 1) + (int64_t)(r[1] - 1) * s2 +
+                          (int64_t)(r[2] - 1) * s3];
+        val = A::add(val, A::add(ur, -eval_fn(fn, coef, v, xr)));
       }
       work[(int64_t)R.block * bs + v * vs + (idx[0] - 1) + (int64_t)(idx[1] - 1) * s2 +
            (int64_t)(idx[2] - 1) * s3] = val;

@@ -60,12 +60,13 @@ TAM_BC_CONSTANT, TAM_BC_POLYNOMIAL, TAM_BC_MAX_TERMS = 1, 2, 20
 
 class tam_boundary_region(C.Structure):
     _fields_ = [("block", C.c_int32), ("first", C.c_int32 * 3), ("n", C.c_int32 * 3),
-                ("ghosts", C.c_int32 * 3), ("stagger", C.c_int32 * 3), ("pad", C.c_int32),
+                ("ghosts", C.c_int32 * 3), ("stagger", C.c_int32 * 3), ("clamps", C.c_int32 * 3),
+                ("pad", C.c_int32),
                 ("base", C.c_int64 * 3), ("lo", C.c_double * 3), ("h", C.c_double)]
 
 
 class tam_boundary_fn(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("nterms", C.c_int32),
+    _fields_ = [("kind", C.c_int32), ("nterms", C.c_int32), ("relative", C.c_int32),
                 ("exps", (C.c_int32 * 3) * TAM_BC_MAX_TERMS)]
 
 

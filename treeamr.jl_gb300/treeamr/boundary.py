@@ -9,12 +9,14 @@ and manufactured solutions use are built in: ``Constant(values)`` and
 roundings.  Either runs between phase 1 and the prolongations, as every
 hook does, over every ghost region facing out through an outer face, with
 the position of a ghost formed exactly as ``nodeposition`` forms it.
-``Relative`` and ``wall = "prescribed"`` are not built.
+``Relative(f)`` with such an ``f`` gives the relative form, run in parts
+after the stages that fill what it reads.  ``wall = "prescribed"`` is not
+built.
 """
 from __future__ import annotations
 
 import ctypes as C
-from typing import Dict, Mapping, Sequence, Tuple
+from typing import Dict, Mapping, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -46,22 +48,37 @@ class Polynomial:
             raise ValueError(f"a Polynomial holds at most {MAX_TERMS} terms")
 
 
+class Relative:
+    """The relative form (``src/ghosts.jl:1431-1475``): every ghost ``x_g``
+    beyond an outer face becomes ``f(x_g) + (u(x_r) - f(x_r))``, ``x_r`` the
+    nearest evolved point, evaluated in that order; ``f`` a ``Constant`` or
+    a ``Polynomial``."""
+
+    def __init__(self, f):
+        if not isinstance(f, (Constant, Polynomial)):
+            raise TypeError("Relative takes a Constant or a Polynomial")
+        self.f = f
+
+
 class CellBoundary:
-    """The device hook: ``CellBoundary(Constant(...))`` or
-    ``CellBoundary(Polynomial(...))``, passed as ``fill_ghosts(...,
-    boundary=hook)``."""
+    """The device hook: ``CellBoundary(Constant(...))``,
+    ``CellBoundary(Polynomial(...))`` or ``CellBoundary(Relative(...))``,
+    passed as ``fill_ghosts(..., boundary=hook)``."""
 
     def __init__(self, g, wall: str = "evolved"):
-        if not isinstance(g, (Constant, Polynomial)):
-            raise TypeError("CellBoundary takes a Constant or a Polynomial: a function "
-                            "written above the C ABI cannot run in the device kernel")
+        if not isinstance(g, (Constant, Polynomial, Relative)):
+            raise TypeError("CellBoundary takes a Constant, a Polynomial or a Relative of one: "
+                            "a function written above the C ABI cannot run in the device "
+                            "kernel")
         if wall != "evolved":
             raise ValueError("wall must be 'evolved': a prescribed wall plane is not built")
-        self.g = g
+        self.relative = isinstance(g, Relative)
+        self.g = g.f if self.relative else g
 
     # -- the device side ---------------------------------------------------------
     def _fn(self, fs: FieldSet):
         fn = _native.tam_boundary_fn()
+        fn.relative = 1 if self.relative else 0
         nv = fs.nvars
         if isinstance(self.g, Constant):
             if len(self.g.values) != nv:
@@ -84,9 +101,24 @@ class CellBoundary:
                 coef[:, q] = coefs
         return fn, coef
 
-    def apply(self, fs: FieldSet, schedule, stream=None):
-        regions = region_table(fs, schedule)
-        if regions is None:
+    def slots(self, schedule):
+        """The stage tags after which this hook runs: phase 1 alone, or for
+        the relative form every slot its regions need."""
+        if not self.relative:
+            return [1]
+        return sorted({r.slot for r in schedule.boundaries})
+
+    def apply(self, fs: FieldSet, schedule, stream=None, slot: Optional[int] = None):
+        """Fill the regions (for the relative form, those of ``slot``)."""
+        table = region_table(fs, schedule)
+        if table is None:
+            return
+        regions, spans = table
+        if self.relative:
+            first, count = spans.get(slot, (0, 0))
+        else:
+            first, count = 0, len(schedule.boundaries)
+        if count == 0:
             return
         key = (np.dtype(fs.T).name, fs.nvars, fs.work.device.index)
         cache = self.__dict__.setdefault("_device", {})
@@ -100,20 +132,33 @@ class CellBoundary:
         stored = (C.c_int32 * 3)(*[fs.stored[d] if d < fs.D else 1 for d in range(3)])
         dtype = _native.TAM_F64 if fs.T == np.float64 else _native.TAM_F32
         rc = _native.lib().tam_boundary_apply(
-            dtype, C.c_void_p(regions.data_ptr()), len(schedule.boundaries), fn,
+            dtype, C.c_void_p(regions.data_ptr() + first * C.sizeof(_native.tam_boundary_region)),
+            count, fn,
             C.c_void_p(dcoef.data_ptr()), C.c_void_p(fs.work.data_ptr()), fs.nvars, stored,
             C.c_void_p(s.cuda_stream))
         if rc != 0:
             raise _native.TamError(f"tam_boundary_apply failed ({rc})")
 
 
+def ordered_regions(schedule):
+    """The hook regions ordered by slot (stably), and per slot its
+    ``(first, count)`` in that order."""
+    regions = sorted(schedule.boundaries, key=lambda r: r.slot)
+    spans = {}
+    for i, r in enumerate(regions):
+        a, n = spans.get(r.slot, (i, 0))
+        spans[r.slot] = (a, n + 1)
+    return regions, spans
+
+
 def region_rows(fs: FieldSet, schedule):
-    """One ``tam_boundary_region`` per hook region, with its block's
-    nodeposition data (``src/storage.jl:1008-1017``)."""
+    """One ``tam_boundary_region`` per hook region, ordered by slot, with its
+    block's nodeposition data (``src/storage.jl:1008-1017``)."""
     f = fs.forest
     D = fs.D
-    rows = (_native.tam_boundary_region * max(1, len(schedule.boundaries)))()
-    for i, r in enumerate(schedule.boundaries):
+    ordered, _ = ordered_regions(schedule)
+    rows = (_native.tam_boundary_region * max(1, len(ordered)))()
+    for i, r in enumerate(ordered):
         k = f.leaves[r.block]
         lo, B = f.block_low(k), f.block_base(k)
         h = f.spacing(k.level, fs.T)
@@ -124,17 +169,19 @@ def region_rows(fs: FieldSet, schedule):
                 a, z = r.region[d]
                 row.first[d], row.n[d] = a, z - a + 1
                 row.ghosts[d], row.stagger[d] = fs.G[d], fs.c[d]
+                row.clamps[d] = r.clamps[d] if r.clamps else 0
                 row.base[d], row.lo[d] = B[d], float(np.dtype(fs.T).type(lo[d]))
             else:
                 row.first[d], row.n[d], row.ghosts[d], row.stagger[d] = 1, 1, 0, 0
+                row.clamps[d] = 0
                 row.base[d], row.lo[d] = 0, 0.0
         row.h = float(h)
     return rows
 
 
 def region_table(fs: FieldSet, schedule):
-    """The regions as a device array, made once per schedule, element type
-    and device."""
+    """The regions as a device array ordered by slot, and the slots' spans,
+    made once per schedule, element type and device."""
     if not schedule.boundaries:
         return None
     cache = schedule.__dict__.setdefault("_boundary_regions", {})
@@ -143,5 +190,6 @@ def region_table(fs: FieldSet, schedule):
         rows = region_rows(fs, schedule)
         raw = np.frombuffer(bytes(rows), dtype=np.uint8)[:C.sizeof(rows[0]) *
                                                          len(schedule.boundaries)]
-        cache[key] = torch.from_numpy(raw.copy()).to(fs.work.device)
+        cache[key] = (torch.from_numpy(raw.copy()).to(fs.work.device),
+                      ordered_regions(schedule)[1])
     return cache[key]

@@ -152,8 +152,19 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
     if boundary is None or not schedule.boundaries:
         ds.run(fs, _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST, method, stream)
         return fs
-    ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
     from .boundary import CellBoundary
+    if isinstance(boundary, CellBoundary) and boundary.relative:
+        # the relative form in parts, each after the stage that fills the
+        # ghosts it reads (src/ghosts.jl:1146-1160)
+        ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
+        slots = set(boundary.slots(schedule))
+        boundary.apply(fs, schedule, stream, slot=PHASE1_TAG)
+        for tag in [t for t in schedule.stage_tags if t > PHASE1_TAG]:
+            ds.run(fs, tag, tag, method, stream)
+            if tag in slots:
+                boundary.apply(fs, schedule, stream, slot=tag)
+        return fs
+    ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
     if isinstance(boundary, CellBoundary):
         boundary.apply(fs, schedule, stream)        # the device hook
     else:

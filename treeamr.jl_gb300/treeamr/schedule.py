@@ -136,10 +136,17 @@ class BoundaryRegion(NamedTuple):
     """A ghost region facing out of the domain through an outer face, filled
     by the boundary hook (``src/schedule.jl:200-232``).  ``block`` is
     0-based; ``region`` holds 1-based inclusive ``(first, last)`` per
-    dimension."""
+    dimension.  For the relative hook, ``clamps`` is per dimension the
+    stored index of the nearest evolved point along a component that leaves
+    through an outer face (``G + N + c`` high, ``G + 1`` low) and 0 along the
+    others, and ``slot`` the stage tag after which the ghosts it reads along
+    those others are filled (phase 1, or the prolongations onto the block's
+    level)."""
     block: int
     direction: Tuple[int, ...]
     region: Tuple[Tuple[int, int], ...]
+    clamps: Tuple[int, ...] = ()
+    slot: int = 1
 
 
 # --- 1-D stencils -----------------------------------------------------------
@@ -288,8 +295,37 @@ def _record(pairs, key, b, s):
     lst[1].append(s + 1)
 
 
-def boundary_region(forest: Forest, k: MortonKey, b: int, delta, region) -> BoundaryRegion:
-    return BoundaryRegion(b, tuple(delta), tuple((r.start, r.stop - 1) for r in region))
+def boundary_region(forest: Forest, k: MortonKey, b: int, delta, region, G=None,
+                    c=None) -> BoundaryRegion:
+    """``src/schedule.jl:2188-2217``: the region, and the relative hook's
+    clamps and stage slot."""
+    D = forest.D
+    N = forest.N
+
+    def exits(d):
+        if delta[d] == 0:
+            return False
+        step = tuple(delta[d] if e == d else 0 for e in range(D))
+        _, faces = forest.wall_direction(k, step)
+        return faces[d] == OUTER and not forest.oriented_neighbors(k, step)
+
+    ex = [exits(d) for d in range(D)]
+    d2 = tuple(0 if ex[d] else delta[d] for d in range(D))
+    slot = PHASE1_TAG
+    if any(x != 0 for x in d2):
+        d3, _ = forest.wall_direction(k, d2)
+        if any(x != 0 for x in d3):
+            nbrs = forest.oriented_neighbors(k, d3)
+            if not nbrs:
+                ex = [x != 0 for x in delta]
+            elif nbrs[0].level < k.level:
+                slot = prolongation_tag(k.level)
+    G = G if G is not None else (0,) * D
+    c = c if c is not None else (0,) * D
+    clamps = tuple((G[d] + N + c[d] if delta[d] > 0 else G[d] + 1) if ex[d] else 0
+                   for d in range(D))
+    return BoundaryRegion(b, tuple(delta), tuple((r.start, r.stop - 1) for r in region),
+                          clamps, slot)
 
 
 def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
@@ -323,7 +359,7 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
         if table is not None:
             table.remember(delta, nbrs)
         if not nbrs:
-            boundaries.append(boundary_region(forest, k, b, delta, region))
+            boundaries.append(boundary_region(forest, k, b, delta, region, G, c))
             continue
         nbl = nbrs[0].level
         if nbl == k.level:
@@ -366,7 +402,7 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
         return
     nbrs = forest.oriented_neighbors(k, dprime)
     if not nbrs:
-        boundaries.append(boundary_region(forest, k, b, delta, region))
+        boundaries.append(boundary_region(forest, k, b, delta, region, G, c))
         return
     nbl = nbrs[0].level
     if nbl == k.level:
