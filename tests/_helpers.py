@@ -148,3 +148,34 @@ def nanbits(a: np.ndarray) -> np.ndarray:
     a = a.copy()
     a[np.isnan(a)] = np.nan
     return a.view(np.uint64 if a.dtype == np.float64 else np.uint32)
+
+
+class Geometry:
+    """Exact positions as integers: root units times ``scale = 2 N 2^L``, L
+    the finest level, so cell centres and half fine spacings are whole
+    (the oracle's ``exact_point`` and ``leafbox``, wrapped where periodic)."""
+
+    def __init__(self, forest):
+        self.f = forest
+        self.L = max(k.level for k in forest.leaves)
+        self.scale = 2 * forest.N * (1 << self.L)
+
+    def low(self, k):
+        rp = self.f.root_position(k.root)
+        return [((rp[d] << k.level) + k.coords[d]) * (self.scale >> k.level)
+                for d in range(self.f.D)]
+
+    def wrap(self, d, x):
+        f = self.f
+        return x % (f.roots[d] * self.scale) if f.periodic[d] else x
+
+    def points(self, k, G, c, N):
+        """Per dimension the positions of own indices 1..N+c (stored G+1..)."""
+        unit = 1 << (self.L - k.level)        # half a cell of this level
+        lo = self.low(k)
+        out = []
+        for d in range(self.f.D):
+            i = np.arange(N + c[d])           # own index 0.. (stored G+1+i)
+            x = lo[d] + (2 * i + (0 if c[d] == 1 else 1)) * unit
+            out.append(self.wrap(d, x))
+        return out

@@ -3,18 +3,27 @@ of new leaves (copy, prolongation from the parent, restriction from the
 children), exactness on polynomial data of degree p-1 for created and
 coarsened blocks with kept blocks copied bit for bit (the properties of
 ``test/regrid_tests.jl``), and on the GPU the device transfer equal to the
-oracle's replay of the same groups bit for bit."""
+oracle's replay of the same groups bit for bit.
+
+The kept-over-created pass (``src/regrid.jl:788-881``) is restated from
+``test/closed_tests.jl:1129-1236``: a periodic brick refined over its high
+half along dimension 1, whose low half the regrid refines, so that created
+fine blocks meet kept fine blocks on the planes x1 = 0 and 1.  After the
+regrid and before any fill every created copy of a point a kept block holds
+at the finest level is the kept block's old value bit for bit, and the
+next fill leaves the kept values there unchanged."""
 import numpy as np
 import pytest
 import torch
 
 import oracle
-from _helpers import exact_values, makepoly, nanbits, nested_forest
-from treeamr import FieldSet, Operators
+from _helpers import Geometry, exact_values, makepoly, nanbits, nested_forest
+from treeamr import FieldSet, Forest, GhostSchedule, Operators
 from treeamr.forest import parentkey
-from treeamr.regrid import REGRID_TAG, RegridTransfer, regrid, regrid_sources
+from treeamr.regrid import (REGRID_KEPT_TAG, REGRID_TAG, RegridTransfer, regrid,
+                            regrid_kept_pairs, regrid_sources)
 from treeamr.schedule import COPY, PROLONG, RESTRICT, TransferGroup
-from treeamr.storage import vertexcentered
+from treeamr.storage import edgecentered, facecentered, vertexcentered
 
 
 def _move(D, N=8):
@@ -52,10 +61,92 @@ class _Concat:
         return self.groups
 
 
-def oracle_regrid(t, old_host, new_host, nvars):
+class _Kept:
+    """The kept-over-created pass as a schedule over the new array."""
+
+    def __init__(self, t):
+        self.T, self.stored, self.forest = t.T, t.stored, t.forest
+        self.groups = t.kept_groups
+
+    def all_groups(self):
+        return self.groups
+
+
+def oracle_regrid(t, old_host, new_host, nvars, kept=True):
+    """The oracle's replay of both stages: the transfer, then the
+    kept-over-created pass within the new array."""
     both = np.concatenate([new_host, old_host], axis=0)
-    oracle.fill(_Concat(t), both, nvars, np.ones((nvars, 3 ** t.forest.D), t.T))
-    return both[:t.nnew]
+    ones = np.ones((nvars, 3 ** t.forest.D), t.T)
+    oracle.fill(_Concat(t), both, nvars, ones)
+    new = np.ascontiguousarray(both[:t.nnew])
+    if kept and t.kept_groups:
+        oracle.fill(_Kept(t), new, nvars, ones)
+    return new
+
+
+def half_refined(D, N=8):
+    """``test/closed_tests.jl:1134-1140``: 2^D periodic roots on (0, 2)^D,
+    those with x1 >= 1 refined once."""
+    f = Forest((2,) * D, N=N, periodic=(True,) * D, extents=((0.0, 2.0),) * D)
+    f.refine([k for k in f.leaves if f.root_position(k.root)[0] >= 1])
+    f.balance()
+    return f
+
+
+def kept_created(forest, oldleaves, G, c):
+    """Per point that kept and created new leaves both hold at the finest
+    level holding it: ``([(new block, old block, own index)], [(new block,
+    own index)])`` (``test/closed_tests.jl:1145-1157``)."""
+    geo = Geometry(forest)
+    N, D = forest.N, forest.D
+    old = {k: i for i, k in enumerate(oldleaves)}
+    byposition = {}
+    for b, k in enumerate(forest.leaves):
+        pts = geo.points(k, G, c, N)
+        for I in np.ndindex(*[len(p) for p in pts]):
+            x = tuple(int(pts[d][I[d]]) for d in range(D))
+            byposition.setdefault(x, []).append((k.level, b, I))
+    out = []
+    for copies in byposition.values():
+        finest = max(x[0] for x in copies)
+        atf = [x for x in copies if x[0] == finest]
+        kept = [(b, old[forest.leaves[b]], I) for _, b, I in atf if forest.leaves[b] in old]
+        created = [(b, I) for _, b, I in atf if forest.leaves[b] not in old]
+        if kept and created:
+            out.append((kept, created))
+    return out
+
+
+def _at(arr, b, I, G):
+    return arr[(b, slice(None)) + tuple(reversed([g + i for g, i in zip(G, I)]))]
+
+
+def kept_cases(D):
+    out = [("vertex",) * D, ("cell",) * D]
+    if D >= 2:
+        out += [facecentered(D, 1), facecentered(D, 2)]
+    if D == 3:
+        out += [edgecentered(3, 1)]
+    return out
+
+
+def _kept_run(D, C, T=np.float64, nvars=2, seed=0):
+    """Fill (unify) the old storage with the oracle, regrid on the host
+    with and without the kept pass; returns everything the checks need."""
+    ops = Operators(prolongation=4, restriction=4)
+    f = half_refined(D)
+    fs = FieldSet(f, nvars, G=2, centering=C, T=T)
+    rng = np.random.default_rng(60 + D + seed)
+    fs.work.copy_(torch.from_numpy(rng.standard_normal(tuple(fs.work.shape)).astype(T)))
+    old_host = oracle.fill_fieldset(fs, GhostSchedule(fs, ops))
+    oldleaves = list(f.leaves)
+    f.refine([k for k in oldleaves if k.level == 0])
+    f.balance()
+    t = RegridTransfer(f, oldleaves, fs.G, C, T, ops)
+    new0 = np.zeros((f.nleaves(),) + tuple(fs.work.shape[1:]), T)
+    moved = oracle_regrid(t, old_host, new0.copy(), nvars)
+    unkept = oracle_regrid(t, old_host, new0.copy(), nvars, kept=False)
+    return f, fs, t, oldleaves, old_host, moved, unkept, ops
 
 
 @pytest.mark.parametrize("D", [2, 3])
@@ -134,3 +225,93 @@ def test_gpu_regrid_of_a_field_set(cuda_lib):
     own = (slice(None), slice(None)) + tuple(slice(2, 10) for _ in range(D))
     got = fs.work.cpu().numpy()
     assert np.max(np.abs(got[own] - want[own])) < 1e-10
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+def test_kept_over_created_oracle(D):
+    """Only a set vertex-like along dimension 1 shares the planes x1 = 0 and
+    1 between kept and created fine blocks; there every created copy is the
+    kept block's old value bit for bit (without the pass the interpolated
+    hanging points of a plane are not), and the next fill keeps the kept
+    values."""
+    for C in kept_cases(D):
+        f, fs, t, oldleaves, old_host, moved, unkept, ops = _kept_run(D, C)
+        c = t.c
+        pairs = kept_created(f, oldleaves, t.G, c)
+        if c[0] == 1:
+            assert pairs and t.kept_groups, C
+            assert all(g.stage == REGRID_KEPT_TAG and g.kind == COPY for g in t.kept_groups)
+        else:
+            assert not pairs and not t.kept_groups, C
+            continue
+        differs = False
+        for kept, created in pairs:
+            b0, o0, I0 = kept[0]
+            want = _at(old_host, o0, I0, t.G).view(np.uint64)
+            for b, o, I in kept:
+                assert np.array_equal(_at(old_host, o, I, t.G).view(np.uint64), want)
+            for b, I in created:
+                assert np.array_equal(_at(moved, b, I, t.G).view(np.uint64), want), (C, b, I)
+                differs |= not np.array_equal(_at(unkept, b, I, t.G).view(np.uint64), want)
+        # in 1-D the shared points are coarse vertices, which a prolongation
+        # injects; on a plane the hanging points are interpolated
+        assert differs == (D >= 2), C
+        # the kept-over-created targets are disjoint: each point written once
+        seen = set()
+        for g in t.kept_groups:
+            box = [range(s.targetfirst, s.targetfirst + s.ntarget) for s in g.stencils]
+            for tb in g.targetblocks:
+                for I in np.ndindex(*[len(r) for r in box]):
+                    p = (int(tb),) + tuple(box[d][I[d]] for d in range(D))
+                    assert p not in seen
+                    seen.add(p)
+        # the next fill keeps every kept value at those points
+        fs2 = FieldSet(f, fs.nvars, G=2, centering=C, T=fs.T)
+        fs2.work.copy_(torch.from_numpy(moved))
+        filled = oracle.fill_fieldset(fs2, GhostSchedule(fs2, ops))
+        for kept, _ in pairs:
+            for b, o, I in kept:
+                assert np.array_equal(_at(filled, b, I, t.G).view(np.uint64),
+                                      _at(old_host, o, I, t.G).view(np.uint64))
+
+
+def test_kept_pairs_need_a_vertex_like_dimension():
+    f = half_refined(2)
+    old = list(f.leaves)
+    f.refine([k for k in old if k.level == 0])
+    f.balance()
+    assert regrid_kept_pairs(f, old, (0, 0)) == {}
+    assert regrid_kept_pairs(f, old, (1, 1))
+    # nothing created: nothing to copy
+    assert regrid_kept_pairs(f, list(f.leaves), (1, 1)) == {}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_kept_over_created_bit_exact(cuda_lib, D, T):
+    """The device transfer with its kept-over-created pass equals the
+    oracle's replay of both stages bit for bit."""
+    for C in (("vertex",) * D, facecentered(D, 1)):
+        f, fs, t, oldleaves, old_host, moved, unkept, ops = _kept_run(D, C, T=T, nvars=3)
+        assert t.kept_groups
+        new_dev = torch.zeros((f.nleaves(),) + tuple(fs.work.shape[1:]), dtype=fs.work.dtype,
+                              device="cuda")
+        t.run(torch.from_numpy(old_host).cuda(), new_dev, 3)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(new_dev.cpu().numpy()), nanbits(moved)), C
+
+
+@pytest.mark.gpu
+def test_gpu_regrid_keeps_evolved_values(cuda_lib):
+    """``regrid`` of a vertex-centred set on the device: fill, transfer,
+    kept-over-created pass, bit for bit the oracle's."""
+    D, C = 3, ("vertex",) * 3
+    f, fs, t, oldleaves, old_host, moved, unkept, ops = _kept_run(D, C)
+    g = half_refined(D)
+    gs = FieldSet(g, fs.nvars, G=2, centering=C, device="cuda")
+    rng = np.random.default_rng(60 + D)
+    gs.work.copy_(torch.from_numpy(rng.standard_normal(tuple(gs.work.shape))))
+    regrid(gs, ops, refine=[k for k in g.leaves if k.level == 0])
+    torch.cuda.synchronize()
+    assert np.array_equal(nanbits(gs.work.cpu().numpy()), nanbits(moved))

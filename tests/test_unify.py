@@ -12,7 +12,7 @@ import pytest
 import torch
 
 import oracle
-from _helpers import nanbits, nested_forest
+from _helpers import Geometry, nanbits, nested_forest
 from treeamr import FieldSet, GhostSchedule, Operators
 from treeamr.storage import edgecentered, facecentered, vertexcentered
 from treeamr.unify import UnifySchedule, unify
@@ -22,37 +22,6 @@ def interface_cases(D):
     return {1: [facecentered(1, 1)],
             2: [facecentered(2, 1), facecentered(2, 2), vertexcentered(2)],
             3: [facecentered(3, 1), facecentered(3, 3), edgecentered(3, 1)]}[D]
-
-
-class Geometry:
-    """Exact positions as integers: root units times ``scale = 2 N 2^L``, L
-    the finest level, so cell centres and half fine spacings are whole
-    (the oracle's ``exact_point`` and ``leafbox``, wrapped where periodic)."""
-
-    def __init__(self, forest):
-        self.f = forest
-        self.L = max(k.level for k in forest.leaves)
-        self.scale = 2 * forest.N * (1 << self.L)
-
-    def low(self, k):
-        rp = self.f.root_position(k.root)
-        return [((rp[d] << k.level) + k.coords[d]) * (self.scale >> k.level)
-                for d in range(self.f.D)]
-
-    def wrap(self, d, x):
-        f = self.f
-        return x % (f.roots[d] * self.scale) if f.periodic[d] else x
-
-    def points(self, k, G, c, N):
-        """Per dimension the positions of own indices 1..N+c (stored G+1..)."""
-        unit = 1 << (self.L - k.level)        # half a cell of this level
-        lo = self.low(k)
-        out = []
-        for d in range(self.f.D):
-            i = np.arange(N + c[d])           # own index 0.. (stored G+1+i)
-            x = lo[d] + (2 * i + (0 if c[d] == 1 else 1)) * unit
-            out.append(self.wrap(d, x))
-        return out
 
 
 def arbitrary(x, v):

@@ -11,10 +11,19 @@ the same kernels, reading the old array and writing the new one
 (``tam_regrid_upload``, ``tam_regrid_transfer``).  The ghosts are left to
 the next fill, as in the reference.  ``regrid`` wraps the serial
 ``regrid!`` of one field set: fill, move the forest, transfer, swap arrays.
+
+A set with a vertex-like dimension takes a second stage, the
+kept-over-created pass (``src/regrid.jl:788-905``): a created block's copy
+of a point that a kept block holds at the finest level holding it takes
+the kept block's value, so that the next fill's stage 0 cannot carry a
+prolongated value over an evolved one.  Its transfers are same-level
+copies of closed sub-pieces within the new array, uploaded as an ordinary
+schedule and run by ``tam_fill`` over its stage tag alone.
 """
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -22,11 +31,13 @@ import torch
 
 from . import _native
 from .forest import Forest, MortonKey, childoffset, parentkey, sortedchildkeys
-from .schedule import (COPY, PROLONG, RESTRICT, GroupKey, TransferGroup, _nospan,
-                       kind_stencil)
+from .schedule import (COPY, PROLONG, RESTRICT, GroupKey, NeighbourTable, TransferGroup,
+                       _nospan, copy_stencil, kind_stencil, merged_transfers, piece_copies,
+                       piece_of, piece_primary, subpiece_list, subpiece_values)
 from .storage import FieldSet
 
 REGRID_TAG = 50                     # the reference's stage tag of the transfer
+REGRID_KEPT_TAG = 51                # and of its kept-over-created pass
 
 
 def regrid_sources(oldleaves: Sequence[MortonKey], newleaves: Sequence[MortonKey]):
@@ -65,6 +76,63 @@ def regrid_sources(oldleaves: Sequence[MortonKey], newleaves: Sequence[MortonKey
     return pairs
 
 
+def regrid_kept_pairs(forest: Forest, oldleaves: Sequence[MortonKey], c):
+    """``GroupKey -> (targets, sources)`` of the kept-over-created pass, both
+    1-based new leaf indices (``regrid_kept_pairs``, ``src/regrid.jl:826-881``).
+
+    ``forest`` holds the new leaves.  For every created leaf with a kept
+    neighbour of its own level across a face, edge or corner of a
+    vertex-like dimension, every closed sub-piece but the open interior
+    that the created leaf holds at the finest level holding it, and that a
+    kept leaf of that level also holds, is copied from the kept holder that
+    would be the primary among the kept holders; the sub-pieces merge into
+    boxes per source as stage 0's do."""
+    D = len(c)
+    pairs: Dict[GroupKey, Tuple[List[int], List[int]]] = {}
+    if not any(cd == 1 for cd in c):
+        return pairs
+    old = set(oldleaves)
+    newleaves = forest.leaves
+    kept = [k in old for k in newleaves]
+    allowed = subpiece_values(c, forest.N)
+    subs = subpiece_list(c, forest.N)
+    steps = list(itertools.product(*[(-1, 0, 1) if cd == 1 else (0,) for cd in c]))
+    nomirror = (0,) * D
+    for j, k in enumerate(newleaves):
+        if kept[j]:
+            continue
+        t = NeighbourTable(forest, j)
+        found = False
+        for delta in steps:
+            if all(x == 0 for x in delta):
+                continue
+            lvl, nbrs = t.neighbours(delta)
+            if lvl == t.level and any(kept[x[0]] for x in nbrs):
+                found = True
+                break
+        if not found:
+            continue
+        entries = []
+        for sub in subs:
+            if all(x == 1 for x in piece_of(sub)):       # the open interior
+                continue
+            copies = piece_copies(t, sub, c)
+            finest = max(x[0] for x in copies)
+            if t.level != finest:
+                continue
+            holders = [x for x in copies if x[0] == finest and kept[x[1]]]
+            if not holders:
+                continue
+            _, s, _, delta, o = piece_primary(holders)
+            entries.append((sub, COPY, s, delta, o))
+        for kind, s, delta, o, spans in merged_transfers(entries, allowed):
+            key = GroupKey(kind, delta, o, 0, nomirror, spans)
+            tb, sb = pairs.setdefault(key, ([], []))
+            tb.append(j + 1)
+            sb.append(s + 1)
+    return pairs
+
+
 class RegridTransfer:
     """The serial regrid transfer's groups (``transfer_groups``,
     ``src/regrid.jl:942-955``) for one layout: built from the old and new
@@ -91,7 +159,15 @@ class RegridTransfer:
                                     operators) for d in range(D))
             groups.append(TransferGroup(key, st, tb, sb, 0, REGRID_TAG))
         self.groups = groups
+        kept = regrid_kept_pairs(forest, oldleaves, self.c)
+        self.kept_groups = []
+        for key in sorted(kept, key=GroupKey.order):
+            tb, sb = kept[key]
+            st = tuple(copy_stencil(self.T, N, self.G[d], self.c[d], key.direction[d],
+                                    span=key.span[d]) for d in range(D))
+            self.kept_groups.append(TransferGroup(key, st, tb, sb, 0, REGRID_KEPT_TAG))
         self._device = {}
+        self._kept_device = {}
 
     def all_groups(self):
         return list(self.groups)
@@ -113,17 +189,36 @@ class RegridTransfer:
             self._device[device] = (lib, ctx, desc, h)
         return self._device[device]
 
+    def kept_counts(self):
+        """The kept-over-created pass's transfers and points."""
+        n = sum(g.ntransfers() for g in self.kept_groups)
+        pts = sum(g.ntransfers() * int(np.prod(g.boxsize())) for g in self.kept_groups)
+        return n, pts
+
+    def _upload_kept(self, device: int):
+        if device not in self._kept_device:
+            lib = _native.lib()
+            ctx = _native.context(device)
+            desc = _native.Descriptor(self, groups=self.kept_groups)
+            h = C.c_void_p()
+            _native.check(lib.tam_schedule_upload(ctx, desc.ref(), C.byref(h)), ctx,
+                          "tam_schedule_upload (kept-over-created pass)")
+            self._kept_device[device] = (lib, ctx, desc, h)
+        return self._kept_device[device]
+
     def __del__(self):
-        for lib, ctx, desc, h in getattr(self, "_device", {}).values():
-            try:
-                lib.tam_schedule_free(h)
-            except Exception:
-                pass
+        for table in (getattr(self, "_device", {}), getattr(self, "_kept_device", {})):
+            for lib, ctx, desc, h in table.values():
+                try:
+                    lib.tam_schedule_free(h)
+                except Exception:
+                    pass
 
     def run(self, old_work: torch.Tensor, new_work: torch.Tensor, nvars: int,
             stream: Optional[torch.cuda.Stream] = None):
         """The transfer from ``old_work`` (old leaves) into ``new_work``'s own
-        points (new leaves), on the device."""
+        points (new leaves), then the kept-over-created pass within
+        ``new_work``, on the device."""
         if old_work.device.type != "cuda" or new_work.device != old_work.device:
             raise ValueError("the old and new arrays must be on one CUDA device")
         if old_work.shape[0] != self.nold or new_work.shape[0] != self.nnew:
@@ -134,6 +229,21 @@ class RegridTransfer:
                                      C.c_void_p(new_work.data_ptr()), self.nnew, nvars,
                                      C.c_void_p(s.cuda_stream))
         _native.check(rc, ctx, "tam_regrid_transfer")
+        if self.kept_groups:
+            self.run_kept(new_work, nvars, stream=s)
+
+    def run_kept(self, new_work: torch.Tensor, nvars: int,
+                 stream: Optional[torch.cuda.Stream] = None):
+        """The kept-over-created pass alone, within ``new_work``."""
+        if new_work.device.type != "cuda" or new_work.shape[0] != self.nnew:
+            raise ValueError("the new array must be on a CUDA device and hold the new leaves")
+        if not self.kept_groups:
+            return
+        lib, ctx, desc, h = self._upload_kept(new_work.device.index or 0)
+        s = stream if stream is not None else torch.cuda.current_stream(new_work.device)
+        rc = lib.tam_fill(h, C.c_void_p(new_work.data_ptr()), nvars, self.nnew, None,
+                          REGRID_KEPT_TAG, REGRID_KEPT_TAG, C.c_void_p(s.cuda_stream))
+        _native.check(rc, ctx, "tam_fill (kept-over-created pass)")
 
 
 def regrid(fs: FieldSet, operators, *, refine: Sequence[MortonKey] = (),
