@@ -3,16 +3,22 @@ with built-in functions of position: the GPU's values equal the oracle's
 host evaluation bit for bit at every outer-face ghost, a full fill with the
 hook equals the oracle's fill with the same boundary values, and a
 polynomial boundary keeps an order-p fill exact for degree p-1 data up to
-the outer faces (``test/ghost_tests.jl:247-281`` with boundaries)."""
+the outer faces (``test/ghost_tests.jl:247-281`` with boundaries).
+
+A hook that prescribes the wall planes (``wall = "prescribed"``, stage W,
+``src/ghosts.jl:1378-1412, 1639-1652``) writes the primaries of every wall
+point of a vertex-like dimension first; after the fill every own copy of
+a wall point is one number, the hook's at the primary."""
 import numpy as np
 import pytest
 import torch
 
 import oracle
-from _helpers import ghost_mask, nanbits, nested_forest
+from _helpers import Geometry, ghost_mask, nanbits, nested_forest
 from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts
-from treeamr.boundary import CellBoundary, Constant, Polynomial
-from treeamr.storage import vertexcentered
+from treeamr.boundary import CellBoundary, Constant, Polynomial, Relative
+from treeamr.schedule import PHASE1_TAG, UNIFY_TAG
+from treeamr.storage import edgecentered, facecentered, vertexcentered
 
 
 def _poly(D, nvars):
@@ -31,7 +37,9 @@ def test_hook_refuses_what_is_not_built():
     with pytest.raises(TypeError):
         CellBoundary(lambda x, v, d: 0.0)
     with pytest.raises(ValueError):
-        CellBoundary(Constant([1.0]), wall="prescribed")
+        CellBoundary(Constant([1.0]), wall="dirichlet")
+    assert CellBoundary(Constant([1.0]), wall="prescribed").prescribes_wall
+    assert not CellBoundary(Constant([1.0])).prescribes_wall
     with pytest.raises(ValueError):
         Polynomial({(i, 0, 0): [1.0] for i in range(21)})
 
@@ -158,3 +166,142 @@ def test_gpu_relative_hook_bit_exact(cuda_lib, D, T):
     fill_ghosts(fs, s, boundary=CellBoundary(g))
     torch.cuda.synchronize()
     assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))
+
+
+# --- stage W: a prescribed wall ---------------------------------------------------
+
+def _oracle_prescribed_fill(fs, s, g, host):
+    """Stage W on the host, then the fill with the hook as usual."""
+    oracle.cell_boundary(fs, host, s.walls, g)
+    if isinstance(g, Relative):
+        return _oracle_relative_fill(fs, s, g, host)
+    oracle.fill(s, host, fs.nvars, fs.factors_host, last=PHASE1_TAG)
+    oracle.cell_boundary(fs, host, s.boundaries, g)
+    return oracle.fill(s, host, fs.nvars, fs.factors_host, first=PHASE1_TAG + 1)
+
+
+def _wall_copies(fs):
+    """Per point on an outer face of a vertex-like dimension, every own copy
+    as ``(block, 1-based stored index)``."""
+    f = fs.forest
+    geo = Geometry(f)
+    D, N = f.D, f.N
+    top = [f.roots[d] * geo.scale for d in range(D)]
+    out = {}
+    for b, k in enumerate(f.leaves):
+        pts = geo.points(k, fs.G, fs.c, N)
+        for I in np.ndindex(*[len(p) for p in pts]):
+            x = tuple(int(pts[d][I[d]]) for d in range(D))
+            if any(fs.c[d] == 1 and x[d] in (0, top[d]) for d in range(D)):
+                out.setdefault(x, []).append((b, tuple(fs.G[d] + 1 + I[d] for d in range(D))))
+    return out
+
+
+def _val(host, b, v, idx):
+    return host[(b, v) + tuple(i - 1 for i in reversed(idx))]
+
+
+def _wall_cases(D):
+    out = [vertexcentered(D)]
+    if D >= 2:
+        out.append(facecentered(D, 2))
+    if D == 3:
+        out.append(edgecentered(3, 1))
+    return out
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+def test_wall_regions(D):
+    """Stage W's regions (``src/schedule.jl:2134-2170``): primaries on the
+    outer wall planes of vertex-like dimensions only, one plane in as the
+    relative form's point, none for a cell-centred set."""
+    f = nested_forest(D, N=8)
+    ops = Operators(prolongation=4, restriction=4)
+    assert GhostSchedule(FieldSet(f, 1, G=2), ops).walls == []
+    for C in _wall_cases(D):
+        fs = FieldSet(f, 1, G=2, centering=C)
+        s = GhostSchedule(fs, ops)
+        assert s.walls, C
+        N, G, c = f.N, fs.G, fs.c
+        for r in s.walls:
+            assert r.slot == UNIFY_TAG and any(r.direction)
+            for d in range(D):
+                a, z = r.region[d]
+                if r.direction[d] < 0:
+                    assert c[d] == 1 and a == z == G[d] + 1 and r.clamps[d] == G[d] + 2
+                elif r.direction[d] > 0:
+                    assert c[d] == 1 and a == z == G[d] + N + 1 and r.clamps[d] == G[d] + N
+                else:
+                    assert r.clamps[d] == 0
+            assert (s.primary_bits[r.block] >> sum(
+                (0 if a == G[d] + 1 and c[d] == 1 else 2 if a == G[d] + N + 1 and c[d] == 1
+                 else 1) * 3 ** d for d, (a, z) in enumerate(r.region))) & 1
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_oracle_prescribed_wall_is_one_number(D):
+    """After a fill with a prescribed wall every own copy of a wall point is
+    one number: the constant, the polynomial at the point, or for the
+    relative form the primary's value one plane in shifted by f."""
+    f = nested_forest(D, N=8)
+    ops = Operators(prolongation=4, restriction=4)
+    for C in _wall_cases(D):
+        fs = FieldSet(f, 2, G=2, centering=C)
+        s = GhostSchedule(fs, ops)
+        copies = _wall_copies(fs)
+        assert copies
+        rng = np.random.default_rng(3 + D)
+        host = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+        for g in (Constant([1.5, -2.25]), _poly(D, 2), Relative(Constant([0.0, 0.0]))):
+            out = _oracle_prescribed_fill(fs, s, g, host.copy())
+            shared = 0
+            for x, cp in copies.items():
+                for v in range(2):
+                    vals = {_val(out, b, v, idx) for b, idx in cp}
+                    assert len(vals) == 1, (C, x, vals)
+                    if isinstance(g, Constant):
+                        assert vals == {g.values[v]}
+                shared += len(cp) > 1
+            # a wall point of a set vertex-like along one dimension alone
+            # lies in one block; along two it is shared across their edges
+            assert (shared > 0) == (sum(fs.c) >= 2), C
+            if isinstance(g, Polynomial):
+                r = s.walls[0]
+                pos = fs.positions(r.block)
+                idx = tuple(a for a, _ in r.region)
+                xw = [pos[d][idx[d] - 1] for d in range(D)]
+                want = 0.5 + sum(0.25 * (d + 1) * xw[d] for d in range(D)) + 0.125 * xw[0] ** 2
+                assert abs(_val(out, r.block, 0, idx) - want) < 1e-12
+            if isinstance(g, Relative):
+                for r in s.walls:
+                    idxs = [range(a, z + 1) for a, z in r.region]
+                    for I in np.ndindex(*[len(i) for i in idxs]):
+                        idx = tuple(idxs[d][I[d]] for d in range(D))
+                        rr = tuple(r.clamps[d] or idx[d] for d in range(D))
+                        assert _val(out, r.block, 1, idx) == _val(out, r.block, 1, rr)
+        # the evolved default leaves the wall planes to the state
+        out = oracle.fill(s, host.copy(), fs.nvars, fs.factors_host)
+        r = s.walls[0]
+        idx = tuple(a for a, _ in r.region)
+        assert _val(out, r.block, 0, idx) == _val(host, r.block, 0, idx)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_prescribed_wall_bit_exact(cuda_lib, D, T):
+    f = nested_forest(D, N=8)
+    ops = Operators(prolongation=4, restriction=4)
+    for C in _wall_cases(D):
+        fs = FieldSet(f, 2, G=2, centering=C, T=T)
+        s = GhostSchedule(fs, ops)
+        rng = np.random.default_rng(11 + D)
+        host = rng.uniform(-1, 1, size=tuple(fs.work.shape)).astype(T)
+        for g in (Constant([1.5, -2.25]), _poly(D, 2), Relative(_poly(D, 2))):
+            expect = _oracle_prescribed_fill(fs, s, g, host.copy())
+            fs.work = torch.from_numpy(host.copy()).cuda()
+            fs.factors = fs.factors.cuda()
+            fill_ghosts(fs, s, boundary=CellBoundary(g, wall="prescribed"))
+            torch.cuda.synchronize()
+            assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), (C, g)
+            fs.factors = fs.factors.cpu()

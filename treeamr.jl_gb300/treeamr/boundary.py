@@ -10,8 +10,11 @@ roundings.  Either runs between phase 1 and the prolongations, as every
 hook does, over every ghost region facing out through an outer face, with
 the position of a ghost formed exactly as ``nodeposition`` forms it.
 ``Relative(f)`` with such an ``f`` gives the relative form, run in parts
-after the stages that fill what it reads.  ``wall = "prescribed"`` is not
-built.
+after the stages that fill what it reads.  ``wall = "prescribed"``
+(``src/ghosts.jl:1378-1412, 1639-1652``) makes the hook write the wall
+planes of vertex-like dimensions too, at their primaries, before stage P
+and stage 0 (stage W), so that every copy of a prescribed point is one
+number.
 """
 from __future__ import annotations
 
@@ -70,10 +73,15 @@ class CellBoundary:
             raise TypeError("CellBoundary takes a Constant, a Polynomial or a Relative of one: "
                             "a function written above the C ABI cannot run in the device "
                             "kernel")
-        if wall != "evolved":
-            raise ValueError("wall must be 'evolved': a prescribed wall plane is not built")
+        if wall not in ("evolved", "prescribed"):
+            raise ValueError("wall must be 'evolved' (the wall plane of a vertex-like "
+                             "dimension is an own point of the state, evolved by the "
+                             "application, and the hook fills the ghosts beyond it) or "
+                             "'prescribed' (the hook gives the wall plane its value too, a "
+                             f"Dirichlet condition), got {wall!r}")
         self.relative = isinstance(g, Relative)
         self.g = g.f if self.relative else g
+        self.prescribes_wall = wall == "prescribed"
 
     # -- the device side ---------------------------------------------------------
     def _fn(self, fs: FieldSet):
@@ -108,6 +116,14 @@ class CellBoundary:
             return [1]
         return sorted({r.slot for r in schedule.boundaries})
 
+    def apply_walls(self, fs: FieldSet, schedule, stream=None):
+        """Stage W (``wall_boundary!``, ``src/ghosts.jl:1639-1652``): a hook
+        that prescribes the wall writes the wall planes' primaries."""
+        if not self.prescribes_wall or not schedule.walls:
+            return
+        table = region_table(fs, schedule, "walls")
+        self._launch(fs, table[0], 0, len(schedule.walls), stream)
+
     def apply(self, fs: FieldSet, schedule, stream=None, slot: Optional[int] = None):
         """Fill the regions (for the relative form, those of ``slot``)."""
         table = region_table(fs, schedule)
@@ -118,6 +134,9 @@ class CellBoundary:
             first, count = spans.get(slot, (0, 0))
         else:
             first, count = 0, len(schedule.boundaries)
+        self._launch(fs, regions, first, count, stream)
+
+    def _launch(self, fs: FieldSet, regions, first: int, count: int, stream):
         if count == 0:
             return
         key = (np.dtype(fs.T).name, fs.nvars, fs.work.device.index)
@@ -140,10 +159,10 @@ class CellBoundary:
             raise _native.TamError(f"tam_boundary_apply failed ({rc})")
 
 
-def ordered_regions(schedule):
-    """The hook regions ordered by slot (stably), and per slot its
-    ``(first, count)`` in that order."""
-    regions = sorted(schedule.boundaries, key=lambda r: r.slot)
+def ordered_regions(schedule, which: str = "boundaries"):
+    """The hook regions (or stage W's, ``which="walls"``) ordered by slot
+    (stably), and per slot its ``(first, count)`` in that order."""
+    regions = sorted(getattr(schedule, which), key=lambda r: r.slot)
     spans = {}
     for i, r in enumerate(regions):
         a, n = spans.get(r.slot, (i, 0))
@@ -151,12 +170,12 @@ def ordered_regions(schedule):
     return regions, spans
 
 
-def region_rows(fs: FieldSet, schedule):
+def region_rows(fs: FieldSet, schedule, which: str = "boundaries"):
     """One ``tam_boundary_region`` per hook region, ordered by slot, with its
     block's nodeposition data (``src/storage.jl:1008-1017``)."""
     f = fs.forest
     D = fs.D
-    ordered, _ = ordered_regions(schedule)
+    ordered, _ = ordered_regions(schedule, which)
     rows = (_native.tam_boundary_region * max(1, len(ordered)))()
     for i, r in enumerate(ordered):
         k = f.leaves[r.block]
@@ -179,17 +198,17 @@ def region_rows(fs: FieldSet, schedule):
     return rows
 
 
-def region_table(fs: FieldSet, schedule):
+def region_table(fs: FieldSet, schedule, which: str = "boundaries"):
     """The regions as a device array ordered by slot, and the slots' spans,
     made once per schedule, element type and device."""
-    if not schedule.boundaries:
+    regions = getattr(schedule, which)
+    if not regions:
         return None
     cache = schedule.__dict__.setdefault("_boundary_regions", {})
-    key = (np.dtype(fs.T).name, fs.work.device.index)
+    key = (which, np.dtype(fs.T).name, fs.work.device.index)
     if key not in cache:
-        rows = region_rows(fs, schedule)
-        raw = np.frombuffer(bytes(rows), dtype=np.uint8)[:C.sizeof(rows[0]) *
-                                                         len(schedule.boundaries)]
+        rows = region_rows(fs, schedule, which)
+        raw = np.frombuffer(bytes(rows), dtype=np.uint8)[:C.sizeof(rows[0]) * len(regions)]
         cache[key] = (torch.from_numpy(raw.copy()).to(fs.work.device),
-                      ordered_regions(schedule)[1])
+                      ordered_regions(schedule, which)[1])
     return cache[key]

@@ -3,8 +3,9 @@
 Mirrors the reference's entry point ``fill_ghosts!(fs, schedule; boundary)``
 (``src/ghosts.jl:1783-1794``) with its checks (``check_fill``,
 ``src/ghosts.jl:2058-2101``) and stage order (``exchange_ghosts!``,
-``src/ghosts.jl:1099-1160``): stage P, stage 0, phase 1, the boundary hook,
-then the prolongations coarsest target level first.  The stages run on the
+``src/ghosts.jl:1099-1160``): stage W (a hook that prescribes the wall
+planes), stage P, stage 0, phase 1, the boundary hook, then the
+prolongations coarsest target level first.  The stages run on the
 device; only the hook, when one is given, runs between two library calls.
 """
 from __future__ import annotations
@@ -149,10 +150,14 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
         raise ValueError(f"method must be one of {METHODS}")
     check_fill(fs, schedule)
     ds = device_schedule(schedule, fs.work.device.index or 0)
+    from .boundary import CellBoundary
+    if isinstance(boundary, CellBoundary):
+        # stage W: a hook that prescribes the wall planes writes their
+        # primaries before stage P and stage 0 (src/ghosts.jl:1111-1113)
+        boundary.apply_walls(fs, schedule, stream)
     if boundary is None or not schedule.boundaries:
         ds.run(fs, _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST, method, stream)
         return fs
-    from .boundary import CellBoundary
     if isinstance(boundary, CellBoundary) and boundary.relative:
         # the relative form in parts, each after the stage that fills the
         # ghosts it reads (src/ghosts.jl:1146-1160)

@@ -247,18 +247,20 @@ class RegridTransfer:
 
 
 def regrid(fs: FieldSet, operators, *, refine: Sequence[MortonKey] = (),
-           coarsen: Sequence[MortonKey] = (), schedule=None) -> RegridTransfer:
+           coarsen: Sequence[MortonKey] = (), schedule=None, boundary=None) -> RegridTransfer:
     """The serial ``regrid!`` of one field set (``src/regrid.jl:1269-1418``):
     fill its ghosts (the prolongations of created blocks read them), refine
     ``refine`` and coarsen ``coarsen`` (parents whose children are leaves),
     2:1 balance, move the own points to the new leaves, and give the field
-    set the new array.  Returns the transfer, which the caller may replay."""
+    set the new array.  ``boundary`` is the fill's hook, applied whole, as
+    every fill applies it.  Returns the transfer, which the caller may
+    replay."""
     from .ghosts import fill_ghosts
     from .schedule import GhostSchedule
     forest = fs.forest
     if schedule is None:
         schedule = GhostSchedule(fs, operators)
-    fill_ghosts(fs, schedule)
+    fill_ghosts(fs, schedule, boundary=boundary)
     oldleaves = list(forest.leaves)
     if refine:
         forest.refine(list(refine))

@@ -328,6 +328,45 @@ def boundary_region(forest: Forest, k: MortonKey, b: int, delta, region, G=None,
                           clamps, slot)
 
 
+def wall_regions(forest: Forest, G, c, b: int, bits: int) -> List[BoundaryRegion]:
+    """Stage W's regions on block ``b`` (``wall_regions!``,
+    ``src/schedule.jl:2134-2170``): every piece of its closed box on an outer
+    face of a vertex-like dimension whose copy is the primary, the piece's
+    own range, with the outward direction along the outer faces it lies on.
+    A hook that prescribes the wall writes them before stage 0, which
+    carries them to every other copy.  The relative form's nearest evolved
+    point is one plane in from the wall (``G + 2`` low, ``G + N`` high), a
+    primary of the same block that stage W does not write."""
+    D, N = forest.D, forest.N
+    k = forest.leaves[b]
+
+    def isouter(d, side):
+        step = tuple(side if e == d else 0 for e in range(D))
+        _, faces = forest.wall_direction(k, step)
+        return faces[d] == OUTER and not forest.oriented_neighbors(k, step)
+
+    outer = [(isouter(d, -1), isouter(d, 1)) if c[d] == 1 else (False, False)
+             for d in range(D)]
+    if not any(lo or hi for lo, hi in outer):
+        return []
+    out = []
+    for cls in closed_pieces(c):
+        delta = tuple(-1 if cls[d] == 0 and outer[d][0] else
+                      1 if cls[d] == 2 and outer[d][1] else 0 for d in range(D))
+        if all(x == 0 for x in delta):
+            continue
+        if not (bits >> piece_index(cls)) & 1:
+            continue
+        region = []
+        for d in range(D):
+            r = piece_range(N, G[d], c[d], piece_span(cls[d]))
+            region.append((r.start, r.stop - 1))
+        clamps = tuple(G[d] + 2 if delta[d] < 0 else G[d] + N if delta[d] > 0 else 0
+                       for d in range(D))
+        out.append(BoundaryRegion(b, delta, tuple(region), clamps, UNIFY_TAG))
+    return out
+
+
 def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
                   boundaries: List[BoundaryRegion], forest: Forest, G, c, b: int, dirs,
                   table: Optional["NeighbourTable"] = None):
@@ -854,6 +893,11 @@ class GhostSchedule:
                 selfimage_sources(ppairs, forest, c, b, parity or [], bits[b])
         self.boundaries = boundaries
         self.primary_bits = bits
+        # stage W's regions, for a hook that prescribes the wall planes
+        self.walls: List[BoundaryRegion] = []
+        if closed:
+            for b in range(forest.nleaves()):
+                self.walls.extend(wall_regions(forest, G, c, b, bits[b]))
 
         built = {}
 
