@@ -1,0 +1,321 @@
+"""Rotating seams (a quarter turn, ``rotating = (d1, d2)``) and half-turn
+seams (``halfturn = (d1, d2)``): the tree and the turned ghost fill.
+
+Restated from the reference's ``test/rotate_tests.jl`` and
+``test/halfturn_tests.jl`` with the unfolded-forest oracles of
+``test/ghost_oracles.jl:770-1000, 1462-1560``: the quadrant (or half plane)
+is checked against the full plane it is a part of, built from turned
+``Fraction`` boxes, never from the seam's own key arithmetic.  The forest's
+neighbours across the seam are the unfolded forest's turned back, every
+orientation meeting every kind of neighbour; balance makes the seam
+conforming; the ghosts of a quadrant filled through the turned transfers
+equal the full plane's filled without a seam, for data covariant under the
+turn; and on the GPU the turned fill is the oracle's bit for bit."""
+import itertools
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from treeamr.forest import (Forest, MortonKey, alldirections, childoffset, real_direction,
+                            virtual_offset)
+
+F = Fraction
+
+
+# --- the unfolded-forest oracle ------------------------------------------------------
+
+def rotate_box(box, r, d1, d2):
+    """``R^r`` of the box about the axis at the origin of the ``(d1, d2)``
+    plane, ``R(x1, x2) = (-x2, x1)`` (``test/ghost_oracles.jl:781-789``)."""
+    lo, hi = list(box[0]), list(box[1])
+    for _ in range(r % 4):
+        nlo, nhi = list(lo), list(hi)
+        nlo[d1], nlo[d2] = -hi[d2], lo[d1]
+        nhi[d1], nhi[d2] = -lo[d2], hi[d1]
+        lo, hi = nlo, nhi
+    return tuple(lo), tuple(hi)
+
+
+def box_orientation(box, d1, d2):
+    lo, hi = box
+    a, b = hi[d1] <= 0, hi[d2] <= 0
+    return (2 if b else 1) if a else (3 if b else 0)
+
+
+def leafbox(forest, k):
+    rp = forest.root_position(k.root)
+    s = F(1, 1 << k.level)
+    lo = tuple(rp[d] + k.coords[d] * s for d in range(forest.D))
+    return lo, tuple(x + s for x in lo)
+
+
+def box_key(roots, box):
+    lo, hi = box
+    D = len(roots)
+    size = hi[0] - lo[0]
+    assert all(hi[d] - lo[d] == size for d in range(D)) and size.numerator == 1
+    lvl = size.denominator.bit_length() - 1
+    assert size.denominator == 1 << lvl
+    pos = [int(np.floor(lo[d])) for d in range(D)]
+    root, stride = 0, 1
+    for d in range(D):
+        root += pos[d] * stride
+        stride *= roots[d]
+    return MortonKey(root, lvl, tuple(int((lo[d] - pos[d]) * (1 << lvl)) for d in range(D)))
+
+
+def unfolded_forest(quad):
+    """``(full, image, back)`` of a rotating quadrant
+    (``test/ghost_oracles.jl:827-846``)."""
+    d1, d2 = quad.seam_plane()
+    M = quad.roots[d1]
+    D = quad.D
+    roots = tuple(2 * M if d in (d1, d2) else quad.roots[d] for d in range(D))
+    shift = tuple(M if d in (d1, d2) else 0 for d in range(D))
+
+    def image(k, r):
+        lo, hi = rotate_box(leafbox(quad, k), r, d1, d2)
+        return box_key(roots, (tuple(x + s for x, s in zip(lo, shift)),
+                               tuple(x + s for x, s in zip(hi, shift))))
+
+    def back(kf, full):
+        lo, hi = leafbox(full, kf)
+        box = (tuple(x - s for x, s in zip(lo, shift)), tuple(x - s for x, s in zip(hi, shift)))
+        r = box_orientation(box, d1, d2)
+        return r, box_key(quad.roots, rotate_box(box, -r, d1, d2))
+
+    refl = tuple((a == 1, b == 1) for a, b in quad.faces)
+    leaves = [image(k, r) for k in quad.leaves for r in range(4)]
+    full = Forest(roots, N=quad.N, periodic=quad.periodic, reflecting=refl, leaves=leaves)
+    return full, image, (lambda kf: back(kf, full))
+
+
+def halfturn_box(box, d1, d2, c):
+    lo, hi = list(box[0]), list(box[1])
+    nlo, nhi = list(lo), list(hi)
+    nlo[d1], nhi[d1] = -hi[d1], -lo[d1]
+    nlo[d2], nhi[d2] = 2 * c - hi[d2], 2 * c - lo[d2]
+    return tuple(nlo), tuple(nhi)
+
+
+def unfolded_halfturn_forest(half):
+    """``test/ghost_oracles.jl:1484-1502``."""
+    d1, d2 = half.seam_plane()
+    M1, c = half.roots[d1], F(half.roots[d2], 2)
+    D = half.D
+    roots = tuple(2 * M1 if d == d1 else half.roots[d] for d in range(D))
+    shift = tuple(M1 if d == d1 else 0 for d in range(D))
+
+    def turn(box, r):
+        return box if r == 0 else halfturn_box(box, d1, d2, c)
+
+    def image(k, r):
+        lo, hi = turn(leafbox(half, k), r)
+        return box_key(roots, (tuple(x + s for x, s in zip(lo, shift)),
+                               tuple(x + s for x, s in zip(hi, shift))))
+
+    def back(kf, full):
+        lo, hi = leafbox(full, kf)
+        box = (tuple(x - s for x, s in zip(lo, shift)), tuple(x - s for x, s in zip(hi, shift)))
+        r = 2 if box[1][d1] <= 0 else 0
+        return r, box_key(half.roots, turn(box, r))
+
+    refl = tuple((a == 1, b == 1) for a, b in half.faces)
+    leaves = [image(k, r) for k in half.leaves for r in (0, 2)]
+    full = Forest(roots, N=half.N, periodic=half.periodic, reflecting=refl, leaves=leaves)
+    return full, image, (lambda kf: back(kf, full))
+
+
+def neighbor_mismatches(quad, half=False):
+    """``seam_neighbor_mismatches`` / ``halfturn_neighbor_mismatches``
+    (``test/ghost_oracles.jl:860-900, 1508-1540``)."""
+    d1, d2 = quad.seam_plane()
+    full, image, back = (unfolded_halfturn_forest if half else unfolded_forest)(quad)
+    bad = 0
+    seen = {}
+    for k in quad.leaves:
+        for delta in alldirections(quad.D):
+            r, keys = quad.turned_neighbors(k, delta)
+            unfolded = full.oriented_neighbors(image(k, 0), delta)
+            expected = [back(kf) for kf in unfolded]
+            if not expected:
+                lo, hi = leafbox(quad, k)
+                s = hi[0] - lo[0]
+                if half:
+                    want = 2 if hi[d1] + s * delta[d1] <= 0 else 0
+                else:
+                    want = box_orientation((tuple(lo[d] + s * delta[d] for d in range(quad.D)),
+                                            tuple(hi[d] + s * delta[d] for d in range(quad.D))),
+                                           d1, d2)
+                ok = not keys and r == want
+            else:
+                ok = all(e[0] == r for e in expected) and \
+                    sorted(keys) == sorted(e[1] for e in expected) and \
+                    all(kf.level <= k.level or
+                        virtual_offset(childoffset(kq), r, d1, d2) == childoffset(kf)
+                        for kf, (_, kq) in zip(unfolded, expected))
+            bad += not ok
+            kind = "none" if not keys else "same" if keys[0].level == k.level else \
+                "coarser" if keys[0].level < k.level else "finer"
+            seen[(r, kind)] = seen.get((r, kind), 0) + 1
+    return bad, seen, full
+
+
+def random_seam_forest(rng, D, *, plane, M, other="outer", nsteps, maxlvl, half=False,
+                       M2=None):
+    """``random_rotating_forest`` / ``random_halfturn_forest``
+    (``test/ghost_oracles.jl:944-961, 1561-1590``)."""
+    d1, d2 = plane
+    roots = []
+    for d in range(1, D + 1):
+        if d == d1:
+            roots.append(M)
+        elif d == d2:
+            roots.append(M2 if half else M)
+        else:
+            roots.append(int(rng.integers(1, 3)))
+    inplane = lambda d: d + 1 in plane                           # noqa: E731
+    periodic = tuple(not inplane(d) and other == "periodic" for d in range(D))
+    reflecting = tuple((not inplane(d) and other == "reflecting", False) for d in range(D))
+    kw = {"halfturn": plane} if half else {"rotating": plane}
+    f = Forest(tuple(roots), N=4, periodic=periodic, reflecting=reflecting, **kw)
+    for _ in range(nsteps):
+        k = f.leaves[int(rng.integers(len(f.leaves)))]
+        if k.level < maxlvl and rng.random() < 0.75:
+            f.refine([k])
+        elif k.level > 0:
+            p = MortonKey(k.root, k.level - 1, tuple(c >> 1 for c in k.coords))
+            kids = [MortonKey(p.root, p.level + 1, tuple(2 * c + o for c, o in zip(p.coords, off)))
+                    for off in itertools.product((0, 1), repeat=D)]
+            if all(f.isleaf(c) for c in kids):
+                f.coarsen([p])
+    return f
+
+
+def seam_conforming(full, d1, d2):
+    """Leaves sharing a face across an image of the seam are at one level
+    (``test/ghost_oracles.jl:906-919``)."""
+    M = full.roots[d1] // 2
+    for kf in full.leaves:
+        for d in (d1, d2):
+            for s in (-1, 1):
+                delta = tuple(s if e == d else 0 for e in range(full.D))
+                hi = leafbox(full, kf)[1][d]
+                for nf in full.oriented_neighbors(kf, delta):
+                    across = (hi <= M) != (leafbox(full, nf)[1][d] <= M)
+                    if across and nf.level != kf.level:
+                        return False
+    return True
+
+
+# --- the tree ----------------------------------------------------------------------------
+
+def test_a_seam_is_refused_where_it_cannot_be_glued():
+    """``test/rotate_tests.jl:19-61``, ``test/halfturn_tests.jl:22-82``."""
+    with pytest.raises(ValueError, match="at least two dimensions"):
+        Forest((2,), N=4, rotating=(1, 2))
+    with pytest.raises(ValueError, match="outside 1:2"):
+        Forest((2, 2), N=4, rotating=(1, 3))
+    with pytest.raises(ValueError, match="twice"):
+        Forest((2, 2), N=4, rotating=(2, 2))
+    with pytest.raises(ValueError, match="as many roots along dimension 1 as along 2"):
+        Forest((2, 1), N=4, rotating=(1, 2))
+    with pytest.raises(ValueError, match="dimension 2 is periodic"):
+        Forest((2, 2), N=4, periodic=(False, True), rotating=(1, 2))
+    with pytest.raises(ValueError, match="dimension 1 has a reflecting face"):
+        Forest((2, 2), N=4, reflecting=((False, True), (False, False)), rotating=(1, 2))
+    assert Forest((2, 2, 1), N=4, periodic=(False, False, True), rotating=(1, 2)).hasrotating()
+    assert Forest((2, 1, 2), N=4, rotating=(3, 1)).rotating_dims() == (3, 1)
+    assert Forest((2, 2), N=4).rotating == (0, 0)
+    with pytest.raises(ValueError, match="both given"):
+        Forest((2, 2), N=4, rotating=(1, 2), halfturn=(1, 2))
+    with pytest.raises(ValueError, match="even number of roots"):
+        Forest((1, 3), N=4, halfturn=(1, 2))
+    h = Forest((1, 2), N=4, halfturn=(1, 2))
+    assert h.hasrotating() and h.ishalfturn() and h.halfturn_dims() == (1, 2)
+    assert h.rotating_dims() is None
+
+
+@pytest.mark.parametrize("d1,d2", [(0, 1), (1, 0), (0, 2), (2, 1)])
+def test_direction_and_offset_maps_turn_by_the_rotation(d1, d2):
+    """``test/rotate_tests.jl:63-83``: against turned unit boxes."""
+    for r in range(4):
+        for delta in alldirections(3):
+            unit = ((F(0),) * 3, tuple(F(x) for x in delta))
+            lo, hi = rotate_box(unit, -r, d1, d2)
+            assert real_direction(delta, r, d1, d2) == tuple(int(lo[d] + hi[d]) for d in range(3))
+        for o in itertools.product((0, 1), repeat=3):
+            box = (tuple(F(o[d] - 1) for d in range(3)), tuple(F(o[d]) for d in range(3)))
+            lo, _ = rotate_box(box, r, d1, d2)
+            assert virtual_offset(o, r, d1, d2) == tuple(int(lo[d]) + 1 for d in range(3))
+
+
+def test_a_block_at_the_axis_is_its_own_neighbour():
+    """``test/rotate_tests.jl:131-156``."""
+    f = Forest((1, 1), N=4, rotating=(1, 2))
+    k = f.leaves[0]
+    assert f.turned_neighbors(k, (-1, 0)) == (1, [k])
+    assert f.turned_neighbors(k, (0, -1)) == (3, [k])
+    assert f.turned_neighbors(k, (-1, -1)) == (2, [k])
+    assert f.turned_neighbors(k, (-1, 1)) == (1, [])
+    assert f.turned_neighbors(k, (1, -1)) == (3, [])
+    assert f.turned_neighbors(k, (1, 0)) == (0, [])
+    octant = Forest((1, 1, 1), N=4, rotating=(1, 2),
+                    reflecting=((False, False), (False, False), (True, False)))
+    k = octant.leaves[0]
+    assert octant.wall_direction(k, (-1, 0, -1))[0] == (-1, 0, 0)
+    assert octant.turned_neighbors(k, (-1, 0, 0)) == (1, [k])
+
+
+@pytest.mark.parametrize("D,plane,other", [(2, (1, 2), "outer"), (2, (2, 1), "outer"),
+                                           (3, (1, 2), "outer"), (3, (1, 2), "periodic"),
+                                           (3, (1, 2), "reflecting"), (3, (3, 1), "periodic"),
+                                           (3, (2, 3), "reflecting")])
+def test_the_seams_neighbours_are_the_unfolded_forests(D, plane, other):
+    """``test/rotate_tests.jl:85-129``: random unbalanced quadrants, then
+    balanced; every orientation meets every kind of neighbour."""
+    rng = np.random.default_rng(1212 + D + 10 * plane[0] + len(other))
+    seen = {}
+    d1, d2 = plane[0] - 1, plane[1] - 1
+    for trial in range(4 if D == 2 else 2):
+        quad = random_seam_forest(rng, D, plane=plane, M=int(rng.integers(1, 3)), other=other,
+                                  nsteps=30 if D == 2 else 12, maxlvl=3)
+        bad, s, _ = neighbor_mismatches(quad)
+        assert bad == 0
+        for key, n in s.items():
+            seen[key] = seen.get(key, 0) + n
+        quad.balance()
+        assert quad.isbalanced()
+        bad, s, full = neighbor_mismatches(quad)
+        assert bad == 0
+        for key, n in s.items():
+            seen[key] = seen.get(key, 0) + n
+        assert full.isbalanced()
+        assert seam_conforming(full, d1, d2)
+    assert all(seen.get((r, "same"), 0) > 0 for r in range(4))
+    assert all(seen.get((r, "none"), 0) > 0 for r in (0, 1, 3))
+
+
+@pytest.mark.parametrize("D,plane,other", [(2, (1, 2), "outer"), (2, (2, 1), "outer"),
+                                           (3, (1, 2), "periodic"), (3, (3, 2), "reflecting")])
+def test_the_half_planes_neighbours_are_the_unfolded_forests(D, plane, other):
+    """``test/halfturn_tests.jl:84-128``."""
+    rng = np.random.default_rng(1414 + D + 10 * plane[0])
+    seen = {}
+    for trial in range(4 if D == 2 else 2):
+        half = random_seam_forest(rng, D, plane=plane, M=int(rng.integers(1, 3)),
+                                  M2=2 * int(rng.integers(1, 3)), other=other,
+                                  nsteps=30 if D == 2 else 12, maxlvl=3, half=True)
+        bad, s, _ = neighbor_mismatches(half, half=True)
+        assert bad == 0
+        for key, n in s.items():
+            seen[key] = seen.get(key, 0) + n
+        half.balance()
+        assert half.isbalanced()
+        bad, s, full = neighbor_mismatches(half, half=True)
+        assert bad == 0
+        for key, n in s.items():
+            seen[key] = seen.get(key, 0) + n
+        assert full.isbalanced()
+    assert seen.get((2, "same"), 0) > 0 and seen.get((0, "same"), 0) > 0

@@ -14,9 +14,15 @@ walks once per regrid (never on the per-fill path):
   ``src/forest.jl:1632-1675``.
 * ``wall_direction`` -- ``src/forest.jl:1617-1630``.
 * ``refine`` / ``coarsen`` / ``balance`` -- ``src/forest.jl:1761-1890``.
+* Rotating seams (a quarter turn, ``rotating = (d1, d2)``) and half-turn
+  seams (``halfturn = (d1, d2)``): the constructor's checks
+  (``src/forest.jl:737-835``), the node a step lands on across the seam
+  and its orientation (``seam_orientation``, ``unrotate_node``,
+  ``stepped_node``, ``src/forest.jl:1406-1501``), the direction and child
+  offset maps (``real_direction``, ``virtual_offset``, :1428-1464) and
+  conformity at the seam in ``balance`` (:1837-1890).
 
-Rotating seams, half turns and glued patches are not implemented here
-(no workload of the ghost-fill engine uses them).
+Glued patches are not implemented here.
 """
 from __future__ import annotations
 
@@ -79,6 +85,40 @@ def childoffset(k: MortonKey) -> Tuple[int, ...]:
     return tuple(c & 1 for c in k.coords)
 
 
+def real_direction(delta, r: int, d1: int, d2: int) -> Tuple[int, ...]:
+    """``R^{-r} delta`` (``src/forest.jl:1428-1438``): a ghost direction as
+    seen from the real leaves across a seam in orientation ``r``; ``d1`` and
+    ``d2`` are 0-based."""
+    a, b = delta[d1], delta[d2]
+    r1, r2 = {1: (b, -a), 3: (-b, a), 2: (-a, -b)}.get(r, (a, b))
+    out = list(delta)
+    out[d1], out[d2] = r1, r2
+    return tuple(out)
+
+
+def virtual_offset(o, r: int, d1: int, d2: int) -> Tuple[int, ...]:
+    """A real leaf's child offset taken into the virtual frame, where the
+    asking block sees it across the seam (``src/forest.jl:1450-1464``)."""
+    a, b = o[d1], o[d2]
+    v1, v2 = {1: (1 - b, a), 3: (b, 1 - a), 2: (1 - a, 1 - b)}.get(r, (a, b))
+    out = list(o)
+    out[d1], out[d2] = v1, v2
+    return tuple(out)
+
+
+def axismap(r: int, d1: int, d2: int, D: int):
+    """The axis map of orientation ``r`` across the seam of the plane
+    ``(d1, d2)`` (0-based), in gather form (``src/ghosts.jl:221-234``):
+    virtual stored index ``k`` reads the real point whose index along ``e``
+    is ``k[perm[e]]``, or ``S + 1 - k[perm[e]]`` where ``flip[e]``."""
+    swapped = r % 2 == 1
+    perm = tuple(d2 if swapped and e == d1 else d1 if swapped and e == d2 else e
+                 for e in range(D))
+    flip = tuple((r >= 2) if e == d1 else (r in (1, 2)) if e == d2 else False
+                 for e in range(D))
+    return perm, flip
+
+
 def alldirections(D: int) -> List[Tuple[int, ...]]:
     """All ``3^D - 1`` directions, dimension 1 fastest, as Julia's
     ``Iterators.product`` gives them (``src/forest.jl:1319-1323``)."""
@@ -103,7 +143,9 @@ class Forest:
                  reflecting: Optional[Sequence[Tuple[bool, bool]]] = None,
                  outflow: Optional[Sequence[Tuple[bool, bool]]] = None,
                  extents: Optional[Sequence[Tuple[float, float]]] = None,
-                 leaves: Optional[Iterable[MortonKey]] = None):
+                 leaves: Optional[Iterable[MortonKey]] = None,
+                 rotating: Optional[Tuple[int, int]] = None,
+                 halfturn: Optional[Tuple[int, int]] = None):
         D = len(roots)
         if not all(r > 0 for r in roots):
             raise ValueError(f"roots must all be positive, got {tuple(roots)}")
@@ -128,6 +170,12 @@ class Forest:
             faces.append(tuple(fk))
         if extents is None:
             extents = tuple((0.0, float(r)) for r in roots)
+        if halfturn is not None:
+            self.rotating = _check_halfturn(halfturn, rotating, tuple(roots), periodic,
+                                            reflecting, outflow)
+        else:
+            self.rotating = _check_rotating(rotating, tuple(roots), periodic, reflecting,
+                                            outflow)
         self.D = D
         self.roots = tuple(int(r) for r in roots)
         self.periodic = periodic
@@ -177,14 +225,73 @@ class Forest:
             stride *= r
         return idx
 
-    # -- neighbours ----------------------------------------------------------
-    def neighbor_anchor(self, k: MortonKey, delta: Sequence[int]):
-        """The same-level node one step from ``k`` in ``delta`` as
-        ``(root, coords)``, wrapping periodic dimensions; ``None`` beyond a
-        non-periodic face (``src/forest.jl:1501-1520``)."""
+    # -- the seam (quarter or half turn) ---------------------------------------
+    def hasrotating(self) -> bool:
+        return self.rotating[0] != 0
+
+    def ishalfturn(self) -> bool:
+        return self.rotating[1] < 0
+
+    def seam_plane(self) -> Tuple[int, int]:
+        """The seam's plane ``(d1, d2)`` as 0-based dimensions."""
+        return self.rotating[0] - 1, abs(self.rotating[1]) - 1
+
+    def rotating_dims(self):
+        """The ``rotating`` keyword's pair (1-based), or ``None``."""
+        return (self.rotating[0], self.rotating[1]) if self.hasrotating() and \
+            not self.ishalfturn() else None
+
+    def halfturn_dims(self):
+        return (self.rotating[0], -self.rotating[1]) if self.ishalfturn() else None
+
+    def seam_orientation(self, g: Sequence[int]) -> int:
+        """The orientation of the naive node at global level coordinates
+        ``g`` (``src/forest.jl:1406-1413``)."""
+        if not self.hasrotating():
+            return 0
+        d1, d2 = self.seam_plane()
+        if self.ishalfturn():
+            return 2 if g[d1] < 0 else 0
+        a, b = g[d1] < 0, g[d2] < 0
+        return (2 if b else 1) if a else (3 if b else 0)
+
+    def stepped_node(self, k: MortonKey, delta: Sequence[int]):
+        """The real node one step from ``k`` in ``delta`` in global level
+        coordinates, and its orientation: the naive step mapped back across
+        the seam it crosses (``unrotate_node``, ``stepped_node``,
+        ``src/forest.jl:1415-1499``).  Periodic wraps and high faces are
+        left to ``neighbor_anchor``."""
         lvl = k.level
         rp = self.root_position(k.root)
         g = [(rp[d] << lvl) + k.coords[d] + delta[d] for d in range(self.D)]
+        r = self.seam_orientation(g)
+        if r == 0:
+            return g, 0
+        d1, d2 = self.seam_plane()
+        n2 = self.roots[d2] << lvl if self.ishalfturn() else 0
+        g1, g2 = g[d1], g[d2]
+        if r == 1:
+            g[d1], g[d2] = g2, -1 - g1
+        elif r == 3:
+            g[d1], g[d2] = -1 - g2, g1
+        else:
+            g[d1], g[d2] = -1 - g1, n2 - 1 - g2
+        return g, r
+
+    def turns(self, k: MortonKey, delta: Sequence[int]) -> int:
+        """The orientation of the region of ``k`` in ``delta``: 0 off the
+        seam, else the quarter turns that carry the real leaves there to
+        where ``k`` sees them (``Crossing.turns``)."""
+        return self.stepped_node(k, delta)[1] if self.hasrotating() else 0
+
+    # -- neighbours ----------------------------------------------------------
+    def neighbor_anchor(self, k: MortonKey, delta: Sequence[int]):
+        """The same-level node one step from ``k`` in ``delta`` as
+        ``(root, coords)``, wrapping periodic dimensions and crossing a seam
+        into the real node; ``None`` beyond a non-periodic face that is not
+        the seam (``src/forest.jl:1501-1520``)."""
+        lvl = k.level
+        g, _ = self.stepped_node(k, delta)
         for d in range(self.D):
             n = self.roots[d] << lvl
             if (g[d] < 0 or g[d] >= n) and not self.periodic[d]:
@@ -224,17 +331,29 @@ class Forest:
                 self._collect_touching(out, root, cl, cc, delta)
         return out
 
-    def oriented_neighbors(self, k: MortonKey, delta: Sequence[int]) -> List[MortonKey]:
-        """The leaves abutting ``k`` across the face, edge or corner ``delta``
-        (``src/forest.jl:1718-1740``; no seams here, so no crossing)."""
+    def turned_neighbors(self, k: MortonKey, delta: Sequence[int]):
+        """``(turns, keys)``: the real leaves abutting ``k`` across the face,
+        edge or corner ``delta`` and the orientation that carries them to
+        where ``k`` sees them (``oriented_neighbors``,
+        ``src/forest.jl:1718-1740``).  Across a seam ``turns`` is the
+        region's orientation even when there is no leaf; the search for
+        finer leaves runs in the real frame, in the direction from them back
+        to ``k``'s image."""
         anchor = self.neighbor_anchor(k, delta)
+        r = self.turns(k, delta)
         if anchor is None:
-            return []
+            return r, []
         root, coords = anchor
         i = self.find_covering_leaf(root, k.level, coords)
         if i is not None:
-            return [self.leaves[i]]
-        return self._collect_touching([], root, k.level, coords, delta)
+            return r, [self.leaves[i]]
+        dreal = real_direction(delta, r, *self.seam_plane()) if r else delta
+        return r, self._collect_touching([], root, k.level, coords, dreal)
+
+    def oriented_neighbors(self, k: MortonKey, delta: Sequence[int]) -> List[MortonKey]:
+        """The leaves abutting ``k`` across the face, edge or corner
+        ``delta`` (``neighbor_keys``): the keys of ``turned_neighbors``."""
+        return self.turned_neighbors(k, delta)[1]
 
     neighbor_keys = oriented_neighbors
 
@@ -306,14 +425,24 @@ class Forest:
         self._reindex()
         return self
 
+    def balance_slack(self, k: MortonKey, delta: Sequence[int]) -> int:
+        """How many levels two adjacent leaves may differ by: one, but none
+        across a seam's face, where the leaves conform
+        (``src/forest.jl:1882-1883``)."""
+        if self.hasrotating() and sum(1 for x in delta if x) == 1 and self.turns(k, delta):
+            return 0
+        return 1
+
     def balance(self):
-        """2:1 balance across faces, edges and corners (``src/forest.jl:1837-1868``)."""
+        """2:1 balance across faces, edges and corners, and conformity at a
+        seam's face (``src/forest.jl:1837-1868``)."""
         dirs = alldirections(self.D)
+        seam = self.hasrotating()
         while True:
             found = []
             seen = set()
             for k in self.leaves:
-                if k.level < 2:
+                if k.level < 2 and not (k.level == 1 and seam):
                     continue
                 for delta in dirs:
                     anchor = self.neighbor_anchor(k, delta)
@@ -323,7 +452,7 @@ class Forest:
                     if i is None:
                         continue
                     nb = self.leaves[i]
-                    if nb.level < k.level - 1 and nb not in seen:
+                    if nb.level < k.level - self.balance_slack(k, delta) and nb not in seen:
                         seen.add(nb)
                         found.append(nb)
             if not found:
@@ -336,7 +465,7 @@ class Forest:
         for k in self.leaves:
             for delta in dirs:
                 for nb in self.oriented_neighbors(k, delta):
-                    if abs(nb.level - k.level) > 1:
+                    if abs(nb.level - k.level) > self.balance_slack(k, delta):
                         return False
         return True
 
@@ -376,6 +505,87 @@ class Forest:
         h = float(self.spacing(k.level))
         return tuple((nodeposition(lo[d], h, B[d], 1, 1), nodeposition(lo[d], h, B[d], self.N + 1, 1))
                      for d in range(self.D))
+
+
+def _check_rotating(rotating, roots, periodic, reflecting, outflow):
+    """The ``rotating`` keyword as the forest stores it, ``(0, 0)`` for none
+    (``check_rotating``, ``src/forest.jl:740-784``)."""
+    if rotating is None:
+        return (0, 0)
+    D = len(roots)
+    d1, d2 = int(rotating[0]), int(rotating[1])
+    rot = (d1, d2)
+    if D < 2:
+        raise ValueError(f"rotating = {rot} needs at least two dimensions, and this forest "
+                         f"has {D}: the rotation turns the plane of two dimensions about the "
+                         "line where their low faces meet")
+    if not (1 <= d1 <= D and 1 <= d2 <= D):
+        raise ValueError(f"rotating = {rot} names a dimension outside 1:{D}: the pair "
+                         "(d1, d2) is the plane of the rotation, two of the forest's own "
+                         "dimensions")
+    if d1 == d2:
+        raise ValueError(f"rotating = {rot} names dimension {d1} twice: the rotation turns "
+                         "the plane of two different dimensions")
+    if roots[d1 - 1] != roots[d2 - 1]:
+        raise ValueError(f"rotating = {rot} needs as many roots along dimension {d1} as "
+                         f"along {d2}, got {roots[d1 - 1]} and {roots[d2 - 1]}: the seam "
+                         f"glues the low face of {d1} onto the low face of {d2}, root for "
+                         "root")
+    for d in (d1, d2):
+        if periodic[d - 1]:
+            raise ValueError(f"rotating = {rot}, but dimension {d} is periodic: its low "
+                             "face is the rotating seam, and a periodic dimension has no "
+                             "faces")
+        if any(reflecting[d - 1]):
+            raise ValueError(f"rotating = {rot}, but dimension {d} has a reflecting face: "
+                             "its low face is the rotating seam and its high face stays "
+                             "outer; a reflecting high wall with the rotation is an open "
+                             "question, not implemented")
+        if any(outflow[d - 1]):
+            raise ValueError(f"rotating = {rot}, but dimension {d} has an outflow face: "
+                             "its low face is the rotating seam and its high face stays "
+                             "outer; an outflow high face with the rotation is an open "
+                             "question, not implemented")
+    return (d1, d2)
+
+
+def _check_halfturn(halfturn, rotating, roots, periodic, reflecting, outflow):
+    """The ``halfturn`` keyword as the forest stores it, ``(d1, -d2)``
+    (``check_halfturn``, ``src/forest.jl:788-834``)."""
+    if rotating is not None:
+        raise ValueError(f"rotating = {tuple(rotating)} and halfturn = {tuple(halfturn)} are "
+                         "both given: a forest has one seam at most. Declare one.")
+    D = len(roots)
+    d1, d2 = int(halfturn[0]), int(halfturn[1])
+    ht = (d1, d2)
+    if D < 2:
+        raise ValueError(f"halfturn = {ht} needs at least two dimensions, and this forest "
+                         f"has {D}")
+    if not (1 <= d1 <= D and 1 <= d2 <= D):
+        raise ValueError(f"halfturn = {ht} names a dimension outside 1:{D}: the pair "
+                         "(d1, d2) is the plane of the rotation")
+    if d1 == d2:
+        raise ValueError(f"halfturn = {ht} names dimension {d1} twice: the half turn glues "
+                         "the low face of the first dimension to itself, reversed along "
+                         "the second, a different one")
+    if roots[d2 - 1] % 2:
+        raise ValueError(f"halfturn = {ht} needs an even number of roots along dimension "
+                         f"{d2}, got {roots[d2 - 1]}: the axis of the turn lies on the "
+                         "centre plane, and it must lie on a root boundary")
+    for d in (d1, d2):
+        if periodic[d - 1]:
+            raise ValueError(f"halfturn = {ht}, but dimension {d} is periodic: a periodic "
+                             "dimension with a half turn is an open question, not "
+                             "implemented")
+        if any(reflecting[d - 1]):
+            raise ValueError(f"halfturn = {ht}, but dimension {d} has a reflecting face: "
+                             "a reflecting face with the half turn is an open question, not "
+                             "implemented")
+        if any(outflow[d - 1]):
+            raise ValueError(f"halfturn = {ht}, but dimension {d} has an outflow face: "
+                             "an outflow face with the half turn is an open question, not "
+                             "implemented")
+    return (d1, -d2)
 
 
 def nodeposition(lo, h, B: int, I: int, c: int, dtype=float):
