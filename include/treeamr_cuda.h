@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TAM_ABI_VERSION 1
+#define TAM_ABI_VERSION 2
 #define TAM_MAX_DIM 3
 
 enum tam_status {
@@ -74,6 +74,16 @@ typedef struct tam_group {
   int32_t stage;     /* stage tag (transfer_stage, src/schedule.jl:656)   */
   int32_t factorcol; /* 0, or the 1-based factor-table column             */
   int32_t bounded;   /* must be 0: bounded operators are not built        */
+  /* A turned group (across a rotating or half-turn seam, TransferGroup's
+   * orientation/perm/flip, src/schedule.jl:150-197, src/ghosts.jl:183-244):
+   * orientation r in 1..3 (0: an ordinary group), and its axis map in
+   * gather form, `axes` = sum_e perm[e] << 2e  +  flip[e] << (8 + e) with
+   * 0-based dimensions: virtual stored index k reads the real point whose
+   * index along e is k[perm[e]], or S_e + 1 - k[perm[e]] where flip[e], and
+   * variable rotvars[v + nvars * r] (1-based) of the real source.  An odd
+   * orientation reads the alternate array of tam_fill_ex. */
+  int32_t orientation;
+  int32_t axes;
   int64_t first;     /* offset into the block lists                        */
   int64_t ntransfers;
   tam_stencil stencil[TAM_MAX_DIM]; /* dimensions >= ndim are ignored      */
@@ -87,7 +97,8 @@ typedef struct tam_schedule_desc {
   int32_t stored[TAM_MAX_DIM];/* S_d                                       */
   int64_t nblocks;
   int32_t ngroups;
-  int32_t nfactorcols;        /* 3^D, the factor table's columns           */
+  int32_t nfactorcols;        /* 3^D, or 4 * 3^D over a seam (the columns
+                                 mirror + 3^D r, src/storage.jl:717-740)   */
   const tam_group *groups;
   int64_t ntransfers;         /* length of both block lists                */
   const int32_t *targetblocks;/* 1-based                                   */
@@ -137,6 +148,20 @@ int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
              const void *factors, int32_t first_stage, int32_t last_stage,
              void *stream);
 
+/* tam_fill and tam_fill_plain with what a turned group reads
+ * (run_group!'s altsrc and rotvars, src/ghosts.jl:420-490): `rotvars`, a
+ * device table of nvars x 4 int32 (column-major, 1-based variables; the
+ * field set's variable map per orientation), required when the schedule has
+ * a turned group, and `alt_work`, the array an odd orientation reads (a
+ * RotationPair's partner; NULL: `work` itself).  `method` is
+ * TAM_METHOD_FUSED or TAM_METHOD_PLAIN.  A turned group runs in its own
+ * launch after the stage's fused launches. */
+#define TAM_METHOD_FUSED 0
+#define TAM_METHOD_PLAIN 1
+int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars,
+                int64_t nblocks, const void *factors, const int32_t *rotvars,
+                int32_t first_stage, int32_t last_stage, int32_t method, void *stream);
+
 /* The fill of a field set whose data live in host memory (the reference's
  * fill_ghosts!, src/ghosts.jl:1783, on host arrays): asynchronous on
  * `stream`, host_in (nblocks * nvars * S1*S2*S3 elements in the layout of
@@ -182,7 +207,8 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
  * the ghosts' own adjoints are zeroed.  Same arguments as tam_fill; `y`
  * has the layout of `work`.  The library allocates its scratch on the
  * first call with a given nvars (so make that call before any stream
- * capture). */
+ * capture).  A schedule with a turned group (a seam) is refused with
+ * TAM_EUNSUPPORTED. */
 int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                      const void *factors, int32_t first_stage, int32_t last_stage,
                      void *stream);

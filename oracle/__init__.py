@@ -58,6 +58,10 @@ def lib():
         l.oracle_fill.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                   C.c_int32, C.c_int, C.c_int]
         l.oracle_fill.restype = C.c_int
+        l.oracle_fill_turned.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                         C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int,
+                                         C.c_int]
+        l.oracle_fill_turned.restype = C.c_int
         l.oracle_fill_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                           C.c_int32, C.c_int32]
         l.oracle_fill_adjoint.restype = C.c_int
@@ -78,21 +82,32 @@ ALL_FIRST, ALL_LAST = -1, 0x7FFFFFFF
 
 
 def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
-         last=ALL_LAST, nthreads: int = 1, one_tap: bool = True) -> np.ndarray:
+         last=ALL_LAST, nthreads: int = 1, one_tap: bool = True, rotvars=None,
+         alt: np.ndarray = None) -> np.ndarray:
     """In place on ``work`` (shape (nblocks, nvars, S_D..S_1), C order).
 
     ``one_tap`` picks the form of the stencil sum (src/ghosts.jl:28-56): the
     reference's CPU form, where a dimension whose weight column has a single
     nonzero weight takes only that tap, or (False) its device form, the full
     sum.  They differ only where a NaN or an infinity sits under a zero
-    weight."""
+    weight.  A schedule that turns transfers across a seam reads the field
+    set's variable table ``rotvars`` (nvars x 4, 1-based) and, for an odd
+    orientation, ``alt`` (default ``work``)."""
     assert work.flags.c_contiguous and work.dtype == np.dtype(schedule.T)
     d = _descriptor(schedule)
     f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=work.dtype)
-    rc = lib().oracle_fill(C.addressof(d.desc), work.ctypes.data, nvars, f.ctypes.data, first,
-                           last, nthreads, 1 if one_tap else 0)
+    if rotvars is None:
+        rc = lib().oracle_fill(C.addressof(d.desc), work.ctypes.data, nvars, f.ctypes.data,
+                               first, last, nthreads, 1 if one_tap else 0)
+    else:
+        rv = np.ascontiguousarray(np.asfortranarray(rotvars).ravel(order="F"), dtype=np.int32)
+        a = work if alt is None else alt
+        assert a.flags.c_contiguous and a.shape == work.shape and a.dtype == work.dtype
+        rc = lib().oracle_fill_turned(C.addressof(d.desc), work.ctypes.data, a.ctypes.data,
+                                      nvars, f.ctypes.data, rv.ctypes.data, first, last,
+                                      nthreads, 1 if one_tap else 0)
     if rc != 0:
-        raise RuntimeError("oracle_fill failed")
+        raise RuntimeError("oracle_fill failed (a turned schedule needs rotvars)")
     return work
 
 
@@ -114,13 +129,15 @@ def fill_fieldset(fs, schedule, *, boundary_values=None, nthreads: int = 1,
     host array; ``boundary_values(host, fs, regions)`` fills the outer-face
     regions between phase 1 and the prolongations."""
     host = fs.work.detach().cpu().numpy().copy()
+    rv = getattr(fs, "rotvars_host", None)
     if boundary_values is None or not schedule.boundaries:
         return fill(schedule, host, fs.nvars, fs.factors_host, nthreads=nthreads,
-                    one_tap=one_tap)
-    fill(schedule, host, fs.nvars, fs.factors_host, last=1, nthreads=nthreads, one_tap=one_tap)
+                    one_tap=one_tap, rotvars=rv)
+    fill(schedule, host, fs.nvars, fs.factors_host, last=1, nthreads=nthreads, one_tap=one_tap,
+         rotvars=rv)
     boundary_values(host, fs, schedule.boundaries)
     return fill(schedule, host, fs.nvars, fs.factors_host, first=2, nthreads=nthreads,
-                one_tap=one_tap)
+                one_tap=one_tap, rotvars=rv)
 
 
 def _own_slices(fs):

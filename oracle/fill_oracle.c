@@ -25,6 +25,8 @@
  *                            (src/threading.jl:50-70 equalsplit), each thread
  *                            running its share of every group of the stage
  *   - exchange_ghosts!       src/ghosts.jl:1099-1160: stages in tag order
+ *   - RotatedSource          src/ghosts.jl:183-244: a turned group's source
+ *                            read through its axis map and variable table
  *   - the adjoint (transpose) of the same linear map, stage by stage in
  *     reverse, in scatter form: a new capability with no reference
  *     counterpart, so its oracle is the linear algebra of the forward.
@@ -63,8 +65,9 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
 
 #define DEFINE_ORACLE(T, SUFFIX)                                                                \
   static void run_transfers_##SUFFIX(const tam_schedule_desc *d, const tam_group *g,            \
-                                     int64_t t0, int64_t t1, T *work, int32_t nvars,           \
-                                     const T *factors, int one_tap) {                           \
+                                     int64_t t0, int64_t t1, T *work, const T *alt,            \
+                                     int32_t nvars, const T *factors, const int32_t *rotvars,  \
+                                     int one_tap) {                                             \
     const int D = d->ndim;                                                                      \
     int n[3] = {1, 1, 1}, o[3] = {1, 1, 1}, tf[3] = {0, 0, 0};                                  \
     int64_t S[3] = {1, 1, 1};                                                                   \
@@ -79,6 +82,19 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
     const T *W = (const T *)d->weights;                                                         \
     const int64_t s2 = S[0], s3 = S[0] * S[1], vs = S[0] * S[1] * S[2];                         \
     const int64_t bs = vs * nvars;                                                              \
+    /* the source's strides per virtual dimension: the identity, or a turned  \
+       group's axis map (RotatedSource, src/ghosts.jl:183-244) */              \
+    int64_t vst[3] = {1, s2, s3}, c0 = 0;                                                       \
+    const int64_t rst[3] = {1, s2, s3};                                                         \
+    const T *from = work;                                                                       \
+    if (g->orientation) {                                                                       \
+      for (int e = 0; e < D; ++e) {                                                             \
+        const int p = (g->axes >> (2 * e)) & 3, f = (g->axes >> (8 + e)) & 1;                  \
+        vst[p] = f ? -rst[e] : rst[e];                                                          \
+        if (f) c0 += rst[e] * (S[e] - 1);                                                       \
+      }                                                                                         \
+      if (g->orientation & 1) from = alt;                                                       \
+    }                                                                                           \
     for (int64_t t = t0; t < t1; ++t) {                                                         \
       const int64_t tb = d->targetblocks[g->first + t] - 1;                                     \
       const int64_t sb = d->sourceblocks[g->first + t] - 1;                                     \
@@ -105,7 +121,10 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
                   hi[k] = row + 1;                                                              \
                 }                                                                               \
               }                                                                                 \
-              const T *src = work + sb * bs + v * vs + base[0] + base[1] * s2 + base[2] * s3;   \
+              const int sv = g->orientation ? rotvars[v + (int64_t)nvars * g->orientation] - 1  \
+                                            : v;                                                \
+              const T *src = from + sb * bs + sv * vs + c0 + base[0] * vst[0] +                 \
+                             base[1] * vst[1] + base[2] * vst[2];                               \
               T acc = (T)0;                                                                     \
               if (unit) {                                                                       \
                 acc = (T)0 + src[0];                                                            \
@@ -116,7 +135,7 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
                       T wp = wc[0][m1];                                                         \
                       if (D >= 2) wp = wp * wc[1][m2];                                          \
                       if (D >= 3) wp = wp * wc[2][m3];                                          \
-                      T term = wp * src[m1 + m2 * s2 + m3 * s3];                                \
+                      T term = wp * src[m1 * vst[0] + m2 * vst[1] + m3 * vst[2]];               \
                       acc = acc + term;                                                         \
                     }                                                                           \
               }                                                                                 \
@@ -132,8 +151,8 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
   }                                                                                             \
                                                                                                 \
   static void run_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *work,             \
-                                 int32_t nvars, const T *factors, int nthreads,                 \
-                                 int one_tap) {                                                 \
+                                 const T *alt, int32_t nvars, const T *factors,                 \
+                                 const int32_t *rotvars, int nthreads, int one_tap) {           \
     _Pragma("omp parallel num_threads(nthreads)") {                                             \
       int c = 0, k = 1;                                                                         \
       ORACLE_THREAD_IDS(c, k);                                                                  \
@@ -145,7 +164,8 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
         const int32_t *owners = d->targetblocks + g->first;                                     \
         int64_t a = lower_bound(owners, 0, g->ntransfers, lo + 1);                              \
         int64_t b = lower_bound(owners, 0, g->ntransfers, hi + 1);                              \
-        if (a < b) run_transfers_##SUFFIX(d, g, a, b, work, nvars, factors, one_tap);           \
+        if (a < b)                                                                              \
+          run_transfers_##SUFFIX(d, g, a, b, work, alt, nvars, factors, rotvars, one_tap);      \
       }                                                                                         \
     }                                                                                           \
   }
@@ -184,23 +204,36 @@ static int collect_tags(const tam_schedule_desc *d, int32_t *tags, int cap) {
 }
 
 /* The serial-forest fill: every stage tag in [first, last], in order.
- * one_tap = 1: the CPU form of the sum, 0: the device form. */
-int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const void *factors,
-                int32_t first, int32_t last, int nthreads, int one_tap) {
+ * one_tap = 1: the CPU form of the sum, 0: the device form.  A turned group
+ * (across a seam) reads variable rotvars[v + nvars r] - 1 (nvars x 4,
+ * column-major, 1-based) of `alt` for an odd orientation r, of `work` for an
+ * even one; `rotvars` may be NULL when the schedule has no turned group. */
+int oracle_fill_turned(const tam_schedule_desc *d, void *work, const void *alt, int32_t nvars,
+                       const void *factors, const int32_t *rotvars, int32_t first,
+                       int32_t last, int nthreads, int one_tap) {
   if (!d || !work || nvars < 1) return -1;
   if (nthreads < 1) nthreads = 1;
+  if (!alt) alt = work;
+  for (int32_t gi = 0; gi < d->ngroups; ++gi)
+    if (d->groups[gi].orientation && !rotvars) return -1;
   int32_t tags[128];
   int nt = collect_tags(d, tags, 128);
   for (int i = 0; i < nt; ++i) {
     if (tags[i] < first || tags[i] > last) continue;
     if (d->dtype == TAM_F64)
-      run_stage_f64(d, tags[i], (double *)work, nvars, (const double *)factors, nthreads,
-                    one_tap);
+      run_stage_f64(d, tags[i], (double *)work, (const double *)alt, nvars,
+                    (const double *)factors, rotvars, nthreads, one_tap);
     else
-      run_stage_f32(d, tags[i], (float *)work, nvars, (const float *)factors, nthreads,
-                    one_tap);
+      run_stage_f32(d, tags[i], (float *)work, (const float *)alt, nvars,
+                    (const float *)factors, rotvars, nthreads, one_tap);
   }
   return 0;
+}
+
+int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const void *factors,
+                int32_t first, int32_t last, int nthreads, int one_tap) {
+  return oracle_fill_turned(d, work, work, nvars, factors, NULL, first, last, nthreads,
+                            one_tap);
 }
 
 /* The transpose of the fill, in scatter form, serial.  Stage s is

@@ -40,7 +40,9 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layout_matches_header():
     # The descriptor structs are the ABI: offsets are plain C layout.
     assert C.sizeof(_native.tam_stencil) == 32
-    assert C.sizeof(_native.tam_group) == 16 + 16 + 3 * 32
+    assert C.sizeof(_native.tam_group) == 24 + 16 + 3 * 32
+    assert _native.tam_group.orientation.offset == 16
+    assert _native.tam_group.first.offset == 24
     assert _native.tam_schedule_desc.groups.offset == 40
     assert C.sizeof(_native.tam_state_layout) == 56
     assert C.sizeof(_native.tam_boundary_region) == 128

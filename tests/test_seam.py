@@ -11,6 +11,7 @@ orientation meeting every kind of neighbour; balance makes the seam
 conforming; the ghosts of a quadrant filled through the turned transfers
 equal the full plane's filled without a seam, for data covariant under the
 turn; and on the GPU the turned fill is the oracle's bit for bit."""
+import ctypes as C
 import itertools
 from fractions import Fraction
 
@@ -319,3 +320,268 @@ def test_the_half_planes_neighbours_are_the_unfolded_forests(D, plane, other):
             seen[key] = seen.get(key, 0) + n
         assert full.isbalanced()
     assert seen.get((2, "same"), 0) > 0 and seen.get((0, "same"), 0) > 0
+
+
+# --- the turned fill -------------------------------------------------------------------
+
+import torch                                                      # noqa: E402
+
+import oracle                                                     # noqa: E402
+from _helpers import nanbits                                      # noqa: E402
+from treeamr import FieldSet, GhostSchedule, Operators            # noqa: E402
+from treeamr.storage import composed_rotation                     # noqa: E402
+
+OPS4 = Operators(prolongation=4, restriction=4)
+
+
+def vector_rotation(D, plane):
+    """A scalar and a vector's components (``test/ghost_oracles.jl:963-967``):
+    the component along d1 becomes minus the one along d2, the one along d2
+    the one along d1."""
+    d1, d2 = plane
+    return [1] + [-(1 + d2) if e == d1 else (1 + d1) if e == d2 else 1 + e
+                  for e in range(1, D + 1)]
+
+
+def vector_halfturn(D, plane):
+    """``test/ghost_oracles.jl:1594``: the in-plane components negate."""
+    return [1] + [-(1 + e) if e in plane else 1 + e for e in range(1, D + 1)]
+
+
+def vector_parity(D, plane, other):
+    """``test/ghost_oracles.jl:974-980``: reflecting at the low face of the
+    dimension outside the plane, the component along its normal odd."""
+    if other != "reflect_lo":
+        return None
+    z = 6 - plane[0] - plane[1]
+    return [tuple("NoParity" if d + 1 != z else "OddParity" if v == z else "EvenParity"
+                  for d in range(D)) for v in range(D + 1)]
+
+
+def seam_forest(D, plane, other, *, half=False, N=8):
+    """A quadrant (or half plane) refined to three levels at the seam and at
+    the axis: 2 roots a side in the plane (the half plane 1 x 2), the third
+    dimension periodic, outer or reflecting at its low face."""
+    d1, d2 = plane
+    roots = []
+    for d in range(1, D + 1):
+        roots.append((1 if d == d1 else 2) if half else 2 if d in plane else 1)
+    periodic = tuple(other == "periodic" and d + 1 not in plane for d in range(D))
+    reflecting = tuple((other == "reflect_lo" and d + 1 not in plane, False) for d in range(D))
+    kw = {"halfturn": plane} if half else {"rotating": plane}
+    f = Forest(tuple(roots), N=N, periodic=periodic, reflecting=reflecting, **kw)
+    # refine the root at the axis, then its children touching the seam face
+    f.refine([f.leaves[0]])
+    f.balance()
+    lo = [k for k in f.leaves if k.level == 1 and k.coords[d1 - 1] == 0 and k.root == 0]
+    f.refine(lo[:1])
+    f.balance()
+    return f
+
+
+def unfold_data(quad, fs, full, image, back, ff, q, half):
+    """The full plane's own points: the quadrant's, turned.  Full leaf
+    ``kf`` is quadrant leaf ``kq`` turned by ``r``, so its own point ``p``
+    holds ``sign[v] * u_kq[sigma[v]](R^{-r} p)``, located with exact
+    positions."""
+    D, N = quad.D, quad.N
+    d1, d2 = quad.seam_plane()
+    G = fs.G
+    host_q = fs.work.numpy()
+    out = np.full(tuple(ff.work.shape), np.nan, dtype=fs.T)
+    qindex = {k: i for i, k in enumerate(quad.leaves)}
+    nv = fs.nvars
+    for bf, kf in enumerate(full.leaves):
+        r, kq = back(kf)
+        bq = qindex[kq]
+        steps = ((q,) if half else (q,) * r) if r else ()
+        sigma, sign = composed_rotation(steps, nv)
+        lof, _ = leafbox(full, kf)
+        loq, _ = leafbox(quad, kq)
+        h = F(1, N << kf.level)
+        shift = tuple(quad.roots[d1] if (d == d1 or (d == d2 and not half)) else 0
+                      for d in range(D))
+        for I in itertools.product(range(N), repeat=D):
+            x = [lof[d] + (I[d] + F(1, 2)) * h - shift[d] for d in range(D)]
+            if r:
+                if half:
+                    c = F(quad.roots[d2], 2)
+                    x[d1], x[d2] = -x[d1], 2 * c - x[d2]
+                else:
+                    for _ in range((4 - r) % 4):             # R^{-r} = R^{4-r}
+                        x[d1], x[d2] = -x[d2], x[d1]
+            J = [int((x[d] - loq[d]) / h - F(1, 2)) for d in range(D)]
+            assert all(0 <= J[d] < N for d in range(D))
+            for v in range(nv):
+                val = host_q[(bq, sigma[v] - 1) + tuple(G[d] + J[d] for d in reversed(range(D)))]
+                out[(bf, v) + tuple(G[d] + I[d] for d in reversed(range(D)))] = \
+                    fs.T.type(sign[v]) * val if sign[v] < 0 else val
+    return out
+
+
+def quadrant_case(D, plane, other, *, half=False, T=np.float64, seed=3):
+    """The quadrant's field set with NaN ghosts and random own points, its
+    schedule, and the full plane's field set with the same data turned."""
+    quad = seam_forest(D, plane, other, half=half)
+    q = (vector_halfturn if half else vector_rotation)(D, plane)
+    kw = {"halfturn": q} if half else {"rotation": q}
+    fs = FieldSet(quad, D + 1, G=2, T=T, parity=vector_parity(D, plane, other), **kw)
+    rng = np.random.default_rng(seed)
+    host = np.full(tuple(fs.work.shape), np.nan, dtype=T)
+    own = (slice(None), slice(None)) + tuple(slice(2, 2 + quad.N) for _ in range(D))
+    host[own] = rng.uniform(-1, 1, size=host[own].shape).astype(T)
+    fs.work = torch.from_numpy(host)
+    s = GhostSchedule(fs, OPS4)
+    full, image, back = (unfolded_halfturn_forest if half else unfolded_forest)(quad)
+    ff = FieldSet(full, D + 1, G=2, T=T, parity=vector_parity(D, plane, other))
+    ff.work = torch.from_numpy(unfold_data(quad, fs, full, image, back, ff, q, half))
+    return quad, fs, s, full, ff, image
+
+
+SEAM_CASES = [(2, (1, 2), "none"), (2, (2, 1), "none"), (3, (1, 2), "periodic"),
+              (3, (2, 1), "reflect_lo"), (3, (3, 1), "outer")]
+HALF_CASES = [(2, (1, 2), "none"), (2, (2, 1), "none"), (3, (1, 2), "periodic"),
+              (3, (3, 2), "reflect_lo")]
+
+
+@pytest.mark.parametrize("D,plane,other", SEAM_CASES)
+def test_a_rotating_quadrant_is_the_turned_full_plane(D, plane, other):
+    """``test/rotate_tests.jl:437-456`` and ``:399-435``: every stored point
+    of the quadrant after the fill, ghosts included, is the full plane's at
+    the same place (the full plane holds the quadrant's data turned, and has
+    no seam), to 1e-13 as in the reference: a turned stencil that reads a
+    source's ghosts reads values the real frame summed in its own order.
+    Every ghost the schedule writes is defined, and every kind of transfer
+    crosses the seam."""
+    quad, fs, s, full, ff, image = quadrant_case(D, plane, other)
+    kinds = {(g.kind, g.orientation) for g in s.groups if g.orientation}
+    assert {k for k, _ in kinds} == {"copy", "restrict", "prolong"}
+    assert {r for _, r in kinds} >= {1, 3}
+    got = zero_hook_fill(s, fs)
+    want = zero_hook_fill(GhostSchedule(ff, OPS4), ff)
+    _agree(quad, full, image, got, want)
+    # every ghost is defined: no transfer read a ghost before it was written
+    assert not np.isnan(got).any()
+
+
+@pytest.mark.parametrize("D,plane,other", HALF_CASES)
+def test_a_half_plane_is_the_turned_full_plane(D, plane, other):
+    """``test/halfturn_tests.jl:349-377``."""
+    quad, fs, s, full, ff, image = quadrant_case(D, plane, other, half=True)
+    assert {g.orientation for g in s.groups} == {0, 2}
+    got = zero_hook_fill(s, fs)
+    want = zero_hook_fill(GhostSchedule(ff, OPS4), ff)
+    _agree(quad, full, image, got, want)
+    assert not np.isnan(got).any()
+
+
+def zero_hook_fill(s, fs):
+    """The oracle's fill with a hook that sets every outer-face region to
+    zero, in both frames alike."""
+    host = fs.work.numpy().copy()
+    oracle.fill(s, host, fs.nvars, fs.factors_host, rotvars=fs.rotvars_host, last=1)
+    for r in s.boundaries:
+        host[(r.block, slice(None)) + tuple(slice(a - 1, z) for a, z in reversed(r.region))] = 0
+    return oracle.fill(s, host, fs.nvars, fs.factors_host, rotvars=fs.rotvars_host, first=2)
+
+
+def _agree(quad, full, image, got, want, tol=1e-13):
+    findex = {k: i for i, k in enumerate(full.leaves)}
+    worst = 0.0
+    for b, k in enumerate(quad.leaves):
+        g, w = got[b], want[findex[image(k, 0)]]
+        assert np.array_equal(np.isnan(g), np.isnan(w)), (b, k)
+        ok = ~np.isnan(g)
+        worst = max(worst, float(np.max(np.abs(g[ok] - w[ok]), initial=0.0)))
+    assert worst < tol, worst
+
+
+@pytest.mark.parametrize("D,plane,other", SEAM_CASES[:3])
+def test_the_schedule_partitions_the_ghosts_across_the_seam(D, plane, other):
+    """``test/rotate_tests.jl:491-524``: every stored point outside the own
+    range is written exactly once, by a transfer or by the hook."""
+    quad, fs, s, *_ = quadrant_case(D, plane, other)
+    counts = s.write_counts()
+    N, G = quad.N, 2
+    inside = np.ones(counts.shape[1:], bool)
+    for ax in range(D):
+        sl = [slice(None)] * D
+        idx = np.arange(counts.shape[1 + ax])
+        mask = (idx >= G) & (idx < G + N)
+        shape = [1] * D
+        shape[ax] = -1
+        inside &= mask.reshape(shape)
+    assert (counts[:, inside] == 0).all() and (counts[:, ~inside] == 1).all()
+
+
+def test_seam_refusals():
+    """A rotation map is required, checked, and its tables composed
+    (``test/rotate_tests.jl:276-353``); a vertex-like set over a seam is
+    refused here; an asymmetric set is refused alone."""
+    f = Forest((2, 2), N=8, rotating=(1, 2))
+    with pytest.raises(ValueError, match="needs `rotation`"):
+        FieldSet(f, 3, G=1)
+    with pytest.raises(ValueError, match="one entry per variable"):
+        FieldSet(f, 3, G=1, rotation=(1, -3))
+    with pytest.raises(ValueError, match="not a signed permutation"):
+        FieldSet(f, 2, G=1, rotation=(1, 1))
+    with pytest.raises(ValueError, match="turned four times"):
+        FieldSet(f, 3, G=1, rotation=(2, 3, 1))
+    assert FieldSet(f, 3, G=1, rotation=(1, -3, 2)).rotation == [1, -3, 2]
+    assert FieldSet(Forest((2, 2), N=8), 1, G=1).rotvars is None
+    with pytest.raises(ValueError, match="vertex-like"):
+        GhostSchedule(FieldSet(f, 1, G=2, centering=("vertex", "vertex"), rotation=(1,)), OPS4)
+    h = Forest((1, 2), N=8, halfturn=(1, 2))
+    with pytest.raises(ValueError, match="needs `halfturn`"):
+        FieldSet(h, 1, G=1)
+    with pytest.raises(ValueError, match="applied twice"):
+        FieldSet(h, 2, G=1, halfturn=(2, -1))
+    fs = FieldSet(h, 3, G=1, halfturn=(1, -2, -3))
+    assert fs.rotvars_host[:, 2].tolist() == [1, 2, 3]
+    assert fs.factors_host[:, 2 * 9].tolist() == [1, -1, -1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [("q",) + c for c in SEAM_CASES] + [("h",) + c for c in HALF_CASES])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_turned_fill_bit_exact(cuda_lib, case, T):
+    """The device fill across a seam, fused (the CPU form of the sum) and
+    plain (the device form), is the oracle's bit for bit."""
+    from treeamr import fill_ghosts
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h", T=T)
+    host = fs.work.numpy().copy()
+    fs.factors, fs.rotvars = fs.factors.cuda(), fs.rotvars.cuda()
+    for method, one_tap in (("fused", True), ("plain", False)):
+        expect = oracle.fill(s, host.copy(), fs.nvars, fs.factors_host,
+                             rotvars=fs.rotvars_host, one_tap=one_tap)
+        fs.work = torch.from_numpy(host.copy()).cuda()
+        fill_ghosts(fs, s, method=method)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), method
+
+
+@pytest.mark.gpu
+def test_gpu_turned_fill_refusals(cuda_lib):
+    """Without the variable table the library refuses a turned schedule;
+    an asymmetric set is refused alone (``test/rotate_tests.jl:526-559``);
+    the adjoint of a turned schedule is not built."""
+    from treeamr import fill_ghosts
+    from treeamr.ghosts import device_schedule
+    quad, fs, s, *_ = quadrant_case(2, (1, 2), "none")
+    fs.work, fs.factors = fs.work.cuda(), fs.factors.cuda()
+    rv = fs.rotvars
+    fs.rotvars = None
+    with pytest.raises(ValueError, match="variable table"):
+        fill_ghosts(fs, s)
+    ds = device_schedule(s, 0)
+    rc = ds.lib.tam_fill(ds.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars, fs.nblocks(),
+                         C.c_void_p(fs.factors.data_ptr()), -1, 0x7FFFFFFF, None)
+    assert rc != 0
+    with pytest.raises(Exception, match="not built"):
+        ds.adjoint_scratch_bytes(fs.nvars)
+    fs.rotvars = rv
+    f = Forest((2, 2), N=8, rotating=(1, 2))
+    asym = FieldSet(f, 1, G=(1, 2), rotation=(1,), device="cuda")
+    with pytest.raises(ValueError, match="RotationPair"):
+        fill_ghosts(asym, GhostSchedule(asym, Operators(prolongation=2, restriction=2)))

@@ -75,6 +75,7 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_csingle);
   cudaFree(s->d_perm);
   cudaFree(s->d_err);
+  cudaFree(s->d_turns);
   tam::side_destroy(s->side);
   s->d_ptiles = nullptr;
   s->d_groups = nullptr;
@@ -85,6 +86,7 @@ void free_sched_device(tam_sched *s) {
   s->d_wtab = nullptr;
   s->d_csingle = s->d_perm = nullptr;
   s->d_err = nullptr;
+  s->d_turns = nullptr;
 }
 
 // Every check that makes a fill memory-safe: indices into the pools, block
@@ -114,6 +116,9 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
     return fail(ctx, TAM_EINVAL, "bad weight pool");
   int64_t maxcols = 1;
   for (int k = 0; k < d->ndim; ++k) maxcols *= 3;
+  if (d->nfactorcols != maxcols && d->nfactorcols != 4 * maxcols)
+    return fail(ctx, TAM_EINVAL, "nfactorcols must be 3^D, or 4 * 3^D over a seam");
+  maxcols = d->nfactorcols;
   for (int k = 0; k < d->ndim; ++k)
     if (d->stored[k] < 1) return fail(ctx, TAM_EINVAL, "stored extents must be positive");
   if (nsource < 0 || nsource > INT32_MAX) return fail(ctx, TAM_EINVAL, "bad source block count");
@@ -137,6 +142,33 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
       return fail(ctx, TAM_EINVAL, "group block range outside the block lists");
     if (g.stage < TAM_STAGE_SELFIMAGE || g.stage > 2 + 64)
       return fail(ctx, TAM_EINVAL, "bad stage tag");
+    if (g.orientation < 0 || g.orientation > 3)
+      return fail(ctx, TAM_EINVAL, "a group's orientation must be 0..3");
+    if (g.orientation == 0 && g.axes != 0)
+      return fail(ctx, TAM_EINVAL, "an ordinary group has the identity axis map (axes = 0)");
+    if (g.orientation != 0) {
+      // the axis map: a permutation of the dimensions that carries each real
+      // dimension onto a virtual one of the same stored extent, so that a
+      // virtual index inside the stored box reads a real one inside it
+      int seen = 0;
+      for (int e = 0; e < 3; ++e) {
+        const int p = (g.axes >> (2 * e)) & 3, f = (g.axes >> (8 + e)) & 1;
+        if (e >= d->ndim) {
+          if (p != 0 || f != 0)
+            return fail(ctx, TAM_EINVAL, "axis map entries beyond ndim must be zero");
+          continue;
+        }
+        if (p >= d->ndim || (seen >> p) & 1)
+          return fail(ctx, TAM_EINVAL, "a turned group's axis map is not a permutation");
+        seen |= 1 << p;
+        if (d->stored[p] != d->stored[e])
+          return fail(ctx, TAM_EINVAL,
+                      "a turned group exchanges dimensions of different stored extents: the "
+                      "layout must be symmetric in the seam's plane");
+      }
+      if ((g.axes & ~0x73F) != 0)
+        return fail(ctx, TAM_EINVAL, "stray bits in a turned group's axis map");
+    }
     for (int k = 0; k < d->ndim; ++k) {
       const tam_stencil &s = g.stencil[k];
       const int S = d->stored[k];
@@ -311,6 +343,7 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
     std::vector<Entry> entries;
     for (int32_t gi : st.groups) {
       const tam::DevGroup &g = s->groups[gi];
+      if (g.turned) continue;  // a turned group has a launch of its own
       for (int64_t t = 0; t < g.ntransfers; ++t)
         entries.push_back({s->h_tb[g.first + t], gi, (int32_t)(g.first + t)});
     }
@@ -333,6 +366,40 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
   return tiles;
+}
+
+// The turned groups of every stage (TurnGroup): the axis map folded into
+// signed strides of the real array.  Virtual stored index k (1-based) along
+// virtual dimension perm[e] reads real index k, or S_e + 1 - k where flip[e],
+// along e; with j = k - 1 the real offset is
+//   sum_e stride_e * (flip[e] ? S_e - 1 - j : j),
+// so vs[perm[e]] = +-stride_e and c0 = sum over flipped e of stride_e (S_e - 1).
+void build_turns(tam_sched *s) {
+  s->h_turns.clear();
+  const int64_t stride[3] = {1, s->S[0], (int64_t)s->S[0] * s->S[1]};
+  for (tam::Stage &st : s->stages) {
+    st.turn0 = (int64_t)s->h_turns.size();
+    for (int32_t gi : st.groups) {
+      const tam_group &h = s->host_groups[gi];
+      if (h.orientation == 0) continue;
+      tam::TurnGroup t{};
+      t.group = gi;
+      t.col = h.orientation;
+      t.odd = h.orientation & 1;
+      t.vs[0] = 1;
+      t.vs[1] = stride[1];
+      t.vs[2] = stride[2];
+      t.c0 = 0;
+      for (int e = 0; e < s->D; ++e) {
+        const int p = (h.axes >> (2 * e)) & 3;
+        const bool f = (h.axes >> (8 + e)) & 1;
+        t.vs[p] = f ? -stride[e] : stride[e];
+        if (f) t.c0 += stride[e] * (s->S[e] - 1);
+      }
+      s->h_turns.push_back(t);
+    }
+    st.nturn = (int64_t)s->h_turns.size() - st.turn0;
+  }
 }
 
 }  // namespace
@@ -461,6 +528,8 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
     g.pclass = unit ? 0 : (uniform && (p0 == 2 || p0 == 3 || p0 == 4 || p0 == 6)) ? p0 : -1;
     g.first = h.first;
     g.ntransfers = h.ntransfers;
+    g.turned = h.orientation;
+    if (h.orientation != 0) s->needs_rotvars = true;
     if (h.factorcol != 0) s->needs_factors = true;
     s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
     // the division-free box decomposition
@@ -522,9 +591,11 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
   s->h_srcstart.assign(d->srcstart, d->srcstart + d->nsrcstart);
   std::vector<tam::Tile> tiles = build_tiles(s);
   std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
+  build_turns(s);
 
   cudaError_t e;
   if ((e = tam::side_create(s->side)) != cudaSuccess ||
+      (e = upload(&s->d_turns, s->h_turns.data(), s->h_turns.size())) != cudaSuccess ||
       (e = upload(&s->d_ptiles, ptiles.data(), ptiles.size())) != cudaSuccess ||
       (e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
       (e = upload(&s->d_tb, d->targetblocks, (size_t)d->ntransfers)) != cudaSuccess ||
@@ -564,6 +635,9 @@ void tam_schedule_free(tam_sched *s) {
 
 static int adjoint_ready(tam_sched *s) {
   if (s->adj.ready) return TAM_OK;
+  if (s->needs_rotvars)
+    return fail(s->ctx, TAM_EUNSUPPORTED,
+                "the adjoint of a schedule with transfers turned across a seam is not built");
   std::string err;
   int rc = tam::adjoint_prepare(s, err);
   if (rc != TAM_OK) return fail(s->ctx, rc, err);
@@ -652,18 +726,48 @@ static int check_fill_args(tam_sched *s, void *work, int32_t nvars, int64_t nblo
 
 int tam_fill(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
              int32_t first_stage, int32_t last_stage, void *stream) {
+  return tam_fill_ex(s, work, nullptr, nvars, nblocks, factors, nullptr, first_stage,
+                     last_stage, TAM_METHOD_FUSED, stream);
+}
+
+int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, int64_t nblocks,
+                const void *factors, const int32_t *rotvars, int32_t first_stage,
+                int32_t last_stage, int32_t method, void *stream) {
   int rc = check_fill_args(s, work, nvars, nblocks, factors);
   if (rc != TAM_OK) return rc;
+  if (method != TAM_METHOD_FUSED && method != TAM_METHOD_PLAIN)
+    return fail(s->ctx, TAM_EINVAL, "method must be TAM_METHOD_FUSED or TAM_METHOD_PLAIN");
+  if (s->needs_rotvars && !rotvars)
+    return fail(s->ctx, TAM_EINVAL,
+                "this schedule turns ghosts across a rotating seam, but no variable table was "
+                "given to turn them with (src/ghosts.jl:431-434)");
   DeviceGuard guard(s->ctx->device);
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
   cudaStream_t st = (cudaStream_t)stream;
+  tam::SchedArgs args = sched_args(s);
+  if (method == TAM_METHOD_PLAIN) args.one_tap = 0;  // the device form
   for (const tam::Stage &stage : s->stages) {
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
-    cudaError_t e = tam::launch_fused_stage(
-        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
-        stage.nptiles,
-        sched_args(s), work, factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr);
-    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
+    cudaError_t e = cudaSuccess;
+    if (method == TAM_METHOD_FUSED) {
+      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0,
+                                  stage.npcopy0, stage.npcopy, stage.nptiles, args, work,
+                                  factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr);
+      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
+    } else {
+      for (int32_t gi : stage.groups) {
+        if (s->groups[gi].turned) continue;
+        e = tam::launch_plain_group(s->dtype, s->D, s->groups[gi], s->d_groups + gi, args,
+                                    work, factors, nvars, s->S, st);
+        if (e != cudaSuccess) return cuda_fail(s->ctx, e, "plain group launch");
+      }
+    }
+    if (stage.nturn > 0) {
+      e = tam::launch_turned(s->dtype, s->D, s->d_turns + stage.turn0, stage.nturn, args, work,
+                             alt_work ? alt_work : work, work, factors, rotvars, nvars, s->S,
+                             s->d_err, st);
+      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "turned group launch");
+    }
   }
   return TAM_OK;
 }
@@ -697,8 +801,8 @@ int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
   if (new_nblocks != s->nblocks || old_nblocks != s->nsource)
     return fail(s->ctx, TAM_ELAYOUT,
                 "tam_regrid_transfer: the block counts differ from the transfer's");
-  if (s->needs_factors)
-    return fail(s->ctx, TAM_EUNSUPPORTED, "a regrid transfer takes no factor column");
+  if (s->needs_factors || s->needs_rotvars)
+    return fail(s->ctx, TAM_EUNSUPPORTED, "a regrid transfer takes no factor column and no turn");
   if (old_work == new_work)
     return fail(s->ctx, TAM_EINVAL, "tam_regrid_transfer: the old and new arrays must differ");
   DeviceGuard guard(s->ctx->device);
@@ -716,20 +820,8 @@ int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
 
 int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
                    int32_t first_stage, int32_t last_stage, void *stream) {
-  int rc = check_fill_args(s, work, nvars, nblocks, factors);
-  if (rc != TAM_OK) return rc;
-  DeviceGuard guard(s->ctx->device);
-  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
-  cudaStream_t st = (cudaStream_t)stream;
-  for (const tam::Stage &stage : s->stages) {
-    if (stage.tag < first_stage || stage.tag > last_stage) continue;
-    for (int32_t gi : stage.groups) {
-      cudaError_t e = tam::launch_plain_group(s->dtype, s->D, s->groups[gi], s->d_groups + gi,
-                                              sched_args(s), work, factors, nvars, s->S, st);
-      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "plain group launch");
-    }
-  }
-  return TAM_OK;
+  return tam_fill_ex(s, work, nullptr, nvars, nblocks, factors, nullptr, first_stage,
+                     last_stage, TAM_METHOD_PLAIN, stream);
 }
 
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {

@@ -38,7 +38,7 @@ struct DevGroup {
   int64_t cls[3];    // class-index pool offsets (one int32 per target row)
   int64_t wtab;      // product-table pool offset
   int32_t member;    // the forest of a batch this group belongs to (0 alone)
-  int32_t pad3;
+  int32_t turned;    // the orientation of a group across a seam (0: none)
   // The one-tap skip of the reference's CPU fill (src/ghosts.jl:28-56): per
   // dimension, for each column class, the row of its only nonzero weight, or
   // -1 (int32 pool entries at csingle[d] + class).  `perm` (or -1) orders the
@@ -55,6 +55,19 @@ struct DevGroup {
   int32_t affine;
   int32_t cs0[3];
   int32_t cstep[3];
+};
+
+// A turned group (across a seam) as its launch reads it: the real source's
+// offset of virtual 0-based stored indices j is c0 + sum_d vs[d] * j[d]
+// (the axis map folded into signed strides of the real array), and target
+// variable v reads real variable rotvars[v + nvars * col] - 1.
+struct TurnGroup {
+  int32_t group;    // index into the schedule's groups
+  int32_t col;      // the orientation r: the rotvars column
+  int32_t odd;      // reads the alternate array
+  int32_t pad;
+  int64_t vs[3];
+  int64_t c0;
 };
 
 // One forest of a batch (tam_batch_fill): where its field data and factor
@@ -124,6 +137,8 @@ struct Stage {
   int64_t npcopy0 = 0;          // packed tiles of the copies without a factor, of
   int64_t npcopy = 0;           // all the copies, then
   int64_t nptiles = 0;          // all packed tiles of the stage
+  int64_t turn0 = 0;            // the stage's turned groups: turns[turn0 .. turn0 + nturn)
+  int64_t nturn = 0;
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -196,6 +211,8 @@ struct tam_sched {
   int64_t nsource = 0;        // source blocks: nblocks, or a regrid's old count
   int32_t nfactorcols = 0;
   bool needs_factors = false;
+  bool needs_rotvars = false;   // a turned group reads the variable table
+  std::vector<tam::TurnGroup> h_turns;
   std::vector<tam_group> host_groups;
   std::vector<int32_t> h_tb;  // target blocks, for re-tiling
   std::vector<int32_t> h_sb;  // source blocks, for the adjoint's lists
@@ -224,6 +241,7 @@ struct tam_sched {
   int32_t *d_perm = nullptr;
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
+  tam::TurnGroup *d_turns = nullptr;
   tam::SideStream side;
   int32_t *d_err = nullptr;
   // the adjoint, prepared on first use (tam_adjoint.cu)
@@ -265,6 +283,15 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side, const void *src);
+
+// The turned groups turns[0 .. n) of one stage: a flat launch per group
+// (blockIdx.y), reading `src` for an even orientation and `alt` for an odd
+// one, target variable v from real variable rotvars[v + nvars * r] - 1
+// (an entry outside 1:nvars skips the item and records TAM_EINVAL in *err).
+cudaError_t launch_turned(int dtype, int D, const TurnGroup *turns, int64_t n,
+                          const SchedArgs &a, const void *src, const void *alt, void *work,
+                          const void *factors, const int32_t *rotvars, int nvars,
+                          const int S[3], int32_t *err, cudaStream_t stream);
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);

@@ -832,6 +832,131 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                S, threads, stream, side);
 }
 
+// ---- turned groups: across a rotating or half-turn seam -----------------------
+// One item = (box point, variable, transfer) of turned group blockIdx.y, read
+// through the group's axis map (RotatedSource, src/ghosts.jl:183-244) folded
+// into signed strides: the virtual source window's points are the real
+// source's at c0 + sum_d vs[d] * j[d], variable rotvars[v + nvars * r] - 1.
+// The sum is stencil_sum's (src/ghosts.jl:75-118): m_1 innermost, the
+// weight product ((w_1*w_2)*w_3), acc from +0, no FMA, and with `one_tap` a
+// dimension whose weight column has a single nonzero weight takes only that
+// tap (src/ghosts.jl:28-56); a copy is +0 + x and a factor x*f + 0.
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+    turned_group_kernel(const TurnGroup *__restrict__ turns, Args<T> a, const T *src,
+                        const T *alt, T *work, const T *__restrict__ factors,
+                        const int32_t *__restrict__ rotvars, int nvars, int S1, int S2, int S3,
+                        int32_t *err) {
+  using A = Arith<T>;
+  const TurnGroup tg = turns[blockIdx.y];
+  const DevGroup &g = a.groups[tg.group];
+  const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
+  const int64_t items = box * nvars * g.ntransfers;
+  const int64_t vol = (int64_t)S1 * S2 * S3;
+  const T *from = tg.odd ? alt : src;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = it;
+    const int i1 = (int)(r % g.n[0]);
+    r /= g.n[0];
+    const int i2 = (int)(r % g.n[1]);
+    r /= g.n[1];
+    const int i3 = (int)(r % g.n[2]);
+    r /= g.n[2];
+    const int v = (int)(r % nvars);
+    const int64_t t = r / nvars + g.first;
+    const int64_t tblock = __ldg(a.tb + t) - 1;
+    const int64_t sblock = __ldg(a.sb + t) - 1;
+    const int sv = __ldg(rotvars + v + (int64_t)nvars * tg.col) - 1;
+    if (sv < 0 || sv >= nvars) {  // a variable table naming no variable: skip, and say so
+      atomicExch(err, (int32_t)TAM_EINVAL);
+      continue;
+    }
+    const T *sp = from + (sblock * nvars + sv) * vol + tg.c0;
+    const int idx[3] = {i1, i2, i3};
+    int64_t j[3];
+    int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    const T *wc[3];
+    for (int k = 0; k < 3; ++k) {
+      j[k] = __ldg(a.srcstart + g.ss[k] + idx[k]) - 1;
+      wc[k] = a.weights + g.w[k] + (int64_t)g.order[k] * idx[k];
+      hi[k] = g.order[k];
+      if (a.one_tap && k < D) {
+        int nonzero = 0, row = 0;
+        for (int m = 0; m < g.order[k]; ++m)
+          if (wc[k][m] != T(0)) {
+            ++nonzero;
+            row = m;
+          }
+        if (nonzero == 1) {
+          lo[k] = row;
+          hi[k] = row + 1;
+        }
+      }
+    }
+    T x;
+    if (g.unit) {
+      x = A::add(T(0), sp[tg.vs[0] * j[0] + tg.vs[1] * j[1] + tg.vs[2] * j[2]]);
+    } else {
+      T acc = T(0);
+      for (int m3 = lo[2]; m3 < hi[2]; ++m3)
+        for (int m2 = lo[1]; m2 < hi[1]; ++m2)
+          for (int m1 = lo[0]; m1 < hi[0]; ++m1) {
+            T w = wc[0][m1];
+            if (D >= 2) w = A::mul(w, wc[1][m2]);
+            if (D >= 3) w = A::mul(w, wc[2][m3]);
+            const T u = sp[tg.vs[0] * (j[0] + m1) + tg.vs[1] * (j[1] + m2) +
+                           tg.vs[2] * (j[2] + m3)];
+            acc = A::add(acc, A::mul(w, u));
+          }
+      x = acc;
+    }
+    const int64_t toff = (tblock * nvars + v) * vol +
+                         ((int64_t)(g.tf[2] + i3) * S2 + (g.tf[1] + i2)) * S1 + g.tf[0] + i1;
+    work[toff] = scaled(x, factors, v, nvars, g.factorcol);
+  }
+}
+
+template <typename T>
+cudaError_t turned_dispatch(int D, const TurnGroup *turns, int64_t n, const Args<T> &a,
+                            const T *src, const T *alt, T *work, const T *factors,
+                            const int32_t *rotvars, int nvars, const int S[3], int32_t *err,
+                            cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  // items of the largest turned group are not known here: a grid-stride
+  // loop over a fixed x extent per group
+  const dim3 grid(64, (unsigned)n), block(256);
+  switch (D) {
+    case 1:
+      turned_group_kernel<T, 1><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+                                                             rotvars, nvars, S[0], S[1], S[2], err);
+      break;
+    case 2:
+      turned_group_kernel<T, 2><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+                                                             rotvars, nvars, S[0], S[1], S[2], err);
+      break;
+    default:
+      turned_group_kernel<T, 3><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+                                                             rotvars, nvars, S[0], S[1], S[2], err);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_turned(int dtype, int D, const TurnGroup *turns, int64_t n,
+                          const SchedArgs &a, const void *src, const void *alt, void *work,
+                          const void *factors, const int32_t *rotvars, int nvars,
+                          const int S[3], int32_t *err, cudaStream_t stream) {
+  if (!alt) alt = src;
+  if (dtype == TAM_F64)
+    return turned_dispatch<double>(D, turns, n, typed<double>(a), (const double *)src,
+                                   (const double *)alt, (double *)work, (const double *)factors,
+                                   rotvars, nvars, S, err, stream);
+  return turned_dispatch<float>(D, turns, n, typed<float>(a), (const float *)src,
+                                (const float *)alt, (float *)work, (const float *)factors,
+                                rotvars, nvars, S, err, stream);
+}
+
 void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
                 std::vector<PTile> &out) {
   int64_t i = begin;

@@ -24,9 +24,10 @@ INCLUDE_DIR = os.path.join(ROOT_DIR, "include")
 BUILD_DIR = os.path.join(CSRC_DIR, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libtreeamr_cuda.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 TAM_F32, TAM_F64 = 1, 2
 TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
+TAM_METHOD_FUSED, TAM_METHOD_PLAIN = 0, 1
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -41,7 +42,8 @@ class tam_stencil(C.Structure):
 
 class tam_group(C.Structure):
     _fields_ = [("kind", C.c_int32), ("stage", C.c_int32), ("factorcol", C.c_int32),
-                ("bounded", C.c_int32), ("first", C.c_int64), ("ntransfers", C.c_int64),
+                ("bounded", C.c_int32), ("orientation", C.c_int32), ("axes", C.c_int32),
+                ("first", C.c_int64), ("ntransfers", C.c_int64),
                 ("stencil", tam_stencil * 3)]
 
 
@@ -102,6 +104,11 @@ class Descriptor:
             cg.stage = g.stage
             cg.factorcol = g.factorcol
             cg.bounded = 0
+            cg.orientation = getattr(g, "orientation", 0)
+            cg.axes = 0
+            if cg.orientation:
+                for e, (p, f) in enumerate(zip(g.perm, g.flip)):
+                    cg.axes |= (int(p) << (2 * e)) | (int(bool(f)) << (8 + e))
             cg.first = ntr
             cg.ntransfers = g.ntransfers()
             tb_list.append(g.targetblocks)
@@ -140,7 +147,8 @@ class Descriptor:
             d.stored[k] = schedule.stored[k] if k < D else 1
         d.nblocks = schedule.forest.nleaves()
         d.ngroups = len(groups)
-        d.nfactorcols = 3 ** D
+        seam = getattr(schedule.forest, "hasrotating", None)
+        d.nfactorcols = 3 ** D * (4 if seam is not None and seam() else 1)
         d.groups = C.cast(self.groups_arr, C.POINTER(tam_group))
         d.ntransfers = ntr
         d.targetblocks = _ptr(self.targetblocks, C.c_int32)
@@ -230,6 +238,8 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_fill_ex.argtypes = [vp, vp, vp, i32, i64, vp, vp, i32, i32, i32, vp]
+    lib.tam_fill_ex.restype = C.c_int
     lib.tam_regrid_upload.argtypes = [vp, C.POINTER(tam_schedule_desc), i64, C.POINTER(vp)]
     lib.tam_regrid_upload.restype = C.c_int
     lib.tam_regrid_transfer.argtypes = [vp, vp, i64, vp, i64, i32, vp]

@@ -51,9 +51,22 @@ class DeviceSchedule:
             self.handle = None
 
     def run(self, fs: FieldSet, first: int, last: int, method: str = "fused",
-            stream: Optional[torch.cuda.Stream] = None):
-        fn = {"fused": self.lib.tam_fill, "plain": self.lib.tam_fill_plain}[method]
+            stream: Optional[torch.cuda.Stream] = None, alt: Optional[torch.Tensor] = None):
         s = stream if stream is not None else torch.cuda.current_stream(fs.work.device)
+        rotvars = getattr(fs, "rotvars", None)
+        if rotvars is not None or alt is not None:
+            # turned transfers across a seam read the variable table, and an
+            # odd orientation the alternate array (tam_fill_ex)
+            rc = self.lib.tam_fill_ex(
+                self.handle, C.c_void_p(fs.work.data_ptr()),
+                C.c_void_p(alt.data_ptr() if alt is not None else 0), fs.nvars, fs.nblocks(),
+                C.c_void_p(fs.factors.data_ptr()),
+                C.c_void_p(rotvars.data_ptr() if rotvars is not None else 0), first, last,
+                _native.TAM_METHOD_PLAIN if method == "plain" else _native.TAM_METHOD_FUSED,
+                C.c_void_p(s.cuda_stream))
+            _native.check(rc, self.ctx, f"tam_fill_ex ({method})")
+            return
+        fn = {"fused": self.lib.tam_fill, "plain": self.lib.tam_fill_plain}[method]
         rc = fn(self.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars, fs.nblocks(),
                 C.c_void_p(fs.factors.data_ptr()), first, last, C.c_void_p(s.cuda_stream))
         _native.check(rc, self.ctx, f"tam_fill ({method})")
@@ -136,6 +149,18 @@ def check_fill(fs: FieldSet, schedule: GhostSchedule):
                          "the field set's; build the schedule from this field set")
     if fs.work.device.type != "cuda":
         raise ValueError("fill_ghosts runs on the GPU: the field set must live on a CUDA device")
+    if getattr(schedule, "odd_turns", False):
+        from .storage import symmetric_layout
+        if not symmetric_layout(fs.forest, fs.G, fs.c):
+            raise ValueError(
+                "this field set's layout is not symmetric in the rotating seam's dimensions "
+                f"{fs.forest.rotating_dims()} (G = {fs.G}, centering {fs.centering}), so its "
+                "ghosts across the seam are its partner's data, turned: fill it together with "
+                "the set of the swapped layout as a RotationPair (src/ghosts.jl:1960-1980)")
+    if getattr(schedule, "turned", False) and fs.rotvars is None:
+        raise ValueError("this schedule turns ghosts across a seam, but the field set has no "
+                         "variable table to turn them with: build it over the same forest, "
+                         "with `rotation` (or `halfturn`)")
 
 
 def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Callable] = None,

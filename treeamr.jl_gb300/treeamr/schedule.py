@@ -27,7 +27,8 @@ from typing import Dict, List, NamedTuple, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .forest import Forest, MortonKey, OUTER, OUTFLOW, REFLECTING, alldirections, childoffset
+from .forest import (Forest, MortonKey, OUTER, OUTFLOW, REFLECTING, alldirections, axismap,
+                     childoffset, virtual_offset)
 from .operators import (Conservative, Operators, check_operators, conservative_prolong_weights,
                         interpolation_weights, round_weights)
 from .storage import FieldSet, ghostwidths, mirrorcolumn, staggers, storedsize
@@ -82,19 +83,21 @@ class Stencil1D:
 
 class GroupKey(NamedTuple):
     """What a ghost region needs: kind, direction, child offset, target level
-    (prolongations only), and the mirror state per dimension
-    (``src/schedule.jl:400-410``; no seam orientation or glue here)."""
+    (prolongations only), the mirror state per dimension, and the orientation
+    of a transfer across a rotating or half-turn seam
+    (``src/schedule.jl:400-410``; no glue here)."""
     kind: str
     direction: Tuple[int, ...]
     offset: Tuple[int, ...]
     level: int
     mirror: Tuple[int, ...]
     span: Tuple[int, ...]
+    orientation: int = 0     # quarter turns across a seam (0 off it)
 
     def order(self):
         """``keyorder`` (``src/schedule.jl:495-497``)."""
         return (KINDRANK[self.kind], self.direction, self.offset, self.level, self.mirror,
-                0, 0, self.span)
+                self.orientation, 0, self.span)
 
 
 def isunify(key: GroupKey) -> bool:
@@ -113,9 +116,17 @@ class TransferGroup:
     block pairs (1-based block indices, targets non-decreasing)."""
 
     def __init__(self, key: GroupKey, stencils, targetblocks, sourceblocks, factorcol: int,
-                 stage: int):
+                 stage: int, axes=None):
         self.key = key
         self.kind = key.kind
+        # A turned group (across a seam) reads its real source through the
+        # axis map ``(perm, flip)`` in gather form (0-based dimensions) and
+        # the variable table's column ``orientation`` (``src/ghosts.jl:183-244``).
+        self.orientation = int(key.orientation)
+        D = len(key.direction)
+        self.perm, self.flip = axes if axes is not None else \
+            (tuple(range(D)), (False,) * D)
+        self.turned = self.orientation != 0
         self.stencils = tuple(stencils)
         self.targetblocks = np.asarray(targetblocks, dtype=np.int32)
         self.sourceblocks = np.asarray(sourceblocks, dtype=np.int32)
@@ -383,8 +394,8 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
     if closed and table is None:
         table = NeighbourTable(forest, b)
 
-    def record(kind, offset, lvl, s, delta, span=nospan):
-        _record(pairs, GroupKey(kind, tuple(delta), offset, lvl, nomirror, span), b, s)
+    def record(kind, offset, lvl, s, delta, span=nospan, turns=0):
+        _record(pairs, GroupKey(kind, tuple(delta), offset, lvl, nomirror, span, turns), b, s)
 
     for delta in dirs:
         region = [target_range(N, G[d], c[d], delta[d], 0, False) for d in range(D)]
@@ -394,7 +405,7 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
         if any(f != OUTER for f in faces):
             mirror_sources(pairs, boundaries, forest, G, c, b, delta, dprime, faces, region)
             continue
-        nbrs = forest.oriented_neighbors(k, delta)
+        r, nbrs = forest.turned_neighbors(k, delta)
         if table is not None:
             table.remember(delta, nbrs)
         if not nbrs:
@@ -402,12 +413,12 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
             continue
         nbl = nbrs[0].level
         if nbl == k.level:
-            record(COPY, zero, 0, forest.find_leaf(nbrs[0]), delta)
+            record(COPY, zero, 0, forest.find_leaf(nbrs[0]), delta, turns=r)
         elif nbl < k.level:
             src = forest.find_leaf(nbrs[0])
             parts = ghost_plane_parts(forest, k, delta, delta, c, src) if closed else None
             if parts is None:
-                record(PROLONG, childoffset(k), k.level, src, delta)
+                record(PROLONG, childoffset(k), k.level, src, delta, turns=r)
             else:
                 for kind, dirn, span, s in parts:
                     if kind == PROLONG:
@@ -415,11 +426,21 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
                     else:
                         record(COPY, zero, 0, s, dirn, span)
         else:
+            # each finer neighbour by its offset in its virtual parent,
+            # where this block sees it across a seam
             for nbr in nbrs:
-                record(RESTRICT, childoffset(nbr), 0, forest.find_leaf(nbr), delta)
+                record(RESTRICT, seam_offset(forest, nbr, r), 0, forest.find_leaf(nbr), delta,
+                       turns=r)
     if closed:
         return unify_sources(pairs, forest, c, b, table)
     return 0
+
+
+def seam_offset(forest: Forest, nbr: MortonKey, r: int) -> Tuple[int, ...]:
+    """A finer neighbour's child offset in the virtual frame
+    (``src/schedule.jl:1411-1420``)."""
+    o = childoffset(nbr)
+    return virtual_offset(o, r, *forest.seam_plane()) if r else o
 
 
 def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, walls, region):
@@ -433,24 +454,26 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
     nospan = _nospan(D)
     closed = any(cd == 1 for cd in c)
 
-    def record(kind, offset, lvl, s, dirn=tuple(delta), span=nospan):
-        _record(pairs, GroupKey(kind, tuple(dirn), offset, lvl, state, span), b, s)
+    def record(kind, offset, lvl, s, dirn=tuple(delta), span=nospan, turns=0):
+        _record(pairs, GroupKey(kind, tuple(dirn), offset, lvl, state, span, turns), b, s)
 
     if dprime == zero:
         record(COPY, zero, 0, b)
         return
-    nbrs = forest.oriented_neighbors(k, dprime)
+    # dprime may still cross a seam, the mirror being outside its plane:
+    # the two compose, the source turned and then mirrored
+    r, nbrs = forest.turned_neighbors(k, dprime)
     if not nbrs:
         boundaries.append(boundary_region(forest, k, b, delta, region, G, c))
         return
     nbl = nbrs[0].level
     if nbl == k.level:
-        record(COPY, zero, 0, forest.find_leaf(nbrs[0]))
+        record(COPY, zero, 0, forest.find_leaf(nbrs[0]), turns=r)
     elif nbl < k.level:
         src = forest.find_leaf(nbrs[0])
         parts = ghost_plane_parts(forest, k, tuple(delta), dprime, c, src) if closed else None
         if parts is None:
-            record(PROLONG, childoffset(k), k.level, src)
+            record(PROLONG, childoffset(k), k.level, src, turns=r)
         else:
             for kind, dirn, span, s in parts:
                 if kind == PROLONG:
@@ -460,9 +483,9 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
     else:
         wallside = [0 if delta[d] < 0 else 1 for d in range(D)]
         for nbr in nbrs:
-            o = childoffset(nbr)
+            o = seam_offset(forest, nbr, r)
             if all((not mask[d]) or o[d] == wallside[d] for d in range(D)):
-                record(RESTRICT, o, 0, forest.find_leaf(nbr))
+                record(RESTRICT, o, 0, forest.find_leaf(nbr), turns=r)
 
 
 # --- closed blocks: the primary of a shared point (vertex-like layouts) ---
@@ -880,6 +903,11 @@ class GhostSchedule:
         self.parities = parity
         self.stored = tuple(N + 2 * g + cd for g, cd in zip(G, c))
         closed = any(cd == 1 for cd in c)
+        if closed and forest.hasrotating():
+            raise ValueError("a set with a vertex-like dimension over a forest with a rotating "
+                             "or half-turn seam is not built here: its seam planes are copies "
+                             "of one another through the turn, which needs stage 0 across the "
+                             "seam and the axis projection; use a cell-centred set")
 
         dirs = alldirections(D)
         pairs: Dict[GroupKey, Tuple[List[int], List[int]]] = {}
@@ -922,19 +950,29 @@ class GhostSchedule:
             return built[key]
 
         def factorcol(key):
+            # the mirror state and the orientation: mirror column + 3^D r
+            # (src/schedule.jl:3218-3229)
             signs = tuple(0 if m == 3 else m for m in key.mirror)
-            return mirrorcolumn(signs) if any(signs) else 0
+            return mirrorcolumn(signs) + 3 ** D * key.orientation \
+                if any(signs) or key.orientation else 0
+
+        def axesof(key):
+            if key.orientation:
+                return axismap(key.orientation, *forest.seam_plane(), D)
+            return None
 
         groups = []
         for key in sorted(pairs, key=GroupKey.order):
             tb, sb = pairs[key]
             groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
-                                        transfer_stage(key)))
+                                        transfer_stage(key), axesof(key)))
         for key in sorted(ppairs, key=GroupKey.order):
             tb, sb = ppairs[key]
             groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
                                         SELFIMAGE_TAG))
         self.groups = groups
+        self.turned = any(g.turned for g in groups)
+        self.odd_turns = any(g.orientation % 2 for g in groups)
         self.selfimage = [g for g in groups if g.stage == SELFIMAGE_TAG]
         self.unify = [g for g in groups if g.stage == UNIFY_TAG]
         self.phase1 = [g for g in groups if g.stage == PHASE1_TAG]

@@ -13,7 +13,7 @@ Restates ``src/storage.jl``:
 """
 from __future__ import annotations
 
-from typing import Callable, Optional, Sequence, Tuple
+from typing import Callable, List, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -93,6 +93,138 @@ def mirrorcolumn(state: Sequence[int]) -> int:
     return 1 + sum(int(s) * 3 ** d for d, s in enumerate(state))
 
 
+# --- seams: the rotation tables (src/storage.jl:557-760) -----------------------
+
+def signed_map(m, nvars: int, name: str, turn: str) -> List[int]:
+    """A signed variable map checked for its shape: one nonzero integer per
+    variable, naming every variable once (``src/storage.jl:632-652``)."""
+    if not isinstance(m, (list, tuple)):
+        raise ValueError(f"{name} must be a vector or tuple with one signed variable index per "
+                         f"variable, got a {type(m).__name__}")
+    if len(m) != nvars:
+        raise ValueError(f"{name} must have one entry per variable: got {len(m)} for "
+                         f"nvars = {nvars}")
+    q = []
+    for x in m:
+        if isinstance(x, bool) or not isinstance(x, (int, np.integer)):
+            raise ValueError(f"each {name} entry must be a nonzero integer, a signed variable "
+                             f"index; got {x!r}")
+        q.append(int(x))
+    if sorted(abs(x) for x in q) != list(range(1, nvars + 1)):
+        raise ValueError(f"{name} = {tuple(q)} is not a signed permutation of 1:{nvars}: {turn} "
+                         "sends each variable to plus or minus exactly one variable")
+    return q
+
+
+def composed_rotation(steps, nvars: int):
+    """After the steps, target variable ``v`` reads variable ``sigma[v]`` of
+    the set the last step reads from, times ``sign[v]`` (1-based variables;
+    ``src/storage.jl:684-694``)."""
+    sigma = list(range(1, nvars + 1))
+    sign = [1] * nvars
+    for q in steps:
+        for v in range(nvars):
+            x = q[sigma[v] - 1]
+            sign[v] *= 1 if x > 0 else -1
+            sigma[v] = abs(x)
+    return sigma, sign
+
+
+def symmetric_layout(forest: Forest, G, c) -> bool:
+    """Whether the layout turns into itself: always under a half turn, and
+    under a quarter turn with equal ghost widths and staggers in the seam's
+    plane (``src/storage.jl:571-575``)."""
+    if forest.ishalfturn():
+        return True
+    d1, d2 = forest.seam_plane()
+    return G[d1] == G[d2] and c[d1] == c[d2]
+
+
+def _check_rotation_parity(forest: Forest, parities, q, what: str):
+    if parities is None:
+        return
+    for v in range(len(q)):
+        w = abs(q[v]) - 1
+        for d in range(forest.D):
+            if REFLECTING not in forest.faces[d]:
+                continue
+            if parities[v][d] != parities[w][d]:
+                raise ValueError(f"{what} sends variable {v + 1} to variable {w + 1}, but in "
+                                 f"dimension {d + 1}, which has a reflecting face, the first has "
+                                 f"{parities[v][d]} and the second {parities[w][d]}: a variable "
+                                 "and its image under the turn must have the same parity there")
+
+
+def rotations_of(rotation, forest: Forest, nvars: int, G, c, parities):
+    """``src/storage.jl:592-628``."""
+    quarter = forest.rotating_dims() is not None
+    if rotation is None:
+        if quarter:
+            raise ValueError(f"this forest has a rotating seam, rotating = "
+                             f"{forest.rotating_dims()}, so the field set needs `rotation`: one "
+                             "signed variable index per variable, saying which variable, and "
+                             "with which sign, each one equals a quarter turn away")
+        return None
+    q = signed_map(rotation, nvars, "rotation", "a quarter turn")
+    if not quarter:
+        return q
+    if symmetric_layout(forest, G, c):
+        sigma, sign = composed_rotation((q, q, q, q), nvars)
+        if sigma != list(range(1, nvars + 1)) or any(x != 1 for x in sign):
+            raise ValueError(f"rotation = {tuple(q)} turned four times is not the identity: "
+                             "four quarter turns are no turn at all")
+        _check_rotation_parity(forest, parities, q, "rotation")
+    return q
+
+
+def halfturns_of(halfturn, forest: Forest, nvars: int, parities):
+    """``src/storage.jl:658-677``."""
+    if halfturn is None:
+        if forest.ishalfturn():
+            raise ValueError(f"this forest has a half-turn seam, halfturn = "
+                             f"{forest.halfturn_dims()}, so the field set needs `halfturn`: one "
+                             "signed variable index per variable")
+        return None
+    q = signed_map(halfturn, nvars, "halfturn", "a half turn")
+    if not forest.ishalfturn():
+        return q
+    sigma, sign = composed_rotation((q, q), nvars)
+    if sigma != list(range(1, nvars + 1)) or any(x != 1 for x in sign):
+        raise ValueError(f"halfturn = {tuple(q)} applied twice is not the identity: two half "
+                         "turns are no turn at all")
+    _check_rotation_parity(forest, parities, q, "halfturn")
+    return q
+
+
+def seamtables(dtype, parities, steps, nvars: int, D: int, half=None):
+    """``(factors, rotvars)`` of the turned transfers (``src/storage.jl:
+    717-740``): ``rotvars[v, r]`` (1-based variables) is the variable
+    ``Q^r`` reads for target ``v``, and the factor at column ``mirror column
+    + 3^D r`` the target variable's parity factor for that mirror state
+    times the sign of ``Q^r``.  ``steps`` is the set's own map three times
+    for a symmetric layout, ``None`` for an asymmetric one (zero factors
+    and the identity for ``r >= 1``); ``half`` the half turn's own map,
+    orientation 2."""
+    nstates = 3 ** D
+    factors = np.empty((nvars, 4 * nstates), dtype=dtype)
+    rotvars = np.empty((nvars, 4), dtype=np.int32)
+    for r in range(4):
+        if r == 0:
+            sigma, sign = list(range(1, nvars + 1)), [1] * nvars
+        elif half is not None and r == 2:
+            sigma, sign = composed_rotation((half,), nvars)
+        elif steps is None or half is not None:
+            sigma, sign = list(range(1, nvars + 1)), [0] * nvars
+        else:
+            sigma, sign = composed_rotation(steps[:r], nvars)
+        rotvars[:, r] = sigma
+        par = parityfactors(dtype, parities, D)
+        for v in range(nvars):
+            for col in range(nstates):
+                factors[v, col + nstates * r] = dtype.type(int(par[v, col]) * sign[v])
+    return factors, rotvars
+
+
 def check_parity(forest: Forest, nvars: int, parity):
     D = forest.D
     anyreflect = any(REFLECTING in forest.faces[d] for d in range(D))
@@ -122,7 +254,7 @@ class FieldSet:
     """Block storage for ``nvars`` variables over every leaf of ``forest``."""
 
     def __init__(self, forest: Forest, nvars: int, *, G, centering=None, T=np.float64,
-                 parity=None, device="cpu"):
+                 parity=None, rotation=None, halfturn=None, device="cpu"):
         D = forest.D
         if nvars < 1:
             raise ValueError(f"nvars must be positive, got {nvars}")
@@ -139,13 +271,30 @@ class FieldSet:
         self.parities = check_parity(forest, self.nvars, parity)
         table = self.parities if self.parities is not None else \
             [("EvenParity",) * D] * self.nvars
-        self.factors_host = parityfactors(self.T, table, D)
+        self.rotation = rotations_of(rotation, forest, self.nvars, self.G, self.c,
+                                     self.parities)
+        self.halfturn = halfturns_of(halfturn, forest, self.nvars, self.parities)
+        # the variable table of turned transfers, nvars x 4 (None off a seam)
+        self.rotvars_host = None
+        if forest.ishalfturn():
+            self.factors_host, self.rotvars_host = seamtables(self.T, table, None, self.nvars,
+                                                              D, half=self.halfturn)
+        elif forest.hasrotating():
+            q = self.rotation
+            steps = (q, q, q) if symmetric_layout(forest, self.G, self.c) else None
+            self.factors_host, self.rotvars_host = seamtables(self.T, table, steps,
+                                                              self.nvars, D)
+        else:
+            self.factors_host = parityfactors(self.T, table, D)
         self.device = torch.device(device)
         shape = (forest.nleaves(), self.nvars) + tuple(reversed(self.stored))
         # zero-filled, as the reference's first touch (src/storage.jl:1433-1446)
         self.work = torch.zeros(shape, dtype=_TORCH[self.T], device=self.device)
         # the factor table column-major (nvars fastest), as the kernel reads it
         self.factors = torch.from_numpy(np.asfortranarray(self.factors_host).ravel(order="F").copy()).to(self.device)
+        # column-major too: rotvars[v + nvars * r]
+        self.rotvars = None if self.rotvars_host is None else torch.from_numpy(
+            np.asfortranarray(self.rotvars_host).ravel(order="F").copy()).to(self.device)
 
     @property
     def D(self) -> int:
