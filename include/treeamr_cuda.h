@@ -79,9 +79,12 @@ typedef struct tam_group {
    * orientation r in 1..3 (0: an ordinary group), and its axis map in
    * gather form, `axes` = sum_e perm[e] << 2e  +  flip[e] << (8 + e) with
    * 0-based dimensions: virtual stored index k reads the real point whose
-   * index along e is k[perm[e]], or S_e + 1 - k[perm[e]] where flip[e], and
-   * variable rotvars[v + nvars * r] (1-based) of the real source.  An odd
-   * orientation reads the alternate array of tam_fill_ex. */
+   * index along e is k[perm[e]], or R_e + 1 - k[perm[e]] where flip[e], and
+   * variable rotvars[v + nvars * r] (1-based) of the real source, an array
+   * of stored extent R_e = S[perm[e]] along e.  An odd orientation reads the
+   * alternate array of tam_fill_ex: the set's own when its layout is
+   * symmetric in the seam's plane, else its RotationPair partner's, the
+   * swapped layout. */
   int32_t orientation;
   int32_t axes;
   int64_t first;     /* offset into the block lists                        */

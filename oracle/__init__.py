@@ -102,7 +102,8 @@ def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=A
     else:
         rv = np.ascontiguousarray(np.asfortranarray(rotvars).ravel(order="F"), dtype=np.int32)
         a = work if alt is None else alt
-        assert a.flags.c_contiguous and a.shape == work.shape and a.dtype == work.dtype
+        # a RotationPair partner holds the swapped layout: as many points a block
+        assert a.flags.c_contiguous and a.size == work.size and a.dtype == work.dtype
         rc = lib().oracle_fill_turned(C.addressof(d.desc), work.ctypes.data, a.ctypes.data,
                                       nvars, f.ctypes.data, rv.ctypes.data, first, last,
                                       nthreads, 1 if one_tap else 0)

@@ -84,14 +84,18 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
     const int64_t bs = vs * nvars;                                                              \
     /* the source's strides per virtual dimension: the identity, or a turned  \
        group's axis map (RotatedSource, src/ghosts.jl:183-244) */              \
+    /* the real array's extent along e is S[perm[e]]: the set's own, or an    \
+       odd orientation's partner with the seam's dimensions swapped */        \
     int64_t vst[3] = {1, s2, s3}, c0 = 0;                                                       \
-    const int64_t rst[3] = {1, s2, s3};                                                         \
     const T *from = work;                                                                       \
     if (g->orientation) {                                                                       \
+      int64_t R[3] = {1, 1, 1};                                                                 \
+      for (int e = 0; e < D; ++e) R[e] = S[(g->axes >> (2 * e)) & 3];                          \
+      const int64_t rst[3] = {1, R[0], R[0] * R[1]};                                            \
       for (int e = 0; e < D; ++e) {                                                             \
         const int p = (g->axes >> (2 * e)) & 3, f = (g->axes >> (8 + e)) & 1;                  \
         vst[p] = f ? -rst[e] : rst[e];                                                          \
-        if (f) c0 += rst[e] * (S[e] - 1);                                                       \
+        if (f) c0 += rst[e] * (R[e] - 1);                                                       \
       }                                                                                         \
       if (g->orientation & 1) from = alt;                                                       \
     }                                                                                           \

@@ -585,3 +585,156 @@ def test_gpu_turned_fill_refusals(cuda_lib):
     asym = FieldSet(f, 1, G=(1, 2), rotation=(1,), device="cuda")
     with pytest.raises(ValueError, match="RotationPair"):
         fill_ghosts(asym, GhostSchedule(asym, Operators(prolongation=2, restriction=2)))
+
+
+# --- RotationPair: asymmetric layouts -----------------------------------------------------
+
+def unfold_member(quad, own_fs, partner_fs, full, back, ff, steps):
+    """The full plane's own points of one member's layout: in quarter ``r``
+    the composed map of ``steps[:r]`` applied to the quadrant data of the
+    member itself (``r`` even) or of its partner (``r`` odd)."""
+    D, N = quad.D, quad.N
+    d1, d2 = quad.seam_plane()
+    out = np.full(tuple(ff.work.shape), np.nan, dtype=own_fs.T)
+    qindex = {k: i for i, k in enumerate(quad.leaves)}
+    nv = own_fs.nvars
+    for bf, kf in enumerate(full.leaves):
+        r, kq = back(kf)
+        src = partner_fs if r % 2 else own_fs
+        hq = src.work.numpy()
+        sigma, sign = composed_rotation(steps[:r], nv)
+        lof, _ = leafbox(full, kf)
+        loq, _ = leafbox(quad, kq)
+        h = F(1, N << kf.level)
+        shift = tuple(quad.roots[d1] if d in (d1, d2) else 0 for d in range(D))
+        for I in itertools.product(range(N), repeat=D):
+            x = [lof[d] + (I[d] + F(1, 2)) * h - shift[d] for d in range(D)]
+            for _ in range((4 - r) % 4):
+                x[d1], x[d2] = -x[d2], x[d1]
+            J = [int((x[d] - loq[d]) / h - F(1, 2)) for d in range(D)]
+            for v in range(nv):
+                val = hq[(qindex[kq], sigma[v] - 1) +
+                         tuple(src.G[d] + J[d] for d in reversed(range(D)))]
+                out[(bf, v) + tuple(ff.G[d] + I[d] for d in reversed(range(D)))] = \
+                    -val if sign[v] < 0 else val
+    return out
+
+
+def pair_case(D, plane, other, T=np.float64, seed=5):
+    """A cell-centred pair whose ghost widths alone are swapped, the vector
+    stored in swapped component orders so that the maps permute
+    (``test/rotate_tests.jl:458-489``)."""
+    from treeamr import RotationPair
+    quad = seam_forest(D, plane, other)
+    d1, d2 = plane[0] - 1, plane[1] - 1
+    Ga = tuple(2 if d == d1 else 1 for d in range(D))
+    Gb = tuple(2 if d == d2 else 1 for d in range(D))
+    # a stores (s, v_1 .. v_D), b the same vector with its d1 and d2
+    # components exchanged, w_{d1} = v_{d2} and w_{d2} = v_{d1}.  A quarter
+    # turn takes v to (v'_{d1}, v'_{d2}) = (-v_{d2}, v_{d1}), so a's data at
+    # R p come from b's at p as Q_a says, and b's from a's as Q_b says.
+    nv = D + 1
+    par = vector_parity(D, plane, other)
+    qa = [1] + [-(2 + d1) if e == d1 else (2 + d2) if e == d2 else e + 2 for e in range(D)]
+    qb = [1] + [(2 + d1) if e == d1 else -(2 + d2) if e == d2 else e + 2 for e in range(D)]
+    perm_b = [0] + [1 + (d2 if e == d1 else d1 if e == d2 else e) for e in range(D)]
+    parb = None if par is None else [par[perm_b[v]] for v in range(nv)]
+    a = FieldSet(quad, nv, G=Ga, T=T, parity=par, rotation=qa)
+    b = FieldSet(quad, nv, G=Gb, T=T, parity=parb, rotation=qb)
+    rng = np.random.default_rng(seed)
+    for fs in (a, b):
+        host = np.full(tuple(fs.work.shape), np.nan, dtype=T)
+        own = (slice(None), slice(None)) + tuple(slice(g, g + quad.N) for g in reversed(fs.G))
+        host[own] = rng.uniform(-1, 1, size=host[own].shape).astype(T)
+        fs.work = torch.from_numpy(host)
+    pair = RotationPair(a, b)
+    ops = Operators(prolongation=2, restriction=2)
+    return quad, pair, (GhostSchedule(a, ops), GhostSchedule(b, ops)), ops
+
+
+def oracle_pair_fill(pair, schedules, hook_zero=True):
+    """The merged fill on the host: stage by stage, a then b, each turned
+    group of odd orientation reading the partner's array."""
+    a, b = pair.a, pair.b
+    ha, hb = a.work.numpy().copy(), b.work.numpy().copy()
+    sa, sb = schedules
+    mem = [(sa, ha, hb, a, pair.afactors_host, pair.arotvars_host),
+           (sb, hb, ha, b, pair.bfactors_host, pair.brotvars_host)]
+    tags = sorted(set(sa.stage_tags) | set(sb.stage_tags))
+    for phase in (0, 1):
+        for tag in [t for t in tags if (t <= 1) == (phase == 0)]:
+            for s, h, alt, fs, fac, rv in mem:
+                oracle.fill(s, h, fs.nvars, fac, first=tag, last=tag, rotvars=rv, alt=alt)
+        if phase == 0 and hook_zero:
+            for s, h, *_ in mem:
+                for r in s.boundaries:
+                    h[(r.block, slice(None)) +
+                      tuple(slice(x - 1, z) for x, z in reversed(r.region))] = 0
+    return ha, hb
+
+
+@pytest.mark.parametrize("D,plane,other", [(2, (1, 2), "none"), (2, (2, 1), "none"),
+                                           (3, (1, 2), "reflect_lo"), (3, (3, 2), "periodic")])
+def test_a_rotation_pair_is_the_turned_full_plane(D, plane, other):
+    """``test/rotate_tests.jl:458-489``: a pair fill reads each set's ghosts
+    across the seam out of the other through the composed maps; each set
+    equals the full plane's set of its layout, which holds the quadrant's
+    data turned, to 1e-13."""
+    quad, pair, (sa, sb), ops = pair_case(D, plane, other)
+    assert sa.odd_turns and sb.odd_turns
+    ga, gb = oracle_pair_fill(pair, (sa, sb))
+    full, image, back = unfolded_forest(quad)
+    a, b = pair.a, pair.b
+    for own, partner, got, steps in ((a, b, ga, (a.rotation, b.rotation, a.rotation)),
+                                     (b, a, gb, (b.rotation, a.rotation, b.rotation))):
+        ff = FieldSet(full, own.nvars, G=own.G, T=own.T, parity=own.parities)
+        ff.work = torch.from_numpy(unfold_member(quad, own, partner, full, back, ff, steps))
+        want = zero_hook_fill(GhostSchedule(ff, ops), ff)
+        _agree(quad, full, image, got, want)
+        assert not np.isnan(got).any()
+
+
+def test_rotation_pair_refusals():
+    """``test/rotate_tests.jl:355-397``."""
+    from treeamr import RotationPair
+    f = Forest((2, 2), N=8, rotating=(1, 2))
+    A = lambda **kw: FieldSet(f, 1, G=(2, 1), rotation=(-1,), **kw)        # noqa: E731
+    B = lambda **kw: FieldSet(f, 1, G=(1, 2), rotation=(1,), **kw)         # noqa: E731
+    p = RotationPair(A(), B())
+    assert p.arotvars_host.tolist() == [[1, 1, 1, 1]]
+    assert p.afactors_host[0, [0, 9, 18, 27]].tolist() == [1, -1, -1, 1]
+    assert p.bfactors_host[0, [0, 9, 18, 27]].tolist() == [1, 1, -1, -1]
+    other = Forest((2, 2), N=8, rotating=(1, 2))
+    with pytest.raises(ValueError, match="over one forest"):
+        RotationPair(A(), FieldSet(other, 1, G=(1, 2), rotation=(1,)))
+    with pytest.raises(ValueError, match="rotating seam"):
+        plain = Forest((2, 2), N=8)
+        RotationPair(FieldSet(plain, 1, G=(2, 1)), FieldSet(plain, 1, G=(1, 2)))
+    with pytest.raises(ValueError, match="each other's layout"):
+        RotationPair(A(), A())
+    with pytest.raises(ValueError, match="turns into itself"):
+        RotationPair(FieldSet(f, 1, G=1, rotation=(1,)), FieldSet(f, 1, G=1, rotation=(1,)))
+    with pytest.raises(ValueError, match="same number of variables"):
+        RotationPair(A(), FieldSet(f, 2, G=(1, 2), rotation=(1, 2)))
+    with pytest.raises(ValueError, match="one element type"):
+        RotationPair(A(), FieldSet(f, 1, G=(1, 2), rotation=(1,), T=np.float32))
+    with pytest.raises(ValueError, match="not the identity"):
+        RotationPair(FieldSet(f, 2, G=(2, 1), rotation=(-2, 1)),
+                     FieldSet(f, 2, G=(1, 2), rotation=(1, 2)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,plane,other", [(2, (1, 2), "none"), (3, (1, 2), "reflect_lo")])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_rotation_pair_bit_exact(cuda_lib, D, plane, other, T):
+    """The device pair fill is the oracle's merged fill bit for bit."""
+    from treeamr import fill_ghosts
+    quad, pair, (sa, sb), ops = pair_case(D, plane, other, T=T)
+    ea, eb = oracle_pair_fill(pair, (sa, sb), hook_zero=False)
+    for fs in (pair.a, pair.b):
+        fs.work, fs.factors = fs.work.cuda(), fs.factors.cuda()
+    pair.to("cuda")
+    fill_ghosts(pair, (sa, sb))
+    torch.cuda.synchronize()
+    assert np.array_equal(nanbits(pair.a.work.cpu().numpy()), nanbits(ea))
+    assert np.array_equal(nanbits(pair.b.work.cpu().numpy()), nanbits(eb))

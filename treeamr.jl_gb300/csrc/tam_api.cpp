@@ -147,9 +147,11 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
     if (g.orientation == 0 && g.axes != 0)
       return fail(ctx, TAM_EINVAL, "an ordinary group has the identity axis map (axes = 0)");
     if (g.orientation != 0) {
-      // the axis map: a permutation of the dimensions that carries each real
-      // dimension onto a virtual one of the same stored extent, so that a
-      // virtual index inside the stored box reads a real one inside it
+      // the axis map: a permutation of the dimensions.  The real array has
+      // stored extent S[perm[e]] along e (the schedule's own layout for a set
+      // symmetric in the seam's plane, the partner's swapped one for an odd
+      // orientation of a RotationPair), so a virtual index inside the stored
+      // box reads a real one inside the real array's box
       int seen = 0;
       for (int e = 0; e < 3; ++e) {
         const int p = (g.axes >> (2 * e)) & 3, f = (g.axes >> (8 + e)) & 1;
@@ -161,10 +163,10 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
         if (p >= d->ndim || (seen >> p) & 1)
           return fail(ctx, TAM_EINVAL, "a turned group's axis map is not a permutation");
         seen |= 1 << p;
-        if (d->stored[p] != d->stored[e])
+        if ((g.orientation & 1) == 0 && d->stored[p] != d->stored[e])
           return fail(ctx, TAM_EINVAL,
-                      "a turned group exchanges dimensions of different stored extents: the "
-                      "layout must be symmetric in the seam's plane");
+                      "an even orientation reads the set's own array, so its axis map must "
+                      "keep the stored extents");
       }
       if ((g.axes & ~0x73F) != 0)
         return fail(ctx, TAM_EINVAL, "stray bits in a turned group's axis map");
@@ -369,14 +371,14 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
 }
 
 // The turned groups of every stage (TurnGroup): the axis map folded into
-// signed strides of the real array.  Virtual stored index k (1-based) along
-// virtual dimension perm[e] reads real index k, or S_e + 1 - k where flip[e],
-// along e; with j = k - 1 the real offset is
-//   sum_e stride_e * (flip[e] ? S_e - 1 - j : j),
-// so vs[perm[e]] = +-stride_e and c0 = sum over flipped e of stride_e (S_e - 1).
+// signed strides of the real array, whose stored extent along e is
+// R_e = S[perm[e]].  Virtual stored index k (1-based) along virtual
+// dimension perm[e] reads real index k, or R_e + 1 - k where flip[e], along
+// e; with j = k - 1 the real offset is
+//   sum_e stride_e * (flip[e] ? R_e - 1 - j : j),   stride = (1, R_0, R_0 R_1),
+// so vs[perm[e]] = +-stride_e and c0 = sum over flipped e of stride_e (R_e - 1).
 void build_turns(tam_sched *s) {
   s->h_turns.clear();
-  const int64_t stride[3] = {1, s->S[0], (int64_t)s->S[0] * s->S[1]};
   for (tam::Stage &st : s->stages) {
     st.turn0 = (int64_t)s->h_turns.size();
     for (int32_t gi : st.groups) {
@@ -386,6 +388,9 @@ void build_turns(tam_sched *s) {
       t.group = gi;
       t.col = h.orientation;
       t.odd = h.orientation & 1;
+      int R[3] = {1, 1, 1};
+      for (int e = 0; e < s->D; ++e) R[e] = s->S[(h.axes >> (2 * e)) & 3];
+      const int64_t stride[3] = {1, R[0], (int64_t)R[0] * R[1]};
       t.vs[0] = 1;
       t.vs[1] = stride[1];
       t.vs[2] = stride[2];
@@ -394,7 +399,7 @@ void build_turns(tam_sched *s) {
         const int p = (h.axes >> (2 * e)) & 3;
         const bool f = (h.axes >> (8 + e)) & 1;
         t.vs[p] = f ? -stride[e] : stride[e];
-        if (f) t.c0 += stride[e] * (s->S[e] - 1);
+        if (f) t.c0 += stride[e] * (R[e] - 1);
       }
       s->h_turns.push_back(t);
     }

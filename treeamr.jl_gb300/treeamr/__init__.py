@@ -7,8 +7,8 @@ library ``libtreeamr_cuda.so`` replays it on one GPU.
 from .forest import (Forest, MortonKey, OUTER, OUTFLOW, REFLECTING, alldirections, childoffset,
                      curve_key, parentkey, sortedchildkeys)
 from .operators import Conservative, Operators, PointValue, check_operators, lagrange_weights
-from .storage import (EvenParity, FieldSet, NoParity, OddParity, cellcentered, coordinates,
-                      staggers, vertexcentered)
+from .storage import (EvenParity, FieldSet, NoParity, OddParity, RotationPair, cellcentered,
+                      coordinates, staggers, vertexcentered)
 from .schedule import GhostSchedule, TransferGroup, Stencil1D, GroupKey
 from .ghosts import boundary_by_coordinates, fill_ghosts
 from .state import gather, scatter, scatter_fill, statearray, statelength, statevector
@@ -17,7 +17,7 @@ __all__ = [
     "Forest", "MortonKey", "alldirections", "childoffset", "curve_key", "parentkey",
     "sortedchildkeys", "OUTER", "OUTFLOW", "REFLECTING",
     "Operators", "PointValue", "Conservative", "check_operators", "lagrange_weights",
-    "FieldSet", "EvenParity", "OddParity", "NoParity", "cellcentered", "vertexcentered",
+    "FieldSet", "RotationPair", "EvenParity", "OddParity", "NoParity", "cellcentered", "vertexcentered",
     "staggers", "coordinates",
     "GhostSchedule", "TransferGroup", "Stencil1D", "GroupKey",
     "fill_ghosts", "boundary_by_coordinates",

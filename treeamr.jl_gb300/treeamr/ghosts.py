@@ -51,16 +51,22 @@ class DeviceSchedule:
             self.handle = None
 
     def run(self, fs: FieldSet, first: int, last: int, method: str = "fused",
-            stream: Optional[torch.cuda.Stream] = None, alt: Optional[torch.Tensor] = None):
+            stream: Optional[torch.cuda.Stream] = None, alt: Optional[torch.Tensor] = None,
+            factors: Optional[torch.Tensor] = None, rotvars: Optional[torch.Tensor] = None):
+        """Stages ``[first, last]`` on ``fs.work``; a RotationPair member's
+        fill passes the pair's tables and its partner's array ``alt``."""
         s = stream if stream is not None else torch.cuda.current_stream(fs.work.device)
-        rotvars = getattr(fs, "rotvars", None)
+        if rotvars is None:
+            rotvars = getattr(fs, "rotvars", None)
+        if factors is None:
+            factors = fs.factors
         if rotvars is not None or alt is not None:
             # turned transfers across a seam read the variable table, and an
             # odd orientation the alternate array (tam_fill_ex)
             rc = self.lib.tam_fill_ex(
                 self.handle, C.c_void_p(fs.work.data_ptr()),
                 C.c_void_p(alt.data_ptr() if alt is not None else 0), fs.nvars, fs.nblocks(),
-                C.c_void_p(fs.factors.data_ptr()),
+                C.c_void_p(factors.data_ptr()),
                 C.c_void_p(rotvars.data_ptr() if rotvars is not None else 0), first, last,
                 _native.TAM_METHOD_PLAIN if method == "plain" else _native.TAM_METHOD_FUSED,
                 C.c_void_p(s.cuda_stream))
@@ -128,7 +134,7 @@ def device_schedule(schedule: GhostSchedule, device: int) -> DeviceSchedule:
     return cache[device]
 
 
-def check_fill(fs: FieldSet, schedule: GhostSchedule):
+def check_fill(fs: FieldSet, schedule: GhostSchedule, pair: bool = False):
     """The reference's refusals before any launch (``src/ghosts.jl:2058-2101``)."""
     if fs.forest is not schedule.forest:
         raise ValueError("the field set and the schedule are over different forests")
@@ -149,7 +155,7 @@ def check_fill(fs: FieldSet, schedule: GhostSchedule):
                          "the field set's; build the schedule from this field set")
     if fs.work.device.type != "cuda":
         raise ValueError("fill_ghosts runs on the GPU: the field set must live on a CUDA device")
-    if getattr(schedule, "odd_turns", False):
+    if getattr(schedule, "odd_turns", False) and not pair:
         from .storage import symmetric_layout
         if not symmetric_layout(fs.forest, fs.G, fs.c):
             raise ValueError(
@@ -157,10 +163,55 @@ def check_fill(fs: FieldSet, schedule: GhostSchedule):
                 f"{fs.forest.rotating_dims()} (G = {fs.G}, centering {fs.centering}), so its "
                 "ghosts across the seam are its partner's data, turned: fill it together with "
                 "the set of the swapped layout as a RotationPair (src/ghosts.jl:1960-1980)")
-    if getattr(schedule, "turned", False) and fs.rotvars is None:
+    if getattr(schedule, "turned", False) and fs.rotvars is None and not pair:
         raise ValueError("this schedule turns ghosts across a seam, but the field set has no "
                          "variable table to turn them with: build it over the same forest, "
                          "with `rotation` (or `halfturn`)")
+
+
+def fill_pair(pair, schedules, *, boundary=None, method: str = "fused",
+              stream: Optional[torch.cuda.Stream] = None):
+    """``fill_ghosts!(pair, (sa, sb); boundary)`` (``src/ghosts.jl:2117-2180``):
+    the two schedules' stages merged by (stage, member), each member's
+    turned transfers of odd orientation reading its partner's array through
+    the pair's tables; the hooks (one for both, or one each) after phase 1
+    of both, before the prolongations."""
+    from .storage import RotationPair
+    if not isinstance(pair, RotationPair):
+        raise TypeError("fill_pair takes a RotationPair")
+    sa, sb = schedules
+    if method not in METHODS:
+        raise ValueError(f"method must be one of {METHODS}")
+    a, b = pair.a, pair.b
+    check_fill(a, sa, pair=True)
+    check_fill(b, sb, pair=True)
+    hooks = boundary if isinstance(boundary, tuple) else (boundary, boundary)
+    members = [(a, sa, pair.afactors, pair.arotvars, b.work, hooks[0]),
+               (b, sb, pair.bfactors, pair.brotvars, a.work, hooks[1])]
+    dss = [device_schedule(s, x.work.device.index or 0) for x, s, *_ in members]
+    tags = sorted(set(sa.stage_tags) | set(sb.stage_tags))
+
+    def run(i, tag):
+        fs, s, fac, rv, alt, _ = members[i]
+        if tag in s.stage_tags:
+            dss[i].run(fs, tag, tag, method, stream, alt=alt, factors=fac, rotvars=rv)
+    for tag in [t for t in tags if t <= PHASE1_TAG]:
+        run(0, tag)
+        run(1, tag)
+    for i in (0, 1):
+        fs, s, *_, hook = members[i]
+        if hook is None or not s.boundaries:
+            continue
+        from .boundary import CellBoundary
+        if isinstance(hook, CellBoundary):
+            hook.apply(fs, s, stream, slot=PHASE1_TAG) if hook.relative else \
+                hook.apply(fs, s, stream)
+        else:
+            hook(fs, s.boundaries)
+    for tag in [t for t in tags if t > PHASE1_TAG]:
+        run(0, tag)
+        run(1, tag)
+    return pair
 
 
 def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Callable] = None,
@@ -170,7 +221,11 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
     ``boundary(fs, regions)`` fills the regions facing out through outer faces;
     it runs after phase 1 and before the prolongations, as the reference's
     hook does (``src/ghosts.jl:1129-1136``).  ``method`` picks the fused
-    batched launch (default) or the plain one-launch-per-group replay."""
+    batched launch (default) or the plain one-launch-per-group replay.
+    ``fill_ghosts(pair, (schedule_a, schedule_b))`` fills a RotationPair."""
+    from .storage import RotationPair
+    if isinstance(fs, RotationPair):
+        return fill_pair(fs, schedule, boundary=boundary, method=method, stream=stream)
     if method not in METHODS:
         raise ValueError(f"method must be one of {METHODS}")
     check_fill(fs, schedule)

@@ -354,3 +354,82 @@ def coordinates(fs: FieldSet, b: int, idx: Sequence[int]):
     """Position of the 1-based stored index ``idx`` of block ``b``."""
     pos = fs.positions(b)
     return tuple(pos[d][idx[d] - 1] for d in range(fs.D))
+
+
+class RotationPair:
+    """Two field sets over one forest with a quarter-turn seam, each of which
+    turns into the other (``RotationPair``, ``src/storage.jl:742-857``): a set
+    whose layout is not symmetric in the seam's plane takes its ghosts across
+    the seam from the set of the swapped layout.  Holds the tables of each
+    set's targets: for ``a`` the maps ``Q_a``, ``Q_a Q_b`` and ``Q_a Q_b Q_a``
+    for one, two and three quarter turns, the odd ones reading ``b``; and
+    symmetrically for ``b``.  Fill it with ``fill_ghosts(pair, (sa, sb))``."""
+
+    def __init__(self, a: FieldSet, b: FieldSet):
+        if a.forest is not b.forest:
+            raise ValueError("the two sets of a RotationPair must be over one forest: each "
+                             "fills its ghosts across the seam from the other's blocks")
+        forest = a.forest
+        if not forest.hasrotating():
+            raise ValueError("a RotationPair needs a forest with a rotating seam: without one "
+                             "no set turns into another")
+        if forest.ishalfturn():
+            raise ValueError("a RotationPair needs a quarter-turn seam, and this forest's is a "
+                             "half turn: every set turns into itself")
+        d1, d2 = forest.seam_plane()
+
+        def swap(t):
+            t = list(t)
+            t[d1], t[d2] = t[d2], t[d1]
+            return tuple(t)
+        if a.G != swap(b.G) or a.centering != swap(b.centering):
+            raise ValueError("the two sets of a RotationPair must have each other's layout "
+                             f"with the seam's dimensions {d1 + 1} and {d2 + 1} exchanged: got "
+                             f"G = {a.G} and {b.G}, centering {a.centering} and {b.centering}")
+        if symmetric_layout(forest, a.G, a.c):
+            raise ValueError("these sets have a layout symmetric in the seam's dimensions, so "
+                             "each turns into itself and fills its ghosts alone")
+        if a.nvars != b.nvars:
+            raise ValueError("the two sets of a RotationPair must have the same number of "
+                             f"variables: got {a.nvars} and {b.nvars}")
+        if a.T != b.T:
+            raise ValueError("the two sets of a RotationPair must store one element type: got "
+                             f"{a.T} and {b.T}")
+        if a.work.device != b.work.device:
+            raise ValueError("the two sets of a RotationPair must live on one device")
+        qa, qb = a.rotation, b.rotation
+        sigma, sign = composed_rotation((qa, qb, qa, qb), a.nvars)
+        if sigma != list(range(1, a.nvars + 1)) or any(x != 1 for x in sign):
+            raise ValueError(f"the rotations of the pair, {tuple(qa)} and {tuple(qb)}, composed "
+                             "four times as Q_a Q_b Q_a Q_b are not the identity")
+        for x, y, q, what in ((a, b, qa, "the first set"), (b, a, qb, "the second set")):
+            if x.parities is not None and y.parities is not None:
+                for v in range(len(q)):
+                    w = abs(q[v]) - 1
+                    for d in range(forest.D):
+                        if REFLECTING in forest.faces[d] and x.parities[v][d] != y.parities[w][d]:
+                            raise ValueError(f"the rotation of {what} sends variable {v + 1} to "
+                                             f"variable {w + 1} of the other, which must have "
+                                             f"the same parity in dimension {d + 1}")
+        self.a, self.b = a, b
+
+        def table(fs):
+            return fs.parities if fs.parities is not None else \
+                [("EvenParity",) * forest.D] * fs.nvars
+        self.afactors_host, self.arotvars_host = seamtables(a.T, table(a), (qa, qb, qa),
+                                                            a.nvars, forest.D)
+        self.bfactors_host, self.brotvars_host = seamtables(b.T, table(b), (qb, qa, qb),
+                                                            b.nvars, forest.D)
+        dev = a.work.device
+
+        def col(x):
+            return torch.from_numpy(np.asfortranarray(x).ravel(order="F").copy()).to(dev)
+        self.afactors, self.bfactors = col(self.afactors_host), col(self.bfactors_host)
+        self.arotvars, self.brotvars = col(self.arotvars_host), col(self.brotvars_host)
+
+    def to(self, device):
+        """The tables on ``device`` (the sets' arrays move with the sets)."""
+        for name in ("afactors", "bfactors", "arotvars", "brotvars"):
+            setattr(self, name, getattr(self, name).to(device))
+        return self
+
