@@ -12,14 +12,16 @@
 module TreeAMRCUDA
 
 using TreeAMR
-using TreeAMR: GhostSchedule, TransferGroup, Stencil1D, FieldSet, CellBoundary
+using TreeAMR: GhostSchedule, TransferGroup, Stencil1D, FieldSet, CellBoundary, RotationPair,
+               hasrotating
 using CUDA
 import ChainRulesCore
 
 const LIB = get(ENV, "TREEAMR_CUDA_LIB", joinpath(@__DIR__, "..", "csrc", "_build",
                                                   "libtreeamr_cuda.so"))
 
-const TAM_ABI_VERSION = Int32(1)
+const TAM_ABI_VERSION = Int32(2)
+const TAM_METHOD_FUSED, TAM_METHOD_PLAIN = Int32(0), Int32(1)
 const TAM_F32, TAM_F64 = Int32(1), Int32(2)
 const TAM_COPY, TAM_RESTRICT, TAM_PROLONG = Int32(1), Int32(2), Int32(3)
 const STAGE_FIRST, STAGE_LAST = Int32(-1), typemax(Int32)
@@ -39,6 +41,8 @@ struct TamGroup
     stage::Int32
     factorcol::Int32
     bounded::Int32
+    orientation::Int32   # a turned group's orientation (0: none)
+    axes::Int32          # its axis map: perm[e] - 1 << 2(e-1), flip[e] << (7 + e)
     first::Int64
     ntransfers::Int64
     stencil::NTuple{3,TamStencil}
@@ -121,8 +125,12 @@ function upload(s::GhostSchedule{T,D}, dev::Int=CUDA.device().handle) where {T,D
             TamStencil(st.targetfirst, length(st.srcstart), size(st.weights, 1), st.unit,
                        off[1], off[2])
         end
+        # a turned group's axis map (src/ghosts.jl:238-244), 0-based in the ABI
+        axes = g.orientation == 0 ? Int32(0) :
+               Int32(sum((Int(g.perm[e]) - 1) << (2 * (e - 1)) + Int(g.flip[e]) << (7 + e)
+                         for e in 1:D))
         push!(groups, TamGroup(kindcode(g.kind), stage, g.factorcol, g.bounded,
-                               length(tb), length(g.targetblocks), sts))
+                               g.orientation, axes, length(tb), length(g.targetblocks), sts))
         append!(tb, Array(g.targetblocks))
         append!(sb, Array(g.sourceblocks))
     end
@@ -132,7 +140,8 @@ function upload(s::GhostSchedule{T,D}, dev::Int=CUDA.device().handle) where {T,D
     out = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve groups tb sb ss ws begin
         desc = TamScheduleDesc(TAM_ABI_VERSION, D, T === Float64 ? TAM_F64 : TAM_F32, stored,
-                               nleaves(s.forest), length(groups), 3^D, pointer(groups),
+                               nleaves(s.forest), length(groups),
+                               (hasrotating(s.forest) ? 4 : 1) * 3^D, pointer(groups),
                                length(tb), pointer(tb), pointer(sb), length(ss), pointer(ss),
                                length(ws), pointer(ws))
         check(ccall((:tam_schedule_upload, LIB), Cint,
@@ -148,16 +157,54 @@ const UPLOADS = WeakKeyDict{GhostSchedule,DeviceSchedule}()
 device_schedule(s::GhostSchedule) = get!(() -> upload(s), UPLOADS, s)
 
 function tam_fill!(fs::FieldSet, ds::DeviceSchedule, first::Int32, last::Int32;
-                   plain::Bool=false)
-    f = plain ? :tam_fill_plain : :tam_fill
+                   plain::Bool=false, factors=fs.factors, rotvars=fs.rotvars, alt=nothing)
     stream = CUDA.stream().handle
-    factors = fs.factors === nothing ? CU_NULL : pointer(fs.factors)
-    rc = ccall((f, LIB), Cint,
-               (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Int32, Ptr{Cvoid}),
-               ds.handle, pointer(fs.work), fs.nvars, size(fs.work, ndims(fs.work)), factors,
-               first, last, stream)
-    check(rc, ds.ctx, String(f))
+    fptr = factors === nothing ? CU_NULL : pointer(factors)
+    if rotvars === nothing && alt === nothing
+        f = plain ? :tam_fill_plain : :tam_fill
+        rc = ccall((f, LIB), Cint,
+                   (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Int32,
+                    Ptr{Cvoid}),
+                   ds.handle, pointer(fs.work), fs.nvars, size(fs.work, ndims(fs.work)), fptr,
+                   first, last, stream)
+        return check(rc, ds.ctx, String(f))
+    end
+    # turned transfers across a seam: the variable table, and for a pair the
+    # partner's array (run_group!'s rotvars and altsrc, src/ghosts.jl:420-490)
+    rc = ccall((:tam_fill_ex, LIB), Cint,
+               (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid},
+                CuPtr{Int32}, Int32, Int32, Int32, Ptr{Cvoid}),
+               ds.handle, pointer(fs.work), alt === nothing ? CU_NULL : pointer(alt),
+               fs.nvars, size(fs.work, ndims(fs.work)), fptr,
+               rotvars === nothing ? CU_NULL : pointer(rotvars), first, last,
+               plain ? TAM_METHOD_PLAIN : TAM_METHOD_FUSED, stream)
+    check(rc, ds.ctx, "tam_fill_ex")
 end
+
+# fill_ghosts!(pair, (sa, sb)) of CuArray sets (src/ghosts.jl:2117): the two
+# schedules' stages merged by (stage, member), each member reading its
+# partner's array through the pair's tables; the hooks after phase 1.
+function fill_pair!(pair::RotationPair, (sa, sb)::Tuple{GhostSchedule,GhostSchedule};
+                    boundary=nothing)
+    a, b = pair.a, pair.b
+    da, db = device_schedule(sa), device_schedule(sb)
+    ha, hb = boundary isa Tuple ? boundary : (boundary, boundary)
+    for (lo, hi) in ((STAGE_FIRST, Int32(1)), (Int32(2), STAGE_LAST))
+        tags = sort!(unique!(vcat(stage_tags(sa), stage_tags(sb))))
+        for t in filter(t -> lo <= t <= hi, tags)
+            tam_fill!(a, da, Int32(t), Int32(t); factors=pair.afactors, rotvars=pair.arotvars,
+                      alt=b.work)
+            tam_fill!(b, db, Int32(t), Int32(t); factors=pair.bfactors, rotvars=pair.brotvars,
+                      alt=a.work)
+        end
+        if lo == STAGE_FIRST
+            ha === nothing || TreeAMR.apply_boundary!(a, ha, sa, CUDABackend())
+            hb === nothing || TreeAMR.apply_boundary!(b, hb, sb, CUDABackend())
+        end
+    end
+    return pair
+end
+stage_tags(s::GhostSchedule) = Int32[first(x) for x in stage_groups(s)]
 
 # The drop-in: fill_ghosts! of a CuArray field set (src/ghosts.jl:1783),
 # after the reference's own checks.
