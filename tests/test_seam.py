@@ -738,3 +738,49 @@ def test_gpu_rotation_pair_bit_exact(cuda_lib, D, plane, other, T):
     torch.cuda.synchronize()
     assert np.array_equal(nanbits(pair.a.work.cpu().numpy()), nanbits(ea))
     assert np.array_equal(nanbits(pair.b.work.cpu().numpy()), nanbits(eb))
+
+
+@pytest.mark.parametrize("D,plane,other", [(2, (1, 2), "none"), (2, (2, 1), "none"),
+                                           (3, (1, 2), "reflect_lo")])
+def test_a_regrid_across_the_seam_is_the_full_planes(D, plane, other):
+    """``test/rotate_tests.jl:561-604``: refining along the low face of d1
+    near the axis makes conformity refine the image on the low face of d2;
+    the regrid transfer's prolongations read their parents' ghosts across
+    the seam, so the moved quadrant, filled again, is the full plane's
+    regrid of the same leaves to 1e-13."""
+    from test_regrid import oracle_regrid
+    from treeamr.regrid import RegridTransfer
+    quad, fs, s, full, ff, image = quadrant_case(D, plane, other)
+    d1, d2 = quad.seam_plane()
+    old_q, old_f = list(quad.leaves), list(full.leaves)
+    hq = zero_hook_fill(s, fs)
+    hf = zero_hook_fill(GhostSchedule(ff, OPS4), ff)
+    marked = [k for k in quad.leaves if leafbox(quad, k)[0][d1] == 0 and
+              leafbox(quad, k)[0][d2] < 1 and k.level < 3]
+    assert marked
+    quad.refine(marked)
+    quad.balance()
+    assert quad.isbalanced()
+    # the full plane's regrid: the images of the quadrant's new leaves
+    full, image, _ = unfolded_forest(quad)
+    assert full.isbalanced() and seam_conforming(full, d1, d2)
+    moved = []
+    for forest, old, host, x in ((quad, old_q, hq, fs), (full, old_f, hf, ff)):
+        t = RegridTransfer(forest, old, x.G, x.centering, x.T, OPS4)
+        new = np.full((forest.nleaves(),) + tuple(x.work.shape[1:]), np.nan, x.T)
+        moved.append(oracle_regrid(t, host, new, x.nvars))
+    nq = FieldSet(quad, fs.nvars, G=2, parity=fs.parities, rotation=fs.rotation)
+    nq.work = torch.from_numpy(moved[0])
+    nf = FieldSet(full, ff.nvars, G=2, parity=ff.parities)
+    nf.work = torch.from_numpy(moved[1])
+    # the moved own points, then everything after a fill
+    findex = {k: i for i, k in enumerate(full.leaves)}
+    own = (slice(None),) + tuple(slice(2, 2 + quad.N) for _ in range(D))
+    worst = 0.0
+    for b, k in enumerate(quad.leaves):
+        g, w = moved[0][b][own], moved[1][findex[image(k, 0)]][own]
+        worst = max(worst, float(np.max(np.abs(g - w))))
+    assert worst < 1e-13
+    got = zero_hook_fill(GhostSchedule(nq, OPS4), nq)
+    want = zero_hook_fill(GhostSchedule(nf, OPS4), nf)
+    _agree(quad, full, image, got, want)
