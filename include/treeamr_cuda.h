@@ -210,14 +210,25 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
  * the ghosts' own adjoints are zeroed.  Same arguments as tam_fill; `y`
  * has the layout of `work`.  The library allocates its scratch on the
  * first call with a given nvars (so make that call before any stream
- * capture).  A schedule with a turned group (a seam) is refused with
- * TAM_EUNSUPPORTED. */
+ * capture).  A schedule with a turned group (a seam) needs the variable
+ * table: use tam_fill_adjoint_ex. */
 int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                      const void *factors, int32_t first_stage, int32_t last_stage,
                      void *stream);
 
 /* Scratch bytes tam_fill_adjoint_scratch needs for `nvars` variables. */
 int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes);
+
+/* The adjoint with the variable table of a schedule that turns transfers
+ * across a seam (the field set's rotvars, as tam_fill_ex takes it; NULL
+ * without turned groups), with the caller's scratch, or, when `scratch` is
+ * NULL, the library's own.  A turned group's transpose adds onto its real
+ * source in the set's own array, so a RotationPair member (a layout not
+ * symmetric in the seam's plane) is refused with TAM_EUNSUPPORTED. */
+int tam_fill_adjoint_ex(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                        const void *factors, const int32_t *rotvars, int32_t first_stage,
+                        int32_t last_stage, void *scratch, size_t scratch_bytes,
+                        void *stream);
 
 /* tam_fill_adjoint with caller-owned device scratch of at least
  * tam_adjoint_scratch_bytes; allocates nothing per call. */

@@ -65,6 +65,9 @@ def lib():
         l.oracle_fill_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                           C.c_int32, C.c_int32]
         l.oracle_fill_adjoint.restype = C.c_int
+        l.oracle_fill_adjoint_turned.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                                 C.c_void_p, C.c_int32, C.c_int32]
+        l.oracle_fill_adjoint_turned.restype = C.c_int
         _lib = l
     return _lib
 
@@ -113,12 +116,15 @@ def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=A
 
 
 def fill_adjoint(schedule, y: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
-                 last=ALL_LAST) -> np.ndarray:
+                 last=ALL_LAST, rotvars=None) -> np.ndarray:
     assert y.flags.c_contiguous and y.dtype == np.dtype(schedule.T)
     d = _descriptor(schedule)
     f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=y.dtype)
-    rc = lib().oracle_fill_adjoint(C.addressof(d.desc), y.ctypes.data, nvars, f.ctypes.data,
-                                   first, last)
+    rv = None if rotvars is None else \
+        np.ascontiguousarray(np.asfortranarray(rotvars).ravel(order="F"), dtype=np.int32)
+    rc = lib().oracle_fill_adjoint_turned(C.addressof(d.desc), y.ctypes.data, nvars,
+                                          f.ctypes.data, None if rv is None else rv.ctypes.data,
+                                          first, last)
     if rc != 0:
         raise RuntimeError("oracle_fill_adjoint failed")
     return y

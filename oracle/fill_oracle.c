@@ -248,7 +248,8 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
  * Stages run in reverse tag order. */
 #define DEFINE_ADJOINT(T, SUFFIX)                                                               \
   static void adjoint_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *y,            \
-                                     int32_t nvars, const T *factors) {                         \
+                                     int32_t nvars, const T *factors,                           \
+                                     const int32_t *rotvars) {                                  \
     const int D = d->ndim;                                                                      \
     int64_t S[3] = {1, 1, 1};                                                                   \
     for (int k = 0; k < D; ++k) S[k] = d->stored[k];                                            \
@@ -263,6 +264,17 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
           n[k] = g->stencil[k].ntarget;                                                         \
           o[k] = g->stencil[k].order;                                                           \
           tf[k] = g->stencil[k].targetfirst - 1;                                                \
+        }                                                                                       \
+        /* a turned group scatters onto its real source (a set symmetric in   \
+           the seam's plane: the real array is y itself) */                   \
+        int64_t vst[3] = {1, s2, s3}, c0 = 0;                                                   \
+        if (g->orientation) {                                                                   \
+          const int64_t rst[3] = {1, s2, s3};                                                   \
+          for (int e = 0; e < D; ++e) {                                                         \
+            const int p = (g->axes >> (2 * e)) & 3, f = (g->axes >> (8 + e)) & 1;              \
+            vst[p] = f ? -rst[e] : rst[e];                                                      \
+            if (f) c0 += rst[e] * (S[e] - 1);                                                   \
+          }                                                                                     \
         }                                                                                       \
         for (int64_t t = 0; t < g->ntransfers; ++t) {                                           \
           const int64_t tb = d->targetblocks[g->first + t] - 1;                                 \
@@ -286,14 +298,17 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
                     base[k] = d->srcstart[g->stencil[k].srcstart + idx[k]] - 1;                 \
                     wc[k] = W + g->stencil[k].weights + (int64_t)o[k] * idx[k];                 \
                   }                                                                             \
-                  T *ys = y + sb * bs + v * vs + base[0] + base[1] * s2 + base[2] * s3;         \
+                  const int sv =                                                                \
+                      g->orientation ? rotvars[v + (int64_t)nvars * g->orientation] - 1 : v;    \
+                  T *ys = y + sb * bs + sv * vs + c0 + base[0] * vst[0] + base[1] * vst[1] +    \
+                          base[2] * vst[2];                                                     \
                   for (int m3 = 0; m3 < o[2]; ++m3)                                             \
                     for (int m2 = 0; m2 < o[1]; ++m2)                                           \
                       for (int m1 = 0; m1 < o[0]; ++m1) {                                       \
                         T wp = wc[0][m1];                                                       \
                         if (D >= 2) wp = wp * wc[1][m2];                                        \
                         if (D >= 3) wp = wp * wc[2][m3];                                        \
-                        ys[m1 + m2 * s2 + m3 * s3] += wp * a;                                   \
+                        ys[m1 * vst[0] + m2 * vst[1] + m3 * vst[2]] += wp * a;                  \
                       }                                                                         \
                 }                                                                               \
         }                                                                                       \
@@ -303,17 +318,32 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
 DEFINE_ADJOINT(double, f64)
 DEFINE_ADJOINT(float, f32)
 
-int oracle_fill_adjoint(const tam_schedule_desc *d, void *y, int32_t nvars, const void *factors,
-                        int32_t first, int32_t last) {
+/* rotvars: the variable table of turned groups (NULL without any); a turned
+ * group must keep the stored extents (a set symmetric in the seam's plane) */
+int oracle_fill_adjoint_turned(const tam_schedule_desc *d, void *y, int32_t nvars,
+                               const void *factors, const int32_t *rotvars, int32_t first,
+                               int32_t last) {
   if (!d || !y || nvars < 1) return -1;
+  for (int32_t gi = 0; gi < d->ngroups; ++gi) {
+    const tam_group *g = &d->groups[gi];
+    if (!g->orientation) continue;
+    if (!rotvars) return -1;
+    for (int e = 0; e < d->ndim; ++e)
+      if (d->stored[(g->axes >> (2 * e)) & 3] != d->stored[e]) return -1;
+  }
   int32_t tags[128];
   int nt = collect_tags(d, tags, 128);
   for (int i = nt - 1; i >= 0; --i) {
     if (tags[i] < first || tags[i] > last) continue;
     if (d->dtype == TAM_F64)
-      adjoint_stage_f64(d, tags[i], (double *)y, nvars, (const double *)factors);
+      adjoint_stage_f64(d, tags[i], (double *)y, nvars, (const double *)factors, rotvars);
     else
-      adjoint_stage_f32(d, tags[i], (float *)y, nvars, (const float *)factors);
+      adjoint_stage_f32(d, tags[i], (float *)y, nvars, (const float *)factors, rotvars);
   }
   return 0;
+}
+
+int oracle_fill_adjoint(const tam_schedule_desc *d, void *y, int32_t nvars, const void *factors,
+                        int32_t first, int32_t last) {
+  return oracle_fill_adjoint_turned(d, y, nvars, factors, NULL, first, last);
 }

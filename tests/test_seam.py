@@ -784,3 +784,65 @@ def test_a_regrid_across_the_seam_is_the_full_planes(D, plane, other):
     got = zero_hook_fill(GhostSchedule(nq, OPS4), nq)
     want = zero_hook_fill(GhostSchedule(nf, OPS4), nf)
     _agree(quad, full, image, got, want)
+
+
+# --- the adjoint across the seam -------------------------------------------------------------
+
+def _dot(a, b):
+    return float(np.dot(a.ravel().astype(np.float64), b.ravel().astype(np.float64)))
+
+
+@pytest.mark.parametrize("case", [("q",) + c for c in SEAM_CASES[:4]] +
+                         [("h",) + c for c in HALF_CASES[:3]])
+def test_oracle_adjoint_dot_product_across_the_seam(case):
+    """``<A x, y> = <x, A^T y>`` to 1e-13 with turned transfers, A the
+    oracle's fill and A^T its scatter-form transpose through the axis map
+    and the variable table."""
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h")
+    rng = np.random.default_rng(17)
+    x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    ax = oracle.fill(s, x.copy(), fs.nvars, fs.factors_host, rotvars=fs.rotvars_host)
+    aty = oracle.fill_adjoint(s, y.copy(), fs.nvars, fs.factors_host, rotvars=fs.rotvars_host)
+    lhs, rhs = _dot(ax, y), _dot(x, aty)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [("q",) + c for c in SEAM_CASES] +
+                         [("h",) + c for c in HALF_CASES])
+def test_gpu_adjoint_across_the_seam(cuda_lib, case):
+    """The device adjoint of a turned schedule: the dot-product test against
+    the device forward fill to 1e-13, and the oracle's scatter-form
+    transpose to the sums' rounding."""
+    from treeamr import fill_ghosts
+    from treeamr.adjoint import fill_ghosts_adjoint
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h")
+    rng = np.random.default_rng(23)
+    x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    fs.factors, fs.rotvars = fs.factors.cuda(), fs.rotvars.cuda()
+    fs.work = torch.from_numpy(x.copy()).cuda()
+    fill_ghosts(fs, s)
+    ax = fs.work.cpu().numpy()
+    yd = torch.from_numpy(y.copy()).cuda()
+    fs.work = torch.from_numpy(x.copy()).cuda()
+    fill_ghosts_adjoint(fs, s, yd)
+    torch.cuda.synchronize()
+    aty = yd.cpu().numpy()
+    lhs, rhs = _dot(ax, y), _dot(x, aty)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+    want = oracle.fill_adjoint(s, y.copy(), fs.nvars, fs.factors_host, rotvars=fs.rotvars_host)
+    assert np.max(np.abs(aty - want)) < 1e-13
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_of_a_pair_member_is_refused(cuda_lib):
+    from treeamr.adjoint import fill_ghosts_adjoint
+    quad, pair, (sa, sb), ops = pair_case(2, (1, 2), "none")
+    a = pair.a
+    a.work, a.factors, a.rotvars = a.work.cuda(), a.factors.cuda(), a.rotvars.cuda()
+    with pytest.raises(Exception, match="RotationPair"):
+        fill_ghosts_adjoint(a, sa, torch.zeros_like(a.work))

@@ -81,6 +81,7 @@ struct AdjArgs {
   const int2 *__restrict__ ent;
   const int64_t *__restrict__ scr;
   const Member *__restrict__ members;  // a batch's, or null
+  const int32_t *__restrict__ rotvars; // turned groups' variable table, or null
 };
 
 // Where a transfer's field data and factors are: the kernel's own layout for
@@ -234,8 +235,15 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
         const int rr = pt - j3 * f01;
         const int j2 = rr / f0;
         const int j1 = rr - j2 * f0;
-        T *dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
-                 (int64_t)(h.flo[2] + j3) * L.s3;
+        T *dst;
+        if (h.col) {  // a turned group: through the axis map and the variable table
+          const int sv = __ldg(a.rotvars + v + (int64_t)nvars * h.col) - 1;
+          dst = yb + sv * L.vs + h.tc0 + h.tvs[0] * (h.flo[0] + j1) +
+                h.tvs[1] * (h.flo[1] + j2) + h.tvs[2] * (h.flo[2] + j3);
+        } else {
+          dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
+                (int64_t)(h.flo[2] + j3) * L.s3;
+        }
         *dst = A::add(*dst, src[p]);
       }
       __syncthreads();
@@ -270,11 +278,39 @@ __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restric
   }
 }
 
+// Zero the targets of a stage's turned groups (they have no forward tiles):
+// group turns[blockIdx.y], every transfer, point and variable.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    adjoint_zero_turned_kernel(const TurnGroup *__restrict__ turns, const DevGroup *groups,
+                               const int32_t *__restrict__ tb, T *y, int nvars, int S1, int S2,
+                               int S3) {
+  const DevGroup &g = groups[turns[blockIdx.y].group];
+  const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
+  const int64_t items = box * nvars * g.ntransfers;
+  const int64_t vol = (int64_t)S1 * S2 * S3;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = it;
+    const int i1 = (int)(r % g.n[0]);
+    r /= g.n[0];
+    const int i2 = (int)(r % g.n[1]);
+    r /= g.n[1];
+    const int i3 = (int)(r % g.n[2]);
+    r /= g.n[2];
+    const int v = (int)(r % nvars);
+    const int64_t t = r / nvars + g.first;
+    const int64_t tblock = __ldg(tb + t) - 1;
+    y[(tblock * nvars + v) * vol + ((int64_t)(g.tf[2] + i3) * S2 + (g.tf[1] + i2)) * S1 +
+      g.tf[0] + i1] = T(0);
+  }
+}
+
 template <typename T, int D, bool BATCH>
 cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const T *factors,
                       int32_t first, int32_t last, T *scratch, cudaStream_t stream) {
   const AdjArgs<T> a{r.groups, p.groups, r.tb, (const T *)r.weights,
-                     p.off,    (const int2 *)p.ent, p.scr, r.members};
+                     p.off,    (const int2 *)p.ent, p.scr, r.members, r.rotvars};
   const int S1 = r.S[0], S2 = r.S[1], S3 = r.S[2];
   const int threads = 256, wpb = threads / 32;
   // stages in reverse order
@@ -308,6 +344,12 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
       const int64_t blocks = std::min<int64_t>((fw.ntiles + wpb - 1) / wpb, (int64_t)1 << 30);
       adjoint_zero_kernel<T, D, BATCH><<<(unsigned)blocks, threads, 0, stream>>>(
           r.fwd_tiles + fw.tile0, fw.ntiles, a, y, nvars, S1, S2, S3);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (fw.nturn > 0 && r.turns) {
+      adjoint_zero_turned_kernel<T><<<dim3(64, (unsigned)fw.nturn), threads, 0, stream>>>(
+          r.turns + fw.turn0, r.groups, r.tb, y, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -412,6 +454,14 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
       err = "the adjoint's transposed stencils exceed 2^31 entries";
       return TAM_EUNSUPPORTED;
     }
+  }
+  // turned groups: their footprints land on the real source through the
+  // strides the forward launch reads it by
+  for (const TurnGroup &t : s->h_turns) {
+    AdjGroup &a = o.ag[t.group];
+    a.col = t.col;
+    for (int d = 0; d < 3; ++d) a.tvs[d] = t.vs[d];
+    a.tc0 = t.c0;
   }
   o.scr.assign(s->ntransfers, 0);
   for (const Stage &fw : s->stages) {
@@ -611,10 +661,11 @@ cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int 
                : run_dim<float, false>(plan, r, y, nvars, factors, first, last, scratch, stream);
 }
 
-cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
-                        int32_t last, void *scratch, cudaStream_t stream) {
+cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
+                        const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
+                        cudaStream_t stream) {
   AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
-           &s->stages, {s->S[0], s->S[1], s->S[2]}};
+           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_turns, rotvars};
   return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
 }
 
@@ -658,6 +709,11 @@ extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int
                "call tam_adjoint_scratch_bytes once first (it allocates)";
     return TAM_EINVAL;
   }
+  if (s->needs_rotvars) {
+    ctx->err = "tam_fill_adjoint_static: this schedule turns transfers across a seam; "
+               "use tam_fill_adjoint_ex with the variable table";
+    return TAM_EINVAL;
+  }
   const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > TAM_STATIC_SCRATCH_BYTES) {
     ctx->err = "tam_fill_adjoint_static: this schedule's adjoint needs " + std::to_string(need) +
@@ -696,8 +752,8 @@ extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int
     }
     scratch = g_static_ptr[ctx->device];
   }
-  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, first_stage, last_stage, scratch,
-                                   (cudaStream_t)stream);
+  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, nullptr, first_stage, last_stage,
+                                   scratch, (cudaStream_t)stream);
   if (prev != ctx->device) cudaSetDevice(prev);
   if (e != cudaSuccess) {
     cudaGetLastError();

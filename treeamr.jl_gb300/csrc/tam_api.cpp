@@ -640,9 +640,16 @@ void tam_schedule_free(tam_sched *s) {
 
 static int adjoint_ready(tam_sched *s) {
   if (s->adj.ready) return TAM_OK;
-  if (s->needs_rotvars)
-    return fail(s->ctx, TAM_EUNSUPPORTED,
-                "the adjoint of a schedule with transfers turned across a seam is not built");
+  // a turned group's transpose writes into the set's own array: the layout
+  // must be symmetric in the seam's plane (not a RotationPair member)
+  for (const tam_group &h : s->host_groups) {
+    if (!h.orientation) continue;
+    for (int e = 0; e < s->D; ++e)
+      if (s->S[(h.axes >> (2 * e)) & 3] != s->S[e])
+        return fail(s->ctx, TAM_EUNSUPPORTED,
+                    "the adjoint of a RotationPair member (a layout not symmetric in the "
+                    "seam's plane) is not built");
+  }
   std::string err;
   int rc = tam::adjoint_prepare(s, err);
   if (rc != TAM_OK) return fail(s->ctx, rc, err);
@@ -661,12 +668,21 @@ int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes) {
 
 static int check_fill_args(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
                            const void *factors);
+static int owned_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                         const void *factors, const int32_t *rotvars, int32_t first_stage,
+                         int32_t last_stage, void *stream);
 
-int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
-                             const void *factors, int32_t first_stage, int32_t last_stage,
-                             void *scratch, size_t scratch_bytes, void *stream) {
+// The adjoint with the caller's scratch (which may be NULL only when the
+// schedule needs none).
+static int adjoint_with(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                        const void *factors, const int32_t *rotvars, int32_t first_stage,
+                        int32_t last_stage, void *scratch, size_t scratch_bytes, void *stream) {
   int rc = check_fill_args(s, y, nvars, nblocks, factors);
   if (rc != TAM_OK) return rc;
+  if (s->needs_rotvars && !rotvars)
+    return fail(s->ctx, TAM_EINVAL,
+                "this schedule turns ghosts across a rotating seam, but no variable table was "
+                "given: use tam_fill_adjoint_ex");
   DeviceGuard guard(s->ctx->device);
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
   rc = adjoint_ready(s);
@@ -674,19 +690,49 @@ int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nbloc
   const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > 0 && (!scratch || scratch_bytes < need))
     return fail(s->ctx, TAM_EINVAL, "adjoint scratch smaller than tam_adjoint_scratch_bytes");
-  cudaError_t e =
-      tam::adjoint_run(s, y, nvars, factors, first_stage, last_stage, scratch, (cudaStream_t)stream);
+  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, rotvars, first_stage, last_stage,
+                                   scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "adjoint launch");
   return TAM_OK;
 }
 
+int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                             const void *factors, int32_t first_stage, int32_t last_stage,
+                             void *scratch, size_t scratch_bytes, void *stream) {
+  return adjoint_with(s, y, nvars, nblocks, factors, nullptr, first_stage, last_stage, scratch,
+                      scratch_bytes, stream);
+}
+
+int tam_fill_adjoint_ex(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                        const void *factors, const int32_t *rotvars, int32_t first_stage,
+                        int32_t last_stage, void *scratch, size_t scratch_bytes, void *stream) {
+  if (!scratch) {
+    int rc = check_fill_args(s, y, nvars, nblocks, factors);
+    if (rc != TAM_OK) return rc;
+    return owned_adjoint(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage,
+                         stream);
+  }
+  return adjoint_with(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage, scratch,
+                      scratch_bytes, stream);
+}
+
 int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, const void *factors,
                      int32_t first_stage, int32_t last_stage, void *stream) {
-  int rc = check_fill_args(s, y, nvars, nblocks, factors);
-  if (rc != TAM_OK) return rc;
+  return tam_fill_adjoint_ex(s, y, nvars, nblocks, factors, nullptr, first_stage, last_stage,
+                             nullptr, 0, stream);
+}
+
+// The adjoint with the library's own scratch, grown on demand.
+static int owned_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+                         const void *factors, const int32_t *rotvars, int32_t first_stage,
+                         int32_t last_stage, void *stream) {
+  if (s->needs_rotvars && !rotvars)
+    return fail(s->ctx, TAM_EINVAL,
+                "this schedule turns ghosts across a rotating seam, but no variable table was "
+                "given: use tam_fill_adjoint_ex");
   DeviceGuard guard(s->ctx->device);
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
-  rc = adjoint_ready(s);
+  int rc = adjoint_ready(s);
   if (rc != TAM_OK) return rc;
   const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > s->adj_scratch_bytes) {
@@ -700,8 +746,8 @@ int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, cons
     if (e != cudaSuccess) return fail(s->ctx, TAM_ENOMEM, "adjoint scratch allocation failed");
     s->adj_scratch_bytes = need;
   }
-  return tam_fill_adjoint_scratch(s, y, nvars, nblocks, factors, first_stage, last_stage,
-                                  s->adj_scratch, s->adj_scratch_bytes, stream);
+  return adjoint_with(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage,
+                      s->adj_scratch, s->adj_scratch_bytes, stream);
 }
 
 int tam_schedule_info(const tam_sched *s, int64_t *ngroups, int64_t *ntransfers, int64_t *points,

@@ -343,7 +343,7 @@ int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32
     b->adj_scratch_bytes = need;
   }
   const tam::AdjRun r{b->dtype, b->D, b->d_groups, b->d_tb, b->d_weights, b->d_members,
-                      b->d_tiles, &b->stages, {1, 1, 1}};
+                      b->d_tiles, &b->stages, {1, 1, 1}, nullptr, nullptr};
   cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena, first_stage,
                                         last_stage, b->adj_scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) {

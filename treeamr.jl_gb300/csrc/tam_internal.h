@@ -151,6 +151,13 @@ struct AdjGroup {
   int32_t fn[3];
   int64_t off[3];    // offset into the row-offset pool (fn + 1 entries)
   int64_t fsize;     // footprint points: fn[0] * fn[1] * fn[2]
+  // A turned group: its footprint (virtual rows) lands on the real source
+  // at tc0 + sum_d tvs[d] * row[d], real variable rotvars[v + nvars * col] - 1
+  // (col 0: an ordinary group, the footprint in place).
+  int32_t col;
+  int32_t pad;
+  int64_t tvs[3];
+  int64_t tc0;
 };
 
 // One stage of the adjoint: its transfers for pass 1 (a CTA each), and the
@@ -299,8 +306,9 @@ cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mi
 // The adjoint (tam_adjoint.cu).
 int adjoint_prepare(tam_sched *s, std::string &err);
 void adjoint_free(tam_sched *s);
-cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors, int32_t first,
-                        int32_t last, void *scratch, cudaStream_t stream);
+cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
+                        const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
+                        cudaStream_t stream);
 
 // A batch's plan from its members' (each member's groups, transfers and
 // weights at the given bases of the batch's concatenated arrays; `stages`
@@ -322,6 +330,8 @@ struct AdjRun {
   const Tile *fwd_tiles;           // the forward fill's tiles (the zero pass)
   const std::vector<Stage> *fwd_stages;
   int S[3];                        // stored extents (a batch: each member's own)
+  const TurnGroup *turns;          // the turned groups (their targets are zeroed too)
+  const int32_t *rotvars;          // the variable table of turned groups, or null
 };
 cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,
                              const void *factors, int32_t first, int32_t last, void *scratch,

@@ -34,7 +34,8 @@ def fill_ghosts_adjoint(fs: FieldSet, schedule: GhostSchedule, y: Optional[torch
         raise ValueError("the adjoint vector must be contiguous")
     ds = device_schedule(schedule, y.device.index or 0)
     ds.run_adjoint(y, fs.nvars, fs.factors, _native.TAM_STAGE_ALL_FIRST,
-                   _native.TAM_STAGE_ALL_LAST, stream, scratch)
+                   _native.TAM_STAGE_ALL_LAST, stream, scratch,
+                   rotvars=getattr(fs, "rotvars", None))
     return y
 
 
