@@ -563,9 +563,9 @@ def test_gpu_turned_fill_bit_exact(cuda_lib, case, T):
 
 @pytest.mark.gpu
 def test_gpu_turned_fill_refusals(cuda_lib):
-    """Without the variable table the library refuses a turned schedule;
-    an asymmetric set is refused alone (``test/rotate_tests.jl:526-559``);
-    the adjoint of a turned schedule is not built."""
+    """Without the variable table the library refuses a turned schedule,
+    forward and adjoint; an asymmetric set is refused alone
+    (``test/rotate_tests.jl:526-559``)."""
     from treeamr import fill_ghosts
     from treeamr.ghosts import device_schedule
     quad, fs, s, *_ = quadrant_case(2, (1, 2), "none")
@@ -578,8 +578,10 @@ def test_gpu_turned_fill_refusals(cuda_lib):
     rc = ds.lib.tam_fill(ds.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars, fs.nblocks(),
                          C.c_void_p(fs.factors.data_ptr()), -1, 0x7FFFFFFF, None)
     assert rc != 0
-    with pytest.raises(Exception, match="not built"):
-        ds.adjoint_scratch_bytes(fs.nvars)
+    rc = ds.lib.tam_fill_adjoint(ds.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars,
+                                 fs.nblocks(), C.c_void_p(fs.factors.data_ptr()), -1,
+                                 0x7FFFFFFF, None)
+    assert rc != 0
     fs.rotvars = rv
     f = Forest((2, 2), N=8, rotating=(1, 2))
     asym = FieldSet(f, 1, G=(1, 2), rotation=(1,), device="cuda")
