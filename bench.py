@@ -651,7 +651,34 @@ def main():
                "api": "tam_fill_host (C ABI, host buffers) through treeamr.host.HostPipeline, "
                       "3 streams and device buffers",
                "single_step_ms": ms_single}
-        del pipe, host_in, host_out
+        del pipe
+        torch.cuda.empty_cache()
+        # the host link's own rate, the e2e step's floor: an upload and a
+        # download of the field data at once, on two streams (copy engines)
+        dbuf = torch.empty_like(fs.work)
+        s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+
+        def link(up=True, down=True):
+            s_up.wait_stream(stream)
+            s_down.wait_stream(stream)
+            if up:
+                with torch.cuda.stream(s_up):
+                    dbuf.copy_(host_in, non_blocking=True)
+            if down:
+                with torch.cuda.stream(s_down):
+                    host_out[0].copy_(fs.work, non_blocking=True)
+            stream.wait_stream(s_up)
+            stream.wait_stream(s_down)
+        link()
+        ms_up = timed(lambda: link(down=False), 3)
+        ms_down = timed(lambda: link(up=False), 3)
+        ms_both = timed(link, 3)
+        gb = field_bytes / 1e9
+        e2e["host_link"] = {"h2d_gbs": gb / (ms_up * 1e-3), "d2h_gbs": gb / (ms_down * 1e-3),
+                            "both_each_way_gbs": gb / (ms_both * 1e-3),
+                            "floor_ms_per_step": ms_both,
+                            "frac": ms_both / ms_e2e}
+        del dbuf, host_in, host_out
         torch.cuda.empty_cache()
 
     cpu = None
