@@ -674,10 +674,15 @@ def main():
         ms_down = timed(lambda: link(up=False), 3)
         ms_both = timed(link, 3)
         gb = field_bytes / 1e9
+        # a step moves the field data up and down: its floor is the two copies
+        # one after the other, or together where the link carries both at once
+        floor = min(ms_up + ms_down, ms_both)
         e2e["host_link"] = {"h2d_gbs": gb / (ms_up * 1e-3), "d2h_gbs": gb / (ms_down * 1e-3),
                             "both_each_way_gbs": gb / (ms_both * 1e-3),
-                            "floor_ms_per_step": ms_both,
-                            "frac": ms_both / ms_e2e}
+                            "serial_floor_ms": ms_up + ms_down,
+                            "concurrent_floor_ms": ms_both,
+                            "floor_ms_per_step": floor,
+                            "frac": floor / ms_e2e}
         del dbuf, host_in, host_out
         torch.cuda.empty_cache()
 
