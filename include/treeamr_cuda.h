@@ -73,7 +73,15 @@ typedef struct tam_group {
   int32_t kind;      /* tam_kind                                          */
   int32_t stage;     /* stage tag (transfer_stage, src/schedule.jl:656)   */
   int32_t factorcol; /* 0, or the 1-based factor-table column             */
-  int32_t bounded;   /* must be 0: bounded operators are not built        */
+  /* 0, or how the kernel bounds the result (boundedmode,
+   * src/operators.jl:417-441): 1 the bounded conservative prolongation
+   * (order-3 stencils, the parent at the window's middle row,
+   * src/ghosts.jl:291-310), 2 the point-value sum clamped into its bracket
+   * (stencils of 2p rows: the order-p weights, then the linear ones over the
+   * same window, src/ghosts.jl:311-361).  A bounded group runs in a launch of
+   * its own after its stage's fused launches; a schedule with one has no
+   * adjoint. */
+  int32_t bounded;
   /* A turned group (across a rotating or half-turn seam, TransferGroup's
    * orientation/perm/flip, src/schedule.jl:150-197, src/ghosts.jl:183-244):
    * orientation r in 1..3 (0: an ordinary group), and its axis map in

@@ -27,6 +27,8 @@
  *   - exchange_ghosts!       src/ghosts.jl:1099-1160: stages in tag order
  *   - RotatedSource          src/ghosts.jl:183-244: a turned group's source
  *                            read through its axis map and variable table
+ *   - bounded_sum,           src/ghosts.jl:291-361: the bounded operators'
+ *     bracket_clamp_sum      kernels, with Julia's min and max
  *   - the adjoint (transpose) of the same linear map, stage by stage in
  *     reverse, in scatter form: a new capability with no reference
  *     counterpart, so its oracle is the linear algebra of the forward.
@@ -34,6 +36,7 @@
  * Build: see oracle/build.py.  Compiled with -ffp-contract=off so that no
  * multiply-add is fused on any host architecture.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -62,6 +65,30 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
   }
   return lo;
 }
+
+/* Julia's min and max of two floats (NaN-propagating, -0 below +0), which the
+ * bounded operators' extremes follow (src/ghosts.jl:291-361), and minmod and
+ * the monotonized central slope (src/ghosts.jl:291-292). */
+#define DEFINE_BOUNDED_HELPERS(T, SUFFIX, ABS)                                                  \
+  static inline T jmin_##SUFFIX(T x, T y) {                                                    \
+    const int c = (y < x) || (signbit(y) && !signbit(x));                                       \
+    return c ? (isnan(x) ? x : y) : (isnan(y) ? y : x);                                         \
+  }                                                                                             \
+  static inline T jmax_##SUFFIX(T x, T y) {                                                    \
+    const int c = (y > x) || (!signbit(y) && signbit(x));                                       \
+    return c ? (isnan(x) ? x : y) : (isnan(y) ? y : x);                                         \
+  }                                                                                             \
+  static inline T minmod_##SUFFIX(T a, T b) {                                                  \
+    return (a > 0 && b > 0) ? jmin_##SUFFIX(a, b)                                               \
+           : (a < 0 && b < 0) ? jmax_##SUFFIX(a, b) : (T)0;                                     \
+  }                                                                                             \
+  static inline T mc_##SUFFIX(T a, T b) {                                                      \
+    return minmod_##SUFFIX((T)2 * a, minmod_##SUFFIX((T)2 * b, (a + b) / (T)2));                \
+  }                                                                                             \
+  static inline T abs_##SUFFIX(T x) { return ABS(x); }
+
+DEFINE_BOUNDED_HELPERS(double, f64, fabs)
+DEFINE_BOUNDED_HELPERS(float, f32, fabsf)
 
 #define DEFINE_ORACLE(T, SUFFIX)                                                                \
   static void run_transfers_##SUFFIX(const tam_schedule_desc *d, const tam_group *g,            \
@@ -130,7 +157,59 @@ static int64_t lower_bound(const int32_t *list, int64_t lo, int64_t hi, int64_t 
               const T *src = from + sb * bs + sv * vs + c0 + base[0] * vst[0] +                 \
                              base[1] * vst[1] + base[2] * vst[2];                               \
               T acc = (T)0;                                                                     \
-              if (unit) {                                                                       \
+              if (g->bounded == 1) {                                                            \
+                /* bounded_sum (src/ghosts.jl:296-310): the parent at the      \
+                   window's middle row and its face neighbours */              \
+                const int64_t *st = vst;                                                        \
+                int64_t o0 = 0;                                                                 \
+                for (int k = 0; k < D; ++k) o0 += st[k];                                        \
+                const T u = src[o0];                                                            \
+                T lov[3], hiv[3], sl[3], M = u, m = u, dl = 0, S = 0;                           \
+                for (int k = 0; k < D; ++k) {                                                   \
+                  lov[k] = src[o0 - st[k]];                                                     \
+                  hiv[k] = src[o0 + st[k]];                                                     \
+                  sl[k] = mc_##SUFFIX(hiv[k] - u, u - lov[k]);                                  \
+                }                                                                               \
+                for (int k = 0; k < D; ++k) M = jmax_##SUFFIX(M, lov[k]);                       \
+                for (int k = 0; k < D; ++k) M = jmax_##SUFFIX(M, hiv[k]);                       \
+                for (int k = 0; k < D; ++k) m = jmin_##SUFFIX(m, lov[k]);                       \
+                for (int k = 0; k < D; ++k) m = jmin_##SUFFIX(m, hiv[k]);                       \
+                for (int k = D - 1; k >= 0; --k) { /* right folds */                          \
+                  const T sg = wc[k][2] > wc[k][0] ? sl[k] : -sl[k];                            \
+                  dl = k == D - 1 ? sg : sg + dl;                                               \
+                  S = k == D - 1 ? abs_##SUFFIX(sl[k]) : abs_##SUFFIX(sl[k]) + S;               \
+                }                                                                               \
+                dl = dl / (T)4;                                                                 \
+                S = S / (T)4;                                                                   \
+                T phi = 1;                                                                      \
+                if (S > 0) phi = jmin_##SUFFIX(jmin_##SUFFIX((T)1, (M - u) / S), (u - m) / S);  \
+                acc = (u + phi * dl) + (T)0 * (M - m);                                          \
+              } else if (g->bounded == 2) {                                                     \
+                /* bracket_clamp_sum (src/ghosts.jl:323-361): the full sum     \
+                   clamped into the points of nonzero linear weight */         \
+                int p[3] = {1, 1, 1};                                                           \
+                for (int k = 0; k < D; ++k) p[k] = o[k] / 2;                                    \
+                T blo = (T)INFINITY, bhi = -(T)INFINITY;                                        \
+                for (int m3 = 0; m3 < p[2]; ++m3)                                               \
+                  for (int m2 = 0; m2 < p[1]; ++m2)                                             \
+                    for (int m1 = 0; m1 < p[0]; ++m1) {                                         \
+                      T wp = wc[0][m1];                                                         \
+                      if (D >= 2) wp = wp * wc[1][m2];                                          \
+                      if (D >= 3) wp = wp * wc[2][m3];                                          \
+                      const T u = src[m1 * vst[0] + m2 * vst[1] + m3 * vst[2]];                 \
+                      T term = wp * u;                                                          \
+                      acc = acc + term;                                                         \
+                      const int in = wc[0][p[0] + m1] != (T)0 &&                                \
+                                     (D < 2 || wc[1][p[1] + m2] != (T)0) &&                     \
+                                     (D < 3 || wc[2][p[2] + m3] != (T)0);                       \
+                      if (in) {                                                                 \
+                        blo = jmin_##SUFFIX(blo, u);                                            \
+                        bhi = jmax_##SUFFIX(bhi, u);                                            \
+                      }                                                                         \
+                    }                                                                           \
+                const T cl = acc > bhi ? bhi : acc < blo ? blo : acc;                           \
+                acc = cl + (T)0 * (bhi - blo);                                                  \
+              } else if (unit) {                                                                \
                 acc = (T)0 + src[0];                                                            \
               } else {                                                                          \
                 for (int m3 = lo[2]; m3 < hi[2]; ++m3)                                          \

@@ -54,7 +54,8 @@ class _Concat:
                 return t.nnew + t.nold
         self.forest = F
         self.groups = [TransferGroup(g.key, g.stencils, g.targetblocks,
-                                     np.asarray(g.sourceblocks) + t.nnew, 0, REGRID_TAG)
+                                     np.asarray(g.sourceblocks) + t.nnew, 0, REGRID_TAG, None,
+                                     g.bounded)
                        for g in t.groups]
 
     def all_groups(self):

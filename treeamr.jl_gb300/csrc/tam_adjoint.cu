@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restric
 // group turns[blockIdx.y], every transfer, point and variable.
 template <typename T>
 __global__ void __launch_bounds__(256)
-    adjoint_zero_turned_kernel(const TurnGroup *__restrict__ turns, const DevGroup *groups,
+    adjoint_zero_solo_kernel(const SoloGroup *__restrict__ turns, const DevGroup *groups,
                                const int32_t *__restrict__ tb, T *y, int nvars, int S1, int S2,
                                int S3) {
   const DevGroup &g = groups[turns[blockIdx.y].group];
@@ -347,9 +347,9 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
-    if (fw.nturn > 0 && r.turns) {
-      adjoint_zero_turned_kernel<T><<<dim3(64, (unsigned)fw.nturn), threads, 0, stream>>>(
-          r.turns + fw.turn0, r.groups, r.tb, y, nvars, S1, S2, S3);
+    if (fw.nsolo > 0 && r.turns) {
+      adjoint_zero_solo_kernel<T><<<dim3(64, (unsigned)fw.nsolo), threads, 0, stream>>>(
+          r.turns + fw.solo0, r.groups, r.tb, y, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -457,7 +457,7 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
   }
   // turned groups: their footprints land on the real source through the
   // strides the forward launch reads it by
-  for (const TurnGroup &t : s->h_turns) {
+  for (const SoloGroup &t : s->h_solos) {
     AdjGroup &a = o.ag[t.group];
     a.col = t.col;
     for (int d = 0; d < 3; ++d) a.tvs[d] = t.vs[d];
@@ -665,7 +665,7 @@ cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
                         const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
                         cudaStream_t stream) {
   AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
-           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_turns, rotvars};
+           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars};
   return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
 }
 

@@ -75,7 +75,7 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_csingle);
   cudaFree(s->d_perm);
   cudaFree(s->d_err);
-  cudaFree(s->d_turns);
+  cudaFree(s->d_solos);
   tam::side_destroy(s->side);
   s->d_ptiles = nullptr;
   s->d_groups = nullptr;
@@ -86,7 +86,7 @@ void free_sched_device(tam_sched *s) {
   s->d_wtab = nullptr;
   s->d_csingle = s->d_perm = nullptr;
   s->d_err = nullptr;
-  s->d_turns = nullptr;
+  s->d_solos = nullptr;
 }
 
 // Every check that makes a fill memory-safe: indices into the pools, block
@@ -134,8 +134,8 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
   for (int32_t gi = 0; gi < d->ngroups; ++gi) {
     const tam_group &g = d->groups[gi];
     if (g.kind < TAM_COPY || g.kind > TAM_PROLONG) return fail(ctx, TAM_EINVAL, "bad group kind");
-    if (g.bounded != 0)
-      return fail(ctx, TAM_EUNSUPPORTED, "bounded operators are not part of this engine");
+    if (g.bounded < 0 || g.bounded > 2)
+      return fail(ctx, TAM_EINVAL, "a group's bound must be 0, 1 or 2");
     if (g.factorcol < 0 || g.factorcol > maxcols)
       return fail(ctx, TAM_EINVAL, "factor column outside the table");
     if (g.first < 0 || g.ntransfers < 0 || g.first + g.ntransfers > d->ntransfers)
@@ -179,6 +179,14 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
                  s.order);
         return fail(ctx, TAM_EINVAL, buf);
       }
+      if (g.bounded == 1 && (s.order != 3 || s.unit))
+        return fail(ctx, TAM_EINVAL,
+                    "a bounded conservative group has order-3 stencils in every dimension");
+      if (g.bounded == 2 && (s.order % 2 || s.unit))
+        return fail(ctx, TAM_EINVAL,
+                    "a bounded point-value group's stencils stack two sets of weights");
+      // the source window: a stacked point-value stencil reads half its rows
+      const int win = g.bounded == 2 ? s.order / 2 : s.order;
       if (s.targetfirst < 1 || s.targetfirst + s.ntarget - 1 > S)
         return fail(ctx, TAM_EINVAL, "target rows outside the stored extent");
       if (s.srcstart < 0 || s.srcstart + s.ntarget > d->nsrcstart)
@@ -187,10 +195,10 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
         return fail(ctx, TAM_EINVAL, "weight offset outside the pool");
       for (int i = 0; i < s.ntarget; ++i) {
         const int32_t b = d->srcstart[s.srcstart + i];
-        if (b < 1 || b + s.order - 1 > S) {
+        if (b < 1 || b + win - 1 > S) {
           snprintf(buf, sizeof buf,
                    "group %d dim %d row %d: source window %d:%d outside 1:%d", gi, k + 1, i + 1,
-                   b, b + s.order - 1, S);
+                   b, b + win - 1, S);
           return fail(ctx, TAM_EINVAL, buf);
         }
       }
@@ -370,24 +378,26 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
   return tiles;
 }
 
-// The turned groups of every stage (TurnGroup): the axis map folded into
-// signed strides of the real array, whose stored extent along e is
-// R_e = S[perm[e]].  Virtual stored index k (1-based) along virtual
-// dimension perm[e] reads real index k, or R_e + 1 - k where flip[e], along
-// e; with j = k - 1 the real offset is
+// The solo groups of every stage (SoloGroup): turned or bounded.  A turned
+// group's axis map is folded into signed strides of the real array, whose
+// stored extent along e is R_e = S[perm[e]].  Virtual stored index k
+// (1-based) along virtual dimension perm[e] reads real index k, or
+// R_e + 1 - k where flip[e], along e; with j = k - 1 the real offset is
 //   sum_e stride_e * (flip[e] ? R_e - 1 - j : j),   stride = (1, R_0, R_0 R_1),
 // so vs[perm[e]] = +-stride_e and c0 = sum over flipped e of stride_e (R_e - 1).
-void build_turns(tam_sched *s) {
-  s->h_turns.clear();
+// An untouched group (a bounded one off the seam) has the identity.
+void build_solos(tam_sched *s) {
+  s->h_solos.clear();
   for (tam::Stage &st : s->stages) {
-    st.turn0 = (int64_t)s->h_turns.size();
+    st.solo0 = (int64_t)s->h_solos.size();
     for (int32_t gi : st.groups) {
       const tam_group &h = s->host_groups[gi];
-      if (h.orientation == 0) continue;
-      tam::TurnGroup t{};
+      if (h.orientation == 0 && h.bounded == 0) continue;
+      tam::SoloGroup t{};
       t.group = gi;
       t.col = h.orientation;
       t.odd = h.orientation & 1;
+      t.bounded = h.bounded;
       int R[3] = {1, 1, 1};
       for (int e = 0; e < s->D; ++e) R[e] = s->S[(h.axes >> (2 * e)) & 3];
       const int64_t stride[3] = {1, R[0], (int64_t)R[0] * R[1]};
@@ -401,9 +411,9 @@ void build_turns(tam_sched *s) {
         t.vs[p] = f ? -stride[e] : stride[e];
         if (f) t.c0 += stride[e] * (R[e] - 1);
       }
-      s->h_turns.push_back(t);
+      s->h_solos.push_back(t);
     }
-    st.nturn = (int64_t)s->h_turns.size() - st.turn0;
+    st.nsolo = (int64_t)s->h_solos.size() - st.solo0;
   }
 }
 
@@ -533,8 +543,9 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
     g.pclass = unit ? 0 : (uniform && (p0 == 2 || p0 == 3 || p0 == 4 || p0 == 6)) ? p0 : -1;
     g.first = h.first;
     g.ntransfers = h.ntransfers;
-    g.turned = h.orientation;
+    g.turned = (h.orientation != 0 || h.bounded != 0) ? 1 : 0;
     if (h.orientation != 0) s->needs_rotvars = true;
+    if (h.bounded != 0) s->has_bounded = true;
     if (h.factorcol != 0) s->needs_factors = true;
     s->points += (int64_t)g.n[0] * g.n[1] * g.n[2] * g.ntransfers;
     // the division-free box decomposition
@@ -596,11 +607,11 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
   s->h_srcstart.assign(d->srcstart, d->srcstart + d->nsrcstart);
   std::vector<tam::Tile> tiles = build_tiles(s);
   std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
-  build_turns(s);
+  build_solos(s);
 
   cudaError_t e;
   if ((e = tam::side_create(s->side)) != cudaSuccess ||
-      (e = upload(&s->d_turns, s->h_turns.data(), s->h_turns.size())) != cudaSuccess ||
+      (e = upload(&s->d_solos, s->h_solos.data(), s->h_solos.size())) != cudaSuccess ||
       (e = upload(&s->d_ptiles, ptiles.data(), ptiles.size())) != cudaSuccess ||
       (e = upload(&s->d_groups, s->groups.data(), s->groups.size())) != cudaSuccess ||
       (e = upload(&s->d_tb, d->targetblocks, (size_t)d->ntransfers)) != cudaSuccess ||
@@ -640,6 +651,9 @@ void tam_schedule_free(tam_sched *s) {
 
 static int adjoint_ready(tam_sched *s) {
   if (s->adj.ready) return TAM_OK;
+  if (s->has_bounded)
+    return fail(s->ctx, TAM_EUNSUPPORTED,
+                "a schedule with bounded operators is not linear, so it has no adjoint");
   // a turned group's transpose writes into the set's own array: the layout
   // must be symmetric in the seam's plane (not a RotationPair member)
   for (const tam_group &h : s->host_groups) {
@@ -813,8 +827,8 @@ int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, i
         if (e != cudaSuccess) return cuda_fail(s->ctx, e, "plain group launch");
       }
     }
-    if (stage.nturn > 0) {
-      e = tam::launch_turned(s->dtype, s->D, s->d_turns + stage.turn0, stage.nturn, args, work,
+    if (stage.nsolo > 0) {
+      e = tam::launch_solo(s->dtype, s->D, s->d_solos + stage.solo0, stage.nsolo, args, work,
                              alt_work ? alt_work : work, work, factors, rotvars, nvars, s->S,
                              s->d_err, st);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "turned group launch");
@@ -865,6 +879,12 @@ int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
         stage.nptiles, sched_args(s), new_work, nullptr, nvars, s->S, s->shape.threads, st,
         &s->side, old_work);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "regrid transfer launch");
+    if (stage.nsolo > 0) {  // bounded children
+      e = tam::launch_solo(s->dtype, s->D, s->d_solos + stage.solo0, stage.nsolo, sched_args(s),
+                           old_work, old_work, new_work, nullptr, nullptr, nvars, s->S, s->d_err,
+                           st);
+      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "regrid transfer launch");
+    }
   }
   return TAM_OK;
 }

@@ -177,10 +177,10 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     if (members[m]->D != first->D || members[m]->dtype != first->dtype)
       return bfail(ctx, TAM_EINVAL,
                    "tam_batch_create: members differ in dimension or element type");
-    if (members[m]->needs_rotvars)
+    if (members[m]->needs_rotvars || members[m]->has_bounded)
       return bfail(ctx, TAM_EUNSUPPORTED,
-                   "tam_batch_create: a member turns transfers across a seam, which a batch "
-                   "does not take; fill it alone with tam_fill_ex");
+                   "tam_batch_create: a member turns transfers across a seam or bounds them, "
+                   "which a batch does not take; fill it alone");
   }
   Guard guard(ctx->device);
   if (!guard.ok) return bfail(ctx, TAM_ECUDA, "cannot make the context's device current");

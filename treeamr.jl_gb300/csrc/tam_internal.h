@@ -38,7 +38,7 @@ struct DevGroup {
   int64_t cls[3];    // class-index pool offsets (one int32 per target row)
   int64_t wtab;      // product-table pool offset
   int32_t member;    // the forest of a batch this group belongs to (0 alone)
-  int32_t turned;    // the orientation of a group across a seam (0: none)
+  int32_t turned;    // a solo group (turned across a seam, or bounded): no tiles
   // The one-tap skip of the reference's CPU fill (src/ghosts.jl:28-56): per
   // dimension, for each column class, the row of its only nonzero weight, or
   // -1 (int32 pool entries at csingle[d] + class).  `perm` (or -1) orders the
@@ -57,15 +57,19 @@ struct DevGroup {
   int32_t cstep[3];
 };
 
-// A turned group (across a seam) as its launch reads it: the real source's
-// offset of virtual 0-based stored indices j is c0 + sum_d vs[d] * j[d]
-// (the axis map folded into signed strides of the real array), and target
-// variable v reads real variable rotvars[v + nvars * col] - 1.
-struct TurnGroup {
+// A group the fused tiles do not take, run in a launch of its own after its
+// stage's fused launches: a turned group (across a seam), whose real source
+// is read at c0 + sum_d vs[d] * j[d] for virtual 0-based stored indices j
+// (the axis map folded into signed strides of the real array), target
+// variable v from real variable rotvars[v + nvars * col] - 1; or a bounded
+// group (`bounded` 1: the bounded conservative prolongation, 2: the
+// point-value sum clamped into its bracket), read in place (col 0, the
+// array's own strides).
+struct SoloGroup {
   int32_t group;    // index into the schedule's groups
-  int32_t col;      // the orientation r: the rotvars column
+  int32_t col;      // the orientation r: the rotvars column (0: not turned)
   int32_t odd;      // reads the alternate array
-  int32_t pad;
+  int32_t bounded;  // 0, or the group's bound (tam_group.bounded)
   int64_t vs[3];
   int64_t c0;
 };
@@ -137,8 +141,8 @@ struct Stage {
   int64_t npcopy0 = 0;          // packed tiles of the copies without a factor, of
   int64_t npcopy = 0;           // all the copies, then
   int64_t nptiles = 0;          // all packed tiles of the stage
-  int64_t turn0 = 0;            // the stage's turned groups: turns[turn0 .. turn0 + nturn)
-  int64_t nturn = 0;
+  int64_t solo0 = 0;            // the stage's solo groups: solos[solo0 .. solo0 + nsolo)
+  int64_t nsolo = 0;
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -219,7 +223,8 @@ struct tam_sched {
   int32_t nfactorcols = 0;
   bool needs_factors = false;
   bool needs_rotvars = false;   // a turned group reads the variable table
-  std::vector<tam::TurnGroup> h_turns;
+  bool has_bounded = false;     // a bounded group: nonlinear, no adjoint
+  std::vector<tam::SoloGroup> h_solos;
   std::vector<tam_group> host_groups;
   std::vector<int32_t> h_tb;  // target blocks, for re-tiling
   std::vector<int32_t> h_sb;  // source blocks, for the adjoint's lists
@@ -248,7 +253,7 @@ struct tam_sched {
   int32_t *d_perm = nullptr;
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
-  tam::TurnGroup *d_turns = nullptr;
+  tam::SoloGroup *d_solos = nullptr;
   tam::SideStream side;
   int32_t *d_err = nullptr;
   // the adjoint, prepared on first use (tam_adjoint.cu)
@@ -291,11 +296,11 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side, const void *src);
 
-// The turned groups turns[0 .. n) of one stage: a flat launch per group
+// The solo groups turns[0 .. n) of one stage: a flat launch per group
 // (blockIdx.y), reading `src` for an even orientation and `alt` for an odd
 // one, target variable v from real variable rotvars[v + nvars * r] - 1
 // (an entry outside 1:nvars skips the item and records TAM_EINVAL in *err).
-cudaError_t launch_turned(int dtype, int D, const TurnGroup *turns, int64_t n,
+cudaError_t launch_solo(int dtype, int D, const SoloGroup *turns, int64_t n,
                           const SchedArgs &a, const void *src, const void *alt, void *work,
                           const void *factors, const int32_t *rotvars, int nvars,
                           const int S[3], int32_t *err, cudaStream_t stream);
@@ -330,7 +335,7 @@ struct AdjRun {
   const Tile *fwd_tiles;           // the forward fill's tiles (the zero pass)
   const std::vector<Stage> *fwd_stages;
   int S[3];                        // stored extents (a batch: each member's own)
-  const TurnGroup *turns;          // the turned groups (their targets are zeroed too)
+  const SoloGroup *turns;          // the solo groups (their targets are zeroed too)
   const int32_t *rotvars;          // the variable table of turned groups, or null
 };
 cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,

@@ -832,23 +832,53 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                S, threads, stream, side);
 }
 
-// ---- turned groups: across a rotating or half-turn seam -----------------------
-// One item = (box point, variable, transfer) of turned group blockIdx.y, read
-// through the group's axis map (RotatedSource, src/ghosts.jl:183-244) folded
-// into signed strides: the virtual source window's points are the real
-// source's at c0 + sum_d vs[d] * j[d], variable rotvars[v + nvars * r] - 1.
-// The sum is stencil_sum's (src/ghosts.jl:75-118): m_1 innermost, the
-// weight product ((w_1*w_2)*w_3), acc from +0, no FMA, and with `one_tap` a
-// dimension whose weight column has a single nonzero weight takes only that
-// tap (src/ghosts.jl:28-56); a copy is +0 + x and a factor x*f + 0.
+// ---- solo groups: turned across a seam, or bounded ------------------------------
+// Julia's min and max of two floats (NaN-propagating, -0 below +0), which the
+// bounded operators' extremes follow (src/ghosts.jl:291-361).
+template <typename T>
+__device__ __forceinline__ T jmin(T x, T y) {
+  const bool c = (y < x) || (signbit(y) && !signbit(x));
+  return c ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+template <typename T>
+__device__ __forceinline__ T jmax(T x, T y) {
+  const bool c = (y > x) || (!signbit(y) && signbit(x));
+  return c ? (isnan(x) ? x : y) : (isnan(y) ? y : x);
+}
+// minmod and the monotonized central slope (src/ghosts.jl:291-292)
+template <typename T>
+__device__ __forceinline__ T minmod(T a, T b) {
+  return (a > T(0) && b > T(0)) ? jmin(a, b) : (a < T(0) && b < T(0)) ? jmax(a, b) : T(0);
+}
+template <typename T>
+__device__ __forceinline__ T mc_slope(T a, T b) {
+  using A = Arith<T>;
+  return minmod(A::mul(T(2), a), minmod(A::mul(T(2), b), A::mul(A::add(a, b), T(0.5))));
+}
+
+// One item = (box point, variable, transfer) of solo group blockIdx.y.
+// A turned group reads its real source through the axis map folded into
+// signed strides: the virtual window's points are the real source's at
+// c0 + sum_d vs[d] * j[d], variable rotvars[v + nvars * r] - 1
+// (RotatedSource, src/ghosts.jl:183-244).  The sum is stencil_sum's
+// (src/ghosts.jl:75-118): m_1 innermost, the weight product ((w_1*w_2)*w_3),
+// acc from +0, no FMA, and with `one_tap` a dimension whose weight column has
+// a single nonzero weight takes only that tap (src/ghosts.jl:28-56); a copy
+// is +0 + x and a factor x*f + 0.  A bounded group computes bounded_sum
+// (the parent at the order-3 window's middle row and its face neighbours,
+// the monotonized central slopes, the child's side read off the stencil
+// column, the largest scaling phi in [0, 1] that keeps every child within the
+// extremes) or bracket_clamp_sum (the full order-p sum clamped into the
+// range of the points with a nonzero linear weight in every dimension),
+// each carrying 0 * (max - min) (src/ghosts.jl:291-361).
 template <typename T, int D>
 __global__ void __launch_bounds__(256)
-    turned_group_kernel(const TurnGroup *__restrict__ turns, Args<T> a, const T *src,
-                        const T *alt, T *work, const T *__restrict__ factors,
-                        const int32_t *__restrict__ rotvars, int nvars, int S1, int S2, int S3,
-                        int32_t *err) {
+    solo_group_kernel(const SoloGroup *__restrict__ turns, Args<T> a, const T *src,
+                      const T *alt, T *work, const T *__restrict__ factors,
+                      const int32_t *__restrict__ rotvars, int nvars, int S1, int S2, int S3,
+                      int32_t *err) {
   using A = Arith<T>;
-  const TurnGroup tg = turns[blockIdx.y];
+  const SoloGroup tg = turns[blockIdx.y];
   const DevGroup &g = a.groups[tg.group];
   const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
   const int64_t items = box * nvars * g.ntransfers;
@@ -867,10 +897,13 @@ __global__ void __launch_bounds__(256)
     const int64_t t = r / nvars + g.first;
     const int64_t tblock = __ldg(a.tb + t) - 1;
     const int64_t sblock = __ldg(a.sb + t) - 1;
-    const int sv = __ldg(rotvars + v + (int64_t)nvars * tg.col) - 1;
-    if (sv < 0 || sv >= nvars) {  // a variable table naming no variable: skip, and say so
-      atomicExch(err, (int32_t)TAM_EINVAL);
-      continue;
+    int sv = v;
+    if (tg.col) {
+      sv = __ldg(rotvars + v + (int64_t)nvars * tg.col) - 1;
+      if (sv < 0 || sv >= nvars) {  // a variable table naming no variable: skip, and say so
+        atomicExch(err, (int32_t)TAM_EINVAL);
+        continue;
+      }
     }
     const T *sp = from + (sblock * nvars + sv) * vol + tg.c0;
     const int idx[3] = {i1, i2, i3};
@@ -880,8 +913,8 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < 3; ++k) {
       j[k] = __ldg(a.srcstart + g.ss[k] + idx[k]) - 1;
       wc[k] = a.weights + g.w[k] + (int64_t)g.order[k] * idx[k];
-      hi[k] = g.order[k];
-      if (a.one_tap && k < D) {
+      hi[k] = (tg.bounded == 2 && k < D) ? g.order[k] / 2 : g.order[k];
+      if (a.one_tap && k < D && !tg.bounded) {
         int nonzero = 0, row = 0;
         for (int m = 0; m < g.order[k]; ++m)
           if (wc[k][m] != T(0)) {
@@ -894,22 +927,67 @@ __global__ void __launch_bounds__(256)
         }
       }
     }
+    const int64_t vs0 = tg.vs[0], vs1 = tg.vs[1], vs2 = tg.vs[2];
     T x;
-    if (g.unit) {
-      x = A::add(T(0), sp[tg.vs[0] * j[0] + tg.vs[1] * j[1] + tg.vs[2] * j[2]]);
+    if (tg.bounded == 1) {
+      // bounded_sum: the parent at the window's middle row
+      int64_t c[3] = {j[0], j[1], j[2]};
+      for (int k = 0; k < D; ++k) c[k] += 1;
+      const int64_t o = vs0 * c[0] + vs1 * c[1] + vs2 * c[2];
+      const int64_t st[3] = {vs0, vs1, vs2};
+      const T u = sp[o];
+      T M = u, m = u, dl = T(0), sl = T(0);
+      T lov[3], hiv[3], s[3];
+      for (int k = 0; k < D; ++k) {
+        lov[k] = sp[o - st[k]];
+        hiv[k] = sp[o + st[k]];
+        s[k] = mc_slope(A::add(hiv[k], -u), A::add(u, -lov[k]));
+      }
+      for (int k = 0; k < D; ++k) M = jmax(M, lov[k]);
+      for (int k = 0; k < D; ++k) M = jmax(M, hiv[k]);
+      for (int k = 0; k < D; ++k) m = jmin(m, lov[k]);
+      for (int k = 0; k < D; ++k) m = jmin(m, hiv[k]);
+      // the sums are right folds, t_1 + (t_2 + t_3)
+      for (int k = D - 1; k >= 0; --k) {
+        const T sg = wc[k][2] > wc[k][0] ? s[k] : -s[k];
+        dl = k == D - 1 ? sg : A::add(sg, dl);
+        const T as = fabs(s[k]);
+        sl = k == D - 1 ? as : A::add(as, sl);
+      }
+      dl = A::mul(dl, T(0.25));
+      sl = A::mul(sl, T(0.25));
+      T phi = T(1);
+      if (sl > T(0)) phi = jmin(jmin(T(1), (M - u) / sl), (u - m) / sl);
+      x = A::add(A::add(u, A::mul(phi, dl)), A::mul(T(0), A::add(M, -m)));
+    } else if (g.unit) {
+      x = A::add(T(0), sp[vs0 * j[0] + vs1 * j[1] + vs2 * j[2]]);
     } else {
       T acc = T(0);
+      T blo = T(INFINITY), bhi = T(-INFINITY);
       for (int m3 = lo[2]; m3 < hi[2]; ++m3)
         for (int m2 = lo[1]; m2 < hi[1]; ++m2)
           for (int m1 = lo[0]; m1 < hi[0]; ++m1) {
             T w = wc[0][m1];
             if (D >= 2) w = A::mul(w, wc[1][m2]);
             if (D >= 3) w = A::mul(w, wc[2][m3]);
-            const T u = sp[tg.vs[0] * (j[0] + m1) + tg.vs[1] * (j[1] + m2) +
-                           tg.vs[2] * (j[2] + m3)];
+            const T u = sp[vs0 * (j[0] + m1) + vs1 * (j[1] + m2) + vs2 * (j[2] + m3)];
             acc = A::add(acc, A::mul(w, u));
+            if (tg.bounded == 2) {
+              // the bracket: a nonzero linear weight in every dimension
+              const bool in = wc[0][hi[0] + m1] != T(0) &&
+                              (D < 2 || wc[1][hi[1] + m2] != T(0)) &&
+                              (D < 3 || wc[2][hi[2] + m3] != T(0));
+              if (in) {
+                blo = jmin(blo, u);
+                bhi = jmax(bhi, u);
+              }
+            }
           }
       x = acc;
+      if (tg.bounded == 2) {
+        const T cl = acc > bhi ? bhi : acc < blo ? blo : acc;
+        x = A::add(cl, A::mul(T(0), A::add(bhi, -blo)));
+      }
     }
     const int64_t toff = (tblock * nvars + v) * vol +
                          ((int64_t)(g.tf[2] + i3) * S2 + (g.tf[1] + i2)) * S1 + g.tf[0] + i1;
@@ -918,7 +996,7 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename T>
-cudaError_t turned_dispatch(int D, const TurnGroup *turns, int64_t n, const Args<T> &a,
+cudaError_t solo_dispatch(int D, const SoloGroup *turns, int64_t n, const Args<T> &a,
                             const T *src, const T *alt, T *work, const T *factors,
                             const int32_t *rotvars, int nvars, const int S[3], int32_t *err,
                             cudaStream_t stream) {
@@ -928,31 +1006,31 @@ cudaError_t turned_dispatch(int D, const TurnGroup *turns, int64_t n, const Args
   const dim3 grid(64, (unsigned)n), block(256);
   switch (D) {
     case 1:
-      turned_group_kernel<T, 1><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+      solo_group_kernel<T, 1><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
                                                              rotvars, nvars, S[0], S[1], S[2], err);
       break;
     case 2:
-      turned_group_kernel<T, 2><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+      solo_group_kernel<T, 2><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
                                                              rotvars, nvars, S[0], S[1], S[2], err);
       break;
     default:
-      turned_group_kernel<T, 3><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
+      solo_group_kernel<T, 3><<<grid, block, 0, stream>>>(turns, a, src, alt, work, factors,
                                                              rotvars, nvars, S[0], S[1], S[2], err);
       break;
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_turned(int dtype, int D, const TurnGroup *turns, int64_t n,
+cudaError_t launch_solo(int dtype, int D, const SoloGroup *turns, int64_t n,
                           const SchedArgs &a, const void *src, const void *alt, void *work,
                           const void *factors, const int32_t *rotvars, int nvars,
                           const int S[3], int32_t *err, cudaStream_t stream) {
   if (!alt) alt = src;
   if (dtype == TAM_F64)
-    return turned_dispatch<double>(D, turns, n, typed<double>(a), (const double *)src,
+    return solo_dispatch<double>(D, turns, n, typed<double>(a), (const double *)src,
                                    (const double *)alt, (double *)work, (const double *)factors,
                                    rotvars, nvars, S, err, stream);
-  return turned_dispatch<float>(D, turns, n, typed<float>(a), (const float *)src,
+  return solo_dispatch<float>(D, turns, n, typed<float>(a), (const float *)src,
                                 (const float *)alt, (float *)work, (const float *)factors,
                                 rotvars, nvars, S, err, stream);
 }

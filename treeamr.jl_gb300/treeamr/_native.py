@@ -103,7 +103,7 @@ class Descriptor:
             cg.kind = KINDCODE[g.kind]
             cg.stage = g.stage
             cg.factorcol = g.factorcol
-            cg.bounded = 0
+            cg.bounded = getattr(g, "bounded", 0)
             cg.orientation = getattr(g, "orientation", 0)
             cg.axes = 0
             if cg.orientation:

@@ -8,6 +8,9 @@ Restates ``src/operators.jl``:
 * ``lagrange_weights`` / ``unit_lagrange_weights`` -- ``src/operators.jl:627-682``:
   exact rationals, rounded once into the stencil's element type.
 * ``conservative_prolong_weights`` -- ``src/schedule.jl:1097-1120``.
+* ``boundedmode`` -- ``src/operators.jl:417-441``: how a group's kernel
+  bounds what it computes (not at all, the bounded conservative
+  prolongation, or the point-value interpolant clamped into its bracket).
 """
 from __future__ import annotations
 
@@ -20,6 +23,8 @@ import numpy as np
 from .forest import round_rational_f32
 
 PointValue, Conservative = "PointValue", "Conservative"
+
+UNBOUNDED, BOUNDED_CONSERVATIVE, BOUNDED_POINTVALUE = 0, 1, 2
 
 
 class Operators:
@@ -51,8 +56,14 @@ class Operators:
                                  f"restriction must be 2, got {restriction}")
         else:
             raise ValueError(f"unknown operator family {family!r}")
-        if bounded:
-            raise NotImplementedError("bounded operators are not part of this engine")
+        if bounded and family == Conservative and prolongation not in (1, 3):
+            raise ValueError("bounded = true with the conservative family needs prolongation = "
+                             "3 or 1: the bounded prolongation is a limited order-3 "
+                             f"reconstruction, and order 1 copies the parent; got {prolongation}")
+        if bounded and vertex_prolongation is not None:
+            raise ValueError("bounded = true together with vertex_prolongation is not "
+                             "implemented: the bounded conservative prolongation is built for an "
+                             "order-3 cell stencil in every dimension")
         if vertex_prolongation is not None:
             if family != Conservative:
                 raise ValueError("vertex_prolongation is for the conservative family only")
@@ -61,13 +72,14 @@ class Operators:
         self.family = family
         self.prolongation = int(prolongation)
         self.restriction = int(restriction)
-        self.bounded = False
+        self.bounded = bool(bounded)
         self.vertex_prolongation = 0 if vertex_prolongation is None else int(vertex_prolongation)
 
     def __repr__(self):
         vp = "" if not self.vertex_prolongation else f", vertex_prolongation={self.vertex_prolongation}"
+        b = ", bounded=true" if self.bounded else ""
         return (f"Operators(prolongation={self.prolongation}, restriction={self.restriction}, "
-                f"family={self.family}{vp})")
+                f"family={self.family}{b}{vp})")
 
     def vertex_order(self) -> int:
         return self.vertex_prolongation if self.family == Conservative else self.prolongation
@@ -162,3 +174,22 @@ def round_weights(ws: Sequence[Fraction], dtype) -> np.ndarray:
         return np.array([round_rational_f32(w.numerator, w.denominator) for w in ws],
                         dtype=np.float32)
     raise TypeError(f"unsupported element type {dtype}")
+
+
+def boundedmode(ops: "Operators", kind: str, mirror, c) -> int:
+    """The bound a group of ``kind`` takes (``src/operators.jl:431-441``):
+    only an operator that can make a new extremum takes one.  Conservative
+    order 1 copies the parent and a point-value width of 2 is linear
+    interpolation, bounded already; injection (a vertex-like restriction) is
+    a copy; a point-value restriction interpolates along every cell-like
+    dimension."""
+    if not ops.bounded:
+        return UNBOUNDED
+    if ops.family == Conservative:
+        return BOUNDED_CONSERVATIVE if kind == "prolong" and ops.prolongation == 3 else UNBOUNDED
+    if kind == "prolong" and ops.prolongation > 2:
+        return BOUNDED_POINTVALUE
+    if kind == "restrict" and ops.restriction > 2 and any(x == 0 for x in c):
+        return BOUNDED_POINTVALUE
+    return UNBOUNDED
+

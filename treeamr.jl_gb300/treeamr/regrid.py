@@ -34,6 +34,7 @@ from .forest import Forest, MortonKey, childoffset, parentkey, sortedchildkeys
 from .schedule import (COPY, PROLONG, RESTRICT, GroupKey, NeighbourTable, TransferGroup,
                        _nospan, copy_stencil, kind_stencil, merged_transfers, piece_copies,
                        piece_of, piece_primary, subpiece_list, subpiece_values)
+from .operators import boundedmode
 from .storage import FieldSet
 
 REGRID_TAG = 50                     # the reference's stage tag of the transfer
@@ -155,9 +156,12 @@ class RegridTransfer:
         groups = []
         for key in sorted(pairs, key=GroupKey.order):
             tb, sb = pairs[key]
+            # a bounded operator bounds the regrid's children too
+            # (src/regrid.jl:765-778)
+            mode = boundedmode(operators, key.kind, key.mirror, self.c)
             st = tuple(kind_stencil(self.T, N, self.G[d], self.c[d], key.kind, 0, key.offset[d],
-                                    operators) for d in range(D))
-            groups.append(TransferGroup(key, st, tb, sb, 0, REGRID_TAG))
+                                    operators, -1, mode) for d in range(D))
+            groups.append(TransferGroup(key, st, tb, sb, 0, REGRID_TAG, None, mode))
         self.groups = groups
         kept = regrid_kept_pairs(forest, oldleaves, self.c)
         self.kept_groups = []

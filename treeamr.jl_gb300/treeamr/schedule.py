@@ -29,7 +29,8 @@ import numpy as np
 
 from .forest import (Forest, MortonKey, OUTER, OUTFLOW, REFLECTING, alldirections, axismap,
                      childoffset, virtual_offset)
-from .operators import (Conservative, Operators, check_operators, conservative_prolong_weights,
+from .operators import (BOUNDED_POINTVALUE, UNBOUNDED, Conservative, Operators, boundedmode,
+                        check_operators, conservative_prolong_weights,
                         interpolation_weights, round_weights)
 from .storage import FieldSet, ghostwidths, mirrorcolumn, staggers, storedsize
 
@@ -116,9 +117,13 @@ class TransferGroup:
     block pairs (1-based block indices, targets non-decreasing)."""
 
     def __init__(self, key: GroupKey, stencils, targetblocks, sourceblocks, factorcol: int,
-                 stage: int, axes=None):
+                 stage: int, axes=None, bounded: int = 0):
         self.key = key
         self.kind = key.kind
+        # how the kernel bounds the group's result (``boundedmode``): 0 not
+        # at all, 1 the bounded conservative prolongation, 2 the point-value
+        # sum clamped into its bracket (stencils with the linear rows stacked)
+        self.bounded = int(bounded)
         # A turned group (across a seam) reads its real source through the
         # axis map ``(perm, flip)`` in gather form (0-based dimensions) and
         # the variable table's column ``orientation`` (``src/ghosts.jl:183-244``).
@@ -239,9 +244,46 @@ def conservative_prolong_stencil(T, N, G, c, dd, od, p) -> Stencil1D:
     return Stencil1D(rng.start, ss, ws, T)
 
 
-def kind_stencil(T, N, G, c, kind, dd, od, ops: Operators, span: int = -1) -> Stencil1D:
-    """``src/schedule.jl:1183-1195`` (no element sets); ``span`` a sub-piece
-    span along a tangential vertex-like dimension (``prolongation_stencil``)."""
+LINEAR_OPERATORS = Operators(prolongation=2, restriction=2)
+
+
+def stack_linear(s: Stencil1D, lin: Stencil1D, T) -> Stencil1D:
+    """A bounded point-value stencil (``src/schedule.jl:1279-1300``): ``s``'s
+    order-p weights in rows ``1:p`` and below them, in rows ``p+1:2p``, the
+    linear stencil's weights over the same targets placed at their points'
+    positions in ``s``'s window; the kernel clamps the order-p sum into the
+    range of the points whose linear weight is nonzero, the bracket."""
+    p, q, n = s.order, lin.order, s.ntarget
+    if s.targetfirst != lin.targetfirst or lin.ntarget != n:
+        raise RuntimeError(f"the linear stencil covers other targets than the order-{p} one")
+    cols = []
+    for i in range(n):
+        col = list(s.exact[i]) + [Fraction(0)] * p
+        for k in range(q):
+            w = lin.exact[i][k]
+            if w == 0:
+                continue
+            off = int(lin.srcstart[i]) + k - int(s.srcstart[i])
+            if not 0 <= off < p:
+                raise RuntimeError(f"the bracket of target {s.targetfirst + i} lies outside "
+                                   f"its order-{p} window")
+            col[p + off] = w
+        cols.append(col)
+    return Stencil1D(s.targetfirst, s.srcstart, cols, T)
+
+
+def kind_stencil(T, N, G, c, kind, dd, od, ops: Operators, span: int = -1,
+                 mode: int = UNBOUNDED) -> Stencil1D:
+    """``src/schedule.jl:1183-1204`` (no element sets); ``span`` a sub-piece
+    span along a tangential vertex-like dimension (``prolongation_stencil``);
+    a bounded point-value group's stencil stacks the linear one."""
+    s = _kind_stencil(T, N, G, c, kind, dd, od, ops, span)
+    if mode != BOUNDED_POINTVALUE:
+        return s
+    return stack_linear(s, _kind_stencil(T, N, G, c, kind, dd, od, LINEAR_OPERATORS, span), T)
+
+
+def _kind_stencil(T, N, G, c, kind, dd, od, ops: Operators, span: int = -1) -> Stencil1D:
     if kind == COPY:
         return copy_stencil(T, N, G, c, dd, span)
     if kind == PROLONG and span >= 0:
@@ -286,10 +328,13 @@ def mirror_rows(s: Stencil1D, N, G, c, dd, T) -> Stencil1D:
     return s.rows(rows, rng.start, T)
 
 
-def mirror_restriction(T, N, G, od, p) -> Stencil1D:
+def mirror_restriction(T, N, G, od, p, mode: int = UNBOUNDED) -> Stencil1D:
     h = N // 2
     rng = range(G + 1, G + 2 + h) if od == 0 else range(G + 1 + h, G + N + 2)
-    return restrict_stencil_over(T, rng, N, G, 1, 0, od, p)
+    s = restrict_stencil_over(T, rng, N, G, 1, 0, od, p)
+    if mode != BOUNDED_POINTVALUE:
+        return s
+    return stack_linear(s, restrict_stencil_over(T, rng, N, G, 1, 0, od, 2), T)
 
 
 # --- the neighbour search ---------------------------------------------------
@@ -857,13 +902,17 @@ def piece_box_spans(pieces, c):
     return [tuple(span_code(fs[p[d]], ls[p[d]]) for d in range(D)) for p in uniq]
 
 
-def unify_stencil(T, N, G, c, key: GroupKey, d: int, p: int) -> Stencil1D:
+def unify_stencil(T, N, G, c, key: GroupKey, d: int, p: int,
+                  mode: int = UNBOUNDED) -> Stencil1D:
     """One dimension of a stage-0 (or stage-P) transfer (``src/schedule.jl:973-984``)."""
     dd, code = key.direction[d], key.span[d]
     if key.kind == COPY:
         return copy_stencil(T, N, G, c, dd, span=code)
     rng = piece_range(N, G, c, code)
-    return restrict_stencil_over(T, rng, N, G, c, dd, key.offset[d], p)
+    s = restrict_stencil_over(T, rng, N, G, c, dd, key.offset[d], p)
+    if mode != BOUNDED_POINTVALUE:
+        return s
+    return stack_linear(s, restrict_stencil_over(T, rng, N, G, c, dd, key.offset[d], 2), T)
 
 
 # --- the schedule -------------------------------------------------------------
@@ -929,15 +978,20 @@ class GhostSchedule:
 
         built = {}
 
+        def boundedof(key):
+            return boundedmode(operators, key.kind, key.mirror, c)
+
         def build1(key: GroupKey, d: int) -> Stencil1D:
+            mode = boundedof(key)
             if isunify(key):
-                return unify_stencil(T, N, G[d], c[d], key, d, operators.restriction)
+                return unify_stencil(T, N, G[d], c[d], key, d, operators.restriction, mode)
             dd, od, state = key.direction[d], key.offset[d], key.mirror[d]
             ds = dd if state == 0 else 0
             if state != 0 and key.kind == RESTRICT and c[d] == 1:
-                s = mirror_restriction(T, N, G[d], od, operators.restriction)
+                s = mirror_restriction(T, N, G[d], od, operators.restriction, mode)
             else:
-                s = kind_stencil(T, N, G[d], c[d], key.kind, ds, od, operators, key.span[d])
+                s = kind_stencil(T, N, G[d], c[d], key.kind, ds, od, operators, key.span[d],
+                                 mode)
             if state == 0:
                 return s
             if state == 3:
@@ -965,11 +1019,11 @@ class GhostSchedule:
         for key in sorted(pairs, key=GroupKey.order):
             tb, sb = pairs[key]
             groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
-                                        transfer_stage(key), axesof(key)))
+                                        transfer_stage(key), axesof(key), boundedof(key)))
         for key in sorted(ppairs, key=GroupKey.order):
             tb, sb = ppairs[key]
             groups.append(TransferGroup(key, build(key), tb, sb, factorcol(key),
-                                        SELFIMAGE_TAG))
+                                        SELFIMAGE_TAG, None, boundedof(key)))
         self.groups = groups
         self.turned = any(g.turned for g in groups)
         self.odd_turns = any(g.orientation % 2 for g in groups)
