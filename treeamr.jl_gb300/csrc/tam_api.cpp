@@ -398,18 +398,23 @@ void build_solos(tam_sched *s) {
       t.col = h.orientation;
       t.odd = h.orientation & 1;
       t.bounded = h.bounded;
+      // the axis map; an unturned (bounded) group reads in place: the identity
+      int perm[3] = {0, 1, 2}, flip[3] = {0, 0, 0};
+      if (h.orientation != 0)
+        for (int e = 0; e < s->D; ++e) {
+          perm[e] = (h.axes >> (2 * e)) & 3;
+          flip[e] = (h.axes >> (8 + e)) & 1;
+        }
       int R[3] = {1, 1, 1};
-      for (int e = 0; e < s->D; ++e) R[e] = s->S[(h.axes >> (2 * e)) & 3];
+      for (int e = 0; e < s->D; ++e) R[e] = s->S[perm[e]];
       const int64_t stride[3] = {1, R[0], (int64_t)R[0] * R[1]};
       t.vs[0] = 1;
       t.vs[1] = stride[1];
       t.vs[2] = stride[2];
       t.c0 = 0;
       for (int e = 0; e < s->D; ++e) {
-        const int p = (h.axes >> (2 * e)) & 3;
-        const bool f = (h.axes >> (8 + e)) & 1;
-        t.vs[p] = f ? -stride[e] : stride[e];
-        if (f) t.c0 += stride[e] * (R[e] - 1);
+        t.vs[perm[e]] = flip[e] ? -stride[e] : stride[e];
+        if (flip[e]) t.c0 += stride[e] * (R[e] - 1);
       }
       s->h_solos.push_back(t);
     }
