@@ -634,24 +634,37 @@ def main():
         del pipe1
         torch.cuda.empty_cache()
         # steps in flight together: each state's upload, fill and download on
-        # its own stream and device buffer, three states at a time
-        pipe = HostPipeline(fs, sched, depth=3)
-
-        def e2e_run(n):
-            pipe.wait_on(stream)                 # after the timing's start event
-            for i in range(n):
-                pipe.submit(host_in, host_out[i % 2])
-            pipe.join(stream)                    # before its end event
-        e2e_run(3)
+        # its own stream and device buffer, three states at a time; the
+        # upload moves what the fill reads, the own points, when the
+        # schedule writes every other point (tam_fill_host_own)
+        own = not sched.boundaries
         e2e_steps = max(6, min(args.steps, 12))
-        ms_e2e = timed(lambda: e2e_run(e2e_steps), 1) / e2e_steps
-        e2e = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
-               "ms_per_step": ms_e2e, "h2d_bytes_per_step": field_bytes,
-               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps,
-               "api": "tam_fill_host (C ABI, host buffers) through treeamr.host.HostPipeline, "
-                      "3 streams and device buffers",
-               "single_step_ms": ms_single}
+
+        def e2e_pipeline(pipe):
+            def run(n):
+                pipe.wait_on(stream)             # after the timing's start event
+                for i in range(n):
+                    pipe.submit(host_in, host_out[i % 2])
+                pipe.join(stream)                # before its end event
+            run(3)
+            return timed(lambda: run(e2e_steps), 1) / e2e_steps
+        pipe = HostPipeline(fs, sched, depth=3)
+        ms_full = e2e_pipeline(pipe)
         del pipe
+        ms_e2e, h2d = ms_full, field_bytes
+        if own:
+            pipe = HostPipeline(fs, sched, depth=3, own=True)
+            ms_e2e, h2d = e2e_pipeline(pipe), pipe.own_bytes()
+            del pipe
+        e2e = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+               "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps,
+               "api": ("tam_fill_host_own (C ABI, page-locked host buffers: the own points "
+                       "up, read by a kernel, the filled array down)" if own else
+                       "tam_fill_host (C ABI, host buffers)") +
+                      " through treeamr.host.HostPipeline, 3 streams and device buffers",
+               "full_upload_ms_per_step": ms_full,
+               "single_step_ms": ms_single}
         torch.cuda.empty_cache()
         # the host link's own rate, the e2e step's floor: an upload and a
         # download of the field data at once, on two streams (copy engines)
@@ -674,15 +687,16 @@ def main():
         ms_down = timed(lambda: link(up=False), 3)
         ms_both = timed(link, 3)
         gb = field_bytes / 1e9
-        # a step moves the field data up and down: its floor is the two copies
-        # one after the other, or together where the link carries both at once
+        # a full-upload step moves the field data up and down: its floor is
+        # the two copies one after the other, or together where the link
+        # carries both at once
         floor = min(ms_up + ms_down, ms_both)
         e2e["host_link"] = {"h2d_gbs": gb / (ms_up * 1e-3), "d2h_gbs": gb / (ms_down * 1e-3),
                             "both_each_way_gbs": gb / (ms_both * 1e-3),
                             "serial_floor_ms": ms_up + ms_down,
                             "concurrent_floor_ms": ms_both,
                             "floor_ms_per_step": floor,
-                            "frac": floor / ms_e2e}
+                            "frac": floor / ms_full}
         del dbuf, host_in, host_out
         torch.cuda.empty_cache()
 

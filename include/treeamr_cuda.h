@@ -386,6 +386,21 @@ typedef struct tam_state_layout {
 int tam_scatter(const tam_state_layout *layout, const void *state, void *work, void *stream);
 int tam_gather(const tam_state_layout *layout, const void *work, void *state, void *stream);
 
+/* tam_fill_host moving only what the fill reads up: the own points of
+ * host_in (the box `layout` describes, ghosts[d] .. ghosts[d] + own[d] - 1
+ * along d) are copied into device_work by a kernel that reads host_in
+ * through its device mapping (so host_in must be page-locked: cudaHostAlloc
+ * or cudaHostRegister), the stages [first_stage, last_stage] are filled,
+ * and device_work comes back into host_out whole.  The fill reads own
+ * points only, so every point it writes is as tam_fill_host would leave
+ * it; a point neither own nor written by the fill (a hook region) comes
+ * back as device_work held it.  Asynchronous on `stream`. */
+int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *host_in,
+                      void *host_out, void *device_work, int32_t nvars, int64_t nblocks,
+                      const void *factors, int32_t first_stage, int32_t last_stage,
+                      void *stream);
+
+
 /* Launch options of the fused fill, per schedule (no reference counterpart:
  * the reference has no tuning; these are what the autotuner sets).  Changing
  * one changes speed only, never a result. */

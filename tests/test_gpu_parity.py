@@ -260,3 +260,45 @@ def test_host_pipeline_equals_device_fill(cuda_lib):
         assert torch.equal(got.view(torch.int64), expect[k].cpu().view(torch.int64))
     with pytest.raises(ValueError):
         pipe.submit(ins[0][:1])
+
+
+def test_host_pipeline_own_uploads_equal_device_fill(cuda_lib):
+    """tam_fill_host_own: only the own points go up (read by a kernel from
+    the page-locked host buffer); the filled array that comes back equals
+    the device fill bit for bit, whatever the host buffer's ghosts held.
+    A schedule with hook regions, and pageable host memory, are refused."""
+    from treeamr.host import HostPipeline
+    f, fs, ops = meshes.sphere_setup(nvars=2, roots=4, levels=2)
+    s = GhostSchedule(fs, ops)
+    assert not s.boundaries
+    fs.work = fs.work.cuda()
+    fs.factors = fs.factors.cuda()
+    states, expect = [], []
+    for k in range(4):
+        g = torch.Generator(device="cuda").manual_seed(60 + k)
+        x = torch.rand(fs.work.shape, dtype=fs.work.dtype, device="cuda", generator=g)
+        states.append(x)
+        fs.work.copy_(x)
+        fill_ghosts(fs, s)
+        expect.append(fs.work.clone())
+    pipe = HostPipeline(fs, s, depth=3, own=True)
+    ins = []
+    for x in states:
+        h = x.cpu()
+        h[:, :, torch.from_numpy(ghost_mask(fs))] = float("nan")     # never uploaded
+        ins.append(h.pin_memory())
+    outs = [torch.empty_like(h).pin_memory() for h in ins]
+    for k in range(4):
+        pipe.submit(ins[k], outs[k] if k % 2 else None)
+    pipe.synchronize()
+    for k in range(4):
+        got = outs[k] if k % 2 else ins[k]
+        assert torch.equal(got.view(torch.int64), expect[k].cpu().view(torch.int64))
+    assert pipe.own_bytes() * 2 < ins[0].numel() * ins[0].element_size()
+    with pytest.raises(Exception, match="page-locked"):
+        pipe.submit(states[0].cpu())
+    fw = nested_forest(2, N=8)
+    fw_s = FieldSet(fw, 1, G=2, device="cuda")
+    with pytest.raises(ValueError, match="hook"):
+        HostPipeline(fw_s, GhostSchedule(fw_s, Operators(prolongation=4, restriction=4)),
+                     own=True)

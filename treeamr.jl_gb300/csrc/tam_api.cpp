@@ -863,6 +863,44 @@ int tam_fill_host(tam_sched *s, const void *host_in, void *host_out, void *devic
   return TAM_OK;
 }
 
+int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *host_in,
+                      void *host_out, void *device_work, int32_t nvars, int64_t nblocks,
+                      const void *factors, int32_t first_stage, int32_t last_stage,
+                      void *stream) {
+  if (!host_in || !host_out || !layout)
+    return fail(s ? s->ctx : nullptr, TAM_EINVAL, "tam_fill_host_own: NULL argument");
+  int rc = check_fill_args(s, device_work, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  if (layout->dtype != s->dtype || layout->ndim != s->D || layout->nvars != nvars ||
+      layout->nblocks != nblocks)
+    return fail(s->ctx, TAM_ELAYOUT, "tam_fill_host_own: the layout is not the schedule's");
+  for (int d = 0; d < s->D; ++d)
+    if (layout->stored[d] != s->S[d])
+      return fail(s->ctx, TAM_ELAYOUT,
+                  "tam_fill_host_own: the layout's stored extents are not the schedule's");
+  DeviceGuard guard(s->ctx->device);
+  if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
+  // the kernel reads host_in through its device mapping: page-locked memory
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, host_in);
+  if (e != cudaSuccess || attr.type != cudaMemoryTypeHost || !attr.devicePointer) {
+    cudaGetLastError();
+    return fail(s->ctx, TAM_EINVAL,
+                "tam_fill_host_own: host_in must be page-locked host memory (cudaHostAlloc "
+                "or cudaHostRegister), which the upload kernel reads directly");
+  }
+  rc = tam::own_box_copy(layout, device_work, attr.devicePointer, stream);
+  if (rc != TAM_OK) return fail(s->ctx, rc, "tam_fill_host_own: own-point upload");
+  rc = tam_fill(s, device_work, nvars, nblocks, factors, first_stage, last_stage, stream);
+  if (rc != TAM_OK) return rc;
+  const size_t bytes = (size_t)nblocks * nvars * s->S[0] * s->S[1] * s->S[2] *
+                       (s->dtype == TAM_F64 ? 8 : 4);
+  e = cudaMemcpyAsync(host_out, device_work, bytes, cudaMemcpyDeviceToHost,
+                      (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "tam_fill_host_own download");
+  return TAM_OK;
+}
+
 int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
                         void *new_work, int64_t new_nblocks, int32_t nvars, void *stream) {
   if (!s || !old_work || !new_work)

@@ -305,6 +305,9 @@ cudaError_t launch_solo(int dtype, int D, const SoloGroup *turns, int64_t n,
                           const void *factors, const int32_t *rotvars, int nvars,
                           const int S[3], int32_t *err, cudaStream_t stream);
 
+// The own boxes of `src` into `dst`, both in the working layout (tam_state.cu).
+int own_box_copy(const tam_state_layout *layout, void *dst, const void *src, void *stream);
+
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);
 

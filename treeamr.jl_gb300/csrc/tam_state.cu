@@ -45,6 +45,30 @@ __global__ void __launch_bounds__(256) state_copy_kernel(T *__restrict__ work,
   }
 }
 
+// The own boxes of one working array into another's (both in the working
+// layout): the rows of state_copy_kernel, read and written at the same
+// working-array offsets.  The upload of tam_fill_host_own, which reads a
+// page-locked host array through its device mapping.
+template <typename T>
+__global__ void __launch_bounds__(256) own_box_kernel(T *__restrict__ dst,
+                                                      const T *__restrict__ src, int64_t nrows,
+                                                      int O1, int O2, int O3, int S1, int S2,
+                                                      int S3, int G1, int G2, int G3) {
+  const int rpi = blockDim.x / O1;
+  const int lr = threadIdx.x / O1, e = threadIdx.x - lr * O1;
+  if (lr >= rpi) return;
+  for (int64_t r0 = (int64_t)blockIdx.x * rpi; r0 < nrows; r0 += (int64_t)gridDim.x * rpi) {
+    const int64_t r = r0 + lr;
+    if (r >= nrows) continue;
+    const int64_t q = r / O2;
+    const int i2 = (int)(r - q * O2);
+    const int64_t vb = q / O3;
+    const int i3 = (int)(q - vb * O3);
+    const int64_t w = ((vb * S3 + i3 + G3) * S2 + i2 + G2) * (int64_t)S1 + G1 + e;
+    dst[w] = src[w];
+  }
+}
+
 template <typename T>
 cudaError_t launch(bool to_work, T *work, T *state, int64_t nrows, const int O[3],
                    const int S[3], const int G[3], cudaStream_t stream) {
@@ -63,6 +87,48 @@ cudaError_t launch(bool to_work, T *work, T *state, int64_t nrows, const int O[3
         work, state, nrows, O[0], O[1], O[2], S[0], S[1], S[2], G[0], G[1], G[2]);
   return cudaGetLastError();
 }
+
+}  // namespace
+
+namespace tam {
+
+int own_box_copy(const tam_state_layout *L, void *dst, const void *src, void *stream) {
+  if (!L || !dst || !src) return TAM_EINVAL;
+  if (L->ndim < 1 || L->ndim > 3 || L->nvars < 1 || L->nblocks < 0) return TAM_EINVAL;
+  int O[3] = {1, 1, 1}, S[3] = {1, 1, 1}, G[3] = {0, 0, 0};
+  for (int d = 0; d < L->ndim; ++d) {
+    O[d] = L->own[d];
+    S[d] = L->stored[d];
+    G[d] = L->ghosts[d];
+    if (O[d] < 1 || G[d] < 0 || G[d] + O[d] > S[d]) return TAM_ELAYOUT;
+  }
+  if (O[0] > 1024) return TAM_EUNSUPPORTED;
+  const int64_t nrows = (int64_t)O[1] * O[2] * L->nvars * L->nblocks;
+  if (nrows == 0) return TAM_OK;
+  const int threads = O[0] <= 256 ? 256 : 1024;
+  const int rpi = threads / O[0];
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t blocks =
+      std::max<int64_t>(1, std::min<int64_t>((nrows + rpi - 1) / rpi, (int64_t)nsm * 32));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (L->dtype == TAM_F64)
+    own_box_kernel<double><<<(unsigned)blocks, threads, 0, st>>>(
+        (double *)dst, (const double *)src, nrows, O[0], O[1], O[2], S[0], S[1], S[2], G[0],
+        G[1], G[2]);
+  else if (L->dtype == TAM_F32)
+    own_box_kernel<float><<<(unsigned)blocks, threads, 0, st>>>(
+        (float *)dst, (const float *)src, nrows, O[0], O[1], O[2], S[0], S[1], S[2], G[0],
+        G[1], G[2]);
+  else
+    return TAM_EINVAL;
+  return cudaGetLastError() == cudaSuccess ? TAM_OK : TAM_ECUDA;
+}
+
+}  // namespace tam
+
+namespace {
 
 int state_copy(bool to_work, const tam_state_layout *L, void *work, void *state,
                void *stream) {

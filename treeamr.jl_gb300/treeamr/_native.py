@@ -238,6 +238,9 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_fill_host_own.argtypes = [vp, C.POINTER(tam_state_layout), vp, vp, vp, i32, i64,
+                                      vp, i32, i32, vp]
+    lib.tam_fill_host_own.restype = C.c_int
     lib.tam_fill_ex.argtypes = [vp, vp, vp, i32, i64, vp, vp, i32, i32, i32, vp]
     lib.tam_fill_ex.restype = C.c_int
     lib.tam_fill_adjoint_ex.argtypes = [vp, vp, i32, i64, vp, vp, i32, i32, vp, C.c_size_t,

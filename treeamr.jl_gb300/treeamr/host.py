@@ -7,6 +7,12 @@ keeps ``depth`` streams, each with its own device buffer, and gives
 consecutive states to them in turn, so one state's upload, another's fill
 and a third's download run together: the copy engines in both directions
 and the SMs stay busy at once.
+
+With ``own=True`` only what the fill reads goes up: the own points, read
+by a kernel straight from the page-locked host buffer
+(``tam_fill_host_own``); the filled array comes back whole.  That needs a
+schedule that writes every point outside the own boxes (no outer-face hook
+regions), since the rest of the device buffer is not uploaded.
 """
 from __future__ import annotations
 
@@ -28,10 +34,18 @@ class HostPipeline:
     ``work`` is not touched.  Host buffers should be page-locked
     (``Tensor.pin_memory()``), or the copies do not overlap other work."""
 
-    def __init__(self, fs: FieldSet, schedule: GhostSchedule, depth: int = 3):
+    def __init__(self, fs: FieldSet, schedule: GhostSchedule, depth: int = 3,
+                 own: bool = False):
         if depth < 1:
             raise ValueError("depth must be at least 1")
         check_fill(fs, schedule)
+        if own and schedule.boundaries:
+            raise ValueError("own-point uploads need a schedule that writes every point outside "
+                             "the own boxes, and this one leaves outer-face regions to a hook")
+        self.own = own
+        if own:
+            from .state import _layout
+            self.layout = _layout(fs)
         self.fs = fs
         self.device = fs.work.device
         self.ds = device_schedule(schedule, self.device.index or 0)
@@ -53,6 +67,15 @@ class HostPipeline:
         k = self.next
         self.next = (k + 1) % len(self.streams)
         st = self.streams[k]
+        if self.own:
+            rc = self.ds.lib.tam_fill_host_own(
+                self.ds.handle, C.byref(self.layout), C.c_void_p(host_in.data_ptr()),
+                C.c_void_p(host_out.data_ptr()), C.c_void_p(self.buffers[k].data_ptr()),
+                self.fs.nvars, self.fs.nblocks(), C.c_void_p(self.fs.factors.data_ptr()),
+                _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST,
+                C.c_void_p(st.cuda_stream))
+            _native.check(rc, self.ds.ctx, "tam_fill_host_own")
+            return k
         rc = self.ds.lib.tam_fill_host(
             self.ds.handle, C.c_void_p(host_in.data_ptr()), C.c_void_p(host_out.data_ptr()),
             C.c_void_p(self.buffers[k].data_ptr()), self.fs.nvars, self.fs.nblocks(),
@@ -60,6 +83,14 @@ class HostPipeline:
             _native.TAM_STAGE_ALL_LAST, C.c_void_p(st.cuda_stream))
         _native.check(rc, self.ds.ctx, "tam_fill_host")
         return k
+
+    def own_bytes(self) -> int:
+        """Bytes an own-point upload moves per state."""
+        import numpy as np
+        n = self.fs.nvars * self.fs.nblocks() * self.fs.T.itemsize
+        for d in range(self.fs.D):
+            n *= self.fs.forest.N + self.fs.c[d]
+        return int(n)
 
     def wait_on(self, stream: torch.cuda.Stream):
         """Make every slot's stream wait for what ``stream`` has queued."""
