@@ -48,7 +48,12 @@ __global__ void __launch_bounds__(256) state_copy_kernel(T *__restrict__ work,
 // The own boxes of one working array into another's (both in the working
 // layout): the rows of state_copy_kernel, read and written at the same
 // working-array offsets.  The upload of tam_fill_host_own, which reads a
-// page-locked host array through its device mapping.
+// page-locked host array through its device mapping: a small grid (it
+// shares the GPU with the fills of the states in flight beside it) with
+// kUnroll independent reads in flight per thread to cover the host link's
+// latency.
+constexpr int kUnroll = 8;
+
 template <typename T>
 __global__ void __launch_bounds__(256) own_box_kernel(T *__restrict__ dst,
                                                       const T *__restrict__ src, int64_t nrows,
@@ -57,15 +62,26 @@ __global__ void __launch_bounds__(256) own_box_kernel(T *__restrict__ dst,
   const int rpi = blockDim.x / O1;
   const int lr = threadIdx.x / O1, e = threadIdx.x - lr * O1;
   if (lr >= rpi) return;
-  for (int64_t r0 = (int64_t)blockIdx.x * rpi; r0 < nrows; r0 += (int64_t)gridDim.x * rpi) {
-    const int64_t r = r0 + lr;
-    if (r >= nrows) continue;
-    const int64_t q = r / O2;
-    const int i2 = (int)(r - q * O2);
-    const int64_t vb = q / O3;
-    const int i3 = (int)(q - vb * O3);
-    const int64_t w = ((vb * S3 + i3 + G3) * S2 + i2 + G2) * (int64_t)S1 + G1 + e;
-    dst[w] = src[w];
+  const int64_t step = (int64_t)gridDim.x * rpi;
+  for (int64_t r0 = (int64_t)blockIdx.x * rpi + lr; r0 < nrows; r0 += step * kUnroll) {
+    int64_t w[kUnroll];
+    T x[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const int64_t r = r0 + u * step;
+      w[u] = -1;
+      if (r < nrows) {
+        const int64_t q = r / O2;
+        const int i2 = (int)(r - q * O2);
+        const int64_t vb = q / O3;
+        const int i3 = (int)(q - vb * O3);
+        w[u] = ((vb * S3 + i3 + G3) * S2 + i2 + G2) * (int64_t)S1 + G1 + e;
+        x[u] = src[w[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+      if (w[u] >= 0) dst[w[u]] = x[u];
   }
 }
 
@@ -110,8 +126,9 @@ int own_box_copy(const tam_state_layout *L, void *dst, const void *src, void *st
   int dev = 0, nsm = 152;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // half the SMs, one CTA each: the rest stay with the fills in flight
   const int64_t blocks =
-      std::max<int64_t>(1, std::min<int64_t>((nrows + rpi - 1) / rpi, (int64_t)nsm * 32));
+      std::max<int64_t>(1, std::min<int64_t>((nrows + rpi - 1) / rpi, std::max(1, nsm / 2)));
   cudaStream_t st = (cudaStream_t)stream;
   if (L->dtype == TAM_F64)
     own_box_kernel<double><<<(unsigned)blocks, threads, 0, st>>>(
