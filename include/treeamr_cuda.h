@@ -319,6 +319,22 @@ int tam_wave_rk4_stage(int32_t dtype, const tam_wave_block *blocks, int32_t nblo
                        int32_t max_points_per_block, const void *x, const void *y,
                        void *t_out, const void *acc_in, void *acc_out, double ct, double ca,
                        void *stream);
+/* `steps` RK4 steps of the wave equation over a batch of forests as one CUDA
+ * graph: per step four tam_batch_fill calls, each followed by one
+ * tam_wave_rk4_stage (stage states in `ta` and `tb`, the step's sum in
+ * `acc`, the state `y` advanced in place), captured on a private stream of
+ * `device` (nothing runs at capture).  tam_graph_launch replays it on a
+ * stream; the arrays, the batch and the block table must outlive the graph.
+ * The reference replays every launch from the host each step. */
+typedef struct tam_graph tam_graph;
+int tam_graph_capture_rk4(tam_batch *b, int32_t dtype, const tam_wave_block *blocks,
+                          int32_t nblocks, int32_t max_points_per_block, void *y, void *ta,
+                          void *tb, void *acc, int64_t arena_elems, int32_t nvars,
+                          const void *factor_arena, int64_t factor_elems, double dt,
+                          int32_t steps, int32_t device, tam_graph **out);
+int tam_graph_launch(tam_graph *g, void *stream);
+void tam_graph_free(tam_graph *g);
+
 /* The transpose of a stage's right-hand side with its cotangent formed on
  * the fly: out = R^T (c1*g + c2*xprev) (xprev may be NULL), and when ybar is
  * not NULL, ybar += xprev at every stored point.  out may alias none of g,
@@ -417,6 +433,17 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
 #define TAM_OPT_ONE_TAP 4
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
+
+/* The launch-option autotuner: times every combination of TAM_OPT_TILE_ITEMS
+ * (32 .. 512), TAM_OPT_THREADS (128, 256, 512) and, for Float64,
+ * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (best of `reps`
+ * fills after a warm-up, CUDA events on `stream`), leaves the fastest set
+ * and returns it.  The fills overwrite `work`'s ghosts (never an own
+ * point).  Synchronizes `stream`; re-tiling allocates, so not inside a
+ * stream capture.  The reference has no tuning. */
+int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
+                 int32_t reps, void *stream, int64_t *tile_items, int64_t *threads,
+                 int64_t *int_mul, double *best_ms);
 
 /* Read (and clear) the device error word of the schedule's last fills:
  * 0, or a tam_status a kernel recorded.  Synchronizes `stream`. */

@@ -122,6 +122,48 @@ def test_wave_graph_equals_eager(cuda_lib):
     assert torch.isfinite(y).all()
 
 
+def test_native_rk4_graph_equals_eager(cuda_lib):
+    """``tam_graph_capture_rk4``: the library's own graph of RK4 steps
+    replays the eager steps bit for bit."""
+    from treeamr.wave import WaveSolver
+    fss, scheds, batch = _small_batch(np.float32)
+    meshes.wave_initial(batch)
+    solver = WaveSolver(batch)
+    y0 = batch.arena.clone()
+    eager = y0.clone()
+    for _ in range(4):
+        solver.step(eager)
+    y = y0.clone()
+    graph = solver.native_graph(y, steps=2)
+    torch.cuda.synchronize()
+    assert torch.equal(y, y0)                       # capture runs nothing
+    graph.launch()
+    graph.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(y.view(torch.int32), eager.view(torch.int32))
+
+
+def test_native_autotune(cuda_lib):
+    """``tam_autotune`` leaves the fastest options set, and a fill with them
+    is the oracle's bit for bit."""
+    from treeamr.autotune import autotune
+    from treeamr.ghosts import device_schedule, fill_ghosts
+    f, fs, ops = meshes.quadrant_setup()
+    s = GhostSchedule(fs, ops)
+    fs.work = fs.work.cuda()
+    fs.factors = fs.factors.cuda()
+    host = np.random.default_rng(9).uniform(size=tuple(fs.work.shape))
+    fs.work.copy_(torch.from_numpy(host))
+    best = autotune(fs, s)
+    assert set(best) == {"tile_items", "threads", "int_mul"} and s._tuned_ms > 0
+    ds = device_schedule(s, 0)
+    assert ds.options()["tile_items"] == best["tile_items"]
+    fs.work.copy_(torch.from_numpy(host))
+    fill_ghosts(fs, s)
+    expect = oracle.fill(s, host.copy(), fs.nvars, fs.factors_host)
+    assert np.array_equal(fs.work.cpu().numpy(), expect)
+
+
 def test_wave_adjoint_dot_product(cuda_lib):
     """<M^n x, y> = <x, (M^T)^n y> for n = 10 RK4 steps, Float64."""
     from treeamr.wave import WaveSolver

@@ -32,7 +32,7 @@ TAM_METHOD_FUSED, TAM_METHOD_PLAIN = 0, 1
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu",
-           "tam_state.cu", "tam_boundary.cu"]
+           "tam_state.cu", "tam_boundary.cu", "tam_runtime.cpp"]
 
 
 class tam_stencil(C.Structure):
@@ -238,6 +238,16 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_autotune.argtypes = [vp, vp, i32, i64, vp, i32, vp, C.POINTER(i64), C.POINTER(i64),
+                                 C.POINTER(i64), C.POINTER(C.c_double)]
+    lib.tam_autotune.restype = C.c_int
+    lib.tam_graph_capture_rk4.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp, vp, i64, i32, vp,
+                                          i64, C.c_double, i32, i32, C.POINTER(vp)]
+    lib.tam_graph_capture_rk4.restype = C.c_int
+    lib.tam_graph_launch.argtypes = [vp, vp]
+    lib.tam_graph_launch.restype = C.c_int
+    lib.tam_graph_free.argtypes = [vp]
+    lib.tam_graph_free.restype = None
     lib.tam_fill_host_own.argtypes = [vp, C.POINTER(tam_state_layout), vp, vp, vp, i32, i64,
                                       vp, i32, i32, vp]
     lib.tam_fill_host_own.restype = C.c_int

@@ -7,7 +7,8 @@ result: the box points per warp tile, the threads per CTA, and whether the
 Float64 multiplies by short weight products run on the integer pipe.  The
 tuner times every candidate on the caller's own field set (CUDA events on the
 fill's stream, best of a few fills after a warm-up), keeps the fastest, and
-caches the choice per schedule and variable count.
+caches the choice per schedule and variable count.  The default grid runs in
+the library (``tam_autotune``); other candidate sets are timed from here.
 """
 from __future__ import annotations
 
@@ -52,6 +53,22 @@ def autotune(fs: FieldSet, sched: GhostSchedule, *, reps: int = 3,
         for k, v in cache[key].items():
             ds.set_option(k, v)
         return dict(cache[key])
+    if tuple(tile_items) == TILE_ITEMS and tuple(threads) == THREADS and int_mul is None:
+        # the native tuner (tam_autotune): the same grid, timed in the library
+        import ctypes as C
+        out = [C.c_int64(), C.c_int64(), C.c_int64()]
+        ms = C.c_double()
+        s = torch.cuda.current_stream(fs.work.device)
+        rc = ds.lib.tam_autotune(ds.handle, C.c_void_p(fs.work.data_ptr()), fs.nvars,
+                                 fs.nblocks(), C.c_void_p(fs.factors.data_ptr()), reps,
+                                 C.c_void_p(s.cuda_stream), C.byref(out[0]), C.byref(out[1]),
+                                 C.byref(out[2]), C.byref(ms))
+        from . import _native
+        _native.check(rc, ds.ctx, "tam_autotune")
+        best = {"tile_items": out[0].value, "threads": out[1].value, "int_mul": out[2].value}
+        cache[key] = dict(best)
+        sched._tuned_ms = ms.value
+        return dict(best)
     if int_mul is None:
         int_mul = (0, 1) if fs.T.itemsize == 8 else (0,)
     # every combination: the best tile and CTA size differ between the two

@@ -155,6 +155,22 @@ class WaveSolver:
                 self.step(y)
         return g
 
+    def native_graph(self, y: torch.Tensor, steps: int = 1) -> "NativeGraph":
+        """The same ``steps`` RK4 steps of ``y`` captured by the library
+        (``tam_graph_capture_rk4``); ``launch()`` replays them."""
+        ta, tb, acc = self.k[0], self.k[1], self.k[2]
+        b = self.batch
+        h = C.c_void_p()
+        rc = self.lib.tam_graph_capture_rk4(
+            b.handle, self.dtype_code, C.c_void_p(self.table.data_ptr()), self.nblocks,
+            self.max_points, C.c_void_p(y.data_ptr()), C.c_void_p(ta.data_ptr()),
+            C.c_void_p(tb.data_ptr()), C.c_void_p(acc.data_ptr()), y.numel(), b.nvars,
+            C.c_void_p(b.factor_arena.data_ptr()), b.factor_arena.numel(), float(self.dt),
+            steps, y.device.index or 0, C.byref(h))
+        if rc != 0:
+            raise _native.TamError(f"tam_graph_capture_rk4 failed ({rc})")
+        return NativeGraph(self.lib, h, (y, ta, tb, acc, self.table, b))
+
     # -- the adjoint -------------------------------------------------------------
     #
     # One step as the forward runs it, with P the fill (applied in place) and
@@ -210,3 +226,27 @@ class WaveSolver:
             ybar.add_(dloss(cur))
             self.step_adjoint(ybar)
         return ybar
+
+
+class NativeGraph:
+    """A graph of RK4 steps captured by the library; keeps what it reads
+    alive and frees the graph with itself."""
+
+    def __init__(self, lib, handle, keep):
+        self.lib, self.handle, self._keep = lib, handle, keep
+
+    def launch(self, stream: Optional[torch.cuda.Stream] = None):
+        s = stream if stream is not None else torch.cuda.current_stream(self._keep[0].device)
+        rc = self.lib.tam_graph_launch(self.handle, C.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise _native.TamError(f"tam_graph_launch failed ({rc})")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.tam_graph_free(h)
+            except Exception:
+                pass
+            self.handle = None
+
