@@ -34,8 +34,9 @@ from .forest import Forest, MortonKey, childoffset, parentkey, sortedchildkeys
 from .schedule import (COPY, PROLONG, RESTRICT, GroupKey, NeighbourTable, TransferGroup,
                        _nospan, copy_stencil, kind_stencil, merged_transfers, piece_copies,
                        piece_of, piece_primary, subpiece_list, subpiece_values)
+from .forest import axismap
 from .operators import boundedmode
-from .storage import FieldSet
+from .storage import FieldSet, mirrorcolumn
 
 REGRID_TAG = 50                     # the reference's stage tag of the transfer
 REGRID_KEPT_TAG = 51                # and of its kept-over-created pass
@@ -124,10 +125,10 @@ def regrid_kept_pairs(forest: Forest, oldleaves: Sequence[MortonKey], c):
             holders = [x for x in copies if x[0] == finest and kept[x[1]]]
             if not holders:
                 continue
-            _, s, _, delta, o = piece_primary(holders)
-            entries.append((sub, COPY, s, delta, o))
-        for kind, s, delta, o, spans in merged_transfers(entries, allowed):
-            key = GroupKey(kind, delta, o, 0, nomirror, spans)
+            _, s, _, delta, o, r = piece_primary(holders)[:6]
+            entries.append((sub, COPY, s, delta, o, r))
+        for kind, s, delta, o, spans, r in merged_transfers(entries, allowed):
+            key = GroupKey(kind, delta, o, 0, nomirror, spans, r)
             tb, sb = pairs.setdefault(key, ([], []))
             tb.append(j + 1)
             sb.append(s + 1)
@@ -169,7 +170,12 @@ class RegridTransfer:
             tb, sb = kept[key]
             st = tuple(copy_stencil(self.T, N, self.G[d], self.c[d], key.direction[d],
                                     span=key.span[d]) for d in range(D))
-            self.kept_groups.append(TransferGroup(key, st, tb, sb, 0, REGRID_KEPT_TAG))
+            # across a seam the turned copy, with the turn's axis map and sign
+            # column (src/regrid.jl:918-920)
+            axes = axismap(key.orientation, *forest.seam_plane(), D) if key.orientation \
+                else None
+            fcol = mirrorcolumn((0,) * D) + 3 ** D * key.orientation if key.orientation else 0
+            self.kept_groups.append(TransferGroup(key, st, tb, sb, fcol, REGRID_KEPT_TAG, axes))
         self._device = {}
         self._kept_device = {}
 
@@ -219,7 +225,7 @@ class RegridTransfer:
                     pass
 
     def run(self, old_work: torch.Tensor, new_work: torch.Tensor, nvars: int,
-            stream: Optional[torch.cuda.Stream] = None):
+            stream: Optional[torch.cuda.Stream] = None, factors=None, rotvars=None):
         """The transfer from ``old_work`` (old leaves) into ``new_work``'s own
         points (new leaves), then the kept-over-created pass within
         ``new_work``, on the device."""
@@ -234,19 +240,29 @@ class RegridTransfer:
                                      C.c_void_p(s.cuda_stream))
         _native.check(rc, ctx, "tam_regrid_transfer")
         if self.kept_groups:
-            self.run_kept(new_work, nvars, stream=s)
+            self.run_kept(new_work, nvars, stream=s, factors=factors, rotvars=rotvars)
 
     def run_kept(self, new_work: torch.Tensor, nvars: int,
-                 stream: Optional[torch.cuda.Stream] = None):
-        """The kept-over-created pass alone, within ``new_work``."""
+                 stream: Optional[torch.cuda.Stream] = None, factors=None, rotvars=None):
+        """The kept-over-created pass alone, within ``new_work``; a copy across
+        a seam reads the field set's factor and variable tables."""
         if new_work.device.type != "cuda" or new_work.shape[0] != self.nnew:
             raise ValueError("the new array must be on a CUDA device and hold the new leaves")
         if not self.kept_groups:
             return
         lib, ctx, desc, h = self._upload_kept(new_work.device.index or 0)
         s = stream if stream is not None else torch.cuda.current_stream(new_work.device)
-        rc = lib.tam_fill(h, C.c_void_p(new_work.data_ptr()), nvars, self.nnew, None,
-                          REGRID_KEPT_TAG, REGRID_KEPT_TAG, C.c_void_p(s.cuda_stream))
+        if any(g.orientation for g in self.kept_groups):
+            if factors is None or rotvars is None:
+                raise ValueError("this regrid's kept-over-created pass turns copies across a "
+                                 "seam: pass the field set's factors and rotvars")
+            rc = lib.tam_fill_ex(h, C.c_void_p(new_work.data_ptr()), None, nvars, self.nnew,
+                                 C.c_void_p(factors.data_ptr()), C.c_void_p(rotvars.data_ptr()),
+                                 REGRID_KEPT_TAG, REGRID_KEPT_TAG, _native.TAM_METHOD_FUSED,
+                                 C.c_void_p(s.cuda_stream))
+        else:
+            rc = lib.tam_fill(h, C.c_void_p(new_work.data_ptr()), nvars, self.nnew, None,
+                              REGRID_KEPT_TAG, REGRID_KEPT_TAG, C.c_void_p(s.cuda_stream))
         _native.check(rc, ctx, "tam_fill (kept-over-created pass)")
 
 
@@ -274,7 +290,7 @@ def regrid(fs: FieldSet, operators, *, refine: Sequence[MortonKey] = (),
     t = RegridTransfer(forest, oldleaves, fs.G, fs.centering, fs.T, operators)
     new = torch.zeros((forest.nleaves(),) + tuple(fs.work.shape[1:]), dtype=fs.work.dtype,
                       device=fs.work.device)
-    t.run(fs.work, new, fs.nvars)
+    t.run(fs.work, new, fs.nvars, factors=fs.factors, rotvars=getattr(fs, "rotvars", None))
     fs.work = new
     fs.generation = forest.generation
     return t

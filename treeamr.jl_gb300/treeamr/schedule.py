@@ -452,7 +452,7 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
             continue
         r, nbrs = forest.turned_neighbors(k, delta)
         if table is not None:
-            table.remember(delta, nbrs)
+            table.remember(delta, nbrs, r)
         if not nbrs:
             boundaries.append(boundary_region(forest, k, b, delta, region, G, c))
             continue
@@ -465,11 +465,11 @@ def block_sources(pairs: Dict[GroupKey, Tuple[List[int], List[int]]],
             if parts is None:
                 record(PROLONG, childoffset(k), k.level, src, delta, turns=r)
             else:
-                for kind, dirn, span, s in parts:
+                for kind, dirn, span, s, via in parts:
                     if kind == PROLONG:
-                        record(PROLONG, childoffset(k), k.level, s, delta, span)
+                        record(PROLONG, childoffset(k), k.level, s, delta, span, turns=r)
                     else:
-                        record(COPY, zero, 0, s, dirn, span)
+                        record(COPY, zero, 0, s, dirn, span, turns=via)
         else:
             # each finer neighbour by its offset in its virtual parent,
             # where this block sees it across a seam
@@ -520,11 +520,11 @@ def mirror_sources(pairs, boundaries, forest: Forest, G, c, b, delta, dprime, wa
         if parts is None:
             record(PROLONG, childoffset(k), k.level, src, turns=r)
         else:
-            for kind, dirn, span, s in parts:
+            for kind, dirn, span, s, via in parts:
                 if kind == PROLONG:
-                    record(PROLONG, childoffset(k), k.level, s, tuple(delta), span)
+                    record(PROLONG, childoffset(k), k.level, s, tuple(delta), span, turns=r)
                 else:
-                    record(COPY, zero, 0, s, dirn, span)
+                    record(COPY, zero, 0, s, dirn, span, turns=via)
     else:
         wallside = [0 if delta[d] < 0 else 1 for d in range(D)]
         for nbr in nbrs:
@@ -605,7 +605,9 @@ def piece_span(cls: int) -> int:
 
 class NeighbourTable:
     """The neighbours of one block per direction, looked up once
-    (``src/schedule.jl:1733-1782``): ``(level or -1, [(leaf, offset)])``."""
+    (``src/schedule.jl:1742-1779``): ``(level or -1, [(leaf, offset, turns)])``,
+    each finer neighbour's child offset taken into the virtual frame where
+    this block sees it across a seam (``seam_offset``)."""
 
     def __init__(self, forest: Forest, j: int):
         self.forest = forest
@@ -613,11 +615,12 @@ class NeighbourTable:
         self.level = forest.leaves[j].level
         self.entries = {}
 
-    def remember(self, delta, nbrs):
+    def remember(self, delta, nbrs, r: int = 0):
         if not nbrs:
             e = (-1, [])
         else:
-            e = (nbrs[0].level, [(self.forest.find_leaf(n), childoffset(n)) for n in nbrs])
+            e = (nbrs[0].level, [(self.forest.find_leaf(n), seam_offset(self.forest, n, r), r)
+                                 for n in nbrs])
         self.entries[tuple(delta)] = e
         return e
 
@@ -625,20 +628,64 @@ class NeighbourTable:
         delta = tuple(delta)
         e = self.entries.get(delta)
         if e is None:
-            e = self.remember(delta, self.forest.oriented_neighbors(self.forest.leaves[self.j],
-                                                                   delta))
+            r, nbrs = self.forest.turned_neighbors(self.forest.leaves[self.j], delta)
+            e = self.remember(delta, nbrs, r)
         return e
+
+
+def subpiece_position(forest: Forest, k: MortonKey, sub) -> Tuple[int, ...]:
+    """The midpoint of sub-piece ``sub`` of leaf ``k`` at ``k``'s level, in
+    units of a quarter of a block's edge (``src/schedule.jl:1856-1861``)."""
+    rp = forest.root_position(k.root)
+    return tuple(4 * ((rp[d] << k.level) + k.coords[d]) + sub[d] for d in range(forest.D))
+
+
+def real_position(forest: Forest, p, r: int, lvl: int) -> Tuple[int, ...]:
+    """A virtual position mapped back across the seam as a naive node is
+    (``src/schedule.jl:1863-1879``); off the seam the position itself."""
+    if r == 0:
+        return tuple(p)
+    d1, d2 = forest.seam_plane()
+    a, b = p[d1], p[d2]
+    if r == 1:
+        a2, b2 = b, -a
+    elif r == 3:
+        a2, b2 = -b, a
+    elif forest.ishalfturn():
+        a2, b2 = -a, 4 * (forest.roots[d2] << lvl) - b
+    else:
+        a2, b2 = -a, -b
+    out = list(p)
+    out[d1], out[d2] = a2, b2
+    return tuple(out)
+
+
+def real_classes(forest: Forest, cls, r: int) -> Tuple[int, ...]:
+    """A piece's classes seen in the virtual frame of orientation ``r``, in
+    the real leaf's own frame (``src/schedule.jl:1900-1912``)."""
+    if r == 0:
+        return tuple(cls)
+    d1, d2 = forest.seam_plane()
+    a, b = cls[d1], cls[d2]
+    a2, b2 = {1: (b, 2 - a), 3: (2 - b, a)}.get(r, (2 - a, 2 - b))
+    out = list(cls)
+    out[d1], out[d2] = a2, b2
+    return tuple(out)
 
 
 def piece_copies(t: NeighbourTable, sub, c):
     """Every copy of sub-piece ``sub`` of ``t``'s block on its level or a finer
-    one, as ``(level, leaf, class, direction, offset)``, its own first
-    (``src/schedule.jl:1794-1854``; one brick, no seams or glue, so every copy
-    lies at the same position)."""
+    one, as ``(level, leaf, class, direction, offset, turns, position)``, its
+    own first (``src/schedule.jl:1794-1854``): a copy across a seam has its
+    classes and position in the real leaf's frame, so that the members of a
+    seam point's orbit compare by position; off the seam every copy lies at
+    the asking block's position."""
     D = len(c)
     zero = (0,) * D
     cls = piece_of(sub)
-    copies = [(t.level, t.j, cls, zero, zero)]
+    forest = t.forest
+    vpos = subpiece_position(forest, forest.leaves[t.j], sub)
+    copies = [(t.level, t.j, cls, zero, zero, 0, vpos)]
     side = tuple((-1 if cls[d] == 0 else 1) if (c[d] == 1 and cls[d] != 1) else 0
                  for d in range(D))
     for m in range(1, 1 << D):
@@ -650,10 +697,11 @@ def piece_copies(t: NeighbourTable, sub, c):
             continue
         across = tuple(cls[d] if delta[d] == 0 else 2 - cls[d] for d in range(D))
         if lvl == t.level:
-            leaf, _ = nbrs[0]
-            copies.append((lvl, leaf, across, delta, zero))
+            leaf, _, r = nbrs[0]
+            copies.append((lvl, leaf, real_classes(forest, across, r), delta, zero, r,
+                           real_position(forest, vpos, r, t.level)))
             continue
-        for leaf, o in nbrs:
+        for leaf, o, r in nbrs:
             holds = all(delta[d] != 0 or
                         (o[d] == (1 if sub[d] == 3 else 0) if c[d] == 0 else
                          (sub[d] == 2 or o[d] == (1 if sub[d] >= 3 else 0)))
@@ -670,16 +718,19 @@ def piece_copies(t: NeighbourTable, sub, c):
                     fcls.append(2 if o[d] == 0 else 0)
                 else:
                     fcls.append(cls[d] if sub[d] in (0, 4) else 1)
-            copies.append((lvl, leaf, tuple(fcls), delta, o))
+            copies.append((lvl, leaf, real_classes(forest, tuple(fcls), r), delta, o, r,
+                           real_position(forest, vpos, r, t.level)))
     return copies
 
 
 def piece_primary(copies):
-    """The finest level, then the greatest class tuple; the first on a tie
-    (``src/schedule.jl:1921``)."""
+    """The finest level, then the lexicographically greatest real position
+    (which picks one member of a seam point's orbit, and is no choice off
+    the seam), then the greatest class tuple; the first on a tie
+    (``src/schedule.jl:1914-1921``)."""
     best, bkey = None, None
     for x in copies:
-        key = (-x[0], tuple(-v for v in x[2]))
+        key = (-x[0], tuple(-v for v in x[6]), tuple(-v for v in x[2]))
         if bkey is None or key < bkey:
             best, bkey = x, key
     return best
@@ -697,14 +748,18 @@ def box_spans(subs, allowed):
 
 def merged_transfers(entries, allowed):
     """Stage 0's merging (``src/schedule.jl:2093-2125``): one transfer per
-    source, direction and offset over the bounding box of its sub-pieces where
-    they fill it; restrictions merged within one piece of the target only."""
+    source, direction, offset and orientation over the bounding box of its
+    sub-pieces where they fill it; restrictions merged within one piece of
+    the target only.  Entries ``(sub, kind, source, direction, offset[,
+    turns])``; out ``(kind, source, direction, offset, spans, turns)``."""
     bysource = {}
-    for sub, kind, s, delta, o in entries:
-        bysource.setdefault((KINDRANK[kind], s, delta, o), []).append(sub)
+    for e in entries:
+        sub, kind, s, delta, o = e[:5]
+        r = e[5] if len(e) > 5 else 0
+        bysource.setdefault((KINDRANK[kind], s, delta, o, r), []).append(sub)
     out = []
     for key in sorted(bysource):
-        rank, s, delta, o = key
+        rank, s, delta, o, r = key
         kind = COPY if rank == KINDRANK[COPY] else RESTRICT
         subs = list(dict.fromkeys(bysource[key]))
         spans = box_spans(subs, allowed) if kind == COPY else None
@@ -714,11 +769,11 @@ def merged_transfers(entries, allowed):
                 spans = box_spans(part, allowed)
                 if spans is None:
                     for p in part:
-                        out.append((kind, s, delta, o, tuple(span_code(x, x) for x in p)))
+                        out.append((kind, s, delta, o, tuple(span_code(x, x) for x in p), r))
                 else:
-                    out.append((kind, s, delta, o, spans))
+                    out.append((kind, s, delta, o, spans, r))
         else:
-            out.append((kind, s, delta, o, spans))
+            out.append((kind, s, delta, o, spans, r))
     return out
 
 
@@ -741,25 +796,26 @@ def unify_transfers(t: NeighbourTable, c):
             copies = piece_copies(t, piece_representative(cls, c), c)
             primaries[i] = piece_primary(copies)
             shared[i] = 1 if all(x[0] == lvl for x in copies) else 2
-            _, s, scls, _, _ = primaries[i]
+            s, scls = primaries[i][1], primaries[i][2]
             if s == b and scls == cls:
                 bits |= 1 << i
         if all(x == 1 for x in cls):
             continue
-        slvl, s, scls, delta, o = primaries[i] if shared[i] == 1 else \
-            piece_primary(piece_copies(t, sub, c))
+        slvl, s, scls, delta, o, r = (primaries[i] if shared[i] == 1 else
+                                      piece_primary(piece_copies(t, sub, c)))[:6]
         if s == b and scls == cls:
             continue
-        entries.append((sub, COPY if slvl == lvl else RESTRICT, s, delta, o))
+        entries.append((sub, COPY if slvl == lvl else RESTRICT, s, delta, o, r))
     return merged_transfers(entries, subpiece_values(c, forest.N)), bits
 
 
 def unify_sources(pairs, forest: Forest, c, b: int, table: NeighbourTable) -> int:
-    """Stage 0's transfers into block ``b`` (``src/schedule.jl:1948-1988``)."""
+    """Stage 0's transfers into block ``b`` (``src/schedule.jl:1948-1988``),
+    a copy across a seam keyed by its orientation."""
     D = len(c)
     out, bits = unify_transfers(table, c)
-    for kind, s, delta, o, spans in out:
-        _record(pairs, GroupKey(kind, delta, o, 0, (0,) * D, spans), b, s)
+    for kind, s, delta, o, spans, r in out:
+        _record(pairs, GroupKey(kind, delta, o, 0, (0,) * D, spans, r), b, s)
     return bits
 
 
@@ -768,7 +824,8 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
     split where a block of ``k``'s level holds a face-plane row along a
     tangential vertex-like dimension (``src/schedule.jl:1432-1507``).
     ``None`` where nothing splits; otherwise parts ``(kind, direction, span,
-    source)`` (0-based source)."""
+    source, turns)`` (0-based source; a copy across a seam keeps its
+    orientation, a prolongation the one its caller has)."""
     D = forest.D
     tdims = [d for d in range(D) if delta[d] == 0 and c[d] == 1]
     if not tdims:
@@ -778,7 +835,7 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
 
     def holder(dirn):
         if dirn not in found:
-            nbrs = forest.oriented_neighbors(k, dirn)
+            r, nbrs = forest.turned_neighbors(k, dirn)
             if not nbrs:
                 found[dirn] = None
             else:
@@ -787,7 +844,7 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
                     raise RuntimeError(f"the ghost of {k} in direction {delta} has a face-plane "
                                        f"row held by a finer block across {dirn}; 2:1 balance "
                                        "forbids that, so this is a bug")
-                found[dirn] = (lv, forest.find_leaf(nbrs[0]))
+                found[dirn] = (lv, forest.find_leaf(nbrs[0]), r)
         return found[dirn]
 
     pieces = list(_product_dim1_fastest([(0, 1, 2)] * len(tdims)))
@@ -804,20 +861,20 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
             h = holder(tuple(dirn))
             if h is None:
                 continue
-            lv, j = h
+            lv, j, r = h
             if j == coarse:
                 continue
             if lv == l and best is None:
-                best = (m, j)
+                best = (m, j, r)
         if best is None:
             sources.append(None)
             continue
-        m, j = best
+        m, j, r = best
         dirn = list(delta)
         for i, (d, s) in enumerate(plane):
             if (m >> i) & 1:
                 dirn[d] = s
-        sources.append((tuple(dirn), j))
+        sources.append((tuple(dirn), j, r))
     if all(s is None for s in sources):
         return None
 
@@ -841,14 +898,14 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
             ls = {0: 0, 1: 3, 2: 4}
             span = tuple(span_code(fs[lo[tdims.index(d)]], ls[hi[tdims.index(d)]])
                          if d in tdims else -1 for d in range(D))
-            parts.append((PROLONG, tuple(delta), span, coarse))
+            parts.append((PROLONG, tuple(delta), span, coarse, 0))
         else:
             for cls in rest:
-                parts.append((PROLONG, tuple(delta), spanof(cls), coarse))
+                parts.append((PROLONG, tuple(delta), spanof(cls), coarse, 0))
     for cls, s in zip(pieces, sources):
         if s is None:
             continue
-        parts.append((COPY, s[0], spanof(cls), s[1]))
+        parts.append((COPY, s[0], spanof(cls), s[1], s[2]))
     return parts
 
 
