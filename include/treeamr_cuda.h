@@ -402,6 +402,22 @@ typedef struct tam_state_layout {
 int tam_scatter(const tam_state_layout *layout, const void *state, void *work, void *stream);
 int tam_gather(const tam_state_layout *layout, const void *work, void *state, void *stream);
 
+/* A seam's axis projection (stage P's axis part, axis_project!,
+ * src/ghosts.jl:599-660, 736-770), run after stage P and before stage 0:
+ * each of the `npoints` axis points, at element offset points[i] of its
+ * variable 0 in `work` (block * nvars * block_points + its offset in the
+ * block), gets for every variable v the mean of its images under the
+ * orbit's powers of the set's map, t_r = factors[v + nvars * ncol * r] *
+ * work[.. variable rotvars[v + nvars * r] - 1 ..] (t_0 the value itself),
+ * summed in pairs a half turn apart: ((t_0 + t_2) + (t_1 + t_3)) / 4 for
+ * members = 4 (a quarter turn) or (t_0 + t_2) / 2 for members = 2 (a half
+ * turn).  `buffer` (npoints * nvars elements) holds the means, all gathered
+ * before any is written.  ncol is 3^D, the factor table's columns per
+ * orientation.  A variable table naming no variable gives NaN. */
+int tam_axis_project(int32_t dtype, const int64_t *points, int64_t npoints, int32_t members,
+                     void *work, int32_t nvars, int64_t block_points, const void *factors,
+                     int32_t ncol, const int32_t *rotvars, void *buffer, void *stream);
+
 /* tam_fill_host moving only what the fill reads up: the own points of
  * host_in (the box `layout` describes, ghosts[d] .. ghosts[d] + own[d] - 1
  * along d) are copied into device_work by a kernel that reads host_in

@@ -213,3 +213,40 @@ def cell_boundary(fs, host: np.ndarray, regions, g) -> np.ndarray:
                     val = T(val + T(ur - ev(xr, v)))
                 host[(r.block, v) + tuple(i - 1 for i in reversed(idx))] = val
     return host
+
+
+def axis_project(schedule, host: np.ndarray, nvars: int, factors: np.ndarray,
+                 rotvars: np.ndarray) -> np.ndarray:
+    """A seam's axis projection on the host, in place (``axis_project!``,
+    ``mean_gather_kernel!`` in its paired form, src/ghosts.jl:599-660,
+    736-770): each axis point's variable ``v`` becomes
+    ``((t_0 + t_2) + (t_1 + t_3)) / 4`` (a half turn: ``(t_0 + t_2) / 2``) with
+    ``t_r = factors[v, 3^D r] * u[rotvars[v, r] - 1]`` (``t_0 = u[v]``), every
+    mean gathered before any is written, in the element type."""
+    pts, orbit = schedule.axis, schedule.axis_orbit
+    if not pts:
+        return host
+    T = host.dtype.type
+    D = schedule.forest.D
+    ncol = 3 ** D
+    M = len(orbit)
+    means = []
+    for b, idx in pts:
+        at = tuple(i - 1 for i in reversed(idx))
+        vals = []
+        for v in range(nvars):
+            def term(r):
+                if r == 0:
+                    return T(host[(b, v) + at])
+                sv = int(rotvars[v, r]) - 1
+                return T(T(factors[v, ncol * r]) * T(host[(b, sv) + at]))
+            acc = T(term(orbit[0]) + term(orbit[1]))
+            if M == 4:
+                acc = T(acc + T(term(orbit[2]) + term(orbit[3])))
+            vals.append(T(acc / T(M)))
+        means.append(vals)
+    for (b, idx), vals in zip(pts, means):
+        at = tuple(i - 1 for i in reversed(idx))
+        for v in range(nvars):
+            host[(b, v) + at] = vals[v]
+    return host

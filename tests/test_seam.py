@@ -383,10 +383,12 @@ def unfold_data(quad, fs, full, image, back, ff, q, half):
     """The full plane's own points: the quadrant's, turned.  Full leaf
     ``kf`` is quadrant leaf ``kq`` turned by ``r``, so its own point ``p``
     holds ``sign[v] * u_kq[sigma[v]](R^{-r} p)``, located with exact
-    positions."""
+    positions (cell centres, or vertices along a vertex-like dimension)."""
     D, N = quad.D, quad.N
     d1, d2 = quad.seam_plane()
     G = fs.G
+    c = fs.c
+    half_cell = [F(0) if c[d] else F(1, 2) for d in range(D)]
     host_q = fs.work.numpy()
     out = np.full(tuple(ff.work.shape), np.nan, dtype=fs.T)
     qindex = {k: i for i, k in enumerate(quad.leaves)}
@@ -401,17 +403,19 @@ def unfold_data(quad, fs, full, image, back, ff, q, half):
         h = F(1, N << kf.level)
         shift = tuple(quad.roots[d1] if (d == d1 or (d == d2 and not half)) else 0
                       for d in range(D))
-        for I in itertools.product(range(N), repeat=D):
-            x = [lof[d] + (I[d] + F(1, 2)) * h - shift[d] for d in range(D)]
+        for I in itertools.product(*[range(N + c[d]) for d in range(D)]):
+            x = [lof[d] + (I[d] + half_cell[d]) * h - shift[d] for d in range(D)]
             if r:
                 if half:
-                    c = F(quad.roots[d2], 2)
-                    x[d1], x[d2] = -x[d1], 2 * c - x[d2]
+                    cc = F(quad.roots[d2], 2)
+                    x[d1], x[d2] = -x[d1], 2 * cc - x[d2]
                 else:
                     for _ in range((4 - r) % 4):             # R^{-r} = R^{4-r}
                         x[d1], x[d2] = -x[d2], x[d1]
-            J = [int((x[d] - loq[d]) / h - F(1, 2)) for d in range(D)]
-            assert all(0 <= J[d] < N for d in range(D))
+            Jf = [(x[d] - loq[d]) / h - half_cell[d] for d in range(D)]
+            assert all(j.denominator == 1 for j in Jf)
+            J = [int(j) for j in Jf]
+            assert all(0 <= J[d] < N + c[d] for d in range(D))
             for v in range(nv):
                 val = host_q[(bq, sigma[v] - 1) + tuple(G[d] + J[d] for d in reversed(range(D)))]
                 out[(bf, v) + tuple(G[d] + I[d] for d in reversed(range(D)))] = \
@@ -419,21 +423,47 @@ def unfold_data(quad, fs, full, image, back, ff, q, half):
     return out
 
 
-def quadrant_case(D, plane, other, *, half=False, T=np.float64, seed=3):
+def seam_fill(s, fs, host, *, one_tap=True, hook_zero=True, first=-1, last=0x7FFFFFFF):
+    """The oracle's fill of a set over a seam, in place: stage P, the axis
+    projection, stage 0 and phase 1, the hook regions set to zero, then the
+    prolongations."""
+    from treeamr.ghosts import turns_variables
+    rv = fs.rotvars_host
+    kw = dict(rotvars=rv, one_tap=one_tap)
+    oracle.fill(s, host, fs.nvars, fs.factors_host, first=first, last=-1, **kw)
+    if s.axis and turns_variables(fs):
+        oracle.axis_project(s, host, fs.nvars, fs.factors_host, rv)
+    oracle.fill(s, host, fs.nvars, fs.factors_host, first=0, last=1, **kw)
+    if hook_zero:
+        for r in s.boundaries:
+            host[(r.block, slice(None)) +
+                 tuple(slice(a - 1, z) for a, z in reversed(r.region))] = 0
+    return oracle.fill(s, host, fs.nvars, fs.factors_host, first=2, last=last, **kw)
+
+
+def quadrant_case(D, plane, other, *, half=False, T=np.float64, seed=3, C=None):
     """The quadrant's field set with NaN ghosts and random own points, its
-    schedule, and the full plane's field set with the same data turned."""
+    schedule, and the full plane's field set with the same data turned.  A
+    set with a vertex-like dimension has its own points unified first (a
+    fill, whose stage 0 makes the copies of a point one number through the
+    turn and whose axis projection makes the axis its own image), so that
+    the full plane's copies of a point agree."""
     quad = seam_forest(D, plane, other, half=half)
     q = (vector_halfturn if half else vector_rotation)(D, plane)
     kw = {"halfturn": q} if half else {"rotation": q}
-    fs = FieldSet(quad, D + 1, G=2, T=T, parity=vector_parity(D, plane, other), **kw)
+    fs = FieldSet(quad, D + 1, G=2, T=T, parity=vector_parity(D, plane, other), centering=C,
+                  **kw)
     rng = np.random.default_rng(seed)
     host = np.full(tuple(fs.work.shape), np.nan, dtype=T)
-    own = (slice(None), slice(None)) + tuple(slice(2, 2 + quad.N) for _ in range(D))
+    own = (slice(None), slice(None)) + fs.interior()
     host[own] = rng.uniform(-1, 1, size=host[own].shape).astype(T)
-    fs.work = torch.from_numpy(host)
     s = GhostSchedule(fs, OPS4)
+    if any(fs.c):
+        unified = seam_fill(s, fs, host.copy())
+        host[own] = unified[own]
+    fs.work = torch.from_numpy(host)
     full, image, back = (unfolded_halfturn_forest if half else unfolded_forest)(quad)
-    ff = FieldSet(full, D + 1, G=2, T=T, parity=vector_parity(D, plane, other))
+    ff = FieldSet(full, D + 1, G=2, T=T, parity=vector_parity(D, plane, other), centering=C)
     ff.work = torch.from_numpy(unfold_data(quad, fs, full, image, back, ff, q, half))
     return quad, fs, s, full, ff, image
 
@@ -848,3 +878,82 @@ def test_gpu_adjoint_of_a_pair_member_is_refused(cuda_lib):
     a.work, a.factors, a.rotvars = a.work.cuda(), a.factors.cuda(), a.rotvars.cuda()
     with pytest.raises(Exception, match="RotationPair"):
         fill_ghosts_adjoint(a, sa, torch.zeros_like(a.work))
+
+
+
+# --- sets with vertex-like dimensions over a seam -----------------------------------------
+
+VERTEX_CASES = [("q", 2, (1, 2), "none"), ("q", 2, (2, 1), "none"),
+                ("q", 3, (1, 2), "periodic"), ("q", 3, (3, 1), "outer"),
+                ("h", 2, (1, 2), "none"), ("h", 3, (1, 2), "periodic")]
+
+
+def _centering(D, plane, which):
+    from treeamr.storage import vertexcentered
+    if which == "vertex":
+        return vertexcentered(D)
+    # vertex-like along the plane's two dimensions only (symmetric in the turn)
+    return tuple("vertex" if d + 1 in plane else "cell" for d in range(D))
+
+
+@pytest.mark.parametrize("case", VERTEX_CASES)
+@pytest.mark.parametrize("which", ["vertex", "plane"])
+def test_a_vertex_like_quadrant_is_the_turned_full_plane(case, which):
+    """``test/rotate_tests.jl:437-456`` for vertex-like sets: the seam
+    planes are copies of each other through the turn (stage 0 across the
+    seam) and the axis its own image (the projection); after a fill every
+    stored point is the full plane's to 1e-13 and none is undefined."""
+    kind, D, plane, other = case
+    C = _centering(D, plane, which)
+    quad, fs, s, full, ff, image = quadrant_case(D, plane, other, half=kind == "h", C=C)
+    assert any(g.orientation and g.stage == 0 for g in s.groups)
+    assert s.axis
+    got = seam_fill(s, fs, fs.work.numpy().copy())
+    want = seam_fill(GhostSchedule(ff, OPS4), ff, ff.work.numpy().copy())
+    _agree(quad, full, image, got, want)
+    assert not np.isnan(got).any()
+    # the fill is idempotent on unified data: a second fill changes no bit
+    again = seam_fill(s, fs, got.copy())
+    assert np.array_equal(nanbits(again), nanbits(got))
+
+
+@pytest.mark.parametrize("case", VERTEX_CASES[:3])
+def test_the_vertex_schedule_partitions_the_ghosts_across_the_seam(case):
+    """Every stored point outside the closed own box is written exactly once
+    by a transfer or the hook (``test/rotate_tests.jl:491-524``)."""
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h",
+                                    C=_centering(D, plane, "vertex"))
+    counts = s.write_counts()
+    N, G = quad.N, 2
+    inside = np.ones(counts.shape[1:], bool)
+    for ax in range(D):
+        idx = np.arange(counts.shape[1 + ax])
+        mask = (idx >= G) & (idx < G + N + 1)
+        shape = [1] * D
+        shape[ax] = -1
+        inside &= mask.reshape(shape)
+    assert (counts[:, inside] == 0).all() and (counts[:, ~inside] == 1).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", VERTEX_CASES)
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_vertex_like_fill_across_the_seam_bit_exact(cuda_lib, case, T):
+    """The device fill of a vertex-like set over a seam (turned stage-0
+    copies, the axis projection) is the oracle's bit for bit."""
+    from treeamr import fill_ghosts
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h", T=T,
+                                    C=_centering(D, plane, "vertex"))
+    host = fs.work.numpy().copy()
+    rng = np.random.default_rng(5)
+    host[(slice(None), slice(None)) + fs.interior()] = \
+        rng.uniform(-1, 1, size=host[(slice(None), slice(None)) + fs.interior()].shape)
+    fs.factors, fs.rotvars = fs.factors.cuda(), fs.rotvars.cuda()
+    for method, one_tap in (("fused", True), ("plain", False)):
+        expect = seam_fill(s, fs, host.copy(), one_tap=one_tap, hook_zero=False)
+        fs.work = torch.from_numpy(host.copy()).cuda()
+        fill_ghosts(fs, s, method=method)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), method

@@ -21,6 +21,12 @@
 
 namespace {
 
+// single roundings, so that no multiply-add is fused
+__device__ __forceinline__ double __fmul_rn_t(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float __fmul_rn_t(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_t(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_t(float a, float b) { return __fadd_rn(a, b); }
+
 template <typename T, bool TO_WORK>
 __global__ void __launch_bounds__(256) state_copy_kernel(T *__restrict__ work,
                                                          T *__restrict__ state, int64_t nrows,
@@ -183,4 +189,87 @@ extern "C" int tam_scatter(const tam_state_layout *layout, const void *state, vo
 extern "C" int tam_gather(const tam_state_layout *layout, const void *work, void *state,
                           void *stream) {
   return state_copy(false, layout, const_cast<void *>(work), state, stream);
+}
+
+// ---- a seam's axis (stage P's axis part) ----------------------------------------
+//
+// Each axis point is its own image under the turn, so its variables become
+// the mean of their images under the orbit's powers of the set's map
+// (axis_project!, mean_gather_kernel! in its paired form, src/ghosts.jl:
+// 599-660, 736-770): t_r = f(v, r) * u[rotvars(v, r)] (t_0 = u[v]), summed in
+// pairs a half turn apart, ((t_0 + t_2) + (t_1 + t_3)) / 4, or (t_0 + t_2) / 2
+// under a half turn.  Every mean is gathered into `buf` before any is
+// written, since a point's variables read one another.
+namespace {
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    axis_gather_kernel(const int64_t *__restrict__ points, int64_t n, int members,
+                       const T *__restrict__ work, int nvars, int64_t vol,
+                       const T *__restrict__ factors, int ncol, const int32_t *__restrict__ rotvars,
+                       T *__restrict__ buf) {
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n * nvars;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = it / nvars;
+    const int v = (int)(it - i * nvars);
+    const int64_t off = points[i];
+    bool bad = false;
+    auto term = [&](int r) -> T {
+      if (r == 0) return work[off + v * vol];
+      const int sv = rotvars[v + (int64_t)nvars * r] - 1;
+      if (sv < 0 || sv >= nvars) {
+        bad = true;
+        return T(0);
+      }
+      return __fmul_rn_t(factors[v + (int64_t)nvars * ((int64_t)ncol * r)], work[off + sv * vol]);
+    };
+    T acc = add_t(term(0), term(2));
+    if (members == 4) acc = add_t(acc, add_t(term(1), term(3)));
+    buf[it] = bad ? T(NAN) : acc / T(members);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) axis_write_kernel(const int64_t *__restrict__ points,
+                                                         int64_t n, T *__restrict__ work,
+                                                         int nvars, int64_t vol,
+                                                         const T *__restrict__ buf) {
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n * nvars;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = it / nvars;
+    const int v = (int)(it - i * nvars);
+    work[points[i] + v * vol] = buf[it];
+  }
+}
+
+}  // namespace
+
+extern "C" int tam_axis_project(int32_t dtype, const int64_t *points, int64_t npoints,
+                                int32_t members, void *work, int32_t nvars,
+                                int64_t block_points, const void *factors, int32_t ncol,
+                                const int32_t *rotvars, void *buffer, void *stream) {
+  if (npoints == 0) return TAM_OK;
+  if (!points || !work || !factors || !rotvars || !buffer || nvars < 1 || npoints < 0 ||
+      (members != 2 && members != 4) || block_points < 1 || ncol < 1)
+    return TAM_EINVAL;
+  const int64_t n = npoints * nvars;
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((n + threads - 1) / threads, 4096);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == TAM_F64) {
+    axis_gather_kernel<double><<<(unsigned)blocks, threads, 0, st>>>(
+        points, npoints, members, (const double *)work, nvars, block_points,
+        (const double *)factors, ncol, rotvars, (double *)buffer);
+    axis_write_kernel<double><<<(unsigned)blocks, threads, 0, st>>>(
+        points, npoints, (double *)work, nvars, block_points, (const double *)buffer);
+  } else if (dtype == TAM_F32) {
+    axis_gather_kernel<float><<<(unsigned)blocks, threads, 0, st>>>(
+        points, npoints, members, (const float *)work, nvars, block_points,
+        (const float *)factors, ncol, rotvars, (float *)buffer);
+    axis_write_kernel<float><<<(unsigned)blocks, threads, 0, st>>>(
+        points, npoints, (float *)work, nvars, block_points, (const float *)buffer);
+  } else {
+    return TAM_EINVAL;
+  }
+  return cudaGetLastError() == cudaSuccess ? TAM_OK : TAM_ECUDA;
 }

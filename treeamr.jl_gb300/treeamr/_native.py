@@ -238,6 +238,8 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i32, i64, vp, i32, i32, vp]
         f.restype = C.c_int
+    lib.tam_axis_project.argtypes = [i32, vp, i64, i32, vp, i32, i64, vp, i32, vp, vp, vp]
+    lib.tam_axis_project.restype = C.c_int
     lib.tam_autotune.argtypes = [vp, vp, i32, i64, vp, i32, vp, C.POINTER(i64), C.POINTER(i64),
                                  C.POINTER(i64), C.POINTER(C.c_double)]
     lib.tam_autotune.restype = C.c_int

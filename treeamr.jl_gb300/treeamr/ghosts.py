@@ -180,6 +180,61 @@ def check_fill(fs: FieldSet, schedule: GhostSchedule, pair: bool = False):
                          "with `rotation` (or `halfturn`)")
 
 
+def turns_variables(fs: FieldSet) -> bool:
+    """Whether the set's map across its forest's seam turns any variable:
+    where it does not, the axis projection is the identity
+    (``src/ghosts.jl:774-778``)."""
+    m = fs.halfturn if fs.forest.ishalfturn() else fs.rotation
+    return m is not None and list(m) != list(range(1, fs.nvars + 1))
+
+
+def run_axis(fs: FieldSet, schedule: GhostSchedule, stream=None):
+    """A seam's axis projection on the device (``tam_axis_project``), stage
+    P's axis part, between stage P and stage 0 (``src/ghosts.jl:1111-1116``)."""
+    if not schedule.axis or not turns_variables(fs):
+        return
+    dev = fs.work.device
+    cache = schedule.__dict__.setdefault("_axis_device", {})
+    key = (dev.index, fs.nvars, fs.T.name)
+    if key not in cache:
+        S = schedule.stored
+        vol = int(np.prod(S))
+        offs = []
+        for b, idx in schedule.axis:
+            o = 0
+            for d in reversed(range(fs.D)):
+                o = o * S[d] + (idx[d] - 1)
+            offs.append(b * fs.nvars * vol + o)
+        pts = torch.tensor(offs, dtype=torch.int64, device=dev)
+        buf = torch.empty(len(offs) * fs.nvars, dtype=fs.work.dtype, device=dev)
+        cache[key] = (pts, buf, vol)
+    pts, buf, vol = cache[key]
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    rc = _native.lib().tam_axis_project(
+        _native.TAM_F64 if fs.T == np.float64 else _native.TAM_F32,
+        C.c_void_p(pts.data_ptr()), pts.numel(), len(schedule.axis_orbit),
+        C.c_void_p(fs.work.data_ptr()), fs.nvars, vol, C.c_void_p(fs.factors.data_ptr()),
+        3 ** fs.D, C.c_void_p(fs.rotvars.data_ptr()), C.c_void_p(buf.data_ptr()),
+        C.c_void_p(s.cuda_stream))
+    if rc != 0:
+        raise _native.TamError(f"tam_axis_project failed ({rc})")
+
+
+def _runner(ds, fs, schedule, method, stream):
+    """``ds.run`` over a stage range, with a seam's axis projection inserted
+    between stage P and stage 0 where the range covers both."""
+    from .schedule import SELFIMAGE_TAG, UNIFY_TAG
+
+    def run(first, last):
+        if schedule.axis and first <= SELFIMAGE_TAG and last >= UNIFY_TAG:
+            ds.run(fs, first, SELFIMAGE_TAG, method, stream)
+            run_axis(fs, schedule, stream)
+            ds.run(fs, UNIFY_TAG, last, method, stream)
+        else:
+            ds.run(fs, first, last, method, stream)
+    return run
+
+
 def fill_pair(pair, schedules, *, boundary=None, method: str = "fused",
               stream: Optional[torch.cuda.Stream] = None):
     """``fill_ghosts!(pair, (sa, sb); boundary)`` (``src/ghosts.jl:2117-2180``):
@@ -246,13 +301,14 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
         # stage W: a hook that prescribes the wall planes writes their
         # primaries before stage P and stage 0 (src/ghosts.jl:1111-1113)
         boundary.apply_walls(fs, schedule, stream)
+    run = _runner(ds, fs, schedule, method, stream)
     if boundary is None or not schedule.boundaries:
-        ds.run(fs, _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST, method, stream)
+        run(_native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST)
         return fs
     if isinstance(boundary, CellBoundary) and boundary.relative:
         # the relative form in parts, each after the stage that fills the
         # ghosts it reads (src/ghosts.jl:1146-1160)
-        ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
+        run(_native.TAM_STAGE_ALL_FIRST, PHASE1_TAG)
         slots = set(boundary.slots(schedule))
         boundary.apply(fs, schedule, stream, slot=PHASE1_TAG)
         for tag in [t for t in schedule.stage_tags if t > PHASE1_TAG]:
@@ -260,7 +316,7 @@ def fill_ghosts(fs: FieldSet, schedule: GhostSchedule, *, boundary: Optional[Cal
             if tag in slots:
                 boundary.apply(fs, schedule, stream, slot=tag)
         return fs
-    ds.run(fs, _native.TAM_STAGE_ALL_FIRST, PHASE1_TAG, method, stream)
+    run(_native.TAM_STAGE_ALL_FIRST, PHASE1_TAG)
     if isinstance(boundary, CellBoundary):
         boundary.apply(fs, schedule, stream)        # the device hook
     else:

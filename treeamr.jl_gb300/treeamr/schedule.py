@@ -909,6 +909,45 @@ def ghost_plane_parts(forest: Forest, k: MortonKey, delta, dlook, c, coarse: int
     return parts
 
 
+def axis_points(forest: Forest, G, c, bits):
+    """A seam's axis points, ``([(block, 1-based stored index)], orbit)``
+    (``axis_points``, ``src/schedule.jl:2653-2690``): the points of the
+    blocks at the low corner of the seam's plane (a quarter turn), or at the
+    low face of d1 meeting the centre plane of d2 (a half turn), on the
+    pieces whose copy is the primary; the axis needs a vertex-like d1 and
+    d2.  Each is its own image under the turn, so its variables become the
+    mean of their images under the orbit's powers of the set's map, summed
+    in pairs a half turn apart: orbit ``(0, 2, 1, 3)``, or ``(0, 2)``."""
+    if not forest.hasrotating():
+        return [], ()
+    d1, d2 = forest.seam_plane()
+    if not (c[d1] == 1 and c[d2] == 1):
+        return [], ()
+    half = forest.ishalfturn()
+    D, N = forest.D, forest.N
+    out = []
+    for b, k in enumerate(forest.leaves):
+        lvl = k.level
+        rp = forest.root_position(k.root)
+        g = [(rp[d] << lvl) + k.coords[d] for d in range(D)]
+        if g[d1] != 0:
+            continue
+        n2 = forest.roots[d2] << lvl
+        if half:
+            cls2 = 0 if g[d2] == n2 // 2 else 2 if g[d2] + 1 == n2 // 2 else -1
+        else:
+            cls2 = 0 if g[d2] == 0 else -1
+        if cls2 < 0:
+            continue
+        for cls in closed_pieces(c):
+            if cls[d1] != 0 or cls[d2] != cls2 or not (bits[b] >> piece_index(cls)) & 1:
+                continue
+            rngs = [piece_range(N, G[d], c[d], piece_span(cls[d])) for d in range(D)]
+            for I in _product_dim1_fastest([list(r) for r in rngs]):
+                out.append((b, tuple(I)))
+    return out, ((0, 2) if half else (0, 2, 1, 3))
+
+
 def selfimage_sources(pairs, forest: Forest, c, b: int, parities, bits: int):
     """Stage P's transfers of block ``b``: every primary piece on a reflecting
     wall plane of a vertex-like dimension, keyed by mirror state 2 there
@@ -1009,11 +1048,6 @@ class GhostSchedule:
         self.parities = parity
         self.stored = tuple(N + 2 * g + cd for g, cd in zip(G, c))
         closed = any(cd == 1 for cd in c)
-        if closed and forest.hasrotating():
-            raise ValueError("a set with a vertex-like dimension over a forest with a rotating "
-                             "or half-turn seam is not built here: its seam planes are copies "
-                             "of one another through the turn, which needs stage 0 across the "
-                             "seam and the axis projection; use a cell-centred set")
 
         dirs = alldirections(D)
         pairs: Dict[GroupKey, Tuple[List[int], List[int]]] = {}
@@ -1027,6 +1061,8 @@ class GhostSchedule:
                 selfimage_sources(ppairs, forest, c, b, parity or [], bits[b])
         self.boundaries = boundaries
         self.primary_bits = bits
+        # a seam's axis, its own image under the turn: projected after stage P
+        self.axis, self.axis_orbit = axis_points(forest, G, c, bits)
         # stage W's regions, for a hook that prescribes the wall planes
         self.walls: List[BoundaryRegion] = []
         if closed:
