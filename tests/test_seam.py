@@ -546,8 +546,7 @@ def test_the_schedule_partitions_the_ghosts_across_the_seam(D, plane, other):
 
 def test_seam_refusals():
     """A rotation map is required, checked, and its tables composed
-    (``test/rotate_tests.jl:276-353``); a vertex-like set over a seam is
-    refused here; an asymmetric set is refused alone."""
+    (``test/rotate_tests.jl:276-353``)."""
     f = Forest((2, 2), N=8, rotating=(1, 2))
     with pytest.raises(ValueError, match="needs `rotation`"):
         FieldSet(f, 3, G=1)
@@ -559,8 +558,9 @@ def test_seam_refusals():
         FieldSet(f, 3, G=1, rotation=(2, 3, 1))
     assert FieldSet(f, 3, G=1, rotation=(1, -3, 2)).rotation == [1, -3, 2]
     assert FieldSet(Forest((2, 2), N=8), 1, G=1).rotvars is None
-    with pytest.raises(ValueError, match="vertex-like"):
-        GhostSchedule(FieldSet(f, 1, G=2, centering=("vertex", "vertex"), rotation=(1,)), OPS4)
+    # a vertex-like set over a seam is built: its axis is known to the schedule
+    vs = GhostSchedule(FieldSet(f, 1, G=2, centering=("vertex", "vertex"), rotation=(1,)), OPS4)
+    assert vs.axis and vs.axis_orbit == (0, 2, 1, 3)
     h = Forest((1, 2), N=8, halfturn=(1, 2))
     with pytest.raises(ValueError, match="needs `halfturn`"):
         FieldSet(h, 1, G=1)
