@@ -14,7 +14,6 @@ import torch
 
 import oracle
 from treeamr import FieldSet, Forest, GhostSchedule, Operators
-from treeamr.meshes import refine_where
 
 
 def nested_forest(D, N=4, roots=4, periodic=None):

@@ -23,7 +23,7 @@ from treeamr.forest import parentkey
 from treeamr.regrid import (REGRID_KEPT_TAG, REGRID_TAG, RegridTransfer, regrid,
                             regrid_kept_pairs, regrid_sources)
 from treeamr.schedule import COPY, PROLONG, RESTRICT, TransferGroup
-from treeamr.storage import edgecentered, facecentered, vertexcentered
+from treeamr.storage import edgecentered, facecentered
 
 
 def _move(D, N=8):

@@ -8,7 +8,7 @@ import torch
 
 import oracle
 from _helpers import awkward_fill, nanbits, nested_forest
-from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+from treeamr import FieldSet, GhostSchedule, fill_ghosts, meshes
 from treeamr.state import (gather, ownextents, scatter, scatter_fill, statearray, statelength,
                            statevector)
 from treeamr.storage import vertexcentered

@@ -10,9 +10,8 @@ keeps working on its own: its ``work`` is a view into the arena.
 from __future__ import annotations
 
 import ctypes as C
-from typing import List, Optional, Sequence
+from typing import Optional, Sequence
 
-import numpy as np
 import torch
 
 from . import _native

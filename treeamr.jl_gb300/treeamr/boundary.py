@@ -19,13 +19,12 @@ number.
 from __future__ import annotations
 
 import ctypes as C
-from typing import Dict, Mapping, Optional, Sequence, Tuple
+from typing import Mapping, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
 
 from . import _native
-from .forest import nodeposition
 from .storage import FieldSet
 
 MAX_TERMS = 20

@@ -8,8 +8,6 @@ reference's tests build theirs (``refine!`` then ``balance!``,
 from __future__ import annotations
 
 import math
-from typing import Tuple
-
 import numpy as np
 
 from .forest import Forest

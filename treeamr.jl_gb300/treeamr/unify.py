@@ -21,8 +21,6 @@ from typing import List, Optional, Sequence, Union
 import numpy as np
 import torch
 
-from . import _native
-from .forest import Forest
 from .schedule import (GhostSchedule, GroupKey, NeighbourTable, SELFIMAGE_TAG, Stencil1D,
                        TransferGroup, UNIFY_TAG, selfimage_sources, unify_sources,
                        unify_stencil)

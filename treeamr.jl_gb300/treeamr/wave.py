@@ -17,7 +17,7 @@ of a ``ForestBatch`` at once:
 from __future__ import annotations
 
 import ctypes as C
-from typing import Callable, List, Optional, Tuple
+from typing import Callable, Optional
 
 import numpy as np
 import torch
