@@ -233,7 +233,7 @@ def bounded_point(U, x, h, cen, p, raw=False):
 def test_a_refined_point_is_the_bounded_interpolant(D, cen):
     """``test/bounded_tests.jl:341-372``: every new point of a brick refined
     everywhere at once is the clamped interpolant; random data clamp often."""
-    N = 8
+    N = 6 if D == 3 else 8
     f = Forest((2,) * D, N=N, periodic=(True,) * D, extents=((0.0, 2.0),) * D)
     n, h = 2 * N, 2 / (2 * N)
     U = np.random.default_rng(80 + D).uniform(size=(n,) * D)
@@ -284,8 +284,9 @@ def test_bounded_point_values_create_no_new_extrema(D, cen):
     surface data stay within their range; the unbounded control overshoots
     a step."""
     C = (cen,) * D
+    N = 6 if D == 3 else 8
     for data in ("random", "step", "surface"):
-        f = nested_forest(D, N=8, periodic=(True,) * D)
+        f = nested_forest(D, N=N, periodic=(True,) * D)
         fs = FieldSet(f, 1, G=2, centering=C)
         rng = np.random.default_rng(90 + D)
         fn = {"random": lambda x: rng.uniform(),
@@ -297,13 +298,13 @@ def test_bounded_point_values_create_no_new_extrema(D, cen):
         lower = 1.0e-13 if data == "surface" else 0.0
         assert lower <= out.min() and out.max() <= 1
     # the unbounded control, refined everywhere at once, overshoots
-    f = nested_forest(D, N=8, periodic=(True,) * D)
+    f = nested_forest(D, N=N, periodic=(True,) * D)
     fs = FieldSet(f, 1, G=2, centering=C)
     _fill_fn(fs, lambda x: 1.0 if x[0] < 1.3 else 1.0e-13)
     plain, _ = _regrid_all(fs, PLAIN_PV)
     own = (slice(None), slice(None)) + plain.interior()     # the regrid moves own points
     assert plain.work.numpy()[own].min() < 0
-    fs = FieldSet(nested_forest(D, N=8, periodic=(True,) * D), 1, G=2, centering=C)
+    fs = FieldSet(nested_forest(D, N=N, periodic=(True,) * D), 1, G=2, centering=C)
     _fill_fn(fs, lambda x: 1.0 if x[0] < 1.3 else 1.0e-13)
     bounded, _ = _regrid_all(fs, BOUNDED_PV)
     assert bounded.work.numpy()[own].min() >= 1.0e-13
