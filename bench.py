@@ -419,6 +419,27 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def footprint_points(sched):
+    """Per variable, the points a fill writes (every target, once) and the
+    distinct points it reads (the union of every transfer's source windows,
+    per source block)."""
+    S = sched.stored
+    nb = sched.forest.nleaves()
+    wr = np.zeros((nb,) + tuple(reversed(S)), bool)
+    rd = np.zeros_like(wr)
+    for g in sched.groups:
+        tbox, sbox = [], []
+        for st in g.stencils:
+            win = st.order // 2 if getattr(g, "bounded", 0) == 2 else st.order
+            tbox.append(slice(st.targetfirst - 1, st.targetfirst - 1 + st.ntarget))
+            sbox.append(slice(int(st.srcstart.min()) - 1, int(st.srcstart.max()) - 1 + win))
+        tbox, sbox = tuple(reversed(tbox)), tuple(reversed(sbox))
+        for t, src in zip(g.targetblocks, g.sourceblocks):
+            wr[(int(t) - 1,) + tbox] = True
+            rd[(int(src) - 1,) + sbox] = True
+    return int(wr.sum()), int(rd.sum())
+
+
 def cpu_fill_rate(sched, fs_host_work, nvars, factors, bytes_per_fill, budget_s=15.0,
                   max_runs=5):
     """The oracle's threaded fill on every host core: (GB/s, seconds per
@@ -711,6 +732,17 @@ def main():
                          f"{threads} OpenMP threads"}
 
     if rank == 0:
+        # ghost points a second, and the unique footprint: every point written
+        # once and every distinct point read once (secondary to the
+        # algorithmic bytes, which count a read and a write per ghost)
+        wr, rd = footprint_points(sched)
+        fp_bytes = (wr + rd) * nvars * 8
+        throughput = {
+            "ghost_points_per_s": world * sched.ghost_items(1) / (ms * 1e-3),
+            "ghost_point_variables_per_s": world * points / (ms * 1e-3),
+            "footprint": {"written_points": wr, "read_points": rd, "bytes": fp_bytes,
+                          "gbs": world * fp_bytes / (ms * 1e-3) / 1e9,
+                          "frac": fp_bytes / (ms * 1e-3) / 1e9 / peak}}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -720,6 +752,7 @@ def main():
             "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
                       "speedup_fused_vs_plain": ms_plain / ms},
             "adjoint": adjoint,
+            "throughput": throughput,
             "state": state,
             "workloads": walls,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
