@@ -20,6 +20,7 @@ torchrun runs N independent replicas (the path does not shard on one GPU machine).
 from __future__ import annotations
 
 import argparse
+import itertools
 import json
 import os
 import statistics
@@ -231,6 +232,12 @@ def measure_walls(T, dev, timed, args, peak):
         fill_ghosts(fs, sched)
     steps = max(3, args.steps // 2)
     ms = timed(lambda: fill_ghosts(fs, sched), steps)
+    # the fill's deviation from a float64 evaluation of the same stencils
+    err = None
+    if T == np.float32:
+        filled = fs.work.cpu().numpy()
+        err = fill_error(sched, filled, filled, fs.nvars, fs.factors_host)
+        del filled
     fill_ghosts(fs, sched, method="plain")
     ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(2, steps // 2))
     # unify! of the set (stages P and 0 alone: every secondary copy of a
@@ -272,6 +279,7 @@ def measure_walls(T, dev, timed, args, peak):
                      "frac": achieved / peak,
                      "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()}},
         "fp64": fp,
+        "error": err,
         "unify": {"ms": ms_unify, "bytes": unify_bytes,
                   "gbs": unify_bytes / (ms_unify * 1e-3) / 1e9},
         "tuned": tuned,
@@ -419,6 +427,103 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def _split(a):
+    """Veltkamp's split of float64 ``a`` into two halves of 26 bits."""
+    c = 134217729.0 * a
+    hi = c - (c - a)
+    return hi, a - hi
+
+
+def _two_prod(a, b):
+    """``a * b`` as an unevaluated float64 sum, exactly (Dekker)."""
+    p = a * b
+    ah, al = _split(a)
+    bh, bl = _split(b)
+    return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
+
+
+def _two_sum(a, b):
+    """``a + b`` as an unevaluated float64 sum, exactly (Knuth)."""
+    s_ = a + b
+    bb = s_ - a
+    return s_, (a - (s_ - bb)) + (b - bb)
+
+
+def fill_error(sched, inp, out, nvars, factors, per_group=2, seed=0):
+    """The fill's deviation from a wider evaluation of the same stencils on
+    the same data: a sample of up to ``per_group`` transfers of every group,
+    all their points and variables, with the stored weights and the factor
+    column.  Float32 results are checked against float64 sums (its products
+    of Float32 values are exact); Float64 ones against double-double sums
+    (products and sums by error-free transformations, about 106 bits).
+    ``inp`` is the data the fill read (a filled array: every source a fill
+    reads is a fixed point of it), ``out`` the result.  Returns the largest
+    absolute deviation, and the largest in units of the last place, in the
+    result's type, of the sum of the terms' magnitudes (a sum's rounding
+    lives on that scale; a result near zero by cancellation has no last
+    place of its own to measure against)."""
+    dd = out.dtype == np.float64
+    rng = np.random.default_rng(seed)
+    D = sched.forest.D
+    worst_abs, worst_ulp, n = 0.0, 0.0, 0
+    for g in sched.groups:
+        if getattr(g, "bounded", 0) or getattr(g, "orientation", 0) or g.stage < 1:
+            continue
+        nt = g.ntransfers()
+        pick = rng.choice(nt, size=min(per_group, nt), replace=False)
+        st = g.stencils
+        tsl = tuple(slice(s_.targetfirst - 1, s_.targetfirst - 1 + s_.ntarget)
+                    for s_ in reversed(st))
+        fcol = (factors[:, g.factorcol - 1].astype(np.float64).reshape((nvars,) + (1,) * D)
+                if g.factorcol else None)
+        shape_t = (nvars,) + tuple(s_.ntarget for s_ in reversed(st))
+        for t in pick:
+            tb, sb = int(g.targetblocks[t]) - 1, int(g.sourceblocks[t]) - 1
+            src = inp[sb].astype(np.float64)              # every variable at once
+            hi = np.zeros(shape_t)
+            lo = np.zeros(shape_t)
+            mag = np.zeros(shape_t)
+            # the tensor-product sum over each dimension's taps
+            for taps in itertools.product(*[range(s_.order) for s_ in st]):
+                wh = np.ones(shape_t[1:])
+                wl = np.zeros(shape_t[1:])
+                idx = []
+                for d, s_ in enumerate(st):
+                    shape = [1] * D
+                    shape[D - 1 - d] = s_.ntarget
+                    wd = s_.weights[taps[d], :].astype(np.float64).reshape(shape)
+                    if dd:
+                        ph, pl = _two_prod(wh, wd)
+                        wh, wl = ph, pl + wl * wd
+                    else:
+                        wh = wh * wd
+                    idx.append((s_.srcstart - 1 + taps[d]).astype(np.int64))
+                u = src[(slice(None),) + np.ix_(*reversed(idx))]
+                if dd:
+                    th, tl = _two_prod(wh, u)
+                    tl = tl + wl * u
+                    s1, e1 = _two_sum(hi, th)
+                    e1 = e1 + lo + tl
+                    hi, lo = _two_sum(s1, e1)
+                    mag = mag + np.abs(th)
+                else:
+                    term = wh * u
+                    hi = hi + term
+                    mag = mag + np.abs(term)
+            if fcol is not None:
+                hi, lo = hi * fcol, lo * fcol
+            got = out[(tb, slice(None)) + tsl].astype(np.float64)
+            dev = np.abs((got - hi) - lo)
+            ulp = dev / np.spacing(mag.astype(out.dtype)).astype(np.float64)
+            worst_abs = max(worst_abs, float(dev.max()))
+            worst_ulp = max(worst_ulp, float(ulp.max()))
+            n += hi.size
+    return {"max_abs": worst_abs, "max_ulp_of_terms": worst_ulp, "points": n,
+            "against": "double-double" if dd else "float64",
+            "sample": f"up to {per_group} transfers of every copy, restriction and "
+                      "prolongation group, every point and variable"}
+
+
 def footprint_points(sched):
     """Per variable, the points a fill writes (every target, once) and the
     distinct points it reads (the union of every transfer's source windows,
@@ -552,6 +657,11 @@ def main():
         ms = timed(lambda: fill_ghosts(fs, sched, method=method), args.steps)
     clocks = clk.summary()
     value = world * bytes_per_fill / (ms * 1e-3) / 1e9
+    # the fill's deviation from a double-double evaluation of the same
+    # stencils on the same data (a sample of every group's transfers)
+    filled = fs.work.cpu().numpy() if rank == 0 else None
+    error = fill_error(sched, filled, filled, nvars, fs.factors_host) if rank == 0 else None
+    del filled
 
     # the plain one-launch-per-group fill on the same data
     for _ in range(max(1, args.warmup // 2)):
@@ -753,6 +863,7 @@ def main():
                       "speedup_fused_vs_plain": ms_plain / ms},
             "adjoint": adjoint,
             "throughput": throughput,
+            "error": error,
             "state": state,
             "workloads": walls,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
