@@ -6,6 +6,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 import torch
 import torch.distributed as dist
@@ -69,3 +70,36 @@ def test_reference_arm_prints_on_rank_zero_only(rank):
         line = json.loads(lines[-1])
         assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
         assert line["cpu_baseline"]["kind"] == "port"
+
+
+def test_fill_error_states_the_sum_rounding():
+    """The error the bench states for a fill: the oracle's sums against a
+    double-double (Float64) or float64 (Float32) evaluation of the same
+    stencils, a few units in the last place of the terms' magnitude (a
+    sequential sum of n terms is within n of them); an error planted in
+    one filled ghost shows."""
+    import bench
+    from _helpers import nested_forest
+    from treeamr import FieldSet, GhostSchedule, Operators
+    import oracle
+    f = nested_forest(3, N=8, periodic=(True,) * 3)
+    for T in (np.float64, np.float32):
+        fs = FieldSet(f, 2, G=2, T=T)
+        s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+        host = np.random.default_rng(1).uniform(-1, 1, size=tuple(fs.work.shape)).astype(T)
+        out = oracle.fill(s, host, 2, fs.factors_host)
+        e = bench.fill_error(s, out, out, 2, fs.factors_host)
+        assert e["points"] > 0
+        assert 0 < e["max_ulp_of_terms"] <= 64
+        assert e["max_abs"] < (1e-14 if T == np.float64 else 1e-5)
+        # a planted error in one filled ghost shows
+        g = next(g for g in s.groups if g.kind == "prolong" and g.stage >= 2)
+        st = g.stencils
+        at = (int(g.targetblocks[0]) - 1, 0) + tuple(s_.targetfirst - 1 for s_ in reversed(st))
+        bad = out.copy()
+        bad[at] += T(1e-3)
+
+        class One:                                  # that group alone, every transfer
+            forest, groups = s.forest, [g]
+        e2 = bench.fill_error(One, out, bad, 2, fs.factors_host, per_group=10 ** 6)
+        assert e2["max_abs"] > 5e-4
