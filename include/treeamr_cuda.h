@@ -280,14 +280,34 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
                      tam_batch **out);
 void tam_batch_free(tam_batch *b);
 /* Every stage tag in [first_stage, last_stage] of every member; the arena
- * holds arena_elems elements (checked against every member's extent). */
+ * holds arena_elems elements (checked against every member's extent), the
+ * factor arena each member's nvars * nfactorcols table.  Members may turn
+ * transfers across a seam (a member's odd turns read its own array, so a
+ * RotationPair member, whose layout is not symmetric in the seam's plane, is
+ * refused by tam_batch_create) or bound them; their solo groups run after
+ * each stage's fused launches, one launch for all members. */
 int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
                    const void *factor_arena, int64_t factor_elems, int32_t first_stage,
                    int32_t last_stage, void *stream);
-/* The adjoint of tam_batch_fill, member by member (tam_fill_adjoint). */
+/* tam_batch_fill with the variable table of turned transfers (tam_fill_ex's
+ * `rotvars`, nvars x 4, shared by every turned member); required when a
+ * member turns transfers, may be NULL otherwise. */
+int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                      const void *factor_arena, int64_t factor_elems, const int32_t *rotvars,
+                      int32_t first_stage, int32_t last_stage, void *stream);
+/* The adjoint of tam_batch_fill, member by member (tam_fill_adjoint); a batch
+ * with a bounded member has none (TAM_EUNSUPPORTED). */
 int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
                            const void *factor_arena, int64_t factor_elems,
                            int32_t first_stage, int32_t last_stage, void *stream);
+/* The adjoint of tam_batch_fill_ex. */
+int tam_batch_fill_adjoint_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                              const void *factor_arena, int64_t factor_elems,
+                              const int32_t *rotvars, int32_t first_stage, int32_t last_stage,
+                              void *stream);
+/* tam_device_status for a batch: its solo launches' error word (a variable
+ * table naming no variable), read on `stream` and cleared. */
+int tam_batch_device_status(tam_batch *b, void *stream, int32_t *code);
 /* tam_schedule_set_option for a batch. */
 int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value);
 

@@ -250,3 +250,35 @@ def axis_project(schedule, host: np.ndarray, nvars: int, factors: np.ndarray,
         for v in range(nvars):
             host[(b, v) + at] = vals[v]
     return host
+
+
+def axis_project_adjoint(schedule, host: np.ndarray, nvars: int, factors: np.ndarray,
+                         rotvars: np.ndarray) -> np.ndarray:
+    """The transpose of ``axis_project``, in place, in scatter form: the
+    projection's mean for variable ``v`` read ``factors[v, 3^D r] *
+    u[rotvars[v, r] - 1]`` over the orbit, so ``y[v] / M`` times that factor
+    is added back onto variable ``rotvars[v, r] - 1`` (``v`` itself for
+    ``r = 0``), summed in float64.  The reference has no adjoint; this is the
+    transpose of ``axis_project!`` (src/ghosts.jl:599-660)."""
+    pts, orbit = schedule.axis, schedule.axis_orbit
+    if not pts:
+        return host
+    D = schedule.forest.D
+    ncol = 3 ** D
+    M = len(orbit)
+    outs = []
+    for b, idx in pts:
+        at = tuple(i - 1 for i in reversed(idx))
+        yv = [float(host[(b, v) + at]) for v in range(nvars)]
+        out = [0.0] * nvars
+        for v in range(nvars):
+            for r in orbit:
+                sv = v if r == 0 else int(rotvars[v, r]) - 1
+                f = 1.0 if r == 0 else float(factors[v, ncol * r])
+                out[sv] += f * yv[v] / M
+        outs.append(out)
+    for (b, idx), out in zip(pts, outs):
+        at = tuple(i - 1 for i in reversed(idx))
+        for v in range(nvars):
+            host[(b, v) + at] = out[v]
+    return host

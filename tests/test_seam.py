@@ -957,3 +957,172 @@ def test_gpu_vertex_like_fill_across_the_seam_bit_exact(cuda_lib, case, T):
         fill_ghosts(fs, s, method=method)
         torch.cuda.synchronize()
         assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), method
+
+
+# --- the adjoint across a vertex seam: the axis projection's transpose --------------------
+
+def oracle_vertex_adjoint(s, fs, y):
+    """``A^T y`` of ``seam_fill`` without the hook (the oracle's transposes
+    of stages 0 and on, of the axis projection, then of stage P)."""
+    from treeamr.ghosts import turns_variables
+    rv = fs.rotvars_host
+    oracle.fill_adjoint(s, y, fs.nvars, fs.factors_host, first=0, rotvars=rv)
+    if s.axis and turns_variables(fs):
+        oracle.axis_project_adjoint(s, y, fs.nvars, fs.factors_host, rv)
+    return oracle.fill_adjoint(s, y, fs.nvars, fs.factors_host, last=-1, rotvars=rv)
+
+
+@pytest.mark.parametrize("case", VERTEX_CASES)
+def test_oracle_adjoint_dot_product_across_a_vertex_seam(case):
+    """``<A x, y> = <x, A^T y>`` to 1e-13 where the fill holds the axis
+    projection between stage P and stage 0, and the projection of the
+    product's transposed tables is the oracle's scatter-form transpose."""
+    from treeamr.ghosts import axis_transposed_tables, turns_variables
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h",
+                                    C=_centering(D, plane, "vertex"))
+    assert s.axis and turns_variables(fs)
+    rng = np.random.default_rng(29)
+    x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    ax = seam_fill(s, fs, x.copy(), hook_zero=False)
+    aty = oracle_vertex_adjoint(s, fs, y.copy())
+    lhs, rhs = _dot(ax, y), _dot(x, aty)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+    # without the projection's transpose the test fails: the axis matters here
+    wrong = oracle.fill_adjoint(s, y.copy(), fs.nvars, fs.factors_host, rotvars=fs.rotvars_host)
+    assert abs(lhs - _dot(x, wrong)) > 1e-10 * max(abs(lhs), 1.0)
+    # the product's transposed tables, run through the projection's own form
+    ft, rt = axis_transposed_tables(fs)
+    got = oracle.axis_project(s, y.copy(), fs.nvars, ft, rt)
+    want = oracle.axis_project_adjoint(s, y.copy(), fs.nvars, fs.factors_host, fs.rotvars_host)
+    assert np.max(np.abs(got - want)) < 1e-15
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", VERTEX_CASES)
+def test_gpu_adjoint_across_a_vertex_seam(cuda_lib, case):
+    """The device adjoint over a vertex seam: the dot-product test against
+    the device forward fill to 1e-13, and the oracle's transpose to the
+    sums' rounding."""
+    from treeamr import fill_ghosts
+    from treeamr.adjoint import fill_ghosts_adjoint
+    kind, D, plane, other = case
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h",
+                                    C=_centering(D, plane, "vertex"))
+    rng = np.random.default_rng(31)
+    x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    fs.factors, fs.rotvars = fs.factors.cuda(), fs.rotvars.cuda()
+    fs.work = torch.from_numpy(x.copy()).cuda()
+    fill_ghosts(fs, s)
+    ax = fs.work.cpu().numpy()
+    yd = torch.from_numpy(y.copy()).cuda()
+    fill_ghosts_adjoint(fs, s, yd)
+    torch.cuda.synchronize()
+    aty = yd.cpu().numpy()
+    lhs, rhs = _dot(ax, y), _dot(x, aty)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+    want = oracle_vertex_adjoint(s, fs, y.copy())
+    assert np.max(np.abs(aty - want)) < 1e-13
+
+
+# --- turned and bounded members in a batch of forests -------------------------------------
+
+def _batch_members(bounded=True):
+    """Field sets of 3 Float64 variables over 2-D forests: a turned
+    cell-centred quadrant, a vertex-like quadrant (its axis projected), a
+    plain nested forest and, with ``bounded``, a bounded one; each with its
+    schedule and random own points."""
+    from _helpers import nested_forest
+    from treeamr import FieldSet, GhostSchedule, Operators
+    from treeamr.operators import Conservative
+    out = []
+    for C in (None, _centering(2, (1, 2), "vertex")):
+        _, fs, s, *_ = quadrant_case(2, (1, 2), "none", C=C)
+        out.append((fs, s))
+    kinds = [OPS4] + ([Operators(prolongation=3, restriction=2, family=Conservative,
+                                 bounded=True)] if bounded else [])
+    for k, ops in enumerate(kinds):
+        fs = FieldSet(nested_forest(2, N=8, periodic=(True, True)), 3, G=1 + (k == 0))
+        fs.work = torch.from_numpy(
+            np.random.default_rng(40 + k).uniform(-1, 1, size=tuple(fs.work.shape)))
+        out.append((fs, GhostSchedule(fs, ops)))
+    return out
+
+
+@pytest.mark.gpu
+def test_gpu_batch_of_turned_and_bounded_members(cuda_lib):
+    """A batch holding turned quadrants (one cell-centred, one vertex-like
+    whose axis is projected between stage P and stage 0), a plain set and a
+    bounded one fills every member as its own fill does, bit for bit."""
+    from treeamr import fill_ghosts
+    from treeamr.batch import ForestBatch
+    members = _batch_members()
+    fss, scheds = [m[0] for m in members], [m[1] for m in members]
+    assert any(g.bounded for g in scheds[3].groups) and scheds[1].axis
+    batch = ForestBatch(fss, scheds)
+    start = batch.arena.clone()
+    batch.fill()
+    alone = start.clone()
+    for m, (fs, s) in enumerate(members):
+        fs.work = batch.member_view(alone, m)
+        fill_ghosts(fs, s)
+    torch.cuda.synchronize()
+    assert batch.device_status() == 0
+    assert np.array_equal(nanbits(batch.arena.cpu().numpy()), nanbits(alone.cpu().numpy()))
+    # and each turned member is the oracle's fill
+    for m in (0, 1):
+        fs, s = members[m]
+        want = seam_fill(s, fs, batch.member_view(start, m).cpu().numpy().copy(),
+                         hook_zero=False)
+        got = batch.member_view(batch.arena, m).cpu().numpy()
+        assert np.array_equal(nanbits(got), nanbits(want)), m
+
+
+@pytest.mark.gpu
+def test_gpu_batch_adjoint_of_turned_members(cuda_lib):
+    """The batch's adjoint over turned members (the axis projection's
+    transpose between stage 0's and stage P's) is each member's own adjoint
+    bit for bit; a batch with a bounded member has none."""
+    from treeamr.adjoint import fill_ghosts_adjoint
+    from treeamr.batch import ForestBatch
+    members = _batch_members(bounded=False)
+    fss, scheds = [m[0] for m in members], [m[1] for m in members]
+    batch = ForestBatch(fss, scheds)
+    y = torch.rand(batch.arena.shape, dtype=batch.arena.dtype, device="cuda",
+                   generator=torch.Generator(device="cuda").manual_seed(8))
+    got = y.clone()
+    batch.fill_adjoint(got)
+    alone = y.clone()
+    for m, (fs, s) in enumerate(members):
+        fill_ghosts_adjoint(fs, s, batch.member_view(alone, m))
+    torch.cuda.synchronize()
+    assert torch.equal(got.view(torch.int64), alone.view(torch.int64))
+    with_bounded = _batch_members()
+    b2 = ForestBatch([m[0] for m in with_bounded], [m[1] for m in with_bounded])
+    with pytest.raises(Exception, match="not linear"):
+        b2.fill_adjoint(b2.arena.clone())
+
+
+@pytest.mark.gpu
+def test_gpu_batch_refuses_a_pair_member_and_flags_a_bad_table(cuda_lib):
+    """A RotationPair member reads its partner's array, which a batch does not
+    hold: the library refuses it.  A variable table naming no variable is
+    skipped by the solo launch and reported through the batch's error word."""
+    from treeamr import _native
+    from treeamr.batch import ForestBatch
+    from treeamr.ghosts import device_schedule
+    quad, pair, (sa, sb), ops = pair_case(2, (1, 2), "none")
+    lib, ctx = _native.lib(), _native.context(0)
+    h = device_schedule(sa, 0).handle
+    out = C.c_void_p()
+    rc = lib.tam_batch_create(ctx, (C.c_void_p * 1)(h.value), 1, (C.c_int64 * 1)(0),
+                              (C.c_int64 * 1)(0), C.byref(out))
+    assert rc != 0 and "RotationPair" in _native.last_error(ctx)
+    fs, s = _batch_members(bounded=False)[0]
+    batch = ForestBatch([fs], [s])
+    batch.rotvars.zero_()
+    batch.fill()
+    assert batch.device_status() == _native.TAM_EINVAL
+    assert batch.device_status() == 0   # read and cleared

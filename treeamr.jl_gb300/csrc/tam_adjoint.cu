@@ -82,6 +82,7 @@ struct AdjArgs {
   const int64_t *__restrict__ scr;
   const Member *__restrict__ members;  // a batch's, or null
   const int32_t *__restrict__ rotvars; // turned groups' variable table, or null
+  int32_t *err;                        // error word, or null
 };
 
 // Where a transfer's field data and factors are: the kernel's own layout for
@@ -238,6 +239,10 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
         T *dst;
         if (h.col) {  // a turned group: through the axis map and the variable table
           const int sv = __ldg(a.rotvars + v + (int64_t)nvars * h.col) - 1;
+          if (sv < 0 || sv >= nvars) {  // a table naming no variable: skip, and say so
+            if (a.err) atomicExch(a.err, (int32_t)TAM_EINVAL);
+            continue;
+          }
           dst = yb + sv * L.vs + h.tc0 + h.tvs[0] * (h.flo[0] + j1) +
                 h.tvs[1] * (h.flo[1] + j2) + h.tvs[2] * (h.flo[2] + j3);
         } else {
@@ -279,13 +284,22 @@ __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restric
 }
 
 // Zero the targets of a stage's turned groups (they have no forward tiles):
-// group turns[blockIdx.y], every transfer, point and variable.
+// group turns[blockIdx.y], every transfer, point and variable; in a batch of
+// forests at its member's place in the arena.
 template <typename T>
 __global__ void __launch_bounds__(256)
     adjoint_zero_solo_kernel(const SoloGroup *__restrict__ turns, const DevGroup *groups,
+                               const Member *__restrict__ members,
                                const int32_t *__restrict__ tb, T *y, int nvars, int S1, int S2,
                                int S3) {
   const DevGroup &g = groups[turns[blockIdx.y].group];
+  if (members) {
+    const Member &m = members[g.member];
+    y += m.work_off;
+    S1 = m.S[0];
+    S2 = m.S[1];
+    S3 = m.S[2];
+  }
   const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
   const int64_t items = box * nvars * g.ntransfers;
   const int64_t vol = (int64_t)S1 * S2 * S3;
@@ -309,8 +323,9 @@ __global__ void __launch_bounds__(256)
 template <typename T, int D, bool BATCH>
 cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const T *factors,
                       int32_t first, int32_t last, T *scratch, cudaStream_t stream) {
-  const AdjArgs<T> a{r.groups, p.groups, r.tb, (const T *)r.weights,
-                     p.off,    (const int2 *)p.ent, p.scr, r.members, r.rotvars};
+  const AdjArgs<T> a{r.groups, p.groups,           r.tb,  (const T *)r.weights,
+                     p.off,    (const int2 *)p.ent, p.scr, r.members,
+                     r.rotvars, r.err};
   const int S1 = r.S[0], S2 = r.S[1], S3 = r.S[2];
   const int threads = 256, wpb = threads / 32;
   // stages in reverse order
@@ -349,7 +364,7 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
     }
     if (fw.nsolo > 0 && r.turns) {
       adjoint_zero_solo_kernel<T><<<dim3(64, (unsigned)fw.nsolo), threads, 0, stream>>>(
-          r.turns + fw.solo0, r.groups, r.tb, y, nvars, S1, S2, S3);
+          r.turns + fw.solo0, r.groups, r.members, r.tb, y, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -665,7 +680,7 @@ cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
                         const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
                         cudaStream_t stream) {
   AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
-           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars};
+           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars, s->d_err};
   return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
 }
 

@@ -7,7 +7,8 @@
 // lists into one schedule-shaped set of device arrays with every group
 // tagged with its member, and tiles each stage tag across all members, so
 // that a whole stage of every forest is one copy launch and one stencil
-// launch.
+// launch.  Members' solo groups (turned across a seam, or bounded) follow
+// each stage's fused launches as one solo launch for all members.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,6 +28,7 @@ struct tam_batch {
   std::vector<tam::Member> layout;     // per member
   std::vector<int64_t> member_points;  // nblocks * prod(S) per member (one variable)
   bool needs_factors = false;
+  bool needs_rotvars = false, has_bounded = false;
   std::vector<tam::DevGroup> groups;
   std::vector<int32_t> h_tb;
   std::vector<tam::Stage> stages;
@@ -38,6 +40,9 @@ struct tam_batch {
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
   tam::Member *d_members = nullptr;
+  std::vector<tam::SoloGroup> h_solos;  // by stage tag, members in order
+  tam::SoloGroup *d_solos = nullptr;
+  int32_t *d_err = nullptr;  // the solo launches' error word
   tam::SideStream side;
   // each member's first group, transfer and weight in the concatenated arrays
   std::vector<int64_t> group_base, transfer_base, weight_base;
@@ -89,6 +94,8 @@ void free_batch_device(tam_batch *b) {
   cudaFree(b->d_members);
   cudaFree(b->d_csingle);
   cudaFree(b->d_perm);
+  cudaFree(b->d_solos);
+  cudaFree(b->d_err);
   tam::adjoint_plan_free(b->adj);
   cudaFree(b->adj_scratch);
   b->adj_scratch = nullptr;
@@ -101,6 +108,8 @@ void free_batch_device(tam_batch *b) {
   b->d_tiles = nullptr;
   b->d_members = nullptr;
   b->d_csingle = b->d_perm = nullptr;
+  b->d_solos = nullptr;
+  b->d_err = nullptr;
 }
 
 // Every stage tag's tiles across all members: per member the transfers by
@@ -116,6 +125,7 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b) {
     std::vector<Entry> entries;
     for (int32_t gi : st.groups) {
       const tam::DevGroup &g = b->groups[gi];
+      if (g.turned) continue;  // a solo group: its own launch
       for (int64_t t = 0; t < g.ntransfers; ++t)
         entries.push_back({g.member, b->h_tb[g.first + t], gi, (int32_t)(g.first + t)});
     }
@@ -142,10 +152,9 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b) {
 int check_arena(tam_batch *b, int64_t arena_elems, int32_t nvars, const void *factor_arena,
                 int64_t factor_elems) {
   if (nvars < 1) return bfail(b->ctx, TAM_EINVAL, "batch fill: nvars must be positive");
-  int64_t cols = 1;
-  for (int k = 0; k < b->D; ++k) cols *= 3;
   for (size_t m = 0; m < b->members.size(); ++m) {
     const tam::Member &L = b->layout[m];
+    const int64_t cols = b->members[m]->nfactorcols;  // 3^D, or 4 * 3^D over a seam
     if (L.work_off < 0 || L.work_off + b->member_points[m] * nvars > arena_elems)
       return bfail(b->ctx, TAM_EINVAL,
                    "batch fill: member " + std::to_string(m) + " lies outside the arena");
@@ -177,10 +186,18 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     if (members[m]->D != first->D || members[m]->dtype != first->dtype)
       return bfail(ctx, TAM_EINVAL,
                    "tam_batch_create: members differ in dimension or element type");
-    if (members[m]->needs_rotvars || members[m]->has_bounded)
-      return bfail(ctx, TAM_EUNSUPPORTED,
-                   "tam_batch_create: a member turns transfers across a seam or bounds them, "
-                   "which a batch does not take; fill it alone");
+    // a member's odd turns read its own array: a RotationPair member, whose
+    // layout is not symmetric in the seam's plane, reads its partner's
+    for (const tam_group &h : members[m]->host_groups) {
+      if (!(h.orientation & 1)) continue;
+      for (int e = 0; e < members[m]->D; ++e)
+        if (members[m]->S[(h.axes >> (2 * e)) & 3] != members[m]->S[e])
+          return bfail(ctx, TAM_EUNSUPPORTED,
+                       "tam_batch_create: member " + std::to_string(m) +
+                           " is a RotationPair member (its layout is not symmetric in the "
+                           "seam's plane) and reads its partner's array; fill the pair with "
+                           "tam_fill_ex");
+    }
   }
   Guard guard(ctx->device);
   if (!guard.ok) return bfail(ctx, TAM_ECUDA, "cannot make the context's device current");
@@ -204,6 +221,8 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     b->layout.push_back(L);
     b->member_points.push_back(s->nblocks * (int64_t)s->S[0] * s->S[1] * s->S[2]);
     b->needs_factors = b->needs_factors || s->needs_factors;
+    b->needs_rotvars = b->needs_rotvars || s->needs_rotvars;
+    b->has_bounded = b->has_bounded || s->has_bounded;
     const int64_t g0 = (int64_t)b->groups.size(), t0 = (int64_t)tb.size();
     const int64_t ss0 = (int64_t)srcstart.size(), c0 = (int64_t)cls.size();
     const int64_t cs0 = (int64_t)csingle.size(), p0 = (int64_t)perm.size();
@@ -251,6 +270,20 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     tam::Stage st;
     st.tag = kv.first;
     st.groups = kv.second;
+    // the members' solo groups of this tag, their group indices moved to the batch's
+    st.solo0 = (int64_t)b->h_solos.size();
+    for (int32_t m = 0; m < n; ++m) {
+      const tam_sched *s = members[m];
+      for (const tam::Stage &ms : s->stages) {
+        if (ms.tag != st.tag) continue;
+        for (int64_t i = ms.solo0; i < ms.solo0 + ms.nsolo; ++i) {
+          tam::SoloGroup t = s->h_solos[i];
+          t.group += (int32_t)b->group_base[m];
+          b->h_solos.push_back(t);
+        }
+      }
+    }
+    st.nsolo = (int64_t)b->h_solos.size() - st.solo0;
     b->stages.push_back(st);
   }
   b->h_tb = tb;
@@ -269,7 +302,10 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
       (e = up((unsigned char **)&b->d_weights, weights.data(), weights.size())) != cudaSuccess ||
       (e = up((unsigned char **)&b->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
       (e = up(&b->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
-      (e = up(&b->d_members, b->layout.data(), b->layout.size())) != cudaSuccess) {
+      (e = up(&b->d_members, b->layout.data(), b->layout.size())) != cudaSuccess ||
+      (e = up(&b->d_solos, b->h_solos.data(), b->h_solos.size())) != cudaSuccess ||
+      (e = cudaMalloc((void **)&b->d_err, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMemset(b->d_err, 0, sizeof(int32_t))) != cudaSuccess) {
     free_batch_device(b);
     delete b;
     return bfail(ctx, e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA,
@@ -289,9 +325,20 @@ void tam_batch_free(tam_batch *b) {
 int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
                    const void *factor_arena, int64_t factor_elems, int32_t first_stage,
                    int32_t last_stage, void *stream) {
+  return tam_batch_fill_ex(b, arena, arena_elems, nvars, factor_arena, factor_elems, nullptr,
+                           first_stage, last_stage, stream);
+}
+
+int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                      const void *factor_arena, int64_t factor_elems, const int32_t *rotvars,
+                      int32_t first_stage, int32_t last_stage, void *stream) {
   if (!b || !arena) return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_fill: NULL argument");
   int rc = check_arena(b, arena_elems, nvars, factor_arena, factor_elems);
   if (rc != TAM_OK) return rc;
+  if (b->needs_rotvars && !rotvars)
+    return bfail(b->ctx, TAM_EINVAL,
+                 "a member of this batch turns ghosts across a rotating seam, but no variable "
+                 "table was given to turn them with: use tam_batch_fill_ex");
   Guard guard(b->ctx->device);
   if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
   const tam::SchedArgs args{b->d_groups,  b->d_tb,      b->d_sb,          b->d_srcstart,
@@ -304,6 +351,10 @@ int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars
                                             st.npcopy0, st.npcopy, st.nptiles, args, arena, factor_arena,
                                             nvars, S, b->shape.threads, (cudaStream_t)stream,
                                             &b->side, nullptr);
+    if (e == cudaSuccess && st.nsolo > 0)
+      e = tam::launch_solo(b->dtype, b->D, b->d_solos + st.solo0, st.nsolo, args, arena, arena,
+                           arena, factor_arena, rotvars, nvars, S, b->d_err,
+                           (cudaStream_t)stream);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return bfail(b->ctx, TAM_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));
@@ -315,10 +366,26 @@ int tam_batch_fill(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars
 int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
                            const void *factor_arena, int64_t factor_elems, int32_t first_stage,
                            int32_t last_stage, void *stream) {
+  return tam_batch_fill_adjoint_ex(b, arena, arena_elems, nvars, factor_arena, factor_elems,
+                                   nullptr, first_stage, last_stage, stream);
+}
+
+int tam_batch_fill_adjoint_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nvars,
+                              const void *factor_arena, int64_t factor_elems,
+                              const int32_t *rotvars, int32_t first_stage, int32_t last_stage,
+                              void *stream) {
   if (!b || !arena)
     return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_fill_adjoint: NULL argument");
   int rc = check_arena(b, arena_elems, nvars, factor_arena, factor_elems);
   if (rc != TAM_OK) return rc;
+  if (b->has_bounded)
+    return bfail(b->ctx, TAM_EUNSUPPORTED,
+                 "a member of this batch has bounded operators, which are not linear, so the "
+                 "batch has no adjoint");
+  if (b->needs_rotvars && !rotvars)
+    return bfail(b->ctx, TAM_EINVAL,
+                 "a member of this batch turns ghosts across a rotating seam, but no variable "
+                 "table was given: use tam_batch_fill_adjoint_ex");
   Guard guard(b->ctx->device);
   if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
   if (!b->adj.ready) {
@@ -342,14 +409,30 @@ int tam_batch_fill_adjoint(tam_batch *b, void *arena, int64_t arena_elems, int32
     }
     b->adj_scratch_bytes = need;
   }
-  const tam::AdjRun r{b->dtype, b->D, b->d_groups, b->d_tb, b->d_weights, b->d_members,
-                      b->d_tiles, &b->stages, {1, 1, 1}, nullptr, nullptr};
+  const tam::AdjRun r{b->dtype,   b->D,      b->d_groups, b->d_tb,   b->d_weights,
+                      b->d_members, b->d_tiles, &b->stages, {1, 1, 1}, b->d_solos,
+                      rotvars,     b->d_err};
   cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena, first_stage,
                                         last_stage, b->adj_scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return bfail(b->ctx, TAM_ECUDA, std::string("batch adjoint launch: ") + cudaGetErrorString(e));
   }
+  return TAM_OK;
+}
+
+int tam_batch_device_status(tam_batch *b, void *stream, int32_t *code) {
+  if (!b || !code) return bfail(b ? b->ctx : nullptr, TAM_EINVAL, "tam_batch_device_status: NULL argument");
+  Guard guard(b->ctx->device);
+  if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, b->d_err, sizeof h, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess)
+    return bfail(b->ctx, TAM_ECUDA, std::string("tam_batch_device_status: ") + cudaGetErrorString(e));
+  *code = h;
   return TAM_OK;
 }
 

@@ -340,6 +340,7 @@ struct AdjRun {
   int S[3];                        // stored extents (a batch: each member's own)
   const SoloGroup *turns;          // the solo groups (their targets are zeroed too)
   const int32_t *rotvars;          // the variable table of turned groups, or null
+  int32_t *err;                    // error word: a variable table naming no variable
 };
 cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,
                              const void *factors, int32_t first, int32_t last, void *scratch,

@@ -870,7 +870,9 @@ __device__ __forceinline__ T mc_slope(T a, T b) {
 // column, the largest scaling phi in [0, 1] that keeps every child within the
 // extremes) or bracket_clamp_sum (the full order-p sum clamped into the
 // range of the points with a nonzero linear weight in every dimension),
-// each carrying 0 * (max - min) (src/ghosts.jl:291-361).
+// each carrying 0 * (max - min) (src/ghosts.jl:291-361).  In a batch of
+// forests the group's member gives the arrays' offsets in the arena and the
+// stored extents; its odd turns read its own array.
 template <typename T, int D>
 __global__ void __launch_bounds__(256)
     solo_group_kernel(const SoloGroup *__restrict__ turns, Args<T> a, const T *src,
@@ -880,6 +882,16 @@ __global__ void __launch_bounds__(256)
   using A = Arith<T>;
   const SoloGroup tg = turns[blockIdx.y];
   const DevGroup &g = a.groups[tg.group];
+  if (a.members) {
+    const Member &m = a.members[g.member];
+    src += m.work_off;
+    alt = src;
+    work += m.work_off;
+    if (factors) factors += m.fac_off;
+    S1 = m.S[0];
+    S2 = m.S[1];
+    S3 = m.S[2];
+  }
   const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
   const int64_t items = box * nvars * g.ntransfers;
   const int64_t vol = (int64_t)S1 * S2 * S3;

@@ -26,6 +26,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "libtreeamr_cuda.so")
 
 ABI_VERSION = 2
 TAM_F32, TAM_F64 = 1, 2
+TAM_OK, TAM_EINVAL, TAM_EUNSUPPORTED = 0, -1, -6
 TAM_STAGE_ALL_FIRST, TAM_STAGE_ALL_LAST = -1, 0x7FFFFFFF
 TAM_METHOD_FUSED, TAM_METHOD_PLAIN = 0, 1
 
@@ -286,6 +287,12 @@ def _declare(lib: C.CDLL):
         f = getattr(lib, name)
         f.argtypes = [vp, vp, i64, i32, vp, i64, i32, i32, vp]
         f.restype = C.c_int
+    for name in ("tam_batch_fill_ex", "tam_batch_fill_adjoint_ex"):
+        f = getattr(lib, name)
+        f.argtypes = [vp, vp, i64, i32, vp, i64, vp, i32, i32, vp]
+        f.restype = C.c_int
+    lib.tam_batch_device_status.argtypes = [vp, vp, C.POINTER(i32)]
+    lib.tam_batch_device_status.restype = C.c_int
     lib.tam_batch_set_option.argtypes = [vp, i32, i64]
     lib.tam_batch_set_option.restype = C.c_int
     lib.tam_schedule_set_option.argtypes = [vp, i32, i64]

@@ -15,8 +15,8 @@ from typing import Optional
 import torch
 
 from . import _native
-from .ghosts import check_fill, device_schedule
-from .schedule import GhostSchedule
+from .ghosts import check_fill, device_schedule, run_axis, turns_variables
+from .schedule import GhostSchedule, SELFIMAGE_TAG, UNIFY_TAG
 from .storage import FieldSet
 
 
@@ -25,7 +25,9 @@ def fill_ghosts_adjoint(fs: FieldSet, schedule: GhostSchedule, y: Optional[torch
                         stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
     """``y <- A^T y`` in place, ``y`` shaped like ``fs.work`` (default: ``fs.work``
     itself).  Stages run in reverse; every ghost's adjoint is pushed onto the
-    points its value was computed from, then zeroed."""
+    points its value was computed from, then zeroed.  Over a seam whose axis
+    projection turns variables, the projection's transpose runs between
+    stage 0's transpose and stage P's."""
     check_fill(fs, schedule)
     y = fs.work if y is None else y
     if y.shape != fs.work.shape or y.dtype != fs.work.dtype or y.device != fs.work.device:
@@ -33,9 +35,19 @@ def fill_ghosts_adjoint(fs: FieldSet, schedule: GhostSchedule, y: Optional[torch
     if not y.is_contiguous():
         raise ValueError("the adjoint vector must be contiguous")
     ds = device_schedule(schedule, y.device.index or 0)
+    rotvars = getattr(fs, "rotvars", None)
+    if schedule.axis and turns_variables(fs):
+        # the fill is (stages >= 0) P (stages <= P), P the axis projection
+        # between them; its transpose runs the three parts' transposes in
+        # reverse order
+        ds.run_adjoint(y, fs.nvars, fs.factors, UNIFY_TAG, _native.TAM_STAGE_ALL_LAST, stream,
+                       scratch, rotvars=rotvars)
+        run_axis(fs, schedule, stream, work=y, transpose=True)
+        ds.run_adjoint(y, fs.nvars, fs.factors, _native.TAM_STAGE_ALL_FIRST, SELFIMAGE_TAG,
+                       stream, scratch, rotvars=rotvars)
+        return y
     ds.run_adjoint(y, fs.nvars, fs.factors, _native.TAM_STAGE_ALL_FIRST,
-                   _native.TAM_STAGE_ALL_LAST, stream, scratch,
-                   rotvars=getattr(fs, "rotvars", None))
+                   _native.TAM_STAGE_ALL_LAST, stream, scratch, rotvars=rotvars)
     return y
 
 

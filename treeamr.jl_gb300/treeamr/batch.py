@@ -6,6 +6,12 @@ forests of any size and block extent, one element type and variable count --
 out in one arena, 256-byte aligned member by member, and fills all of them
 with one launch per stage (``tam_batch_fill``).  Each member's ``FieldSet``
 keeps working on its own: its ``work`` is a view into the arena.
+
+Members may turn ghosts across a seam (sets symmetric in the seam's plane:
+a RotationPair reads its partner's array and is filled as a pair) or bound
+their prolongations; their solo groups run after each stage's fused
+launches, one launch for all members.  Turned members share one variable
+table, and a seam's axis projection runs between stage P and stage 0.
 """
 from __future__ import annotations
 
@@ -15,8 +21,8 @@ from typing import Optional, Sequence
 import torch
 
 from . import _native
-from .ghosts import check_fill, device_schedule
-from .schedule import GhostSchedule
+from .ghosts import check_fill, device_schedule, run_axis, turns_variables
+from .schedule import GhostSchedule, SELFIMAGE_TAG, UNIFY_TAG
 from .storage import FieldSet, _TORCH
 
 ALIGN_BYTES = 256
@@ -42,9 +48,10 @@ class ForestBatch:
             offs.append(total)
             n = fs.work.numel()
             total += (n + align - 1) // align * align
-        ncols = 3 ** D
+        # each member's factor table: nvars x 3^D, or nvars x 4 * 3^D over a seam
+        fsizes = [fs.factors.numel() for fs in fieldsets]
         self.arena = torch.zeros(max(total, 1), dtype=_TORCH[T], device=self.device)
-        self.factor_arena = torch.zeros(len(fieldsets) * nvars * ncols, dtype=_TORCH[T],
+        self.factor_arena = torch.zeros(max(sum(fsizes), 1), dtype=_TORCH[T],
                                         device=self.device)
         foffs = []
         for m, fs in enumerate(fieldsets):
@@ -52,8 +59,8 @@ class ForestBatch:
             view = self.arena[offs[m]:offs[m] + fs.work.numel()].view(tuple(fs.work.shape))
             view.copy_(host)
             fs.work = view
-            fo = m * nvars * ncols
-            fview = self.factor_arena[fo:fo + nvars * ncols]
+            fo = sum(fsizes[:m])
+            fview = self.factor_arena[fo:fo + fsizes[m]]
             fview.copy_(fs.factors.detach().cpu())
             fs.factors = fview
             foffs.append(fo)
@@ -63,6 +70,25 @@ class ForestBatch:
         self.factor_offsets = foffs
         for fs, s in zip(fieldsets, schedules):
             check_fill(fs, s)
+        # the variable table of the turned members, which they share
+        self.rotvars = None
+        for fs, s in zip(fieldsets, schedules):
+            if not getattr(s, "turned", False):
+                continue
+            rv = fs.rotvars.detach().cpu()
+            if self.rotvars is None:
+                self.rotvars = rv
+            elif not torch.equal(self.rotvars, rv):
+                raise ValueError("the turned members of a batch share one variable table: "
+                                 "build their field sets with the same rotation")
+        if self.rotvars is not None:
+            self.rotvars = self.rotvars.to(torch.int32).to(self.device)
+        for fs in fieldsets:  # the axis projection reads each member's own table
+            if getattr(fs, "rotvars", None) is not None:
+                fs.rotvars = fs.rotvars.to(self.device)
+        # members whose seam axis is projected between stage P and stage 0
+        self.axis_members = [m for m, (fs, s) in enumerate(zip(fieldsets, schedules))
+                             if s.axis and turns_variables(fs)]
         dev = self.device.index or 0
         self.uploads = [device_schedule(s, dev) for s in schedules]
         self.lib = _native.lib()
@@ -90,27 +116,50 @@ class ForestBatch:
     def _stream(self, stream):
         return stream if stream is not None else torch.cuda.current_stream(self.device)
 
+    def _run(self, name: str, a: torch.Tensor, first: int, last: int, stream):
+        rv = self.rotvars
+        rc = getattr(self.lib, name)(
+            self.handle, C.c_void_p(a.data_ptr()), a.numel(), self.nvars,
+            C.c_void_p(self.factor_arena.data_ptr()), self.factor_arena.numel(),
+            C.c_void_p(rv.data_ptr() if rv is not None else 0), first, last,
+            C.c_void_p(self._stream(stream).cuda_stream))
+        _native.check(rc, self.ctx, name)
+
+    def _axis(self, a: torch.Tensor, stream, transpose: bool):
+        for m in self.axis_members:
+            run_axis(self.fieldsets[m], self.schedules[m], self._stream(stream),
+                     work=self.member_view(a, m), transpose=transpose)
+
     def fill(self, arena: Optional[torch.Tensor] = None, stream=None):
         """Fill every member's ghosts; ``arena`` (default: the batch's own) is
         any tensor laid out like the batch's arena."""
         a = self.arena if arena is None else arena
-        rc = self.lib.tam_batch_fill(self.handle, C.c_void_p(a.data_ptr()), a.numel(), self.nvars,
-                                     C.c_void_p(self.factor_arena.data_ptr()),
-                                     self.factor_arena.numel(), _native.TAM_STAGE_ALL_FIRST,
-                                     _native.TAM_STAGE_ALL_LAST,
-                                     C.c_void_p(self._stream(stream).cuda_stream))
-        _native.check(rc, self.ctx, "tam_batch_fill")
+        first, last = _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST
+        if self.axis_members:
+            self._run("tam_batch_fill_ex", a, first, SELFIMAGE_TAG, stream)
+            self._axis(a, stream, transpose=False)
+            first = UNIFY_TAG
+        self._run("tam_batch_fill_ex", a, first, last, stream)
         return a
 
     def fill_adjoint(self, y: torch.Tensor, stream=None):
         """``y <- A^T y`` for every member, ``y`` laid out like the arena."""
-        rc = self.lib.tam_batch_fill_adjoint(
-            self.handle, C.c_void_p(y.data_ptr()), y.numel(), self.nvars,
-            C.c_void_p(self.factor_arena.data_ptr()), self.factor_arena.numel(),
-            _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST,
-            C.c_void_p(self._stream(stream).cuda_stream))
-        _native.check(rc, self.ctx, "tam_batch_fill_adjoint")
+        first, last = _native.TAM_STAGE_ALL_FIRST, _native.TAM_STAGE_ALL_LAST
+        if self.axis_members:
+            self._run("tam_batch_fill_adjoint_ex", y, UNIFY_TAG, last, stream)
+            self._axis(y, stream, transpose=True)
+            last = SELFIMAGE_TAG
+        self._run("tam_batch_fill_adjoint_ex", y, first, last, stream)
         return y
+
+    def device_status(self, stream=None) -> int:
+        """The solo launches' error word (nonzero: a variable table named no
+        variable), read and cleared."""
+        code = C.c_int32()
+        _native.check(self.lib.tam_batch_device_status(
+            self.handle, C.c_void_p(self._stream(stream).cuda_stream), C.byref(code)),
+            self.ctx, "tam_batch_device_status")
+        return code.value
 
     def set_option(self, name: str, value: int):
         code = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4}[name]

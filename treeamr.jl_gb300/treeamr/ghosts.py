@@ -188,12 +188,39 @@ def turns_variables(fs: FieldSet) -> bool:
     return m is not None and list(m) != list(range(1, fs.nvars + 1))
 
 
-def run_axis(fs: FieldSet, schedule: GhostSchedule, stream=None):
+def axis_transposed_tables(fs: FieldSet):
+    """The tables of the axis projection's transpose.  The projection maps an
+    axis point's variables ``u`` to ``(1/M) sum_r f[v, r] u[sigma_r(v)]``
+    (``f[v, r]`` the factor at column ``3^D r``, ``sigma_r`` the variable
+    table's column ``r``), so its transpose maps ``y`` to ``(1/M) sum_r
+    f[sigma_r^-1(w), r] y[sigma_r^-1(w)]``: the same form, with column ``r``
+    of the variable table inverted and each factor moved with its variable."""
+    fac = np.asarray(fs.factors_host)
+    rv = np.asarray(fs.rotvars_host)
+    nvars, ncol = fs.nvars, 3 ** fs.D
+    ft = np.zeros_like(fac)
+    rt = np.empty_like(rv)
+    for r in range(rv.shape[1]):
+        sigma = rv[:, r].astype(np.int64) - 1
+        if sorted(sigma.tolist()) != list(range(nvars)):
+            raise ValueError(f"column {r} of the variable table is not a permutation, so the "
+                             "axis projection has no transpose of its own form")
+        for v in range(nvars):
+            rt[sigma[v], r] = v + 1
+            ft[sigma[v], ncol * r] = fac[v, ncol * r]
+    return ft, rt
+
+
+def run_axis(fs: FieldSet, schedule: GhostSchedule, stream=None, *,
+             work: Optional[torch.Tensor] = None, transpose: bool = False):
     """A seam's axis projection on the device (``tam_axis_project``), stage
-    P's axis part, between stage P and stage 0 (``src/ghosts.jl:1111-1116``)."""
+    P's axis part, between stage P and stage 0 (``src/ghosts.jl:1111-1116``),
+    on ``work`` (default: the set's own array); ``transpose``: the
+    projection's transpose, for the adjoint fill."""
     if not schedule.axis or not turns_variables(fs):
         return
-    dev = fs.work.device
+    work = fs.work if work is None else work
+    dev = work.device
     cache = schedule.__dict__.setdefault("_axis_device", {})
     key = (dev.index, fs.nvars, fs.T.name)
     if key not in cache:
@@ -206,15 +233,24 @@ def run_axis(fs: FieldSet, schedule: GhostSchedule, stream=None):
                 o = o * S[d] + (idx[d] - 1)
             offs.append(b * fs.nvars * vol + o)
         pts = torch.tensor(offs, dtype=torch.int64, device=dev)
-        buf = torch.empty(len(offs) * fs.nvars, dtype=fs.work.dtype, device=dev)
+        buf = torch.empty(len(offs) * fs.nvars, dtype=work.dtype, device=dev)
         cache[key] = (pts, buf, vol)
     pts, buf, vol = cache[key]
+    if transpose:
+        tcache = fs.__dict__.setdefault("_axis_transposed", {})
+        if dev.index not in tcache:
+            ft, rt = axis_transposed_tables(fs)
+            col = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).to(dev)
+            tcache[dev.index] = (col(ft), col(rt))
+        factors, rotvars = tcache[dev.index]
+    else:
+        factors, rotvars = fs.factors, fs.rotvars
     s = stream if stream is not None else torch.cuda.current_stream(dev)
     rc = _native.lib().tam_axis_project(
         _native.TAM_F64 if fs.T == np.float64 else _native.TAM_F32,
         C.c_void_p(pts.data_ptr()), pts.numel(), len(schedule.axis_orbit),
-        C.c_void_p(fs.work.data_ptr()), fs.nvars, vol, C.c_void_p(fs.factors.data_ptr()),
-        3 ** fs.D, C.c_void_p(fs.rotvars.data_ptr()), C.c_void_p(buf.data_ptr()),
+        C.c_void_p(work.data_ptr()), fs.nvars, vol, C.c_void_p(factors.data_ptr()),
+        3 ** fs.D, C.c_void_p(rotvars.data_ptr()), C.c_void_p(buf.data_ptr()),
         C.c_void_p(s.cuda_stream))
     if rc != 0:
         raise _native.TamError(f"tam_axis_project failed ({rc})")

@@ -160,6 +160,9 @@ class WaveSolver:
         (``tam_graph_capture_rk4``); ``launch()`` replays them."""
         ta, tb, acc = self.k[0], self.k[1], self.k[2]
         b = self.batch
+        if b.rotvars is not None or b.axis_members:
+            raise ValueError("the library's RK4 graph fills with tam_batch_fill, which turns no "
+                             "ghosts across a seam: capture() the batch's own fills instead")
         h = C.c_void_p()
         rc = self.lib.tam_graph_capture_rk4(
             b.handle, self.dtype_code, C.c_void_p(self.table.data_ptr()), self.nblocks,
