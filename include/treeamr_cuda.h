@@ -238,6 +238,17 @@ int tam_fill_adjoint_ex(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                         int32_t last_stage, void *scratch, size_t scratch_bytes,
                         void *stream);
 
+/* The adjoint of tam_fill_ex with `alt_work`: the transposes of odd turns add
+ * onto `alt_y` (the partner's cotangent, in the partner's layout), the rest
+ * onto `y`.  The adjoint of a RotationPair fill runs, stage tag by stage tag
+ * from the last, the second member's stage, then the first's, each with the
+ * other's cotangent as `alt_y` (the forward order reversed).  NULL `alt_y`:
+ * tam_fill_adjoint_ex. */
+int tam_fill_adjoint_alt(tam_sched *s, void *y, void *alt_y, int32_t nvars, int64_t nblocks,
+                         const void *factors, const int32_t *rotvars, int32_t first_stage,
+                         int32_t last_stage, void *scratch, size_t scratch_bytes,
+                         void *stream);
+
 /* tam_fill_adjoint with caller-owned device scratch of at least
  * tam_adjoint_scratch_bytes; allocates nothing per call. */
 int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,

@@ -68,6 +68,9 @@ def lib():
         l.oracle_fill_adjoint_turned.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                                  C.c_void_p, C.c_int32, C.c_int32]
         l.oracle_fill_adjoint_turned.restype = C.c_int
+        l.oracle_fill_adjoint_pair.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                               C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+        l.oracle_fill_adjoint_pair.restype = C.c_int
         _lib = l
     return _lib
 
@@ -116,15 +119,24 @@ def fill(schedule, work: np.ndarray, nvars: int, factors: np.ndarray, *, first=A
 
 
 def fill_adjoint(schedule, y: np.ndarray, nvars: int, factors: np.ndarray, *, first=ALL_FIRST,
-                 last=ALL_LAST, rotvars=None) -> np.ndarray:
+                 last=ALL_LAST, rotvars=None, alt: np.ndarray = None) -> np.ndarray:
+    """In place on ``y``: the scatter-form transpose of ``fill``; with ``alt``
+    (a RotationPair partner's cotangent, in the partner's layout) odd turns
+    scatter onto ``alt``."""
     assert y.flags.c_contiguous and y.dtype == np.dtype(schedule.T)
     d = _descriptor(schedule)
     f = np.ascontiguousarray(np.asfortranarray(factors).ravel(order="F"), dtype=y.dtype)
     rv = None if rotvars is None else \
         np.ascontiguousarray(np.asfortranarray(rotvars).ravel(order="F"), dtype=np.int32)
-    rc = lib().oracle_fill_adjoint_turned(C.addressof(d.desc), y.ctypes.data, nvars,
-                                          f.ctypes.data, None if rv is None else rv.ctypes.data,
-                                          first, last)
+    if alt is not None:
+        assert alt.flags.c_contiguous and alt.size == y.size and alt.dtype == y.dtype
+        rc = lib().oracle_fill_adjoint_pair(C.addressof(d.desc), y.ctypes.data, alt.ctypes.data,
+                                            nvars, f.ctypes.data,
+                                            None if rv is None else rv.ctypes.data, first, last)
+    else:
+        rc = lib().oracle_fill_adjoint_turned(C.addressof(d.desc), y.ctypes.data, nvars,
+                                              f.ctypes.data,
+                                              None if rv is None else rv.ctypes.data, first, last)
     if rc != 0:
         raise RuntimeError("oracle_fill_adjoint failed")
     return y

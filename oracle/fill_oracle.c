@@ -327,7 +327,7 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
  * Stages run in reverse tag order. */
 #define DEFINE_ADJOINT(T, SUFFIX)                                                               \
   static void adjoint_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *y,            \
-                                     int32_t nvars, const T *factors,                           \
+                                     T *yalt, int32_t nvars, const T *factors,                  \
                                      const int32_t *rotvars) {                                  \
     const int D = d->ndim;                                                                      \
     int64_t S[3] = {1, 1, 1};                                                                   \
@@ -344,15 +344,20 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
           o[k] = g->stencil[k].order;                                                           \
           tf[k] = g->stencil[k].targetfirst - 1;                                                \
         }                                                                                       \
-        /* a turned group scatters onto its real source (a set symmetric in   \
-           the seam's plane: the real array is y itself) */                   \
+        /* a turned group scatters onto its real source: for an odd turn the  \
+           array yalt (a RotationPair's partner, or y itself for a set        \
+           symmetric in the seam's plane), whose extent along e is           \
+           R_e = S[perm[e]] (the same block and variable strides) */          \
         int64_t vst[3] = {1, s2, s3}, c0 = 0;                                                   \
+        T *from = (g->orientation & 1) ? yalt : y;                                              \
         if (g->orientation) {                                                                   \
-          const int64_t rst[3] = {1, s2, s3};                                                   \
+          int64_t R[3] = {1, 1, 1};                                                             \
+          for (int e = 0; e < D; ++e) R[e] = S[(g->axes >> (2 * e)) & 3];                       \
+          const int64_t rst[3] = {1, R[0], R[0] * R[1]};                                        \
           for (int e = 0; e < D; ++e) {                                                         \
             const int p = (g->axes >> (2 * e)) & 3, f = (g->axes >> (8 + e)) & 1;              \
             vst[p] = f ? -rst[e] : rst[e];                                                      \
-            if (f) c0 += rst[e] * (S[e] - 1);                                                   \
+            if (f) c0 += rst[e] * (R[e] - 1);                                                   \
           }                                                                                     \
         }                                                                                       \
         for (int64_t t = 0; t < g->ntransfers; ++t) {                                           \
@@ -379,8 +384,8 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
                   }                                                                             \
                   const int sv =                                                                \
                       g->orientation ? rotvars[v + (int64_t)nvars * g->orientation] - 1 : v;    \
-                  T *ys = y + sb * bs + sv * vs + c0 + base[0] * vst[0] + base[1] * vst[1] +    \
-                          base[2] * vst[2];                                                     \
+                  T *ys = from + sb * bs + sv * vs + c0 + base[0] * vst[0] +                    \
+                          base[1] * vst[1] + base[2] * vst[2];                                  \
                   for (int m3 = 0; m3 < o[2]; ++m3)                                             \
                     for (int m2 = 0; m2 < o[1]; ++m2)                                           \
                       for (int m1 = 0; m1 < o[0]; ++m1) {                                       \
@@ -397,6 +402,30 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
 DEFINE_ADJOINT(double, f64)
 DEFINE_ADJOINT(float, f32)
 
+/* The transpose of oracle_fill_turned with `alt`: odd turns scatter onto
+ * yalt (a RotationPair's partner cotangent, in the partner's layout).  For
+ * the pair's whole fill a caller runs, tag by tag from the last, the second
+ * member's stage and then the first's, each with the other's cotangent. */
+int oracle_fill_adjoint_pair(const tam_schedule_desc *d, void *y, void *yalt, int32_t nvars,
+                             const void *factors, const int32_t *rotvars, int32_t first,
+                             int32_t last) {
+  if (!d || !y || !yalt || nvars < 1) return -1;
+  for (int32_t gi = 0; gi < d->ngroups; ++gi)
+    if (d->groups[gi].orientation && !rotvars) return -1;
+  int32_t tags[128];
+  int nt = collect_tags(d, tags, 128);
+  for (int i = nt - 1; i >= 0; --i) {
+    if (tags[i] < first || tags[i] > last) continue;
+    if (d->dtype == TAM_F64)
+      adjoint_stage_f64(d, tags[i], (double *)y, (double *)yalt, nvars, (const double *)factors,
+                        rotvars);
+    else
+      adjoint_stage_f32(d, tags[i], (float *)y, (float *)yalt, nvars, (const float *)factors,
+                        rotvars);
+  }
+  return 0;
+}
+
 /* rotvars: the variable table of turned groups (NULL without any); a turned
  * group must keep the stored extents (a set symmetric in the seam's plane) */
 int oracle_fill_adjoint_turned(const tam_schedule_desc *d, void *y, int32_t nvars,
@@ -410,16 +439,7 @@ int oracle_fill_adjoint_turned(const tam_schedule_desc *d, void *y, int32_t nvar
     for (int e = 0; e < d->ndim; ++e)
       if (d->stored[(g->axes >> (2 * e)) & 3] != d->stored[e]) return -1;
   }
-  int32_t tags[128];
-  int nt = collect_tags(d, tags, 128);
-  for (int i = nt - 1; i >= 0; --i) {
-    if (tags[i] < first || tags[i] > last) continue;
-    if (d->dtype == TAM_F64)
-      adjoint_stage_f64(d, tags[i], (double *)y, nvars, (const double *)factors, rotvars);
-    else
-      adjoint_stage_f32(d, tags[i], (float *)y, nvars, (const float *)factors, rotvars);
-  }
-  return 0;
+  return oracle_fill_adjoint_pair(d, y, y, nvars, factors, rotvars, first, last);
 }
 
 int oracle_fill_adjoint(const tam_schedule_desc *d, void *y, int32_t nvars, const void *factors,

@@ -878,6 +878,12 @@ def test_gpu_adjoint_of_a_pair_member_is_refused(cuda_lib):
     a.work, a.factors, a.rotvars = a.work.cuda(), a.factors.cuda(), a.rotvars.cuda()
     with pytest.raises(Exception, match="RotationPair"):
         fill_ghosts_adjoint(a, sa, torch.zeros_like(a.work))
+    # the library itself: without the partner's cotangent the member is refused
+    from treeamr.ghosts import device_schedule
+    ds = device_schedule(sa, 0)
+    with pytest.raises(Exception, match="tam_fill_adjoint_alt"):
+        ds.run_adjoint(torch.zeros_like(a.work), a.nvars, a.factors, -1, 0x7FFFFFFF,
+                       rotvars=a.rotvars)
 
 
 
@@ -1126,3 +1132,72 @@ def test_gpu_batch_refuses_a_pair_member_and_flags_a_bad_table(cuda_lib):
     batch.fill()
     assert batch.device_status() == _native.TAM_EINVAL
     assert batch.device_status() == 0   # read and cleared
+
+
+# --- the adjoint of a RotationPair ------------------------------------------------------------
+
+PAIR_ADJ_CASES = [(2, (1, 2), "none"), (2, (2, 1), "none"), (3, (1, 2), "reflect_lo"),
+                  (3, (3, 2), "periodic")]
+
+
+def oracle_pair_adjoint(pair, schedules, ya, yb):
+    """The oracle's transpose of ``oracle_pair_fill`` without the hook: tag by
+    tag from the last, b's stage transpose then a's, odd turns scattering
+    onto the partner's cotangent."""
+    sa, sb = schedules
+    mem = [(sa, ya, yb, pair.a, pair.afactors_host, pair.arotvars_host),
+           (sb, yb, ya, pair.b, pair.bfactors_host, pair.brotvars_host)]
+    tags = sorted(set(sa.stage_tags) | set(sb.stage_tags))
+    for tag in reversed(tags):
+        for s, y, alt, fs, fac, rv in reversed(mem):
+            oracle.fill_adjoint(s, y, fs.nvars, fac, first=tag, last=tag, rotvars=rv, alt=alt)
+    return ya, yb
+
+
+def _pair_vectors(pair, seed):
+    rng = np.random.default_rng(seed)
+    return [rng.uniform(-1, 1, size=tuple(fs.work.shape)) for fs in (pair.a, pair.b)]
+
+
+@pytest.mark.parametrize("D,plane,other", PAIR_ADJ_CASES)
+def test_oracle_adjoint_dot_product_of_a_rotation_pair(D, plane, other):
+    """``<A x, y> = <x, A^T y>`` to 1e-13 over both members of a pair, whose
+    odd turns read (and whose transposes add onto) the partner's array."""
+    quad, pair, (sa, sb), ops = pair_case(D, plane, other)
+    xa, xb = _pair_vectors(pair, 11)
+    ya, yb = _pair_vectors(pair, 12)
+    pair.a.work, pair.b.work = torch.from_numpy(xa.copy()), torch.from_numpy(xb.copy())
+    axa, axb = oracle_pair_fill(pair, (sa, sb), hook_zero=False)
+    ata, atb = oracle_pair_adjoint(pair, (sa, sb), ya.copy(), yb.copy())
+    lhs = _dot(axa, ya) + _dot(axb, yb)
+    rhs = _dot(xa, ata) + _dot(xb, atb)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,plane,other", PAIR_ADJ_CASES)
+def test_gpu_adjoint_of_a_rotation_pair(cuda_lib, D, plane, other):
+    """The device adjoint of a pair fill (``fill_pair_adjoint``): the dot
+    test against the device pair fill to 1e-13, and the oracle's transpose
+    to the sums' rounding."""
+    from treeamr.adjoint import fill_pair_adjoint
+    from treeamr.ghosts import fill_pair
+    quad, pair, (sa, sb), ops = pair_case(D, plane, other)
+    for fs in (pair.a, pair.b):
+        fs.factors = fs.factors.cuda()
+    pair.to("cuda")
+    xa, xb = _pair_vectors(pair, 13)
+    ya, yb = _pair_vectors(pair, 14)
+    pair.a.work = torch.from_numpy(xa.copy()).cuda()
+    pair.b.work = torch.from_numpy(xb.copy()).cuda()
+    fill_pair(pair, (sa, sb))
+    axa, axb = pair.a.work.cpu().numpy(), pair.b.work.cpu().numpy()
+    da, db = torch.from_numpy(ya.copy()).cuda(), torch.from_numpy(yb.copy()).cuda()
+    fill_pair_adjoint(pair, (sa, sb), da, db)
+    torch.cuda.synchronize()
+    ata, atb = da.cpu().numpy(), db.cpu().numpy()
+    lhs = _dot(axa, ya) + _dot(axb, yb)
+    rhs = _dot(xa, ata) + _dot(xb, atb)
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+    wa, wb = oracle_pair_adjoint(pair, (sa, sb), ya.copy(), yb.copy())
+    assert np.max(np.abs(ata - wa)) < 1e-13 and np.max(np.abs(atb - wb)) < 1e-13

@@ -212,20 +212,25 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
 }
 
 // Pass 2: one CTA per source block, its transfers' boxes added in order.
+// An odd turn adds onto the block of the alternate array `yalt` (a
+// RotationPair's partner: the same block and variable strides, the plane's
+// extents swapped, which the turn's strides carry; or y itself), so every
+// add into either array's block is this CTA's, in transfer order.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
     const AdjReduce *__restrict__ red, int64_t nred, const int2 *__restrict__ list,
-    AdjArgs<T> a, T *y, const T *scratch, int nvars, int S1, int S2, int S3) {
+    AdjArgs<T> a, T *y, T *yalt, const T *scratch, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
   for (int64_t b = blockIdx.x; b < nred; b += gridDim.x) {
     const AdjReduce r = red[b];
     // the transfers reading one block all belong to its forest
     const int member = a.groups[list[r.first].y].member;
     const AdjLayout<T, BATCH> L(a, member, y, nullptr, nvars, S1, S2, S3);
-    T *yb = L.y + (int64_t)r.sblock * L.bs;
+    const AdjLayout<T, BATCH> La(a, member, yalt, nullptr, nvars, S1, S2, S3);
     for (int q = 0; q < r.count; ++q) {
       const int2 tg = list[r.first + q];  // (transfer, group)
       const AdjGroup &h = a.ag[tg.y];
+      T *yb = ((h.col & 1) ? La.y : L.y) + (int64_t)r.sblock * L.bs;
       const T *src = scratch + __ldg(a.scr + tg.x) * nvars;
       const int64_t n = h.fsize * nvars;
       const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
@@ -351,7 +356,8 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
     if (st.nred > 0) {
       const int64_t blocks = std::min<int64_t>(st.nred, (int64_t)1 << 30);
       adjoint_reduce_kernel<T, D, BATCH><<<(unsigned)blocks, threads, 0, stream>>>(
-          p.red + st.red0, st.nred, (const int2 *)p.list, a, y, scratch, nvars, S1, S2, S3);
+          p.red + st.red0, st.nred, (const int2 *)p.list, a, y, r.alt ? (T *)r.alt : y, scratch,
+          nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -516,7 +522,8 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
                         (int64_t)a.fn[0] * a.fn[1] * g.n[2];
       st.smem_elems = std::max(st.smem_elems, n);
     }
-    // pass-2 lists by source block, transfers in transfer order
+    // pass-2 lists by source block, transfers in transfer order (a block's
+    // list holds the odd turns that read the alternate array's block too)
     std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) {
       return x.sblock != y.sblock ? x.sblock < y.sblock : x.transfer < y.transfer;
     });
@@ -676,11 +683,12 @@ cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int 
                : run_dim<float, false>(plan, r, y, nvars, factors, first, last, scratch, stream);
 }
 
-cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
+cudaError_t adjoint_run(tam_sched *s, void *y, void *alt, int nvars, const void *factors,
                         const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
                         cudaStream_t stream) {
   AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
-           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars, s->d_err};
+           &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars, s->d_err,
+           alt ? alt : y};
   return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
 }
 
@@ -767,8 +775,8 @@ extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int
     }
     scratch = g_static_ptr[ctx->device];
   }
-  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, nullptr, first_stage, last_stage,
-                                   scratch, (cudaStream_t)stream);
+  cudaError_t e = tam::adjoint_run(s, y, nullptr, nvars, factors, nullptr, first_stage,
+                                   last_stage, scratch, (cudaStream_t)stream);
   if (prev != ctx->device) cudaSetDevice(prev);
   if (e != cudaSuccess) {
     cudaGetLastError();

@@ -654,21 +654,22 @@ void tam_schedule_free(tam_sched *s) {
   delete s;
 }
 
+// Whether odd turns read another array than the set's own: a RotationPair
+// member, whose layout is not symmetric in the seam's plane.
+static bool reads_partner(const tam_sched *s) {
+  for (const tam_group &h : s->host_groups) {
+    if (!(h.orientation & 1)) continue;
+    for (int e = 0; e < s->D; ++e)
+      if (s->S[(h.axes >> (2 * e)) & 3] != s->S[e]) return true;
+  }
+  return false;
+}
+
 static int adjoint_ready(tam_sched *s) {
   if (s->adj.ready) return TAM_OK;
   if (s->has_bounded)
     return fail(s->ctx, TAM_EUNSUPPORTED,
                 "a schedule with bounded operators is not linear, so it has no adjoint");
-  // a turned group's transpose writes into the set's own array: the layout
-  // must be symmetric in the seam's plane (not a RotationPair member)
-  for (const tam_group &h : s->host_groups) {
-    if (!h.orientation) continue;
-    for (int e = 0; e < s->D; ++e)
-      if (s->S[(h.axes >> (2 * e)) & 3] != s->S[e])
-        return fail(s->ctx, TAM_EUNSUPPORTED,
-                    "the adjoint of a RotationPair member (a layout not symmetric in the "
-                    "seam's plane) is not built");
-  }
   std::string err;
   int rc = tam::adjoint_prepare(s, err);
   if (rc != TAM_OK) return fail(s->ctx, rc, err);
@@ -687,16 +688,28 @@ int tam_adjoint_scratch_bytes(tam_sched *s, int32_t nvars, size_t *bytes) {
 
 static int check_fill_args(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
                            const void *factors);
-static int owned_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+static int owned_adjoint(tam_sched *s, void *y, void *alt, int32_t nvars, int64_t nblocks,
                          const void *factors, const int32_t *rotvars, int32_t first_stage,
                          int32_t last_stage, void *stream);
 
+// A turned group's transpose adds onto the array its forward fill read: the
+// set's own, or for odd turns of a RotationPair member the partner's.
+static int check_partner(tam_sched *s, const void *alt) {
+  if (!alt && reads_partner(s))
+    return fail(s->ctx, TAM_EUNSUPPORTED,
+                "this is a RotationPair member (a layout not symmetric in the seam's plane): "
+                "its adjoint adds onto the partner's array, so use tam_fill_adjoint_alt");
+  return TAM_OK;
+}
+
 // The adjoint with the caller's scratch (which may be NULL only when the
 // schedule needs none).
-static int adjoint_with(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+static int adjoint_with(tam_sched *s, void *y, void *alt, int32_t nvars, int64_t nblocks,
                         const void *factors, const int32_t *rotvars, int32_t first_stage,
                         int32_t last_stage, void *scratch, size_t scratch_bytes, void *stream) {
   int rc = check_fill_args(s, y, nvars, nblocks, factors);
+  if (rc != TAM_OK) return rc;
+  rc = check_partner(s, alt);
   if (rc != TAM_OK) return rc;
   if (s->needs_rotvars && !rotvars)
     return fail(s->ctx, TAM_EINVAL,
@@ -709,7 +722,7 @@ static int adjoint_with(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
   const size_t need = (size_t)s->adj.scratch_points * nvars * (s->dtype == TAM_F64 ? 8 : 4);
   if (need > 0 && (!scratch || scratch_bytes < need))
     return fail(s->ctx, TAM_EINVAL, "adjoint scratch smaller than tam_adjoint_scratch_bytes");
-  cudaError_t e = tam::adjoint_run(s, y, nvars, factors, rotvars, first_stage, last_stage,
+  cudaError_t e = tam::adjoint_run(s, y, alt, nvars, factors, rotvars, first_stage, last_stage,
                                    scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "adjoint launch");
   return TAM_OK;
@@ -718,21 +731,28 @@ static int adjoint_with(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
 int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                              const void *factors, int32_t first_stage, int32_t last_stage,
                              void *scratch, size_t scratch_bytes, void *stream) {
-  return adjoint_with(s, y, nvars, nblocks, factors, nullptr, first_stage, last_stage, scratch,
-                      scratch_bytes, stream);
+  return adjoint_with(s, y, nullptr, nvars, nblocks, factors, nullptr, first_stage, last_stage,
+                      scratch, scratch_bytes, stream);
 }
 
 int tam_fill_adjoint_ex(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                         const void *factors, const int32_t *rotvars, int32_t first_stage,
                         int32_t last_stage, void *scratch, size_t scratch_bytes, void *stream) {
+  return tam_fill_adjoint_alt(s, y, nullptr, nvars, nblocks, factors, rotvars, first_stage,
+                              last_stage, scratch, scratch_bytes, stream);
+}
+
+int tam_fill_adjoint_alt(tam_sched *s, void *y, void *alt_y, int32_t nvars, int64_t nblocks,
+                         const void *factors, const int32_t *rotvars, int32_t first_stage,
+                         int32_t last_stage, void *scratch, size_t scratch_bytes, void *stream) {
   if (!scratch) {
     int rc = check_fill_args(s, y, nvars, nblocks, factors);
     if (rc != TAM_OK) return rc;
-    return owned_adjoint(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage,
-                         stream);
+    return owned_adjoint(s, y, alt_y, nvars, nblocks, factors, rotvars, first_stage,
+                         last_stage, stream);
   }
-  return adjoint_with(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage, scratch,
-                      scratch_bytes, stream);
+  return adjoint_with(s, y, alt_y, nvars, nblocks, factors, rotvars, first_stage, last_stage,
+                      scratch, scratch_bytes, stream);
 }
 
 int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, const void *factors,
@@ -742,9 +762,11 @@ int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks, cons
 }
 
 // The adjoint with the library's own scratch, grown on demand.
-static int owned_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
+static int owned_adjoint(tam_sched *s, void *y, void *alt, int32_t nvars, int64_t nblocks,
                          const void *factors, const int32_t *rotvars, int32_t first_stage,
                          int32_t last_stage, void *stream) {
+  int rc0 = check_partner(s, alt);
+  if (rc0 != TAM_OK) return rc0;
   if (s->needs_rotvars && !rotvars)
     return fail(s->ctx, TAM_EINVAL,
                 "this schedule turns ghosts across a rotating seam, but no variable table was "
@@ -765,7 +787,7 @@ static int owned_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
     if (e != cudaSuccess) return fail(s->ctx, TAM_ENOMEM, "adjoint scratch allocation failed");
     s->adj_scratch_bytes = need;
   }
-  return adjoint_with(s, y, nvars, nblocks, factors, rotvars, first_stage, last_stage,
+  return adjoint_with(s, y, alt, nvars, nblocks, factors, rotvars, first_stage, last_stage,
                       s->adj_scratch, s->adj_scratch_bytes, stream);
 }
 

@@ -411,7 +411,7 @@ int tam_batch_fill_adjoint_ex(tam_batch *b, void *arena, int64_t arena_elems, in
   }
   const tam::AdjRun r{b->dtype,   b->D,      b->d_groups, b->d_tb,   b->d_weights,
                       b->d_members, b->d_tiles, &b->stages, {1, 1, 1}, b->d_solos,
-                      rotvars,     b->d_err};
+                      rotvars,     b->d_err,    arena};
   cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena, first_stage,
                                         last_stage, b->adj_scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) {

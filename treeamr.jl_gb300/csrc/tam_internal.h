@@ -314,7 +314,9 @@ cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mi
 // The adjoint (tam_adjoint.cu).
 int adjoint_prepare(tam_sched *s, std::string &err);
 void adjoint_free(tam_sched *s);
-cudaError_t adjoint_run(tam_sched *s, void *y, int nvars, const void *factors,
+// `alt`: the array odd turns read in the forward fill (a RotationPair's
+// partner), onto which their transposes add; null: `y` itself.
+cudaError_t adjoint_run(tam_sched *s, void *y, void *alt, int nvars, const void *factors,
                         const int32_t *rotvars, int32_t first, int32_t last, void *scratch,
                         cudaStream_t stream);
 
@@ -341,6 +343,7 @@ struct AdjRun {
   const SoloGroup *turns;          // the solo groups (their targets are zeroed too)
   const int32_t *rotvars;          // the variable table of turned groups, or null
   int32_t *err;                    // error word: a variable table naming no variable
+  void *alt;                       // odd turns' sources (a RotationPair's partner), or null
 };
 cudaError_t adjoint_run_plan(const AdjPlan &plan, const AdjRun &r, void *y, int nvars,
                              const void *factors, int32_t first, int32_t last, void *scratch,

@@ -259,6 +259,9 @@ def _declare(lib: C.CDLL):
     lib.tam_fill_adjoint_ex.argtypes = [vp, vp, i32, i64, vp, vp, i32, i32, vp, C.c_size_t,
                                         vp]
     lib.tam_fill_adjoint_ex.restype = C.c_int
+    lib.tam_fill_adjoint_alt.argtypes = [vp, vp, vp, i32, i64, vp, vp, i32, i32, vp,
+                                         C.c_size_t, vp]
+    lib.tam_fill_adjoint_alt.restype = C.c_int
     lib.tam_regrid_upload.argtypes = [vp, C.POINTER(tam_schedule_desc), i64, C.POINTER(vp)]
     lib.tam_regrid_upload.restype = C.c_int
     lib.tam_regrid_transfer.argtypes = [vp, vp, i64, vp, i64, i32, vp]

@@ -51,6 +51,45 @@ def fill_ghosts_adjoint(fs: FieldSet, schedule: GhostSchedule, y: Optional[torch
     return y
 
 
+def fill_pair_adjoint(pair, schedules, ya: Optional[torch.Tensor] = None,
+                      yb: Optional[torch.Tensor] = None, *,
+                      stream: Optional[torch.cuda.Stream] = None):
+    """``(y_a, y_b) <- A^T (y_a, y_b)`` in place for a RotationPair's fill
+    (``fill_pair``, without hooks), ``y_a`` and ``y_b`` shaped like the
+    members' arrays (default: the arrays themselves).  The forward fill runs,
+    tag by tag, the first member's stage and then the second's, each member's
+    odd turns reading its partner's array; the transpose runs the tags from
+    the last, the second member's stage transpose and then the first's, each
+    adding its odd turns' transposes onto the partner's cotangent
+    (``tam_fill_adjoint_alt``)."""
+    from .storage import RotationPair
+    if not isinstance(pair, RotationPair):
+        raise TypeError("fill_pair_adjoint takes a RotationPair")
+    sa, sb = schedules
+    a, b = pair.a, pair.b
+    check_fill(a, sa, pair=True)
+    check_fill(b, sb, pair=True)
+    ya = a.work if ya is None else ya
+    yb = b.work if yb is None else yb
+    for fs, y in ((a, ya), (b, yb)):
+        if y.shape != fs.work.shape or y.dtype != fs.work.dtype or y.device != fs.work.device:
+            raise ValueError("each adjoint vector must have its member's shape, type and device")
+        if not y.is_contiguous():
+            raise ValueError("the adjoint vectors must be contiguous")
+    if ya.data_ptr() == yb.data_ptr():
+        raise ValueError("the members' adjoint vectors must be distinct arrays")
+    members = [(a, sa, pair.afactors, pair.arotvars, ya, yb),
+               (b, sb, pair.bfactors, pair.brotvars, yb, ya)]
+    dss = [device_schedule(s, y.device.index or 0) for _, s, _, _, y, _ in members]
+    tags = sorted(set(sa.stage_tags) | set(sb.stage_tags))
+    for tag in reversed(tags):
+        for i in (1, 0):
+            fs, s, fac, rv, y, alt = members[i]
+            if tag in s.stage_tags:
+                dss[i].run_adjoint(y, fs.nvars, fac, tag, tag, stream, rotvars=rv, alt=alt)
+    return ya, yb
+
+
 class GhostFill(torch.autograd.Function):
     """``out = A(x)``: the filled copy of ``x`` (the field set's layout), with
     ``d out / d x`` applied by the adjoint kernel."""

@@ -80,19 +80,24 @@ class DeviceSchedule:
     def run_adjoint(self, y: torch.Tensor, nvars: int, factors: torch.Tensor, first: int,
                     last: int, stream: Optional[torch.cuda.Stream] = None,
                     scratch: Optional[torch.Tensor] = None,
-                    rotvars: Optional[torch.Tensor] = None):
+                    rotvars: Optional[torch.Tensor] = None,
+                    alt: Optional[torch.Tensor] = None):
         """``y <- A^T y`` in place (``tam_fill_adjoint``), or with the caller's
         scratch tensor (``tam_fill_adjoint_scratch``); a schedule across a
-        seam passes the variable table (``tam_fill_adjoint_ex``)."""
+        seam passes the variable table (``tam_fill_adjoint_ex``), and a
+        RotationPair member its partner's cotangent ``alt``, onto which its
+        odd turns' transposes add (``tam_fill_adjoint_alt``)."""
         s = stream if stream is not None else torch.cuda.current_stream(y.device)
-        if rotvars is not None:
-            rc = self.lib.tam_fill_adjoint_ex(
-                self.handle, C.c_void_p(y.data_ptr()), nvars, y.shape[0],
-                C.c_void_p(factors.data_ptr()), C.c_void_p(rotvars.data_ptr()), first, last,
+        if rotvars is not None or alt is not None:
+            rc = self.lib.tam_fill_adjoint_alt(
+                self.handle, C.c_void_p(y.data_ptr()),
+                C.c_void_p(alt.data_ptr() if alt is not None else 0), nvars, y.shape[0],
+                C.c_void_p(factors.data_ptr()),
+                C.c_void_p(rotvars.data_ptr() if rotvars is not None else 0), first, last,
                 C.c_void_p(scratch.data_ptr() if scratch is not None else 0),
                 0 if scratch is None else scratch.numel() * scratch.element_size(),
                 C.c_void_p(s.cuda_stream))
-            _native.check(rc, self.ctx, "tam_fill_adjoint_ex")
+            _native.check(rc, self.ctx, "tam_fill_adjoint_alt")
             return
         if scratch is None:
             rc = self.lib.tam_fill_adjoint(self.handle, C.c_void_p(y.data_ptr()), nvars,
