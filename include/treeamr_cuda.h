@@ -444,7 +444,11 @@ int tam_gather(const tam_state_layout *layout, const void *work, void *state, vo
  * members = 4 (a quarter turn) or (t_0 + t_2) / 2 for members = 2 (a half
  * turn).  `buffer` (npoints * nvars elements) holds the means, all gathered
  * before any is written.  ncol is 3^D, the factor table's columns per
- * orientation.  A variable table naming no variable gives NaN. */
+ * orientation.  A variable table naming no variable gives NaN.  The
+ * projection's transpose (for the adjoint fill, between stage 0's transpose
+ * and stage P's) is the same call with each column r of the variable table
+ * inverted and each factor moved with its variable: rotvars'[w, r] = v and
+ * factors'[w, ncol r] = factors[v, ncol r] where rotvars[v, r] = w. */
 int tam_axis_project(int32_t dtype, const int64_t *points, int64_t npoints, int32_t members,
                      void *work, int32_t nvars, int64_t block_points, const void *factors,
                      int32_t ncol, const int32_t *rotvars, void *buffer, void *stream);

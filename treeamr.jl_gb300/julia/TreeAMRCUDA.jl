@@ -206,31 +206,117 @@ function fill_pair!(pair::RotationPair, (sa, sb)::Tuple{GhostSchedule,GhostSched
 end
 stage_tags(s::GhostSchedule) = Int32[first(x) for x in stage_groups(s)]
 
+# Stage P's axis part (run_axis!, src/ghosts.jl:757-766) through
+# tam_axis_project, between stage P and stage 0: the schedule's axis points
+# (a MeanPoints, src/ghosts.jl:677-689) as element offsets of variable 0 in
+# the working array, kept per schedule.  `transpose` runs the projection's
+# transpose, the same call with each column of the variable table inverted
+# and each factor moved with its variable, which the adjoint runs between
+# stage 0's transpose and stage P's.
+const AXIS_OFFSETS = WeakKeyDict{GhostSchedule,Any}()
+function axis_offsets(fs::FieldSet, schedule::GhostSchedule)
+    get!(AXIS_OFFSETS, schedule) do
+        ax = schedule.axis
+        S = size(fs.work)[1:end-2]
+        vol = prod(S)
+        blocks, points = Array(ax.blocks), Array(ax.points)
+        offs = Int64[]
+        for i in eachindex(blocks)
+            o = 0
+            for d in length(S):-1:1
+                o = o * S[d] + (points[i][d] - 1)
+            end
+            push!(offs, (Int64(blocks[i]) - 1) * fs.nvars * vol + o)
+        end
+        (CuArray(offs), vol)
+    end
+end
+function transposed_tables(fs::FieldSet{T,D}) where {T,D}
+    fac, rv = Array(fs.factors), Array(fs.rotvars)
+    ncol = 3^D
+    ft, rt = zero(fac), similar(rv)
+    for r in 0:3, v in 1:fs.nvars
+        w = rv[v, r+1]
+        rt[w, r+1] = v
+        ft[w, ncol*r+1] = fac[v, ncol*r+1]
+    end
+    return CuArray(ft), CuArray(rt)
+end
+function run_axis!(A::CuArray{T}, fs::FieldSet{T,D}, schedule::GhostSchedule;
+                   transpose::Bool=false) where {T,D}
+    schedule.axis === nothing && return nothing
+    TreeAMR.turns_variables(fs) || return nothing
+    offs, vol = axis_offsets(fs, schedule)
+    factors, rotvars = transpose ? transposed_tables(fs) : (fs.factors, fs.rotvars)
+    buf = CuArray{T}(undef, length(offs) * fs.nvars)
+    members = TreeAMR.ishalfturn(fs.forest) ? Int32(2) : Int32(4)
+    rc = ccall((:tam_axis_project, LIB), Cint,
+               (Int32, CuPtr{Int64}, Int64, Int32, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid},
+                Int32, CuPtr{Int32}, CuPtr{Cvoid}, Ptr{Cvoid}),
+               T === Float64 ? TAM_F64 : TAM_F32, pointer(offs), length(offs), members,
+               pointer(A), fs.nvars, vol, pointer(factors), Int32(3^D), pointer(rotvars),
+               pointer(buf), CUDA.stream().handle)
+    rc == 0 || error("tam_axis_project failed ($rc)")
+    return nothing
+end
+
 # The drop-in: fill_ghosts! of a CuArray field set (src/ghosts.jl:1783),
-# after the reference's own checks.
+# after the reference's own checks: stage P, the axis, then the rest, the
+# hook after phase 1 (src/ghosts.jl:1111-1136).
 function TreeAMR.exchange_ghosts!(fs::FieldSet{T,D,R,<:CuArray}, schedule::GhostSchedule,
                                   boundary, backend) where {T,D,R}
     ds = device_schedule(schedule)
+    tam_fill!(fs, ds, STAGE_FIRST, Int32(-1))
+    run_axis!(fs.work, fs, schedule)
     if boundary === nothing
-        tam_fill!(fs, ds, STAGE_FIRST, STAGE_LAST)
+        tam_fill!(fs, ds, Int32(0), STAGE_LAST)
     else
-        tam_fill!(fs, ds, STAGE_FIRST, Int32(1))
+        tam_fill!(fs, ds, Int32(0), Int32(1))
         TreeAMR.apply_boundary!(fs, boundary, schedule, backend)
         tam_fill!(fs, ds, Int32(2), STAGE_LAST)
     end
     return fs
 end
 
-# y <- A^T y (tam_fill_adjoint): the pullback of the fill.
+# y <- A^T y over stages [first, last] (tam_fill_adjoint_alt): with the
+# variable table across a seam, and for a pair member the partner's
+# cotangent `alt`, onto which odd turns' transposes add.
+function tam_fill_adjoint!(y::CuArray, fs::FieldSet, ds::DeviceSchedule, first::Int32,
+                           last::Int32; factors=fs.factors, rotvars=fs.rotvars, alt=nothing)
+    rc = ccall((:tam_fill_adjoint_alt, LIB), Cint,
+               (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid},
+                CuPtr{Int32}, Int32, Int32, CuPtr{Cvoid}, Csize_t, Ptr{Cvoid}),
+               ds.handle, pointer(y), alt === nothing ? CU_NULL : pointer(alt), fs.nvars,
+               size(y, ndims(y)), factors === nothing ? CU_NULL : pointer(factors),
+               rotvars === nothing ? CU_NULL : pointer(rotvars), first, last, CU_NULL, 0,
+               CUDA.stream().handle)
+    check(rc, ds.ctx, "tam_fill_adjoint_alt")
+end
+
+# y <- A^T y: the pullback of the fill, the axis projection's transpose
+# between stage 0's and stage P's.
 function fill_ghosts_adjoint!(y::CuArray, fs::FieldSet, schedule::GhostSchedule)
     ds = device_schedule(schedule)
-    factors = fs.factors === nothing ? CU_NULL : pointer(fs.factors)
-    rc = ccall((:tam_fill_adjoint, LIB), Cint,
-               (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Int32, Ptr{Cvoid}),
-               ds.handle, pointer(y), fs.nvars, size(y, ndims(y)), factors, STAGE_FIRST,
-               STAGE_LAST, CUDA.stream().handle)
-    check(rc, ds.ctx, "tam_fill_adjoint")
+    tam_fill_adjoint!(y, fs, ds, Int32(0), STAGE_LAST)
+    run_axis!(y, fs, schedule; transpose=true)
+    tam_fill_adjoint!(y, fs, ds, STAGE_FIRST, Int32(-1))
     return y
+end
+
+# (ya, yb) <- A^T (ya, yb) for a pair fill without hooks: tag by tag from the
+# last, b's stage transpose then a's, each adding onto the other's cotangent.
+function fill_pair_adjoint!(ya::CuArray, yb::CuArray, pair::RotationPair,
+                            (sa, sb)::Tuple{GhostSchedule,GhostSchedule})
+    a, b = pair.a, pair.b
+    da, db = device_schedule(sa), device_schedule(sb)
+    ta, tb = stage_tags(sa), stage_tags(sb)
+    for t in reverse(sort!(unique!(vcat(ta, tb))))
+        t in tb && tam_fill_adjoint!(yb, b, db, t, t; factors=pair.bfactors,
+                                     rotvars=pair.brotvars, alt=ya)
+        t in ta && tam_fill_adjoint!(ya, a, da, t, t; factors=pair.afactors,
+                                     rotvars=pair.arotvars, alt=yb)
+    end
+    return ya, yb
 end
 
 # A field set held in host memory, filled on the GPU (tam_fill_host): the
