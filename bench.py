@@ -63,6 +63,9 @@ def parse():
                     help="walls: time only the walls mesh (for profiling)")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32",
                     help="element type of --workload walls")
+    ap.add_argument("--sector-minimum", type=int, default=None, metavar="TAG",
+                    help="with --workload walls: count, on the CPU, the 32-byte sectors the "
+                         "unit copies of stage TAG read and write, print them and exit")
     return ap.parse_args()
 
 
@@ -545,6 +548,49 @@ def footprint_points(sched):
     return int(wr.sum()), int(rd.sum())
 
 
+def sector_minimum(sched, nvars: int, esize: int, tag: int):
+    """The least DRAM traffic of the unit copies of stage ``tag`` that the
+    layout allows: every distinct 32-byte sector they read fetched once, every
+    sector they write stored once, and (with read-modify-write) every partly
+    written sector fetched once too.  Per variable plane, in bytes."""
+    S1, S2, S3 = (tuple(sched.stored) + (1, 1))[:3]
+    vol = S1 * S2 * S3
+    groups = [g for g in sched.groups if g.stage == tag and g.unit]
+    rd_s = wr_s = part_s = rp_s = 0
+    alg = 0
+    for v in range(nvars):
+        rd, wr = [], []
+        for g in groups:
+            st = list(g.stencils) + [None] * (3 - len(g.stencils))
+            tx = [np.arange(x.targetfirst - 1, x.targetfirst - 1 + x.ntarget) if x else
+                  np.zeros(1, np.int64) for x in st]
+            sx = [np.asarray(x.srcstart, np.int64) - 1 if x else np.zeros(1, np.int64)
+                  for x in st]
+            toff = (tx[2][:, None, None] * S2 + tx[1][None, :, None]) * S1 + tx[0][None, None, :]
+            soff = (sx[2][:, None, None] * S2 + sx[1][None, :, None]) * S1 + sx[0][None, None, :]
+            tb = np.asarray(g.targetblocks, np.int64) - 1
+            sb = np.asarray(g.sourceblocks, np.int64) - 1
+            wr.append(((tb[:, None] * nvars + v) * vol + toff.ravel()[None, :]).ravel())
+            rd.append(((sb[:, None] * nvars + v) * vol + soff.ravel()[None, :]).ravel())
+        if not wr:
+            break
+        w = np.concatenate(wr) * esize
+        r = np.concatenate(rd) * esize
+        alg += (w.size + r.size) * esize
+        ws, wc = np.unique(w // 32, return_counts=True)
+        rs = np.unique(r // 32)
+        partial = ws[wc < 32 // esize]
+        wr_s += ws.size
+        rd_s += rs.size
+        part_s += partial.size
+        rp_s += np.union1d(rs, partial).size
+    return {"stage": tag, "groups": len(groups), "algorithmic_bytes": alg,
+            "sectors_read_bytes": rd_s * 32, "sectors_written_bytes": wr_s * 32,
+            "partly_written_bytes": part_s * 32,
+            "minimum_bytes": (rd_s + wr_s) * 32,
+            "minimum_bytes_with_rmw": (rp_s + wr_s) * 32}
+
+
 def cpu_fill_rate(sched, fs_host_work, nvars, factors, bytes_per_fill, budget_s=15.0,
                   max_runs=5):
     """The oracle's threaded fill on every host core: (GB/s, seconds per
@@ -573,6 +619,18 @@ def main():
         if rank != 0:
             return 0
         return run_reference(args)
+
+    if args.sector_minimum is not None:
+        if args.workload != "walls":
+            raise SystemExit("--sector-minimum counts the walls mesh: give --workload walls")
+        from treeamr import GhostSchedule, meshes
+        T = np.dtype(args.dtype).type
+        f, fs, ops = meshes.walls_setup(T=T, roots=args.roots)
+        sched = GhostSchedule(fs, ops)
+        out = sector_minimum(sched, fs.nvars, np.dtype(T).itemsize, args.sector_minimum)
+        out.update({"roots": args.roots, "dtype": args.dtype, "blocks": f.nleaves()})
+        print(json.dumps(out), flush=True)
+        return 0
 
     import torch
     import torch.distributed as dist
