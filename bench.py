@@ -325,6 +325,43 @@ def measure_hook(dev, timed, args):
     return out
 
 
+def measure_pv6(dev, timed, args):
+    """The sphere mesh with the order-6 variant of its operators, PV(6,6):
+    the same 8^3 periodic roots, N=16, G=3, 3 levels and 4 Float64
+    variables; fused (autotuned) and plain fills, and the stated error."""
+    import torch
+    from treeamr import GhostSchedule, fill_ghosts, meshes
+    from treeamr.autotune import autotune
+    f, fs, ops = meshes.sphere_setup(device=dev, nvars=args.nvars, roots=args.roots,
+                                     levels=args.levels, p=6)
+    sched = GhostSchedule(fs, ops)
+    g = torch.Generator(device=dev).manual_seed(11)
+    fs.work.uniform_(-1.0, 1.0, generator=g)
+    tuned = autotune(fs, sched)
+    bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * 8
+    fill_ghosts(fs, sched)
+    steps = max(3, args.steps // 2)
+    ms = timed(lambda: fill_ghosts(fs, sched), steps)
+    filled = fs.work.cpu().numpy()
+    err = fill_error(sched, filled, filled, fs.nvars, fs.factors_host, per_group=1)
+    del filled
+    fill_ghosts(fs, sched, method="plain")
+    ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(2, steps // 2))
+    out = {"workload": f"sphere, PV(6,6): {args.roots}^3 periodic roots, N=16, G=3, "
+                       f"{args.levels} levels, {args.nvars} vars F64",
+           "blocks": f.nleaves(), "groups": len(sched.groups),
+           "value": bytes_per_fill / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
+           "plain": {"ms_per_step": ms_plain, "speedup_fused_vs_plain": ms_plain / ms},
+           # the stencils' algorithmic FP64 operations over the whole fill's
+           # time (copies included): a lower bound of the stencil stages' rate
+           "fp64_tflops_over_fill": sum(stencil_flops(sched, fs.nvars).values()) / (ms * 1e-3)
+           / 1e12,
+           "error": err, "tuned": tuned}
+    del fs, sched
+    torch.cuda.empty_cache()
+    return out
+
+
 def measure_regrid(dev, timed, args):
     """The regrid transfer (``regrid!``'s move of the own points) on the
     sphere mesh: every level-0 leaf with x < 0.25 refined and a tenth of the
@@ -807,6 +844,7 @@ def main():
         walls["batch64_float32"] = measure_batch(dev, timed, args, peak)
         walls["boundary_hook"] = measure_hook(dev, timed, args)
         walls["regrid"] = measure_regrid(dev, timed, args)
+        walls["sphere_pv6"] = measure_pv6(dev, timed, args)
 
     # end to end through the public call, host buffers, copies inside the timing
     e2e = None

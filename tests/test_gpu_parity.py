@@ -80,6 +80,17 @@ def test_nested_bit_exact(cuda_lib, method, D, T, p, G, N):
 
 
 @pytest.mark.parametrize("method", METHODS)
+def test_sphere_order6_bit_exact(cuda_lib, method):
+    """The sphere mesh's order-6 variant, PV(6,6) in 3-D (216 taps a
+    prolonged point), on a small case of the same construction: 2^3
+    periodic roots, N=16, G=3, 2 levels, 4 Float64 variables."""
+    f, fs, ops = meshes.sphere_setup(roots=2, levels=2, p=6)
+    meshes.random_fill(fs, seed=13)
+    got, expect = _gpu_vs_oracle(fs, ops, method)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+
+
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("D", [1, 2, 3])
 @pytest.mark.parametrize("T", [np.float64, np.float32])
 def test_awkward_data_bit_exact(cuda_lib, method, D, T):
