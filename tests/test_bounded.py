@@ -342,6 +342,29 @@ def test_gpu_bounded_fill_bit_exact(cuda_lib, D, T):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("D", [2, 3])
+def test_gpu_bounded_awkward_data_bit_exact(cuda_lib, D):
+    """+-0, NaN, +-Inf and subnormals through both bounds (the extrema and
+    the clamp with Julia's NaN-propagating min and max): the device fill,
+    fused and plain, is the oracle's bit for bit."""
+    from _helpers import awkward_fill
+    from treeamr import fill_ghosts
+    for name, C, ops, G in _gpu_cases(D):
+        f = nested_forest(D, N=8, periodic=(True,) * D)
+        fs = FieldSet(f, 2, G=G, centering=C)
+        s = GhostSchedule(fs, ops)
+        host = awkward_fill(tuple(fs.work.shape), np.float64, seed=D + 3)
+        fs.factors = fs.factors.cuda()
+        for method, one_tap in (("fused", True), ("plain", False)):
+            expect = oracle.fill(s, host.copy(), 2, fs.factors_host, one_tap=one_tap)
+            fs.work = torch.from_numpy(host.copy()).cuda()
+            fill_ghosts(fs, s, method=method)
+            torch.cuda.synchronize()
+            assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), \
+                (name, method)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D", [2, 3])
 def test_gpu_bounded_regrid_bit_exact(cuda_lib, D):
     """A bounded regrid on the device (the children bounded) is the
     oracle's replay bit for bit; the adjoint of a bounded schedule is

@@ -1201,3 +1201,28 @@ def test_gpu_adjoint_of_a_rotation_pair(cuda_lib, D, plane, other):
     assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
     wa, wb = oracle_pair_adjoint(pair, (sa, sb), ya.copy(), yb.copy())
     assert np.max(np.abs(ata - wa)) < 1e-13 and np.max(np.abs(atb - wb)) < 1e-13
+
+
+# --- awkward data across the seam ---------------------------------------------------------
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [("q", 2, (1, 2), "none", None), ("q", 3, (1, 2), "periodic", None),
+                                  ("h", 3, (1, 2), "periodic", None),
+                                  ("q", 2, (1, 2), "none", "vertex")])
+def test_gpu_awkward_data_across_the_seam(cuda_lib, case):
+    """+-0, NaN, +-Inf and subnormals through turned copies, restrictions,
+    prolongations and the axis projection (``test/ghost_tests.jl:507-560``):
+    the device fill, fused and plain, is the oracle's bit for bit."""
+    from _helpers import awkward_fill
+    from treeamr import fill_ghosts
+    kind, D, plane, other, which = case
+    C = _centering(D, plane, which) if which else None
+    quad, fs, s, *_ = quadrant_case(D, plane, other, half=kind == "h", C=C)
+    host = awkward_fill(tuple(fs.work.shape), np.float64, seed=D + 7)
+    fs.factors, fs.rotvars = fs.factors.cuda(), fs.rotvars.cuda()
+    for method, one_tap in (("fused", True), ("plain", False)):
+        expect = seam_fill(s, fs, host.copy(), one_tap=one_tap, hook_zero=False)
+        fs.work = torch.from_numpy(host.copy()).cuda()
+        fill_ghosts(fs, s, method=method)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), method
