@@ -313,3 +313,56 @@ def test_host_pipeline_own_uploads_equal_device_fill(cuda_lib):
     with pytest.raises(ValueError, match="hook"):
         HostPipeline(fw_s, GhostSchedule(fw_s, Operators(prolongation=4, restriction=4)),
                      own=True)
+
+
+# --- edge cases: no transfers, a block its own neighbour, ragged variable chunks ------------
+
+@pytest.mark.parametrize("method", METHODS)
+def test_a_schedule_without_transfers_changes_nothing(cuda_lib, method):
+    """A lone root with no periodic dimension has no neighbour: its schedule
+    has no group, and the fill (and its adjoint) leaves every bit as it was."""
+    from treeamr.adjoint import fill_ghosts_adjoint
+    f = Forest((1, 1, 1), N=8)
+    fs = FieldSet(f, 2, G=2)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    assert not [g for g in s.groups if g.ntransfers()]
+    host = awkward_fill(tuple(fs.work.shape), np.float64, seed=4)
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fill_ghosts(fs, s, method=method)
+    fill_ghosts_adjoint(fs, s)
+    torch.cuda.synchronize()
+    assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(host))
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_a_lone_periodic_root_is_its_own_neighbour(cuda_lib, method, T):
+    """One root per periodic dimension (``test/ghost_tests.jl:455-466``): the
+    block is its own neighbour in all 26 directions, and every ghost is the
+    own point a period away, bit for bit (the periodic tiling), as the
+    oracle's fill."""
+    N, G = 8, 2
+    f = Forest((1, 1, 1), N=N, periodic=(True, True, True))
+    fs = FieldSet(f, 3, G=G, T=T)
+    host = np.random.default_rng(6).uniform(-1, 1, size=tuple(fs.work.shape)).astype(T)
+    got, expect = _gpu_vs_oracle(fs, Operators(prolongation=4, restriction=4), method, host=host)
+    assert np.array_equal(nanbits(got), nanbits(expect))
+    own = host[0][:, G:G + N, G:G + N, G:G + N]
+    idx = (np.arange(N + 2 * G) - G) % N
+    tiled = own[:, idx][:, :, idx][:, :, :, idx]
+    assert np.array_equal(got[0].view(np.uint64 if T == np.float64 else np.uint32),
+                          tiled.view(np.uint64 if T == np.float64 else np.uint32))
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+@pytest.mark.parametrize("nvars", [1, 5, 11])
+def test_ragged_variable_counts_bit_exact(cuda_lib, method, T, nvars):
+    """Variable counts that leave ragged tails in the kernels' chunks (8
+    variables a copy chunk, 4 or 1 a stencil chunk): copies, restrictions
+    and prolongations in 3-D, bit for bit as the oracle."""
+    f = nested_forest(3, N=8, periodic=(True,) * 3)
+    fs = FieldSet(f, nvars, G=2, T=T)
+    host = np.random.default_rng(nvars).uniform(-1, 1, size=tuple(fs.work.shape)).astype(T)
+    got, expect = _gpu_vs_oracle(fs, Operators(prolongation=4, restriction=4), method, host=host)
+    assert np.array_equal(nanbits(got), nanbits(expect))
