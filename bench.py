@@ -592,7 +592,7 @@ def sector_minimum(sched, nvars: int, esize: int, tag: int):
     written sector fetched once too.  Per variable plane, in bytes."""
     S1, S2, S3 = (tuple(sched.stored) + (1, 1))[:3]
     vol = S1 * S2 * S3
-    groups = [g for g in sched.groups if g.stage == tag and g.unit]
+    groups = [g for g in sched.groups if g.stage == tag and g.unit()]
     rd_s = wr_s = part_s = rp_s = 0
     alg = 0
     for v in range(nvars):

@@ -103,3 +103,42 @@ def test_fill_error_states_the_sum_rounding():
             forest, groups = s.forest, [g]
         e2 = bench.fill_error(One, out, bad, 2, fs.factors_host, per_group=10 ** 6)
         assert e2["max_abs"] > 5e-4
+
+
+def test_sector_minimum_counts_every_copied_element():
+    """The layout's sector minimum the bench states for a stage's unit
+    copies equals a brute-force count over every copied element, on a small
+    2-D mesh (2 x 2 periodic roots, one refined, N=8, G=2, 3 Float32
+    variables): the distinct 32-byte sectors read and written, and those
+    written in part."""
+    import bench
+    from treeamr import FieldSet, Forest, GhostSchedule, Operators
+    from treeamr.schedule import PHASE1_TAG
+    f = Forest((2, 2), N=8, periodic=(True, True))
+    f.refine(f.leaves[0])
+    f.balance()
+    fs = FieldSet(f, 3, G=2, T=np.float32)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    got = bench.sector_minimum(s, fs.nvars, 4, PHASE1_TAG)
+    S1, S2 = s.stored[0], s.stored[1]
+    vol = S1 * S2
+    rd, wr = set(), {}
+    for g in s.groups:
+        if g.stage != PHASE1_TAG or not g.unit():
+            continue
+        s1, s2 = g.stencils
+        for t, src in zip(g.targetblocks, g.sourceblocks):
+            for v in range(fs.nvars):
+                for j in range(s2.ntarget):
+                    for i in range(s1.ntarget):
+                        ta = (((int(t) - 1) * fs.nvars + v) * vol +
+                              (s2.targetfirst - 1 + j) * S1 + s1.targetfirst - 1 + i) * 4
+                        sa = (((int(src) - 1) * fs.nvars + v) * vol +
+                              (int(s2.srcstart[j]) - 1) * S1 + int(s1.srcstart[i]) - 1) * 4
+                        wr[ta // 32] = wr.get(ta // 32, 0) + 1
+                        rd.add(sa // 32)
+    partial = {k for k, n in wr.items() if n < 8}
+    assert got["sectors_written_bytes"] == 32 * len(wr)
+    assert got["sectors_read_bytes"] == 32 * len(rd)
+    assert got["partly_written_bytes"] == 32 * len(partial)
+    assert got["minimum_bytes_with_rmw"] == 32 * (len(rd | partial) + len(wr))
