@@ -1226,3 +1226,26 @@ def test_gpu_awkward_data_across_the_seam(cuda_lib, case):
         fill_ghosts(fs, s, method=method)
         torch.cuda.synchronize()
         assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), method
+
+
+@pytest.mark.gpu
+def test_gpu_a_table_naming_no_variable_is_flagged(cuda_lib):
+    """A variable table naming no variable (every entry 0): the forward's
+    solo launch and the adjoint's pass 2 skip the writes it would steer and
+    set the schedule's error word, which the host reads and clears."""
+    from treeamr import _native, fill_ghosts
+    from treeamr.ghosts import device_schedule
+    quad, fs, s, *_ = quadrant_case(2, (1, 2), "none")
+    fs.factors = fs.factors.cuda()
+    fs.rotvars = torch.zeros_like(fs.rotvars).cuda()
+    fs.work = fs.work.cuda()
+    ds = device_schedule(s, 0)
+    ds.status(fs)
+    fill_ghosts(fs, s)
+    assert ds.status(fs) == _native.TAM_EINVAL
+    assert ds.status(fs) == 0
+    y = torch.ones_like(fs.work)
+    ds.run_adjoint(y, fs.nvars, fs.factors, _native.TAM_STAGE_ALL_FIRST,
+                   _native.TAM_STAGE_ALL_LAST, rotvars=fs.rotvars)
+    assert ds.status(fs) == _native.TAM_EINVAL
+    assert ds.status(fs) == 0
