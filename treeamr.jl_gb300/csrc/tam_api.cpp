@@ -368,8 +368,7 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
         if (tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
         for (int i0 = 0; i0 < box; i0 += ti)
-          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0),
-                           s->h_tb[e.transfer] - 1, s->h_sb[e.transfer] - 1});
+          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
       }
       if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
       if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;

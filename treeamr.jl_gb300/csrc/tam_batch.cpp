@@ -30,7 +30,7 @@ struct tam_batch {
   bool needs_factors = false;
   bool needs_rotvars = false, has_bounded = false;
   std::vector<tam::DevGroup> groups;
-  std::vector<int32_t> h_tb, h_sb;
+  std::vector<int32_t> h_tb;
   std::vector<tam::Stage> stages;
   tam::LaunchShape shape;
   tam::DevGroup *d_groups = nullptr;
@@ -139,8 +139,7 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b) {
         if (tam::tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
         for (int i0 = 0; i0 < box; i0 += ti)
-          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0),
-                           b->h_tb[e.transfer] - 1, b->h_sb[e.transfer] - 1});
+          tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
       }
       if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
       if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;
@@ -288,7 +287,6 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     b->stages.push_back(st);
   }
   b->h_tb = tb;
-  b->h_sb = sb;
   std::vector<tam::Tile> tiles = batch_tiles(b);
   std::vector<tam::PTile> ptiles = tam::pack_stages(b->stages, tiles, b->shape.tile_items);
   cudaError_t e;

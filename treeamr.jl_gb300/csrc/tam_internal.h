@@ -91,8 +91,6 @@ struct Tile {
   int32_t transfer;
   int32_t item0;
   int32_t nitems;
-  int32_t tblock;  // the transfer's target and source blocks, 0-based: carried here
-  int32_t sblock;  // so that a warp reads them with its tile, not from the block lists
 };
 
 // What a warp of the fused kernels takes: up to 32 consecutive tiles

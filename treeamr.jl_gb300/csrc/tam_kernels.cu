@@ -583,13 +583,12 @@ struct TileLayout {
 // warp: the rounds loop to the tile's size, uniform across lanes.
 struct SegPoint {
   int group, transfer, item;
-  int tblock, sblock;
   bool on;
 };
 
 __device__ __forceinline__ void load_segments(const Tile *__restrict__ tiles, const PTile &pt,
                                               int lane, Tile &seg, int &pref) {
-  seg = Tile{0, 0, 0, 0, 0, 0};
+  seg = Tile{0, 0, 0, 0};
   if (lane < pt.nseg) seg = tiles[pt.seg0 + lane];
   int incl = seg.nitems;
 #pragma unroll
@@ -607,8 +606,6 @@ __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int ns
   SegPoint p;
   p.group = __shfl_sync(0xffffffffu, seg.group, mine);
   p.transfer = __shfl_sync(0xffffffffu, seg.transfer, mine);
-  p.tblock = __shfl_sync(0xffffffffu, seg.tblock, mine);
-  p.sblock = __shfl_sync(0xffffffffu, seg.sblock, mine);
   p.item = __shfl_sync(0xffffffffu, seg.item0, mine) + k - __shfl_sync(0xffffffffu, pref, mine);
   p.on = true;
   return p;
@@ -651,8 +648,8 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
         on[p] = k < pt.nitems;
         const DevGroup &g = a.groups[q.group];
         const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-        const int64_t tblock = q.tblock;
-        const int64_t sblock = q.sblock;
+        const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+        const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
         int i1, i2, i3;
         box_point(g, q.item, i1, i2, i3);
         o[p] = g.affine ? copy_geometry<D>(g, i1, i2, i3, tblock, sblock, nvars, L.S1, L.S2, L.S3)
@@ -693,8 +690,8 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
       if (k >= pt.nitems) continue;
       const DevGroup &g = a.groups[q.group];
       const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-      const int64_t tblock = q.tblock;
-      const int64_t sblock = q.sblock;
+      const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+      const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
       const int item = g.perm >= 0 ? __ldg(a.perm + g.perm + q.item) : q.item;
       int i1, i2, i3;
       box_point(g, item, i1, i2, i3);
