@@ -1,18 +1,25 @@
-"""Ghost-fill benchmark: GB/s of the fused fill on the sphere mesh, one GB300.
+"""Ghost-fill benchmark: GB/s of the batched fused fill on the walls mesh, one GB300.
 
-Workload (the default): 3-D, 8^3 periodic roots, N = 16, G = 3, cell-centred,
-4 Float64 variables, point-value operators of order 4, three levels nested
-around the sphere |x - 1/2| = 0.25 (14,736 blocks, 5.0 GB of field data).
-A step is one whole ghost fill.  ``value`` counts the reference's algorithmic
-bytes (one read plus one write per ghost point-variable written,
-``bench/copies.jl:17-21``) per second with the field data resident in HBM;
-``e2e`` is the same through ``fill_ghosts`` with the field data copied from
-pinned host memory and back every step.  The field data (5 GB) are far larger
-than L2 (129 MB), so no flush is needed between steps.
+Workload (the default): the walls mesh, 3-D vertex-centred, 8^3 roots over
+the unit cube, N = 32, G = 2, low faces reflecting and high faces outflow,
+five levels nested around two seeded points, 8 Float64 variables (5 even, a
+vector's 3 components odd in their own dimension), point-value operators of
+order 4 (2,374 blocks, 7.7 GB of field data), filled with its stated data
+(Gaussian bumps of width 0.05 plus seeded uniform noise in [-1, 1]).  A step
+is one whole ghost fill, stages P and 0 included.  ``value`` counts the
+reference's algorithmic bytes (one read plus one write per ghost
+point-variable written, ``bench/copies.jl:17-21``) per second with the field
+data resident in HBM; ``e2e`` is the same through the C ABI with the field
+data copied from pinned host memory and back every step.  The field data are
+far larger than L2 (129 MB), so no flush is needed between steps.  The
+sphere mesh, the adjoint's mesh, the walls mesh in the other element type,
+the batch of 64 forests and the other parts of the path are measured in the
+same line under ``workloads``.
 
 ``--impl reference`` times the CPU restatement of the reference's threaded
-fill (the oracle, ``oracle/fill_oracle.c``) on this machine's host cores:
-the reference itself is Julia, which this machine does not have.
+fill (the oracle, ``oracle/fill_oracle.c``) on this machine's host cores, on
+the same mesh and data: the reference itself is Julia, which this machine
+does not have.
 
 Launch: ``python bench.py [--gpus N] [--steps K] [--warmup W]``; N > 1 under
 torchrun runs N independent replicas (the path does not shard on one GPU machine).
@@ -59,10 +66,11 @@ def parse():
     ap.add_argument("--options", default=None,
                     help="fixed launch options instead of the autotuner's, e.g. "
                          "tile_items=64,threads=128,int_mul=1")
-    ap.add_argument("--workload", choices=["sphere", "walls"], default="sphere",
-                    help="walls: time only the walls mesh (for profiling)")
-    ap.add_argument("--dtype", choices=["float32", "float64"], default="float32",
-                    help="element type of --workload walls")
+    ap.add_argument("--workload", choices=["sphere", "walls"], default="walls",
+                    help="walls: the headline line (the walls mesh); sphere: time only the "
+                         "sphere mesh and print its entry")
+    ap.add_argument("--dtype", choices=["float32", "float64"], default="float64",
+                    help="element type of the walls mesh")
     ap.add_argument("--sector-minimum", type=int, default=None, metavar="TAG",
                     help="with --workload walls: count, on the CPU, the 32-byte sectors the "
                          "unit copies of stage TAG read and write, print them and exit")
@@ -219,8 +227,7 @@ def measure_walls(T, dev, timed, args, peak):
     from treeamr.ghosts import device_schedule
     f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots)
     sched = GhostSchedule(fs, ops)
-    g = torch.Generator(device=dev).manual_seed(7)
-    fs.work.uniform_(-1.0, 1.0, generator=g)
+    meshes.config_fill(fs, "walls", seed=3)
     esize = np.dtype(T).itemsize
     bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * esize
     if args.options:
@@ -231,16 +238,15 @@ def measure_walls(T, dev, timed, args, peak):
         tuned = ds0.options()
     else:
         tuned = autotune(fs, sched)
+        meshes.config_fill(fs, "walls", seed=3)
     for _ in range(args.warmup):
         fill_ghosts(fs, sched)
     steps = max(3, args.steps // 2)
     ms = timed(lambda: fill_ghosts(fs, sched), steps)
-    # the fill's deviation from a float64 evaluation of the same stencils
-    err = None
-    if T == np.float32:
-        filled = fs.work.cpu().numpy()
-        err = fill_error(sched, filled, filled, fs.nvars, fs.factors_host)
-        del filled
+    # the fill's deviation from a wider evaluation of the same stencils
+    filled = fs.work.cpu().numpy()
+    err = fill_error(sched, filled, filled, fs.nvars, fs.factors_host)
+    del filled
     fill_ghosts(fs, sched, method="plain")
     ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(2, steps // 2))
     # unify! of the set (stages P and 0 alone: every secondary copy of a
@@ -273,6 +279,8 @@ def measure_walls(T, dev, timed, args, peak):
     out = {
         "workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
                     "faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd), PV(4,4)",
+        "data": "Gaussian bumps of width 0.05 at the 2 seeded refinement centres + seeded "
+                "U[-1,1]",
         "dtype": np.dtype(T).name, "blocks": f.nleaves(), "groups": len(sched.groups),
         "field_bytes": fs.work.numel() * esize,
         "value": bytes_per_fill / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
@@ -335,9 +343,8 @@ def measure_pv6(dev, timed, args):
     f, fs, ops = meshes.sphere_setup(device=dev, nvars=args.nvars, roots=args.roots,
                                      levels=args.levels, p=6)
     sched = GhostSchedule(fs, ops)
-    g = torch.Generator(device=dev).manual_seed(11)
-    fs.work.uniform_(-1.0, 1.0, generator=g)
     tuned = autotune(fs, sched)
+    meshes.config_fill(fs, "sphere", seed=11)
     bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * 8
     fill_ghosts(fs, sched)
     steps = max(3, args.steps // 2)
@@ -398,20 +405,6 @@ def measure_regrid(dev, timed, args):
     del a, b, t
     torch.cuda.empty_cache()
     return out
-
-
-def workload_config(args, f, sched):
-    return {
-        "workload": "sphere: 3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, PV(4,4), "
-                    "3 levels nested around |x-1/2|=0.25" if (args.roots, args.levels, args.nvars) == (8, 3, 4)
-                    else f"sphere: {args.roots}^3 roots, {args.levels} levels, {args.nvars} vars",
-        "blocks": f.nleaves(),
-        "groups": len(sched.groups),
-        "ghost_points_per_var": int(sched.ghost_items(1)),
-        "nvars": args.nvars,
-        "field_bytes": None,
-        "l2": "inputs larger than L2 (5 GB field data vs 129 MB L2); no flush",
-    }
 
 
 class ClockSampler:
@@ -646,6 +639,160 @@ def cpu_fill_rate(sched, fs_host_work, nvars, factors, bytes_per_fill, budget_s=
     return bytes_per_fill / best / 1e9, best, len(times), threads
 
 
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def stage_times(ds, fs, sched, stream, dev, reps):
+    """Per stage tag, the fused launches' times (CUDA events on the launching
+    stream, ``reps`` fills' worth), and the algorithmic bytes of the stage."""
+    import torch
+    tags = sorted({gr.stage for gr in sched.groups})
+    esize = fs.T.itemsize
+    stage_bytes = {tag: 2 * esize * fs.nvars * sum(int(np.prod(gr.boxsize())) * gr.ntransfers()
+                                                  for gr in sched.groups if gr.stage == tag)
+                   for tag in tags}
+    evs = []
+    torch.cuda.synchronize(dev)
+    for _ in range(reps):
+        for tag in tags:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ds.run(fs, tag, tag, "fused")
+            b.record(stream)
+            evs.append((tag, a, b))
+    torch.cuda.synchronize(dev)
+    stage_ms = {}
+    for tag, a, b in evs:
+        stage_ms.setdefault(tag, []).append(a.elapsed_time(b))
+    return stage_ms, stage_bytes
+
+
+def measure_sphere(dev, timed, args, peak, world):
+    """The sphere mesh with its stated data: 3-D, 8^3 periodic roots, N=16,
+    G=3, cell-centred, 4 Float64 variables, PV(4,4), three levels around
+    |x - 1/2| = 0.25, filled with sin(2 pi x) sin(2 pi y) sin(2 pi z) plus
+    seeded noise of 1e-3.  Fused (autotuned) and plain fills, the per-stage
+    HBM and FP64 rooflines, the fill's stated error, and the state vector's
+    copies (scatter!/gather!) on the same mesh."""
+    import torch
+    from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+    from treeamr.autotune import autotune
+    from treeamr.ghosts import device_schedule
+    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
+    fs = FieldSet(f, 4, G=3, T=np.float64, device=dev)
+    meshes.config_fill(fs, "sphere", seed=1)
+    sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    nvars = fs.nvars
+    bytes_per_fill = 2 * sched.ghost_items(nvars) * 8
+    tuned = autotune(fs, sched)
+    for _ in range(args.warmup):
+        fill_ghosts(fs, sched)
+    steps = max(3, args.steps // 2)
+    ms = timed(lambda: fill_ghosts(fs, sched), steps)
+    filled = fs.work.cpu().numpy()
+    error = fill_error(sched, filled, filled, nvars, fs.factors_host)
+    del filled
+    fill_ghosts(fs, sched, method="plain")
+    ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(3, steps // 2))
+    ds = device_schedule(sched, dev.index)
+    stream = torch.cuda.current_stream(dev)
+    stage_ms, stage_bytes = stage_times(ds, fs, sched, stream, dev, 3)
+    kern_ms = sum(statistics.mean(v) for v in stage_ms.values())
+    achieved = sum(stage_bytes.values()) / (kern_ms * 1e-3) / 1e9
+    fp64 = fp64_roofline(stencil_flops(sched, nvars), stage_ms, args.fp64_peak) \
+        if args.fp64_peak else None
+    # the state vector's copies and one right-hand side's scatter + fill
+    from treeamr.state import gather, scatter, scatter_fill, statevector
+    u = statevector(fs)
+    gather(u, fs)
+    state_bytes = 2 * u.numel() * u.element_size()
+    ms_scatter = timed(lambda: scatter(fs, u), steps)
+    ms_gather = timed(lambda: gather(u, fs), steps)
+    ms_sf = timed(lambda: scatter_fill(fs, sched, u), steps)
+    state = {"entries": u.numel(), "bytes_per_copy": state_bytes,
+             "scatter_ms": ms_scatter, "gather_ms": ms_gather,
+             "scatter_gbs": state_bytes / (ms_scatter * 1e-3) / 1e9,
+             "gather_gbs": state_bytes / (ms_gather * 1e-3) / 1e9,
+             "scatter_frac_of_hbm": state_bytes / (ms_scatter * 1e-3) / 1e9 / peak,
+             "scatter_fill_ms": ms_sf}
+    del u
+    wr, rd = footprint_points(sched)
+    out = {
+        "workload": "sphere: 3-D 8^3 periodic roots, N=16, G=3, cell, 4 vars F64, PV(4,4), "
+                    "3 levels nested around |x-1/2|=0.25",
+        "data": "sin(2 pi x) sin(2 pi y) sin(2 pi z) + seeded 1e-3 U[-1,1]",
+        "dtype": "float64", "blocks": f.nleaves(), "groups": len(sched.groups),
+        "field_bytes": fs.work.numel() * 8,
+        "value": world * bytes_per_fill / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
+        "plain": {"value": world * bytes_per_fill / (ms_plain * 1e-3) / 1e9,
+                  "ms_per_step": ms_plain, "speedup_fused_vs_plain": ms_plain / ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
+                     "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
+        "fp64": fp64,
+        "error": error,
+        "footprint": {"written_points": wr, "read_points": rd,
+                      "bytes": (wr + rd) * nvars * 8},
+        "ghost_points_per_s": sched.ghost_items(1) / (ms * 1e-3),
+        "state": state,
+        "tuned": tuned,
+        "gpu_launches_per_fill": fused_launches(sched),
+    }
+    del fs, sched, ds
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_adjoint_sphere(dev, timed, args):
+    """The adjoint's workload: the sphere mesh with 2 Float64 variables.  The
+    transposed fill's time against the forward fill's on the same field set,
+    and the dot-product test <A x, y> = <x, A^T y> with seeded uniform x, y
+    (each inner product summed in float64 chunks, the chunks summed exactly)."""
+    import math
+    import torch
+    from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+    from treeamr.adjoint import fill_ghosts_adjoint
+    from treeamr.autotune import autotune
+    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
+    fs = FieldSet(f, 2, G=3, T=np.float64, device=dev)
+    sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    g = torch.Generator(device=dev).manual_seed(21)
+    x = torch.empty_like(fs.work).uniform_(-1.0, 1.0, generator=g)
+    y = torch.empty_like(fs.work).uniform_(-1.0, 1.0, generator=g)
+    fs.work.copy_(x)
+    autotune(fs, sched)
+    fs.work.copy_(x)
+    fill_ghosts(fs, sched)
+    aty = y.clone()
+    fill_ghosts_adjoint(fs, sched, aty)                    # prepares the transpose
+
+    def dot(a, b):
+        a, b = a.reshape(-1), b.reshape(-1)
+        step = 1 << 22
+        return math.fsum(float(torch.dot(a[i:i + step], b[i:i + step]))
+                         for i in range(0, a.numel(), step))
+    lhs, rhs = dot(fs.work, y), dot(x, aty)
+    steps = max(3, args.steps // 2)
+    work = fs.work.clone()
+    ms_fwd = timed(lambda: fill_ghosts(fs, sched), steps)
+    ms_adj = timed(lambda: fill_ghosts_adjoint(fs, sched, work), steps)
+    bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * 8
+    out = {"workload": "sphere (8^3 periodic roots, N=16, G=3, 3 levels), 2 vars F64, PV(4,4)",
+           "forward_ms": ms_fwd, "adjoint_ms": ms_adj, "time_vs_forward": ms_adj / ms_fwd,
+           "value": bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
+           "dot_test": {"lhs": lhs, "rhs": rhs,
+                        "relative_residual": abs(lhs - rhs) / max(abs(lhs), abs(rhs)),
+                        "bound": 1e-13}}
+    del fs, sched, x, y, aty, work
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -658,8 +805,6 @@ def main():
         return run_reference(args)
 
     if args.sector_minimum is not None:
-        if args.workload != "walls":
-            raise SystemExit("--sector-minimum counts the walls mesh: give --workload walls")
         from treeamr import GhostSchedule, meshes
         T = np.dtype(args.dtype).type
         f, fs, ops = meshes.walls_setup(T=T, roots=args.roots)
@@ -677,45 +822,12 @@ def main():
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
 
-    from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+    from treeamr import GhostSchedule, fill_ghosts, meshes
     from treeamr.ghosts import device_schedule
-    from treeamr import _native
 
-    if args.workload == "walls":
-        stream = torch.cuda.current_stream(dev)
-
-        def timed_walls(fn, steps):
-            torch.cuda.synchronize(dev)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            for _ in range(steps):
-                fn()
-            b.record(stream)
-            torch.cuda.synchronize(dev)
-            return a.elapsed_time(b) / steps
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
-        out = measure_walls(np.dtype(args.dtype).type, dev, timed_walls, args,
-                            float(peaks.get("hbm_gbs", 6800.0)))
-        print(json.dumps(out), flush=True)
-        return 0
-
-    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
-    fs = FieldSet(f, args.nvars, G=3, T=np.float64, device=dev)
-    ops = Operators(prolongation=4, restriction=4)
-    sched = GhostSchedule(fs, ops)
-    g = torch.Generator(device=dev).manual_seed(1 + rank)
-    fs.work.uniform_(-1.0, 1.0, generator=g)
-    cfg = workload_config(args, f, sched)
-    field_bytes = fs.work.numel() * fs.work.element_size()
-    cfg["field_bytes"] = field_bytes
-    nvars = args.nvars
-    points = sched.ghost_items(nvars)
-    bytes_per_fill = 2 * points * 8                     # one read + one write per point-variable
-    ds = device_schedule(sched, dev.index)
+    peaks = load_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     stream = torch.cuda.current_stream(dev)
 
     def barrier():
@@ -735,8 +847,33 @@ def main():
         barrier()
         return max_over_ranks(a.elapsed_time(b), world, dev) / steps
 
+    if args.workload == "sphere":
+        args.fp64_peak = None
+        print(json.dumps(measure_sphere(dev, timed, args, peak, world)), flush=True)
+        return 0
+
+    # ---- the headline: the walls mesh (vertex-centred, reflecting low and
+    # outflow high faces, stages P and 0), its stated data
+    T = np.dtype(args.dtype).type
+    esize = np.dtype(T).itemsize
+    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots)
+    meshes.config_fill(fs, "walls", seed=3 + rank)
+    sched = GhostSchedule(fs, ops)
+    nvars = fs.nvars
+    points = sched.ghost_items(nvars)
+    bytes_per_fill = 2 * points * esize                # one read + one write per point-variable
+    field_bytes = fs.work.numel() * esize
+    ds = device_schedule(sched, dev.index)
+    cfg = {"workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
+                       f"faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd) "
+                       f"{'F64' if esize == 8 else 'F32'}, PV(4,4)"
+           if args.roots == 8 else f"walls: {args.roots}^3 roots",
+           "blocks": f.nleaves(), "groups": len(sched.groups),
+           "ghost_points_per_var": int(sched.ghost_items(1)), "nvars": nvars,
+           "field_bytes": field_bytes,
+           "l2": f"inputs larger than L2 ({field_bytes / 1e9:.1f} GB field data vs 129 MB L2); "
+                 "no flush"}
     method = args.method
-    tuned = None
     if method == "fused" and args.options:
         for kv in args.options.split(","):
             k, v = kv.split("=")
@@ -744,193 +881,66 @@ def main():
         cfg["options"] = ds.options()
     elif method == "fused":
         from treeamr.autotune import autotune
-        tuned = autotune(fs, sched)
-        cfg["tuned"] = tuned
+        cfg["tuned"] = autotune(fs, sched)
+        meshes.config_fill(fs, "walls", seed=3 + rank)
     for _ in range(args.warmup):
         fill_ghosts(fs, sched, method=method)
     with ClockSampler(dev.index) as clk:
         ms = timed(lambda: fill_ghosts(fs, sched, method=method), args.steps)
     clocks = clk.summary()
     value = world * bytes_per_fill / (ms * 1e-3) / 1e9
-    # the fill's deviation from a double-double evaluation of the same
-    # stencils on the same data (a sample of every group's transfers)
     filled = fs.work.cpu().numpy() if rank == 0 else None
     error = fill_error(sched, filled, filled, nvars, fs.factors_host) if rank == 0 else None
     del filled
 
     # the plain one-launch-per-group fill on the same data
-    for _ in range(max(1, args.warmup // 2)):
-        fill_ghosts(fs, sched, method="plain")
+    fill_ghosts(fs, sched, method="plain")
     ms_plain = timed(lambda: fill_ghosts(fs, sched, method="plain"), max(3, args.steps // 2))
-    plain_value = world * bytes_per_fill / (ms_plain * 1e-3) / 1e9
 
-    # the adjoint fill (transpose, gather form) on the same mesh
+    # the adjoint of the same fill
     from treeamr.adjoint import fill_ghosts_adjoint
     yadj = fs.work.clone()
-    fill_ghosts_adjoint(fs, sched, yadj)                  # prepares the transpose, scratch
+    fill_ghosts_adjoint(fs, sched, yadj)
     ms_adj = timed(lambda: fill_ghosts_adjoint(fs, sched, yadj), max(3, args.steps // 2))
-    adjoint = {"value": world * bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
-               "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms}
     del yadj
 
-    # the state vector's copies (scatter!/gather!) and one right-hand side's
-    # scatter + fill, on the same mesh
-    from treeamr.state import gather, scatter, scatter_fill, statelength, statevector
-    u = statevector(fs)
-    gather(u, fs)
-    state_bytes = 2 * u.numel() * u.element_size()         # one read + one write per entry
-    ms_scatter = timed(lambda: scatter(fs, u), max(3, args.steps // 2))
-    ms_gather = timed(lambda: gather(u, fs), max(3, args.steps // 2))
-    ms_sf = timed(lambda: scatter_fill(fs, sched, u), max(3, args.steps // 2))
-    peaks0 = {}
-    try:
-        peaks0 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = float(peaks0.get("hbm_gbs", 6800.0))
-    state = {"entries": u.numel(), "bytes_per_copy": state_bytes,
-             "scatter_ms": ms_scatter, "gather_ms": ms_gather,
-             "scatter_gbs": state_bytes / (ms_scatter * 1e-3) / 1e9,
-             "gather_gbs": state_bytes / (ms_gather * 1e-3) / 1e9,
-             "scatter_frac_of_hbm": state_bytes / (ms_scatter * 1e-3) / 1e9 / hbm,
-             "scatter_fill_ms": ms_sf}
-    del u
-
-    # per-stage launches of the fused kernel, CUDA events on the launching stream
-    stage_ms = {}
-    stage_bytes = {}
-    tags = sorted({gr.stage for gr in sched.groups})
-    for tag in tags:
-        stage_bytes[tag] = 2 * 8 * nvars * sum(int(np.prod(gr.boxsize())) * gr.ntransfers()
-                                               for gr in sched.groups if gr.stage == tag)
-    reps = max(3, args.steps // 2)
-    evs = []
-    torch.cuda.synchronize(dev)
-    for _ in range(reps):
-        for tag in tags:
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ds.run(fs, tag, tag, "fused")
-            b.record(stream)
-            evs.append((tag, a, b))
-    torch.cuda.synchronize(dev)
-    for tag, a, b in evs:
-        stage_ms.setdefault(tag, []).append(a.elapsed_time(b))
+    stage_ms, stage_bytes = stage_times(ds, fs, sched, stream, dev, max(3, args.steps // 2))
     kern_ms = sum(statistics.mean(v) for v in stage_ms.values())
     achieved = sum(stage_bytes.values()) / (kern_ms * 1e-3) / 1e9
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    args.fp64_peak = None if args.no_fp64_peak else fp64_peak_tflops(dev)
+    args.fp64_peak = None if (args.no_fp64_peak or esize != 8) else fp64_peak_tflops(dev)
     fp64 = fp64_roofline(stencil_flops(sched, nvars), stage_ms, args.fp64_peak) \
         if args.fp64_peak else None
-
     traffic = None
     try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "fused_stage_traffic.json")))
-        traffic = prof.get("traffic_bytes_per_fill")
+        prof = json.load(open(os.path.join(ROOT, "profiles", "walls_fill_traffic.json")))
+        traffic = prof.get("traffic_bytes_per_fill_" + np.dtype(T).name)
     except Exception:
         pass
 
-    # the walls mesh (vertex-centred, reflecting/outflow, stages 0 and P), F32 and F64
-    walls = {}
-    if not args.no_walls:
-        for T in (np.float32, np.float64):
-            walls["walls_" + np.dtype(T).name] = measure_walls(T, dev, timed, args, peak)
-        walls["batch64_float32"] = measure_batch(dev, timed, args, peak)
-        walls["boundary_hook"] = measure_hook(dev, timed, args)
-        walls["regrid"] = measure_regrid(dev, timed, args)
-        walls["sphere_pv6"] = measure_pv6(dev, timed, args)
-
-    # end to end through the public call, host buffers, copies inside the timing
+    # end to end through the C ABI from page-locked host buffers
     e2e = None
     if not args.no_e2e:
-        from treeamr.host import HostPipeline
-        host_in = torch.empty_like(fs.work, device="cpu").pin_memory()
-        host_in.copy_(fs.work)
-        host_out = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
-        # one step in isolation: upload, fill, download on one stream
-        pipe1 = HostPipeline(fs, sched, depth=1)
-        pipe1.submit(host_in, host_out[0])
-        pipe1.synchronize()
-        ms_single = timed(lambda: (pipe1.submit(host_in, host_out[0]), pipe1.join(stream)), 3)
-        del pipe1
-        torch.cuda.empty_cache()
-        # steps in flight together: each state's upload, fill and download on
-        # its own stream and device buffer, three states at a time; the
-        # upload moves what the fill reads, the own points, when the
-        # schedule writes every other point (tam_fill_host_own)
-        own = not sched.boundaries
-        e2e_steps = max(6, min(args.steps, 12))
+        e2e = measure_e2e(fs, sched, timed, stream, args, world, bytes_per_fill, field_bytes)
 
-        def e2e_pipeline(pipe):
-            def run(n):
-                pipe.wait_on(stream)             # after the timing's start event
-                for i in range(n):
-                    pipe.submit(host_in, host_out[i % 2])
-                pipe.join(stream)                # before its end event
-            run(3)
-            return timed(lambda: run(e2e_steps), 1) / e2e_steps
-        pipe = HostPipeline(fs, sched, depth=3)
-        ms_full = e2e_pipeline(pipe)
-        del pipe
-        ms_e2e, h2d = ms_full, field_bytes
-        if own:
-            pipe = HostPipeline(fs, sched, depth=3, own=True)
-            ms_e2e, h2d = e2e_pipeline(pipe), pipe.own_bytes()
-            del pipe
-        e2e = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
-               "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": field_bytes, "steps": e2e_steps,
-               "api": ("tam_fill_host_own (C ABI, page-locked host buffers: the own points "
-                       "up, read by a kernel, the filled array down)" if own else
-                       "tam_fill_host (C ABI, host buffers)") +
-                      " through treeamr.host.HostPipeline, 3 streams and device buffers",
-               "full_upload_ms_per_step": ms_full,
-               "single_step_ms": ms_single}
+    # the other workloads, each on its own mesh
+    host_data = fs.work.cpu().numpy() if (not args.no_cpu and rank == 0) else None
+    factors_host = fs.factors_host
+    workloads = {}
+    if not args.no_walls:
+        del fs
         torch.cuda.empty_cache()
-        # the host link's own rate, the e2e step's floor: an upload and a
-        # download of the field data at once, on two streams (copy engines)
-        dbuf = torch.empty_like(fs.work)
-        s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
-
-        def link(up=True, down=True):
-            s_up.wait_stream(stream)
-            s_down.wait_stream(stream)
-            if up:
-                with torch.cuda.stream(s_up):
-                    dbuf.copy_(host_in, non_blocking=True)
-            if down:
-                with torch.cuda.stream(s_down):
-                    host_out[0].copy_(fs.work, non_blocking=True)
-            stream.wait_stream(s_up)
-            stream.wait_stream(s_down)
-        link()
-        ms_up = timed(lambda: link(down=False), 3)
-        ms_down = timed(lambda: link(up=False), 3)
-        ms_both = timed(link, 3)
-        gb = field_bytes / 1e9
-        # a full-upload step moves the field data up and down: its floor is
-        # the two copies one after the other, or together where the link
-        # carries both at once
-        floor = min(ms_up + ms_down, ms_both)
-        e2e["host_link"] = {"h2d_gbs": gb / (ms_up * 1e-3), "d2h_gbs": gb / (ms_down * 1e-3),
-                            "both_each_way_gbs": gb / (ms_both * 1e-3),
-                            "serial_floor_ms": ms_up + ms_down,
-                            "concurrent_floor_ms": ms_both,
-                            "floor_ms_per_step": floor,
-                            "frac": floor / ms_full}
-        del dbuf, host_in, host_out
-        torch.cuda.empty_cache()
+        workloads["sphere_float64"] = measure_sphere(dev, timed, args, peak, world)
+        workloads["adjoint_sphere_2vars"] = measure_adjoint_sphere(dev, timed, args)
+        other = np.float32 if esize == 8 else np.float64
+        workloads["walls_" + np.dtype(other).name] = measure_walls(other, dev, timed, args, peak)
+        workloads["batch64_float32"] = measure_batch(dev, timed, args, peak)
+        workloads["boundary_hook"] = measure_hook(dev, timed, args)
+        workloads["regrid"] = measure_regrid(dev, timed, args)
+        workloads["sphere_pv6"] = measure_pv6(dev, timed, args)
 
     cpu = None
-    if not args.no_cpu and rank == 0:
-        host = fs.work.cpu().numpy().copy()
-        gbs, best, runs, threads = cpu_fill_rate(sched, host, nvars, fs.factors_host,
+    if host_data is not None:
+        gbs, best, runs, threads = cpu_fill_rate(sched, host_data, nvars, factors_host,
                                                  bytes_per_fill)
         cpu = {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"whole fills of the same mesh and data, best of {runs} after one "
@@ -938,11 +948,8 @@ def main():
                          f"{threads} OpenMP threads"}
 
     if rank == 0:
-        # ghost points a second, and the unique footprint: every point written
-        # once and every distinct point read once (secondary to the
-        # algorithmic bytes, which count a read and a write per ghost)
         wr, rd = footprint_points(sched)
-        fp_bytes = (wr + rd) * nvars * 8
+        fp_bytes = (wr + rd) * nvars * esize
         throughput = {
             "ghost_points_per_s": world * sched.ghost_items(1) / (ms * 1e-3),
             "ghost_point_variables_per_s": world * points / (ms * 1e-3),
@@ -953,19 +960,27 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded uniform [-1,1] field data on the sphere mesh)",
+            "dtype": "f64" if esize == 8 else "f32",
+            "data": "synthetic: the walls mesh's stated data (Gaussian bumps of width 0.05 at "
+                    "the 2 seeded refinement centres + seeded U[-1,1])",
             "config": dict(cfg, method=method, parallelism=f"replicas{world}"),
-            "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
-                      "speedup_fused_vs_plain": ms_plain / ms},
-            "adjoint": adjoint,
+            "plain": {"value": world * bytes_per_fill / (ms_plain * 1e-3) / 1e9, "unit": UNIT,
+                      "ms_per_step": ms_plain, "speedup_fused_vs_plain": ms_plain / ms},
+            "adjoint": {"value": world * bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
+                        "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms},
             "throughput": throughput,
             "error": error,
-            "state": state,
-            "workloads": walls,
+            "workloads": workloads,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                           "of every launch of one fill, captured on the walls "
+                                           "mesh at 4^3 roots and scaled by the algorithmic "
+                                           "bytes (profiles/walls_fill_traffic.json)"
+                         if traffic else None,
                          "peak_source": peak_src,
-                         "kernel": "fused_stage_kernel",
+                         "scope": "the whole fill: algorithmic bytes over the sum of the "
+                                  "stages' fused launches (CUDA events)",
                          "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
                          "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
             "fp64": fp64,
@@ -973,7 +988,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": args.steps * fused_launches(sched) if method == "fused" else
-            args.steps * ds.ngroups,
+            args.steps * len(sched.groups),
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -981,34 +996,135 @@ def main():
     return 0
 
 
-def run_reference(args):
-    """The CPU restatement of the reference's threaded fill on the host cores."""
+def measure_e2e(fs, sched, timed, stream, args, world, bytes_per_fill, field_bytes):
+    """The fill of a host-resident field through the C ABI from page-locked
+    host buffers, copies inside the timed region.
+
+    - ``value``: three independent fills in flight (``HostPipeline``, each
+      step's upload, fill and download on its own stream and device buffer),
+      the own points uploaded (``tam_fill_host_own``).
+    - ``dependent``: what a solver gets, each step's input the previous
+      step's output, upload, fill and download on one stream, one after the
+      other (``tam_fill_host_own``).
+    - ``full_upload_ms_per_step``: the pipelined steps uploading the whole
+      array (``tam_fill_host``)."""
     import torch
-    from treeamr import FieldSet, GhostSchedule, Operators, meshes
+    from treeamr.host import HostPipeline
+    host_in = torch.empty_like(fs.work, device="cpu").pin_memory()
+    host_in.copy_(fs.work)
+    host_out = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
+    own = not sched.boundaries
+    e2e_steps = max(6, min(args.steps, 12))
+
+    def e2e_pipeline(pipe):
+        def run(n):
+            pipe.wait_on(stream)
+            for i in range(n):
+                pipe.submit(host_in, host_out[i % 2])
+            pipe.join(stream)
+        run(3)
+        return timed(lambda: run(e2e_steps), 1) / e2e_steps
+    pipe = HostPipeline(fs, sched, depth=3)
+    ms_full = e2e_pipeline(pipe)
+    del pipe
+    ms_e2e, h2d = ms_full, field_bytes
+    if own:
+        pipe = HostPipeline(fs, sched, depth=3, own=True)
+        ms_e2e, h2d = e2e_pipeline(pipe), pipe.own_bytes()
+        del pipe
+    # dependent steps: the output of one is the input of the next
+    pipe1 = HostPipeline(fs, sched, depth=1, own=own)
+    a, b = host_out
+
+    def chain(n):
+        pipe1.wait_on(stream)
+        src, dst = host_in, a
+        for _ in range(n):
+            pipe1.submit(src, dst)
+            src, dst = dst, (b if dst is a else a)
+        pipe1.join(stream)
+    chain(2)
+    dep_steps = 4
+    ms_dep = timed(lambda: chain(dep_steps), 1) / dep_steps
+    h2d_dep = pipe1.own_bytes() if own else field_bytes
+    del pipe1
+    out = {"value": world * bytes_per_fill / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+           "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": field_bytes, "steps": e2e_steps,
+           "api": ("tam_fill_host_own (C ABI, page-locked host buffers: the own points up, "
+                   "read by a kernel, the filled array down)" if own else
+                   "tam_fill_host (C ABI, host buffers)") +
+                  " through treeamr.host.HostPipeline, 3 independent steps in flight",
+           "full_upload_ms_per_step": ms_full,
+           "dependent": {"value": world * bytes_per_fill / (ms_dep * 1e-3) / 1e9, "unit": UNIT,
+                         "ms_per_step": ms_dep, "steps": dep_steps,
+                         "h2d_bytes_per_step": h2d_dep, "d2h_bytes_per_step": field_bytes,
+                         "what": "each step's input is the previous step's output: upload, "
+                                 "fill and download one after the other on one stream, what "
+                                 "a time-stepping solver holding its state on the host gets"}}
+    torch.cuda.empty_cache()
+    # the host link's own rate
+    dbuf = torch.empty_like(fs.work)
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def link(up=True, down=True):
+        s_up.wait_stream(stream)
+        s_down.wait_stream(stream)
+        if up:
+            with torch.cuda.stream(s_up):
+                dbuf.copy_(host_in, non_blocking=True)
+        if down:
+            with torch.cuda.stream(s_down):
+                host_out[0].copy_(fs.work, non_blocking=True)
+        stream.wait_stream(s_up)
+        stream.wait_stream(s_down)
+    link()
+    ms_up = timed(lambda: link(down=False), 3)
+    ms_down = timed(lambda: link(up=False), 3)
+    ms_both = timed(link, 3)
+    gb = field_bytes / 1e9
+    floor = min(ms_up + ms_down, ms_both)
+    out["host_link"] = {"h2d_gbs": gb / (ms_up * 1e-3), "d2h_gbs": gb / (ms_down * 1e-3),
+                        "both_each_way_gbs": gb / (ms_both * 1e-3),
+                        "serial_floor_ms": ms_up + ms_down, "concurrent_floor_ms": ms_both,
+                        "floor_ms_per_step": floor, "frac": floor / ms_full}
+    del dbuf, host_in, host_out
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_reference(args):
+    """The CPU restatement of the reference's threaded fill (the oracle) on
+    every host core, on the headline's walls mesh and data."""
+    from treeamr import GhostSchedule, meshes
     import oracle
-    f = meshes.sphere_forest(roots=args.roots, N=16, levels=args.levels)
-    fs = FieldSet(f, args.nvars, G=3, T=np.float64, device="cpu")
-    meshes.random_fill(fs, seed=1)
-    sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
-    cfg = workload_config(args, f, sched)
-    cfg["field_bytes"] = fs.work.numel() * 8
-    points = sched.ghost_items(args.nvars)
-    bytes_per_fill = 2 * points * 8
+    T = np.dtype(args.dtype).type
+    esize = np.dtype(T).itemsize
+    f, fs, ops = meshes.walls_setup(T=T, roots=args.roots)
+    meshes.config_fill(fs, "walls", seed=3)
+    sched = GhostSchedule(fs, ops)
+    nvars = fs.nvars
+    bytes_per_fill = 2 * sched.ghost_items(nvars) * esize
+    cfg = {"workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
+                       f"faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd) "
+                       f"{'F64' if esize == 8 else 'F32'}, PV(4,4)"
+           if args.roots == 8 else f"walls: {args.roots}^3 roots",
+           "blocks": f.nleaves(), "groups": len(sched.groups),
+           "ghost_points_per_var": int(sched.ghost_items(1)), "nvars": nvars,
+           "field_bytes": fs.work.numel() * esize}
     host = fs.work.numpy()
     threads = os.cpu_count() or 1
     oracle.build()
-    # every step is one whole fill; the count is capped so the run stays
-    # within about two minutes
     t0 = time.perf_counter()
-    oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+    oracle.fill(sched, host, nvars, fs.factors_host, nthreads=threads)
     one = time.perf_counter() - t0
     warm = max(0, min(args.warmup - 1, int(20 / max(one, 1e-3))))
     for _ in range(warm):
-        oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+        oracle.fill(sched, host, nvars, fs.factors_host, nthreads=threads)
     steps = max(1, min(args.steps, int(90 / max(one, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(steps):
-        oracle.fill(sched, host, args.nvars, fs.factors_host, nthreads=threads)
+        oracle.fill(sched, host, nvars, fs.factors_host, nthreads=threads)
     sec = (time.perf_counter() - t0) / steps
     value = bytes_per_fill / sec / 1e9
     line = {
@@ -1016,8 +1132,9 @@ def run_reference(args):
         "n_gpus": args.gpus,
         "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded uniform [-1,1] field data on the sphere mesh)",
+        "vs_baseline": None, "dtype": "f64" if esize == 8 else "f32",
+        "data": "synthetic: the walls mesh's stated data (Gaussian bumps of width 0.05 at the "
+                "2 seeded refinement centres + seeded U[-1,1])",
         "config": dict(cfg, method="cpu threaded fill", parallelism="host threads"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{steps} whole fills after {warm + 1} warm-up, "

@@ -268,7 +268,10 @@ int tam_fill_adjoint_scratch(tam_sched *s, void *y, int32_t nvars, int64_t nbloc
  * a first tam_fill_adjoint), and a schedule without them is refused with
  * TAM_EINVAL.  The first call on each device looks up the array's device
  * address once (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the one array and leave their results in
+ * stream capture.  The address is kept for the life of the process: after
+ * cudaDeviceReset (or anything else that destroys the device's primary
+ * context) the kept address is stale, so a caller that resets a device
+ * must not call this entry point on it again.  All calls share the one array and leave their results in
  * it, so calls that overlap on the GPU (two streams, two threads) race and
  * must be serialised by the caller.  Nothing in the array needs to start
  * at zero: each call writes every scratch element before reading it. */

@@ -62,6 +62,10 @@ def test_calls_fail_cleanly_without_arguments():
     assert lib.tam_schedule_upload(None, None, None) != 0
     assert lib.tam_scatter(None, None, None, None) != 0
     assert lib.tam_gather(None, None, None, None) != 0
+    # the adjoint without allocation names a NULL schedule in the last error
+    assert lib.tam_fill_adjoint_static(None, None, 1, 1, None, -1, 1, None) == -1
+    assert lib.tam_last_error(None, buf, 256) == 0
+    assert b"NULL schedule" in buf.value
 
 
 def test_no_gpu_init_reports_an_error():

@@ -713,7 +713,7 @@ void *g_static_ptr[kMaxDevices] = {};
 extern "C" int tam_fill_adjoint_static(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                                        const void *factors, int32_t first_stage,
                                        int32_t last_stage, void *stream) {
-  if (!s) return TAM_EINVAL;
+  if (!s) return tam::record_error(nullptr, TAM_EINVAL, "tam_fill_adjoint_static: NULL schedule");
   tam_ctx *ctx = s->ctx;
   if (!y || nvars < 1) {
     ctx->err = "tam_fill_adjoint_static: NULL vector or no variables";

@@ -28,6 +28,14 @@ int fail(tam_ctx *ctx, int code, const std::string &msg) {
   return code;
 }
 
+}  // namespace
+
+namespace tam {
+int record_error(tam_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
+}  // namespace tam
+
+namespace {
+
 int cuda_fail(tam_ctx *ctx, cudaError_t e, const char *what) {
   cudaGetLastError();  // clear a sticky-free error so the next call starts clean
   return fail(ctx, TAM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));

@@ -264,6 +264,10 @@ struct tam_sched {
 
 namespace tam {
 
+// Records `msg` as the last error of `ctx` (or, for a NULL context, as the
+// library's last error without a context) and returns `code`.
+int record_error(tam_ctx *ctx, int code, const std::string &msg);
+
 // Kernel launchers (tam_kernels.cu).  All asynchronous on `stream`.
 // The read-only schedule arrays every kernel gets.
 struct SchedArgs {

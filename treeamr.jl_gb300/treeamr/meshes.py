@@ -69,6 +69,61 @@ def sphere_data(seed: int = 1, noise: float = 1e-3):
     return fn
 
 
+def _stored_positions(fs: FieldSet, device):
+    """Per dimension a float64 tensor (nblocks, S_d) of every block's stored
+    positions: ``lo + (B + I - 1) h`` along a vertex-like dimension and
+    ``lo + (B + I - 1/2) h`` along a cell-like one.  On the dyadic extents of
+    the synthetic meshes both are exact, so they equal the single-rounding
+    positions of ``FieldSet.positions``."""
+    import torch
+    f = fs.forest
+    nb = f.nleaves()
+    B = torch.tensor([f.block_base(k) for k in f.leaves], dtype=torch.float64, device=device)
+    h = torch.tensor([float(f.spacing(k.level)) for k in f.leaves], dtype=torch.float64,
+                     device=device)
+    lo = f.block_low(f.leaves[0]) if nb else (0.0,) * f.D
+    out = []
+    for d in range(f.D):
+        i = torch.arange(fs.stored[d], dtype=torch.float64, device=device) - fs.G[d]
+        off = 0.0 if fs.c[d] == 1 else 0.5
+        out.append(lo[d] + (B[:, d:d + 1] + i[None, :] + off) * h[:, None])
+    return out
+
+
+def config_fill(fs: FieldSet, workload: str, seed: int = 1) -> FieldSet:
+    """Every stored point of a 3-D field set set to a workload's stated data,
+    computed on the field set's device: ``"sphere"`` is ``sin(2 pi x)
+    sin(2 pi y) sin(2 pi z)`` plus seeded uniform noise of 1e-3 (every
+    variable), ``"walls"`` Gaussian bumps of width 0.05 at the two seeded
+    refinement centres plus seeded uniform noise in [-1, 1]."""
+    import torch
+    dev = fs.work.device
+    X = _stored_positions(fs, dev)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    nb = fs.nblocks()
+    shape = (nb,) + tuple(reversed(fs.stored))
+    if workload == "sphere":
+        s = [torch.sin(2 * math.pi * x) for x in X]
+        base = (s[2][:, :, None, None] * s[1][:, None, :, None] * s[0][:, None, None, :])
+        for v in range(fs.nvars):
+            noise = torch.empty(shape, dtype=torch.float64, device=dev).uniform_(
+                -1e-3, 1e-3, generator=g)
+            fs.work[:, v].copy_(base + noise)
+    elif workload == "walls":
+        bump = torch.zeros(shape, dtype=torch.float64, device=dev)
+        w2 = 2 * 0.05 ** 2
+        for p in walls_points():
+            e = [torch.exp(-(x - c) ** 2 / w2) for x, c in zip(X, p)]
+            bump += e[2][:, :, None, None] * e[1][:, None, :, None] * e[0][:, None, None, :]
+        for v in range(fs.nvars):
+            noise = torch.empty(shape, dtype=torch.float64, device=dev).uniform_(
+                -1.0, 1.0, generator=g)
+            fs.work[:, v].copy_(bump + noise)
+    else:
+        raise ValueError(f"no stated data for workload {workload!r}")
+    return fs
+
+
 def uniform_data(seed: int = 1):
     rng = np.random.default_rng(seed)
 
