@@ -10,8 +10,16 @@ host package's ``operators`` module and are pinned by the reference's
 known-answer tests in ``tests/test_operators.py``.
 
 Parity status: pinned by the reference's known-answer and property tests
-(restated in tests/).  No golden vectors exist in the reference and the
-reference (Julia) cannot run in this environment.
+(restated in tests/), and by a second oracle independent of the product's
+schedule (``oracle/pointwise.py``, ``pointwise.c``): the meshes rebuilt from
+their construction rules and every ghost derived point by point from the
+forest's geometry, equal to this replay bit for bit.  No golden vectors exist
+in the reference and the reference (Julia) cannot run in this environment.
+What this replay takes from the product: the flattened schedule (which
+transfer writes which ghost, windows, weights, stage order).  What the
+point-by-point oracle takes from it: the forest's leaves and their order
+(checked against a rebuild and the curve order), the field layout and the
+parity table's meaning, nothing else.
 """
 from __future__ import annotations
 
@@ -38,16 +46,19 @@ def build(force: bool = False) -> str:
     with _lock:
         os.makedirs(BUILD_DIR, exist_ok=True)
         newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
-        if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
-            return LIB_PATH
-        tmp = LIB_PATH + ".tmp"
-        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
-               "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), SRC, "-o", tmp]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-        os.replace(tmp, LIB_PATH)
-        return LIB_PATH
+        fresh = not force and os.path.exists(LIB_PATH) and \
+            os.path.getmtime(LIB_PATH) >= newest
+        if not fresh:
+            tmp = LIB_PATH + ".tmp"
+            cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+                   "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), SRC, "-o", tmp]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+            os.replace(tmp, LIB_PATH)
+    from . import pointwise
+    pointwise.build(force)
+    return LIB_PATH
 
 
 def lib():

@@ -5,7 +5,9 @@ variables) in Float32 and Float64, and the batch of 64 uneven forests.
 
 - Every fill is compared with the oracle's fill of the same data bit for bit
   (the fused kernels take the reference's CPU form of the sum, the plain one
-  its device form; on finite data the two have the same bits).
+  its device form; on finite data the two have the same bits), and that fill
+  with the point-by-point oracle's, which derives every ghost from the
+  forest's geometry without the product's schedule.
 - Polynomial exactness at full size (``test/ghost_tests.jl:247-281``): data of
   degree 3 in each coordinate come back exact to 1e-10 of their scale at
   order 4 at every ghost, across every level jump of the mesh.  On the
@@ -24,6 +26,7 @@ import torch
 
 import oracle
 from _helpers import nanbits
+from oracle import pointwise
 from _props import NTHREADS, _dot, sphere_polynomial_error, walls_properties
 from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
 from treeamr.storage import vertexcentered
@@ -61,6 +64,10 @@ def test_sphere_full_bit_exact(cuda_lib, sphere_forest):
     sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
     start = fs.work.clone()
     expect = _oracle_expect(fs, sched)
+    # the point-by-point oracle, which uses no schedule, agrees with the replay
+    point = pointwise.fill(fs, start.cpu().numpy(), 4, nthreads=NTHREADS)
+    assert np.array_equal(nanbits(point), nanbits(expect))
+    del point
     for method in ("fused", "plain"):
         fs.work.copy_(start)
         fill_ghosts(fs, sched, method=method)
@@ -78,6 +85,9 @@ def test_walls_full_bit_exact(cuda_lib, walls_forest):
         sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
         start = fs.work.clone()
         expect = _oracle_expect(fs, sched)
+        point = pointwise.fill(fs, start.cpu().numpy(), 4, nthreads=NTHREADS)
+        assert np.array_equal(nanbits(point), nanbits(expect)), np.dtype(T).name
+        del point
         for method in ("fused", "plain"):
             fs.work.copy_(start)
             fill_ghosts(fs, sched, method=method)
@@ -98,7 +108,9 @@ def test_batch64_full_bit_exact(cuda_lib):
     after = batch.arena
     for m, (fs, s) in enumerate(zip(fss, scheds)):
         host = batch.member_view(before, m).numpy().copy()
+        point = pointwise.fill(fs, host, 4, nthreads=NTHREADS)
         expect = oracle.fill(s, host, fs.nvars, fs.factors_host, nthreads=NTHREADS)
+        assert np.array_equal(nanbits(point), nanbits(expect)), m
         assert _same(batch.member_view(after, m), expect) == 0, m
 
 
@@ -113,7 +125,7 @@ def test_walls_full_polynomial_and_outflow(cuda_lib, walls_forest):
     fs = FieldSet(walls_forest, 8, G=2, centering=vertexcentered(3),
                   parity=meshes.walls_parities(), T=np.float64, device="cuda")
     sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
-    worst, scale, bad = walls_properties(fs, sched, "gpu", margin=1.0 / 32)
+    worst, scale, bad = walls_properties(fs, sched, "gpu", margin=1.0 / 64)
     assert worst <= 1e-10 * scale, (worst, scale)
     assert bad == 0
 
