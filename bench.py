@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--roots", type=int, default=8)
     ap.add_argument("--levels", type=int, default=3)
     ap.add_argument("--nvars", type=int, default=4)
+    ap.add_argument("--walls-levels", type=int, default=5,
+                    help="refinement levels of the walls mesh (5 as stated; fewer for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-walls", action="store_true")
@@ -109,13 +111,23 @@ def stencil_flops(sched, nvars, one_tap=True):
     return out
 
 
-def fused_launches(sched):
-    """Kernel launches of one fused fill: per stage a copy launch when it has
-    unit copies and a stencil launch when it has stencils."""
+def fused_launches(sched, ds=None):
+    """Kernel launches of one fused fill: per stage (or stage group, when the
+    uploaded schedule ``ds`` runs consecutive stages as one) a copy launch
+    when it has unit copies and a stencil launch when it has stencils."""
+    tags = sorted({gr.stage for gr in sched.groups})
+    merged = []
+    if ds is not None and ds.options().get("merge_stages", 0):
+        ng, nin = ds.stage_groups()
+        merged = [ng, nin]
     n = 0
-    for tag in sorted({gr.stage for gr in sched.groups}):
+    for tag in tags:
         grs = [gr for gr in sched.groups if gr.stage == tag]
         n += any(gr.unit() for gr in grs) + any(not gr.unit() for gr in grs)
+    if merged and merged[0]:
+        # a group of k prolongation stages runs one stencil launch instead of
+        # k (their stencils only, on the walls and sphere meshes)
+        n -= merged[1] - merged[0]
     return n
 
 
@@ -225,7 +237,7 @@ def measure_walls(T, dev, timed, args, peak):
     from treeamr import GhostSchedule, fill_ghosts, meshes
     from treeamr.autotune import autotune
     from treeamr.ghosts import device_schedule
-    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots)
+    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots, levels=args.walls_levels)
     sched = GhostSchedule(fs, ops)
     meshes.config_fill(fs, "walls", seed=3)
     esize = np.dtype(T).itemsize
@@ -294,9 +306,9 @@ def measure_walls(T, dev, timed, args, peak):
         "unify": {"ms": ms_unify, "bytes": unify_bytes,
                   "gbs": unify_bytes / (ms_unify * 1e-3) / 1e9},
         "tuned": tuned,
-        "gpu_launches_per_fill": fused_launches(sched),
+        "gpu_launches_per_fill": fused_launches(sched, ds),
     }
-    del fs, sched
+    del fs, sched, ds
     torch.cuda.empty_cache()
     return out
 
@@ -741,7 +753,7 @@ def measure_sphere(dev, timed, args, peak, world):
         "ghost_points_per_s": sched.ghost_items(1) / (ms * 1e-3),
         "state": state,
         "tuned": tuned,
-        "gpu_launches_per_fill": fused_launches(sched),
+        "gpu_launches_per_fill": fused_launches(sched, ds),
     }
     del fs, sched, ds
     torch.cuda.empty_cache()
@@ -807,7 +819,7 @@ def main():
     if args.sector_minimum is not None:
         from treeamr import GhostSchedule, meshes
         T = np.dtype(args.dtype).type
-        f, fs, ops = meshes.walls_setup(T=T, roots=args.roots)
+        f, fs, ops = meshes.walls_setup(T=T, roots=args.roots, levels=args.walls_levels)
         sched = GhostSchedule(fs, ops)
         out = sector_minimum(sched, fs.nvars, np.dtype(T).itemsize, args.sector_minimum)
         out.update({"roots": args.roots, "dtype": args.dtype, "blocks": f.nleaves()})
@@ -856,7 +868,7 @@ def main():
     # outflow high faces, stages P and 0), its stated data
     T = np.dtype(args.dtype).type
     esize = np.dtype(T).itemsize
-    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots)
+    f, fs, ops = meshes.walls_setup(device=dev, T=T, roots=args.roots, levels=args.walls_levels)
     meshes.config_fill(fs, "walls", seed=3 + rank)
     sched = GhostSchedule(fs, ops)
     nvars = fs.nvars
@@ -867,7 +879,8 @@ def main():
     cfg = {"workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
                        f"faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd) "
                        f"{'F64' if esize == 8 else 'F32'}, PV(4,4)"
-           if args.roots == 8 else f"walls: {args.roots}^3 roots",
+           if (args.roots, args.walls_levels) == (8, 5) else
+           f"walls: {args.roots}^3 roots, {args.walls_levels} levels",
            "blocks": f.nleaves(), "groups": len(sched.groups),
            "ghost_points_per_var": int(sched.ghost_items(1)), "nvars": nvars,
            "field_bytes": field_bytes,
@@ -987,7 +1000,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": args.steps * fused_launches(sched) if method == "fused" else
+            "gpu_launches": args.steps * fused_launches(sched, ds) if method == "fused" else
             args.steps * len(sched.groups),
         }
         print(json.dumps(line), flush=True)
@@ -1100,7 +1113,7 @@ def run_reference(args):
     import oracle
     T = np.dtype(args.dtype).type
     esize = np.dtype(T).itemsize
-    f, fs, ops = meshes.walls_setup(T=T, roots=args.roots)
+    f, fs, ops = meshes.walls_setup(T=T, roots=args.roots, levels=args.walls_levels)
     meshes.config_fill(fs, "walls", seed=3)
     sched = GhostSchedule(fs, ops)
     nvars = fs.nvars
@@ -1108,7 +1121,8 @@ def run_reference(args):
     cfg = {"workload": "walls: 3-D vertex, 8^3 roots, N=32, G=2, reflecting low / outflow high "
                        f"faces, 5 levels around 2 seeded points, 8 vars (5 even, 3 odd) "
                        f"{'F64' if esize == 8 else 'F32'}, PV(4,4)"
-           if args.roots == 8 else f"walls: {args.roots}^3 roots",
+           if (args.roots, args.walls_levels) == (8, 5) else
+           f"walls: {args.roots}^3 roots, {args.walls_levels} levels",
            "blocks": f.nleaves(), "groups": len(sched.groups),
            "ghost_points_per_var": int(sched.ghost_items(1)), "nvars": nvars,
            "field_bytes": fs.work.numel() * esize}

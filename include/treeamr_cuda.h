@@ -485,14 +485,40 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
  * sits under a zero weight, which the full sum carries into the result.
  * tam_fill_plain always takes the device form. */
 #define TAM_OPT_ONE_TAP 4
+/* Points a lane of the unit-copy launches takes at once, 1 (the default), 2
+ * or 4: each point's every variable is loaded before any is stored, so more
+ * points a lane put more loads in flight a warp, for more registers a
+ * thread. */
+#define TAM_OPT_COPY_POINTS 5
+/* The order in which a fill's launches visit target blocks: 0 (the default)
+ * the blocks' own order, 1 a reverse Cuthill-McKee order of the graph of
+ * the schedule's transfers, which keeps blocks that exchange ghosts close
+ * together in time (the sectors they share stay in L2). */
+#define TAM_OPT_BLOCK_ORDER 6
+/* 1: a stage's stencil points grouped by their path through the kernel
+ * (the order class and, in the CPU form, the dimensions that take one tap),
+ * so that no warp mixes paths; 0: by target block only.  The default is 1
+ * for Float64 (the FP64 pipe spends a warp instruction's time whatever
+ * lanes are off) and 0 for Float32. */
+#define TAM_OPT_PATH_TILES 7
+/* 1 (the default): consecutive prolongation stages none of whose points
+ * conflict (src/schedule.jl:2735-2931, stage_groups) run as one launch pair
+ * when a fill's stage range holds them all; 0: one launch pair a stage. */
+#define TAM_OPT_MERGE_STAGES 8
+/* The stage groups the schedule found: how many, and how many stages they
+ * hold in all (a whole fill runs `nstages - stages_in_groups + groups`
+ * launch pairs).  No reference counterpart beyond stage_groups itself. */
+int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stages_in_groups);
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
 /* The launch-option autotuner: times every combination of TAM_OPT_TILE_ITEMS
  * (32 .. 512), TAM_OPT_THREADS (128, 256, 512) and, for Float64,
  * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (best of `reps`
- * fills after a warm-up, CUDA events on `stream`), leaves the fastest set
- * and returns it.  The fills overwrite `work`'s ghosts (never an own
+ * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
+ * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_BLOCK_ORDER and
+ * TAM_OPT_COPY_POINTS one at a time; leaves the fastest set and returns the first three (the others
+ * through tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an own
  * point).  Synchronizes `stream`; re-tiling allocates, so not inside a
  * stream capture.  The reference has no tuning. */
 int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,

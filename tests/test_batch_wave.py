@@ -34,6 +34,15 @@ def test_batch_fill_equals_member_fills(cuda_lib):
     for m in range(len(fss)):
         got = batch.member_view(batch.arena, m).cpu().numpy()
         assert np.array_equal(got.view(np.uint32), expect[m].view(np.uint32)), m
+    # every grouping of the batch's work gives the same bits
+    for opt, val in (("path_tiles", 1), ("copy_points", 4), ("tile_items", 48)):
+        batch.set_option(opt, val)
+        batch.arena.copy_(start)
+        batch.fill()
+        torch.cuda.synchronize()
+        for m in range(len(fss)):
+            got = batch.member_view(batch.arena, m).cpu().numpy()
+            assert np.array_equal(got.view(np.uint32), expect[m].view(np.uint32)), (opt, m)
     # and each member through its own fill gives the same
     alone = start.clone()
     for m, (fs, s) in enumerate(zip(fss, scheds)):
@@ -155,7 +164,8 @@ def test_native_autotune(cuda_lib):
     host = np.random.default_rng(9).uniform(size=tuple(fs.work.shape))
     fs.work.copy_(torch.from_numpy(host))
     best = autotune(fs, s)
-    assert set(best) == {"tile_items", "threads", "int_mul"} and s._tuned_ms > 0
+    assert set(best) == {"tile_items", "threads", "int_mul", "merge_stages", "path_tiles",
+                         "block_order", "copy_points"} and s._tuned_ms > 0
     ds = device_schedule(s, 0)
     assert ds.options()["tile_items"] == best["tile_items"]
     fs.work.copy_(torch.from_numpy(host))

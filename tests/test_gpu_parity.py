@@ -209,17 +209,21 @@ def test_launch_options_change_no_bit(cuda_lib):
     fs.work = torch.from_numpy(host).cuda()
     fs.factors = fs.factors.cuda()
     ds = device_schedule(s, 0)
-    for ti, th, im in ((16, 64, 0), (37, 96, 1), (512, 512, 1), (4096, 128, 0)):
-        ds.set_option("tile_items", ti)
-        ds.set_option("threads", th)
-        ds.set_option("int_mul", im)
-        assert ds.options() == {"tile_items": ti, "threads": th, "int_mul": im, "one_tap": 1}
+    for ti, th, im, cp, bo, pt, ms in ((16, 64, 0, 1, 0, 0, 1), (37, 96, 1, 2, 1, 1, 0),
+                                       (512, 512, 1, 4, 0, 1, 1), (4096, 128, 0, 2, 1, 0, 0)):
+        opts = {"tile_items": ti, "threads": th, "int_mul": im, "one_tap": 1,
+                "copy_points": cp, "block_order": bo, "path_tiles": pt, "merge_stages": ms}
+        for k, v in opts.items():
+            ds.set_option(k, v)
+        assert ds.options() == opts
         fs.work.copy_(torch.from_numpy(host))
         fill_ghosts(fs, s)
         torch.cuda.synchronize()
-        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect))
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), opts
     with pytest.raises(Exception):
         ds.set_option("threads", 100)
+    with pytest.raises(Exception):
+        ds.set_option("copy_points", 3)
 
 
 def test_autotune_keeps_results(cuda_lib):

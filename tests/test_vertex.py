@@ -12,7 +12,7 @@ import oracle
 from _helpers import (awkward_fill, boundary_from, exact_values, ghost_mask, makepoly, nanbits,
                       nested_forest)
 from treeamr import (EvenParity, FieldSet, Forest, GhostSchedule, OddParity, Operators,
-                     fill_ghosts, vertexcentered)
+                     fill_ghosts, meshes, vertexcentered)
 from treeamr.schedule import SELFIMAGE_TAG, UNIFY_TAG
 
 
@@ -248,3 +248,74 @@ def test_gpu_one_tap_option_selects_the_form(cuda_lib, one_tap, T):
     finally:
         ds.set_option("one_tap", 1)
         ds.set_option("int_mul", 0)
+
+
+def _predicted_stage_groups(sched):
+    """The stage groups restated from ``stage_groups`` (src/schedule.jl:2735-2931):
+    after phase 1, a stage joins the group below it when its tag is the next
+    one and none of its target boxes or source windows, per block, meets a
+    target box of the group, nor its target boxes a source window of it."""
+    import collections
+    bytag = collections.defaultdict(list)
+    for g in sched.groups:
+        bytag[g.stage].append(g)
+
+    def boxes(tag):
+        out = []
+        for g in bytag[tag]:
+            w = [(st.targetfirst, st.targetfirst + st.ntarget - 1) for st in g.stencils]
+            r = [(int(st.srcstart.min()), int(st.srcstart.max()) + st.order - 1)
+                 for st in g.stencils]
+            for tb, sb in zip(g.targetblocks, g.sourceblocks):
+                out.append((int(tb), w, True))
+                out.append((int(sb), r, False))
+        return out
+
+    def meets(a, b):
+        return all(max(x[0], y[0]) <= min(x[1], y[1]) for x, y in zip(a, b))
+    groups, W, R, prev = [], collections.defaultdict(list), collections.defaultdict(list), None
+    for tag in sorted(bytag):
+        if tag <= 1:
+            prev = None
+            continue
+        acc = boxes(tag)
+        joins = prev is not None and tag == prev + 1 and not any(
+            any(meets(box, b) for b in W[blk]) or (wr and any(meets(box, b) for b in R[blk]))
+            for blk, box, wr in acc)
+        if not joins:
+            W.clear()
+            R.clear()
+            groups.append([tag])
+        else:
+            groups[-1].append(tag)
+        for blk, box, wr in acc:
+            (W if wr else R)[blk].append(box)
+        prev = tag
+    merged = [g for g in groups if len(g) > 1]
+    return len(merged), sum(len(g) for g in merged)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_gpu_stage_groups_bit_exact(cuda_lib, T):
+    """Consecutive prolongation stages that conflict nowhere run as one launch
+    pair: the library finds the groups the restated rule predicts, and the
+    fill with them equals the fill stage by stage and the oracle, bit for
+    bit, on the walls mesh at 4^3 roots, N=16, 3 levels."""
+    from treeamr.ghosts import device_schedule
+    f, fs, ops = meshes.walls_setup(roots=4, N=16, levels=3, T=T)
+    meshes.config_fill(fs, "walls", seed=3)
+    sched = GhostSchedule(fs, ops)
+    host = fs.work.numpy().copy()
+    expect = oracle.fill(sched, host.copy(), fs.nvars, fs.factors_host)
+    fs.work = torch.from_numpy(host.copy()).cuda()
+    fs.factors = fs.factors.cuda()
+    ds = device_schedule(sched, 0)
+    assert ds.stage_groups() == _predicted_stage_groups(sched)
+    assert ds.stage_groups()[0] >= 1
+    for merge in (1, 0):
+        ds.set_option("merge_stages", merge)
+        fs.work.copy_(torch.from_numpy(host))
+        fill_ghosts(fs, sched)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), merge

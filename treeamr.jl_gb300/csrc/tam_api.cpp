@@ -80,6 +80,7 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_ptiles);
   cudaFree(s->d_cls);
   cudaFree(s->d_wtab);
+  cudaFree(s->d_wshort);
   cudaFree(s->d_csingle);
   cudaFree(s->d_perm);
   cudaFree(s->d_err);
@@ -92,6 +93,7 @@ void free_sched_device(tam_sched *s) {
   s->d_tiles = nullptr;
   s->d_cls = nullptr;
   s->d_wtab = nullptr;
+  s->d_wshort = nullptr;
   s->d_csingle = s->d_perm = nullptr;
   s->d_err = nullptr;
   s->d_solos = nullptr;
@@ -345,15 +347,73 @@ void build_singles(const tam_schedule_desc *d, const tam_group &h, tam::DevGroup
 tam::SchedArgs sched_args(const tam_sched *s) {
   return tam::SchedArgs{s->d_groups, s->d_tb,     s->d_sb,        s->d_srcstart,
                         s->d_weights, s->d_cls,   s->d_wtab,      s->shape.int_mul,
-                        nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap};
+                        nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap,
+                        s->shape.copy_points, s->d_wshort};
+}
+
+// The order in which the fused launches visit target blocks: with
+// TAM_OPT_BLOCK_ORDER 1, a reverse Cuthill-McKee numbering of the graph whose
+// edges are the schedule's transfers (breadth first from a block of least
+// degree, each block's neighbours in increasing degree, the whole reversed),
+// so that blocks that exchange ghosts are visited close together in time and
+// the sectors they share -- a block's faces are one transfer's source and
+// another's target -- stay in L2 between the two; otherwise the blocks' own
+// (curve) order.  rank[b] for 1-based block b - 1.
+std::vector<int32_t> block_rank(const tam_sched *s) {
+  const int64_t n = s->nblocks;
+  std::vector<int32_t> rank(n);
+  for (int64_t b = 0; b < n; ++b) rank[b] = (int32_t)b;
+  if (s->shape.block_order != 1 || s->nsource != s->nblocks || n < 2) return rank;
+  std::vector<std::vector<int32_t>> adj(n);
+  for (size_t t = 0; t < s->h_tb.size(); ++t) {
+    const int32_t a = s->h_tb[t] - 1, c = s->h_sb[t] - 1;
+    if (a == c) continue;
+    adj[a].push_back(c);
+    adj[c].push_back(a);
+  }
+  for (auto &l : adj) {
+    std::sort(l.begin(), l.end());
+    l.erase(std::unique(l.begin(), l.end()), l.end());
+  }
+  auto deg_less = [&](int32_t x, int32_t y) {
+    return adj[x].size() != adj[y].size() ? adj[x].size() < adj[y].size() : x < y;
+  };
+  for (auto &l : adj) std::sort(l.begin(), l.end(), deg_less);
+  std::vector<int32_t> order;
+  order.reserve(n);
+  std::vector<char> seen(n, 0);
+  std::vector<int32_t> by_degree(n);
+  for (int64_t b = 0; b < n; ++b) by_degree[b] = (int32_t)b;
+  std::sort(by_degree.begin(), by_degree.end(), deg_less);
+  for (int32_t start : by_degree) {  // every connected component
+    if (seen[start]) continue;
+    size_t head = order.size();
+    order.push_back(start);
+    seen[start] = 1;
+    while (head < order.size()) {
+      const int32_t v = order[head++];
+      for (int32_t w : adj[v])
+        if (!seen[w]) {
+          seen[w] = 1;
+          order.push_back(w);
+        }
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) rank[order[n - 1 - i]] = (int32_t)i;
+  return rank;
 }
 
 // The fused tiles of every stage: each stage's transfers ordered by target
-// block, then group, each cut into runs of `tile_items` box points.
-std::vector<tam::Tile> build_tiles(tam_sched *s) {
-  std::vector<tam::Tile> tiles;
+// block (in block_rank's order), then group, each cut into runs of
+// `tile_items` box points; the
+// stencil tiles cut where their points' path through the kernel changes and
+// ordered by it, each path's tiles in that order (tam::StencilRuns), with
+// the path's key in `keys` (0 for a copy tile).
+void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int32_t> &rank,
+              tam::StencilRuns &runs, std::vector<tam::Tile> &tiles,
+              std::vector<uint16_t> &keys) {
   const int ti = s->shape.tile_items;
-  for (tam::Stage &st : s->stages) {
+  for (tam::Stage &st : list) {
     st.tile0 = (int64_t)tiles.size();
     struct Entry {
       int32_t tblock, group, transfer;
@@ -363,27 +423,178 @@ std::vector<tam::Tile> build_tiles(tam_sched *s) {
       const tam::DevGroup &g = s->groups[gi];
       if (g.turned) continue;  // a turned group has a launch of its own
       for (int64_t t = 0; t < g.ntransfers; ++t)
-        entries.push_back({s->h_tb[g.first + t], gi, (int32_t)(g.first + t)});
+        entries.push_back({rank[s->h_tb[g.first + t] - 1], gi, (int32_t)(g.first + t)});
     }
     std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
       return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
     });
     // unit copies first (the light kernel; those without a factor column
     // first of all), then the stencils
-    for (int pass = 0; pass < 3; ++pass) {
+    for (int pass = 0; pass < 2; ++pass) {
       for (const Entry &e : entries) {
         const tam::DevGroup &g = s->groups[e.group];
         if (tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
-        for (int i0 = 0; i0 < box; i0 += ti)
+        for (int i0 = 0; i0 < box; i0 += ti) {
           tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+          keys.push_back(0);
+        }
       }
       if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
       if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;
     }
+    std::vector<tam::Tile> sten;
+    std::vector<uint16_t> skeys;
+    for (const Entry &e : entries) {
+      const tam::DevGroup &g = s->groups[e.group];
+      if (tile_pass(g) != 2) continue;
+      if (!s->shape.path_tiles) {  // by target block alone: one key
+        const int box = g.n[0] * g.n[1] * g.n[2];
+        for (int i0 = 0; i0 < box; i0 += ti) {
+          sten.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+          skeys.push_back(0);
+        }
+        continue;
+      }
+      if (!runs.cache.count(e.group))
+        tam::StencilRuns::of(g, s->h_pool_csingle.data(), s->h_pool_perm.data(), s->D,
+                             runs.cache[e.group]);
+      runs.tiles(e.group, e.transfer, ti, sten, skeys);
+    }
+    std::vector<size_t> order(sten.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t x, size_t y) { return skeys[x] < skeys[y]; });
+    for (size_t i : order) {
+      tiles.push_back(sten[i]);
+      keys.push_back(skeys[i]);
+    }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
+}
+
+// The tiles of every stage, then of every stage group, in one array.
+std::vector<tam::Tile> build_tiles(tam_sched *s, std::vector<uint16_t> &keys) {
+  std::vector<tam::Tile> tiles;
+  keys.clear();
+  tam::StencilRuns runs;
+  const std::vector<int32_t> rank = block_rank(s);
+  tiles_of(s, s->stages, rank, runs, tiles, keys);
+  tiles_of(s, s->merged, rank, runs, tiles, keys);
   return tiles;
+}
+
+// Packed tiles of every stage, then of every stage group.
+std::vector<tam::PTile> pack_all(tam_sched *s, const std::vector<tam::Tile> &tiles,
+                                 const std::vector<uint16_t> &keys) {
+  std::vector<tam::PTile> out = tam::pack_stages(s->stages, tiles, s->shape.tile_items, &keys);
+  std::vector<tam::PTile> more = tam::pack_stages(s->merged, tiles, s->shape.tile_items, &keys);
+  for (tam::Stage &m : s->merged) m.ptile0 += (int64_t)out.size();
+  out.insert(out.end(), more.begin(), more.end());
+  return out;
+}
+
+// The stage groups (src/schedule.jl:2735-2931, stage_groups): after phase 1,
+// a prolongation stage joins the group of the stage below it when its tag is
+// the next one, none of its groups is turned or bounded (those run in
+// launches of their own), and none of its points conflicts with a stage
+// already in the group: nothing it reads or writes is written by one of
+// them, and nothing it writes is read by one.  Per block, every group's
+// target box is a write and its source window (the srcstart range widened
+// by the order) a read.  Running a group's stages as one launch pair is
+// then the same as running them one after another.
+void build_stage_groups(tam_sched *s) {
+  s->merged.clear();
+  s->merged_at.assign(s->stages.size(), -1);
+  if (s->nsource != s->nblocks) return;  // a regrid reads another array
+  struct Box {
+    int32_t lo[3], hi[3];
+  };
+  auto meets = [](const Box &a, const Box &b) {
+    for (int d = 0; d < 3; ++d)
+      if (std::max(a.lo[d], b.lo[d]) > std::min(a.hi[d], b.hi[d])) return false;
+    return true;
+  };
+  std::vector<std::vector<Box>> writes(s->nblocks), reads(s->nblocks);
+  std::vector<int32_t> touched;
+  struct Access {
+    int32_t block;
+    Box box;
+    bool write;
+  };
+  auto access_of = [&](const tam::Stage &st, std::vector<Access> &out, bool &eligible) {
+    out.clear();
+    eligible = true;
+    for (int32_t gi : st.groups) {
+      const tam_group &h = s->host_groups[gi];
+      if (h.orientation != 0 || h.bounded != 0) eligible = false;
+      Box w{{0, 0, 0}, {0, 0, 0}}, r{{0, 0, 0}, {0, 0, 0}};
+      for (int d = 0; d < s->D; ++d) {
+        const tam_stencil &sd = h.stencil[d];
+        w.lo[d] = sd.targetfirst;
+        w.hi[d] = sd.targetfirst + sd.ntarget - 1;
+        int32_t lo = INT32_MAX, hi = INT32_MIN;
+        for (int i = 0; i < sd.ntarget; ++i) {
+          const int32_t v = s->h_srcstart[sd.srcstart + i];
+          lo = std::min(lo, v);
+          hi = std::max(hi, v);
+        }
+        r.lo[d] = lo;
+        r.hi[d] = hi + sd.order - 1;
+      }
+      for (int64_t t = h.first; t < h.first + h.ntransfers; ++t) {
+        out.push_back({s->h_tb[t] - 1, w, true});
+        out.push_back({s->h_sb[t] - 1, r, false});
+      }
+    }
+  };
+  std::vector<Access> acc;
+  size_t open = SIZE_MAX;  // first stage of the group being formed
+  for (size_t i = 0; i < s->stages.size(); ++i) {
+    const tam::Stage &st = s->stages[i];
+    bool eligible = false;
+    if (st.tag > 1) access_of(st, acc, eligible);
+    bool joins = eligible && open != SIZE_MAX && st.tag == s->stages[i - 1].tag + 1;
+    if (joins) {
+      for (const Access &a : acc) {
+        for (const Box &b : writes[a.block])
+          if (meets(a.box, b)) joins = false;
+        if (a.write)
+          for (const Box &b : reads[a.block])
+            if (meets(a.box, b)) joins = false;
+        if (!joins) break;
+      }
+    }
+    if (!joins) {
+      // a new group starts here (or none, for an ineligible stage)
+      for (int32_t b : touched) {
+        writes[b].clear();
+        reads[b].clear();
+      }
+      touched.clear();
+      open = eligible ? i : SIZE_MAX;
+    }
+    if (eligible) {
+      for (const Access &a : acc) {
+        (a.write ? writes : reads)[a.block].push_back(a.box);
+        touched.push_back(a.block);
+      }
+      if (joins) {
+        if (s->merged_at[open] < 0) {
+          tam::Stage m;
+          m.tag = s->stages[open].tag;
+          m.groups = s->stages[open].groups;
+          m.span = 1;
+          s->merged_at[open] = (int32_t)s->merged.size();
+          s->merged.push_back(m);
+        }
+        tam::Stage &m = s->merged[s->merged_at[open]];
+        m.groups.insert(m.groups.end(), st.groups.begin(), st.groups.end());
+        m.span += 1;
+        m.last_tag = st.tag;
+      }
+    }
+  }
 }
 
 // The solo groups of every stage (SoloGroup): turned or bounded.  A turned
@@ -618,9 +829,19 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
   s->h_tb.assign(d->targetblocks, d->targetblocks + d->ntransfers);
   s->h_sb.assign(d->sourceblocks, d->sourceblocks + d->ntransfers);
   s->h_srcstart.assign(d->srcstart, d->srcstart + d->nsrcstart);
-  std::vector<tam::Tile> tiles = build_tiles(s);
-  std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
+  s->h_pool_csingle = std::move(csingle);
+  s->h_pool_perm = std::move(perm);
+  // Float64 stencils are bound by the FP64 pipe, which a divergent warp
+  // wastes; Float32 ones by memory, which the blocks' order serves best
+  s->shape.path_tiles = d->dtype == TAM_F64 ? 1 : 0;
+  build_stage_groups(s);
+  std::vector<uint16_t> keys;
+  std::vector<tam::Tile> tiles = build_tiles(s, keys);
+  std::vector<tam::PTile> ptiles = pack_all(s, tiles, keys);
   build_solos(s);
+  std::vector<uint64_t> wshort;
+  if (d->dtype == TAM_F64) wshort = tam::short_weights(wtab);
+  if (wshort.empty()) wshort.push_back(0);
 
   cudaError_t e;
   if ((e = tam::side_create(s->side)) != cudaSuccess ||
@@ -635,8 +856,10 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
       (e = upload(&s->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
       (e = upload(&s->d_cls, cls.data(), cls.size())) != cudaSuccess ||
       (e = upload((unsigned char **)&s->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
-      (e = upload(&s->d_csingle, csingle.data(), csingle.size())) != cudaSuccess ||
-      (e = upload(&s->d_perm, perm.data(), perm.size())) != cudaSuccess ||
+      (e = upload(&s->d_wshort, wshort.data(), wshort.size())) != cudaSuccess ||
+      (e = upload(&s->d_csingle, s->h_pool_csingle.data(), s->h_pool_csingle.size())) !=
+          cudaSuccess ||
+      (e = upload(&s->d_perm, s->h_pool_perm.data(), s->h_pool_perm.size())) != cudaSuccess ||
       (e = upload(&s->d_err, (const int32_t *)nullptr, 1)) != cudaSuccess) {
     free_sched_device(s);
     delete s;
@@ -648,8 +871,6 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
   s->h_pool_weights = std::move(weights);
   s->h_pool_cls = std::move(cls);
   s->h_pool_wtab = std::move(wtab);
-  s->h_pool_csingle = std::move(csingle);
-  s->h_pool_perm = std::move(perm);
   *out = s;
   return TAM_OK;
 }
@@ -799,6 +1020,15 @@ static int owned_adjoint(tam_sched *s, void *y, void *alt, int32_t nvars, int64_
                       s->adj_scratch, s->adj_scratch_bytes, stream);
 }
 
+int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stages_in_groups) {
+  if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_stage_groups: NULL schedule");
+  int32_t n = 0;
+  for (const tam::Stage &m : s->merged) n += m.span;
+  if (groups) *groups = (int32_t)s->merged.size();
+  if (stages_in_groups) *stages_in_groups = n;
+  return TAM_OK;
+}
+
 int tam_schedule_info(const tam_sched *s, int64_t *ngroups, int64_t *ntransfers, int64_t *points,
                       int32_t *nstages) {
   if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_info: NULL schedule");
@@ -846,9 +1076,22 @@ int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, i
   cudaStream_t st = (cudaStream_t)stream;
   tam::SchedArgs args = sched_args(s);
   if (method == TAM_METHOD_PLAIN) args.one_tap = 0;  // the device form
-  for (const tam::Stage &stage : s->stages) {
+  for (size_t i = 0; i < s->stages.size(); ++i) {
+    const tam::Stage &stage = s->stages[i];
     if (stage.tag < first_stage || stage.tag > last_stage) continue;
     cudaError_t e = cudaSuccess;
+    const int32_t mi = s->merged_at.empty() ? -1 : s->merged_at[i];
+    if (method == TAM_METHOD_FUSED && s->shape.merge_stages && mi >= 0 &&
+        s->merged[mi].last_tag <= last_stage) {
+      // a stage group inside the range: one launch pair for all its stages
+      const tam::Stage &m = s->merged[mi];
+      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + m.ptile0,
+                                  m.npcopy0, m.npcopy, m.nptiles, args, work, factors, nvars,
+                                  s->S, s->shape.threads, st, &s->side, nullptr);
+      if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage-group launch");
+      i += m.span - 1;
+      continue;
+    }
     if (method == TAM_METHOD_FUSED) {
       e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0,
                                   stage.npcopy0, stage.npcopy, stage.nptiles, args, work,
@@ -971,15 +1214,23 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, con
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
   if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_set_option: NULL schedule");
   switch (option) {
-    case TAM_OPT_TILE_ITEMS: {
-      if (value < 16 || value > 4096)
+    case TAM_OPT_TILE_ITEMS:
+    case TAM_OPT_BLOCK_ORDER:
+    case TAM_OPT_PATH_TILES: {
+      int *field = option == TAM_OPT_TILE_ITEMS    ? &s->shape.tile_items
+                   : option == TAM_OPT_BLOCK_ORDER ? &s->shape.block_order
+                                                   : &s->shape.path_tiles;
+      if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
         return fail(s->ctx, TAM_EINVAL, "tile items must be in 16..4096");
-      if (value == s->shape.tile_items) return TAM_OK;
+      if (option != TAM_OPT_TILE_ITEMS && value != 0 && value != 1)
+        return fail(s->ctx, TAM_EINVAL, "block_order and path_tiles are 0 or 1");
+      if (value == *field) return TAM_OK;
       DeviceGuard guard(s->ctx->device);
-      const int old = s->shape.tile_items;
-      s->shape.tile_items = (int)value;
-      std::vector<tam::Tile> tiles = build_tiles(s);
-      std::vector<tam::PTile> ptiles = tam::pack_stages(s->stages, tiles, s->shape.tile_items);
+      const int old = *field;
+      *field = (int)value;
+      std::vector<uint16_t> keys;
+      std::vector<tam::Tile> tiles = build_tiles(s, keys);
+      std::vector<tam::PTile> ptiles = pack_all(s, tiles, keys);
       tam::Tile *d = nullptr;
       tam::PTile *dp = nullptr;
       cudaError_t e = upload(&d, tiles.data(), tiles.size());
@@ -987,9 +1238,9 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
       if (e != cudaSuccess) {
         cudaFree(d);
         cudaFree(dp);
-        s->shape.tile_items = old;
-        std::vector<tam::Tile> back = build_tiles(s);
-        tam::pack_stages(s->stages, back, old);
+        *field = old;
+        std::vector<tam::Tile> back = build_tiles(s, keys);
+        pack_all(s, back, keys);
         return cuda_fail(s->ctx, e, "re-tiling");
       }
       cudaDeviceSynchronize();  // no fill may still read the old tiles
@@ -1012,6 +1263,15 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
       if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "one_tap is 0 or 1");
       s->shape.one_tap = (int)value;
       return TAM_OK;
+    case TAM_OPT_MERGE_STAGES:
+      if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "merge_stages is 0 or 1");
+      s->shape.merge_stages = (int)value;
+      return TAM_OK;
+    case TAM_OPT_COPY_POINTS:
+      if (value != 1 && value != 2 && value != 4)
+        return fail(s->ctx, TAM_EINVAL, "copy_points is 1, 2 or 4");
+      s->shape.copy_points = (int)value;
+      return TAM_OK;
     default:
       return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
@@ -1024,6 +1284,10 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_THREADS: *value = s->shape.threads; return TAM_OK;
     case TAM_OPT_INT_MUL: *value = s->shape.int_mul; return TAM_OK;
     case TAM_OPT_ONE_TAP: *value = s->shape.one_tap; return TAM_OK;
+    case TAM_OPT_COPY_POINTS: *value = s->shape.copy_points; return TAM_OK;
+    case TAM_OPT_MERGE_STAGES: *value = s->shape.merge_stages; return TAM_OK;
+    case TAM_OPT_BLOCK_ORDER: *value = s->shape.block_order; return TAM_OK;
+    case TAM_OPT_PATH_TILES: *value = s->shape.path_tiles; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
 }

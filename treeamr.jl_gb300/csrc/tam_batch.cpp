@@ -31,12 +31,14 @@ struct tam_batch {
   bool needs_rotvars = false, has_bounded = false;
   std::vector<tam::DevGroup> groups;
   std::vector<int32_t> h_tb;
+  std::vector<int32_t> h_csingle, h_perm;  // the concatenated pools, for the tiling
   std::vector<tam::Stage> stages;
   tam::LaunchShape shape;
   tam::DevGroup *d_groups = nullptr;
   int32_t *d_tb = nullptr, *d_sb = nullptr, *d_srcstart = nullptr, *d_cls = nullptr;
   int32_t *d_csingle = nullptr, *d_perm = nullptr;
   void *d_weights = nullptr, *d_wtab = nullptr;
+  uint64_t *d_wshort = nullptr;
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
   tam::Member *d_members = nullptr;
@@ -89,6 +91,7 @@ void free_batch_device(tam_batch *b) {
   cudaFree(b->d_cls);
   cudaFree(b->d_weights);
   cudaFree(b->d_wtab);
+  cudaFree(b->d_wshort);
   cudaFree(b->d_tiles);
   cudaFree(b->d_ptiles);
   cudaFree(b->d_members);
@@ -105,6 +108,7 @@ void free_batch_device(tam_batch *b) {
   b->d_groups = nullptr;
   b->d_tb = b->d_sb = b->d_srcstart = b->d_cls = nullptr;
   b->d_weights = b->d_wtab = nullptr;
+  b->d_wshort = nullptr;
   b->d_tiles = nullptr;
   b->d_members = nullptr;
   b->d_csingle = b->d_perm = nullptr;
@@ -114,8 +118,10 @@ void free_batch_device(tam_batch *b) {
 
 // Every stage tag's tiles across all members: per member the transfers by
 // target block, unit copies of every member first, then the stencils.
-std::vector<tam::Tile> batch_tiles(tam_batch *b) {
+std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys) {
   std::vector<tam::Tile> tiles;
+  keys.clear();
+  tam::StencilRuns runs;
   const int ti = b->shape.tile_items;
   for (tam::Stage &st : b->stages) {
     st.tile0 = (int64_t)tiles.size();
@@ -133,16 +139,45 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b) {
       if (x.member != y.member) return x.member < y.member;
       return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
     });
-    for (int pass = 0; pass < 3; ++pass) {
+    for (int pass = 0; pass < 2; ++pass) {
       for (const Entry &e : entries) {
         const tam::DevGroup &g = b->groups[e.group];
         if (tam::tile_pass(g) != pass) continue;
         const int box = g.n[0] * g.n[1] * g.n[2];
-        for (int i0 = 0; i0 < box; i0 += ti)
+        for (int i0 = 0; i0 < box; i0 += ti) {
           tiles.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+          keys.push_back(0);
+        }
       }
       if (pass == 0) st.ncopy0 = (int64_t)tiles.size() - st.tile0;
       if (pass == 1) st.ncopy = (int64_t)tiles.size() - st.tile0;
+    }
+    // the stencils by their path through the kernel (tam::StencilRuns)
+    std::vector<tam::Tile> sten;
+    std::vector<uint16_t> skeys;
+    for (const Entry &e : entries) {
+      const tam::DevGroup &g = b->groups[e.group];
+      if (tam::tile_pass(g) != 2) continue;
+      if (!b->shape.path_tiles) {  // by target block alone: one key
+        const int box = g.n[0] * g.n[1] * g.n[2];
+        for (int i0 = 0; i0 < box; i0 += ti) {
+          sten.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+          skeys.push_back(0);
+        }
+        continue;
+      }
+      if (!runs.cache.count(e.group))
+        tam::StencilRuns::of(g, b->h_csingle.data(), b->h_perm.data(), b->D,
+                             runs.cache[e.group]);
+      runs.tiles(e.group, e.transfer, ti, sten, skeys);
+    }
+    std::vector<size_t> order(sten.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t x, size_t y) { return skeys[x] < skeys[y]; });
+    for (size_t i : order) {
+      tiles.push_back(sten[i]);
+      keys.push_back(skeys[i]);
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
   }
@@ -287,8 +322,16 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
     b->stages.push_back(st);
   }
   b->h_tb = tb;
-  std::vector<tam::Tile> tiles = batch_tiles(b);
-  std::vector<tam::PTile> ptiles = tam::pack_stages(b->stages, tiles, b->shape.tile_items);
+  b->h_csingle = csingle;
+  b->h_perm = perm;
+  b->shape.path_tiles = b->dtype == TAM_F64 ? 1 : 0;
+  std::vector<uint16_t> keys;
+  std::vector<tam::Tile> tiles = batch_tiles(b, keys);
+  std::vector<tam::PTile> ptiles =
+      tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
+  std::vector<uint64_t> wshort;
+  if (b->dtype == TAM_F64) wshort = tam::short_weights(wtab);
+  if (wshort.empty()) wshort.push_back(0);
   cudaError_t e;
   if ((e = tam::side_create(b->side)) != cudaSuccess ||
       (e = up(&b->d_ptiles, ptiles.data(), ptiles.size())) != cudaSuccess ||
@@ -301,6 +344,7 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
       (e = up(&b->d_perm, perm.data(), perm.size())) != cudaSuccess ||
       (e = up((unsigned char **)&b->d_weights, weights.data(), weights.size())) != cudaSuccess ||
       (e = up((unsigned char **)&b->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
+      (e = up(&b->d_wshort, wshort.data(), wshort.size())) != cudaSuccess ||
       (e = up(&b->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
       (e = up(&b->d_members, b->layout.data(), b->layout.size())) != cudaSuccess ||
       (e = up(&b->d_solos, b->h_solos.data(), b->h_solos.size())) != cudaSuccess ||
@@ -343,7 +387,8 @@ int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nv
   if (!guard.ok) return bfail(b->ctx, TAM_ECUDA, "cannot make the context's device current");
   const tam::SchedArgs args{b->d_groups,  b->d_tb,      b->d_sb,          b->d_srcstart,
                             b->d_weights, b->d_cls,     b->d_wtab,        b->shape.int_mul,
-                            b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap};
+                            b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap,
+                            b->shape.copy_points, b->d_wshort};
   const int S[3] = {1, 1, 1};  // each member's own, from the member table
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
@@ -438,13 +483,19 @@ int tam_batch_device_status(tam_batch *b, void *stream, int32_t *code) {
 
 int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (!b) return TAM_EINVAL;
-  if (option == TAM_OPT_TILE_ITEMS) {
-    if (value < 16 || value > 4096) return bfail(b->ctx, TAM_EINVAL, "tile items must be in 16..4096");
+  if (option == TAM_OPT_TILE_ITEMS || option == TAM_OPT_PATH_TILES) {
+    int *field = option == TAM_OPT_TILE_ITEMS ? &b->shape.tile_items : &b->shape.path_tiles;
+    if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
+      return bfail(b->ctx, TAM_EINVAL, "tile items must be in 16..4096");
+    if (option == TAM_OPT_PATH_TILES && value != 0 && value != 1)
+      return bfail(b->ctx, TAM_EINVAL, "path_tiles is 0 or 1");
     Guard guard(b->ctx->device);
-    const int old = b->shape.tile_items;
-    b->shape.tile_items = (int)value;
-    std::vector<tam::Tile> tiles = batch_tiles(b);
-    std::vector<tam::PTile> ptiles = tam::pack_stages(b->stages, tiles, b->shape.tile_items);
+    const int old = *field;
+    *field = (int)value;
+    std::vector<uint16_t> keys;
+    std::vector<tam::Tile> tiles = batch_tiles(b, keys);
+    std::vector<tam::PTile> ptiles =
+        tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
     tam::Tile *d = nullptr;
     tam::PTile *dp = nullptr;
     cudaError_t e = up(&d, tiles.data(), tiles.size());
@@ -452,9 +503,9 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
     if (e != cudaSuccess) {
       cudaFree(d);
       cudaFree(dp);
-      b->shape.tile_items = old;
-      std::vector<tam::Tile> back = batch_tiles(b);
-      tam::pack_stages(b->stages, back, old);
+      *field = old;
+      std::vector<tam::Tile> back = batch_tiles(b, keys);
+      tam::pack_stages(b->stages, back, b->shape.tile_items, &keys);
       return bfail(b->ctx, TAM_ECUDA, "re-tiling the batch failed");
     }
     cudaDeviceSynchronize();
@@ -478,6 +529,12 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (option == TAM_OPT_ONE_TAP) {
     if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "one_tap is 0 or 1");
     b->shape.one_tap = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_COPY_POINTS) {
+    if (value != 1 && value != 2 && value != 4)
+      return bfail(b->ctx, TAM_EINVAL, "copy_points is 1, 2 or 4");
+    b->shape.copy_points = (int)value;
     return TAM_OK;
   }
   return bfail(b->ctx, TAM_EINVAL, "unknown option");

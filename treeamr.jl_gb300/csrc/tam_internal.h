@@ -111,14 +111,35 @@ inline int tile_pass(const DevGroup &g) {
 }
 
 // The packing: consecutive tiles of [begin, end) joined while they fit in
-// `target` points and 32 segments.
-void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
-                std::vector<PTile> &out);
+// `target` points and 32 segments and, with `keys`, share their key.
+void pack_tiles(const std::vector<Tile> &tiles, const std::vector<uint16_t> *keys,
+                int64_t begin, int64_t end, int target, std::vector<PTile> &out);
 
 struct Stage;
 // Every stage's packed tiles (sets the stages' ptile0, npcopy, nptiles).
 std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
-                               int target);
+                               int target, const std::vector<uint16_t> *keys = nullptr);
+
+// A stencil group's box points in tile order cut into runs that take the
+// same path through the stencil kernel: the same order class and, in the
+// CPU form of the sum, the same set of dimensions that take one tap.  The
+// key of a run is ((pclass + 2) << 4) | mask (mask 8: no one-tap rows).
+// Tiles cut from runs and packed only with tiles of their key keep every
+// lane of a warp on one path: GB300's FP64 pipe spends the same time on a
+// warp instruction whatever lanes are off.
+struct StencilRuns {
+  struct Run {
+    int first, n;
+    uint16_t key;
+  };
+  std::map<int32_t, std::vector<Run>> cache;  // by group index
+  static void of(const DevGroup &g, const int32_t *csingle, const int32_t *perm, int D,
+                 std::vector<Run> &runs);
+  // Tiles of at most `ti` points of transfer `transfer` of group `gi`
+  // (its runs in `cache`), with their keys.
+  void tiles(int32_t gi, int32_t transfer, int ti, std::vector<Tile> &out,
+             std::vector<uint16_t> &keys);
+};
 
 // A second stream and two events, so a stage's copy and stencil launches run
 // side by side (fork and join on the caller's stream; capturable).
@@ -143,6 +164,8 @@ struct Stage {
   int64_t nptiles = 0;          // all packed tiles of the stage
   int64_t solo0 = 0;            // the stage's solo groups: solos[solo0 .. solo0 + nsolo)
   int64_t nsolo = 0;
+  int32_t span = 1;             // a stage group: the consecutive stages it runs as one
+  int32_t last_tag = 0;         // and the last one's tag
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -203,6 +226,10 @@ struct LaunchShape {
   int threads = 256;        // threads per CTA of the fused kernel
   int int_mul = 0;          // Float64 short-weight multiplies on the integer pipe
   int one_tap = 1;          // the CPU form of the sum (TAM_OPT_ONE_TAP)
+  int copy_points = 1;      // points a lane of the copy kernel takes at once (TAM_OPT_COPY_POINTS)
+  int block_order = 0;      // 0: the blocks' order, 1: a locality order (TAM_OPT_BLOCK_ORDER)
+  int path_tiles = 0;       // stencil tiles grouped by path (TAM_OPT_PATH_TILES)
+  int merge_stages = 1;     // stage groups run as one launch pair (TAM_OPT_MERGE_STAGES)
 };
 
 }  // namespace tam
@@ -238,6 +265,12 @@ struct tam_sched {
   std::vector<int32_t> h_pool_perm;
   std::vector<tam::DevGroup> groups;
   std::vector<tam::Stage> stages;
+  // Stage groups: consecutive prolongation stages that may run as one launch
+  // pair (no point one writes is read or written by another), each a Stage
+  // over the union of their groups, with its own tiles; merged_at[i] is the
+  // group starting at stage i, or -1.
+  std::vector<tam::Stage> merged;
+  std::vector<int32_t> merged_at;
   int64_t ntransfers = 0;
   int64_t points = 0;
   tam::LaunchShape shape;
@@ -249,6 +282,7 @@ struct tam_sched {
   void *d_weights = nullptr;
   int32_t *d_cls = nullptr;
   void *d_wtab = nullptr;
+  uint64_t *d_wshort = nullptr;
   int32_t *d_csingle = nullptr;
   int32_t *d_perm = nullptr;
   tam::Tile *d_tiles = nullptr;
@@ -283,7 +317,15 @@ struct SchedArgs {
   const int32_t *csingle;  // per group, dimension and target row: the single row or -1
   const int32_t *perm;     // per group with singles: the box points in tile order
   int one_tap;             // take the single rows (the CPU form) in the fused kernels
+  int copy_points;         // points a lane of the copy kernel takes at once (1, 2 or 4)
+  const void *wshort;      // Float64: the product table's entries as mul_short takes them
 };
+
+// The Float64 product table `wtab` (doubles) with each entry split as the
+// integer-pipe multiply takes it, one uint64 an entry at the same index:
+// the low word the significand as an integer in [2^23, 2^24), the high word
+// the sign bit and the unbiased exponent plus 8192 (a zero weight: -4096).
+std::vector<uint64_t> short_weights(const std::vector<unsigned char> &wtab);
 
 cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGroup *d_g,
                                const SchedArgs &a, void *work, const void *factors, int nvars,

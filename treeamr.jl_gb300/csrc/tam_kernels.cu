@@ -23,6 +23,7 @@
 //     sectors merge in L2 before they reach HBM.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "tam_internal.h"
 
@@ -98,13 +99,15 @@ struct Args {
   const int32_t *__restrict__ csingle;
   const int32_t *__restrict__ perm;
   int one_tap;
+  int copy_points;
+  const uint2 *__restrict__ wshort;
 };
 
 template <typename T>
 __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
   return Args<T>{a.groups,  a.tb,      a.sb,   a.srcstart, (const T *)a.weights,
                  a.cls,     (const T *)a.wtab, a.int_mul, a.members, a.csingle,
-                 a.perm,    a.one_tap};
+                 a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort};
 }
 
 struct Geom {
@@ -249,6 +252,17 @@ struct ShortW {
   uint32_t wm, wsign;
   int we;
 };
+
+// The same parts from the table of them built at upload (short_weights):
+// {significand, sign | (exponent + 8192)}.
+__device__ __forceinline__ ShortW unpack_short(uint2 q) {
+  ShortW r;
+  r.w = 0.0;
+  r.wm = q.x;
+  r.wsign = q.y & 0x80000000u;
+  r.we = (int)(q.y & 0x7FFFFFFFu) - 8192;
+  return r;
+}
 __device__ __forceinline__ ShortW short_weight(double w) {
   const uint32_t whi = (uint32_t)__double2hiint(w);
   const uint32_t wlo = (uint32_t)__double2loint(w);
@@ -272,21 +286,21 @@ __device__ __forceinline__ ShortW short_weight(double w) {
 // all loads of a chunk issued before its stores; fac[p] is point p's factor
 // column (FACTOR only), x * f + 0 (src/ghosts.jl:369-370).
 template <typename T, int NP, int VC, bool FACTOR>
-__device__ __forceinline__ void copy_points(const T *const (&fac)[NP], const Geom (&o)[NP],
+__device__ __forceinline__ void copy_point_vars(const T *const (&fac)[NP], const Geom (&o)[NP],
                                             const bool (&on)[NP], const T *__restrict__ src,
-                                            T *__restrict__ dst, int nvars) {
-  for (int v0 = 0; v0 < nvars; v0 += VC) {
+                                            T *__restrict__ dst, int vbegin, int vend) {
+  for (int v0 = vbegin; v0 < vend; v0 += VC) {
     T x[NP][VC];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
       for (int j = 0; j < VC; ++j)
-        if (on[p] && v0 + j < nvars) x[p][j] = src[o[p].soff + (v0 + j) * o[p].vstride];
+        if (on[p] && v0 + j < vend) x[p][j] = src[o[p].soff + (v0 + j) * o[p].vstride];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
       for (int j = 0; j < VC; ++j)
-        if (on[p] && v0 + j < nvars)
+        if (on[p] && v0 + j < vend)
           dst[o[p].toff + (v0 + j) * o[p].vstride] =
               FACTOR ? Arith<T>::add(Arith<T>::mul(plus_zero(x[p][j]), __ldg(fac[p] + v0 + j)),
                                      T(0))
@@ -338,8 +352,10 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
         for (int j = 0; j < VC; ++j) acc[j] = 0.0;
         const double *src = work + o.soff + v0 * o.vstride;
         bool bad = false;
+        const uint2 *__restrict__ WS =
+            a.wshort + g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * PD;
         auto tap = [&](int m1, int m2, int m3) {
-          const ShortW sw = short_weight(__ldg(W + (m3 * P2 + m2) * P + m1));
+          const ShortW sw = unpack_short(__ldg(WS + (m3 * P2 + m2) * P + m1));
           const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
           for (int j = 0; j < VC; ++j)
@@ -611,16 +627,17 @@ __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int ns
   return p;
 }
 
-// Points a lane of the copy kernel takes at once, and variables per chunk.
-constexpr int kCopyPoints = 1;
+// Variables per chunk of the copy kernel.
 constexpr int kCopyVars = 8;
 
-// The unit-copy tiles of a stage: a light kernel, every variable's load of a
-// point in flight together.  Copies without a factor column run the FACTOR =
-// false form, which holds no floating-point operation at all: with the
-// factor's multiply in the same code the compiler issues it predicated, and
-// on GB300's narrow FP64 pipe that competes with the stencils alongside.
-template <typename T, int D, bool BATCH, bool FACTOR>
+// The unit-copy tiles of a stage: a light kernel, the loads of every
+// variable of NP points a lane in flight together (NP, TAM_OPT_COPY_POINTS,
+// trades registers, and so resident warps, for loads in flight per warp).
+// Copies without a factor column run the FACTOR = false form, which holds
+// no floating-point operation at all: with the factor's multiply in the
+// same code the compiler issues it predicated, and on GB300's narrow FP64
+// pipe that competes with the stencils alongside.
+template <typename T, int D, bool BATCH, bool FACTOR, int NP>
 __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict__ tiles,
                                                          const PTile *__restrict__ ptiles,
                                                          int64_t nptiles, Args<T> a,
@@ -636,13 +653,13 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
     Tile seg;
     int pref;
     load_segments(tiles, pt, lane, seg, pref);
-    // kCopyPoints points a lane: their loads in flight together
-    for (int base = 0; base < pt.nitems; base += 32 * kCopyPoints) {
-      Geom o[kCopyPoints];
-      bool on[kCopyPoints];
-      const T *fac[kCopyPoints];
+    // NP points a lane: their loads in flight together
+    for (int base = 0; base < pt.nitems; base += 32 * NP) {
+      Geom o[NP];
+      bool on[NP];
+      const T *fac[NP];
 #pragma unroll
-      for (int p = 0; p < kCopyPoints; ++p) {
+      for (int p = 0; p < NP; ++p) {
         const int k = base + 32 * p + lane;
         SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
         on[p] = k < pt.nitems;
@@ -662,7 +679,7 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
         }
         fac[p] = FACTOR ? L.factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
       }
-      copy_points<T, kCopyPoints, kCopyVars, FACTOR>(fac, o, on, src, dst, nvars);
+      copy_point_vars<T, NP, kCopyVars, FACTOR>(fac, o, on, src, dst, 0, nvars);
     }
   }
 }
@@ -734,8 +751,15 @@ cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, con
   if (n <= 0) return cudaSuccess;
   const int wpb = threads / 32;
   const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
-  fused_copy_kernel<T, D, BATCH, FACTOR><<<(unsigned)blocks, threads, 0, stream>>>(
-      tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  if (a.copy_points >= 4)
+    fused_copy_kernel<T, D, BATCH, FACTOR, 4><<<(unsigned)blocks, threads, 0, stream>>>(
+        tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  else if (a.copy_points == 2)
+    fused_copy_kernel<T, D, BATCH, FACTOR, 2><<<(unsigned)blocks, threads, 0, stream>>>(
+        tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  else
+    fused_copy_kernel<T, D, BATCH, FACTOR, 1><<<(unsigned)blocks, threads, 0, stream>>>(
+        tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
   return cudaSuccess;
 }
 
@@ -1047,12 +1071,29 @@ cudaError_t launch_solo(int dtype, int D, const SoloGroup *turns, int64_t n,
                                 rotvars, nvars, S, err, stream);
 }
 
-void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int target,
-                std::vector<PTile> &out) {
+std::vector<uint64_t> short_weights(const std::vector<unsigned char> &wtab) {
+  std::vector<uint64_t> out(wtab.size() / 8);
+  for (size_t i = 0; i < out.size(); ++i) {
+    uint64_t b;
+    memcpy(&b, wtab.data() + 8 * i, 8);
+    const uint32_t whi = (uint32_t)(b >> 32), wlo = (uint32_t)b;
+    const uint32_t wm = (((whi & 0xFFFFFu) | 0x100000u) << 3) | (wlo >> 29);
+    const int ew = (int)((whi >> 20) & 0x7FF);
+    const int we = ew == 0 ? -4096 : ew - 1023;   // as short_weight: a zero is flagged
+    const uint32_t hi = (whi & 0x80000000u) | (uint32_t)(we + 8192);
+    out[i] = ((uint64_t)hi << 32) | wm;
+  }
+  return out;
+}
+
+void pack_tiles(const std::vector<Tile> &tiles, const std::vector<uint16_t> *keys,
+                int64_t begin, int64_t end, int target, std::vector<PTile> &out) {
   int64_t i = begin;
   while (i < end) {
     PTile p{(int32_t)i, 0, 0, 0};
-    while (i < end && p.nseg < 32 && (p.nseg == 0 || p.nitems + tiles[i].nitems <= target)) {
+    while (i < end && p.nseg < 32 &&
+           (p.nseg == 0 || (p.nitems + tiles[i].nitems <= target &&
+                            (!keys || (*keys)[i] == (*keys)[p.seg0])))) {
       p.nitems += tiles[i].nitems;
       ++p.nseg;
       ++i;
@@ -1062,18 +1103,52 @@ void pack_tiles(const std::vector<Tile> &tiles, int64_t begin, int64_t end, int 
 }
 
 std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
-                               int target) {
+                               int target, const std::vector<uint16_t> *keys) {
   std::vector<PTile> out;
   for (Stage &st : stages) {
     st.ptile0 = (int64_t)out.size();
-    pack_tiles(tiles, st.tile0, st.tile0 + st.ncopy0, target, out);
+    pack_tiles(tiles, keys, st.tile0, st.tile0 + st.ncopy0, target, out);
     st.npcopy0 = (int64_t)out.size() - st.ptile0;
-    pack_tiles(tiles, st.tile0 + st.ncopy0, st.tile0 + st.ncopy, target, out);
+    pack_tiles(tiles, keys, st.tile0 + st.ncopy0, st.tile0 + st.ncopy, target, out);
     st.npcopy = (int64_t)out.size() - st.ptile0;
-    pack_tiles(tiles, st.tile0 + st.ncopy, st.tile0 + st.ntiles, target, out);
+    pack_tiles(tiles, keys, st.tile0 + st.ncopy, st.tile0 + st.ntiles, target, out);
     st.nptiles = (int64_t)out.size() - st.ptile0;
   }
   return out;
+}
+
+void StencilRuns::of(const DevGroup &g, const int32_t *csingle, const int32_t *perm, int D,
+                     std::vector<Run> &runs) {
+  runs.clear();
+  const int box = g.n[0] * g.n[1] * g.n[2];
+  const int base = (g.pclass + 2) << 4;
+  auto mask_of = [&](int k) {
+    if (g.perm < 0) return 8;
+    const int p = perm[g.perm + k];
+    const int idx[3] = {p % g.n[0], (p / g.n[0]) % g.n[1], p / (g.n[0] * g.n[1])};
+    int m = 0;
+    for (int d = 0; d < D; ++d)
+      if (csingle[g.csingle[d] + idx[d]] >= 0) m |= 1 << d;
+    return m;
+  };
+  int i0 = 0;
+  while (i0 < box) {
+    const int m = mask_of(i0);
+    int i1 = i0 + 1;
+    while (i1 < box && mask_of(i1) == m) ++i1;
+    runs.push_back({i0, i1 - i0, (uint16_t)(base | m)});
+    i0 = i1;
+  }
+}
+
+void StencilRuns::tiles(int32_t gi, int32_t transfer, int ti, std::vector<Tile> &out,
+                        std::vector<uint16_t> &keys) {
+  const std::vector<Run> &runs = cache[gi];
+  for (const Run &r : runs)
+    for (int i0 = r.first; i0 < r.first + r.n; i0 += ti) {
+      out.push_back({gi, transfer, i0, std::min(ti, r.first + r.n - i0)});
+      keys.push_back(r.key);
+    }
 }
 
 cudaError_t side_create(SideStream &s) {

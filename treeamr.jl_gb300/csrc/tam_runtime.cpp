@@ -107,6 +107,42 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
           bim = im;
         }
       }
+  // then the work's grouping and order, one option at a time from the best
+  // so far: stage groups as one launch or stage by stage, stencil tiles by
+  // path or by block, the blocks' visiting order, points a lane of the copy
+  // kernel
+  int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1;
+  tam_schedule_get_option(s, TAM_OPT_PATH_TILES, &old_pt);
+  tam_schedule_get_option(s, TAM_OPT_BLOCK_ORDER, &old_bo);
+  tam_schedule_get_option(s, TAM_OPT_COPY_POINTS, &old_cp);
+  tam_schedule_get_option(s, TAM_OPT_MERGE_STAGES, &old_ms);
+  if (rc == TAM_OK) {
+    (void)((rc = tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim)) == TAM_OK &&
+           (rc = tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt)) == TAM_OK &&
+           (rc = tam_schedule_set_option(s, TAM_OPT_THREADS, bth)) == TAM_OK);
+  }
+  struct Dim {
+    int32_t option;
+    int values[3];
+    int n;
+    int64_t best;
+  } dims[] = {{TAM_OPT_MERGE_STAGES, {1, 0, 0}, 2, old_ms},
+              {TAM_OPT_PATH_TILES, {0, 1, 0}, 2, old_pt},
+              {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
+              {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp}};
+  for (Dim &dm : dims) {
+    for (int i = 0; i < dm.n && rc == TAM_OK; ++i) {
+      if ((rc = tam_schedule_set_option(s, dm.option, dm.values[i])) != TAM_OK) break;
+      const double ms =
+          time_fill(s, work, nvars, nblocks, factors, reps, (cudaStream_t)stream, a, b, &rc);
+      if (rc != TAM_OK) break;
+      if (ms < best) {
+        best = ms;
+        dm.best = dm.values[i];
+      }
+    }
+    if (rc == TAM_OK) rc = tam_schedule_set_option(s, dm.option, dm.best);
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   // leave the best (or, after a failure, the options the call found)
@@ -114,11 +150,12 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     tam_schedule_set_option(s, TAM_OPT_INT_MUL, old_im);
     tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, old_t);
     tam_schedule_set_option(s, TAM_OPT_THREADS, old_th);
+    tam_schedule_set_option(s, TAM_OPT_PATH_TILES, old_pt);
+    tam_schedule_set_option(s, TAM_OPT_BLOCK_ORDER, old_bo);
+    tam_schedule_set_option(s, TAM_OPT_COPY_POINTS, old_cp);
+    tam_schedule_set_option(s, TAM_OPT_MERGE_STAGES, old_ms);
     return rc;
   }
-  tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim);
-  tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt);
-  tam_schedule_set_option(s, TAM_OPT_THREADS, bth);
   if (tile_items) *tile_items = bt;
   if (threads) *threads = bth;
   if (int_mul) *int_mul = bim;

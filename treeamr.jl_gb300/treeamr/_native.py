@@ -233,6 +233,8 @@ def _declare(lib: C.CDLL):
     lib.tam_schedule_free.restype = None
     lib.tam_schedule_info.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                                       C.POINTER(i32)]
+    lib.tam_schedule_stage_groups.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
+    lib.tam_schedule_stage_groups.restype = C.c_int
     for name in ("tam_fill", "tam_fill_plain", "tam_fill_adjoint", "tam_fill_adjoint_static"):
         if not hasattr(lib, name):
             continue

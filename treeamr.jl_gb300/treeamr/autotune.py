@@ -3,8 +3,11 @@
 The reference has no tuning: its device fill is one launch per group with
 KernelAbstractions' default workgroup.  Here each uploaded schedule carries
 launch options (``tam_schedule_set_option``) that change speed but never a
-result: the box points per warp tile, the threads per CTA, and whether the
-Float64 multiplies by short weight products run on the integer pipe.  The
+result: the box points per warp tile, the threads per CTA, whether the
+Float64 multiplies by short weight products run on the integer pipe, and the
+grouping and order of the work (stencil tiles grouped by their path through
+the kernel or by target block, the order the blocks are visited in, points
+a lane of the copy kernel takes at once).  The
 tuner times every candidate on the caller's own field set (CUDA events on the
 fill's stream, best of a few fills after a warm-up), keeps the fastest, and
 caches the choice per schedule and variable count.  The default grid runs in
@@ -66,6 +69,9 @@ def autotune(fs: FieldSet, sched: GhostSchedule, *, reps: int = 3,
         from . import _native
         _native.check(rc, ds.ctx, "tam_autotune")
         best = {"tile_items": out[0].value, "threads": out[1].value, "int_mul": out[2].value}
+        opts = ds.options()
+        for k in ("merge_stages", "path_tiles", "block_order", "copy_points"):
+            best[k] = opts[k]
         cache[key] = dict(best)
         sched._tuned_ms = ms.value
         return dict(best)

@@ -110,6 +110,14 @@ class DeviceSchedule:
                 scratch.numel() * scratch.element_size(), C.c_void_p(s.cuda_stream))
         _native.check(rc, self.ctx, "tam_fill_adjoint")
 
+    def stage_groups(self):
+        """(stage groups, stages they hold): consecutive prolongation stages a
+        fill runs as one launch pair (``tam_schedule_stage_groups``)."""
+        g, n = C.c_int32(), C.c_int32()
+        _native.check(self.lib.tam_schedule_stage_groups(self.handle, C.byref(g), C.byref(n)),
+                      self.ctx, "tam_schedule_stage_groups")
+        return g.value, n.value
+
     def adjoint_scratch_bytes(self, nvars: int) -> int:
         b = C.c_size_t()
         _native.check(self.lib.tam_adjoint_scratch_bytes(self.handle, nvars, C.byref(b)),
@@ -118,7 +126,8 @@ class DeviceSchedule:
 
     # one_tap picks the form of the sum (1: the reference's CPU form, 0: its
     # device form; the same bits for finite data), the others speed only.
-    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4}
+    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
+               "block_order": 6, "path_tiles": 7, "merge_stages": 8}
 
     def set_option(self, name: str, value: int):
         _native.check(self.lib.tam_schedule_set_option(self.handle, self.OPTIONS[name], int(value)),
