@@ -68,14 +68,18 @@ def parse():
     ap.add_argument("--options", default=None,
                     help="fixed launch options instead of the autotuner's, e.g. "
                          "tile_items=64,threads=128,int_mul=1")
-    ap.add_argument("--workload", choices=["sphere", "walls"], default="walls",
-                    help="walls: the headline line (the walls mesh); sphere: time only the "
-                         "sphere mesh and print its entry")
+    ap.add_argument("--workload", choices=["sphere", "walls", "batch"], default="walls",
+                    help="walls: the headline line (the walls mesh); sphere, batch: time only "
+                         "the sphere mesh or the batch of forests and print its entry")
+    ap.add_argument("--forests", type=int, default=64,
+                    help="forests of the batch (64 as stated; fewer for profiling)")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float64",
                     help="element type of the walls mesh")
-    ap.add_argument("--sector-minimum", type=int, default=None, metavar="TAG",
-                    help="with --workload walls: count, on the CPU, the 32-byte sectors the "
-                         "unit copies of stage TAG read and write, print them and exit")
+    ap.add_argument("--sector-minimum", default=None, metavar="TAG",
+                    help="count, on the CPU, the 32-byte sectors the unit copies of stage TAG "
+                         "of the walls mesh read and write, print them and exit; 'all': every "
+                         "stage, stencils with their whole source windows, and the whole fill's "
+                         "least traffic against its algorithmic bytes")
     return ap.parse_args()
 
 
@@ -180,7 +184,7 @@ def measure_batch(dev, timed, args, peak):
     import torch
     from treeamr import fill_ghosts, meshes
     from treeamr.wave import WaveSolver
-    fss, scheds, batch = meshes.forest_batch_setup(device=dev)
+    fss, scheds, batch = meshes.forest_batch_setup(n=args.forests, device=dev)
     g = torch.Generator(device=dev).manual_seed(9)
     batch.arena.uniform_(-1.0, 1.0, generator=g)
     esize = 4
@@ -189,6 +193,29 @@ def measure_batch(dev, timed, args, peak):
         batch.fill()
     steps = max(3, args.steps // 2)
     ms = timed(batch.fill, steps)
+    # each stage's launches for every forest, CUDA events on the launching stream
+    stream = torch.cuda.current_stream(dev)
+    tags = sorted({gr.stage for s in scheds for gr in s.groups})
+    evs = []
+    for _ in range(3):
+        for tag in tags:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            batch._run("tam_batch_fill_ex", batch.arena, tag, tag, stream)
+            b.record(stream)
+            evs.append((tag, a, b))
+    torch.cuda.synchronize(dev)
+    stage_ms = {}
+    for tag, a, b in evs:
+        stage_ms.setdefault(str(tag), []).append(a.elapsed_time(b))
+    stage_ms = {k: statistics.mean(v) for k, v in stage_ms.items()}
+    stage_bytes = {str(tag): 2 * esize * batch.nvars * sum(
+        int(np.prod(gr.boxsize())) * gr.ntransfers() for s in scheds for gr in s.groups
+        if gr.stage == tag) for tag in tags}
+    if args.workload == "batch":
+        return {"forests": len(fss), "blocks": sum(fs.forest.nleaves() for fs in fss),
+                "ms_per_fill": ms, "value": bytes_per_fill / (ms * 1e-3) / 1e9,
+                "stage_ms": stage_ms, "stage_bytes": stage_bytes}
 
     def separate():
         for fs, s in zip(fss, scheds):
@@ -217,6 +244,7 @@ def measure_batch(dev, timed, args, peak):
         "rk4_10_steps": {"graph_ms": graph_ms, "eager_ms": eager_ms,
                          "fills": 40, "dt": solver.dt},
         "adjoint_10_steps_checkpoint_2_ms": bwd_ms,
+        "stage_ms": stage_ms, "stage_bytes": stage_bytes,
         "roofline": {"bound": "hbm", "achieved": bytes_per_fill / (ms * 1e-3) / 1e9,
                      "peak": peak, "unit": "GB/s",
                      "frac": bytes_per_fill / (ms * 1e-3) / 1e9 / peak},
@@ -590,14 +618,16 @@ def footprint_points(sched):
     return int(wr.sum()), int(rd.sum())
 
 
-def sector_minimum(sched, nvars: int, esize: int, tag: int):
-    """The least DRAM traffic of the unit copies of stage ``tag`` that the
-    layout allows: every distinct 32-byte sector they read fetched once, every
-    sector they write stored once, and (with read-modify-write) every partly
-    written sector fetched once too.  Per variable plane, in bytes."""
+def sector_minimum(sched, nvars: int, esize: int, tag: int, stencils: bool = False):
+    """The least DRAM traffic of the unit copies of stage ``tag`` (with
+    ``stencils``, of all its transfers, a stencil reading its whole source
+    window) that the layout allows: every distinct 32-byte sector they read
+    fetched once, every sector they write stored once, and (with
+    read-modify-write) every partly written sector fetched once too.  Per
+    variable plane, in bytes."""
     S1, S2, S3 = (tuple(sched.stored) + (1, 1))[:3]
     vol = S1 * S2 * S3
-    groups = [g for g in sched.groups if g.stage == tag and g.unit()]
+    groups = [g for g in sched.groups if g.stage == tag and (g.unit() or stencils)]
     rd_s = wr_s = part_s = rp_s = 0
     alg = 0
     for v in range(nvars):
@@ -606,8 +636,12 @@ def sector_minimum(sched, nvars: int, esize: int, tag: int):
             st = list(g.stencils) + [None] * (3 - len(g.stencils))
             tx = [np.arange(x.targetfirst - 1, x.targetfirst - 1 + x.ntarget) if x else
                   np.zeros(1, np.int64) for x in st]
-            sx = [np.asarray(x.srcstart, np.int64) - 1 if x else np.zeros(1, np.int64)
-                  for x in st]
+            if g.unit():
+                sx = [np.asarray(x.srcstart, np.int64) - 1 if x else np.zeros(1, np.int64)
+                      for x in st]
+            else:  # the window every column of the group reads
+                sx = [np.arange(int(x.srcstart.min()) - 1, int(x.srcstart.max()) - 1 + x.order)
+                      if x else np.zeros(1, np.int64) for x in st]
             toff = (tx[2][:, None, None] * S2 + tx[1][None, :, None]) * S1 + tx[0][None, None, :]
             soff = (sx[2][:, None, None] * S2 + sx[1][None, :, None]) * S1 + sx[0][None, None, :]
             tb = np.asarray(g.targetblocks, np.int64) - 1
@@ -618,7 +652,7 @@ def sector_minimum(sched, nvars: int, esize: int, tag: int):
             break
         w = np.concatenate(wr) * esize
         r = np.concatenate(rd) * esize
-        alg += (w.size + r.size) * esize
+        alg += 2 * w.size * esize              # a read and a write per point written
         ws, wc = np.unique(w // 32, return_counts=True)
         rs = np.unique(r // 32)
         partial = ws[wc < 32 // esize]
@@ -821,8 +855,18 @@ def main():
         T = np.dtype(args.dtype).type
         f, fs, ops = meshes.walls_setup(T=T, roots=args.roots, levels=args.walls_levels)
         sched = GhostSchedule(fs, ops)
-        out = sector_minimum(sched, fs.nvars, np.dtype(T).itemsize, args.sector_minimum)
-        out.update({"roots": args.roots, "dtype": args.dtype, "blocks": f.nleaves()})
+        esize = np.dtype(T).itemsize
+        if args.sector_minimum == "all":
+            tags = sorted({g.stage for g in sched.groups})
+            per = [sector_minimum(sched, fs.nvars, esize, t, stencils=True) for t in tags]
+            alg = sum(p["algorithmic_bytes"] for p in per)
+            least = sum(p["minimum_bytes_with_rmw"] for p in per)
+            out = {"stages": per, "algorithmic_bytes": alg, "minimum_bytes_with_rmw": least,
+                   "ceiling_frac_of_peak": alg / least}
+        else:
+            out = sector_minimum(sched, fs.nvars, esize, int(args.sector_minimum))
+        out.update({"roots": args.roots, "dtype": args.dtype, "blocks": f.nleaves(),
+                    "levels": args.walls_levels})
         print(json.dumps(out), flush=True)
         return 0
 
@@ -862,6 +906,9 @@ def main():
     if args.workload == "sphere":
         args.fp64_peak = None
         print(json.dumps(measure_sphere(dev, timed, args, peak, world)), flush=True)
+        return 0
+    if args.workload == "batch":
+        print(json.dumps(measure_batch(dev, timed, args, peak)), flush=True)
         return 0
 
     # ---- the headline: the walls mesh (vertex-centred, reflecting low and

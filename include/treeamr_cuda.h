@@ -509,6 +509,16 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
  * hold in all (a whole fill runs `nstages - stages_in_groups + groups`
  * launch pairs).  No reference counterpart beyond stage_groups itself. */
 int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stages_in_groups);
+/* 1: every stencil transfer of a large box (64 points or more, its source
+ * window within 48 KiB a variable) runs in a kernel that stages the window
+ * in shared memory, a CTA a transfer, and sums each point's taps from there;
+ * 0 (the default): every stencil point reads its taps in place.  The same
+ * bits either way. */
+#define TAM_OPT_STAGED 9
+/* 1: a Float64 order-4 stencil point sums two variables at a time (two
+ * independent chains sharing each tap's weight product); 0 (the default):
+ * one at a time.  The same bits either way. */
+#define TAM_OPT_PAIR_VARS 10
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
@@ -516,8 +526,9 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
  * (32 .. 512), TAM_OPT_THREADS (128, 256, 512) and, for Float64,
  * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (best of `reps`
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
- * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_BLOCK_ORDER and
- * TAM_OPT_COPY_POINTS one at a time; leaves the fastest set and returns the first three (the others
+ * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
+ * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER and TAM_OPT_COPY_POINTS one
+ * at a time; leaves the fastest set and returns the first three (the others
  * through tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an own
  * point).  Synchronizes `stream`; re-tiling allocates, so not inside a
  * stream capture.  The reference has no tuning. */

@@ -29,6 +29,7 @@ from _helpers import nanbits
 from oracle import pointwise
 from _props import NTHREADS, _dot, sphere_polynomial_error, walls_properties
 from treeamr import FieldSet, GhostSchedule, Operators, fill_ghosts, meshes
+from treeamr.ghosts import device_schedule
 from treeamr.storage import vertexcentered
 
 pytestmark = pytest.mark.gpu
@@ -68,11 +69,15 @@ def test_sphere_full_bit_exact(cuda_lib, sphere_forest):
     point = pointwise.fill(fs, start.cpu().numpy(), 4, nthreads=NTHREADS)
     assert np.array_equal(nanbits(point), nanbits(expect))
     del point
-    for method in ("fused", "plain"):
+    ds = device_schedule(sched, 0)
+    for method, staged, pair in (("fused", 0, 0), ("fused", 1, 0), ("fused", 0, 1),
+                                 ("plain", 0, 0)):
+        ds.set_option("staged", staged)
+        ds.set_option("pair_vars", pair)
         fs.work.copy_(start)
         fill_ghosts(fs, sched, method=method)
         torch.cuda.synchronize()
-        assert _same(fs.work, expect) == 0, method
+        assert _same(fs.work, expect) == 0, (method, staged, pair)
 
 
 def test_walls_full_bit_exact(cuda_lib, walls_forest):
@@ -88,12 +93,16 @@ def test_walls_full_bit_exact(cuda_lib, walls_forest):
         point = pointwise.fill(fs, start.cpu().numpy(), 4, nthreads=NTHREADS)
         assert np.array_equal(nanbits(point), nanbits(expect)), np.dtype(T).name
         del point
-        for method in ("fused", "plain"):
+        ds = device_schedule(sched, 0)
+        for method, staged, pair in (("fused", 0, 0), ("fused", 1, 0), ("fused", 0, 1),
+                                     ("plain", 0, 0)):
+            ds.set_option("staged", staged)
+            ds.set_option("pair_vars", pair)
             fs.work.copy_(start)
             fill_ghosts(fs, sched, method=method)
             torch.cuda.synchronize()
-            assert _same(fs.work, expect) == 0, (np.dtype(T).name, method)
-        del fs, start, expect
+            assert _same(fs.work, expect) == 0, (np.dtype(T).name, method, staged, pair)
+        del fs, start, expect, ds
         torch.cuda.empty_cache()
 
 

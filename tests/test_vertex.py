@@ -313,9 +313,10 @@ def test_gpu_stage_groups_bit_exact(cuda_lib, T):
     ds = device_schedule(sched, 0)
     assert ds.stage_groups() == _predicted_stage_groups(sched)
     assert ds.stage_groups()[0] >= 1
-    for merge in (1, 0):
+    for merge, staged in ((1, 0), (0, 0), (1, 1), (0, 1)):
         ds.set_option("merge_stages", merge)
+        ds.set_option("staged", staged)
         fs.work.copy_(torch.from_numpy(host))
         fill_ghosts(fs, sched)
         torch.cuda.synchronize()
-        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), merge
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), (merge, staged)

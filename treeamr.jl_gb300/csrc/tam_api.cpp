@@ -81,6 +81,7 @@ void free_sched_device(tam_sched *s) {
   cudaFree(s->d_cls);
   cudaFree(s->d_wtab);
   cudaFree(s->d_wshort);
+  cudaFree(s->d_staged);
   cudaFree(s->d_csingle);
   cudaFree(s->d_perm);
   cudaFree(s->d_err);
@@ -94,6 +95,7 @@ void free_sched_device(tam_sched *s) {
   s->d_cls = nullptr;
   s->d_wtab = nullptr;
   s->d_wshort = nullptr;
+  s->d_staged = nullptr;
   s->d_csingle = s->d_perm = nullptr;
   s->d_err = nullptr;
   s->d_solos = nullptr;
@@ -348,7 +350,7 @@ tam::SchedArgs sched_args(const tam_sched *s) {
   return tam::SchedArgs{s->d_groups, s->d_tb,     s->d_sb,        s->d_srcstart,
                         s->d_weights, s->d_cls,   s->d_wtab,      s->shape.int_mul,
                         nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap,
-                        s->shape.copy_points, s->d_wshort};
+                        s->shape.copy_points, s->d_wshort, s->shape.pair_vars};
 }
 
 // The order in which the fused launches visit target blocks: with
@@ -411,7 +413,7 @@ std::vector<int32_t> block_rank(const tam_sched *s) {
 // the path's key in `keys` (0 for a copy tile).
 void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int32_t> &rank,
               tam::StencilRuns &runs, std::vector<tam::Tile> &tiles,
-              std::vector<uint16_t> &keys) {
+              std::vector<uint16_t> &keys, std::vector<tam::Tile> &staged) {
   const int ti = s->shape.tile_items;
   for (tam::Stage &st : list) {
     st.tile0 = (int64_t)tiles.size();
@@ -461,26 +463,51 @@ void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int
                              runs.cache[e.group]);
       runs.tiles(e.group, e.transfer, ti, sten, skeys);
     }
+    // with TAM_OPT_STAGED, a staged group's tiles go last: the stencil kernel
+    // leaves them to the staged kernel, which takes the group's transfers
+    // whole (the tiles still list every target, for the adjoint's zeroing)
+    const bool staging = s->shape.staged != 0;
+    auto is_staged = [&](size_t i) { return staging && s->groups[sten[i].group].staged; };
     std::vector<size_t> order(sten.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t x, size_t y) { return skeys[x] < skeys[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+      const bool sx = is_staged(x), sy = is_staged(y);
+      return sx != sy ? sy : skeys[x] < skeys[y];
+    });
+    st.nsten = 0;
     for (size_t i : order) {
       tiles.push_back(sten[i]);
       keys.push_back(skeys[i]);
+      if (!is_staged(i)) ++st.nsten;
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
+    st.staged0 = (int64_t)staged.size();
+    st.staged_window = 0;
+    if (staging)
+      for (const Entry &e : entries) {
+        const tam::DevGroup &g = s->groups[e.group];
+        if (tile_pass(g) == 2 && g.staged) {
+          staged.push_back({e.group, e.transfer, 0, g.n[0] * g.n[1] * g.n[2]});
+          st.staged_window =
+              std::max<int64_t>(st.staged_window, (int64_t)g.wn[0] * g.wn[1] * g.wn[2]);
+        }
+      }
+    st.nstaged = (int64_t)staged.size() - st.staged0;
   }
 }
 
-// The tiles of every stage, then of every stage group, in one array.
-std::vector<tam::Tile> build_tiles(tam_sched *s, std::vector<uint16_t> &keys) {
+// The tiles of every stage, then of every stage group, in one array, and
+// their staged transfers in `staged`.
+std::vector<tam::Tile> build_tiles(tam_sched *s, std::vector<uint16_t> &keys,
+                                   std::vector<tam::Tile> &staged) {
   std::vector<tam::Tile> tiles;
   keys.clear();
+  staged.clear();
   tam::StencilRuns runs;
   const std::vector<int32_t> rank = block_rank(s);
-  tiles_of(s, s->stages, rank, runs, tiles, keys);
-  tiles_of(s, s->merged, rank, runs, tiles, keys);
+  tiles_of(s, s->stages, rank, runs, tiles, keys, staged);
+  tiles_of(s, s->merged, rank, runs, tiles, keys, staged);
+  if (staged.empty()) staged.push_back({0, 0, 0, 0});  // a valid pool even when unused
   return tiles;
 }
 
@@ -814,6 +841,28 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
       else
         build_singles<float>(d, h, g, csingle, perm);
     }
+    // the source window, and whether the staged kernel takes the group
+    int64_t wvol = 1;
+    for (int k = 0; k < 3; ++k) {
+      g.wlo[k] = 0;
+      g.wn[k] = 1;
+      if (k >= d->ndim) continue;
+      const tam_stencil &sd = h.stencil[k];
+      int32_t lo = INT32_MAX, hi = INT32_MIN;
+      for (int i = 0; i < sd.ntarget; ++i) {
+        lo = std::min(lo, d->srcstart[sd.srcstart + i]);
+        hi = std::max(hi, d->srcstart[sd.srcstart + i]);
+      }
+      if (sd.ntarget > 0) {
+        g.wlo[k] = lo - 1;
+        g.wn[k] = hi - lo + sd.order;
+      }
+      wvol *= g.wn[k];
+    }
+    const int64_t box = (int64_t)g.n[0] * g.n[1] * g.n[2];
+    g.staged = g.pclass != 0 && h.orientation == 0 && h.bounded == 0 &&
+               box >= tam::kStagedMinBox &&
+               wvol * (d->dtype == TAM_F64 ? 8 : 4) <= tam::kStagedBytes;
   }
 
   // Stages in tag order, and the fused tiles of each: ordered by target
@@ -836,7 +885,8 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
   s->shape.path_tiles = d->dtype == TAM_F64 ? 1 : 0;
   build_stage_groups(s);
   std::vector<uint16_t> keys;
-  std::vector<tam::Tile> tiles = build_tiles(s, keys);
+  std::vector<tam::Tile> staged;
+  std::vector<tam::Tile> tiles = build_tiles(s, keys, staged);
   std::vector<tam::PTile> ptiles = pack_all(s, tiles, keys);
   build_solos(s);
   std::vector<uint64_t> wshort;
@@ -854,6 +904,7 @@ static int schedule_upload(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nso
       (e = upload((unsigned char **)&s->d_weights, weights.data(), weights.size())) !=
           cudaSuccess ||
       (e = upload(&s->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
+      (e = upload(&s->d_staged, staged.data(), staged.size())) != cudaSuccess ||
       (e = upload(&s->d_cls, cls.data(), cls.size())) != cudaSuccess ||
       (e = upload((unsigned char **)&s->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
       (e = upload(&s->d_wshort, wshort.data(), wshort.size())) != cudaSuccess ||
@@ -1087,7 +1138,8 @@ int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, i
       const tam::Stage &m = s->merged[mi];
       e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + m.ptile0,
                                   m.npcopy0, m.npcopy, m.nptiles, args, work, factors, nvars,
-                                  s->S, s->shape.threads, st, &s->side, nullptr);
+                                  s->S, s->shape.threads, st, &s->side, nullptr,
+                                  s->d_staged + m.staged0, m.nstaged, m.staged_window);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage-group launch");
       i += m.span - 1;
       continue;
@@ -1095,7 +1147,9 @@ int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, i
     if (method == TAM_METHOD_FUSED) {
       e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0,
                                   stage.npcopy0, stage.npcopy, stage.nptiles, args, work,
-                                  factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr);
+                                  factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr,
+                                  s->d_staged + stage.staged0, stage.nstaged,
+                                  stage.staged_window);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
     } else {
       for (int32_t gi : stage.groups) {
@@ -1193,7 +1247,7 @@ int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
     cudaError_t e = tam::launch_fused_stage(
         s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
         stage.nptiles, sched_args(s), new_work, nullptr, nvars, s->S, s->shape.threads, st,
-        &s->side, old_work);
+        &s->side, old_work, s->d_staged + stage.staged0, stage.nstaged, stage.staged_window);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "regrid transfer launch");
     if (stage.nsolo > 0) {  // bounded children
       e = tam::launch_solo(s->dtype, s->D, s->d_solos + stage.solo0, stage.nsolo, sched_args(s),
@@ -1216,38 +1270,45 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
   switch (option) {
     case TAM_OPT_TILE_ITEMS:
     case TAM_OPT_BLOCK_ORDER:
-    case TAM_OPT_PATH_TILES: {
+    case TAM_OPT_PATH_TILES:
+    case TAM_OPT_STAGED: {
       int *field = option == TAM_OPT_TILE_ITEMS    ? &s->shape.tile_items
                    : option == TAM_OPT_BLOCK_ORDER ? &s->shape.block_order
-                                                   : &s->shape.path_tiles;
+                   : option == TAM_OPT_PATH_TILES  ? &s->shape.path_tiles
+                                                   : &s->shape.staged;
       if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
         return fail(s->ctx, TAM_EINVAL, "tile items must be in 16..4096");
       if (option != TAM_OPT_TILE_ITEMS && value != 0 && value != 1)
-        return fail(s->ctx, TAM_EINVAL, "block_order and path_tiles are 0 or 1");
+        return fail(s->ctx, TAM_EINVAL, "block_order, path_tiles and staged are 0 or 1");
       if (value == *field) return TAM_OK;
       DeviceGuard guard(s->ctx->device);
       const int old = *field;
       *field = (int)value;
       std::vector<uint16_t> keys;
-      std::vector<tam::Tile> tiles = build_tiles(s, keys);
+      std::vector<tam::Tile> staged;
+      std::vector<tam::Tile> tiles = build_tiles(s, keys, staged);
       std::vector<tam::PTile> ptiles = pack_all(s, tiles, keys);
-      tam::Tile *d = nullptr;
+      tam::Tile *d = nullptr, *dst = nullptr;
       tam::PTile *dp = nullptr;
       cudaError_t e = upload(&d, tiles.data(), tiles.size());
       if (e == cudaSuccess) e = upload(&dp, ptiles.data(), ptiles.size());
+      if (e == cudaSuccess) e = upload(&dst, staged.data(), staged.size());
       if (e != cudaSuccess) {
         cudaFree(d);
         cudaFree(dp);
+        cudaFree(dst);
         *field = old;
-        std::vector<tam::Tile> back = build_tiles(s, keys);
+        std::vector<tam::Tile> back = build_tiles(s, keys, staged);
         pack_all(s, back, keys);
         return cuda_fail(s->ctx, e, "re-tiling");
       }
       cudaDeviceSynchronize();  // no fill may still read the old tiles
       cudaFree(s->d_tiles);
       cudaFree(s->d_ptiles);
+      cudaFree(s->d_staged);
       s->d_tiles = d;
       s->d_ptiles = dp;
+      s->d_staged = dst;
       return TAM_OK;
     }
     case TAM_OPT_THREADS:
@@ -1262,6 +1323,10 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
     case TAM_OPT_ONE_TAP:
       if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "one_tap is 0 or 1");
       s->shape.one_tap = (int)value;
+      return TAM_OK;
+    case TAM_OPT_PAIR_VARS:
+      if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "pair_vars is 0 or 1");
+      s->shape.pair_vars = (int)value;
       return TAM_OK;
     case TAM_OPT_MERGE_STAGES:
       if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "merge_stages is 0 or 1");
@@ -1286,6 +1351,8 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_ONE_TAP: *value = s->shape.one_tap; return TAM_OK;
     case TAM_OPT_COPY_POINTS: *value = s->shape.copy_points; return TAM_OK;
     case TAM_OPT_MERGE_STAGES: *value = s->shape.merge_stages; return TAM_OK;
+    case TAM_OPT_STAGED: *value = s->shape.staged; return TAM_OK;
+    case TAM_OPT_PAIR_VARS: *value = s->shape.pair_vars; return TAM_OK;
     case TAM_OPT_BLOCK_ORDER: *value = s->shape.block_order; return TAM_OK;
     case TAM_OPT_PATH_TILES: *value = s->shape.path_tiles; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");

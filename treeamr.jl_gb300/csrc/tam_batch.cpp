@@ -41,6 +41,7 @@ struct tam_batch {
   uint64_t *d_wshort = nullptr;
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
+  tam::Tile *d_staged = nullptr;
   tam::Member *d_members = nullptr;
   std::vector<tam::SoloGroup> h_solos;  // by stage tag, members in order
   tam::SoloGroup *d_solos = nullptr;
@@ -92,6 +93,7 @@ void free_batch_device(tam_batch *b) {
   cudaFree(b->d_weights);
   cudaFree(b->d_wtab);
   cudaFree(b->d_wshort);
+  cudaFree(b->d_staged);
   cudaFree(b->d_tiles);
   cudaFree(b->d_ptiles);
   cudaFree(b->d_members);
@@ -109,6 +111,7 @@ void free_batch_device(tam_batch *b) {
   b->d_tb = b->d_sb = b->d_srcstart = b->d_cls = nullptr;
   b->d_weights = b->d_wtab = nullptr;
   b->d_wshort = nullptr;
+  b->d_staged = nullptr;
   b->d_tiles = nullptr;
   b->d_members = nullptr;
   b->d_csingle = b->d_perm = nullptr;
@@ -118,9 +121,11 @@ void free_batch_device(tam_batch *b) {
 
 // Every stage tag's tiles across all members: per member the transfers by
 // target block, unit copies of every member first, then the stencils.
-std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys) {
+std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys,
+                                   std::vector<tam::Tile> &staged) {
   std::vector<tam::Tile> tiles;
   keys.clear();
+  staged.clear();
   tam::StencilRuns runs;
   const int ti = b->shape.tile_items;
   for (tam::Stage &st : b->stages) {
@@ -171,16 +176,36 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys) {
                              runs.cache[e.group]);
       runs.tiles(e.group, e.transfer, ti, sten, skeys);
     }
+    // staged groups' tiles last (the staged kernel takes their transfers)
+    const bool staging = b->shape.staged != 0;
+    auto is_staged = [&](size_t i) { return staging && b->groups[sten[i].group].staged; };
     std::vector<size_t> order(sten.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t x, size_t y) { return skeys[x] < skeys[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+      const bool sx = is_staged(x), sy = is_staged(y);
+      return sx != sy ? sy : skeys[x] < skeys[y];
+    });
+    st.nsten = 0;
     for (size_t i : order) {
       tiles.push_back(sten[i]);
       keys.push_back(skeys[i]);
+      if (!is_staged(i)) ++st.nsten;
     }
     st.ntiles = (int64_t)tiles.size() - st.tile0;
+    st.staged0 = (int64_t)staged.size();
+    st.staged_window = 0;
+    if (staging)
+      for (const Entry &e : entries) {
+        const tam::DevGroup &g = b->groups[e.group];
+        if (tam::tile_pass(g) == 2 && g.staged) {
+          staged.push_back({e.group, e.transfer, 0, g.n[0] * g.n[1] * g.n[2]});
+          st.staged_window =
+              std::max<int64_t>(st.staged_window, (int64_t)g.wn[0] * g.wn[1] * g.wn[2]);
+        }
+      }
+    st.nstaged = (int64_t)staged.size() - st.staged0;
   }
+  if (staged.empty()) staged.push_back({0, 0, 0, 0});  // a valid pool even when unused
   return tiles;
 }
 
@@ -326,7 +351,8 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
   b->h_perm = perm;
   b->shape.path_tiles = b->dtype == TAM_F64 ? 1 : 0;
   std::vector<uint16_t> keys;
-  std::vector<tam::Tile> tiles = batch_tiles(b, keys);
+  std::vector<tam::Tile> staged;
+  std::vector<tam::Tile> tiles = batch_tiles(b, keys, staged);
   std::vector<tam::PTile> ptiles =
       tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
   std::vector<uint64_t> wshort;
@@ -346,6 +372,7 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
       (e = up((unsigned char **)&b->d_wtab, wtab.data(), wtab.size())) != cudaSuccess ||
       (e = up(&b->d_wshort, wshort.data(), wshort.size())) != cudaSuccess ||
       (e = up(&b->d_tiles, tiles.data(), tiles.size())) != cudaSuccess ||
+      (e = up(&b->d_staged, staged.data(), staged.size())) != cudaSuccess ||
       (e = up(&b->d_members, b->layout.data(), b->layout.size())) != cudaSuccess ||
       (e = up(&b->d_solos, b->h_solos.data(), b->h_solos.size())) != cudaSuccess ||
       (e = cudaMalloc((void **)&b->d_err, sizeof(int32_t))) != cudaSuccess ||
@@ -388,14 +415,15 @@ int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nv
   const tam::SchedArgs args{b->d_groups,  b->d_tb,      b->d_sb,          b->d_srcstart,
                             b->d_weights, b->d_cls,     b->d_wtab,        b->shape.int_mul,
                             b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap,
-                            b->shape.copy_points, b->d_wshort};
+                            b->shape.copy_points, b->d_wshort, b->shape.pair_vars};
   const int S[3] = {1, 1, 1};  // each member's own, from the member table
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
     cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles + st.ptile0,
                                             st.npcopy0, st.npcopy, st.nptiles, args, arena, factor_arena,
                                             nvars, S, b->shape.threads, (cudaStream_t)stream,
-                                            &b->side, nullptr);
+                                            &b->side, nullptr, b->d_staged + st.staged0,
+                                            st.nstaged, st.staged_window);
     if (e == cudaSuccess && st.nsolo > 0)
       e = tam::launch_solo(b->dtype, b->D, b->d_solos + st.solo0, st.nsolo, args, arena, arena,
                            arena, factor_arena, rotvars, nvars, S, b->d_err,
@@ -483,36 +511,44 @@ int tam_batch_device_status(tam_batch *b, void *stream, int32_t *code) {
 
 int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (!b) return TAM_EINVAL;
-  if (option == TAM_OPT_TILE_ITEMS || option == TAM_OPT_PATH_TILES) {
-    int *field = option == TAM_OPT_TILE_ITEMS ? &b->shape.tile_items : &b->shape.path_tiles;
+  if (option == TAM_OPT_TILE_ITEMS || option == TAM_OPT_PATH_TILES ||
+      option == TAM_OPT_STAGED) {
+    int *field = option == TAM_OPT_TILE_ITEMS   ? &b->shape.tile_items
+                 : option == TAM_OPT_PATH_TILES ? &b->shape.path_tiles
+                                                : &b->shape.staged;
     if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
       return bfail(b->ctx, TAM_EINVAL, "tile items must be in 16..4096");
-    if (option == TAM_OPT_PATH_TILES && value != 0 && value != 1)
-      return bfail(b->ctx, TAM_EINVAL, "path_tiles is 0 or 1");
+    if (option != TAM_OPT_TILE_ITEMS && value != 0 && value != 1)
+      return bfail(b->ctx, TAM_EINVAL, "path_tiles and staged are 0 or 1");
     Guard guard(b->ctx->device);
     const int old = *field;
     *field = (int)value;
     std::vector<uint16_t> keys;
-    std::vector<tam::Tile> tiles = batch_tiles(b, keys);
+    std::vector<tam::Tile> staged;
+    std::vector<tam::Tile> tiles = batch_tiles(b, keys, staged);
     std::vector<tam::PTile> ptiles =
         tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
-    tam::Tile *d = nullptr;
+    tam::Tile *d = nullptr, *dst = nullptr;
     tam::PTile *dp = nullptr;
     cudaError_t e = up(&d, tiles.data(), tiles.size());
     if (e == cudaSuccess) e = up(&dp, ptiles.data(), ptiles.size());
+    if (e == cudaSuccess) e = up(&dst, staged.data(), staged.size());
     if (e != cudaSuccess) {
       cudaFree(d);
       cudaFree(dp);
+      cudaFree(dst);
       *field = old;
-      std::vector<tam::Tile> back = batch_tiles(b, keys);
+      std::vector<tam::Tile> back = batch_tiles(b, keys, staged);
       tam::pack_stages(b->stages, back, b->shape.tile_items, &keys);
       return bfail(b->ctx, TAM_ECUDA, "re-tiling the batch failed");
     }
     cudaDeviceSynchronize();
     cudaFree(b->d_tiles);
     cudaFree(b->d_ptiles);
+    cudaFree(b->d_staged);
     b->d_tiles = d;
     b->d_ptiles = dp;
+    b->d_staged = dst;
     return TAM_OK;
   }
   if (option == TAM_OPT_THREADS) {
@@ -529,6 +565,11 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (option == TAM_OPT_ONE_TAP) {
     if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "one_tap is 0 or 1");
     b->shape.one_tap = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_PAIR_VARS) {
+    if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "pair_vars is 0 or 1");
+    b->shape.pair_vars = (int)value;
     return TAM_OK;
   }
   if (option == TAM_OPT_COPY_POINTS) {

@@ -55,6 +55,13 @@ struct DevGroup {
   int32_t affine;
   int32_t cs0[3];
   int32_t cstep[3];
+  // A stencil group's source window, every transfer's the same in its source
+  // block: rows wlo[d] .. wlo[d] + wn[d] - 1 (0-based stored indices), the
+  // rows its columns read (the staged stencil kernel loads it into shared
+  // memory).  staged: the group's transfers run in that kernel.
+  int32_t wlo[3];
+  int32_t wn[3];
+  int32_t staged;
 };
 
 // A group the fused tiles do not take, run in a launch of its own after its
@@ -166,6 +173,11 @@ struct Stage {
   int64_t nsolo = 0;
   int32_t span = 1;             // a stage group: the consecutive stages it runs as one
   int32_t last_tag = 0;         // and the last one's tag
+  int64_t staged0 = 0;          // its staged stencil transfers: staged[staged0 ..
+  int64_t nstaged = 0;          //   staged0 + nstaged) (tam::Tile, the whole box)
+  int64_t staged_window = 0;    // the largest window of them, one variable, in elements
+  int64_t nsten = 0;            // stencil tiles the stencil kernel takes (the first
+                                //   ones after the copies; the staged ones follow)
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -230,6 +242,8 @@ struct LaunchShape {
   int block_order = 0;      // 0: the blocks' order, 1: a locality order (TAM_OPT_BLOCK_ORDER)
   int path_tiles = 0;       // stencil tiles grouped by path (TAM_OPT_PATH_TILES)
   int merge_stages = 1;     // stage groups run as one launch pair (TAM_OPT_MERGE_STAGES)
+  int staged = 0;           // large stencil boxes from a shared-memory window (TAM_OPT_STAGED)
+  int pair_vars = 0;        // Float64 order-4 stencils two variables a lane (TAM_OPT_PAIR_VARS)
 };
 
 }  // namespace tam
@@ -287,6 +301,7 @@ struct tam_sched {
   int32_t *d_perm = nullptr;
   tam::Tile *d_tiles = nullptr;
   tam::PTile *d_ptiles = nullptr;
+  tam::Tile *d_staged = nullptr;  // staged stencil transfers, by stage then stage group
   tam::SoloGroup *d_solos = nullptr;
   tam::SideStream side;
   int32_t *d_err = nullptr;
@@ -319,6 +334,7 @@ struct SchedArgs {
   int one_tap;             // take the single rows (the CPU form) in the fused kernels
   int copy_points;         // points a lane of the copy kernel takes at once (1, 2 or 4)
   const void *wshort;      // Float64: the product table's entries as mul_short takes them
+  int pair_vars;           // Float64 order-4 stencils: two variables a lane
 };
 
 // The Float64 product table `wtab` (doubles) with each entry split as the
@@ -340,7 +356,16 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                int64_t npcopy0, int64_t npcopy, int64_t nptiles,
                                const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream, SideStream *side, const void *src);
+                               cudaStream_t stream, SideStream *side, const void *src,
+                               const Tile *staged = nullptr, int64_t nstaged = 0,
+                               int64_t staged_window = 0);
+
+// Shared memory a block of the staged stencil kernel holds, and the largest
+// window (in bytes, one variable) a group may have to be staged.
+constexpr int kStagedBytes = 48 * 1024;
+// A stencil group's transfers go to the staged kernel when each holds this
+// many box points or more (smaller ones keep the packed tiles).
+constexpr int kStagedMinBox = 64;
 
 // The solo groups turns[0 .. n) of one stage: a flat launch per group
 // (blockIdx.y), reading `src` for an even orientation and `alt` for an odd

@@ -101,20 +101,22 @@ struct Args {
   int one_tap;
   int copy_points;
   const uint2 *__restrict__ wshort;
+  int pair_vars;
 };
 
 template <typename T>
 __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
   return Args<T>{a.groups,  a.tb,      a.sb,   a.srcstart, (const T *)a.weights,
                  a.cls,     (const T *)a.wtab, a.int_mul, a.members, a.csingle,
-                 a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort};
+                 a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort, a.pair_vars};
 }
 
 struct Geom {
-  int64_t toff;     // element offset of the target point, variable 0
-  int64_t soff;     // element offset of the source window's first point, variable 0
-  int64_t vstride;  // elements between variables
-  int64_t s2, s3;   // strides of dimensions 2 and 3
+  int64_t toff;      // element offset of the target point, variable 0
+  int64_t soff;      // element offset of the source window's first point, variable 0
+  int64_t vstride;   // elements between variables of the target
+  int64_t s2, s3;    // strides of dimensions 2 and 3 of the source
+  int64_t svstride;  // elements between variables of the source (a staged window's own)
 };
 
 template <int D>
@@ -134,6 +136,7 @@ __device__ __forceinline__ Geom geometry(const DevGroup &g, int i1, int i2, int 
            (D >= 2 ? (int64_t)(g.tf[1] + i2) * o.s2 : 0) +
            (D >= 3 ? (int64_t)(g.tf[2] + i3) * o.s3 : 0);
   o.soff = sblock * bstride + b1 + (int64_t)b2 * o.s2 + (int64_t)b3 * o.s3;
+  o.svstride = o.vstride;
   return o;
 }
 
@@ -155,6 +158,7 @@ __device__ __forceinline__ Geom copy_geometry(const DevGroup &g, int i1, int i2,
            (D >= 2 ? (int64_t)(g.tf[1] + i2) * o.s2 : 0) +
            (D >= 3 ? (int64_t)(g.tf[2] + i3) * o.s3 : 0);
   o.soff = sblock * bstride + b1 + (int64_t)b2 * o.s2 + (int64_t)b3 * o.s3;
+  o.svstride = o.vstride;
   return o;
 }
 
@@ -327,7 +331,8 @@ template <typename T, int D, int P, int VC, bool SKIP>
 __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, int i3,
                                             const Geom &o, const Args<T> &a,
                                             const T *__restrict__ work, T *__restrict__ dst,
-                                            const T *__restrict__ factors, int nvars) {
+                                            const T *__restrict__ factors, int nvars,
+                                            int vbegin, int vend) {
   using A = Arith<T>;
   constexpr int P2 = D >= 2 ? P : 1;
   constexpr int P3 = D >= 3 ? P : 1;
@@ -346,11 +351,11 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
     if (g.shortw && a.int_mul) {
       // F64 with short weight products: the multiplies on the integer pipe,
       // only the adds on the FP64 pipe.
-      for (int v0 = 0; v0 < nvars; v0 += VC) {
+      for (int v0 = vbegin; v0 < vend; v0 += VC) {
         double acc[VC];
 #pragma unroll
         for (int j = 0; j < VC; ++j) acc[j] = 0.0;
-        const double *src = work + o.soff + v0 * o.vstride;
+        const double *src = work + (o.soff + v0 * o.svstride);
         bool bad = false;
         const uint2 *__restrict__ WS =
             a.wshort + g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * PD;
@@ -359,8 +364,8 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
           const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
           for (int j = 0; j < VC; ++j)
-            if (v0 + j < nvars) {
-              const double p = mul_short_flag(sw.wm, sw.we, sw.wsign, src[off + j * o.vstride], bad);
+            if (v0 + j < vend) {
+              const double p = mul_short_flag(sw.wm, sw.we, sw.wsign, src[off + j * o.svstride], bad);
               acc[j] = __dadd_rn(acc[j], p);
             }
         };
@@ -389,30 +394,30 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
                 const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
                 for (int j = 0; j < VC; ++j)
-                  if (v0 + j < nvars)
-                    acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.vstride]));
+                  if (v0 + j < vend)
+                    acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.svstride]));
               }
         }
 #pragma unroll
         for (int j = 0; j < VC; ++j)
-          if (v0 + j < nvars)
+          if (v0 + j < vend)
             dst[o.toff + (v0 + j) * o.vstride] =
                 scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
       }
       return;
     }
   }
-  for (int v0 = 0; v0 < nvars; v0 += VC) {
+  for (int v0 = vbegin; v0 < vend; v0 += VC) {
     T acc[VC];
 #pragma unroll
     for (int j = 0; j < VC; ++j) acc[j] = T(0);
-    const T *src = work + o.soff + v0 * o.vstride;
+    const T *src = work + (o.soff + v0 * o.svstride);
     auto tap = [&](int m1, int m2, int m3) {
       const T w = __ldg(W + (m3 * P2 + m2) * P + m1);
       const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
       for (int j = 0; j < VC; ++j)
-        if (v0 + j < nvars) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.vstride]));
+        if (v0 + j < vend) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.svstride]));
     };
 #pragma unroll(SKIP ? 1 : P3)
     for (int m3 = lo3; m3 < hi3; ++m3) {
@@ -428,7 +433,7 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
     }
 #pragma unroll
     for (int j = 0; j < VC; ++j)
-      if (v0 + j < nvars)
+      if (v0 + j < vend)
         dst[o.toff + (v0 + j) * o.vstride] = scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
   }
 }
@@ -440,7 +445,7 @@ __device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2,
                                               const Geom &o, const Args<T> &a,
                                               const T *__restrict__ work, T *__restrict__ dst,
                                               const T *__restrict__ factors, int nvars,
-                                              bool skip) {
+                                              bool skip, int vbegin, int vend) {
   const T *w1 = a.weights + g.w[0] + (int64_t)g.order[0] * i1;
   const T *w2 = a.weights + g.w[1] + (int64_t)g.order[1] * i2;
   const T *w3 = a.weights + g.w[2] + (int64_t)g.order[2] * i3;
@@ -463,8 +468,8 @@ __device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2,
     w2 = w[1];
     w3 = w[2];
   }
-  for (int v = 0; v < nvars; ++v) {
-    T acc = stencil_sum<T, D, 0>(work + soff + v * o.vstride, o.s2, o.s3, w1, w2, w3, ord);
+  for (int v = vbegin; v < vend; ++v) {
+    T acc = stencil_sum<T, D, 0>(work + (soff + v * o.svstride), o.s2, o.s3, w1, w2, w3, ord);
     dst[o.toff + v * o.vstride] = scaled(acc, factors, v, nvars, g.factorcol);
   }
 }
@@ -474,14 +479,58 @@ __device__ __forceinline__ void table_dispatch(const DevGroup &g, int i1, int i2
                                                const Geom &o, const Args<T> &a,
                                                const T *__restrict__ work, T *__restrict__ dst,
                                                const T *__restrict__ factors, int nvars,
-                                               bool skip) {
+                                               bool skip, int vbegin, int vend) {
   if (skip)
-    table_point<T, D, P, VC, true>(g, i1, i2, i3, o, a, work, dst, factors, nvars);
+    table_point<T, D, P, VC, true>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
+                                   vend);
   else
-    table_point<T, D, P, VC, false>(g, i1, i2, i3, o, a, work, dst, factors, nvars);
+    table_point<T, D, P, VC, false>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
+                                    vend);
 }
 
-// Every variable of one box point of one stencil transfer, by the group's class.
+// Variables [vbegin, vend) of one box point of one stencil transfer, by the
+// group's class; `src` with `o` locates the source window (the array
+// itself, or a window staged in shared memory).
+template <typename T, int D>
+__device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int i2, int i3,
+                                                 const Geom &o, const Args<T> &a,
+                                                 const T *__restrict__ src, T *__restrict__ dst,
+                                                 const T *__restrict__ factors, int nvars,
+                                                 int vbegin, int vend) {
+  const bool skip = a.one_tap && g.perm >= 0;
+  // Float64 one variable at a time: the FP64 pipe binds, and the fewer
+  // registers a lane holds the more warps hide the loads' latency.
+  constexpr int VC = sizeof(T) == 8 ? 1 : 4;
+  switch (g.pclass) {
+    case 2:
+      table_dispatch<T, D, 2, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                  vend);
+      break;
+    case 3:
+      table_dispatch<T, D, 3, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                  vend);
+      break;
+    case 4:
+      // Float64 order 4: one variable a lane, or (TAM_OPT_PAIR_VARS) two, whose
+      // sums share each tap's weight and run as two independent chains
+      if (sizeof(T) == 8 && a.pair_vars)
+        table_dispatch<T, D, 4, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                   vend);
+      else
+        table_dispatch<T, D, 4, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                    vend);
+      break;
+    case 6:
+      table_dispatch<T, D, 6, sizeof(T) == 8 ? 1 : 2>(g, i1, i2, i3, o, a, src, dst, factors,
+                                                      nvars, skip, vbegin, vend);
+      break;
+    default:
+      generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin, vend);
+      break;
+  }
+}
+
+// Every variable of one box point of one stencil transfer, read in place.
 template <typename T, int D>
 __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2, int i3,
                                               int64_t tblock, int64_t sblock, const Args<T> &a,
@@ -489,28 +538,7 @@ __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2,
                                               const T *__restrict__ factors, int nvars, int S1,
                                               int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
-  const bool skip = a.one_tap && g.perm >= 0;
-  // Float64 one variable at a time: the FP64 pipe binds, and the fewer
-  // registers a lane holds the more warps hide the loads' latency.
-  constexpr int VC = sizeof(T) == 8 ? 1 : 4;
-  switch (g.pclass) {
-    case 2:
-      table_dispatch<T, D, 2, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
-      break;
-    case 3:
-      table_dispatch<T, D, 3, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
-      break;
-    case 4:
-      table_dispatch<T, D, 4, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
-      break;
-    case 6:
-      table_dispatch<T, D, 6, sizeof(T) == 8 ? 1 : 2>(g, i1, i2, i3, o, a, src, dst, factors,
-                                                      nvars, skip);
-      break;
-    default:
-      generic_point<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip);
-      break;
-  }
+  stencil_dispatch<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, 0, nvars);
 }
 
 // ---- plain: one launch per group, one thread per (point, variable) ---------
@@ -718,6 +746,83 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
   }
 }
 
+// The stencil transfers of large boxes, each from its source window staged in
+// shared memory: a CTA per transfer loads the window (rows of the source
+// block, a warp a row, a few variables at a time) and then every thread
+// takes box points in tile order (the group's points by path), summing its
+// taps from shared memory in the reference's order (src/ghosts.jl:75-118),
+// so the result is the same bits as the in-place kernel's.  The window is
+// what every point's columns read (tam::DevGroup::wlo, wn); in a
+// prolongation each window point serves about P^D / 2^D box points.
+template <typename T, int D, bool BATCH>
+__global__ void __launch_bounds__(256, 4) staged_stencil_kernel(const Tile *__restrict__ items,
+                                                                int64_t nitems, Args<T> a,
+                                                                const T *__restrict__ src,
+                                                                T *__restrict__ dst,
+                                                                const T *__restrict__ factors,
+                                                                int nvars, int S1, int S2,
+                                                                int S3, int kElems) {
+  extern __shared__ __align__(16) unsigned char staged_smem[];
+  T *sm = reinterpret_cast<T *>(staged_smem);
+  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const Tile item = items[it];
+    const DevGroup &g = a.groups[item.group];
+    const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+    const int64_t tblock = __ldg(a.tb + item.transfer) - 1;
+    const int64_t sblock = __ldg(a.sb + item.transfer) - 1;
+    const int wn1 = g.wn[0], wn2 = g.wn[1], wn3 = g.wn[2];
+    const int wvol = wn1 * wn2 * wn3;
+    const int vchunk = max(1, min(nvars, kElems / wvol));
+    const int64_t s2 = L.S1, s3 = (int64_t)L.S1 * L.S2, vol = s3 * L.S3;
+    const T *__restrict__ wsrc =
+        L.src + sblock * nvars * vol + g.wlo[0] + g.wlo[1] * s2 + g.wlo[2] * s3;
+    const int box = g.n[0] * g.n[1] * g.n[2];
+    for (int v0 = 0; v0 < nvars; v0 += vchunk) {
+      const int vc = min(vchunk, nvars - v0);
+      __syncthreads();  // every thread is done with the previous window
+      // the window's points in order, four loads a thread in flight
+      const int nload = vc * wvol;
+      for (int e0 = threadIdx.x; e0 < nload; e0 += 4 * blockDim.x) {
+        T val[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * blockDim.x;
+          if (e < nload) {
+            const int x = e % wn1, r = e / wn1;
+            const int y = r % wn2, rest = r / wn2;
+            const int z = rest % wn3, v = rest / wn3;
+            val[u] = wsrc[(int64_t)(v0 + v) * vol + z * s3 + y * s2 + x];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * blockDim.x;
+          if (e < nload) sm[e] = val[u];
+        }
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < box; k += blockDim.x) {
+        const int pt = g.perm >= 0 ? __ldg(a.perm + g.perm + k) : k;
+        int i1, i2, i3;
+        box_point(g, pt, i1, i2, i3);
+        Geom o;
+        o.s2 = wn1;
+        o.s3 = (int64_t)wn1 * wn2;
+        o.svstride = wvol;
+        o.vstride = vol;
+        const int b1 = __ldg(a.srcstart + g.ss[0] + i1) - 1 - g.wlo[0];
+        const int b2 = D >= 2 ? __ldg(a.srcstart + g.ss[1] + i2) - 1 - g.wlo[1] : 0;
+        const int b3 = D >= 3 ? __ldg(a.srcstart + g.ss[2] + i3) - 1 - g.wlo[2] : 0;
+        // the window holds variables v0 .. v0 + vc - 1 from its start
+        o.soff = b1 + (int64_t)b2 * o.s2 + (int64_t)b3 * o.s3 - (int64_t)v0 * wvol;
+        o.toff = tblock * nvars * vol + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * s2 +
+                 (int64_t)(g.tf[2] + i3) * s3;
+        stencil_dispatch<T, D>(g, i1, i2, i3, o, a, sm, L.dst, L.factors, nvars, v0, v0 + vc);
+      }
+    }
+  }
+}
+
 template <typename T>
 cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const Args<T> &a,
                            T *work, const T *factors, int nvars, const int S[3],
@@ -767,12 +872,13 @@ template <typename T, int D>
 cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
                         int64_t nptiles, const Args<T> &a, const T *src, T *work,
                         const T *factors, int nvars, const int S[3], int threads,
-                        cudaStream_t stream, SideStream *side) {
+                        cudaStream_t stream, SideStream *side, const Tile *staged,
+                        int64_t nstaged, int64_t staged_window_elems) {
   const int wpb = threads / 32;
   const bool batch = a.members != nullptr;
   const int64_t nst = nptiles - npcopy;
   // both present: the stencils on the side stream, alongside the copies
-  const bool fork = side && side->ok() && npcopy > 0 && nst > 0;
+  const bool fork = side && side->ok() && npcopy > 0 && (nst > 0 || nstaged > 0);
   cudaStream_t sst = stream;
   if (fork) {
     cudaError_t e = cudaEventRecord(side->fork, stream);
@@ -788,6 +894,20 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
     else
       fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, sst>>>(
           tiles, ptiles + npcopy, nst, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  }
+  if (nstaged > 0) {
+    // the shared memory a CTA holds: the stage's largest window for one
+    // variable (the staged items' nitems field carries it, in elements),
+    // as many variables at a time as fit twice that
+    const int64_t blocks = std::min<int64_t>(nstaged, (int64_t)1 << 30);
+    const int elems = (int)std::min<int64_t>(2 * staged_window_elems, kStagedBytes / sizeof(T));
+    const size_t bytes = (size_t)elems * sizeof(T);
+    if (batch)
+      staged_stencil_kernel<T, D, true><<<(unsigned)blocks, 256, bytes, sst>>>(
+          staged, nstaged, a, src, work, factors, nvars, S[0], S[1], S[2], elems);
+    else
+      staged_stencil_kernel<T, D, false><<<(unsigned)blocks, 256, bytes, sst>>>(
+          staged, nstaged, a, src, work, factors, nvars, S[0], S[1], S[2], elems);
   }
   if (batch) {
     launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
@@ -814,18 +934,19 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
 template <typename T>
 cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
                            int64_t nptiles, const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
-                           const int S[3], int threads, cudaStream_t stream, SideStream *side) {
-  if (nptiles == 0) return cudaSuccess;
+                           const int S[3], int threads, cudaStream_t stream, SideStream *side,
+                           const Tile *staged, int64_t nstaged, int64_t staged_window) {
+  if (nptiles == 0 && nstaged == 0) return cudaSuccess;
   switch (D) {
     case 1:
       return launch_both<T, 1>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side);
+                               threads, stream, side, staged, nstaged, staged_window);
     case 2:
       return launch_both<T, 2>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side);
+                               threads, stream, side, staged, nstaged, staged_window);
     default:
       return launch_both<T, 3>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side);
+                               threads, stream, side, staged, nstaged, staged_window);
   }
 }
 
@@ -845,15 +966,16 @@ cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile 
                                int64_t npcopy0, int64_t npcopy, int64_t nptiles,
                                const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
-                               cudaStream_t stream, SideStream *side, const void *src) {
+                               cudaStream_t stream, SideStream *side, const void *src,
+                               const Tile *staged, int64_t nstaged, int64_t staged_window) {
   if (!src) src = work;
   if (dtype == TAM_F64)
     return fused_dispatch<double>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<double>(a),
                                   (const double *)src, (double *)work, (const double *)factors,
-                                  nvars, S, threads, stream, side);
+                                  nvars, S, threads, stream, side, staged, nstaged, staged_window);
   return fused_dispatch<float>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<float>(a),
                                (const float *)src, (float *)work, (const float *)factors, nvars,
-                               S, threads, stream, side);
+                               S, threads, stream, side, staged, nstaged, staged_window);
 }
 
 // ---- solo groups: turned across a seam, or bounded ------------------------------
@@ -1111,7 +1233,7 @@ std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Til
     st.npcopy0 = (int64_t)out.size() - st.ptile0;
     pack_tiles(tiles, keys, st.tile0 + st.ncopy0, st.tile0 + st.ncopy, target, out);
     st.npcopy = (int64_t)out.size() - st.ptile0;
-    pack_tiles(tiles, keys, st.tile0 + st.ncopy, st.tile0 + st.ntiles, target, out);
+    pack_tiles(tiles, keys, st.tile0 + st.ncopy, st.tile0 + st.ncopy + st.nsten, target, out);
     st.nptiles = (int64_t)out.size() - st.ptile0;
   }
   return out;

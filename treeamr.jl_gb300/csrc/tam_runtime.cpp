@@ -109,13 +109,16 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
       }
   // then the work's grouping and order, one option at a time from the best
   // so far: stage groups as one launch or stage by stage, stencil tiles by
-  // path or by block, the blocks' visiting order, points a lane of the copy
-  // kernel
-  int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1;
+  // path or by block, large stencil boxes staged in shared memory or read in
+  // place, Float64 variables a lane, the blocks' visiting order, points a
+  // lane of the copy kernel
+  int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1, old_sg = 0, old_pv = 0;
   tam_schedule_get_option(s, TAM_OPT_PATH_TILES, &old_pt);
   tam_schedule_get_option(s, TAM_OPT_BLOCK_ORDER, &old_bo);
   tam_schedule_get_option(s, TAM_OPT_COPY_POINTS, &old_cp);
   tam_schedule_get_option(s, TAM_OPT_MERGE_STAGES, &old_ms);
+  tam_schedule_get_option(s, TAM_OPT_STAGED, &old_sg);
+  tam_schedule_get_option(s, TAM_OPT_PAIR_VARS, &old_pv);
   if (rc == TAM_OK) {
     (void)((rc = tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim)) == TAM_OK &&
            (rc = tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt)) == TAM_OK &&
@@ -128,6 +131,8 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     int64_t best;
   } dims[] = {{TAM_OPT_MERGE_STAGES, {1, 0, 0}, 2, old_ms},
               {TAM_OPT_PATH_TILES, {0, 1, 0}, 2, old_pt},
+              {TAM_OPT_STAGED, {0, 1, 0}, 2, old_sg},
+              {TAM_OPT_PAIR_VARS, {0, 1, 0}, dtype_f64 ? 2 : 1, old_pv},
               {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
               {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp}};
   for (Dim &dm : dims) {
@@ -154,6 +159,8 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     tam_schedule_set_option(s, TAM_OPT_BLOCK_ORDER, old_bo);
     tam_schedule_set_option(s, TAM_OPT_COPY_POINTS, old_cp);
     tam_schedule_set_option(s, TAM_OPT_MERGE_STAGES, old_ms);
+    tam_schedule_set_option(s, TAM_OPT_STAGED, old_sg);
+    tam_schedule_set_option(s, TAM_OPT_PAIR_VARS, old_pv);
     return rc;
   }
   if (tile_items) *tile_items = bt;
