@@ -644,9 +644,16 @@ __device__ __forceinline__ void load_segments(const Tile *__restrict__ tiles, co
 }
 
 __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int k) {
+  // the last segment whose first point is at or before k: a binary search
+  // over the lanes' prefix offsets (increasing, the first one 0), five
+  // shuffles whatever the segment count
   int mine = 0;
-  for (int s = 1; s < nseg; ++s)
-    if (k >= __shfl_sync(0xffffffffu, pref, s)) mine = s;
+#pragma unroll
+  for (int step = 16; step >= 1; step >>= 1) {
+    const int mid = mine + step;
+    const int pm = __shfl_sync(0xffffffffu, pref, mid & 31);
+    if (mid < nseg && k >= pm) mine = mid;
+  }
   SegPoint p;
   p.group = __shfl_sync(0xffffffffu, seg.group, mine);
   p.transfer = __shfl_sync(0xffffffffu, seg.transfer, mine);
