@@ -734,7 +734,14 @@ def measure_sphere(dev, timed, args, peak, world):
     sched = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
     nvars = fs.nvars
     bytes_per_fill = 2 * sched.ghost_items(nvars) * 8
-    tuned = autotune(fs, sched)
+    if args.options:
+        ds0 = device_schedule(sched, dev.index)
+        for kv in args.options.split(","):
+            k, v = kv.split("=")
+            ds0.set_option(k.strip(), int(v))
+        tuned = ds0.options()
+    else:
+        tuned = autotune(fs, sched)
     for _ in range(args.warmup):
         fill_ghosts(fs, sched)
     steps = max(3, args.steps // 2)

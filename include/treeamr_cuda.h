@@ -519,6 +519,14 @@ int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stag
  * independent chains sharing each tap's weight product); 0 (the default):
  * one at a time.  The same bits either way. */
 #define TAM_OPT_PAIR_VARS 10
+/* How a stage's unit copies share the GPU with its stencils: 0 (the
+ * default) the stencil launch first and the copies after it, each with a
+ * CTA for every few tiles; n > 0 the copy launch first with n CTAs per
+ * multiprocessor, walking its tiles grid-strided, and the stencil launch
+ * beside it, whose CTAs fill the rest of every multiprocessor and take over
+ * the copies' room as they finish: memory-bound copies and FP64-bound
+ * stencils on the same multiprocessors at once.  The same bits either way. */
+#define TAM_OPT_COPY_SHARE 11
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
@@ -527,8 +535,8 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
  * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (best of `reps`
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
  * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
- * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER and TAM_OPT_COPY_POINTS one
- * at a time; leaves the fastest set and returns the first three (the others
+ * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER, TAM_OPT_COPY_POINTS and
+ * TAM_OPT_COPY_SHARE (0, 1, 2, 4) one at a time; leaves the fastest set and returns the first three (the others
  * through tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an own
  * point).  Synchronizes `stream`; re-tiling allocates, so not inside a
  * stream capture.  The reference has no tuning. */

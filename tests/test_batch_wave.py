@@ -35,7 +35,8 @@ def test_batch_fill_equals_member_fills(cuda_lib):
         got = batch.member_view(batch.arena, m).cpu().numpy()
         assert np.array_equal(got.view(np.uint32), expect[m].view(np.uint32)), m
     # every grouping of the batch's work gives the same bits
-    for opt, val in (("path_tiles", 1), ("copy_points", 4), ("tile_items", 48), ("staged", 1)):
+    for opt, val in (("path_tiles", 1), ("copy_points", 4), ("tile_items", 48), ("staged", 1),
+                     ("copy_share", 2)):
         batch.set_option(opt, val)
         batch.arena.copy_(start)
         batch.fill()
@@ -165,7 +166,8 @@ def test_native_autotune(cuda_lib):
     fs.work.copy_(torch.from_numpy(host))
     best = autotune(fs, s)
     assert set(best) == {"tile_items", "threads", "int_mul", "merge_stages", "path_tiles",
-                         "staged", "pair_vars", "block_order", "copy_points"} and s._tuned_ms > 0
+                         "staged", "pair_vars", "block_order", "copy_points",
+                         "copy_share"} and s._tuned_ms > 0
     ds = device_schedule(s, 0)
     assert ds.options()["tile_items"] == best["tile_items"]
     fs.work.copy_(torch.from_numpy(host))

@@ -209,13 +209,13 @@ def test_launch_options_change_no_bit(cuda_lib):
     fs.work = torch.from_numpy(host).cuda()
     fs.factors = fs.factors.cuda()
     ds = device_schedule(s, 0)
-    for ti, th, im, cp, bo, pt, ms, sg, pv in ((16, 64, 0, 1, 0, 0, 1, 1, 1),
-                                               (37, 96, 1, 2, 1, 1, 0, 1, 0),
-                                               (512, 512, 1, 4, 0, 1, 1, 0, 1),
-                                               (4096, 128, 0, 2, 1, 0, 0, 1, 1)):
+    for ti, th, im, cp, bo, pt, ms, sg, pv, cs in ((16, 64, 0, 1, 0, 0, 1, 1, 1, 1),
+                                                   (37, 96, 1, 2, 1, 1, 0, 1, 0, 0),
+                                                   (512, 512, 1, 4, 0, 1, 1, 0, 1, 2),
+                                                   (4096, 128, 0, 2, 1, 0, 0, 1, 1, 4)):
         opts = {"tile_items": ti, "threads": th, "int_mul": im, "one_tap": 1,
                 "copy_points": cp, "block_order": bo, "path_tiles": pt, "merge_stages": ms,
-                "staged": sg, "pair_vars": pv}
+                "staged": sg, "pair_vars": pv, "copy_share": cs}
         for k, v in opts.items():
             ds.set_option(k, v)
         assert ds.options() == opts
@@ -227,6 +227,8 @@ def test_launch_options_change_no_bit(cuda_lib):
         ds.set_option("threads", 100)
     with pytest.raises(Exception):
         ds.set_option("copy_points", 3)
+    with pytest.raises(Exception):
+        ds.set_option("copy_share", -1)
 
 
 def test_autotune_keeps_results(cuda_lib):

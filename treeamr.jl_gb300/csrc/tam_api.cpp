@@ -350,7 +350,8 @@ tam::SchedArgs sched_args(const tam_sched *s) {
   return tam::SchedArgs{s->d_groups, s->d_tb,     s->d_sb,        s->d_srcstart,
                         s->d_weights, s->d_cls,   s->d_wtab,      s->shape.int_mul,
                         nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap,
-                        s->shape.copy_points, s->d_wshort, s->shape.pair_vars};
+                        s->shape.copy_points, s->d_wshort, s->shape.pair_vars,
+                        s->shape.copy_share * s->ctx->nsm};
 }
 
 // The order in which the fused launches visit target blocks: with
@@ -1136,20 +1137,17 @@ int tam_fill_ex(tam_sched *s, void *work, const void *alt_work, int32_t nvars, i
         s->merged[mi].last_tag <= last_stage) {
       // a stage group inside the range: one launch pair for all its stages
       const tam::Stage &m = s->merged[mi];
-      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + m.ptile0,
-                                  m.npcopy0, m.npcopy, m.nptiles, args, work, factors, nvars,
-                                  s->S, s->shape.threads, st, &s->side, nullptr,
-                                  s->d_staged + m.staged0, m.nstaged, m.staged_window);
+      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles, m, args, work,
+                                  factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr,
+                                  s->d_staged);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage-group launch");
       i += m.span - 1;
       continue;
     }
     if (method == TAM_METHOD_FUSED) {
-      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0,
-                                  stage.npcopy0, stage.npcopy, stage.nptiles, args, work,
+      e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles, stage, args, work,
                                   factors, nvars, s->S, s->shape.threads, st, &s->side, nullptr,
-                                  s->d_staged + stage.staged0, stage.nstaged,
-                                  stage.staged_window);
+                                  s->d_staged);
       if (e != cudaSuccess) return cuda_fail(s->ctx, e, "fused stage launch");
     } else {
       for (int32_t gi : stage.groups) {
@@ -1244,10 +1242,10 @@ int tam_regrid_transfer(tam_sched *s, const void *old_work, int64_t old_nblocks,
   if (!guard.ok()) return fail(s->ctx, TAM_ECUDA, "cannot make the context's device current");
   cudaStream_t st = (cudaStream_t)stream;
   for (const tam::Stage &stage : s->stages) {
-    cudaError_t e = tam::launch_fused_stage(
-        s->dtype, s->D, s->d_tiles, s->d_ptiles + stage.ptile0, stage.npcopy0, stage.npcopy,
-        stage.nptiles, sched_args(s), new_work, nullptr, nvars, s->S, s->shape.threads, st,
-        &s->side, old_work, s->d_staged + stage.staged0, stage.nstaged, stage.staged_window);
+    cudaError_t e = tam::launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles, stage,
+                                            sched_args(s), new_work, nullptr, nvars, s->S,
+                                            s->shape.threads, st, &s->side, old_work,
+                                            s->d_staged);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "regrid transfer launch");
     if (stage.nsolo > 0) {  // bounded children
       e = tam::launch_solo(s->dtype, s->D, s->d_solos + stage.solo0, stage.nsolo, sched_args(s),
@@ -1337,6 +1335,10 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
         return fail(s->ctx, TAM_EINVAL, "copy_points is 1, 2 or 4");
       s->shape.copy_points = (int)value;
       return TAM_OK;
+    case TAM_OPT_COPY_SHARE:
+      if (value < 0 || value > 32) return fail(s->ctx, TAM_EINVAL, "copy_share is 0..32");
+      s->shape.copy_share = (int)value;
+      return TAM_OK;
     default:
       return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
@@ -1355,6 +1357,7 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_PAIR_VARS: *value = s->shape.pair_vars; return TAM_OK;
     case TAM_OPT_BLOCK_ORDER: *value = s->shape.block_order; return TAM_OK;
     case TAM_OPT_PATH_TILES: *value = s->shape.path_tiles; return TAM_OK;
+    case TAM_OPT_COPY_SHARE: *value = s->shape.copy_share; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
 }

@@ -415,15 +415,15 @@ int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nv
   const tam::SchedArgs args{b->d_groups,  b->d_tb,      b->d_sb,          b->d_srcstart,
                             b->d_weights, b->d_cls,     b->d_wtab,        b->shape.int_mul,
                             b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap,
-                            b->shape.copy_points, b->d_wshort, b->shape.pair_vars};
+                            b->shape.copy_points, b->d_wshort, b->shape.pair_vars,
+                            b->shape.copy_share * b->ctx->nsm};
   const int S[3] = {1, 1, 1};  // each member's own, from the member table
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
-    cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles + st.ptile0,
-                                            st.npcopy0, st.npcopy, st.nptiles, args, arena, factor_arena,
-                                            nvars, S, b->shape.threads, (cudaStream_t)stream,
-                                            &b->side, nullptr, b->d_staged + st.staged0,
-                                            st.nstaged, st.staged_window);
+    cudaError_t e = tam::launch_fused_stage(b->dtype, b->D, b->d_tiles, b->d_ptiles, st, args,
+                                            arena, factor_arena, nvars, S, b->shape.threads,
+                                            (cudaStream_t)stream, &b->side, nullptr,
+                                            b->d_staged);
     if (e == cudaSuccess && st.nsolo > 0)
       e = tam::launch_solo(b->dtype, b->D, b->d_solos + st.solo0, st.nsolo, args, arena, arena,
                            arena, factor_arena, rotvars, nvars, S, b->d_err,
@@ -576,6 +576,11 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
     if (value != 1 && value != 2 && value != 4)
       return bfail(b->ctx, TAM_EINVAL, "copy_points is 1, 2 or 4");
     b->shape.copy_points = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_COPY_SHARE) {
+    if (value < 0 || value > 32) return bfail(b->ctx, TAM_EINVAL, "copy_share is 0..32");
+    b->shape.copy_share = (int)value;
     return TAM_OK;
   }
   return bfail(b->ctx, TAM_EINVAL, "unknown option");

@@ -178,6 +178,8 @@ struct Stage {
   int64_t staged_window = 0;    // the largest window of them, one variable, in elements
   int64_t nsten = 0;            // stencil tiles the stencil kernel takes (the first
                                 //   ones after the copies; the staged ones follow)
+  int64_t np4_0 = 0;            // packed tiles [np4_0, np4_0 + np4) of the stage: the
+  int64_t np4 = 0;              //   run of uniform order-4 stencils (tiles by path)
 };
 
 // The transpose of one group, for the adjoint fill (tam_adjoint.cu): per
@@ -244,6 +246,7 @@ struct LaunchShape {
   int merge_stages = 1;     // stage groups run as one launch pair (TAM_OPT_MERGE_STAGES)
   int staged = 0;           // large stencil boxes from a shared-memory window (TAM_OPT_STAGED)
   int pair_vars = 0;        // Float64 order-4 stencils two variables a lane (TAM_OPT_PAIR_VARS)
+  int copy_share = 0;       // copy CTAs a multiprocessor beside the stencils (TAM_OPT_COPY_SHARE)
 };
 
 }  // namespace tam
@@ -335,6 +338,7 @@ struct SchedArgs {
   int copy_points;         // points a lane of the copy kernel takes at once (1, 2 or 4)
   const void *wshort;      // Float64: the product table's entries as mul_short takes them
   int pair_vars;           // Float64 order-4 stencils: two variables a lane
+  int copy_ctas;           // beside stencils: the copy launch first, at most this grid (0: after)
 };
 
 // The Float64 product table `wtab` (doubles) with each entry split as the
@@ -347,18 +351,19 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
                                const SchedArgs &a, void *work, const void *factors, int nvars,
                                const int S[3], cudaStream_t stream);
 
-// One stage: the packed tiles [0, npcopy) run the copy kernel (those from
-// npcopy0 on with their factor column) and [npcopy, nptiles) the stencil
-// kernel, on `stream` and, when `side` is given and both are present, the
+// One stage `st` (or stage group): its packed tiles (from ptiles +
+// st.ptile0) [0, npcopy) run the copy kernel (those from npcopy0 on with
+// their factor column) and [npcopy, nptiles) the stencil kernel, the run
+// [np4_0, np4_0 + np4) of them in its order-4 form, and its staged
+// transfers (from staged + st.staged0) the staged kernel; on `stream` and,
+// when `side` is given and both copies and stencils are present, the
 // stencils on the side stream alongside.  Sources are read from `src` when
 // given (a regrid's old array), else from `work`.
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
-                               int64_t npcopy0, int64_t npcopy, int64_t nptiles,
-                               const SchedArgs &a, void *work,
+                               const Stage &st, const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side, const void *src,
-                               const Tile *staged = nullptr, int64_t nstaged = 0,
-                               int64_t staged_window = 0);
+                               const Tile *staged);
 
 // Shared memory a block of the staged stencil kernel holds, and the largest
 // window (in bytes, one variable) a group may have to be staged.

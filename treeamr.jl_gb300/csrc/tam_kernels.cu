@@ -25,6 +25,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "tam_internal.h"
 
 namespace tam {
@@ -102,13 +104,15 @@ struct Args {
   int copy_points;
   const uint2 *__restrict__ wshort;
   int pair_vars;
+  int copy_ctas;
 };
 
 template <typename T>
 __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
   return Args<T>{a.groups,  a.tb,      a.sb,   a.srcstart, (const T *)a.weights,
                  a.cls,     (const T *)a.wtab, a.int_mul, a.members, a.csingle,
-                 a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort, a.pair_vars};
+                 a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort, a.pair_vars,
+                 a.copy_ctas};
 }
 
 struct Geom {
@@ -353,33 +357,45 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
       // only the adds on the FP64 pipe.
       for (int v0 = vbegin; v0 < vend; v0 += VC) {
         double acc[VC];
-#pragma unroll
-        for (int j = 0; j < VC; ++j) acc[j] = 0.0;
         const double *src = work + (o.soff + v0 * o.svstride);
         bool bad = false;
         const uint2 *__restrict__ WS =
             a.wshort + g.wtab + (int64_t)((c3 * g.C[1] + c2) * g.C[0] + c1) * PD;
-        auto tap = [&](int m1, int m2, int m3) {
+        // FIRST: the sum's first term, 0 + p, is p itself (the fast path's
+        // p is a nonzero finite number; anything else is flagged and summed
+        // again below), so the sum costs one FP64 add a tap less
+        auto tap = [&](int m1, int m2, int m3, auto first) {
           const ShortW sw = unpack_short(__ldg(WS + (m3 * P2 + m2) * P + m1));
           const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
           for (int j = 0; j < VC; ++j)
             if (v0 + j < vend) {
               const double p = mul_short_flag(sw.wm, sw.we, sw.wsign, src[off + j * o.svstride], bad);
-              acc[j] = __dadd_rn(acc[j], p);
+              acc[j] = decltype(first)::value ? p : __dadd_rn(acc[j], p);
             }
         };
+        using Head = std::true_type;
+        using Rest = std::false_type;
+        auto row = [&](int m2, int m3, bool head) {
+          if (SKIP && hi1 - lo1 == 1) {
+            if (head)
+              tap(lo1, m2, m3, Head{});
+            else
+              tap(lo1, m2, m3, Rest{});
+          } else {
+            if (head)
+              tap(0, m2, m3, Head{});
+            else
+              tap(0, m2, m3, Rest{});
+#pragma unroll
+            for (int m1 = 1; m1 < P; ++m1) tap(m1, m2, m3, Rest{});
+          }
+        };
+        row(lo2, lo3, true);
 #pragma unroll 1
         for (int m3 = lo3; m3 < hi3; ++m3) {
 #pragma unroll 1
-          for (int m2 = lo2; m2 < hi2; ++m2) {
-            if (SKIP && hi1 - lo1 == 1) {
-              tap(lo1, m2, m3);
-            } else {
-#pragma unroll
-              for (int m1 = 0; m1 < P; ++m1) tap(m1, m2, m3);
-            }
-          }
+          for (int m2 = m3 == lo3 ? lo2 + 1 : lo2; m2 < hi2; ++m2) row(m2, m3, false);
         }
         if (bad) {  // a zero, subnormal or special datum, or an out-of-range product
 #pragma unroll
@@ -419,9 +435,11 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
       for (int j = 0; j < VC; ++j)
         if (v0 + j < vend) acc[j] = A::add(acc[j], A::mul(w, src[off + j * o.svstride]));
     };
-#pragma unroll(SKIP ? 1 : P3)
+    // Float64 rows one at a time (a whole unrolled nest holds more
+    // registers than the stencil kernels' budget and spills)
+#pragma unroll(SKIP || sizeof(T) == 8 ? 1 : P3)
     for (int m3 = lo3; m3 < hi3; ++m3) {
-#pragma unroll(SKIP ? 1 : P2)
+#pragma unroll(SKIP || sizeof(T) == 8 ? 1 : P2)
       for (int m2 = lo2; m2 < hi2; ++m2) {
         if (SKIP && hi1 - lo1 == 1) {
           tap(lo1, m2, m3);
@@ -490,8 +508,9 @@ __device__ __forceinline__ void table_dispatch(const DevGroup &g, int i1, int i2
 
 // Variables [vbegin, vend) of one box point of one stencil transfer, by the
 // group's class; `src` with `o` locates the source window (the array
-// itself, or a window staged in shared memory).
-template <typename T, int D>
+// itself, or a window staged in shared memory).  PC = 4: the caller's
+// groups are all of uniform order 4, and only that path is compiled.
+template <typename T, int D, int PC = 0>
 __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int i2, int i3,
                                                  const Geom &o, const Args<T> &a,
                                                  const T *__restrict__ src, T *__restrict__ dst,
@@ -501,6 +520,15 @@ __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int 
   // Float64 one variable at a time: the FP64 pipe binds, and the fewer
   // registers a lane holds the more warps hide the loads' latency.
   constexpr int VC = sizeof(T) == 8 ? 1 : 4;
+  if constexpr (PC == 4) {
+    if (sizeof(T) == 8 && a.pair_vars)
+      table_dispatch<T, D, 4, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                 vend);
+    else
+      table_dispatch<T, D, 4, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
+                                  vend);
+    return;
+  }
   switch (g.pclass) {
     case 2:
       table_dispatch<T, D, 2, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
@@ -531,14 +559,14 @@ __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int 
 }
 
 // Every variable of one box point of one stencil transfer, read in place.
-template <typename T, int D>
+template <typename T, int D, int PC = 0>
 __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2, int i3,
                                               int64_t tblock, int64_t sblock, const Args<T> &a,
                                               const T *__restrict__ src, T *__restrict__ dst,
                                               const T *__restrict__ factors, int nvars, int S1,
                                               int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
-  stencil_dispatch<T, D>(g, i1, i2, i3, o, a, src, dst, factors, nvars, 0, nvars);
+  stencil_dispatch<T, D, PC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, 0, nvars);
 }
 
 // ---- plain: one launch per group, one thread per (point, variable) ---------
@@ -643,21 +671,27 @@ __device__ __forceinline__ void load_segments(const Tile *__restrict__ tiles, co
   pref = incl - seg.nitems;
 }
 
-__device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int k) {
-  // the last segment whose first point is at or before k: a binary search
-  // over the lanes' prefix offsets (increasing, the first one 0), five
-  // shuffles whatever the segment count
-  int mine = 0;
-#pragma unroll
-  for (int step = 16; step >= 1; step >>= 1) {
-    const int mid = mine + step;
-    const int pm = __shfl_sync(0xffffffffu, pref, mid & 31);
-    if (mid < nseg && k >= pm) mine = mid;
-  }
+// The segment of point k = b + lane (the warp's 32 consecutive points from b;
+// kc is k clamped to the tile's last point).  Lane s (1 <= s < nseg) holds
+// the first point pref of segment s, and the prefixes increase: one ballot
+// counts the segments that start at or before b, another those that start
+// within the window (b, b + 31], and only the latter are searched, so a tile
+// of long segments takes no shuffle here and one of short ones at most 31.
+// (The search stays a loop: straight-line forms of it let the compiler
+// schedule the point's loads so early that the kernel needs half again the
+// registers.)
+__device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int lane,
+                                               int b, int kc) {
+  const bool starts = lane >= 1 && lane < nseg;
+  const int before = __popc(__ballot_sync(0xffffffffu, starts && pref <= b));
+  const int inwin = __popc(__ballot_sync(0xffffffffu, starts && pref > b && pref <= b + 31));
+  int mine = before;
+  for (int s = before + 1; s <= before + inwin; ++s)
+    if (kc >= __shfl_sync(0xffffffffu, pref, s)) mine = s;
   SegPoint p;
   p.group = __shfl_sync(0xffffffffu, seg.group, mine);
   p.transfer = __shfl_sync(0xffffffffu, seg.transfer, mine);
-  p.item = __shfl_sync(0xffffffffu, seg.item0, mine) + k - __shfl_sync(0xffffffffu, pref, mine);
+  p.item = __shfl_sync(0xffffffffu, seg.item0, mine) + kc - __shfl_sync(0xffffffffu, pref, mine);
   p.on = true;
   return p;
 }
@@ -696,7 +730,8 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
         const int k = base + 32 * p + lane;
-        SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
+        SegPoint q = find_point(seg, pref, pt.nseg, lane, base + 32 * p,
+                                k < pt.nitems ? k : pt.nitems - 1);
         on[p] = k < pt.nitems;
         const DevGroup &g = a.groups[q.group];
         const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
@@ -719,8 +754,11 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
   }
 }
 
-// The stencil tiles of a stage: one point a lane, every variable.
-template <typename T, int D, bool BATCH>
+// The stencil tiles of a stage: one point a lane, every variable.  PC = 4:
+// tiles of uniform order-4 groups only (a stage's tiles grouped by path hold
+// them in one run), the only path compiled, so that the registers it keeps
+// are its own.
+template <typename T, int D, bool BATCH, int PC>
 __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tiles,
                                                           const PTile *__restrict__ ptiles,
                                                           int64_t nptiles, Args<T> a,
@@ -738,7 +776,7 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
     load_segments(tiles, pt, lane, seg, pref);
     for (int base = 0; base < pt.nitems; base += 32) {
       const int k = base + lane;
-      SegPoint q = find_point(seg, pref, pt.nseg, k < pt.nitems ? k : pt.nitems - 1);
+      SegPoint q = find_point(seg, pref, pt.nseg, lane, base, k < pt.nitems ? k : pt.nitems - 1);
       if (k >= pt.nitems) continue;
       const DevGroup &g = a.groups[q.group];
       const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
@@ -747,7 +785,8 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
       const int item = g.perm >= 0 ? __ldg(a.perm + g.perm + q.item) : q.item;
       int i1, i2, i3;
       box_point(g, item, i1, i2, i3);
-      stencil_point<T, D>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars, L.S1,
+      stencil_point<T, D, PC>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars,
+                              L.S1,
                           L.S2, L.S3);
     }
   }
@@ -859,10 +898,11 @@ cudaError_t plain_dispatch(int D, const DevGroup &g, const DevGroup *d_g, const 
 template <typename T, int D, bool BATCH, bool FACTOR>
 cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, const Args<T> &a,
                           const T *src, T *work, const T *factors, int nvars, const int S[3],
-                          int threads, cudaStream_t stream) {
+                          int threads, cudaStream_t stream, int64_t cap) {
   if (n <= 0) return cudaSuccess;
   const int wpb = threads / 32;
-  const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
+  int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
+  if (cap > 0) blocks = std::min(blocks, cap);
   if (a.copy_points >= 4)
     fused_copy_kernel<T, D, BATCH, FACTOR, 4><<<(unsigned)blocks, threads, 0, stream>>>(
         tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
@@ -876,11 +916,13 @@ cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, con
 }
 
 template <typename T, int D>
-cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
-                        int64_t nptiles, const Args<T> &a, const T *src, T *work,
-                        const T *factors, int nvars, const int S[3], int threads,
-                        cudaStream_t stream, SideStream *side, const Tile *staged,
-                        int64_t nstaged, int64_t staged_window_elems) {
+cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, const Stage &stg,
+                        const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
+                        const int S[3], int threads, cudaStream_t stream, SideStream *side,
+                        const Tile *staged) {
+  const int64_t npcopy0 = stg.npcopy0, npcopy = stg.npcopy, nptiles = stg.nptiles;
+  const int64_t np4_0 = stg.np4_0, np4 = stg.np4;
+  const int64_t nstaged = stg.nstaged, staged_window_elems = stg.staged_window;
   const int wpb = threads / 32;
   const bool batch = a.members != nullptr;
   const int64_t nst = nptiles - npcopy;
@@ -893,14 +935,49 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
     if (e != cudaSuccess) return e;
     sst = side->stream;
   }
-  if (nst > 0) {
-    const int64_t blocks = std::min<int64_t>((nst + wpb - 1) / wpb, (int64_t)1 << 30);
-    if (batch)
-      fused_stage_kernel<T, D, true><<<(unsigned)blocks, threads, 0, sst>>>(
-          tiles, ptiles + npcopy, nst, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  // TAM_OPT_COPY_SHARE: the copies' CTAs resident first, a few a
+  // multiprocessor, and the stencils' around them
+  const bool copies_first = fork && a.copy_ctas > 0;
+  const int64_t cap = copies_first ? a.copy_ctas : 0;
+  auto copies = [&]() {
+    if (batch) {
+      launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
+                                       threads, stream, cap);
+      launch_copies<T, D, true, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
+                                      factors, nvars, S, threads, stream, cap);
+    } else {
+      launch_copies<T, D, false, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
+                                        threads, stream, cap);
+      launch_copies<T, D, false, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
+                                       factors, nvars, S, threads, stream, cap);
+    }
+  };
+  if (copies_first) copies();
+  // the stencil tiles: the order-4 run (tiles grouped by path) in the
+  // kernel compiled for that order alone, the others in the general one
+  auto stencils = [&](int64_t p0, int64_t n, bool four) {
+    if (n <= 0) return;
+    const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
+    const PTile *pt = ptiles + p0;
+    if (batch && four)
+      fused_stage_kernel<T, D, true, 4><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+    else if (batch)
+      fused_stage_kernel<T, D, true, 0><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+    else if (four)
+      fused_stage_kernel<T, D, false, 4><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
     else
-      fused_stage_kernel<T, D, false><<<(unsigned)blocks, threads, 0, sst>>>(
-          tiles, ptiles + npcopy, nst, a, src, work, factors, nvars, S[0], S[1], S[2]);
+      fused_stage_kernel<T, D, false, 0><<<(unsigned)blocks, threads, 0, sst>>>(
+          tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+  };
+  if (nst > 0) {
+    const int64_t f0 = std::min(std::max(np4_0, npcopy), nptiles);
+    const int64_t f1 = std::min(f0 + np4, nptiles);
+    stencils(npcopy, f0 - npcopy, false);
+    stencils(f0, f1 - f0, true);
+    stencils(f1, nptiles - f1, false);
   }
   if (nstaged > 0) {
     // the shared memory a CTA holds: the stage's largest window for one
@@ -916,17 +993,7 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
       staged_stencil_kernel<T, D, false><<<(unsigned)blocks, 256, bytes, sst>>>(
           staged, nstaged, a, src, work, factors, nvars, S[0], S[1], S[2], elems);
   }
-  if (batch) {
-    launch_copies<T, D, true, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
-                                     threads, stream);
-    launch_copies<T, D, true, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
-                                    factors, nvars, S, threads, stream);
-  } else {
-    launch_copies<T, D, false, false>(tiles, ptiles, npcopy0, a, src, work, factors, nvars, S,
-                                      threads, stream);
-    launch_copies<T, D, false, true>(tiles, ptiles + npcopy0, npcopy - npcopy0, a, src, work,
-                                     factors, nvars, S, threads, stream);
-  }
+  if (!copies_first) copies();
   if (fork) {
     cudaError_t e = cudaEventRecord(side->join, side->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, side->join, 0);
@@ -939,21 +1006,21 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, int64_t npcopy0,
 // dependency between them (their targets are disjoint and neither reads a
 // point of the stage's targets).
 template <typename T>
-cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, int64_t npcopy0, int64_t npcopy,
-                           int64_t nptiles, const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
+cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, const Stage &st,
+                           const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
                            const int S[3], int threads, cudaStream_t stream, SideStream *side,
-                           const Tile *staged, int64_t nstaged, int64_t staged_window) {
-  if (nptiles == 0 && nstaged == 0) return cudaSuccess;
+                           const Tile *staged) {
+  if (st.nptiles == 0 && st.nstaged == 0) return cudaSuccess;
   switch (D) {
     case 1:
-      return launch_both<T, 1>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side, staged, nstaged, staged_window);
+      return launch_both<T, 1>(tiles, ptiles, st, a, src, work, factors, nvars, S, threads,
+                               stream, side, staged);
     case 2:
-      return launch_both<T, 2>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side, staged, nstaged, staged_window);
+      return launch_both<T, 2>(tiles, ptiles, st, a, src, work, factors, nvars, S, threads,
+                               stream, side, staged);
     default:
-      return launch_both<T, 3>(tiles, ptiles, npcopy0, npcopy, nptiles, a, src, work, factors, nvars, S,
-                               threads, stream, side, staged, nstaged, staged_window);
+      return launch_both<T, 3>(tiles, ptiles, st, a, src, work, factors, nvars, S, threads,
+                               stream, side, staged);
   }
 }
 
@@ -970,19 +1037,20 @@ cudaError_t launch_plain_group(int dtype, int D, const DevGroup &g, const DevGro
 }
 
 cudaError_t launch_fused_stage(int dtype, int D, const Tile *tiles, const PTile *ptiles,
-                               int64_t npcopy0, int64_t npcopy, int64_t nptiles,
-                               const SchedArgs &a, void *work,
+                               const Stage &st, const SchedArgs &a, void *work,
                                const void *factors, int nvars, const int S[3], int threads,
                                cudaStream_t stream, SideStream *side, const void *src,
-                               const Tile *staged, int64_t nstaged, int64_t staged_window) {
+                               const Tile *staged) {
   if (!src) src = work;
+  ptiles += st.ptile0;
+  staged += st.staged0;
   if (dtype == TAM_F64)
-    return fused_dispatch<double>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<double>(a),
-                                  (const double *)src, (double *)work, (const double *)factors,
-                                  nvars, S, threads, stream, side, staged, nstaged, staged_window);
-  return fused_dispatch<float>(D, tiles, ptiles, npcopy0, npcopy, nptiles, typed<float>(a),
-                               (const float *)src, (float *)work, (const float *)factors, nvars,
-                               S, threads, stream, side, staged, nstaged, staged_window);
+    return fused_dispatch<double>(D, tiles, ptiles, st, typed<double>(a), (const double *)src,
+                                  (double *)work, (const double *)factors, nvars, S, threads,
+                                  stream, side, staged);
+  return fused_dispatch<float>(D, tiles, ptiles, st, typed<float>(a), (const float *)src,
+                               (float *)work, (const float *)factors, nvars, S, threads, stream,
+                               side, staged);
 }
 
 // ---- solo groups: turned across a seam, or bounded ------------------------------
@@ -1240,7 +1308,21 @@ std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Til
     st.npcopy0 = (int64_t)out.size() - st.ptile0;
     pack_tiles(tiles, keys, st.tile0 + st.ncopy0, st.tile0 + st.ncopy, target, out);
     st.npcopy = (int64_t)out.size() - st.ptile0;
-    pack_tiles(tiles, keys, st.tile0 + st.ncopy, st.tile0 + st.ncopy + st.nsten, target, out);
+    // the stencils: with keys (tiles by path, sorted by key) the order-4
+    // run packed on its own, so that its packed tiles are a run too
+    int64_t b4 = st.tile0 + st.ncopy, e4 = b4;
+    const int64_t send = st.tile0 + st.ncopy + st.nsten;
+    if (keys) {
+      auto four = [&](int64_t t) { return ((*keys)[t] >> 4) == 4 + 2; };
+      while (b4 < send && !four(b4) && (*keys)[b4] < ((4 + 2) << 4)) ++b4;
+      e4 = b4;
+      while (e4 < send && four(e4)) ++e4;
+    }
+    pack_tiles(tiles, keys, st.tile0 + st.ncopy, b4, target, out);
+    st.np4_0 = (int64_t)out.size() - st.ptile0;
+    pack_tiles(tiles, keys, b4, e4, target, out);
+    st.np4 = (int64_t)out.size() - st.ptile0 - st.np4_0;
+    pack_tiles(tiles, keys, e4, send, target, out);
     st.nptiles = (int64_t)out.size() - st.ptile0;
   }
   return out;

@@ -111,14 +111,16 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   // so far: stage groups as one launch or stage by stage, stencil tiles by
   // path or by block, large stencil boxes staged in shared memory or read in
   // place, Float64 variables a lane, the blocks' visiting order, points a
-  // lane of the copy kernel
-  int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1, old_sg = 0, old_pv = 0;
+  // lane of the copy kernel, the copies' share of the machine beside the
+  // stencils
+  int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1, old_sg = 0, old_pv = 0, old_cs = 0;
   tam_schedule_get_option(s, TAM_OPT_PATH_TILES, &old_pt);
   tam_schedule_get_option(s, TAM_OPT_BLOCK_ORDER, &old_bo);
   tam_schedule_get_option(s, TAM_OPT_COPY_POINTS, &old_cp);
   tam_schedule_get_option(s, TAM_OPT_MERGE_STAGES, &old_ms);
   tam_schedule_get_option(s, TAM_OPT_STAGED, &old_sg);
   tam_schedule_get_option(s, TAM_OPT_PAIR_VARS, &old_pv);
+  tam_schedule_get_option(s, TAM_OPT_COPY_SHARE, &old_cs);
   if (rc == TAM_OK) {
     (void)((rc = tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim)) == TAM_OK &&
            (rc = tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt)) == TAM_OK &&
@@ -126,7 +128,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   }
   struct Dim {
     int32_t option;
-    int values[3];
+    int values[4];
     int n;
     int64_t best;
   } dims[] = {{TAM_OPT_MERGE_STAGES, {1, 0, 0}, 2, old_ms},
@@ -134,7 +136,8 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
               {TAM_OPT_STAGED, {0, 1, 0}, 2, old_sg},
               {TAM_OPT_PAIR_VARS, {0, 1, 0}, dtype_f64 ? 2 : 1, old_pv},
               {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
-              {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp}};
+              {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp},
+              {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs}};
   for (Dim &dm : dims) {
     for (int i = 0; i < dm.n && rc == TAM_OK; ++i) {
       if ((rc = tam_schedule_set_option(s, dm.option, dm.values[i])) != TAM_OK) break;
@@ -161,6 +164,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     tam_schedule_set_option(s, TAM_OPT_MERGE_STAGES, old_ms);
     tam_schedule_set_option(s, TAM_OPT_STAGED, old_sg);
     tam_schedule_set_option(s, TAM_OPT_PAIR_VARS, old_pv);
+    tam_schedule_set_option(s, TAM_OPT_COPY_SHARE, old_cs);
     return rc;
   }
   if (tile_items) *tile_items = bt;

@@ -163,7 +163,8 @@ class ForestBatch:
 
     def set_option(self, name: str, value: int):
         code = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
-                "path_tiles": 7, "staged": 9, "pair_vars": 10}[name]
+                "path_tiles": 7, "staged": 9, "pair_vars": 10,
+                "copy_share": 11}[name]
         _native.check(self.lib.tam_batch_set_option(self.handle, code, int(value)), self.ctx,
                       f"tam_batch_set_option({name})")
 
