@@ -536,9 +536,10 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
  * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
  * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER, TAM_OPT_COPY_POINTS and
- * TAM_OPT_COPY_SHARE (0, 1, 2, 4) one at a time; leaves the fastest set and returns the first three (the others
- * through tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an own
- * point).  Synchronizes `stream`; re-tiling allocates, so not inside a
+ * TAM_OPT_COPY_SHARE (0, 1, 2, 4) one at a time, twice over; leaves the
+ * fastest set and returns the first three (the others through
+ * tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an
+ * own point).  Synchronizes `stream`; re-tiling allocates, so not inside a
  * stream capture.  The reference has no tuning. */
 int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const void *factors,
                  int32_t reps, void *stream, int64_t *tile_items, int64_t *threads,

@@ -53,6 +53,29 @@ def test_batch_fill_equals_member_fills(cuda_lib):
 
 
 @pytest.mark.parametrize("T", [np.float32, np.float64])
+def test_batch_autotune_keeps_results(cuda_lib, T):
+    """The batch's tuner leaves a set of its choices, and the fill with them
+    is each member's oracle fill bit for bit."""
+    fss, scheds, batch = _small_batch(T, n=4, seed=11)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    batch.arena.uniform_(-1, 1, generator=g)
+    start = batch.arena.clone()
+    best = batch.autotune(reps=1, sweeps=1)
+    assert set(best) >= {name for name, _ in batch.TUNE} and batch.tuned_ms > 0
+    for name, values in batch.TUNE:
+        assert best[name] in values
+    batch.arena.copy_(start)
+    batch.fill()
+    torch.cuda.synchronize()
+    bits = np.uint32 if T == np.float32 else np.uint64
+    for m, (fs, s) in enumerate(zip(fss, scheds)):
+        host = batch.member_view(start, m).cpu().numpy().copy()
+        expect = oracle.fill(s, host, fs.nvars, fs.factors_host)
+        got = batch.member_view(batch.arena, m).cpu().numpy()
+        assert np.array_equal(got.view(bits), expect.view(bits)), m
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float64])
 def test_batch_adjoint_equals_member_adjoints(cuda_lib, T):
     """The batched adjoint (one launch per pass and stage for every forest)
     equals each member's own adjoint bit for bit, and its transpose identity

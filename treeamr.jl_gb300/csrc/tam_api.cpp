@@ -131,8 +131,13 @@ int validate(tam_ctx *ctx, const tam_schedule_desc *d, int64_t nsource) {
   if (d->nfactorcols != maxcols && d->nfactorcols != 4 * maxcols)
     return fail(ctx, TAM_EINVAL, "nfactorcols must be 3^D, or 4 * 3^D over a seam");
   maxcols = d->nfactorcols;
-  for (int k = 0; k < d->ndim; ++k)
+  int64_t vol = 1;
+  for (int k = 0; k < d->ndim; ++k) {
     if (d->stored[k] < 1) return fail(ctx, TAM_EINVAL, "stored extents must be positive");
+    vol = std::min<int64_t>(vol * d->stored[k], (int64_t)INT32_MAX + 1);
+  }
+  // the kernels address within a block's variable in 32 bits
+  if (vol > INT32_MAX) return fail(ctx, TAM_EUNSUPPORTED, "a block of 2^31 points or more");
   if (nsource < 0 || nsource > INT32_MAX) return fail(ctx, TAM_EINVAL, "bad source block count");
   for (int64_t t = 0; t < d->ntransfers; ++t) {
     if (d->targetblocks[t] < 1 || d->targetblocks[t] > d->nblocks ||

@@ -680,14 +680,19 @@ __device__ __forceinline__ void load_segments(const Tile *__restrict__ tiles, co
 // (The search stays a loop: straight-line forms of it let the compiler
 // schedule the point's loads so early that the kernel needs half again the
 // registers.)
-__device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int lane,
-                                               int b, int kc) {
+__device__ __forceinline__ int find_segment(int pref, int nseg, int lane, int b, int kc) {
   const bool starts = lane >= 1 && lane < nseg;
   const int before = __popc(__ballot_sync(0xffffffffu, starts && pref <= b));
   const int inwin = __popc(__ballot_sync(0xffffffffu, starts && pref > b && pref <= b + 31));
   int mine = before;
   for (int s = before + 1; s <= before + inwin; ++s)
     if (kc >= __shfl_sync(0xffffffffu, pref, s)) mine = s;
+  return mine;
+}
+
+__device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int nseg, int lane,
+                                               int b, int kc) {
+  const int mine = find_segment(pref, nseg, lane, b, kc);
   SegPoint p;
   p.group = __shfl_sync(0xffffffffu, seg.group, mine);
   p.transfer = __shfl_sync(0xffffffffu, seg.transfer, mine);
@@ -696,12 +701,66 @@ __device__ __forceinline__ SegPoint find_point(const Tile &seg, int pref, int ns
   return p;
 }
 
-// Variables per chunk of the copy kernel.
+// A segment of a batch's copy tile as its points need it, formed once per
+// segment (by the lane that holds it) and kept in shared memory for the
+// warp: the group's, the transfer's and the member's geometry folded into two
+// base offsets and per-row strides, so that a point costs its segment's
+// lookup, four shared loads and a few integer multiply-adds.  (A batch's
+// blocks are small and its tiles hold many short segments; one schedule's
+// tiles of long boxes do better forming each point's geometry from its
+// group's loads, which broadcast across the warp.)
+struct CopySeg {
+  int64_t toff;        // target element of box point 0, variable 0
+  int64_t soff;        // source element of box point 0, variable 0; -1: a copy
+                       //   whose source rows are a table (no affine form)
+  int32_t s2, s3;      // target strides of dimensions 2 and 3
+  int32_t c1, c2, c3;  // source strides of a target row step in each dimension
+  int32_t vstride;     // elements between variables
+  int32_t n1, n12;     // box rows: the point decomposition
+  uint32_t mag1, mag12;
+  int32_t itemoff;     // box point of the tile's point k: k + itemoff
+  int32_t fac;         // factor column's first element (FACTOR), from `factors`
+};
+static_assert(sizeof(CopySeg) == 64, "four 16-byte shared loads a point");
+
+template <typename T, int D, bool BATCH, bool FACTOR>
+__device__ __forceinline__ CopySeg copy_seg(const Tile &seg, int pref, const Args<T> &a,
+                                            const T *src, T *dst, const T *factors, int nvars,
+                                            int S1, int S2, int S3) {
+  const DevGroup &g = a.groups[seg.group];
+  const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+  const int64_t s2 = L.S1, s3 = (int64_t)L.S1 * L.S2, vs = s3 * L.S3, bs = vs * nvars;
+  const int64_t tblock = __ldg(a.tb + seg.transfer) - 1;
+  const int64_t sblock = __ldg(a.sb + seg.transfer) - 1;
+  CopySeg c;
+  c.toff = tblock * bs + g.tf[0] + (D >= 2 ? g.tf[1] * s2 : 0) + (D >= 3 ? g.tf[2] * s3 : 0) +
+           (L.dst - dst);
+  c.soff = g.affine ? sblock * bs + g.cs0[0] + (D >= 2 ? g.cs0[1] * s2 : 0) +
+                          (D >= 3 ? g.cs0[2] * s3 : 0) + (L.src - src)
+                    : -1;
+  c.s2 = (int32_t)s2;
+  c.s3 = (int32_t)s3;
+  c.c1 = g.cstep[0];
+  c.c2 = D >= 2 ? g.cstep[1] * (int32_t)s2 : 0;
+  c.c3 = D >= 3 ? g.cstep[2] * (int32_t)s3 : 0;
+  c.vstride = (int32_t)vs;
+  c.n1 = g.n[0];
+  c.n12 = g.n[0] * g.n[1];
+  c.mag1 = g.mag1;
+  c.mag12 = g.mag12;
+  c.itemoff = seg.item0 - pref;
+  c.fac = FACTOR ? (int32_t)((L.factors - factors) + (int64_t)nvars * (g.factorcol - 1)) : 0;
+  return c;
+}
+
+// Loads a lane of the copy kernel keeps in flight: NP points, kCopyVars / NP
+// variables of each at a time.
 constexpr int kCopyVars = 8;
 
-// The unit-copy tiles of a stage: a light kernel, the loads of every
-// variable of NP points a lane in flight together (NP, TAM_OPT_COPY_POINTS,
-// trades registers, and so resident warps, for loads in flight per warp).
+// The unit-copy tiles of a stage: a light kernel, the loads of NP points a
+// lane in flight together (NP, TAM_OPT_COPY_POINTS: with few variables a
+// point, as in a batch of two-variable forests, more points a lane keep more
+// loads in flight).
 // Copies without a factor column run the FACTOR = false form, which holds
 // no floating-point operation at all: with the factor's multiply in the
 // same code the compiler issues it predicated, and on GB300's narrow FP64
@@ -714,7 +773,9 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
                                                          T *__restrict__ dst,
                                                          const T *__restrict__ factors,
                                                          int nvars, int S1, int S2, int S3) {
+  extern __shared__ __align__(16) unsigned char copy_smem[];
   const int lane = threadIdx.x & 31;
+  CopySeg *segs = reinterpret_cast<CopySeg *>(copy_smem) + (threadIdx.x >> 5) * 32;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nptiles;
        w += warps) {
@@ -722,6 +783,55 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
     Tile seg;
     int pref;
     load_segments(tiles, pt, lane, seg, pref);
+    if constexpr (!BATCH) {
+      // one schedule's tiles (long boxes, few segments a tile): each point
+      // forms its geometry from its group's loads, which broadcast
+      for (int base = 0; base < pt.nitems; base += 32 * NP) {
+        Geom o[NP];
+        bool on[NP];
+        const T *fac[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int k = base + 32 * p + lane;
+          SegPoint q = find_point(seg, pref, pt.nseg, lane, base + 32 * p,
+                                  k < pt.nitems ? k : pt.nitems - 1);
+          on[p] = k < pt.nitems;
+          const DevGroup &g = a.groups[q.group];
+          const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
+          const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
+          int i1, i2, i3;
+          box_point(g, q.item, i1, i2, i3);
+          o[p] = g.affine ? copy_geometry<D>(g, i1, i2, i3, tblock, sblock, nvars, S1, S2, S3)
+                          : geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1,
+                                        S2, S3);
+          fac[p] = FACTOR ? factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
+        }
+        copy_point_vars<T, NP, kCopyVars / NP, FACTOR>(fac, o, on, src, dst, 0, nvars);
+      }
+      continue;
+    }
+    // A batch's tiles (small blocks, many short segments a tile).
+    // A tile of one segment: every lane
+    // forms its geometry itself, in registers, from loads that broadcast.
+    // Several segments: each formed once, by its lane, into shared memory.
+    const bool one = pt.nseg == 1;
+    bool general = false;
+    if (one) {
+      seg.group = __shfl_sync(0xffffffffu, seg.group, 0);
+      seg.transfer = __shfl_sync(0xffffffffu, seg.transfer, 0);
+      seg.item0 = __shfl_sync(0xffffffffu, seg.item0, 0);
+      pref = 0;
+    } else {
+      if (lane < pt.nseg) {
+        const CopySeg c = copy_seg<T, D, BATCH, FACTOR>(seg, pref, a, src, dst, factors, nvars,
+                                                        S1, S2, S3);
+        segs[lane] = c;
+        general = c.soff < 0;
+      }
+      // a tile with a table-sourced segment takes the general form for it
+      general = __any_sync(0xffffffffu, general);
+      __syncwarp();
+    }
     // NP points a lane: their loads in flight together
     for (int base = 0; base < pt.nitems; base += 32 * NP) {
       Geom o[NP];
@@ -730,27 +840,41 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
         const int k = base + 32 * p + lane;
-        SegPoint q = find_point(seg, pref, pt.nseg, lane, base + 32 * p,
-                                k < pt.nitems ? k : pt.nitems - 1);
+        const int kc = k < pt.nitems ? k : pt.nitems - 1;
+        const int mine = one ? 0 : find_segment(pref, pt.nseg, lane, base + 32 * p, kc);
         on[p] = k < pt.nitems;
-        const DevGroup &g = a.groups[q.group];
-        const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-        const int64_t tblock = __ldg(a.tb + q.transfer) - 1;
-        const int64_t sblock = __ldg(a.sb + q.transfer) - 1;
-        int i1, i2, i3;
-        box_point(g, q.item, i1, i2, i3);
-        o[p] = g.affine ? copy_geometry<D>(g, i1, i2, i3, tblock, sblock, nvars, L.S1, L.S2, L.S3)
-                        : geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1,
-                                      L.S2, L.S3);
-        // a batch member's offsets folded into the point's own
-        if (BATCH) {
-          o[p].soff += L.src - src;
-          o[p].toff += L.dst - dst;
+        const CopySeg c = one ? copy_seg<T, D, BATCH, FACTOR>(seg, 0, a, src, dst, factors,
+                                                              nvars, S1, S2, S3)
+                              : segs[mine];
+        const int item = kc + c.itemoff;
+        const int i3 = c.mag12 ? (int)__umulhi((uint32_t)item, c.mag12) : item / c.n12;
+        const int rem = item - i3 * c.n12;
+        const int i2 = c.mag1 ? (int)__umulhi((uint32_t)rem, c.mag1) : rem / c.n1;
+        const int i1 = rem - i2 * c.n1;
+        o[p].vstride = c.vstride;
+        o[p].toff = c.toff + (i1 + i2 * c.s2 + i3 * c.s3);
+        o[p].soff = c.soff + (i1 * c.c1 + i2 * c.c2 + i3 * c.c3);
+        fac[p] = FACTOR ? factors + c.fac : nullptr;
+        if (one ? c.soff < 0 : general) {  // warp-uniform either way
+          const int gi = one ? seg.group : __shfl_sync(0xffffffffu, seg.group, mine);
+          const int tr = one ? seg.transfer : __shfl_sync(0xffffffffu, seg.transfer, mine);
+          if (c.soff < 0) {
+            const DevGroup &g = a.groups[gi];
+            const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+            const int64_t tblock = __ldg(a.tb + tr) - 1;
+            const int64_t sblock = __ldg(a.sb + tr) - 1;
+            o[p] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2,
+                               L.S3);
+            if (BATCH) {
+              o[p].soff += L.src - src;
+              o[p].toff += L.dst - dst;
+            }
+          }
         }
-        fac[p] = FACTOR ? L.factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
       }
-      copy_point_vars<T, NP, kCopyVars, FACTOR>(fac, o, on, src, dst, 0, nvars);
+      copy_point_vars<T, NP, kCopyVars / NP, FACTOR>(fac, o, on, src, dst, 0, nvars);
     }
+    __syncwarp();  // every lane is done with the segments before the next tile's
   }
 }
 
@@ -903,14 +1027,16 @@ cudaError_t launch_copies(const Tile *tiles, const PTile *ptiles, int64_t n, con
   const int wpb = threads / 32;
   int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
   if (cap > 0) blocks = std::min(blocks, cap);
+  // a batch's segments in shared memory: 2 KiB a warp, 32 KiB at most
+  const size_t smem = BATCH ? (size_t)wpb * 32 * sizeof(CopySeg) : 0;
   if (a.copy_points >= 4)
-    fused_copy_kernel<T, D, BATCH, FACTOR, 4><<<(unsigned)blocks, threads, 0, stream>>>(
+    fused_copy_kernel<T, D, BATCH, FACTOR, 4><<<(unsigned)blocks, threads, smem, stream>>>(
         tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
   else if (a.copy_points == 2)
-    fused_copy_kernel<T, D, BATCH, FACTOR, 2><<<(unsigned)blocks, threads, 0, stream>>>(
+    fused_copy_kernel<T, D, BATCH, FACTOR, 2><<<(unsigned)blocks, threads, smem, stream>>>(
         tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
   else
-    fused_copy_kernel<T, D, BATCH, FACTOR, 1><<<(unsigned)blocks, threads, 0, stream>>>(
+    fused_copy_kernel<T, D, BATCH, FACTOR, 1><<<(unsigned)blocks, threads, smem, stream>>>(
         tiles, ptiles, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
   return cudaSuccess;
 }

@@ -138,18 +138,24 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
               {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
               {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp},
               {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs}};
-  for (Dim &dm : dims) {
-    for (int i = 0; i < dm.n && rc == TAM_OK; ++i) {
-      if ((rc = tam_schedule_set_option(s, dm.option, dm.values[i])) != TAM_OK) break;
-      const double ms =
-          time_fill(s, work, nvars, nblocks, factors, reps, (cudaStream_t)stream, a, b, &rc);
-      if (rc != TAM_OK) break;
-      if (ms < best) {
-        best = ms;
-        dm.best = dm.values[i];
+  // two sweeps: the options interact (the copies' share of the machine and
+  // the stencils' tiling, for one), so the second revisits each from the
+  // others' best
+  for (int sweep = 0; sweep < 2; ++sweep) {
+    for (Dim &dm : dims) {
+      for (int i = 0; i < dm.n && rc == TAM_OK; ++i) {
+        if (sweep == 1 && dm.values[i] == dm.best) continue;
+        if ((rc = tam_schedule_set_option(s, dm.option, dm.values[i])) != TAM_OK) break;
+        const double ms =
+            time_fill(s, work, nvars, nblocks, factors, reps, (cudaStream_t)stream, a, b, &rc);
+        if (rc != TAM_OK) break;
+        if (ms < best) {
+          best = ms;
+          dm.best = dm.values[i];
+        }
       }
+      if (rc == TAM_OK) rc = tam_schedule_set_option(s, dm.option, dm.best);
     }
-    if (rc == TAM_OK) rc = tam_schedule_set_option(s, dm.option, dm.best);
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);

@@ -167,6 +167,58 @@ class ForestBatch:
                 "copy_share": 11}[name]
         _native.check(self.lib.tam_batch_set_option(self.handle, code, int(value)), self.ctx,
                       f"tam_batch_set_option({name})")
+        self.options[name] = int(value)
+
+    @property
+    def options(self) -> dict:
+        """The launch options set so far (the library's defaults until set)."""
+        if "_options" not in self.__dict__:
+            self._options = {"tile_items": 128, "threads": 256, "int_mul": 0, "one_tap": 1,
+                             "copy_points": 1, "path_tiles": 1 if self.T.itemsize == 8 else 0,
+                             "staged": 0, "pair_vars": 0, "copy_share": 0}
+        return self._options
+
+    # the batch's tuning choices: every value of each, one option at a time
+    TUNE = (("tile_items", (32, 64, 128, 256, 512)), ("threads", (128, 256, 512)),
+            ("copy_points", (1, 2, 4)), ("copy_share", (0, 2, 4)), ("path_tiles", (0, 1)))
+
+    def autotune(self, reps: int = 3, sweeps: int = 2) -> dict:
+        """Pick the batch's launch options by timing whole fills (CUDA events,
+        best of ``reps`` after a warm-up) one option at a time, ``sweeps``
+        times over (for Float64 the integer-pipe multiply too).  The fills
+        overwrite the arena's ghosts, never an own point; every choice gives
+        the same bits.  Returns the options left set."""
+        stream = torch.cuda.current_stream(self.device)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+        def timed() -> float:
+            self.fill()
+            best = float("inf")
+            for _ in range(reps):
+                start.record(stream)
+                self.fill()
+                end.record(stream)
+                end.synchronize()
+                best = min(best, start.elapsed_time(end))
+            return best
+
+        dims = list(self.TUNE)
+        if self.T.itemsize == 8:
+            dims.append(("int_mul", (0, 1)))
+        best = timed()
+        for _ in range(sweeps):
+            for name, values in dims:
+                keep = self.options[name]
+                for v in values:
+                    if v == keep:
+                        continue
+                    self.set_option(name, v)
+                    ms = timed()
+                    if ms < best:
+                        best, keep = ms, v
+                self.set_option(name, keep)
+        self.tuned_ms = best
+        return dict(self.options)
 
     def member_view(self, arena: torch.Tensor, m: int) -> torch.Tensor:
         fs = self.fieldsets[m]
