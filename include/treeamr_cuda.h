@@ -527,6 +527,12 @@ int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stag
  * the copies' room as they finish: memory-bound copies and FP64-bound
  * stencils on the same multiprocessors at once.  The same bits either way. */
 #define TAM_OPT_COPY_SHARE 11
+/* 1: in Float64 order-4 stencils with the integer-pipe multiply, the last
+ * tap of every row of four adds on the integer pipe (an exact
+ * round-to-nearest adder, tam_selftest 2) instead of the FP64 pipe, which
+ * GB300 gives 1/64 of the FP32 rate; the sum keeps the reference's order,
+ * so the same bits.  0 (the default): every add on the FP64 pipe. */
+#define TAM_OPT_SOFT_ADD 12
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
@@ -536,7 +542,8 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
  * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
  * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER, TAM_OPT_COPY_POINTS and
- * TAM_OPT_COPY_SHARE (0, 1, 2, 4) one at a time, twice over; leaves the
+ * TAM_OPT_COPY_SHARE (0, 1, 2, 4) and, for Float64, TAM_OPT_SOFT_ADD one at
+ * a time, twice over; leaves the
  * fastest set and returns the first three (the others through
  * tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an
  * own point).  Synchronizes `stream`; re-tiling allocates, so not inside a
@@ -553,8 +560,14 @@ int tam_device_status(tam_sched *s, void *stream, int32_t *code);
  * integer-pipe Float64 multiply the fills use for short weight products
  * with the hardware multiply on n pseudo-random pairs (all bit patterns of
  * the data, specials included) and returns the number of results that
- * differ in any bit (NaNs compared as one pattern).  Synchronous. */
+ * differ in any bit (NaNs compared as one pattern).  which = 2 compares the
+ * integer-pipe Float64 add (TAM_OPT_SOFT_ADD) with the hardware add on n
+ * pairs of a running sum (every kind of value) and a product (normal),
+ * weighted to equal and adjacent exponents, cancellations and the edges of
+ * the normal range, and returns the results that differ in any bit (pairs
+ * the adder hands back to the FP64 pipe are not compared).  Synchronous. */
 #define TAM_SELFTEST_MUL 1
+#define TAM_SELFTEST_ADD 2
 int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches);
 
 #ifdef __cplusplus

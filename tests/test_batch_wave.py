@@ -190,7 +190,7 @@ def test_native_autotune(cuda_lib):
     best = autotune(fs, s)
     assert set(best) == {"tile_items", "threads", "int_mul", "merge_stages", "path_tiles",
                          "staged", "pair_vars", "block_order", "copy_points",
-                         "copy_share"} and s._tuned_ms > 0
+                         "copy_share", "soft_add"} and s._tuned_ms > 0
     ds = device_schedule(s, 0)
     assert ds.options()["tile_items"] == best["tile_items"]
     fs.work.copy_(torch.from_numpy(host))

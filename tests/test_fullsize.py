@@ -70,15 +70,18 @@ def test_sphere_full_bit_exact(cuda_lib, sphere_forest):
     assert np.array_equal(nanbits(point), nanbits(expect))
     del point
     ds = device_schedule(sched, 0)
-    for method, staged, pair, share in (("fused", 0, 0, 0), ("fused", 1, 0, 0),
-                                        ("fused", 0, 1, 2), ("plain", 0, 0, 0)):
+    for method, staged, pair, share, soft in (("fused", 0, 0, 0, 0), ("fused", 1, 0, 0, 0),
+                                              ("fused", 0, 1, 2, 1), ("fused", 0, 0, 2, 1),
+                                              ("plain", 0, 0, 0, 0)):
         ds.set_option("staged", staged)
         ds.set_option("pair_vars", pair)
         ds.set_option("copy_share", share)
+        ds.set_option("soft_add", soft)
+        ds.set_option("int_mul", 1 if (staged or pair or share or soft) else 0)
         fs.work.copy_(start)
         fill_ghosts(fs, sched, method=method)
         torch.cuda.synchronize()
-        assert _same(fs.work, expect) == 0, (method, staged, pair, share)
+        assert _same(fs.work, expect) == 0, (method, staged, pair, share, soft)
 
 
 def test_walls_full_bit_exact(cuda_lib, walls_forest):
@@ -95,15 +98,19 @@ def test_walls_full_bit_exact(cuda_lib, walls_forest):
         assert np.array_equal(nanbits(point), nanbits(expect)), np.dtype(T).name
         del point
         ds = device_schedule(sched, 0)
-        for method, staged, pair, share in (("fused", 0, 0, 0), ("fused", 1, 0, 0),
-                                            ("fused", 0, 1, 2), ("plain", 0, 0, 0)):
+        for method, staged, pair, share, soft in (("fused", 0, 0, 0, 0), ("fused", 1, 0, 0, 0),
+                                                  ("fused", 0, 1, 2, 1), ("fused", 0, 0, 2, 1),
+                                                  ("plain", 0, 0, 0, 0)):
             ds.set_option("staged", staged)
             ds.set_option("pair_vars", pair)
             ds.set_option("copy_share", share)
+            ds.set_option("soft_add", soft)
+            ds.set_option("int_mul", 1 if (staged or pair or share or soft) else 0)
             fs.work.copy_(start)
             fill_ghosts(fs, sched, method=method)
             torch.cuda.synchronize()
-            assert _same(fs.work, expect) == 0, (np.dtype(T).name, method, staged, pair, share)
+            assert _same(fs.work, expect) == 0, (np.dtype(T).name, method, staged, pair, share,
+                                                 soft)
         del fs, start, expect, ds
         torch.cuda.empty_cache()
 

@@ -198,6 +198,21 @@ def test_integer_pipe_multiply_matches_hardware(cuda_lib):
         assert bad.value == 0
 
 
+def test_integer_pipe_add_matches_hardware(cuda_lib):
+    """The Float64 add a stencil row's last tap may take on the integer pipe
+    equals the hardware add in every bit wherever it does not hand the pair
+    back, over 3 x 2^26 pairs weighted to its hard cases (equal and adjacent
+    exponents, cancellations, the edges of the normal range)."""
+    import ctypes as C
+    from treeamr import _native
+    ctx = _native.context(0)
+    bad = C.c_int64(-1)
+    for seed in (1, 2, 3):
+        _native.check(cuda_lib.tam_selftest(ctx, 2, 1 << 26, seed, C.byref(bad)), ctx,
+                      "tam_selftest")
+        assert bad.value == 0
+
+
 def test_launch_options_change_no_bit(cuda_lib):
     """Every launch option of the fused fill gives the same bits."""
     from treeamr.ghosts import device_schedule
@@ -209,13 +224,15 @@ def test_launch_options_change_no_bit(cuda_lib):
     fs.work = torch.from_numpy(host).cuda()
     fs.factors = fs.factors.cuda()
     ds = device_schedule(s, 0)
-    for ti, th, im, cp, bo, pt, ms, sg, pv, cs in ((16, 64, 0, 1, 0, 0, 1, 1, 1, 1),
-                                                   (37, 96, 1, 2, 1, 1, 0, 1, 0, 0),
-                                                   (512, 512, 1, 4, 0, 1, 1, 0, 1, 2),
-                                                   (4096, 128, 0, 2, 1, 0, 0, 1, 1, 4)):
+    for ti, th, im, cp, bo, pt, ms, sg, pv, cs, sa in (
+            (16, 64, 0, 1, 0, 0, 1, 1, 1, 1, 1),
+            (37, 96, 1, 2, 1, 1, 0, 1, 0, 0, 1),
+            (512, 512, 1, 4, 0, 1, 1, 0, 1, 2, 1),
+            (64, 128, 1, 1, 0, 1, 1, 0, 0, 2, 1),
+            (4096, 128, 0, 2, 1, 0, 0, 1, 1, 4, 0)):
         opts = {"tile_items": ti, "threads": th, "int_mul": im, "one_tap": 1,
                 "copy_points": cp, "block_order": bo, "path_tiles": pt, "merge_stages": ms,
-                "staged": sg, "pair_vars": pv, "copy_share": cs}
+                "staged": sg, "pair_vars": pv, "copy_share": cs, "soft_add": sa}
         for k, v in opts.items():
             ds.set_option(k, v)
         assert ds.options() == opts

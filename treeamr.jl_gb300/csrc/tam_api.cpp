@@ -356,7 +356,7 @@ tam::SchedArgs sched_args(const tam_sched *s) {
                         s->d_weights, s->d_cls,   s->d_wtab,      s->shape.int_mul,
                         nullptr,      s->d_csingle, s->d_perm,    s->shape.one_tap,
                         s->shape.copy_points, s->d_wshort, s->shape.pair_vars,
-                        s->shape.copy_share * s->ctx->nsm};
+                        s->shape.copy_share * s->ctx->nsm, s->shape.soft_add};
 }
 
 // The order in which the fused launches visit target blocks: with
@@ -1344,6 +1344,10 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
       if (value < 0 || value > 32) return fail(s->ctx, TAM_EINVAL, "copy_share is 0..32");
       s->shape.copy_share = (int)value;
       return TAM_OK;
+    case TAM_OPT_SOFT_ADD:
+      if (value != 0 && value != 1) return fail(s->ctx, TAM_EINVAL, "soft_add is 0 or 1");
+      s->shape.soft_add = (int)value;
+      return TAM_OK;
     default:
       return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
@@ -1363,23 +1367,27 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_BLOCK_ORDER: *value = s->shape.block_order; return TAM_OK;
     case TAM_OPT_PATH_TILES: *value = s->shape.path_tiles; return TAM_OK;
     case TAM_OPT_COPY_SHARE: *value = s->shape.copy_share; return TAM_OK;
+    case TAM_OPT_SOFT_ADD: *value = s->shape.soft_add; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
 }
 
 int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches) {
   if (!ctx || !mismatches || n < 0) return fail(ctx, TAM_EINVAL, "tam_selftest: bad argument");
-  if (which != TAM_SELFTEST_MUL) return fail(ctx, TAM_EINVAL, "tam_selftest: unknown test");
+  if (which != TAM_SELFTEST_MUL && which != TAM_SELFTEST_ADD)
+    return fail(ctx, TAM_EINVAL, "tam_selftest: unknown test");
   DeviceGuard guard(ctx->device);
   if (!guard.ok()) return fail(ctx, TAM_ECUDA, "cannot make the context's device current");
-  unsigned long long *d = nullptr, h = 0;
+  unsigned long long *d = nullptr, h[2] = {0, 0};
   cudaError_t e = cudaMalloc((void **)&d, sizeof h);
   if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof h);
-  if (e == cudaSuccess) e = tam::launch_selftest_mul(n, seed, d, 0);
-  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = which == TAM_SELFTEST_MUL ? tam::launch_selftest_mul(n, seed, d, 0)
+                                  : tam::launch_selftest_add(n, seed, d, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tam_selftest");
-  *mismatches = (int64_t)h;
+  *mismatches = (int64_t)h[0];
   return TAM_OK;
 }
 

@@ -416,7 +416,7 @@ int tam_batch_fill_ex(tam_batch *b, void *arena, int64_t arena_elems, int32_t nv
                             b->d_weights, b->d_cls,     b->d_wtab,        b->shape.int_mul,
                             b->d_members, b->d_csingle, b->d_perm,        b->shape.one_tap,
                             b->shape.copy_points, b->d_wshort, b->shape.pair_vars,
-                            b->shape.copy_share * b->ctx->nsm};
+                            b->shape.copy_share * b->ctx->nsm, b->shape.soft_add};
   const int S[3] = {1, 1, 1};  // each member's own, from the member table
   for (const tam::Stage &st : b->stages) {
     if (st.tag < first_stage || st.tag > last_stage) continue;
@@ -581,6 +581,11 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (option == TAM_OPT_COPY_SHARE) {
     if (value < 0 || value > 32) return bfail(b->ctx, TAM_EINVAL, "copy_share is 0..32");
     b->shape.copy_share = (int)value;
+    return TAM_OK;
+  }
+  if (option == TAM_OPT_SOFT_ADD) {
+    if (value != 0 && value != 1) return bfail(b->ctx, TAM_EINVAL, "soft_add is 0 or 1");
+    b->shape.soft_add = (int)value;
     return TAM_OK;
   }
   return bfail(b->ctx, TAM_EINVAL, "unknown option");

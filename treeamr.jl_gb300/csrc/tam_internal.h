@@ -247,6 +247,7 @@ struct LaunchShape {
   int staged = 0;           // large stencil boxes from a shared-memory window (TAM_OPT_STAGED)
   int pair_vars = 0;        // Float64 order-4 stencils two variables a lane (TAM_OPT_PAIR_VARS)
   int copy_share = 0;       // copy CTAs a multiprocessor beside the stencils (TAM_OPT_COPY_SHARE)
+  int soft_add = 0;         // Float64 order 4: a tap a row added on the integer pipe (TAM_OPT_SOFT_ADD)
 };
 
 }  // namespace tam
@@ -339,6 +340,7 @@ struct SchedArgs {
   const void *wshort;      // Float64: the product table's entries as mul_short takes them
   int pair_vars;           // Float64 order-4 stencils: two variables a lane
   int copy_ctas;           // beside stencils: the copy launch first, at most this grid (0: after)
+  int soft_add;            // Float64 order 4: a tap a row added on the integer pipe
 };
 
 // The Float64 product table `wtab` (doubles) with each entry split as the
@@ -385,6 +387,10 @@ cudaError_t launch_solo(int dtype, int D, const SoloGroup *turns, int64_t n,
 int own_box_copy(const tam_state_layout *layout, void *dst, const void *src, void *stream);
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                cudaStream_t stream);
+// add_soft against the hardware add: mismatches[0] the differing results,
+// mismatches[1] the pairs the adder hands back to the FP64 pipe.
+cudaError_t launch_selftest_add(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);
 
 // The adjoint (tam_adjoint.cu).

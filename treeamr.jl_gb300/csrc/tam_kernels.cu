@@ -105,6 +105,7 @@ struct Args {
   const uint2 *__restrict__ wshort;
   int pair_vars;
   int copy_ctas;
+  int soft_add;
 };
 
 template <typename T>
@@ -112,7 +113,7 @@ __host__ __device__ inline Args<T> typed(const SchedArgs &a) {
   return Args<T>{a.groups,  a.tb,      a.sb,   a.srcstart, (const T *)a.weights,
                  a.cls,     (const T *)a.wtab, a.int_mul, a.members, a.csingle,
                  a.perm,    a.one_tap, a.copy_points, (const uint2 *)a.wshort, a.pair_vars,
-                 a.copy_ctas};
+                 a.copy_ctas, a.soft_add};
 }
 
 struct Geom {
@@ -254,6 +255,63 @@ __device__ __forceinline__ double mul_short_flag(uint32_t wm, int we, uint32_t w
   return __hiloint2double((int)rhi, (int)(uint32_t)m);
 }
 
+// RN(a + b) on the integer pipe: the textbook IEEE adder.  The operands in
+// order of magnitude, the smaller one's significand shifted to the larger's
+// exponent with three extra bits (guard, round and sticky), added or
+// subtracted, normalised (a carry one place right, a cancellation any number
+// left) and rounded to nearest-even on the extra bits; three extra bits
+// round every sum and difference correctly.  For the running sum `a` of a
+// stencil and a product `b` of the integer-pipe multiply (normal, nonzero,
+// finite).  A zero `a` gives b exactly; `bad` is set where `a` is
+// subnormal, infinite or NaN or the result is not a normal number (the
+// caller sums the point again on the FP64 pipe).  Bit-identical to
+// __dadd_rn(a, b) wherever `bad` stays clear (checked by tam_selftest).
+__device__ __forceinline__ double add_soft(double a, double b, bool &bad) {
+  constexpr uint64_t kMag = 0x7FFFFFFFFFFFFFFFull, kFrac = 0x000FFFFFFFFFFFFFull;
+  const uint64_t ua = (uint64_t)__double_as_longlong(a);
+  const uint64_t ub = (uint64_t)__double_as_longlong(b);
+  const bool swap = (ub & kMag) > (ua & kMag);
+  const uint64_t x = swap ? ub : ua, y = swap ? ua : ub;  // |x| >= |y|
+  const int ex = (int)((x >> 52) & 0x7FF), ey = (int)((y >> 52) & 0x7FF);
+  if ((y & kMag) == 0) return __longlong_as_double((long long)x);  // a zero: b itself
+  bad |= (ex == 0x7FF) | (ey == 0);
+  const uint64_t mx = ((x & kFrac) | (1ull << 52)) << 3;  // bits 55 .. 3, 3 extra
+  const uint64_t my = ((y & kFrac) | (1ull << 52)) << 3;
+  const int d = ex - ey;
+  uint64_t yd;
+  if (d == 0)
+    yd = my;
+  else if (d < 56)
+    yd = (my >> d) | (uint64_t)((my << (64 - d)) != 0);  // sticky
+  else
+    yd = 1;  // below every kept bit: sticky only
+  int e = ex;
+  uint64_t s;
+  if (((ua ^ ub) >> 63) == 0) {
+    s = mx + yd;
+    if (s >> 56) {  // a carry: one place right, the lost bit kept sticky
+      s = (s >> 1) | (s & 1);
+      e += 1;
+    }
+  } else {
+    s = mx - yd;
+    if (s == 0) return 0.0;  // exact cancellation: +0 in round-to-nearest
+    const int sh = __clzll((long long)s) - 8;  // bring the top bit to bit 55
+    s <<= sh;
+    e -= sh;
+  }
+  uint64_t m = s >> 3;
+  const uint32_t low = (uint32_t)s & 7u;
+  m += (low > 4u) | ((low == 4u) & (uint32_t)m & 1u);
+  if (m >> 53) {  // rounded up to the next power of two
+    m >>= 1;
+    e += 1;
+  }
+  bad |= (e <= 0) | (e >= 0x7FF);
+  return __longlong_as_double(
+      (long long)((x & 0x8000000000000000ull) | ((uint64_t)(e & 0x7FF) << 52) | (m & kFrac)));
+}
+
 // The parts of a weight mul_short takes.
 struct ShortW {
   double w;
@@ -331,7 +389,7 @@ __device__ __forceinline__ void tap_rows(const int32_t *__restrict__ single, int
 // VC variables at a time.  SKIP: the one-tap rows of `tap_rows`, which
 // leave out only terms 0 * u, so the remaining products are summed in the
 // same order (m_1 fastest) as the full nest.
-template <typename T, int D, int P, int VC, bool SKIP>
+template <typename T, int D, int P, int VC, bool SKIP, bool SOFT = false>
 __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, int i3,
                                             const Geom &o, const Args<T> &a,
                                             const T *__restrict__ work, T *__restrict__ dst,
@@ -364,31 +422,37 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
         // FIRST: the sum's first term, 0 + p, is p itself (the fast path's
         // p is a nonzero finite number; anything else is flagged and summed
         // again below), so the sum costs one FP64 add a tap less
-        auto tap = [&](int m1, int m2, int m3, auto first) {
+        // SOFT (TAM_OPT_SOFT_ADD): the last tap of every whole row adds on
+        // the integer pipe (add_soft), beside the FP64 pipe's adds
+        auto tap = [&](int m1, int m2, int m3, auto first, auto soft) {
           const ShortW sw = unpack_short(__ldg(WS + (m3 * P2 + m2) * P + m1));
           const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
 #pragma unroll
           for (int j = 0; j < VC; ++j)
             if (v0 + j < vend) {
               const double p = mul_short_flag(sw.wm, sw.we, sw.wsign, src[off + j * o.svstride], bad);
-              acc[j] = decltype(first)::value ? p : __dadd_rn(acc[j], p);
+              acc[j] = decltype(first)::value  ? p
+                       : decltype(soft)::value ? add_soft(acc[j], p, bad)
+                                               : __dadd_rn(acc[j], p);
             }
         };
-        using Head = std::true_type;
-        using Rest = std::false_type;
+        using Yes = std::true_type;
+        using No = std::false_type;
+        using Last = std::integral_constant<bool, SOFT>;
         auto row = [&](int m2, int m3, bool head) {
           if (SKIP && hi1 - lo1 == 1) {
             if (head)
-              tap(lo1, m2, m3, Head{});
+              tap(lo1, m2, m3, Yes{}, No{});
             else
-              tap(lo1, m2, m3, Rest{});
+              tap(lo1, m2, m3, No{}, No{});
           } else {
             if (head)
-              tap(0, m2, m3, Head{});
+              tap(0, m2, m3, Yes{}, No{});
             else
-              tap(0, m2, m3, Rest{});
+              tap(0, m2, m3, No{}, No{});
 #pragma unroll
-            for (int m1 = 1; m1 < P; ++m1) tap(m1, m2, m3, Rest{});
+            for (int m1 = 1; m1 < P - 1; ++m1) tap(m1, m2, m3, No{}, No{});
+            tap(P - 1, m2, m3, No{}, Last{});
           }
         };
         row(lo2, lo3, true);
@@ -492,25 +556,26 @@ __device__ __forceinline__ void generic_point(const DevGroup &g, int i1, int i2,
   }
 }
 
-template <typename T, int D, int P, int VC>
+template <typename T, int D, int P, int VC, bool SOFT = false>
 __device__ __forceinline__ void table_dispatch(const DevGroup &g, int i1, int i2, int i3,
                                                const Geom &o, const Args<T> &a,
                                                const T *__restrict__ work, T *__restrict__ dst,
                                                const T *__restrict__ factors, int nvars,
                                                bool skip, int vbegin, int vend) {
   if (skip)
-    table_point<T, D, P, VC, true>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
-                                   vend);
+    table_point<T, D, P, VC, true, SOFT>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
+                                         vend);
   else
-    table_point<T, D, P, VC, false>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
+    table_point<T, D, P, VC, false, SOFT>(g, i1, i2, i3, o, a, work, dst, factors, nvars, vbegin,
                                     vend);
 }
 
 // Variables [vbegin, vend) of one box point of one stencil transfer, by the
 // group's class; `src` with `o` locates the source window (the array
 // itself, or a window staged in shared memory).  PC = 4: the caller's
-// groups are all of uniform order 4, and only that path is compiled.
-template <typename T, int D, int PC = 0>
+// groups are all of uniform order 4, and only that path is compiled (SOFT:
+// with the integer-pipe add for a tap a row).
+template <typename T, int D, int PC = 0, bool SOFT = false>
 __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int i2, int i3,
                                                  const Geom &o, const Args<T> &a,
                                                  const T *__restrict__ src, T *__restrict__ dst,
@@ -518,15 +583,18 @@ __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int 
                                                  int vbegin, int vend) {
   const bool skip = a.one_tap && g.perm >= 0;
   // Float64 one variable at a time: the FP64 pipe binds, and the fewer
-  // registers a lane holds the more warps hide the loads' latency.
+  // registers a lane holds the more warps hide the loads' latency.  Float32
+  // four at a time, or two where no more are left (a two-variable set would
+  // otherwise issue half its taps' instructions predicated off).
   constexpr int VC = sizeof(T) == 8 ? 1 : 4;
+  const bool two = sizeof(T) == 4 && vend - vbegin <= 2;
   if constexpr (PC == 4) {
-    if (sizeof(T) == 8 && a.pair_vars)
-      table_dispatch<T, D, 4, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
-                                 vend);
+    if ((sizeof(T) == 8 && a.pair_vars) || two)
+      table_dispatch<T, D, 4, 2, SOFT>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip,
+                                       vbegin, vend);
     else
-      table_dispatch<T, D, 4, VC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
-                                  vend);
+      table_dispatch<T, D, 4, VC, SOFT>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip,
+                                        vbegin, vend);
     return;
   }
   switch (g.pclass) {
@@ -541,7 +609,7 @@ __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int 
     case 4:
       // Float64 order 4: one variable a lane, or (TAM_OPT_PAIR_VARS) two, whose
       // sums share each tap's weight and run as two independent chains
-      if (sizeof(T) == 8 && a.pair_vars)
+      if ((sizeof(T) == 8 && a.pair_vars) || two)
         table_dispatch<T, D, 4, 2>(g, i1, i2, i3, o, a, src, dst, factors, nvars, skip, vbegin,
                                    vend);
       else
@@ -559,14 +627,14 @@ __device__ __forceinline__ void stencil_dispatch(const DevGroup &g, int i1, int 
 }
 
 // Every variable of one box point of one stencil transfer, read in place.
-template <typename T, int D, int PC = 0>
+template <typename T, int D, int PC = 0, bool SOFT = false>
 __device__ __forceinline__ void stencil_point(const DevGroup &g, int i1, int i2, int i3,
                                               int64_t tblock, int64_t sblock, const Args<T> &a,
                                               const T *__restrict__ src, T *__restrict__ dst,
                                               const T *__restrict__ factors, int nvars, int S1,
                                               int S2, int S3) {
   const Geom o = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, S1, S2, S3);
-  stencil_dispatch<T, D, PC>(g, i1, i2, i3, o, a, src, dst, factors, nvars, 0, nvars);
+  stencil_dispatch<T, D, PC, SOFT>(g, i1, i2, i3, o, a, src, dst, factors, nvars, 0, nvars);
 }
 
 // ---- plain: one launch per group, one thread per (point, variable) ---------
@@ -808,20 +876,10 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
         }
         copy_point_vars<T, NP, kCopyVars / NP, FACTOR>(fac, o, on, src, dst, 0, nvars);
       }
-      continue;
-    }
-    // A batch's tiles (small blocks, many short segments a tile).
-    // A tile of one segment: every lane
-    // forms its geometry itself, in registers, from loads that broadcast.
-    // Several segments: each formed once, by its lane, into shared memory.
-    const bool one = pt.nseg == 1;
-    bool general = false;
-    if (one) {
-      seg.group = __shfl_sync(0xffffffffu, seg.group, 0);
-      seg.transfer = __shfl_sync(0xffffffffu, seg.transfer, 0);
-      seg.item0 = __shfl_sync(0xffffffffu, seg.item0, 0);
-      pref = 0;
     } else {
+      // A batch's tiles (small blocks, many short segments a tile): each
+      // segment formed once, by its lane, into shared memory.
+      bool general = false;
       if (lane < pt.nseg) {
         const CopySeg c = copy_seg<T, D, BATCH, FACTOR>(seg, pref, a, src, dst, factors, nvars,
                                                         S1, S2, S3);
@@ -831,58 +889,54 @@ __global__ void __launch_bounds__(512) fused_copy_kernel(const Tile *__restrict_
       // a tile with a table-sourced segment takes the general form for it
       general = __any_sync(0xffffffffu, general);
       __syncwarp();
-    }
-    // NP points a lane: their loads in flight together
-    for (int base = 0; base < pt.nitems; base += 32 * NP) {
-      Geom o[NP];
-      bool on[NP];
-      const T *fac[NP];
-#pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        const int k = base + 32 * p + lane;
-        const int kc = k < pt.nitems ? k : pt.nitems - 1;
-        const int mine = one ? 0 : find_segment(pref, pt.nseg, lane, base + 32 * p, kc);
-        on[p] = k < pt.nitems;
-        const CopySeg c = one ? copy_seg<T, D, BATCH, FACTOR>(seg, 0, a, src, dst, factors,
-                                                              nvars, S1, S2, S3)
-                              : segs[mine];
-        const int item = kc + c.itemoff;
-        const int i3 = c.mag12 ? (int)__umulhi((uint32_t)item, c.mag12) : item / c.n12;
-        const int rem = item - i3 * c.n12;
-        const int i2 = c.mag1 ? (int)__umulhi((uint32_t)rem, c.mag1) : rem / c.n1;
-        const int i1 = rem - i2 * c.n1;
-        o[p].vstride = c.vstride;
-        o[p].toff = c.toff + (i1 + i2 * c.s2 + i3 * c.s3);
-        o[p].soff = c.soff + (i1 * c.c1 + i2 * c.c2 + i3 * c.c3);
-        fac[p] = FACTOR ? factors + c.fac : nullptr;
-        if (one ? c.soff < 0 : general) {  // warp-uniform either way
-          const int gi = one ? seg.group : __shfl_sync(0xffffffffu, seg.group, mine);
-          const int tr = one ? seg.transfer : __shfl_sync(0xffffffffu, seg.transfer, mine);
-          if (c.soff < 0) {
-            const DevGroup &g = a.groups[gi];
-            const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
-            const int64_t tblock = __ldg(a.tb + tr) - 1;
-            const int64_t sblock = __ldg(a.sb + tr) - 1;
-            o[p] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2,
-                               L.S3);
-            if (BATCH) {
+      // NP points a lane: their loads in flight together
+      for (int base = 0; base < pt.nitems; base += 32 * NP) {
+        Geom o[NP];
+        bool on[NP];
+        const T *fac[NP];
+  #pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int k = base + 32 * p + lane;
+          const int kc = k < pt.nitems ? k : pt.nitems - 1;
+          const int mine = find_segment(pref, pt.nseg, lane, base + 32 * p, kc);
+          on[p] = k < pt.nitems;
+          const CopySeg c = segs[mine];
+          const int item = kc + c.itemoff;
+          const int i3 = c.mag12 ? (int)__umulhi((uint32_t)item, c.mag12) : item / c.n12;
+          const int rem = item - i3 * c.n12;
+          const int i2 = c.mag1 ? (int)__umulhi((uint32_t)rem, c.mag1) : rem / c.n1;
+          const int i1 = rem - i2 * c.n1;
+          o[p].vstride = c.vstride;
+          o[p].toff = c.toff + (i1 + i2 * c.s2 + i3 * c.s3);
+          o[p].soff = c.soff + (i1 * c.c1 + i2 * c.c2 + i3 * c.c3);
+          fac[p] = FACTOR ? factors + c.fac : nullptr;
+          if (general) {  // warp-uniform: the shuffles take every lane
+            const int gi = __shfl_sync(0xffffffffu, seg.group, mine);
+            const int tr = __shfl_sync(0xffffffffu, seg.transfer, mine);
+            if (c.soff < 0) {
+              const DevGroup &g = a.groups[gi];
+              const TileLayout<T, BATCH> L(g, a, src, dst, factors, S1, S2, S3);
+              const int64_t tblock = __ldg(a.tb + tr) - 1;
+              const int64_t sblock = __ldg(a.sb + tr) - 1;
+              o[p] = geometry<D>(g, i1, i2, i3, tblock, sblock, a.srcstart, nvars, L.S1, L.S2,
+                                 L.S3);
               o[p].soff += L.src - src;
               o[p].toff += L.dst - dst;
             }
           }
         }
+        copy_point_vars<T, NP, kCopyVars / NP, FACTOR>(fac, o, on, src, dst, 0, nvars);
       }
-      copy_point_vars<T, NP, kCopyVars / NP, FACTOR>(fac, o, on, src, dst, 0, nvars);
+      __syncwarp();  // every lane is done with the segments before the next tile's
     }
-    __syncwarp();  // every lane is done with the segments before the next tile's
   }
 }
 
 // The stencil tiles of a stage: one point a lane, every variable.  PC = 4:
 // tiles of uniform order-4 groups only (a stage's tiles grouped by path hold
 // them in one run), the only path compiled, so that the registers it keeps
-// are its own.
-template <typename T, int D, bool BATCH, int PC>
+// are its own; SOFT, Float64 order 4 with TAM_OPT_SOFT_ADD.
+template <typename T, int D, bool BATCH, int PC, bool SOFT = false>
 __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tiles,
                                                           const PTile *__restrict__ ptiles,
                                                           int64_t nptiles, Args<T> a,
@@ -909,7 +963,8 @@ __global__ void __maxnreg__(64) fused_stage_kernel(const Tile *__restrict__ tile
       const int item = g.perm >= 0 ? __ldg(a.perm + g.perm + q.item) : q.item;
       int i1, i2, i3;
       box_point(g, item, i1, i2, i3);
-      stencil_point<T, D, PC>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors, nvars,
+      stencil_point<T, D, PC, SOFT>(g, i1, i2, i3, tblock, sblock, a, L.src, L.dst, L.factors,
+                                    nvars,
                               L.S1,
                           L.S2, L.S3);
     }
@@ -1085,6 +1140,17 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, const Stage &stg
     if (n <= 0) return;
     const int64_t blocks = std::min<int64_t>((n + wpb - 1) / wpb, (int64_t)1 << 30);
     const PTile *pt = ptiles + p0;
+    if constexpr (sizeof(T) == 8) {  // the integer-pipe add: Float64 only
+      if (four && a.soft_add && a.int_mul) {
+        if (batch)
+          fused_stage_kernel<T, D, true, 4, true><<<(unsigned)blocks, threads, 0, sst>>>(
+              tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+        else
+          fused_stage_kernel<T, D, false, 4, true><<<(unsigned)blocks, threads, 0, sst>>>(
+              tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
+        return;
+      }
+    }
     if (batch && four)
       fused_stage_kernel<T, D, true, 4><<<(unsigned)blocks, threads, 0, sst>>>(
           tiles, pt, n, a, src, work, factors, nvars, S[0], S[1], S[2]);
@@ -1548,11 +1614,67 @@ __global__ void selftest_mul_kernel(int64_t n, uint64_t seed,
   }
 }
 
+// add_soft against __dadd_rn: a the running sum (any sign and exponent,
+// zeros, subnormals and specials among them), b a normal nonzero product at
+// a distance from a that favours the adder's cases: equal exponents, one
+// apart, cancellations (b near -a), far apart, and sums at the edges of the
+// normal range.  A result the adder flags is not compared (the caller sums
+// that point on the FP64 pipe); mismatches[1] counts them.
+__global__ void selftest_add_kernel(int64_t n, uint64_t seed,
+                                    unsigned long long *__restrict__ mismatches) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r1 = splitmix(seed ^ (uint64_t)(3 * i));
+    const uint64_t r2 = splitmix(seed ^ (uint64_t)(3 * i + 1));
+    const uint64_t r3 = splitmix(seed ^ (uint64_t)(3 * i + 2));
+    uint64_t abits = r1;
+    const int mode = (int)(r3 & 7);
+    if (mode < 6) {  // a normal a, exponent in the middle or near an edge
+      const int ea = (r3 & 8) ? 1 + (int)((r3 >> 8) % 80)
+                              : (r3 & 16) ? 1940 + (int)((r3 >> 8) % 107)
+                                          : 900 + (int)((r3 >> 8) % 250);
+      abits = (r1 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)ea << 52);
+    } else if (mode == 6) {  // a zero or a subnormal
+      abits = (r1 & 0x8000000000000000ull) | ((r3 & 32) ? 0 : (r1 & 0x000FFFFFFFFFFFFFull));
+    }
+    const int eA = (int)((abits >> 52) & 0x7FF);
+    // b's exponent: a's plus a distance, mostly small
+    const int sel = (int)((r3 >> 20) & 15);
+    int dist = sel < 4 ? 0 : sel < 7 ? 1 : sel < 9 ? -1 : sel < 11 ? 2 : sel < 12 ? -2
+                                       : (int)((r3 >> 24) % 121) - 60;
+    int eb = (eA == 0 ? 1 + (int)((r3 >> 24) % 2000) : eA) + dist;
+    eb = eb < 1 ? 1 : eb > 2046 ? 2046 : eb;
+    uint64_t bbits = (r2 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)eb << 52);
+    if (((r3 >> 32) & 3) == 0 && eA > 0 && eA < 2047) {
+      // near -a: a's bits with the sign flipped and the low bits changed
+      bbits = (abits ^ 0x8000000000000000ull) ^ (r2 & ((1ull << ((r3 >> 40) % 53)) - 1));
+    }
+    const double a = __longlong_as_double((long long)abits);
+    const double b = __longlong_as_double((long long)bbits);
+    const int be = (int)((bbits >> 52) & 0x7FF);
+    if (be == 0 || be == 0x7FF) continue;  // b is a product of the fast path
+    bool bad = false;
+    const double s = add_soft(a, b, bad);
+    if (bad) {
+      atomicAdd(mismatches + 1, 1ull);
+      continue;
+    }
+    const double t = __dadd_rn(a, b);
+    if (__double_as_longlong(s) != __double_as_longlong(t)) atomicAdd(mismatches, 1ull);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream) {
   selftest_mul_kernel<<<1216, 256, 0, stream>>>(n, seed, mismatches);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_selftest_add(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                cudaStream_t stream) {
+  selftest_add_kernel<<<1216, 256, 0, stream>>>(n, seed, mismatches);
   return cudaGetLastError();
 }
 

@@ -114,6 +114,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   // lane of the copy kernel, the copies' share of the machine beside the
   // stencils
   int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1, old_sg = 0, old_pv = 0, old_cs = 0;
+  int64_t old_sa = 0;
   tam_schedule_get_option(s, TAM_OPT_PATH_TILES, &old_pt);
   tam_schedule_get_option(s, TAM_OPT_BLOCK_ORDER, &old_bo);
   tam_schedule_get_option(s, TAM_OPT_COPY_POINTS, &old_cp);
@@ -121,6 +122,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   tam_schedule_get_option(s, TAM_OPT_STAGED, &old_sg);
   tam_schedule_get_option(s, TAM_OPT_PAIR_VARS, &old_pv);
   tam_schedule_get_option(s, TAM_OPT_COPY_SHARE, &old_cs);
+  tam_schedule_get_option(s, TAM_OPT_SOFT_ADD, &old_sa);
   if (rc == TAM_OK) {
     (void)((rc = tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim)) == TAM_OK &&
            (rc = tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt)) == TAM_OK &&
@@ -137,7 +139,8 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
               {TAM_OPT_PAIR_VARS, {0, 1, 0}, dtype_f64 ? 2 : 1, old_pv},
               {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
               {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp},
-              {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs}};
+              {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs},
+              {TAM_OPT_SOFT_ADD, {0, 1, 0, 0}, dtype_f64 ? 2 : 1, old_sa}};
   // two sweeps: the options interact (the copies' share of the machine and
   // the stencils' tiling, for one), so the second revisits each from the
   // others' best
@@ -171,6 +174,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     tam_schedule_set_option(s, TAM_OPT_STAGED, old_sg);
     tam_schedule_set_option(s, TAM_OPT_PAIR_VARS, old_pv);
     tam_schedule_set_option(s, TAM_OPT_COPY_SHARE, old_cs);
+    tam_schedule_set_option(s, TAM_OPT_SOFT_ADD, old_sa);
     return rc;
   }
   if (tile_items) *tile_items = bt;

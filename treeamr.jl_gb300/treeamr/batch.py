@@ -164,7 +164,7 @@ class ForestBatch:
     def set_option(self, name: str, value: int):
         code = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
                 "path_tiles": 7, "staged": 9, "pair_vars": 10,
-                "copy_share": 11}[name]
+                "copy_share": 11, "soft_add": 12}[name]
         _native.check(self.lib.tam_batch_set_option(self.handle, code, int(value)), self.ctx,
                       f"tam_batch_set_option({name})")
         self.options[name] = int(value)
@@ -175,7 +175,7 @@ class ForestBatch:
         if "_options" not in self.__dict__:
             self._options = {"tile_items": 128, "threads": 256, "int_mul": 0, "one_tap": 1,
                              "copy_points": 1, "path_tiles": 1 if self.T.itemsize == 8 else 0,
-                             "staged": 0, "pair_vars": 0, "copy_share": 0}
+                             "staged": 0, "pair_vars": 0, "copy_share": 0, "soft_add": 0}
         return self._options
 
     # the batch's tuning choices: every value of each, one option at a time
@@ -204,7 +204,7 @@ class ForestBatch:
 
         dims = list(self.TUNE)
         if self.T.itemsize == 8:
-            dims.append(("int_mul", (0, 1)))
+            dims += [("int_mul", (0, 1)), ("soft_add", (0, 1))]
         best = timed()
         for _ in range(sweeps):
             for name, values in dims:
