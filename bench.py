@@ -80,6 +80,9 @@ def parse():
                          "of the walls mesh read and write, print them and exit; 'all': every "
                          "stage, stencils with their whole source windows, and the whole fill's "
                          "least traffic against its algorithmic bytes")
+    ap.add_argument("--sector-unit", type=int, default=32,
+                    help="the access unit --sector-minimum counts in bytes (32: an L2 "
+                         "sector; 64: the DRAM's access unit)")
     return ap.parse_args()
 
 
@@ -189,7 +192,13 @@ def measure_batch(dev, timed, args, peak):
     batch.arena.uniform_(-1.0, 1.0, generator=g)
     esize = 4
     bytes_per_fill = 2 * batch.ghost_points() * esize
-    tuned = batch.autotune()
+    if args.options:
+        for kv in args.options.split(","):
+            k, v = kv.split("=")
+            batch.set_option(k.strip(), int(v))
+        tuned = dict(batch.options)
+    else:
+        tuned = batch.autotune()
     batch.arena.uniform_(-1.0, 1.0, generator=g)
     for _ in range(args.warmup):
         batch.fill()
@@ -620,11 +629,12 @@ def footprint_points(sched):
     return int(wr.sum()), int(rd.sum())
 
 
-def sector_minimum(sched, nvars: int, esize: int, tag: int, stencils: bool = False):
+def sector_minimum(sched, nvars: int, esize: int, tag: int, stencils: bool = False,
+                   unit: int = 32):
     """The least DRAM traffic of the unit copies of stage ``tag`` (with
     ``stencils``, of all its transfers, a stencil reading its whole source
-    window) that the layout allows: every distinct 32-byte sector they read
-    fetched once, every sector they write stored once, and (with
+    window) that the layout allows: every distinct ``unit``-byte sector they
+    read fetched once, every sector they write stored once, and (with
     read-modify-write) every partly written sector fetched once too.  Per
     variable plane, in bytes."""
     S1, S2, S3 = (tuple(sched.stored) + (1, 1))[:3]
@@ -655,18 +665,18 @@ def sector_minimum(sched, nvars: int, esize: int, tag: int, stencils: bool = Fal
         w = np.concatenate(wr) * esize
         r = np.concatenate(rd) * esize
         alg += 2 * w.size * esize              # a read and a write per point written
-        ws, wc = np.unique(w // 32, return_counts=True)
-        rs = np.unique(r // 32)
-        partial = ws[wc < 32 // esize]
+        ws, wc = np.unique(w // unit, return_counts=True)
+        rs = np.unique(r // unit)
+        partial = ws[wc < unit // esize]
         wr_s += ws.size
         rd_s += rs.size
         part_s += partial.size
         rp_s += np.union1d(rs, partial).size
-    return {"stage": tag, "groups": len(groups), "algorithmic_bytes": alg,
-            "sectors_read_bytes": rd_s * 32, "sectors_written_bytes": wr_s * 32,
-            "partly_written_bytes": part_s * 32,
-            "minimum_bytes": (rd_s + wr_s) * 32,
-            "minimum_bytes_with_rmw": (rp_s + wr_s) * 32}
+    return {"stage": tag, "groups": len(groups), "unit_bytes": unit, "algorithmic_bytes": alg,
+            "sectors_read_bytes": rd_s * unit, "sectors_written_bytes": wr_s * unit,
+            "partly_written_bytes": part_s * unit,
+            "minimum_bytes": (rd_s + wr_s) * unit,
+            "minimum_bytes_with_rmw": (rp_s + wr_s) * unit}
 
 
 def cpu_fill_rate(sched, fs_host_work, nvars, factors, bytes_per_fill, budget_s=15.0,
@@ -867,13 +877,15 @@ def main():
         esize = np.dtype(T).itemsize
         if args.sector_minimum == "all":
             tags = sorted({g.stage for g in sched.groups})
-            per = [sector_minimum(sched, fs.nvars, esize, t, stencils=True) for t in tags]
+            per = [sector_minimum(sched, fs.nvars, esize, t, stencils=True,
+                                  unit=args.sector_unit) for t in tags]
             alg = sum(p["algorithmic_bytes"] for p in per)
             least = sum(p["minimum_bytes_with_rmw"] for p in per)
             out = {"stages": per, "algorithmic_bytes": alg, "minimum_bytes_with_rmw": least,
                    "ceiling_frac_of_peak": alg / least}
         else:
-            out = sector_minimum(sched, fs.nvars, esize, int(args.sector_minimum))
+            out = sector_minimum(sched, fs.nvars, esize, int(args.sector_minimum),
+                                 unit=args.sector_unit)
         out.update({"roots": args.roots, "dtype": args.dtype, "blocks": f.nleaves(),
                     "levels": args.walls_levels})
         print(json.dumps(out), flush=True)

@@ -493,7 +493,9 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
 /* The order in which a fill's launches visit target blocks: 0 (the default)
  * the blocks' own order, 1 a reverse Cuthill-McKee order of the graph of
  * the schedule's transfers, which keeps blocks that exchange ghosts close
- * together in time (the sectors they share stay in L2). */
+ * together in time (the sectors they share stay in L2); 2 by source block
+ * first (the blocks' own order), then target: the transfers that read one
+ * block run together, so each source sector comes from DRAM once. */
 #define TAM_OPT_BLOCK_ORDER 6
 /* 1: a stage's stencil points grouped by their path through the kernel
  * (the order class and, in the CPU form, the dimensions that take one tap),
@@ -533,6 +535,10 @@ int tam_schedule_stage_groups(const tam_sched *s, int32_t *groups, int32_t *stag
  * GB300 gives 1/64 of the FP32 rate; the sum keeps the reference's order,
  * so the same bits.  0 (the default): every add on the FP64 pipe. */
 #define TAM_OPT_SOFT_ADD 12
+/* Box points per warp tile of the stencils, 16..4096, or 0 (the default):
+ * TAM_OPT_TILE_ITEMS for copies and stencils alike.  Copies want short
+ * tiles (their warps wait on memory), order-4 stencils longer ones. */
+#define TAM_OPT_STENCIL_TILE 13
 int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value);
 int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
@@ -542,8 +548,8 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
  * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
  * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER, TAM_OPT_COPY_POINTS and
- * TAM_OPT_COPY_SHARE (0, 1, 2, 4) and, for Float64, TAM_OPT_SOFT_ADD one at
- * a time, twice over; leaves the
+ * TAM_OPT_COPY_SHARE (0, 1, 2, 4), TAM_OPT_STENCIL_TILE (0, 32, 64, 128) and,
+ * for Float64, TAM_OPT_SOFT_ADD one at a time, twice over; leaves the
  * fastest set and returns the first three (the others through
  * tam_schedule_get_option).  The fills overwrite `work`'s ghosts (never an
  * own point).  Synchronizes `stream`; re-tiling allocates, so not inside a

@@ -36,7 +36,7 @@ def test_batch_fill_equals_member_fills(cuda_lib):
         assert np.array_equal(got.view(np.uint32), expect[m].view(np.uint32)), m
     # every grouping of the batch's work gives the same bits
     for opt, val in (("path_tiles", 1), ("copy_points", 4), ("tile_items", 48), ("staged", 1),
-                     ("copy_share", 2)):
+                     ("copy_share", 2), ("stencil_tile", 80)):
         batch.set_option(opt, val)
         batch.arena.copy_(start)
         batch.fill()
@@ -190,7 +190,7 @@ def test_native_autotune(cuda_lib):
     best = autotune(fs, s)
     assert set(best) == {"tile_items", "threads", "int_mul", "merge_stages", "path_tiles",
                          "staged", "pair_vars", "block_order", "copy_points",
-                         "copy_share", "soft_add"} and s._tuned_ms > 0
+                         "copy_share", "soft_add", "stencil_tile"} and s._tuned_ms > 0
     ds = device_schedule(s, 0)
     assert ds.options()["tile_items"] == best["tile_items"]
     fs.work.copy_(torch.from_numpy(host))

@@ -224,15 +224,16 @@ def test_launch_options_change_no_bit(cuda_lib):
     fs.work = torch.from_numpy(host).cuda()
     fs.factors = fs.factors.cuda()
     ds = device_schedule(s, 0)
-    for ti, th, im, cp, bo, pt, ms, sg, pv, cs, sa in (
-            (16, 64, 0, 1, 0, 0, 1, 1, 1, 1, 1),
-            (37, 96, 1, 2, 1, 1, 0, 1, 0, 0, 1),
-            (512, 512, 1, 4, 0, 1, 1, 0, 1, 2, 1),
-            (64, 128, 1, 1, 0, 1, 1, 0, 0, 2, 1),
-            (4096, 128, 0, 2, 1, 0, 0, 1, 1, 4, 0)):
+    for ti, th, im, cp, bo, pt, ms, sg, pv, cs, sa, st in (
+            (16, 64, 0, 1, 0, 0, 1, 1, 1, 1, 1, 0),
+            (37, 96, 1, 2, 1, 1, 0, 1, 0, 0, 1, 48),
+            (512, 512, 1, 4, 0, 1, 1, 0, 1, 2, 1, 16),
+            (64, 128, 1, 1, 2, 1, 1, 0, 0, 2, 1, 128),
+            (4096, 128, 0, 2, 1, 0, 0, 1, 1, 4, 0, 0)):
         opts = {"tile_items": ti, "threads": th, "int_mul": im, "one_tap": 1,
                 "copy_points": cp, "block_order": bo, "path_tiles": pt, "merge_stages": ms,
-                "staged": sg, "pair_vars": pv, "copy_share": cs, "soft_add": sa}
+                "staged": sg, "pair_vars": pv, "copy_share": cs, "soft_add": sa,
+                "stencil_tile": st}
         for k, v in opts.items():
             ds.set_option(k, v)
         assert ds.options() == opts

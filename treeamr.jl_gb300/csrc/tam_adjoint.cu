@@ -24,9 +24,14 @@
 //           sum the P^D taps of a point in the reference's order; its
 //           transpose has no reference rounding to follow, so the tensor
 //           product is applied as D passes of P taps each (3P multiply-adds
-//           a point instead of P^3 on the narrow FP64 pipe);
+//           a point instead of P^3 on the narrow FP64 pipe).  A copy that
+//           translates or mirrors (AdjGroup::direct) has no pass 1: its
+//           footprint is its target box read back through the same map;
 //   pass 2  one CTA per source block adds the boxes of the transfers reading
-//           it, in transfer order, one transfer at a time;
+//           it (a direct copy's read from its target box in place), in
+//           waves of transfers whose footprints do not meet, a barrier
+//           between waves, so that every point takes its adds in transfer
+//           order;
 //   zero    the stage's target points are set to zero.
 //
 // The transpose differs from the exact transpose of the rounded forward
@@ -136,13 +141,10 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int64_t tblock = __ldg(a.tb + tg.x) - 1;
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
     const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
-    // A unit copy whose source rows step by +-1 (a translation or a mirror):
-    // its transpose is the same permutation read backwards, so the box is
-    // the target values in place, +0 + f * y as the weight-one passes give.
-    const bool direct = g.pclass == 0 && g.affine &&
-                        (n1 == 1 || g.cstep[0] != 0) && (n2 == 1 || g.cstep[1] != 0) &&
-                        (n3 == 1 || g.cstep[2] != 0);
-    if (direct) {
+    // A direct copy (AdjGroup::direct) has no pass-1 work: the host leaves
+    // it out of the list, and pass 2 reads its target box in place.  The
+    // form below is that read, for a list that holds one all the same.
+    if (h.direct) {
       for (int v = 0; v < nvars; ++v) {
         const T *yv = L.y + tblock * L.bs + v * L.vs;
         const T f =
@@ -216,47 +218,82 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
 // RotationPair's partner: the same block and variable strides, the plane's
 // extents swapped, which the turn's strides carry; or y itself), so every
 // add into either array's block is this CTA's, in transfer order.
+// A CTA takes one source block and one variable (blockIdx.y): the
+// variables' adds are independent.  A block read by a turned transfer, which
+// moves a variable onto another, is one CTA's for every variable.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
     const AdjReduce *__restrict__ red, int64_t nred, const int2 *__restrict__ list,
-    AdjArgs<T> a, T *y, T *yalt, const T *scratch, int nvars, int S1, int S2, int S3) {
+    const uint8_t *__restrict__ wend, AdjArgs<T> a, T *y, T *yalt, const T *scratch,
+    const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
   using A = AArith<T>;
   for (int64_t b = blockIdx.x; b < nred; b += gridDim.x) {
     const AdjReduce r = red[b];
+    if (r.turned && blockIdx.y != 0) continue;
+    const int vlo = r.turned ? 0 : (int)blockIdx.y, vn = r.turned ? nvars : 1;
     // the transfers reading one block all belong to its forest
     const int member = a.groups[list[r.first].y].member;
-    const AdjLayout<T, BATCH> L(a, member, y, nullptr, nvars, S1, S2, S3);
+    const AdjLayout<T, BATCH> L(a, member, y, factors, nvars, S1, S2, S3);
     const AdjLayout<T, BATCH> La(a, member, yalt, nullptr, nvars, S1, S2, S3);
     for (int q = 0; q < r.count; ++q) {
       const int2 tg = list[r.first + q];  // (transfer, group)
       const AdjGroup &h = a.ag[tg.y];
       T *yb = ((h.col & 1) ? La.y : L.y) + (int64_t)r.sblock * L.bs;
-      const T *src = scratch + __ldg(a.scr + tg.x) * nvars;
-      const int64_t n = h.fsize * nvars;
+      const int64_t n = h.fsize * vn;
       const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
-      for (int64_t p = threadIdx.x; p < n; p += blockDim.x) {
-        const int v = (int)(p / h.fsize);
-        const int pt = (int)(p - (int64_t)v * h.fsize);
-        const int j3 = pt / f01;
-        const int rr = pt - j3 * f01;
-        const int j2 = rr / f0;
-        const int j1 = rr - j2 * f0;
-        T *dst;
-        if (h.col) {  // a turned group: through the axis map and the variable table
-          const int sv = __ldg(a.rotvars + v + (int64_t)nvars * h.col) - 1;
-          if (sv < 0 || sv >= nvars) {  // a table naming no variable: skip, and say so
-            if (a.err) atomicExch(a.err, (int32_t)TAM_EINVAL);
-            continue;
-          }
-          dst = yb + sv * L.vs + h.tc0 + h.tvs[0] * (h.flo[0] + j1) +
-                h.tvs[1] * (h.flo[1] + j2) + h.tvs[2] * (h.flo[2] + j3);
-        } else {
-          dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
-                (int64_t)(h.flo[2] + j3) * L.s3;
+      if (h.direct) {
+        // the target box in place: footprint point j reads target row
+        // j or n - 1 - j (a mirror) in each dimension, +0 + f * y
+        const DevGroup &g = a.groups[tg.y];
+        const T *yt = L.y + (int64_t)(__ldg(a.tb + tg.x) - 1) * L.bs;
+        const T *fc = g.factorcol ? L.factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
+        for (int64_t p = threadIdx.x; p < n; p += blockDim.x) {
+          const int vq = (int)(p / h.fsize);
+          const int pt = (int)(p - (int64_t)vq * h.fsize);
+          const int v = vlo + vq;
+          const int j3 = pt / f01;
+          const int rr = pt - j3 * f01;
+          const int j2 = rr / f0;
+          const int j1 = rr - j2 * f0;
+          const int i1 = g.cstep[0] < 0 ? g.n[0] - 1 - j1 : j1;
+          const int i2 = g.cstep[1] < 0 ? g.n[1] - 1 - j2 : j2;
+          const int i3 = g.cstep[2] < 0 ? g.n[2] - 1 - j3 : j3;
+          T x = yt[v * L.vs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
+                   (int64_t)(g.tf[2] + i3) * L.s3];
+          if (fc) x = A::mul(x, __ldg(fc + v));
+          x = A::add(x, T(0));
+          T *dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
+                   (int64_t)(h.flo[2] + j3) * L.s3;
+          *dst = A::add(*dst, x);
         }
-        *dst = A::add(*dst, src[p]);
+      } else {
+        const T *src = scratch + __ldg(a.scr + tg.x) * nvars + (int64_t)vlo * h.fsize;
+        for (int64_t p = threadIdx.x; p < n; p += blockDim.x) {
+          const int vq = (int)(p / h.fsize);
+          const int pt = (int)(p - (int64_t)vq * h.fsize);
+          const int v = vlo + vq;
+          const int j3 = pt / f01;
+          const int rr = pt - j3 * f01;
+          const int j2 = rr / f0;
+          const int j1 = rr - j2 * f0;
+          T *dst;
+          if (h.col) {  // a turned group: through the axis map and the variable table
+            const int sv = __ldg(a.rotvars + v + (int64_t)nvars * h.col) - 1;
+            if (sv < 0 || sv >= nvars) {  // a table naming no variable: skip, and say so
+              if (a.err) atomicExch(a.err, (int32_t)TAM_EINVAL);
+              continue;
+            }
+            dst = yb + sv * L.vs + h.tc0 + h.tvs[0] * (h.flo[0] + j1) +
+                  h.tvs[1] * (h.flo[1] + j2) + h.tvs[2] * (h.flo[2] + j3);
+          } else {
+            dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
+                  (int64_t)(h.flo[2] + j3) * L.s3;
+          }
+          *dst = A::add(*dst, src[p]);
+        }
       }
-      __syncthreads();
+      // the next wave may add onto points this one did
+      if (wend[r.first + q]) __syncthreads();
     }
   }
 }
@@ -354,10 +391,12 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
       if (e != cudaSuccess) return e;
     }
     if (st.nred > 0) {
+      if (nvars > 65535) return cudaErrorInvalidValue;  // a CTA row per variable
       const int64_t blocks = std::min<int64_t>(st.nred, (int64_t)1 << 30);
-      adjoint_reduce_kernel<T, D, BATCH><<<(unsigned)blocks, threads, 0, stream>>>(
-          p.red + st.red0, st.nred, (const int2 *)p.list, a, y, r.alt ? (T *)r.alt : y, scratch,
-          nvars, S1, S2, S3);
+      adjoint_reduce_kernel<T, D, BATCH><<<dim3((unsigned)blocks, (unsigned)nvars), threads, 0,
+                                           stream>>>(
+          p.red + st.red0, st.nred, (const int2 *)p.list, p.wend, a, y,
+          r.alt ? (T *)r.alt : y, scratch, factors, nvars, S1, S2, S3);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -413,6 +452,7 @@ struct AdjHost {
   std::vector<int2> xfers;       // per stage, by target block
   std::vector<AdjReduce> red;
   std::vector<int2> list;
+  std::vector<uint8_t> wend;     // per list entry: 1 ends a wave
   std::vector<AdjStage> stages;  // one per forward stage
   int64_t maxpts = 0;
 };
@@ -475,6 +515,8 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
       err = "the adjoint's transposed stencils exceed 2^31 entries";
       return TAM_EUNSUPPORTED;
     }
+    a.direct = g.pclass == 0 && g.affine && !g.turned && (g.n[0] == 1 || g.cstep[0] != 0) &&
+               (g.n[1] == 1 || g.cstep[1] != 0) && (g.n[2] == 1 || g.cstep[2] != 0);
   }
   // turned groups: their footprints land on the real source through the
   // strides the forward launch reads it by
@@ -503,9 +545,9 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
     std::vector<E> byt = es;
     std::sort(byt.begin(), byt.end(), [](const E &x, const E &y) { return x.transfer < y.transfer; });
     int64_t pts = 0;
-    for (const E &e : byt) {
+    for (const E &e : byt) {  // a direct copy needs none
       o.scr[e.transfer] = pts;
-      pts += o.ag[e.group].fsize;
+      if (!o.ag[e.group].direct) pts += o.ag[e.group].fsize;
     }
     st.scratch_points = pts;
     o.maxpts = std::max(o.maxpts, pts);
@@ -513,7 +555,9 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
     std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
       return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
     });
-    for (const E &e : es) o.xfers.push_back(make_int2(e.transfer, e.group));
+    // (a direct copy has no pass-1 work)
+    for (const E &e : es)
+      if (!o.ag[e.group].direct) o.xfers.push_back(make_int2(e.transfer, e.group));
     st.ntiles = (int64_t)o.xfers.size() - st.tile0;
     for (int32_t gi : fw.groups) {
       const DevGroup &g = s->groups[gi];
@@ -530,8 +574,33 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
     for (size_t i = 0; i < byt.size();) {
       size_t j = i;
       while (j < byt.size() && byt[j].sblock == byt[i].sblock) ++j;
-      o.red.push_back({byt[i].sblock - 1, (int32_t)(j - i), (int64_t)o.list.size()});
-      for (size_t k = i; k < j; ++k) o.list.push_back(make_int2(byt[k].transfer, byt[k].group));
+      bool turned = false;
+      for (size_t k = i; k < j; ++k) turned = turned || o.ag[byt[k].group].col != 0;
+      o.red.push_back({byt[i].sblock - 1, (int32_t)(j - i), (int64_t)o.list.size(),
+                       turned ? 1 : 0, 0});
+      // waves: a transfer goes one past the last wave of an earlier one whose
+      // footprint it meets (a turned one meets every other: its footprint
+      // lands through the turn, and an odd turn on the partner's array)
+      std::vector<int> wave(j - i, 0);
+      auto meets = [&](const E &p, const E &q) {
+        const AdjGroup &x = o.ag[p.group], &y = o.ag[q.group];
+        if (x.col || y.col) return true;
+        for (int d = 0; d < 3; ++d)
+          if (x.flo[d] + x.fn[d] <= y.flo[d] || y.flo[d] + y.fn[d] <= x.flo[d]) return false;
+        return true;
+      };
+      for (size_t k = i; k < j; ++k)
+        for (size_t l = i; l < k; ++l)
+          if (wave[l - i] >= wave[k - i] && meets(byt[l], byt[k])) wave[k - i] = wave[l - i] + 1;
+      std::vector<size_t> ord(j - i);
+      for (size_t k = 0; k < ord.size(); ++k) ord[k] = k;
+      std::stable_sort(ord.begin(), ord.end(),
+                       [&](size_t x, size_t y) { return wave[x] < wave[y]; });
+      for (size_t k = 0; k < ord.size(); ++k) {
+        const E &e = byt[i + ord[k]];
+        o.list.push_back(make_int2(e.transfer, e.group));
+        o.wend.push_back(k + 1 == ord.size() || wave[ord[k + 1]] != wave[ord[k]] ? 1 : 0);
+      }
       i = j;
     }
     st.nred = (int64_t)o.red.size() - st.red0;
@@ -551,7 +620,8 @@ int upload_plan(AdjPlan &p, const AdjHost &o, int dtype, std::string &err) {
   if ((e = up(&p.groups, o.ag)) != cudaSuccess || (e = up(&p.off, o.off)) != cudaSuccess ||
       (e = up((int2 **)&p.ent, o.ent)) != cudaSuccess || (e = up(&p.scr, o.scr)) != cudaSuccess ||
       (e = up((int2 **)&p.xfers, o.xfers)) != cudaSuccess || (e = up(&p.red, o.red)) != cudaSuccess ||
-      (e = up((int2 **)&p.list, o.list)) != cudaSuccess) {
+      (e = up((int2 **)&p.list, o.list)) != cudaSuccess ||
+      (e = up(&p.wend, o.wend)) != cudaSuccess) {
     adjoint_plan_free(p);
     err = std::string("adjoint upload: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? TAM_ENOMEM : TAM_ECUDA;
@@ -572,6 +642,7 @@ void adjoint_plan_free(AdjPlan &p) {
   cudaFree(p.xfers);
   cudaFree(p.red);
   cudaFree(p.list);
+  cudaFree(p.wend);
   p = AdjPlan{};
 }
 
@@ -649,6 +720,7 @@ int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members
         for (int32_t q = 0; q < r.count; ++q) {
           const int2 x = h.list[r.first + q];
           o.list.push_back(make_int2(x.x + T0, x.y + G0));
+          o.wend.push_back(h.wend[r.first + q]);
         }
         r.first = first;
         o.red.push_back(r);

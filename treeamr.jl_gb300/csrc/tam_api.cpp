@@ -420,20 +420,26 @@ std::vector<int32_t> block_rank(const tam_sched *s) {
 void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int32_t> &rank,
               tam::StencilRuns &runs, std::vector<tam::Tile> &tiles,
               std::vector<uint16_t> &keys, std::vector<tam::Tile> &staged) {
-  const int ti = s->shape.tile_items;
+  const int ti = s->shape.tile_items, tst = s->shape.stencil_items();
   for (tam::Stage &st : list) {
     st.tile0 = (int64_t)tiles.size();
     struct Entry {
-      int32_t tblock, group, transfer;
+      int32_t tblock, group, transfer, sblock;
     };
     std::vector<Entry> entries;
     for (int32_t gi : st.groups) {
       const tam::DevGroup &g = s->groups[gi];
       if (g.turned) continue;  // a turned group has a launch of its own
       for (int64_t t = 0; t < g.ntransfers; ++t)
-        entries.push_back({rank[s->h_tb[g.first + t] - 1], gi, (int32_t)(g.first + t)});
+        entries.push_back({rank[s->h_tb[g.first + t] - 1], gi, (int32_t)(g.first + t),
+                           s->h_sb[g.first + t] - 1});
     }
-    std::stable_sort(entries.begin(), entries.end(), [](const Entry &a, const Entry &b) {
+    // by target block, or (TAM_OPT_BLOCK_ORDER 2) by source block first: the
+    // transfers that read one block's edges then run together, and its
+    // sectors come from DRAM once
+    const bool by_source = s->shape.block_order == 2;
+    std::stable_sort(entries.begin(), entries.end(), [&](const Entry &a, const Entry &b) {
+      if (by_source && a.sblock != b.sblock) return a.sblock < b.sblock;
       return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
     });
     // unit copies first (the light kernel; those without a factor column
@@ -458,8 +464,8 @@ void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int
       if (tile_pass(g) != 2) continue;
       if (!s->shape.path_tiles) {  // by target block alone: one key
         const int box = g.n[0] * g.n[1] * g.n[2];
-        for (int i0 = 0; i0 < box; i0 += ti) {
-          sten.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+        for (int i0 = 0; i0 < box; i0 += tst) {
+          sten.push_back({e.group, e.transfer, i0, std::min(tst, box - i0)});
           skeys.push_back(0);
         }
         continue;
@@ -467,7 +473,7 @@ void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int
       if (!runs.cache.count(e.group))
         tam::StencilRuns::of(g, s->h_pool_csingle.data(), s->h_pool_perm.data(), s->D,
                              runs.cache[e.group]);
-      runs.tiles(e.group, e.transfer, ti, sten, skeys);
+      runs.tiles(e.group, e.transfer, tst, sten, skeys);
     }
     // with TAM_OPT_STAGED, a staged group's tiles go last: the stencil kernel
     // leaves them to the staged kernel, which takes the group's transfers
@@ -520,8 +526,10 @@ std::vector<tam::Tile> build_tiles(tam_sched *s, std::vector<uint16_t> &keys,
 // Packed tiles of every stage, then of every stage group.
 std::vector<tam::PTile> pack_all(tam_sched *s, const std::vector<tam::Tile> &tiles,
                                  const std::vector<uint16_t> &keys) {
-  std::vector<tam::PTile> out = tam::pack_stages(s->stages, tiles, s->shape.tile_items, &keys);
-  std::vector<tam::PTile> more = tam::pack_stages(s->merged, tiles, s->shape.tile_items, &keys);
+  std::vector<tam::PTile> out =
+      tam::pack_stages(s->stages, tiles, s->shape.tile_items, &keys, s->shape.stencil_items());
+  std::vector<tam::PTile> more =
+      tam::pack_stages(s->merged, tiles, s->shape.tile_items, &keys, s->shape.stencil_items());
   for (tam::Stage &m : s->merged) m.ptile0 += (int64_t)out.size();
   out.insert(out.end(), more.begin(), more.end());
   return out;
@@ -1272,17 +1280,24 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
   if (!s) return fail(nullptr, TAM_EINVAL, "tam_schedule_set_option: NULL schedule");
   switch (option) {
     case TAM_OPT_TILE_ITEMS:
+    case TAM_OPT_STENCIL_TILE:
     case TAM_OPT_BLOCK_ORDER:
     case TAM_OPT_PATH_TILES:
     case TAM_OPT_STAGED: {
-      int *field = option == TAM_OPT_TILE_ITEMS    ? &s->shape.tile_items
-                   : option == TAM_OPT_BLOCK_ORDER ? &s->shape.block_order
-                   : option == TAM_OPT_PATH_TILES  ? &s->shape.path_tiles
-                                                   : &s->shape.staged;
+      int *field = option == TAM_OPT_TILE_ITEMS     ? &s->shape.tile_items
+                   : option == TAM_OPT_STENCIL_TILE ? &s->shape.stencil_tile
+                   : option == TAM_OPT_BLOCK_ORDER  ? &s->shape.block_order
+                   : option == TAM_OPT_PATH_TILES   ? &s->shape.path_tiles
+                                                    : &s->shape.staged;
       if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
         return fail(s->ctx, TAM_EINVAL, "tile items must be in 16..4096");
-      if (option != TAM_OPT_TILE_ITEMS && value != 0 && value != 1)
-        return fail(s->ctx, TAM_EINVAL, "block_order, path_tiles and staged are 0 or 1");
+      if (option == TAM_OPT_STENCIL_TILE && value != 0 && (value < 16 || value > 4096))
+        return fail(s->ctx, TAM_EINVAL, "stencil tile items are 0 or in 16..4096");
+      if (option == TAM_OPT_BLOCK_ORDER && (value < 0 || value > 2))
+        return fail(s->ctx, TAM_EINVAL, "block_order is 0, 1 or 2");
+      if ((option == TAM_OPT_PATH_TILES || option == TAM_OPT_STAGED) && value != 0 &&
+          value != 1)
+        return fail(s->ctx, TAM_EINVAL, "path_tiles and staged are 0 or 1");
       if (value == *field) return TAM_OK;
       DeviceGuard guard(s->ctx->device);
       const int old = *field;
@@ -1368,6 +1383,7 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
     case TAM_OPT_PATH_TILES: *value = s->shape.path_tiles; return TAM_OK;
     case TAM_OPT_COPY_SHARE: *value = s->shape.copy_share; return TAM_OK;
     case TAM_OPT_SOFT_ADD: *value = s->shape.soft_add; return TAM_OK;
+    case TAM_OPT_STENCIL_TILE: *value = s->shape.stencil_tile; return TAM_OK;
     default: return fail(s->ctx, TAM_EINVAL, "unknown option");
   }
 }

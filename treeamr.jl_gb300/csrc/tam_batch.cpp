@@ -127,7 +127,7 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys,
   keys.clear();
   staged.clear();
   tam::StencilRuns runs;
-  const int ti = b->shape.tile_items;
+  const int ti = b->shape.tile_items, tst = b->shape.stencil_items();
   for (tam::Stage &st : b->stages) {
     st.tile0 = (int64_t)tiles.size();
     struct Entry {
@@ -165,8 +165,8 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys,
       if (tam::tile_pass(g) != 2) continue;
       if (!b->shape.path_tiles) {  // by target block alone: one key
         const int box = g.n[0] * g.n[1] * g.n[2];
-        for (int i0 = 0; i0 < box; i0 += ti) {
-          sten.push_back({e.group, e.transfer, i0, std::min(ti, box - i0)});
+        for (int i0 = 0; i0 < box; i0 += tst) {
+          sten.push_back({e.group, e.transfer, i0, std::min(tst, box - i0)});
           skeys.push_back(0);
         }
         continue;
@@ -174,7 +174,7 @@ std::vector<tam::Tile> batch_tiles(tam_batch *b, std::vector<uint16_t> &keys,
       if (!runs.cache.count(e.group))
         tam::StencilRuns::of(g, b->h_csingle.data(), b->h_perm.data(), b->D,
                              runs.cache[e.group]);
-      runs.tiles(e.group, e.transfer, ti, sten, skeys);
+      runs.tiles(e.group, e.transfer, tst, sten, skeys);
     }
     // staged groups' tiles last (the staged kernel takes their transfers)
     const bool staging = b->shape.staged != 0;
@@ -354,7 +354,8 @@ int tam_batch_create(tam_ctx *ctx, tam_sched *const *members, int32_t n,
   std::vector<tam::Tile> staged;
   std::vector<tam::Tile> tiles = batch_tiles(b, keys, staged);
   std::vector<tam::PTile> ptiles =
-      tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
+      tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys,
+                         b->shape.stencil_items());
   std::vector<uint64_t> wshort;
   if (b->dtype == TAM_F64) wshort = tam::short_weights(wtab);
   if (wshort.empty()) wshort.push_back(0);
@@ -511,14 +512,17 @@ int tam_batch_device_status(tam_batch *b, void *stream, int32_t *code) {
 
 int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
   if (!b) return TAM_EINVAL;
-  if (option == TAM_OPT_TILE_ITEMS || option == TAM_OPT_PATH_TILES ||
-      option == TAM_OPT_STAGED) {
-    int *field = option == TAM_OPT_TILE_ITEMS   ? &b->shape.tile_items
-                 : option == TAM_OPT_PATH_TILES ? &b->shape.path_tiles
-                                                : &b->shape.staged;
+  if (option == TAM_OPT_TILE_ITEMS || option == TAM_OPT_STENCIL_TILE ||
+      option == TAM_OPT_PATH_TILES || option == TAM_OPT_STAGED) {
+    int *field = option == TAM_OPT_TILE_ITEMS     ? &b->shape.tile_items
+                 : option == TAM_OPT_STENCIL_TILE ? &b->shape.stencil_tile
+                 : option == TAM_OPT_PATH_TILES   ? &b->shape.path_tiles
+                                                  : &b->shape.staged;
     if (option == TAM_OPT_TILE_ITEMS && (value < 16 || value > 4096))
       return bfail(b->ctx, TAM_EINVAL, "tile items must be in 16..4096");
-    if (option != TAM_OPT_TILE_ITEMS && value != 0 && value != 1)
+    if (option == TAM_OPT_STENCIL_TILE && value != 0 && (value < 16 || value > 4096))
+      return bfail(b->ctx, TAM_EINVAL, "stencil tile items are 0 or in 16..4096");
+    if ((option == TAM_OPT_PATH_TILES || option == TAM_OPT_STAGED) && value != 0 && value != 1)
       return bfail(b->ctx, TAM_EINVAL, "path_tiles and staged are 0 or 1");
     Guard guard(b->ctx->device);
     const int old = *field;
@@ -527,7 +531,8 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
     std::vector<tam::Tile> staged;
     std::vector<tam::Tile> tiles = batch_tiles(b, keys, staged);
     std::vector<tam::PTile> ptiles =
-        tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys);
+        tam::pack_stages(b->stages, tiles, b->shape.tile_items, &keys,
+                         b->shape.stencil_items());
     tam::Tile *d = nullptr, *dst = nullptr;
     tam::PTile *dp = nullptr;
     cudaError_t e = up(&d, tiles.data(), tiles.size());
@@ -539,7 +544,7 @@ int tam_batch_set_option(tam_batch *b, int32_t option, int64_t value) {
       cudaFree(dst);
       *field = old;
       std::vector<tam::Tile> back = batch_tiles(b, keys, staged);
-      tam::pack_stages(b->stages, back, b->shape.tile_items, &keys);
+      tam::pack_stages(b->stages, back, b->shape.tile_items, &keys, b->shape.stencil_items());
       return bfail(b->ctx, TAM_ECUDA, "re-tiling the batch failed");
     }
     cudaDeviceSynchronize();

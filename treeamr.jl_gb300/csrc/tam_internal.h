@@ -125,7 +125,8 @@ void pack_tiles(const std::vector<Tile> &tiles, const std::vector<uint16_t> *key
 struct Stage;
 // Every stage's packed tiles (sets the stages' ptile0, npcopy, nptiles).
 std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
-                               int target, const std::vector<uint16_t> *keys = nullptr);
+                               int target, const std::vector<uint16_t> *keys = nullptr,
+                               int stencil_target = 0);
 
 // A stencil group's box points in tile order cut into runs that take the
 // same path through the stencil kernel: the same order class and, in the
@@ -196,7 +197,11 @@ struct AdjGroup {
   // at tc0 + sum_d tvs[d] * row[d], real variable rotvars[v + nvars * col] - 1
   // (col 0: an ordinary group, the footprint in place).
   int32_t col;
-  int32_t pad;
+  // A unit copy whose source rows step by +-1 in every dimension of more
+  // than one row (a translation or a mirror, not turned): its transpose is
+  // the target box read back through the same map, which pass 2 reads in
+  // place (pass 1 has nothing to do for it).
+  int32_t direct;
   int64_t tvs[3];
   int64_t tc0;
 };
@@ -212,11 +217,16 @@ struct AdjStage {
 };
 
 // Pass 2's work for one source block: the transfers reading it,
-// list[first .. first + count), in transfer order.
+// list[first .. first + count), in waves: a transfer's footprint meets no
+// other footprint of its wave, and one that meets an earlier transfer's
+// (in transfer order) is in a later wave, so every point's adds keep
+// transfer order; wend[i] marks the last entry of a wave.
 struct AdjReduce {
   int32_t sblock;  // 0-based
   int32_t count;
   int64_t first;
+  int32_t turned;  // a turned transfer among them: one CTA takes every variable
+  int32_t pad;
 };
 
 // The adjoint's arrays on the device (tam_adjoint.cu), for one schedule or a
@@ -230,6 +240,7 @@ struct AdjPlan {
   void *xfers = nullptr;         // pass-1 transfers, int2 (transfer, group)
   AdjReduce *red = nullptr;      // pass-2 reduction blocks
   void *list = nullptr;          // their transfers, int2 (transfer, group)
+  uint8_t *wend = nullptr;       // per list entry: 1 ends a wave
   std::vector<AdjStage> stages;  // one per forward stage, in the same order
   int64_t scratch_points = 0;    // max over stages, per variable
   bool ready = false;
@@ -248,6 +259,8 @@ struct LaunchShape {
   int pair_vars = 0;        // Float64 order-4 stencils two variables a lane (TAM_OPT_PAIR_VARS)
   int copy_share = 0;       // copy CTAs a multiprocessor beside the stencils (TAM_OPT_COPY_SHARE)
   int soft_add = 0;         // Float64 order 4: a tap a row added on the integer pipe (TAM_OPT_SOFT_ADD)
+  int stencil_tile = 0;     // box points per stencil tile, 0: tile_items (TAM_OPT_STENCIL_TILE)
+  int stencil_items() const { return stencil_tile ? stencil_tile : tile_items; }
 };
 
 }  // namespace tam

@@ -1492,7 +1492,9 @@ void pack_tiles(const std::vector<Tile> &tiles, const std::vector<uint16_t> *key
 }
 
 std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Tile> &tiles,
-                               int target, const std::vector<uint16_t> *keys) {
+                               int target, const std::vector<uint16_t> *keys,
+                               int stencil_target) {
+  const int ts = stencil_target > 0 ? stencil_target : target;
   std::vector<PTile> out;
   for (Stage &st : stages) {
     st.ptile0 = (int64_t)out.size();
@@ -1510,11 +1512,11 @@ std::vector<PTile> pack_stages(std::vector<Stage> &stages, const std::vector<Til
       e4 = b4;
       while (e4 < send && four(e4)) ++e4;
     }
-    pack_tiles(tiles, keys, st.tile0 + st.ncopy, b4, target, out);
+    pack_tiles(tiles, keys, st.tile0 + st.ncopy, b4, ts, out);
     st.np4_0 = (int64_t)out.size() - st.ptile0;
-    pack_tiles(tiles, keys, b4, e4, target, out);
+    pack_tiles(tiles, keys, b4, e4, ts, out);
     st.np4 = (int64_t)out.size() - st.ptile0 - st.np4_0;
-    pack_tiles(tiles, keys, e4, send, target, out);
+    pack_tiles(tiles, keys, e4, send, ts, out);
     st.nptiles = (int64_t)out.size() - st.ptile0;
   }
   return out;

@@ -114,7 +114,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   // lane of the copy kernel, the copies' share of the machine beside the
   // stencils
   int64_t old_pt = 0, old_bo = 0, old_cp = 1, old_ms = 1, old_sg = 0, old_pv = 0, old_cs = 0;
-  int64_t old_sa = 0;
+  int64_t old_sa = 0, old_st = 0;
   tam_schedule_get_option(s, TAM_OPT_PATH_TILES, &old_pt);
   tam_schedule_get_option(s, TAM_OPT_BLOCK_ORDER, &old_bo);
   tam_schedule_get_option(s, TAM_OPT_COPY_POINTS, &old_cp);
@@ -123,6 +123,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
   tam_schedule_get_option(s, TAM_OPT_PAIR_VARS, &old_pv);
   tam_schedule_get_option(s, TAM_OPT_COPY_SHARE, &old_cs);
   tam_schedule_get_option(s, TAM_OPT_SOFT_ADD, &old_sa);
+  tam_schedule_get_option(s, TAM_OPT_STENCIL_TILE, &old_st);
   if (rc == TAM_OK) {
     (void)((rc = tam_schedule_set_option(s, TAM_OPT_INT_MUL, bim)) == TAM_OK &&
            (rc = tam_schedule_set_option(s, TAM_OPT_TILE_ITEMS, bt)) == TAM_OK &&
@@ -137,10 +138,11 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
               {TAM_OPT_PATH_TILES, {0, 1, 0}, 2, old_pt},
               {TAM_OPT_STAGED, {0, 1, 0}, 2, old_sg},
               {TAM_OPT_PAIR_VARS, {0, 1, 0}, dtype_f64 ? 2 : 1, old_pv},
-              {TAM_OPT_BLOCK_ORDER, {0, 1, 0}, 2, old_bo},
+              {TAM_OPT_BLOCK_ORDER, {0, 1, 2}, 3, old_bo},
               {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp},
               {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs},
-              {TAM_OPT_SOFT_ADD, {0, 1, 0, 0}, dtype_f64 ? 2 : 1, old_sa}};
+              {TAM_OPT_SOFT_ADD, {0, 1, 0, 0}, dtype_f64 ? 2 : 1, old_sa},
+              {TAM_OPT_STENCIL_TILE, {0, 32, 64, 128}, 4, old_st}};
   // two sweeps: the options interact (the copies' share of the machine and
   // the stencils' tiling, for one), so the second revisits each from the
   // others' best
@@ -175,6 +177,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
     tam_schedule_set_option(s, TAM_OPT_PAIR_VARS, old_pv);
     tam_schedule_set_option(s, TAM_OPT_COPY_SHARE, old_cs);
     tam_schedule_set_option(s, TAM_OPT_SOFT_ADD, old_sa);
+    tam_schedule_set_option(s, TAM_OPT_STENCIL_TILE, old_st);
     return rc;
   }
   if (tile_items) *tile_items = bt;

@@ -71,7 +71,7 @@ def autotune(fs: FieldSet, sched: GhostSchedule, *, reps: int = 3,
         best = {"tile_items": out[0].value, "threads": out[1].value, "int_mul": out[2].value}
         opts = ds.options()
         for k in ("merge_stages", "path_tiles", "staged", "pair_vars", "block_order",
-                  "copy_points", "copy_share", "soft_add"):
+                  "copy_points", "copy_share", "soft_add", "stencil_tile"):
             best[k] = opts[k]
         cache[key] = dict(best)
         sched._tuned_ms = ms.value

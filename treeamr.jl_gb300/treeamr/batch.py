@@ -164,7 +164,7 @@ class ForestBatch:
     def set_option(self, name: str, value: int):
         code = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
                 "path_tiles": 7, "staged": 9, "pair_vars": 10,
-                "copy_share": 11, "soft_add": 12}[name]
+                "copy_share": 11, "soft_add": 12, "stencil_tile": 13}[name]
         _native.check(self.lib.tam_batch_set_option(self.handle, code, int(value)), self.ctx,
                       f"tam_batch_set_option({name})")
         self.options[name] = int(value)
@@ -175,12 +175,14 @@ class ForestBatch:
         if "_options" not in self.__dict__:
             self._options = {"tile_items": 128, "threads": 256, "int_mul": 0, "one_tap": 1,
                              "copy_points": 1, "path_tiles": 1 if self.T.itemsize == 8 else 0,
-                             "staged": 0, "pair_vars": 0, "copy_share": 0, "soft_add": 0}
+                             "staged": 0, "pair_vars": 0, "copy_share": 0, "soft_add": 0,
+                             "stencil_tile": 0}
         return self._options
 
     # the batch's tuning choices: every value of each, one option at a time
     TUNE = (("tile_items", (32, 64, 128, 256, 512)), ("threads", (128, 256, 512)),
-            ("copy_points", (1, 2, 4)), ("copy_share", (0, 2, 4)), ("path_tiles", (0, 1)))
+            ("copy_points", (1, 2, 4)), ("copy_share", (0, 2, 4)), ("path_tiles", (0, 1)),
+            ("stencil_tile", (0, 32, 64, 128)))
 
     def autotune(self, reps: int = 3, sweeps: int = 2) -> dict:
         """Pick the batch's launch options by timing whole fills (CUDA events,

@@ -129,7 +129,7 @@ class DeviceSchedule:
     OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
                "block_order": 6, "path_tiles": 7, "merge_stages": 8,
                "staged": 9, "pair_vars": 10, "copy_share": 11,
-               "soft_add": 12}
+               "soft_add": 12, "stencil_tile": 13}
 
     def set_option(self, name: str, value: int):
         _native.check(self.lib.tam_schedule_set_option(self.handle, self.OPTIONS[name], int(value)),
