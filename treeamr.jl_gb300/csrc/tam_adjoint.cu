@@ -115,7 +115,7 @@ struct AdjLayout {
   }
 };
 
-// Pass 1: one CTA per transfer, the box passes in shared memory.  Entries of
+// Pass 1: one CTA per transfer and variable, the box passes in shared memory.  Entries of
 // dimension d's transposed stencil are (i, w): target row i, weight index w
 // into the weight pool; a dimension beyond D has one entry of weight one.
 // Per variable: A = f * y over the target box (n1 x n2 x n3, row 1 fastest),
@@ -141,29 +141,11 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int64_t tblock = __ldg(a.tb + tg.x) - 1;
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
     const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
-    // A direct copy (AdjGroup::direct) has no pass-1 work: the host leaves
-    // it out of the list, and pass 2 reads its target box in place.  The
-    // form below is that read, for a list that holds one all the same.
-    if (h.direct) {
-      for (int v = 0; v < nvars; ++v) {
-        const T *yv = L.y + tblock * L.bs + v * L.vs;
-        const T f =
-            g.factorcol ? __ldg(L.factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
-        T *ov = out + (int64_t)v * h.fsize;
-        for (int k = tid; k < nO; k += nt) {
-          const int j3 = k / (f1 * f2), r = k - j3 * (f1 * f2), j2 = r / f1, j1 = r - j2 * f1;
-          const int i1 = g.cstep[0] < 0 ? n1 - 1 - j1 : j1;
-          const int i2 = g.cstep[1] < 0 ? n2 - 1 - j2 : j2;
-          const int i3 = g.cstep[2] < 0 ? n3 - 1 - j3 : j3;
-          T x = yv[(g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
-                   (int64_t)(g.tf[2] + i3) * L.s3];
-          if (g.factorcol) x = A::mul(x, f);
-          ov[k] = A::add(x, T(0));
-        }
-      }
-      continue;
-    }
-    for (int v = 0; v < nvars; ++v) {
+    // a direct copy (AdjGroup::direct) has no pass-1 work and no scratch:
+    // the host leaves it out of the list
+    if (h.direct) continue;
+    // a variable a CTA row (blockIdx.y): the variables' passes are independent
+    for (int v = blockIdx.y; v < nvars; v += gridDim.y) {
       const T *yv = L.y + tblock * L.bs + v * L.vs;
       const T f =
           g.factorcol ? __ldg(L.factors + v + (int64_t)nvars * (g.factorcol - 1)) : T(1);
@@ -213,14 +195,14 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
   }
 }
 
-// Pass 2: one CTA per source block, its transfers' boxes added in order.
-// An odd turn adds onto the block of the alternate array `yalt` (a
+// Pass 2: one CTA per source block and variable (blockIdx.y; the variables'
+// adds are independent), its transfers' boxes added in waves (AdjReduce), so
+// every point takes its adds in transfer order.  A block read by a turned
+// transfer, which moves a variable onto another, is one CTA's for every
+// variable.  An odd turn adds onto the block of the alternate array `yalt` (a
 // RotationPair's partner: the same block and variable strides, the plane's
 // extents swapped, which the turn's strides carry; or y itself), so every
 // add into either array's block is this CTA's, in transfer order.
-// A CTA takes one source block and one variable (blockIdx.y): the
-// variables' adds are independent.  A block read by a turned transfer, which
-// moves a variable onto another, is one CTA's for every variable.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
     const AdjReduce *__restrict__ red, int64_t nred, const int2 *__restrict__ list,
@@ -384,7 +366,9 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
         if (e != cudaSuccess) return e;
       }
       const int64_t blocks = std::min<int64_t>(st.ntiles, (int64_t)1 << 30);
-      adjoint_box_kernel<T, D, BATCH><<<(unsigned)blocks, 128, smem, stream>>>(
+      if (nvars > 65535) return cudaErrorInvalidValue;  // a CTA row per variable
+      adjoint_box_kernel<T, D, BATCH><<<dim3((unsigned)blocks, (unsigned)nvars), 128, smem,
+                                       stream>>>(
           (const int2 *)p.xfers + st.tile0, st.ntiles, a, y, scratch, factors, nvars, S1, S2,
           S3);
       cudaError_t e = cudaGetLastError();
