@@ -32,8 +32,7 @@
 //           waves of transfers whose footprints do not meet, a barrier
 //           between waves, so that every point takes its adds in transfer
 //           order;
-//   zero    the stage's target points are set to zero (a direct copy's by
-//           pass 2 as it reads them).
+//   zero    the stage's target points are set to zero.
 //
 // The transpose differs from the exact transpose of the rounded forward
 // weights ((w_1*w_2)*w_3) by the rounding of the products, a few units in
@@ -226,12 +225,9 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
       const int f0 = h.fn[0], f01 = h.fn[0] * h.fn[1];
       if (h.direct) {
         // the target box in place: footprint point j reads target row
-        // j or n - 1 - j (a mirror) in each dimension, +0 + f * y, and
-        // zeroes it (no other transfer of the stage reads it: every target
-        // point is one transfer's, and no target is a source); the zero
-        // pass leaves direct copies' targets alone
+        // j or n - 1 - j (a mirror) in each dimension, +0 + f * y
         const DevGroup &g = a.groups[tg.y];
-        T *yt = L.y + (int64_t)(__ldg(a.tb + tg.x) - 1) * L.bs;
+        const T *yt = L.y + (int64_t)(__ldg(a.tb + tg.x) - 1) * L.bs;
         const T *fc = g.factorcol ? L.factors + (int64_t)nvars * (g.factorcol - 1) : nullptr;
         for (int64_t p = threadIdx.x; p < n; p += blockDim.x) {
           const int vq = (int)(p / h.fsize);
@@ -244,10 +240,8 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
           const int i1 = g.cstep[0] < 0 ? g.n[0] - 1 - j1 : j1;
           const int i2 = g.cstep[1] < 0 ? g.n[1] - 1 - j2 : j2;
           const int i3 = g.cstep[2] < 0 ? g.n[2] - 1 - j3 : j3;
-          T *tp = yt + v * L.vs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
-                  (int64_t)(g.tf[2] + i3) * L.s3;
-          T x = *tp;
-          *tp = T(0);
+          T x = yt[v * L.vs + (g.tf[0] + i1) + (int64_t)(g.tf[1] + i2) * L.s2 +
+                   (int64_t)(g.tf[2] + i3) * L.s3];
           if (fc) x = A::mul(x, __ldg(fc + v));
           x = A::add(x, T(0));
           T *dst = yb + v * L.vs + (h.flo[0] + j1) + (int64_t)(h.flo[1] + j2) * L.s2 +
@@ -286,8 +280,7 @@ __global__ void __launch_bounds__(256) adjoint_reduce_kernel(
   }
 }
 
-// Zero the targets of a stage: the forward tiles of the stage (a direct
-// copy's, pass 2 zeroed already).
+// Zero the targets of a stage: the forward tiles of the stage.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restrict__ tiles,
                                                            int64_t ntiles, AdjArgs<T> a, T *y,
@@ -297,7 +290,6 @@ __global__ void __launch_bounds__(256) adjoint_zero_kernel(const Tile *__restric
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ntiles;
        w += warps) {
     const Tile tile = tiles[w];
-    if (a.ag[tile.group].direct) continue;  // pass 2 zeroed it as it read it
     const DevGroup &g = a.groups[tile.group];
     const AdjLayout<T, BATCH> L(a, g.member, y, nullptr, nvars, S1, S2, S3);
     const int64_t tblock = __ldg(a.tb + tile.transfer) - 1;
