@@ -495,7 +495,8 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
  * the schedule's transfers, which keeps blocks that exchange ghosts close
  * together in time (the sectors they share stay in L2); 2 by source block
  * first (the blocks' own order), then target: the transfers that read one
- * block run together, so each source sector comes from DRAM once. */
+ * block run together, so each source sector comes from DRAM once; 3 the
+ * copies by target block and the stencils by source block. */
 #define TAM_OPT_BLOCK_ORDER 6
 /* 1: a stage's stencil points grouped by their path through the kernel
  * (the order class and, in the CPU form, the dimensions that take one tap),

@@ -225,7 +225,7 @@ def test_launch_options_change_no_bit(cuda_lib):
     fs.factors = fs.factors.cuda()
     ds = device_schedule(s, 0)
     for ti, th, im, cp, bo, pt, ms, sg, pv, cs, sa, st in (
-            (16, 64, 0, 1, 0, 0, 1, 1, 1, 1, 1, 0),
+            (16, 64, 0, 1, 3, 0, 1, 1, 1, 1, 1, 0),
             (37, 96, 1, 2, 1, 1, 0, 1, 0, 0, 1, 48),
             (512, 512, 1, 4, 0, 1, 1, 0, 1, 2, 1, 16),
             (64, 128, 1, 1, 2, 1, 1, 0, 0, 2, 1, 128),

@@ -436,12 +436,17 @@ void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int
     }
     // by target block, or (TAM_OPT_BLOCK_ORDER 2) by source block first: the
     // transfers that read one block's edges then run together, and its
-    // sectors come from DRAM once
-    const bool by_source = s->shape.block_order == 2;
-    std::stable_sort(entries.begin(), entries.end(), [&](const Entry &a, const Entry &b) {
-      if (by_source && a.sblock != b.sblock) return a.sblock < b.sblock;
-      return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
-    });
+    // sectors come from DRAM once; 3: the copies by target block and the
+    // stencils, whose source windows several targets share, by source
+    auto by = [](bool source) {
+      return [source](const Entry &a, const Entry &b) {
+        if (source && a.sblock != b.sblock) return a.sblock < b.sblock;
+        return a.tblock != b.tblock ? a.tblock < b.tblock : a.group < b.group;
+      };
+    };
+    std::stable_sort(entries.begin(), entries.end(), by(s->shape.block_order == 2));
+    std::vector<Entry> sentries = entries;
+    if (s->shape.block_order == 3) std::stable_sort(sentries.begin(), sentries.end(), by(true));
     // unit copies first (the light kernel; those without a factor column
     // first of all), then the stencils
     for (int pass = 0; pass < 2; ++pass) {
@@ -459,7 +464,7 @@ void tiles_of(tam_sched *s, std::vector<tam::Stage> &list, const std::vector<int
     }
     std::vector<tam::Tile> sten;
     std::vector<uint16_t> skeys;
-    for (const Entry &e : entries) {
+    for (const Entry &e : sentries) {
       const tam::DevGroup &g = s->groups[e.group];
       if (tile_pass(g) != 2) continue;
       if (!s->shape.path_tiles) {  // by target block alone: one key
@@ -1293,8 +1298,8 @@ int tam_schedule_set_option(tam_sched *s, int32_t option, int64_t value) {
         return fail(s->ctx, TAM_EINVAL, "tile items must be in 16..4096");
       if (option == TAM_OPT_STENCIL_TILE && value != 0 && (value < 16 || value > 4096))
         return fail(s->ctx, TAM_EINVAL, "stencil tile items are 0 or in 16..4096");
-      if (option == TAM_OPT_BLOCK_ORDER && (value < 0 || value > 2))
-        return fail(s->ctx, TAM_EINVAL, "block_order is 0, 1 or 2");
+      if (option == TAM_OPT_BLOCK_ORDER && (value < 0 || value > 3))
+        return fail(s->ctx, TAM_EINVAL, "block_order is 0..3");
       if ((option == TAM_OPT_PATH_TILES || option == TAM_OPT_STAGED) && value != 0 &&
           value != 1)
         return fail(s->ctx, TAM_EINVAL, "path_tiles and staged are 0 or 1");

@@ -138,7 +138,7 @@ int tam_autotune(tam_sched *s, void *work, int32_t nvars, int64_t nblocks, const
               {TAM_OPT_PATH_TILES, {0, 1, 0}, 2, old_pt},
               {TAM_OPT_STAGED, {0, 1, 0}, 2, old_sg},
               {TAM_OPT_PAIR_VARS, {0, 1, 0}, dtype_f64 ? 2 : 1, old_pv},
-              {TAM_OPT_BLOCK_ORDER, {0, 1, 2}, 3, old_bo},
+              {TAM_OPT_BLOCK_ORDER, {0, 1, 2, 3}, 4, old_bo},
               {TAM_OPT_COPY_POINTS, {1, 2, 4}, 3, old_cp},
               {TAM_OPT_COPY_SHARE, {0, 1, 2, 4}, 4, old_cs},
               {TAM_OPT_SOFT_ADD, {0, 1, 0, 0}, dtype_f64 ? 2 : 1, old_sa},
