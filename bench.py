@@ -339,7 +339,11 @@ def measure_walls(T, dev, timed, args, peak):
                   "speedup_fused_vs_plain": ms_plain / ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()}},
+                     "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
+                     "kernels": kernel_rooflines(sched, stage_ms, {
+                         t: 2 * esize * fs.nvars * sum(int(np.prod(g.boxsize())) * g.ntransfers()
+                                                       for g in sched.groups if g.stage == t)
+                         for t in tags}, peak)},
         "fp64": fp,
         "error": err,
         "unify": {"ms": ms_unify, "bytes": unify_bytes,
@@ -704,6 +708,27 @@ def load_peaks():
         return {}
 
 
+def kernel_rooflines(sched, stage_ms, stage_bytes, peak):
+    """The HBM roofline of each fused kernel over the stages that run it
+    alone: the copy kernel over the stages that hold only unit copies, the
+    stencil kernel over those that hold only stencils (a stage with both runs
+    the two side by side and is left out)."""
+    import statistics
+    kinds = {}
+    for g in sched.groups:
+        kinds.setdefault(g.stage, set()).add("copy" if g.unit() else "stencil")
+    out = {}
+    for name, kind in (("fused_copy_kernel", "copy"), ("fused_stage_kernel", "stencil")):
+        tags = [t for t, k in kinds.items() if k == {kind} and t in stage_ms]
+        if not tags:
+            continue
+        ms = sum(statistics.mean(stage_ms[t]) for t in tags)
+        b = sum(stage_bytes[t] for t in tags)
+        out[name] = {"stages": sorted(tags), "ms": ms, "algorithmic_bytes": b,
+                     "achieved": b / (ms * 1e-3) / 1e9, "frac": b / (ms * 1e-3) / 1e9 / peak}
+    return out
+
+
 def stage_times(ds, fs, sched, stream, dev, reps):
     """Per stage tag, the fused launches' times (CUDA events on the launching
     stream, ``reps`` fills' worth), and the algorithmic bytes of the stage."""
@@ -798,7 +823,8 @@ def measure_sphere(dev, timed, args, peak, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
-                     "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
+                     "stage_bytes": {str(k): v for k, v in stage_bytes.items()},
+                     "kernels": kernel_rooflines(sched, stage_ms, stage_bytes, peak)},
         "fp64": fp64,
         "error": error,
         "footprint": {"written_points": wr, "read_points": rd,
@@ -1063,7 +1089,8 @@ def main():
                          "scope": "the whole fill: algorithmic bytes over the sum of the "
                                   "stages' fused launches (CUDA events)",
                          "stage_ms": {str(k): statistics.mean(v) for k, v in stage_ms.items()},
-                         "stage_bytes": {str(k): v for k, v in stage_bytes.items()}},
+                         "stage_bytes": {str(k): v for k, v in stage_bytes.items()},
+                         "kernels": kernel_rooflines(sched, stage_ms, stage_bytes, peak)},
             "fp64": fp64,
             "e2e": e2e,
             "cpu_baseline": cpu,
