@@ -52,6 +52,40 @@ def test_batch_fill_equals_member_fills(cuda_lib):
     assert torch.equal(alone.view(torch.int32), batch.arena.view(torch.int32))
 
 
+def test_batch_of_walls_forests_equals_member_fills(cuda_lib):
+    """Vertex-centred members with reflecting and outflow faces (the walls
+    mesh's layout at two sizes): stages P and 0, mirrored copies with their
+    factor column, and copies whose source rows are a table, not a step, all
+    through the batch's shared-memory copy segments, bit for bit against each
+    member's oracle fill, at one and at four copy points a lane."""
+    from treeamr import FieldSet, Operators, meshes as M
+    from treeamr.batch import ForestBatch
+    from treeamr.storage import vertexcentered
+    fss, scheds = [], []
+    for roots, levels in ((2, 2), (3, 3)):
+        f = M.walls_forest(roots=roots, N=16, levels=levels)
+        fs = FieldSet(f, 8, G=2, centering=vertexcentered(3), parity=M.walls_parities(),
+                      T=np.float64)
+        fss.append(fs)
+        scheds.append(GhostSchedule(fs, Operators(prolongation=4, restriction=4)))
+    batch = ForestBatch(fss, scheds, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(4)
+    batch.arena.uniform_(-1, 1, generator=g)
+    start = batch.arena.clone()
+    expect = []
+    for m, (fs, s) in enumerate(zip(fss, scheds)):
+        host = batch.member_view(start, m).cpu().numpy().copy()
+        expect.append(oracle.fill(s, host, fs.nvars, fs.factors_host))
+    for cp in (1, 4):
+        batch.set_option("copy_points", cp)
+        batch.arena.copy_(start)
+        batch.fill()
+        torch.cuda.synchronize()
+        for m in range(len(fss)):
+            got = batch.member_view(batch.arena, m).cpu().numpy()
+            assert np.array_equal(got.view(np.uint64), expect[m].view(np.uint64)), (cp, m)
+
+
 @pytest.mark.parametrize("T", [np.float32, np.float64])
 def test_batch_autotune_keeps_results(cuda_lib, T):
     """The batch's tuner leaves a set of its choices, and the fill with them
