@@ -476,8 +476,8 @@ int tam_fill_host_own(tam_sched *s, const tam_state_layout *layout, const void *
  * one changes speed only, never a result. */
 #define TAM_OPT_TILE_ITEMS 1 /* box points per warp tile, 16..4096           */
 #define TAM_OPT_THREADS 2    /* threads per CTA, 64..512, a multiple of 32    */
-#define TAM_OPT_INT_MUL 3    /* 1: Float64 short-weight multiplies on the     */
-                             /* integer pipe (see tam_selftest), 0: FP64 pipe  */
+#define TAM_OPT_INT_MUL 3    /* 1: Float64 stencil multiplies on the integer  */
+                             /* pipe (see tam_selftest), 0: FP64 pipe          */
 /* The form of the stencil sum (src/ghosts.jl:28-56): 1 (the default) is the
  * reference's CPU form, a dimension whose weight column has one nonzero
  * weight takes that one tap; 0 is its device form, every tap.  The two give
@@ -572,9 +572,14 @@ int tam_device_status(tam_sched *s, void *stream, int32_t *code);
  * pairs of a running sum (every kind of value) and a product (normal),
  * weighted to equal and adjacent exponents, cancellations and the edges of
  * the normal range, and returns the results that differ in any bit (pairs
- * the adder hands back to the FP64 pipe are not compared).  Synchronous. */
+ * the adder hands back to the FP64 pipe are not compared).  which = 3
+ * compares the integer-pipe multiply of weights of any width (the Float64
+ * order-6 products) with the hardware multiply on n pairs of normal
+ * factors, exponents across the range and products near its edges.
+ * Synchronous. */
 #define TAM_SELFTEST_MUL 1
 #define TAM_SELFTEST_ADD 2
+#define TAM_SELFTEST_MUL_FULL 3
 int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches);
 
 #ifdef __cplusplus

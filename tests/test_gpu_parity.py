@@ -90,6 +90,31 @@ def test_sphere_order6_bit_exact(cuda_lib, method):
     assert np.array_equal(nanbits(got), nanbits(expect))
 
 
+def test_sphere_order6_integer_pipe_multiply_bit_exact(cuda_lib):
+    """The order-6 products have up to 53 significant bits: with the
+    multiplies on the integer pipe (mul_full) the fill is the oracle's bit for
+    bit, on seeded data and on awkward data (zeros, subnormals, infinities and
+    NaNs, which hand their points back to the FP64 pipe)."""
+    from treeamr.ghosts import device_schedule
+    for fill in ("random", "awkward"):
+        f, fs, ops = meshes.sphere_setup(roots=2, levels=2, p=6)
+        if fill == "random":
+            meshes.random_fill(fs, seed=14)
+            host = fs.work.numpy().copy()
+        else:
+            host = awkward_fill(tuple(fs.work.shape), np.float64, seed=15)
+            fs.work = torch.from_numpy(host.copy())
+        s = GhostSchedule(fs, ops)
+        expect = oracle.fill_fieldset(fs, s, one_tap=True)
+        fs.work = torch.from_numpy(host).cuda()
+        fs.factors = fs.factors.cuda()
+        ds = device_schedule(s, 0)
+        ds.set_option("int_mul", 1)
+        fill_ghosts(fs, s)
+        torch.cuda.synchronize()
+        assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), fill
+
+
 @pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("D", [1, 2, 3])
 @pytest.mark.parametrize("T", [np.float64, np.float32])
@@ -194,6 +219,21 @@ def test_integer_pipe_multiply_matches_hardware(cuda_lib):
     bad = C.c_int64(-1)
     for seed in (1, 2, 3):
         _native.check(cuda_lib.tam_selftest(ctx, 1, 1 << 26, seed, C.byref(bad)), ctx,
+                      "tam_selftest")
+        assert bad.value == 0
+
+
+def test_integer_pipe_wide_multiply_matches_hardware(cuda_lib):
+    """The Float64 multiply of weights of any width (order 6) on the integer
+    pipe equals the hardware multiply in every bit wherever it does not hand
+    the pair back, over 3 x 2^26 pairs, products near the normal range's
+    edges among them."""
+    import ctypes as C
+    from treeamr import _native
+    ctx = _native.context(0)
+    bad = C.c_int64(-1)
+    for seed in (1, 2, 3):
+        _native.check(cuda_lib.tam_selftest(ctx, 3, 1 << 26, seed, C.byref(bad)), ctx,
                       "tam_selftest")
         assert bad.value == 0
 

@@ -1395,7 +1395,7 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value) 
 
 int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t *mismatches) {
   if (!ctx || !mismatches || n < 0) return fail(ctx, TAM_EINVAL, "tam_selftest: bad argument");
-  if (which != TAM_SELFTEST_MUL && which != TAM_SELFTEST_ADD)
+  if (which != TAM_SELFTEST_MUL && which != TAM_SELFTEST_ADD && which != TAM_SELFTEST_MUL_FULL)
     return fail(ctx, TAM_EINVAL, "tam_selftest: unknown test");
   DeviceGuard guard(ctx->device);
   if (!guard.ok()) return fail(ctx, TAM_ECUDA, "cannot make the context's device current");
@@ -1403,8 +1403,9 @@ int tam_selftest(tam_ctx *ctx, int32_t which, int64_t n, uint64_t seed, int64_t 
   cudaError_t e = cudaMalloc((void **)&d, sizeof h);
   if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof h);
   if (e == cudaSuccess)
-    e = which == TAM_SELFTEST_MUL ? tam::launch_selftest_mul(n, seed, d, 0)
-                                  : tam::launch_selftest_add(n, seed, d, 0);
+    e = which == TAM_SELFTEST_MUL   ? tam::launch_selftest_mul(n, seed, d, 0)
+        : which == TAM_SELFTEST_ADD ? tam::launch_selftest_add(n, seed, d, 0)
+                                    : tam::launch_selftest_mul_full(n, seed, d, 0);
   if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tam_selftest");

@@ -401,6 +401,9 @@ int own_box_copy(const tam_state_layout *layout, void *dst, const void *src, voi
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);
+// mul_full against the hardware multiply, the same counts.
+cudaError_t launch_selftest_mul_full(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                     cudaStream_t stream);
 // add_soft against the hardware add: mismatches[0] the differing results,
 // mismatches[1] the pairs the adder hands back to the FP64 pipe.
 cudaError_t launch_selftest_add(int64_t n, uint64_t seed, unsigned long long *mismatches,

@@ -255,6 +255,42 @@ __device__ __forceinline__ double mul_short_flag(uint32_t wm, int we, uint32_t w
   return __hiloint2double((int)rhi, (int)(uint32_t)m);
 }
 
+// RN(w * u) on the integer pipe for any weight: the 106-bit product of the
+// two 53-bit significands from four 32 x 32 multiplies (the high words have
+// 21 bits), its top 53 bits rounded to nearest-even on the next bit and the
+// rest.  `bad` is set where w or u is zero, subnormal, infinite or NaN, or
+// the result leaves the normal range; the caller sums the point again on
+// the FP64 pipe.  Bit-identical to __dmul_rn(w, u) wherever `bad` stays
+// clear (checked by tam_selftest).
+__device__ __forceinline__ double mul_full(double w, double u, bool &bad) {
+  constexpr uint64_t kFrac = 0x000FFFFFFFFFFFFFull;
+  const uint64_t bw = (uint64_t)__double_as_longlong(w);
+  const uint64_t bu = (uint64_t)__double_as_longlong(u);
+  const int ew = (int)((bw >> 52) & 0x7FF), eu = (int)((bu >> 52) & 0x7FF);
+  const uint64_t mw = (bw & kFrac) | (1ull << 52), mu = (bu & kFrac) | (1ull << 52);
+  const uint32_t wl = (uint32_t)mw, wh = (uint32_t)(mw >> 32);
+  const uint32_t ul = (uint32_t)mu, uh = (uint32_t)(mu >> 32);
+  const uint64_t ll = (uint64_t)wl * ul;
+  const uint64_t mid = (uint64_t)wh * ul + (uint64_t)wl * uh;  // < 2^54
+  const uint64_t lo = ll + (mid << 32);
+  const uint64_t hi = (uint64_t)wh * uh + (mid >> 32) + (lo < ll);  // the product: hi 2^64 + lo
+  const int t = (int)(hi >> 41);  // 1: the product has 106 bits, 0: 105
+  const int sh = 52 + t;
+  uint64_t m = (hi << (64 - sh)) | (lo >> sh);
+  const uint64_t guard = (lo >> (sh - 1)) & 1u;
+  const uint64_t sticky = (lo & ((1ull << (sh - 1)) - 1)) != 0;
+  m += guard & (sticky | (m & 1u));
+  int E = ew + eu - 1023 + t;
+  if (m >> 53) {  // rounded up to the next power of two
+    m >>= 1;
+    E += 1;
+  }
+  bad |= ((unsigned)(ew - 1) >= 2046u) | ((unsigned)(eu - 1) >= 2046u) |
+         ((unsigned)(E - 1) >= 2046u);
+  return __longlong_as_double((long long)(((bw ^ bu) & 0x8000000000000000ull) |
+                                          ((uint64_t)(E & 0x7FF) << 52) | (m & kFrac)));
+}
+
 // RN(a + b) on the integer pipe: the textbook IEEE adder.  The operands in
 // order of magnitude, the smaller one's significand shifted to the larger's
 // exponent with three extra bits (guard, round and sticky), added or
@@ -462,6 +498,72 @@ __device__ __forceinline__ void table_point(const DevGroup &g, int i1, int i2, i
           for (int m2 = m3 == lo3 ? lo2 + 1 : lo2; m2 < hi2; ++m2) row(m2, m3, false);
         }
         if (bad) {  // a zero, subnormal or special datum, or an out-of-range product
+#pragma unroll
+          for (int j = 0; j < VC; ++j) acc[j] = 0.0;
+#pragma unroll 1
+          for (int m3 = lo3; m3 < hi3; ++m3)
+#pragma unroll 1
+            for (int m2 = lo2; m2 < hi2; ++m2)
+#pragma unroll 1
+              for (int m1 = lo1; m1 < hi1; ++m1) {
+                const double w = __ldg(W + (m3 * P2 + m2) * P + m1);
+                const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+                for (int j = 0; j < VC; ++j)
+                  if (v0 + j < vend)
+                    acc[j] = __dadd_rn(acc[j], __dmul_rn(w, src[off + j * o.svstride]));
+              }
+        }
+#pragma unroll
+        for (int j = 0; j < VC; ++j)
+          if (v0 + j < vend)
+            dst[o.toff + (v0 + j) * o.vstride] =
+                scaled(acc[j], factors, v0 + j, nvars, g.factorcol);
+      }
+      return;
+    }
+    if (!g.shortw && a.int_mul) {
+      // F64 with weight products of up to 53 significant bits (order 6): the
+      // multiplies exact on the integer pipe all the same (mul_full), only
+      // the adds on the FP64 pipe
+      for (int v0 = vbegin; v0 < vend; v0 += VC) {
+        double acc[VC];
+        const double *src = work + (o.soff + v0 * o.svstride);
+        bool bad = false;
+        auto tap = [&](int m1, int m2, int m3, auto first) {
+          const double w = __ldg(W + (m3 * P2 + m2) * P + m1);
+          const int64_t off = m3 * o.s3 + m2 * o.s2 + m1;
+#pragma unroll
+          for (int j = 0; j < VC; ++j)
+            if (v0 + j < vend) {
+              const double p = mul_full(w, src[off + j * o.svstride], bad);
+              acc[j] = decltype(first)::value ? p : __dadd_rn(acc[j], p);
+            }
+        };
+        using Yes = std::true_type;
+        using No = std::false_type;
+        auto row = [&](int m2, int m3, bool head) {
+          if (SKIP && hi1 - lo1 == 1) {
+            if (head)
+              tap(lo1, m2, m3, Yes{});
+            else
+              tap(lo1, m2, m3, No{});
+          } else {
+            if (head)
+              tap(0, m2, m3, Yes{});
+            else
+              tap(0, m2, m3, No{});
+#pragma unroll
+            for (int m1 = 1; m1 < P; ++m1) tap(m1, m2, m3, No{});
+          }
+        };
+        row(lo2, lo3, true);
+#pragma unroll 1
+        for (int m3 = lo3; m3 < hi3; ++m3) {
+#pragma unroll 1
+          for (int m2 = m3 == lo3 ? lo2 + 1 : lo2; m2 < hi2; ++m2) row(m2, m3, false);
+        }
+        if (bad) {  // a zero, subnormal or special datum or weight, or an out-of-range product
 #pragma unroll
           for (int j = 0; j < VC; ++j) acc[j] = 0.0;
 #pragma unroll 1
@@ -1666,7 +1768,48 @@ __global__ void selftest_add_kernel(int64_t n, uint64_t seed,
   }
 }
 
+// mul_full against __dmul_rn: both factors of any sign and significand,
+// exponents across the normal range and pairs whose product lands near its
+// edges.  A product the multiply flags is not compared; mismatches[1]
+// counts them.
+__global__ void selftest_mul_full_kernel(int64_t n, uint64_t seed,
+                                         unsigned long long *__restrict__ mismatches) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r1 = splitmix(seed ^ (uint64_t)(3 * i));
+    const uint64_t r2 = splitmix(seed ^ (uint64_t)(3 * i + 1));
+    const uint64_t r3 = splitmix(seed ^ (uint64_t)(3 * i + 2));
+    const int ew = 1 + (int)((r3 & 0xFFFF) % 2046);
+    int eu;
+    switch ((r3 >> 16) & 3) {
+      case 0: eu = 1 + (int)((r3 >> 20) % 2046); break;          // anywhere
+      case 1: eu = 2046 + 1023 - ew + (int)((r3 >> 20) % 7) - 3; break;  // near overflow
+      case 2: eu = 1023 + 1 - ew + (int)((r3 >> 20) % 64) - 3; break;   // near underflow
+      default: eu = 2046 - ew + (int)((r3 >> 20) % 41) - 20; break;      // mid-range
+    }
+    eu = eu < 1 ? 1 : eu > 2046 ? 2046 : eu;
+    const uint64_t wb = (r1 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)ew << 52);
+    const uint64_t ub = (r2 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)eu << 52);
+    const double w = __longlong_as_double((long long)wb);
+    const double u = __longlong_as_double((long long)ub);
+    bool bad = false;
+    const double p = mul_full(w, u, bad);
+    if (bad) {
+      atomicAdd(mismatches + 1, 1ull);
+      continue;
+    }
+    if (__double_as_longlong(p) != __double_as_longlong(__dmul_rn(w, u)))
+      atomicAdd(mismatches, 1ull);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_selftest_mul_full(int64_t n, uint64_t seed, unsigned long long *mismatches,
+                                     cudaStream_t stream) {
+  selftest_mul_full_kernel<<<1216, 256, 0, stream>>>(n, seed, mismatches);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_selftest_mul(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream) {
