@@ -1009,6 +1009,20 @@ def main():
     yadj = fs.work.clone()
     fill_ghosts_adjoint(fs, sched, yadj)
     ms_adj = timed(lambda: fill_ghosts_adjoint(fs, sched, yadj), max(3, args.steps // 2))
+    # and stage by stage (the transposes run in reverse stage order)
+    adj_evs = []
+    for _ in range(3):
+        for tag in sorted({g.stage for g in sched.groups}, reverse=True):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ds.run_adjoint(yadj, nvars, fs.factors, tag, tag, stream)
+            b.record(stream)
+            adj_evs.append((tag, a, b))
+    torch.cuda.synchronize(dev)
+    adj_stage_ms = {}
+    for tag, a, b in adj_evs:
+        adj_stage_ms.setdefault(str(tag), []).append(a.elapsed_time(b))
+    adj_stage_ms = {k: statistics.mean(v) for k, v in adj_stage_ms.items()}
     del yadj
 
     stage_ms, stage_bytes = stage_times(ds, fs, sched, stream, dev, max(3, args.steps // 2))
@@ -1074,7 +1088,8 @@ def main():
             "plain": {"value": world * bytes_per_fill / (ms_plain * 1e-3) / 1e9, "unit": UNIT,
                       "ms_per_step": ms_plain, "speedup_fused_vs_plain": ms_plain / ms},
             "adjoint": {"value": world * bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
-                        "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms},
+                        "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms,
+                        "stage_ms": adj_stage_ms},
             "throughput": throughput,
             "error": error,
             "workloads": workloads,

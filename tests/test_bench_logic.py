@@ -1,0 +1,55 @@
+"""The bench line's host-side arithmetic, on the CPU: which stages each
+kernel's roofline covers, and the layout's sector counts in 32- and 64-byte
+units."""
+import numpy as np
+
+from treeamr import meshes
+from treeamr.schedule import GhostSchedule
+
+
+def _walls_small():
+    f, fs, ops = meshes.walls_setup(roots=2, N=16, levels=2)
+    return fs, GhostSchedule(fs, ops)
+
+
+def test_kernel_rooflines_split_copy_and_stencil_stages():
+    import bench
+    fs, s = _walls_small()
+    tags = sorted({g.stage for g in s.groups})
+    kinds = {t: {g.unit() for g in s.groups if g.stage == t} for t in tags}
+    stage_ms = {t: [0.5, 0.5] for t in tags}
+    stage_bytes = {t: 1_000_000 * (i + 1) for i, t in enumerate(tags)}
+    out = bench.kernel_rooflines(s, stage_ms, stage_bytes, peak=1000.0)
+    copies = [t for t in tags if kinds[t] == {True}]
+    stencils = [t for t in tags if kinds[t] == {False}]
+    assert out["fused_copy_kernel"]["stages"] == copies
+    assert out["fused_stage_kernel"]["stages"] == stencils
+    for name, tt in (("fused_copy_kernel", copies), ("fused_stage_kernel", stencils)):
+        k = out[name]
+        assert k["ms"] == 0.5 * len(tt)
+        assert k["algorithmic_bytes"] == sum(stage_bytes[t] for t in tt)
+        assert abs(k["achieved"] - k["algorithmic_bytes"] / (k["ms"] * 1e-3) / 1e9) < 1e-9
+        assert abs(k["frac"] - k["achieved"] / 1000.0) < 1e-12
+    # a stage with both kinds is in neither
+    mixed = {t: [0.5] for t in tags}
+    out2 = bench.kernel_rooflines(s, mixed, stage_bytes, peak=1000.0)
+    assert set(out2) <= {"fused_copy_kernel", "fused_stage_kernel"}
+
+
+def test_sector_counts_in_wider_units_are_no_smaller():
+    """Counting the same accesses in 64-byte units can only merge sectors into
+    fewer, larger units: bytes never fall below the 32-byte count, the
+    algorithmic bytes do not change, and every count covers the bytes the
+    copies actually move."""
+    import bench
+    fs, s = _walls_small()
+    esize = np.dtype(fs.T).itemsize
+    a = bench.sector_minimum(s, fs.nvars, esize, 1, unit=32)
+    b = bench.sector_minimum(s, fs.nvars, esize, 1, unit=64)
+    assert a["unit_bytes"] == 32 and b["unit_bytes"] == 64
+    assert a["algorithmic_bytes"] == b["algorithmic_bytes"]
+    for key in ("sectors_read_bytes", "sectors_written_bytes", "minimum_bytes",
+                "minimum_bytes_with_rmw"):
+        assert b[key] >= a[key], key
+    # each written point is in some written sector: the writes cover half the algorithmic bytes
+    assert a["sectors_written_bytes"] >= a["algorithmic_bytes"] // 2
