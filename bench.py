@@ -398,6 +398,9 @@ def measure_pv6(dev, timed, args):
     f, fs, ops = meshes.sphere_setup(device=dev, nvars=args.nvars, roots=args.roots,
                                      levels=args.levels, p=6)
     sched = GhostSchedule(fs, ops)
+    # tuned on the stated data: on zeros the integer-pipe multiplies hand
+    # every point back to the FP64 pipe and would look slower than they are
+    meshes.config_fill(fs, "sphere", seed=11)
     tuned = autotune(fs, sched)
     meshes.config_fill(fs, "sphere", seed=11)
     bytes_per_fill = 2 * sched.ghost_items(fs.nvars) * 8

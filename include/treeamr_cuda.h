@@ -545,7 +545,9 @@ int tam_schedule_get_option(const tam_sched *s, int32_t option, int64_t *value);
 
 /* The launch-option autotuner: times every combination of TAM_OPT_TILE_ITEMS
  * (32 .. 512), TAM_OPT_THREADS (128, 256, 512) and, for Float64,
- * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (best of `reps`
+ * TAM_OPT_INT_MUL (0, 1) on the caller's own field data (which should be
+ * representative: zeros, subnormals and specials send the integer-pipe
+ * multiplies' points back to the FP64 pipe) (best of `reps`
  * fills after a warm-up, CUDA events on `stream`), then, from the fastest,
  * TAM_OPT_MERGE_STAGES, TAM_OPT_PATH_TILES, TAM_OPT_STAGED,
  * TAM_OPT_PAIR_VARS (Float64), TAM_OPT_BLOCK_ORDER, TAM_OPT_COPY_POINTS and
