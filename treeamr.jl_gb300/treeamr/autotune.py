@@ -3,14 +3,17 @@
 The reference has no tuning: its device fill is one launch per group with
 KernelAbstractions' default workgroup.  Here each uploaded schedule carries
 launch options (``tam_schedule_set_option``) that change speed but never a
-result: the box points per warp tile, the threads per CTA, whether the
-Float64 multiplies by short weight products run on the integer pipe, and the
-grouping and order of the work (stencil tiles grouped by their path through
-the kernel or by target block, the order the blocks are visited in, points
-a lane of the copy kernel takes at once).  The
-tuner times every candidate on the caller's own field set (CUDA events on the
-fill's stream, best of a few fills after a warm-up), keeps the fastest, and
-caches the choice per schedule and variable count.  The default grid runs in
+result: the box points per warp tile (copies and stencils apart), the threads
+per CTA, whether the Float64 stencil multiplies (and a quarter of the adds)
+run on the integer pipe, and the grouping and order of the work (stage
+groups, stencil tiles grouped by their path through the kernel or by target
+block, the order the blocks are visited in, points a lane of the copy kernel
+takes at once, the copies' share of the multiprocessors beside the
+stencils).  The tuner times every candidate on the caller's own field set
+(CUDA events on the fill's stream, best of a few fills after a warm-up; the
+data should be representative, since zeros and specials send the
+integer-pipe multiplies' points back to the FP64 pipe), keeps the fastest,
+and caches the choice per schedule and variable count.  The default grid runs in
 the library (``tam_autotune``); other candidate sets are timed from here.
 """
 from __future__ import annotations
