@@ -123,10 +123,17 @@ struct AdjLayout {
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int2 *__restrict__ xfers, int64_t nxfers, AdjArgs<T> a, T *y, T *scratch,
-    const T *__restrict__ factors, int nvars, int S1, int S2, int S3) {
+    const T *__restrict__ factors, int nvars, int S1, int S2, int S3, int box_elems,
+    int csr_ents) {
   using A = AArith<T>;
   extern __shared__ __align__(16) unsigned char adj_smem[];
   T *SA = (T *)adj_smem;
+  // after the boxes, the transfer's transposed stencils: each entry's weight
+  // and target row, and each footprint row's first entry, three dimensions
+  // one after another
+  T *SW = SA + box_elems;
+  int *SE = (int *)(SW + csr_ents);
+  int *SO = SE + csr_ents;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int64_t q = blockIdx.x; q < nxfers; q += gridDim.x) {
     const int2 tg = xfers[q];  // (transfer, group)
@@ -137,13 +144,40 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int f1 = h.fn[0], f2 = h.fn[1], f3 = h.fn[2];
     T *SB = SA + n1 * n2 * n3;
     T *SC = SB + f1 * n2 * n3;
-    const int32_t *o1 = a.off + h.off[0], *o2 = a.off + h.off[1], *o3 = a.off + h.off[2];
     const int64_t tblock = __ldg(a.tb + tg.x) - 1;
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
     const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
     // a direct copy (AdjGroup::direct) has no pass-1 work and no scratch:
     // the host leaves it out of the list
     if (h.direct) continue;
+    // the transposed stencils into shared memory, weights looked up once:
+    // the passes then read no global memory but the target box
+    const int fn[3] = {f1, f2, f3};
+    int rbase[3], ebase[3];
+    {
+      int r = 0, e = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        rbase[d] = r;
+        ebase[d] = e;
+        r += fn[d] + 1;
+        e += __ldg(a.off + h.off[d] + fn[d]) - __ldg(a.off + h.off[d]);
+      }
+    }
+    __syncthreads();  // the previous transfer's passes are done with the tables
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int32_t *od = a.off + h.off[d];
+      const int e0 = __ldg(od);
+      for (int k = tid; k <= fn[d]; k += nt) SO[rbase[d] + k] = __ldg(od + k) - e0 + ebase[d];
+      const int ne = __ldg(od + fn[d]) - e0;
+      for (int k = tid; k < ne; k += nt) {
+        const int2 q = __ldg(a.ent + e0 + k);
+        SE[ebase[d] + k] = q.x;
+        SW[ebase[d] + k] = __ldg(a.weights + q.y);
+      }
+    }
+    const int *o1 = SO + rbase[0], *o2 = SO + rbase[1], *o3 = SO + rbase[2];
     // a variable a CTA row (blockIdx.y): the variables' passes are independent
     for (int v = blockIdx.y; v < nvars; v += gridDim.y) {
       const T *yv = L.y + tblock * L.bs + v * L.vs;
@@ -161,10 +195,7 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
         const int row = k / f1, j1 = k - row * f1;
         const T *src = SA + row * n1;
         T acc = T(0);
-        for (int e = __ldg(o1 + j1), e1 = __ldg(o1 + j1 + 1); e < e1; ++e) {
-          const int2 q1 = __ldg(a.ent + e);
-          acc = A::fma(__ldg(a.weights + q1.y), src[q1.x], acc);
-        }
+        for (int e = o1[j1], e1 = o1[j1 + 1]; e < e1; ++e) acc = A::fma(SW[e], src[SE[e]], acc);
         SB[k] = acc;
       }
       __syncthreads();
@@ -172,10 +203,8 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
         const int i3 = k / (f1 * f2), r = k - i3 * (f1 * f2), j2 = r / f1, j1 = r - j2 * f1;
         const T *src = SB + i3 * n2 * f1 + j1;
         T acc = T(0);
-        for (int e = __ldg(o2 + j2), e1 = __ldg(o2 + j2 + 1); e < e1; ++e) {
-          const int2 q2 = __ldg(a.ent + e);
-          acc = A::fma(__ldg(a.weights + q2.y), src[q2.x * f1], acc);
-        }
+        for (int e = o2[j2], e1 = o2[j2 + 1]; e < e1; ++e)
+          acc = A::fma(SW[e], src[SE[e] * f1], acc);
         SC[k] = acc;
       }
       __syncthreads();
@@ -184,10 +213,8 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
         const int j3 = k / (f1 * f2), r = k - j3 * (f1 * f2);
         const T *src = SC + r;
         T acc = T(0);
-        for (int e = __ldg(o3 + j3), e1 = __ldg(o3 + j3 + 1); e < e1; ++e) {
-          const int2 q3 = __ldg(a.ent + e);
-          acc = A::fma(__ldg(a.weights + q3.y), src[q3.x * f1 * f2], acc);
-        }
+        for (int e = o3[j3], e1 = o3[j3 + 1]; e < e1; ++e)
+          acc = A::fma(SW[e], src[SE[e] * f1 * f2], acc);
         ov[k] = acc;
       }
       __syncthreads();
@@ -358,7 +385,9 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
     if (st.tag < first || st.tag > last) continue;
     const Stage &fw = (*r.fwd_stages)[k];
     if (st.ntiles > 0) {
-      const size_t smem = (size_t)st.smem_elems * sizeof(T);
+      const size_t smem = (size_t)st.smem_elems * sizeof(T) +
+                          (size_t)st.csr_ents * (sizeof(T) + sizeof(int)) +
+                          (size_t)st.csr_rows * sizeof(int);
       if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(adjoint_box_kernel<T, D, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -370,7 +399,7 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
       adjoint_box_kernel<T, D, BATCH><<<dim3((unsigned)blocks, (unsigned)nvars), 128, smem,
                                        stream>>>(
           (const int2 *)p.xfers + st.tile0, st.ntiles, a, y, scratch, factors, nvars, S1, S2,
-          S3);
+          S3, (int)st.smem_elems, (int)st.csr_ents);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -546,9 +575,17 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
     for (int32_t gi : fw.groups) {
       const DevGroup &g = s->groups[gi];
       const AdjGroup &a = o.ag[gi];
+      if (a.direct) continue;  // no pass 1
       const int64_t n = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
                         (int64_t)a.fn[0] * a.fn[1] * g.n[2];
       st.smem_elems = std::max(st.smem_elems, n);
+      int64_t ents = 0, rows = 0;
+      for (int d = 0; d < 3; ++d) {
+        ents += o.off[a.off[d] + a.fn[d]] - o.off[a.off[d]];
+        rows += a.fn[d] + 1;
+      }
+      st.csr_ents = std::max(st.csr_ents, ents);
+      st.csr_rows = std::max(st.csr_rows, rows);
     }
     // pass-2 lists by source block, transfers in transfer order (a block's
     // list holds the odd turns that read the alternate array's block too)
@@ -596,7 +633,8 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
 int upload_plan(AdjPlan &p, const AdjHost &o, int dtype, std::string &err) {
   const size_t esz = dtype == TAM_F64 ? 8 : 4, limit = smem_limit();
   for (const AdjStage &st : o.stages)
-    if ((size_t)st.smem_elems * esz > limit) {
+    if ((size_t)st.smem_elems * esz + (size_t)st.csr_ents * (esz + 4) + (size_t)st.csr_rows * 4 >
+        limit) {
       err = "a transfer box too large for the adjoint's shared memory";
       return TAM_EUNSUPPORTED;
     }
@@ -711,6 +749,8 @@ int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members
       }
       base += ms.scratch_points;
       st.smem_elems = std::max(st.smem_elems, ms.smem_elems);
+      st.csr_ents = std::max(st.csr_ents, ms.csr_ents);
+      st.csr_rows = std::max(st.csr_rows, ms.csr_rows);
     }
     st.ntiles = (int64_t)o.xfers.size() - st.tile0;
     st.nred = (int64_t)o.red.size() - st.red0;

@@ -211,7 +211,9 @@ struct AdjGroup {
 struct AdjStage {
   int32_t tag;
   int64_t tile0 = 0, ntiles = 0;  // into the pass-1 transfer list ((transfer, group) pairs)
-  int64_t smem_elems = 0;         // shared memory of pass 1, in elements
+  int64_t smem_elems = 0;         // shared memory of pass 1's boxes, in elements
+  int64_t csr_ents = 0;           // and of a transfer's transposed stencils: entries
+  int64_t csr_rows = 0;           //   and row offsets, all three dimensions
   int64_t red0 = 0, nred = 0;     // into the reduction block list
   int64_t scratch_points = 0;     // footprint points of the stage (per variable)
 };
