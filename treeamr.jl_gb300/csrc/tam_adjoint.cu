@@ -384,22 +384,23 @@ cudaError_t run_typed(const AdjPlan &p, const AdjRun &r, T *y, int nvars, const 
     const AdjStage &st = p.stages[k];
     if (st.tag < first || st.tag > last) continue;
     const Stage &fw = (*r.fwd_stages)[k];
-    if (st.ntiles > 0) {
-      const size_t smem = (size_t)st.smem_elems * sizeof(T) +
-                          (size_t)st.csr_ents * (sizeof(T) + sizeof(int)) +
-                          (size_t)st.csr_rows * sizeof(int);
+    for (const AdjPass1 &pc : st.p1) {
+      if (pc.count == 0) continue;
+      const size_t smem = (size_t)pc.smem_elems * sizeof(T) +
+                          (size_t)pc.csr_ents * (sizeof(T) + sizeof(int)) +
+                          (size_t)pc.csr_rows * sizeof(int);
       if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(adjoint_box_kernel<T, D, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
       }
-      const int64_t blocks = std::min<int64_t>(st.ntiles, (int64_t)1 << 30);
+      const int64_t blocks = std::min<int64_t>(pc.count, (int64_t)1 << 30);
       if (nvars > 65535) return cudaErrorInvalidValue;  // a CTA row per variable
       adjoint_box_kernel<T, D, BATCH><<<dim3((unsigned)blocks, (unsigned)nvars), 128, smem,
                                        stream>>>(
-          (const int2 *)p.xfers + st.tile0, st.ntiles, a, y, scratch, factors, nvars, S1, S2,
-          S3, (int)st.smem_elems, (int)st.csr_ents);
+          (const int2 *)p.xfers + pc.first, pc.count, a, y, scratch, factors, nvars, S1, S2,
+          S3, (int)pc.smem_elems, (int)pc.csr_ents);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -543,7 +544,6 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
   for (const Stage &fw : s->stages) {
     AdjStage st;
     st.tag = fw.tag;
-    st.tile0 = (int64_t)o.xfers.size();
     st.red0 = (int64_t)o.red.size();
     struct E {
       int32_t tblock, sblock, group, transfer;
@@ -564,28 +564,39 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
     }
     st.scratch_points = pts;
     o.maxpts = std::max(o.maxpts, pts);
-    // pass-1 transfers by target block; the shared memory of the largest box
-    std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
-      return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
-    });
-    // (a direct copy has no pass-1 work)
-    for (const E &e : es)
-      if (!o.ag[e.group].direct) o.xfers.push_back(make_int2(e.transfer, e.group));
-    st.ntiles = (int64_t)o.xfers.size() - st.tile0;
+    // pass-1 transfers by size class, then by target block; each class's
+    // shared memory is that of its largest box
+    std::vector<int64_t> gsm(s->groups.size(), 0), gents(s->groups.size(), 0),
+        grows(s->groups.size(), 0);
+    std::vector<int> gcls(s->groups.size(), 0);
     for (int32_t gi : fw.groups) {
       const DevGroup &g = s->groups[gi];
       const AdjGroup &a = o.ag[gi];
       if (a.direct) continue;  // no pass 1
-      const int64_t n = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
-                        (int64_t)a.fn[0] * a.fn[1] * g.n[2];
-      st.smem_elems = std::max(st.smem_elems, n);
-      int64_t ents = 0, rows = 0;
+      gsm[gi] = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
+                (int64_t)a.fn[0] * a.fn[1] * g.n[2];
       for (int d = 0; d < 3; ++d) {
-        ents += o.off[a.off[d] + a.fn[d]] - o.off[a.off[d]];
-        rows += a.fn[d] + 1;
+        gents[gi] += o.off[a.off[d] + a.fn[d]] - o.off[a.off[d]];
+        grows[gi] += a.fn[d] + 1;
       }
-      st.csr_ents = std::max(st.csr_ents, ents);
-      st.csr_rows = std::max(st.csr_rows, rows);
+      const int64_t bytes = 8 * gsm[gi] + 12 * gents[gi] + 4 * grows[gi];
+      while (gcls[gi] < kAdjClasses - 1 && bytes > kAdjClassBytes[gcls[gi]]) ++gcls[gi];
+    }
+    std::stable_sort(es.begin(), es.end(), [&](const E &x, const E &y) {
+      if (gcls[x.group] != gcls[y.group]) return gcls[x.group] < gcls[y.group];
+      return x.tblock != y.tblock ? x.tblock < y.tblock : x.group < y.group;
+    });
+    for (int c = 0; c < kAdjClasses; ++c) {
+      AdjPass1 &pc = st.p1[c];
+      pc.first = (int64_t)o.xfers.size();
+      for (const E &e : es) {  // (a direct copy has no pass-1 work)
+        if (o.ag[e.group].direct || gcls[e.group] != c) continue;
+        o.xfers.push_back(make_int2(e.transfer, e.group));
+        pc.smem_elems = std::max(pc.smem_elems, gsm[e.group]);
+        pc.csr_ents = std::max(pc.csr_ents, gents[e.group]);
+        pc.csr_rows = std::max(pc.csr_rows, grows[e.group]);
+      }
+      pc.count = (int64_t)o.xfers.size() - pc.first;
     }
     // pass-2 lists by source block, transfers in transfer order (a block's
     // list holds the odd turns that read the alternate array's block too)
@@ -633,11 +644,13 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
 int upload_plan(AdjPlan &p, const AdjHost &o, int dtype, std::string &err) {
   const size_t esz = dtype == TAM_F64 ? 8 : 4, limit = smem_limit();
   for (const AdjStage &st : o.stages)
-    if ((size_t)st.smem_elems * esz + (size_t)st.csr_ents * (esz + 4) + (size_t)st.csr_rows * 4 >
-        limit) {
-      err = "a transfer box too large for the adjoint's shared memory";
-      return TAM_EUNSUPPORTED;
-    }
+    for (const AdjPass1 &pc : st.p1)
+      if ((size_t)pc.smem_elems * esz + (size_t)pc.csr_ents * (esz + 4) +
+              (size_t)pc.csr_rows * 4 >
+          limit) {
+        err = "a transfer box too large for the adjoint's shared memory";
+        return TAM_EUNSUPPORTED;
+      }
   cudaError_t e;
   if ((e = up(&p.groups, o.ag)) != cudaSuccess || (e = up(&p.off, o.off)) != cudaSuccess ||
       (e = up((int2 **)&p.ent, o.ent)) != cudaSuccess || (e = up(&p.scr, o.scr)) != cudaSuccess ||
@@ -720,22 +733,43 @@ int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members
   for (const Stage &fw : stages) {
     AdjStage st;
     st.tag = fw.tag;
-    st.tile0 = (int64_t)o.xfers.size();
     st.red0 = (int64_t)o.red.size();
-    int64_t base = 0;
+    // each member's stage of this tag, and where its scratch starts
+    std::vector<const AdjStage *> mst(members.size(), nullptr);
+    std::vector<int64_t> base(members.size() + 1, 0);
     for (size_t m = 0; m < members.size(); ++m) {
-      const AdjHost &h = hs[m];
       const tam_sched *s = members[m];
       size_t k = 0;
       while (k < s->stages.size() && s->stages[k].tag != fw.tag) ++k;
-      if (k == s->stages.size()) continue;
-      const AdjStage &ms = h.stages[k];
-      const int32_t G0 = (int32_t)group_base[m], T0 = (int32_t)transfer_base[m];
-      for (int64_t i = ms.tile0; i < ms.tile0 + ms.ntiles; ++i) {
-        const int2 x = h.xfers[i];
-        o.xfers.push_back(make_int2(x.x + T0, x.y + G0));
-        o.scr[x.x + T0] = base + h.scr[x.x];
+      if (k < s->stages.size()) mst[m] = &hs[m].stages[k];
+      base[m + 1] = base[m] + (mst[m] ? mst[m]->scratch_points : 0);
+    }
+    // pass 1: the members' transfers class by class
+    for (int c = 0; c < kAdjClasses; ++c) {
+      AdjPass1 &pc = st.p1[c];
+      pc.first = (int64_t)o.xfers.size();
+      for (size_t m = 0; m < members.size(); ++m) {
+        if (!mst[m]) continue;
+        const AdjHost &h = hs[m];
+        const AdjPass1 &mc = mst[m]->p1[c];
+        const int32_t G0 = (int32_t)group_base[m], T0 = (int32_t)transfer_base[m];
+        for (int64_t i = mc.first; i < mc.first + mc.count; ++i) {
+          const int2 x = h.xfers[i];
+          o.xfers.push_back(make_int2(x.x + T0, x.y + G0));
+          o.scr[x.x + T0] = base[m] + h.scr[x.x];
+        }
+        pc.smem_elems = std::max(pc.smem_elems, mc.smem_elems);
+        pc.csr_ents = std::max(pc.csr_ents, mc.csr_ents);
+        pc.csr_rows = std::max(pc.csr_rows, mc.csr_rows);
       }
+      pc.count = (int64_t)o.xfers.size() - pc.first;
+    }
+    // pass 2: the members' source blocks
+    for (size_t m = 0; m < members.size(); ++m) {
+      if (!mst[m]) continue;
+      const AdjHost &h = hs[m];
+      const AdjStage &ms = *mst[m];
+      const int32_t G0 = (int32_t)group_base[m], T0 = (int32_t)transfer_base[m];
       for (int64_t i = ms.red0; i < ms.red0 + ms.nred; ++i) {
         AdjReduce r = h.red[i];
         const int64_t first = (int64_t)o.list.size();
@@ -747,15 +781,10 @@ int adjoint_prepare_batch(AdjPlan &plan, const std::vector<tam_sched *> &members
         r.first = first;
         o.red.push_back(r);
       }
-      base += ms.scratch_points;
-      st.smem_elems = std::max(st.smem_elems, ms.smem_elems);
-      st.csr_ents = std::max(st.csr_ents, ms.csr_ents);
-      st.csr_rows = std::max(st.csr_rows, ms.csr_rows);
     }
-    st.ntiles = (int64_t)o.xfers.size() - st.tile0;
     st.nred = (int64_t)o.red.size() - st.red0;
-    st.scratch_points = base;
-    o.maxpts = std::max(o.maxpts, base);
+    st.scratch_points = base[members.size()];
+    o.maxpts = std::max(o.maxpts, st.scratch_points);
     o.stages.push_back(st);
   }
   return upload_plan(plan, o, dtype, err);

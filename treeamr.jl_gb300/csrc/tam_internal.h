@@ -206,14 +206,26 @@ struct AdjGroup {
   int64_t tc0;
 };
 
+// Pass 1's transfers of one size class: list[first .. first + count) of the
+// pass-1 transfer list ((transfer, group) pairs), and the shared memory a CTA
+// of the class reserves: the boxes (elements) and the transposed stencils
+// (entries and row offsets, all three dimensions), the class's maxima.
+struct AdjPass1 {
+  int64_t first = 0, count = 0;
+  int64_t smem_elems = 0, csr_ents = 0, csr_rows = 0;
+};
+
+// Shared-memory classes of pass 1, by a transfer's bytes at 8-byte elements:
+// a launch per class, so that one large box does not set every CTA's share
+// (and with it the CTAs a multiprocessor holds).
+constexpr int kAdjClasses = 3;
+constexpr int64_t kAdjClassBytes[kAdjClasses - 1] = {12 * 1024, 48 * 1024};
+
 // One stage of the adjoint: its transfers for pass 1 (a CTA each), and the
 // source blocks pass 2 reduces into.
 struct AdjStage {
   int32_t tag;
-  int64_t tile0 = 0, ntiles = 0;  // into the pass-1 transfer list ((transfer, group) pairs)
-  int64_t smem_elems = 0;         // shared memory of pass 1's boxes, in elements
-  int64_t csr_ents = 0;           // and of a transfer's transposed stencils: entries
-  int64_t csr_rows = 0;           //   and row offsets, all three dimensions
+  AdjPass1 p1[kAdjClasses];
   int64_t red0 = 0, nred = 0;     // into the reduction block list
   int64_t scratch_points = 0;     // footprint points of the stage (per variable)
 };
