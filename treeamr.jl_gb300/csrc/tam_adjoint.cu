@@ -119,7 +119,7 @@ struct AdjLayout {
 // dimension d's transposed stencil are (i, w): target row i, weight index w
 // into the weight pool; a dimension beyond D has one entry of weight one.
 // Per variable: A = f * y over the target box (n1 x n2 x n3, row 1 fastest),
-// B = T1 A (fn1 x n2 x n3), C = T2 B (fn1 x fn2 x n3), box = T3 C.
+// B = T1 A (fn1 x n2 x n3), C = T2 B (fn1 x fn2 x n3) in A's place, box = T3 C.
 template <typename T, int D, bool BATCH>
 __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const int2 *__restrict__ xfers, int64_t nxfers, AdjArgs<T> a, T *y, T *scratch,
@@ -142,11 +142,12 @@ __global__ void __launch_bounds__(256) adjoint_box_kernel(
     const AdjLayout<T, BATCH> L(a, g.member, y, factors, nvars, S1, S2, S3);
     const int n1 = g.n[0], n2 = g.n[1], n3 = g.n[2];
     const int f1 = h.fn[0], f2 = h.fn[1], f3 = h.fn[2];
-    T *SB = SA + n1 * n2 * n3;
-    T *SC = SB + f1 * n2 * n3;
+    const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
+    // C takes A's place (A is done with once B is formed), B after the larger
+    T *SC = SA;
+    T *SB = SA + (nA > nC ? nA : nC);
     const int64_t tblock = __ldg(a.tb + tg.x) - 1;
     T *out = scratch + __ldg(a.scr + tg.x) * nvars;
-    const int nA = n1 * n2 * n3, nB = f1 * n2 * n3, nC = f1 * f2 * n3, nO = f1 * f2 * f3;
     // a direct copy (AdjGroup::direct) has no pass-1 work and no scratch:
     // the host leaves it out of the list
     if (h.direct) continue;
@@ -573,8 +574,10 @@ int adjoint_build(const tam_sched *s, AdjHost &o, std::string &err) {
       const DevGroup &g = s->groups[gi];
       const AdjGroup &a = o.ag[gi];
       if (a.direct) continue;  // no pass 1
-      gsm[gi] = (int64_t)g.n[0] * g.n[1] * g.n[2] + (int64_t)a.fn[0] * g.n[1] * g.n[2] +
-                (int64_t)a.fn[0] * a.fn[1] * g.n[2];
+      // the larger of the target box and the second pass (which takes its
+      // place), and the first pass
+      gsm[gi] = std::max((int64_t)g.n[0] * g.n[1] * g.n[2], (int64_t)a.fn[0] * a.fn[1] * g.n[2]) +
+                (int64_t)a.fn[0] * g.n[1] * g.n[2];
       for (int d = 0; d < 3; ++d) {
         gents[gi] += o.off[a.off[d] + a.fn[d]] - o.off[a.off[d]];
         grows[gi] += a.fn[d] + 1;
