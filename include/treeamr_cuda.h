@@ -219,7 +219,12 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
  * has the layout of `work`.  The library allocates its scratch on the
  * first call with a given nvars (so make that call before any stream
  * capture).  A schedule with a turned group (a seam) needs the variable
- * table: use tam_fill_adjoint_ex. */
+ * table: use tam_fill_adjoint_ex.  A stencil transfer's transpose runs in
+ * one CTA's shared memory (its target box, two intermediate boxes and its
+ * transposed stencils); a schedule with a transfer too large for it is
+ * refused with TAM_EUNSUPPORTED on the first call.  In 3-D at order 4 the
+ * largest is an x-face prolongation (G x N x N points): blocks of N up to 56
+ * fit in Float64, up to 80 in Float32. */
 int tam_fill_adjoint(tam_sched *s, void *y, int32_t nvars, int64_t nblocks,
                      const void *factors, int32_t first_stage, int32_t last_stage,
                      void *stream);
