@@ -156,6 +156,52 @@ end
 const UPLOADS = WeakKeyDict{GhostSchedule,DeviceSchedule}()
 device_schedule(s::GhostSchedule) = get!(() -> upload(s), UPLOADS, s)
 
+# Launch options of an uploaded schedule (TAM_OPT_* of include/treeamr_cuda.h):
+# they change how a fill is launched, never its bits.  The reference has no
+# tuning (its device fill is one launch per group).
+const OPTIONS = (tile_items=Int32(1), threads=Int32(2), int_mul=Int32(3), one_tap=Int32(4),
+                 copy_points=Int32(5), block_order=Int32(6), path_tiles=Int32(7),
+                 merge_stages=Int32(8), staged=Int32(9), pair_vars=Int32(10),
+                 copy_share=Int32(11), soft_add=Int32(12), stencil_tile=Int32(13))
+
+function set_option!(schedule::GhostSchedule, name::Symbol, value::Integer)
+    ds = device_schedule(schedule)
+    check(ccall((:tam_schedule_set_option, LIB), Cint, (Ptr{Cvoid}, Int32, Int64),
+                ds.handle, OPTIONS[name], value), ds.ctx, "tam_schedule_set_option")
+    return schedule
+end
+
+function get_option(schedule::GhostSchedule, name::Symbol)
+    ds = device_schedule(schedule)
+    out = Ref{Int64}(0)
+    check(ccall((:tam_schedule_get_option, LIB), Cint, (Ptr{Cvoid}, Int32, Ref{Int64}),
+                ds.handle, OPTIONS[name], out), ds.ctx, "tam_schedule_get_option")
+    return out[]
+end
+
+# The library's autotuner (tam_autotune) on the caller's own field set, whose
+# data should be representative (zeros and specials send the integer-pipe
+# multiplies' points back to the FP64 pipe).  Its fills overwrite the ghosts,
+# never an own point.  Leaves the fastest options set on the schedule and
+# returns them, with the best fill's time in milliseconds.
+function autotune!(fs::FieldSet{T,D,R,<:CuArray}, schedule::GhostSchedule;
+                   reps::Integer=3) where {T,D,R}
+    TreeAMR.check_fill(fs, schedule)
+    ds = device_schedule(schedule)
+    ti, th, im = Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0)
+    ms = Ref{Cdouble}(0)
+    rc = ccall((:tam_autotune, LIB), Cint,
+               (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, Int64, CuPtr{Cvoid}, Int32, Ptr{Cvoid},
+                Ref{Int64}, Ref{Int64}, Ref{Int64}, Ref{Cdouble}),
+               ds.handle, pointer(fs.work), fs.nvars, size(fs.work, ndims(fs.work)),
+               fs.factors === nothing ? CU_NULL : pointer(fs.factors), reps,
+               CUDA.stream().handle, ti, th, im, ms)
+    check(rc, ds.ctx, "tam_autotune")
+    names = keys(OPTIONS)
+    return merge(NamedTuple{names}(map(k -> get_option(schedule, k), names)),
+                 (best_ms=ms[],))
+end
+
 function tam_fill!(fs::FieldSet, ds::DeviceSchedule, first::Int32, last::Int32;
                    plain::Bool=false, factors=fs.factors, rotvars=fs.rotvars, alt=nothing)
     stream = CUDA.stream().handle
