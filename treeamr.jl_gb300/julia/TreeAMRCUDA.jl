@@ -324,6 +324,60 @@ function TreeAMR.exchange_ghosts!(fs::FieldSet{T,D,R,<:CuArray}, schedule::Ghost
     return fs
 end
 
+# unify! of a CuArray field set over a GhostSchedule (src/ghosts.jl:1836-1840,
+# unify_arrays!): stage P, the axis, stage 0, after the reference's checks.
+# The state-vector form and a UnifySchedule stay on the reference's path.
+function TreeAMR.unify!(fs::FieldSet{T,D,R,<:CuArray}, schedule::GhostSchedule) where {T,D,R}
+    TreeAMR.check_fill(fs, schedule)
+    TreeAMR.check_unpartnered(fs, "unify!")
+    ds = device_schedule(schedule)
+    tam_fill!(fs, ds, STAGE_FIRST, Int32(-1))
+    run_axis!(fs.work, fs, schedule)
+    tam_fill!(fs, ds, Int32(0), Int32(0))
+    return fs
+end
+
+# scatter! / gather! of a device-resident state (src/state.jl:101-160)
+# through tam_scatter / tam_gather: one launch each, the state vector read
+# or written linearly, the working array in runs of the own x-extent.
+struct TamStateLayout
+    dtype::Int32
+    ndim::Int32
+    own::NTuple{3,Int32}
+    stored::NTuple{3,Int32}
+    ghosts::NTuple{3,Int32}
+    nvars::Int32
+    nblocks::Int64
+end
+
+function state_layout(fs::FieldSet{T,D}) where {T,D}
+    own = TreeAMR.ownextents(fs)
+    S = size(fs.work)
+    return TamStateLayout(T === Float64 ? TAM_F64 : TAM_F32, D,
+                          ntuple(d -> d <= D ? Int32(own[d]) : Int32(1), 3),
+                          ntuple(d -> d <= D ? Int32(S[d]) : Int32(1), 3),
+                          ntuple(d -> d <= D ? Int32(fs.G[d]) : Int32(0), 3),
+                          fs.nvars, TreeAMR.nblocks(fs))
+end
+
+function TreeAMR.scatter!(fs::FieldSet{T,D,R,<:CuArray}, u::CuVector{T}) where {T,D,R}
+    TreeAMR.check_statelength(u, fs)
+    rc = ccall((:tam_scatter, LIB), Cint,
+               (Ref{TamStateLayout}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}),
+               state_layout(fs), pointer(u), pointer(fs.work), CUDA.stream().handle)
+    check(rc, C_NULL, "tam_scatter")
+    return fs
+end
+
+function TreeAMR.gather!(u::CuVector{T}, fs::FieldSet{T,D,R,<:CuArray}) where {T,D,R}
+    TreeAMR.check_statelength(u, fs)
+    rc = ccall((:tam_gather, LIB), Cint,
+               (Ref{TamStateLayout}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}),
+               state_layout(fs), pointer(fs.work), pointer(u), CUDA.stream().handle)
+    check(rc, C_NULL, "tam_gather")
+    return u
+end
+
 # y <- A^T y over stages [first, last] (tam_fill_adjoint_alt): with the
 # variable table across a seam, and for a pair member the partner's
 # cotangent `alt`, onto which odd turns' transposes add.
