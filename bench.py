@@ -466,7 +466,13 @@ def measure_regrid(dev, timed, args):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms.
+
+    nvidia-smi takes a moment to start, longer than a short timed region, so
+    ``wait_first`` runs the step (untimed) until the first sample is written,
+    and ``hold`` keeps the GPU on the same step after the timed region until
+    the window is long enough for several samples: every sample is taken
+    under the timed work's load."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -475,6 +481,40 @@ class ClockSampler:
         self.index = index
         self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
         self.proc = None
+        self.t0 = None
+        self.before = 0
+        self.held = 0
+
+    def wait_first(self, fn, sync, timeout: float = 3.0, batch: int = 10):
+        """Run ``fn`` in batches of ``batch`` until the first sample is written
+        (or ``timeout`` seconds pass, or nvidia-smi is not running)."""
+        t = time.time()
+        while self.proc is not None and time.time() - t < timeout:
+            if self.proc.poll() is not None:
+                break
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            for _ in range(batch):
+                fn()
+            sync()
+            self.before += batch
+        self.t0 = time.time()
+
+    def hold(self, fn, sync, seconds: float = 1.0, batch: int = 10):
+        """Run ``fn`` (the timed step, untimed here) in batches of ``batch``
+        until ``seconds`` have passed since the load window started."""
+        if self.proc is None:
+            return
+        if self.t0 is None:
+            self.t0 = time.time()
+        while time.time() - self.t0 < seconds:
+            for _ in range(batch):
+                fn()
+            sync()
+            self.held += batch
 
     def __enter__(self):
         try:
@@ -514,8 +554,13 @@ class ClockSampler:
         os.unlink(self.path)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+               "reasons": sorted(reasons)}
+        if self.before or self.held:
+            out["window"] = (f"the timed region, with {self.before} of the same steps before it "
+                             f"and {self.held} after it, untimed, holding its load while "
+                             "nvidia-smi samples")
+        return out
 
 
 def _split(a):
@@ -996,7 +1041,11 @@ def main():
     for _ in range(args.warmup):
         fill_ghosts(fs, sched, method=method)
     with ClockSampler(dev.index) as clk:
-        ms = timed(lambda: fill_ghosts(fs, sched, method=method), args.steps)
+        step = lambda: fill_ghosts(fs, sched, method=method)  # noqa: E731
+        sync = lambda: torch.cuda.synchronize(dev)  # noqa: E731
+        clk.wait_first(step, sync)
+        ms = timed(step, args.steps)
+        clk.hold(step, sync)
     clocks = clk.summary()
     value = world * bytes_per_fill / (ms * 1e-3) / 1e9
     filled = fs.work.cpu().numpy() if rank == 0 else None

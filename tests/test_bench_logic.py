@@ -53,3 +53,46 @@ def test_sector_counts_in_wider_units_are_no_smaller():
         assert b[key] >= a[key], key
     # each written point is in some written sector: the writes cover half the algorithmic bytes
     assert a["sectors_written_bytes"] >= a["algorithmic_bytes"] // 2
+
+
+def test_clock_sampler_holds_the_load_for_its_samples(tmp_path, monkeypatch):
+    """The sampler runs the step until nvidia-smi's first sample is written,
+    keeps running it after the timed region until the window is long enough,
+    and reads clocks and throttle reasons from what nvidia-smi wrote (a fake
+    one here, writing a sample every 50 ms)."""
+    import os
+    import bench
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\nwhile true; do\n"
+                    "  echo '0, 2070, 2070, 901.5, 0x4, Not Active, Not Active, Not Active, Active'\n"
+                    "  sleep 0.05\ndone\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+    calls = {"fn": 0, "sync": 0}
+
+    def fn():
+        calls["fn"] += 1
+
+    def sync():
+        calls["sync"] += 1
+    with bench.ClockSampler(0) as clk:
+        clk.wait_first(fn, sync)
+        clk.hold(fn, sync, seconds=0.4)
+    out = clk.summary()
+    assert out["samples"] >= 3
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"]
+    assert clk.held > 0 and calls["fn"] == clk.before + clk.held
+    assert calls["sync"] * 10 == calls["fn"]
+    assert "window" in out
+
+
+def test_clock_sampler_without_nvidia_smi_runs_nothing(tmp_path, monkeypatch):
+    import bench
+    monkeypatch.setenv("PATH", str(tmp_path))
+    ran = []
+    with bench.ClockSampler(0) as clk:
+        clk.wait_first(lambda: ran.append(1), lambda: None)
+        clk.hold(lambda: ran.append(1), lambda: None)
+    assert not ran
+    assert clk.summary()["reasons"] == ["nvidia-smi unavailable"]
