@@ -479,7 +479,7 @@ class ClockSampler:
 
     def __init__(self, index: int):
         self.index = index
-        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+        self.path = None
         self.proc = None
         self.t0 = None
         self.before = 0
@@ -517,13 +517,15 @@ class ClockSampler:
             self.held += batch
 
     def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
-        except Exception:
-            self.proc = None
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        with os.fdopen(fd, "w") as out:  # the child keeps its own descriptor
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=out, stderr=subprocess.DEVNULL)
+            except Exception:
+                self.proc = None
         return self
 
     def __exit__(self, *exc):
@@ -535,7 +537,9 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if self.proc is None or not os.path.exists(self.path):
+        if self.proc is None or self.path is None or not os.path.exists(self.path):
+            if self.path is not None and os.path.exists(self.path):
+                os.unlink(self.path)
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
