@@ -284,7 +284,7 @@ void build_product_table(const tam_schedule_desc *d, const tam_group &h, tam::De
               out[n++] = p;
             }
   // Float64 products whose significands fit 24 bits take the integer-pipe
-  // multiply (mul_short in tam_kernels.cu); it needs normal nonzero weights.
+  // multiply (mul_short in tam_kernels.cuh); it needs normal nonzero weights.
   g.shortw = 0;
   if (sizeof(T) == 8) {
     bool ok = true;

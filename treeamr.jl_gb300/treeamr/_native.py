@@ -32,8 +32,10 @@ TAM_METHOD_FUSED, TAM_METHOD_PLAIN = 0, 1
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["tam_kernels.cu", "tam_api.cpp", "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu",
-           "tam_state.cu", "tam_boundary.cu", "tam_runtime.cpp"]
+SOURCES = ["tam_fused_f64_d3.cu", "tam_fused_f64_d2.cu", "tam_fused_f64_d1.cu",
+           "tam_fused_f32.cu", "tam_kernels.cu", "tam_api.cpp",
+           "tam_adjoint.cu", "tam_batch.cpp", "tam_wave.cu", "tam_state.cu", "tam_boundary.cu",
+           "tam_runtime.cpp"]
 
 
 class tam_stencil(C.Structure):
@@ -183,7 +185,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with _build_lock:
         os.makedirs(BUILD_DIR, exist_ok=True)
         srcs = [os.path.join(CSRC_DIR, s) for s in SOURCES]
-        hdrs = [os.path.join(CSRC_DIR, "tam_internal.h"), os.path.join(INCLUDE_DIR, "treeamr_cuda.h")]
+        hdrs = [os.path.join(CSRC_DIR, "tam_internal.h"), os.path.join(CSRC_DIR, "tam_kernels.cuh"),
+                os.path.join(INCLUDE_DIR, "treeamr_cuda.h")]
         newest = max(os.path.getmtime(p) for p in srcs + hdrs + [__file__])
         if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
             return LIB_PATH
