@@ -4,7 +4,7 @@ toolchain to run it.  Every struct the shim mirrors has the header's fields in
 the header's order and widths; every ``ccall`` names a declared function with
 its number of arguments, each a pointer where the header has one and a scalar
 of the header's width where it has a scalar; the option codes are the
-header's."""
+header's, in the shim and in the Python host's tables."""
 import os
 import re
 
@@ -184,3 +184,17 @@ def test_option_codes_match_the_header():
 def test_abi_version_matches():
     v = int(re.search(r"#define TAM_ABI_VERSION (\d+)", _header()).group(1))
     assert re.search(r"const TAM_ABI_VERSION = Int32\(%d\)" % v, _shim())
+
+
+def test_python_option_codes_match_the_header():
+    """The Python host's option tables (one schedule's and a batch's, the
+    batch taking a subset) carry the header's codes."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "treeamr.jl_gb300"))
+    from treeamr.batch import ForestBatch
+    from treeamr.ghosts import DeviceSchedule
+    defines = {k.lower(): int(v) for k, v in
+               re.findall(r"#define TAM_OPT_(\w+) (\d+)", _header())}
+    assert DeviceSchedule.OPTIONS == defines
+    assert ForestBatch.OPTIONS.items() <= defines.items()
+    assert set(defines) - set(ForestBatch.OPTIONS) == {"block_order", "merge_stages"}

@@ -161,10 +161,14 @@ class ForestBatch:
             self.ctx, "tam_batch_device_status")
         return code.value
 
+    # the launch options a batch takes (TAM_OPT_*; the block order and stage
+    # groups are a single schedule's)
+    OPTIONS = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
+               "path_tiles": 7, "staged": 9, "pair_vars": 10,
+               "copy_share": 11, "soft_add": 12, "stencil_tile": 13}
+
     def set_option(self, name: str, value: int):
-        code = {"tile_items": 1, "threads": 2, "int_mul": 3, "one_tap": 4, "copy_points": 5,
-                "path_tiles": 7, "staged": 9, "pair_vars": 10,
-                "copy_share": 11, "soft_add": 12, "stencil_tile": 13}[name]
+        code = self.OPTIONS[name]
         _native.check(self.lib.tam_batch_set_option(self.handle, code, int(value)), self.ctx,
                       f"tam_batch_set_option({name})")
         self.options[name] = int(value)
