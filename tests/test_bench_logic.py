@@ -96,3 +96,21 @@ def test_clock_sampler_without_nvidia_smi_runs_nothing(tmp_path, monkeypatch):
         clk.hold(lambda: ran.append(1), lambda: None)
     assert not ran
     assert clk.summary()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_a_failing_side_workload_keeps_the_line():
+    """On one GPU a side workload that raises is recorded as its error; the
+    others and the headline go on.  Under torchrun it raises."""
+    import pytest
+    import bench
+    workloads = {}
+
+    def bad(x):
+        raise MemoryError(f"no room for {x}")
+    bench.run_side(workloads, "good", 1, lambda a, b: a + b, 2, 3)
+    bench.run_side(workloads, "bad", 1, bad, "the batch")
+    assert workloads["good"] == 5
+    assert workloads["bad"] == {"error": "MemoryError: no room for the batch"}
+    with pytest.raises(MemoryError):
+        bench.run_side(workloads, "bad2", 2, bad, "it")
+    assert "bad2" not in workloads
