@@ -22,7 +22,7 @@ the same mesh and data: the reference itself is Julia, which this machine
 does not have.
 
 Launch: ``python bench.py [--gpus N] [--steps K] [--warmup W]``; N > 1 under
-torchrun runs N independent replicas (the path does not shard on one GPU machine).
+torchrun runs N independent replicas, one a GPU (a fill is one forest's, on one GPU).
 """
 from __future__ import annotations
 
