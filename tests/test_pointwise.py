@@ -12,7 +12,9 @@ the primary copy of a shared vertex point), with no schedule at all.
 - The point-by-point fill equals the schedule replay bit for bit on the
   quadrant mesh and on the sphere, walls and batch meshes at reduced size
   (the GPU fill is compared with the point-by-point one at full size in
-  ``test_fullsize.py``).
+  ``test_fullsize.py``), and on 1-D to 3-D layouts, cell- and vertex-centred,
+  periodic or with reflecting and outflow walls, orders 2, 4 and 6, ghost
+  widths 1 to 3.
 - A wrong order or a wrong parity is caught."""
 import numpy as np
 import pytest
@@ -152,3 +154,56 @@ def test_pointwise_comparison_catches_mistakes():
     replay = oracle.fill(s, data.copy(), 8, fs.factors_host, nthreads=8)
     bad = FieldSet(f, 8, G=2, centering=vertexcentered(3), parity=good[::-1])
     assert np.count_nonzero(nanbits(pw.fill(bad, data, 4)) != nanbits(replay)) > 0
+
+
+# ---- more layouts: 1-D to 3-D, cell and vertex, walls, orders 2 to 6 ---------
+
+def _layout(D, vertex, walls, N, G, levels, nvars=2):
+    """A brick of 4 roots a side over the unit box, periodic, or with
+    reflecting low and outflow high faces; ``levels`` passes refining the
+    leaves within a box width of a point off the centre, each balanced.  With
+    walls, variable 2 is odd in dimension 1."""
+    from treeamr import Forest, EvenParity, OddParity
+    kw = dict(N=N, extents=((0.0, 1.0),) * D)
+    if walls:
+        kw.update(reflecting=((True, False),) * D, outflow=((False, True),) * D)
+    else:
+        kw.update(periodic=(True,) * D)
+    f = Forest((4,) * D, **kw)
+    meshes.refine_where(f, _near([(0.3, 0.6, 0.45)[:D]]), range(levels))
+    parity = None
+    if walls:
+        parity = [(EvenParity,) * D,
+                  tuple(OddParity if d == 0 else EvenParity for d in range(D))][:nvars]
+    centering = vertexcentered(D) if vertex else None
+    return FieldSet(f, nvars, G=G, centering=centering, parity=parity, T=np.float64)
+
+
+LAYOUTS = [
+    # D, vertex, walls, N, G, levels, p
+    (1, False, False, 8, 2, 3, 4),
+    (1, False, True, 8, 3, 3, 6),
+    (1, True, False, 8, 2, 3, 4),
+    (1, True, True, 16, 2, 3, 2),
+    (2, False, True, 8, 2, 2, 4),
+    (2, False, False, 8, 1, 2, 2),
+    (2, True, True, 8, 2, 2, 4),
+    (2, True, False, 16, 3, 2, 6),
+    (3, False, True, 8, 2, 2, 4),
+    (3, True, False, 8, 1, 2, 2),
+    (3, True, True, 8, 3, 2, 6),
+    (3, False, False, 8, 2, 3, 4),
+    (2, False, True, 16, 3, 3, 6),
+    (2, True, True, 8, 1, 3, 4),
+    (1, False, False, 16, 1, 4, 2),
+    (1, True, True, 8, 3, 4, 6),
+]
+
+
+@pytest.mark.parametrize("D,vertex,walls,N,G,levels,p", LAYOUTS)
+def test_more_layouts_pointwise_equal_replay(D, vertex, walls, N, G, levels, p):
+    """The schedule of each layout, replayed, equals the point-by-point fill
+    derived from the forest's geometry, bit for bit."""
+    fs = _layout(D, vertex, walls, N, G, levels)
+    assert fs.forest.nleaves() > 4 ** D  # refined somewhere
+    assert _compare(fs, p) == 0
