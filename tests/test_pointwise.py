@@ -170,7 +170,7 @@ def _layout(D, vertex, walls, N, G, levels, nvars=2):
     else:
         kw.update(periodic=(True,) * D)
     f = Forest((4,) * D, **kw)
-    meshes.refine_where(f, _near([(0.3, 0.6, 0.45)[:D]]), range(levels))
+    meshes.refine_where(f, _near([(0.3, 0.6, 0.45)[:D]]), range(levels))  # as rebuilt below
     parity = None
     if walls:
         parity = [(EvenParity,) * D,
@@ -206,4 +206,8 @@ def test_more_layouts_pointwise_equal_replay(D, vertex, walls, N, G, levels, p):
     derived from the forest's geometry, bit for bit."""
     fs = _layout(D, vertex, walls, N, G, levels)
     assert fs.forest.nleaves() > 4 ** D  # refined somewhere
+    brick = pw.Brick((4,) * D, N, (not walls,) * D, ((0.0, 1.0),) * D)
+    point = (0.3, 0.6, 0.45)[:D]
+    _same_forest(fs.forest, pw.rebuild_forest(brick, [(l, _near([point]))
+                                                      for l in range(levels)]))
     assert _compare(fs, p) == 0
