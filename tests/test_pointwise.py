@@ -14,7 +14,9 @@ the primary copy of a shared vertex point), with no schedule at all.
   (the GPU fill is compared with the point-by-point one at full size in
   ``test_fullsize.py``), and on 1-D to 3-D layouts, cell- and vertex-centred,
   periodic or with reflecting and outflow walls, orders 2, 4 and 6, ghost
-  widths 1 to 3.
+  widths 1 to 3; and on 40 seeded random layouts (each dimension periodic
+  or walled, either kind of wall on either side, random parities, Float32
+  or Float64), whose leaves the oracle also rebuilds.
 - A wrong order or a wrong parity is caught."""
 import numpy as np
 import pytest
@@ -211,3 +213,49 @@ def test_more_layouts_pointwise_equal_replay(D, vertex, walls, N, G, levels, p):
     _same_forest(fs.forest, pw.rebuild_forest(brick, [(l, _near([point]))
                                                       for l in range(levels)]))
     assert _compare(fs, p) == 0
+
+
+def _random_layout(rng):
+    """A seeded layout: 1 to 3 dimensions, cell or vertex, each dimension
+    periodic or walled (reflecting or outflow on each side), N 8 or 16, an
+    order of 2, 4 or 6 with the least ghost width it allows (or one more),
+    one to three levels around two random points, random parities."""
+    from treeamr import Forest, EvenParity, OddParity
+    D = int(rng.integers(1, 4))
+    vertex = bool(rng.integers(2))
+    N = int(rng.choice([8, 16]))
+    p = int(rng.choice([2, 4, 6]))
+    periodic = tuple(bool(rng.integers(2)) for _ in range(D))
+    kinds = [tuple(int(rng.integers(2)) for _ in range(2)) for _ in range(D)]
+    reflecting = tuple((k[0] == 0 and not periodic[d], k[1] == 0 and not periodic[d])
+                       for d, k in enumerate(kinds))
+    outflow = tuple((k[0] == 1 and not periodic[d], k[1] == 1 and not periodic[d])
+                    for d, k in enumerate(kinds))
+    G = (max(1, p // 2 - 1) if vertex else p // 2) + int(rng.integers(2))
+    from treeamr.operators import check_operators
+    try:  # a layout the reference refuses (N too small for G and the order)
+        check_operators(N, (G,) * D, (int(vertex),) * D, Operators(prolongation=p, restriction=p))
+    except ValueError:
+        N = 16
+    levels = int(rng.integers(1, 4 if D < 3 else 3))
+    points = [tuple(float(x) for x in rng.uniform(0.05, 0.95, size=D)) for _ in range(2)]
+    f = Forest((4,) * D, N=N, periodic=periodic, reflecting=reflecting, outflow=outflow,
+               extents=((0.0, 1.0),) * D)
+    meshes.refine_where(f, _near(points), range(levels))
+    nvars = 3
+    parity = [tuple(OddParity if rng.integers(2) else EvenParity for _ in range(D))
+              for _ in range(nvars)]
+    fs = FieldSet(f, nvars, G=G, centering=vertexcentered(D) if vertex else None,
+                  parity=parity, T=np.float64 if rng.integers(2) else np.float32)
+    brick = pw.Brick((4,) * D, N, periodic, ((0.0, 1.0),) * D)
+    return fs, p, brick, [(l, _near(points)) for l in range(levels)]
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_random_layouts_pointwise_equal_replay(seed):
+    """Seeded random layouts: the leaves rebuilt independently equal the
+    product's, and the schedule replay equals the point-by-point fill bit for
+    bit."""
+    fs, p, brick, passes = _random_layout(np.random.default_rng(1000 + seed))
+    _same_forest(fs.forest, pw.rebuild_forest(brick, passes))
+    assert _compare(fs, p, seed=seed) == 0
