@@ -215,7 +215,9 @@ int tam_fill_plain(tam_sched *s, void *work, int32_t nvars, int64_t nblocks,
  * fill_ghosts! (src/ghosts.jl:1783) would call for its pullback.  For each
  * stage s, y <- (I - E_s) y + A_s^T E_s y with E_s the stage's targets: the
  * ghosts' adjoints are pushed onto the points their values came from, and
- * the ghosts' own adjoints are zeroed.  Same arguments as tam_fill; `y`
+ * the ghosts' own adjoints are zeroed.  Stage P, which scales each point of
+ * a reflecting wall plane in place by its variable's factor, is diagonal
+ * and its own transpose: it runs as in the fill.  Same arguments as tam_fill; `y`
  * has the layout of `work`.  The library allocates its scratch on the
  * first call with a given nvars (so make that call before any stream
  * capture).  A schedule with a turned group (a seam) needs the variable

@@ -321,12 +321,14 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
 
 /* The transpose of the fill, in scatter form, serial.  Stage s is
  * x <- (I - E_s) x + E_s A_s x, with E_s the projection on its targets and
- * A_s reading only points that are not its targets; its transpose is
- * y <- (I - E_s) y + A_s^T E_s y: every target's adjoint is scattered onto
- * its sources with the transfer's weights, then the targets are zeroed.
+ * A_s reading the stage's sources as they were before it; its transpose is
+ * y <- (I - E_s) y + A_s^T E_s y.  A stage may read its own targets (stage P
+ * scales each wall-plane point in place), so the targets' adjoints are read
+ * first (pass 0), the targets zeroed (pass 1), and then the values read
+ * scattered onto their sources with the transfer's weights (pass 2).
  * Stages run in reverse tag order. */
 #define DEFINE_ADJOINT(T, SUFFIX)                                                               \
-  static void adjoint_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *y,            \
+  static int adjoint_stage_##SUFFIX(const tam_schedule_desc *d, int32_t tag, T *y,            \
                                      T *yalt, int32_t nvars, const T *factors,                  \
                                      const int32_t *rotvars) {                                  \
     const int D = d->ndim;                                                                      \
@@ -334,7 +336,18 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
     for (int k = 0; k < D; ++k) S[k] = d->stored[k];                                            \
     const int64_t s2 = S[0], s3 = S[0] * S[1], vs = S[0] * S[1] * S[2], bs = vs * nvars;        \
     const T *W = (const T *)d->weights;                                                         \
-    for (int pass = 0; pass < 2; ++pass)                                                        \
+    int64_t ntarget = 0;                                                                        \
+    for (int32_t gi = 0; gi < d->ngroups; ++gi) {                                               \
+      const tam_group *g = &d->groups[gi];                                                      \
+      if (g->stage != tag) continue;                                                            \
+      int64_t box = g->ntransfers * nvars;                                                      \
+      for (int k = 0; k < D; ++k) box *= g->stencil[k].ntarget;                                 \
+      ntarget += box;                                                                           \
+    }                                                                                           \
+    T *snap = (T *)malloc((size_t)(ntarget > 0 ? ntarget : 1) * sizeof(T));                    \
+    if (!snap) return -1;                                                                       \
+    for (int pass = 0; pass < 3; ++pass) {                                                      \
+      int64_t k_snap = 0;                                                                       \
       for (int32_t gi = 0; gi < d->ngroups; ++gi) {                                             \
         const tam_group *g = &d->groups[gi];                                                    \
         if (g->stage != tag) continue;                                                          \
@@ -369,11 +382,15 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
                 for (int i1 = 0; i1 < n[0]; ++i1) {                                             \
                   T *yt = y + tb * bs + v * vs + (tf[0] + i1) + (int64_t)(tf[1] + i2) * s2 +    \
                           (int64_t)(tf[2] + i3) * s3;                                           \
+                  if (pass == 0) {                                                              \
+                    snap[k_snap++] = *yt;                                                       \
+                    continue;                                                                   \
+                  }                                                                             \
                   if (pass == 1) {                                                              \
                     *yt = (T)0;                                                                 \
                     continue;                                                                   \
                   }                                                                             \
-                  T a = *yt;                                                                    \
+                  T a = snap[k_snap++];                                                         \
                   if (g->factorcol) a = a * factors[v + (int64_t)nvars * (g->factorcol - 1)];   \
                   int idx[3] = {i1, i2, i3};                                                    \
                   int64_t base[3] = {0, 0, 0};                                                  \
@@ -397,6 +414,9 @@ int oracle_fill(const tam_schedule_desc *d, void *work, int32_t nvars, const voi
                 }                                                                               \
         }                                                                                       \
       }                                                                                         \
+    }                                                                                           \
+    free(snap);                                                                                 \
+    return 0;                                                                                   \
   }
 
 DEFINE_ADJOINT(double, f64)
@@ -416,12 +436,13 @@ int oracle_fill_adjoint_pair(const tam_schedule_desc *d, void *y, void *yalt, in
   int nt = collect_tags(d, tags, 128);
   for (int i = nt - 1; i >= 0; --i) {
     if (tags[i] < first || tags[i] > last) continue;
-    if (d->dtype == TAM_F64)
-      adjoint_stage_f64(d, tags[i], (double *)y, (double *)yalt, nvars, (const double *)factors,
-                        rotvars);
-    else
-      adjoint_stage_f32(d, tags[i], (float *)y, (float *)yalt, nvars, (const float *)factors,
-                        rotvars);
+    const int rc =
+        d->dtype == TAM_F64
+            ? adjoint_stage_f64(d, tags[i], (double *)y, (double *)yalt, nvars,
+                                (const double *)factors, rotvars)
+            : adjoint_stage_f32(d, tags[i], (float *)y, (float *)yalt, nvars,
+                                (const float *)factors, rotvars);
+    if (rc != 0) return rc;
   }
   return 0;
 }

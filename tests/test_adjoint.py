@@ -58,6 +58,22 @@ def test_oracle_dot_product(case):
     assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
 
 
+@pytest.mark.parametrize("seed", range(40))
+def test_oracle_dot_product_random_layouts(seed):
+    """The oracle's scatter-form transpose against its forward fill on the
+    seeded random layouts of the point-by-point tests (1-D to 3-D, cell and
+    vertex, periodic or walled, orders 2 to 6), in Float64."""
+    from test_pointwise import _random_layout
+    fs, p, _, _ = _random_layout(np.random.default_rng(1000 + seed), dtype=np.float64)
+    s = GhostSchedule(fs, Operators(prolongation=p, restriction=p))
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
+    lhs = _dot(_forward(s, fs, x), y)
+    rhs = _dot(x, _adjoint(s, fs, y))
+    assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
+
+
 def test_oracle_dense_transpose_2d():
     """Every entry of A^T from the scatter-form transpose equals the entry of
     A from the forward fill on unit vectors (a tiny 2-D mesh, all columns)."""

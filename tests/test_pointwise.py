@@ -215,7 +215,7 @@ def test_more_layouts_pointwise_equal_replay(D, vertex, walls, N, G, levels, p):
     assert _compare(fs, p) == 0
 
 
-def _random_layout(rng):
+def _random_layout(rng, dtype=None):
     """A seeded layout: 1 to 3 dimensions, cell or vertex, each dimension
     periodic or walled (reflecting or outflow on each side), N 8 or 16, an
     order of 2, 4 or 6 with the least ghost width it allows (or one more),
@@ -247,6 +247,9 @@ def _random_layout(rng):
               for _ in range(nvars)]
     fs = FieldSet(f, nvars, G=G, centering=vertexcentered(D) if vertex else None,
                   parity=parity, T=np.float64 if rng.integers(2) else np.float32)
+    if dtype is not None:  # the same layout in another element type
+        fs = FieldSet(f, nvars, G=G, centering=vertexcentered(D) if vertex else None,
+                      parity=parity, T=dtype)
     brick = pw.Brick((4,) * D, N, periodic, ((0.0, 1.0),) * D)
     return fs, p, brick, [(l, _near(points)) for l in range(levels)]
 

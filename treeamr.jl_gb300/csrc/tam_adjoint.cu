@@ -817,7 +817,12 @@ cudaError_t adjoint_run(tam_sched *s, void *y, void *alt, int nvars, const void 
   AdjRun r{s->dtype, s->D, s->d_groups, s->d_tb, s->d_weights, nullptr, s->d_tiles,
            &s->stages, {s->S[0], s->S[1], s->S[2]}, s->d_solos, rotvars, s->d_err,
            alt ? alt : y};
-  return adjoint_run_plan(s->adj, r, y, nvars, factors, first, last, scratch, stream);
+  // stages from the last down to 0 transposed, then stage P (diagonal) forward
+  const bool p = first <= TAM_STAGE_SELFIMAGE && TAM_STAGE_SELFIMAGE <= last;
+  cudaError_t e = adjoint_run_plan(s->adj, r, y, nvars, factors,
+                                   p ? TAM_STAGE_SELFIMAGE + 1 : first, last, scratch, stream);
+  if (e != cudaSuccess || !p) return e;
+  return fill_one_stage(s, y, nvars, factors, TAM_STAGE_SELFIMAGE, stream);
 }
 
 }  // namespace tam

@@ -689,6 +689,24 @@ void build_solos(tam_sched *s) {
 
 }  // namespace
 
+namespace tam {
+
+cudaError_t fill_one_stage(tam_sched *s, void *work, int nvars, const void *factors,
+                           int32_t tag, cudaStream_t stream) {
+  const SchedArgs args = sched_args(s);
+  for (const Stage &stage : s->stages) {
+    if (stage.tag != tag) continue;
+    if (stage.nsolo > 0) return cudaErrorNotSupported;  // no turned or bounded group here
+    cudaError_t e = launch_fused_stage(s->dtype, s->D, s->d_tiles, s->d_ptiles, stage, args,
+                                       work, factors, nvars, s->S, s->shape.threads, stream,
+                                       &s->side, nullptr, s->d_staged);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace tam
+
 extern "C" {
 
 int tam_abi_version(void) { return TAM_ABI_VERSION; }

@@ -486,12 +486,19 @@ int tam_batch_fill_adjoint_ex(tam_batch *b, void *arena, int64_t arena_elems, in
   const tam::AdjRun r{b->dtype,   b->D,      b->d_groups, b->d_tb,   b->d_weights,
                       b->d_members, b->d_tiles, &b->stages, {1, 1, 1}, b->d_solos,
                       rotvars,     b->d_err,    arena};
-  cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena, first_stage,
-                                        last_stage, b->adj_scratch, (cudaStream_t)stream);
+  // stages from the last down to 0 transposed, then stage P forward: it
+  // scales each wall-plane point in place, a diagonal map, its own transpose
+  const bool p = first_stage <= TAM_STAGE_SELFIMAGE && TAM_STAGE_SELFIMAGE <= last_stage;
+  cudaError_t e = tam::adjoint_run_plan(b->adj, r, arena, nvars, factor_arena,
+                                        p ? TAM_STAGE_SELFIMAGE + 1 : first_stage, last_stage,
+                                        b->adj_scratch, (cudaStream_t)stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return bfail(b->ctx, TAM_ECUDA, std::string("batch adjoint launch: ") + cudaGetErrorString(e));
   }
+  if (p)
+    return tam_batch_fill_ex(b, arena, arena_elems, nvars, factor_arena, factor_elems, rotvars,
+                             TAM_STAGE_SELFIMAGE, TAM_STAGE_SELFIMAGE, stream);
   return TAM_OK;
 }
 

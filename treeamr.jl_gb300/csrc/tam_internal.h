@@ -423,7 +423,17 @@ cudaError_t launch_selftest_mul_full(int64_t n, uint64_t seed, unsigned long lon
 cudaError_t launch_selftest_add(int64_t n, uint64_t seed, unsigned long long *mismatches,
                                 cudaStream_t stream);
 
-// The adjoint (tam_adjoint.cu).
+// The forward fill of the one stage `tag` of `s` on `work`, its fused
+// launches as tam_fill runs them (tam_api.cpp); a stage with turned or
+// bounded groups is refused (cudaErrorNotSupported).
+cudaError_t fill_one_stage(tam_sched *s, void *work, int nvars, const void *factors,
+                           int32_t tag, cudaStream_t stream);
+
+// The adjoint (tam_adjoint.cu).  Stage P (TAM_STAGE_SELFIMAGE) scales each
+// point of a reflecting wall plane in place by its variable's factor, a
+// diagonal map and so its own transpose: the adjoint runs it forward, since
+// the transposed passes (which zero a stage's targets after adding onto its
+// sources) assume a stage reads none of its own targets.
 int adjoint_prepare(tam_sched *s, std::string &err);
 void adjoint_free(tam_sched *s);
 // `alt`: the array odd turns read in the forward fill (a RotationPair's
