@@ -74,6 +74,41 @@ def test_oracle_dot_product_random_layouts(seed):
     assert abs(lhs - rhs) <= 1e-13 * max(abs(lhs), abs(rhs))
 
 
+@pytest.mark.parametrize("seed", range(16))
+def test_oracle_dot_product_random_conservative_layouts(seed):
+    """The conservative family (odd prolongation orders, the exact volume
+    average as restriction) on seeded random cell-centred layouts: periodic
+    or walled dimensions, random parities.  The tolerance is relative to the
+    sum of the products' magnitudes, which the rounding of a dot product
+    scales with."""
+    from test_pointwise import _near
+    from treeamr.operators import Conservative
+    rng = np.random.default_rng(9000 + seed)
+    D, N, p = int(rng.integers(1, 4)), int(rng.choice([8, 16])), int(rng.choice([1, 3, 5]))
+    periodic = tuple(bool(rng.integers(2)) for _ in range(D))
+    kinds = [tuple(int(rng.integers(2)) for _ in range(2)) for _ in range(D)]
+    refl = tuple((k[0] == 0 and not periodic[d], k[1] == 0 and not periodic[d])
+                 for d, k in enumerate(kinds))
+    outf = tuple((k[0] == 1 and not periodic[d], k[1] == 1 and not periodic[d])
+                 for d, k in enumerate(kinds))
+    G = (p - 1) // 2 + int(rng.integers(1, 3))
+    levels = int(rng.integers(1, 4 if D < 3 else 3))
+    pts = [tuple(float(x) for x in rng.uniform(0.05, 0.95, size=D)) for _ in range(2)]
+    f = Forest((4,) * D, N=N, periodic=periodic, reflecting=refl, outflow=outf,
+               extents=((0.0, 1.0),) * D)
+    meshes.refine_where(f, _near(pts), range(levels))
+    par = [tuple(OddParity if rng.integers(2) else EvenParity for _ in range(D))
+           for _ in range(2)]
+    fs = FieldSet(f, 2, G=G, parity=par, T=np.float64)
+    s = GhostSchedule(fs, Operators(prolongation=p, restriction=2, family=Conservative))
+    r = np.random.default_rng(seed)
+    x = r.uniform(-1, 1, size=tuple(fs.work.shape))
+    y = r.uniform(-1, 1, size=tuple(fs.work.shape))
+    ax = _forward(s, fs, x)
+    lhs, rhs = _dot(ax, y), _dot(x, _adjoint(s, fs, y))
+    assert abs(lhs - rhs) <= 1e-15 * _dot(np.abs(ax), np.abs(y))
+
+
 def test_oracle_dense_transpose_2d():
     """Every entry of A^T from the scatter-form transpose equals the entry of
     A from the forward fill on unit vectors (a tiny 2-D mesh, all columns)."""
