@@ -316,3 +316,58 @@ def test_gpu_regrid_keeps_evolved_values(cuda_lib):
     regrid(gs, ops, refine=[k for k in g.leaves if k.level == 0])
     torch.cuda.synchronize()
     assert np.array_equal(nanbits(gs.work.cpu().numpy()), nanbits(moved))
+
+
+def _random_grown(D, seed):
+    """A brick of 3^D roots on (0, 3)^D, one or two passes refining a seeded
+    third of the leaves, each balanced."""
+    rng = np.random.default_rng(seed)
+    f = Forest((3,) * D, N=8, periodic=(False,) * D, extents=[(0.0, 3.0)] * D)
+    for _ in range(int(rng.integers(1, 3))):
+        pick = [k for k in f.leaves if rng.random() < 0.3]
+        if pick:
+            f.refine(pick)
+            f.balance()
+    return f
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_oracle_regrid_random_moves(seed):
+    """Seeded regrids: a random forest, then a random set of complete
+    families coarsened and of leaves refined, and balance.  The transfer of
+    degree p-1 data is exact at every own point of every new block (cell or
+    vertex sets, orders 2 and 4, 1-D to 3-D), and kept blocks keep their own
+    points bit for bit."""
+    rng = np.random.default_rng(7000 + seed)
+    D, p, vertex = int(rng.integers(1, 4)), int(rng.choice([2, 4])), bool(rng.integers(2))
+    grow = int(rng.integers(1 << 30))
+    f, f_old = _random_grown(D, grow), _random_grown(D, grow)
+    old = list(f.leaves)
+    assert list(f_old.leaves) == old
+    children = {}
+    for k in old:
+        if k.level > 0:
+            children.setdefault(parentkey(k), []).append(k)
+    families = [q for q, ch in children.items() if len(ch) == 2 ** D]
+    coarse = [q for q in families if rng.random() < 0.4]
+    if coarse:
+        f.coarsen(coarse)
+    fine = [k for k in f.leaves if k not in set(coarse) and rng.random() < 0.15]
+    if fine:
+        f.refine(fine)
+    f.balance()
+    C = ("vertex",) * D if vertex else ("cell",) * D
+    poly = makepoly(D, p - 1)
+    fs_old = FieldSet(f_old, 2, G=2, centering=C)
+    fs_new = FieldSet(f, 2, G=2, centering=C)
+    old_host = exact_values(fs_old, poly)
+    want = exact_values(fs_new, poly)
+    t = RegridTransfer(f, old, (2,) * D, C, np.float64, Operators(prolongation=p, restriction=p))
+    got = oracle_regrid(t, old_host, np.full(tuple(fs_new.work.shape), np.nan), 2)
+    own = (slice(None), slice(None)) + tuple(slice(2, 10 + int(vertex)) for _ in range(D))
+    assert not np.isnan(got[own]).any()
+    assert np.max(np.abs(got[own] - want[own])) < 1e-9
+    index = {k: i for i, k in enumerate(old)}
+    for b, k in enumerate(f.leaves):
+        if k in index:
+            assert np.array_equal(got[(b,) + own[1:]], old_host[(index[k],) + own[1:]])
