@@ -234,3 +234,40 @@ def test_gpu_unify_with_a_ghost_schedule(cuda_lib):
     unify(fs, s)
     torch.cuda.synchronize()
     assert np.array_equal(fs.work.cpu().numpy(), expect)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_unify_random_forests(seed):
+    """The interface restriction on seeded random forests (2 or 3 roots a
+    side, each dimension periodic or not, one to three passes refining a
+    random quarter of the leaves, balanced), for every interface centering
+    of the dimension and G = 0, 1: each coarse copy is the fine mean, and
+    nothing else moves."""
+    from treeamr import Forest
+    rng = np.random.default_rng(8000 + seed)
+    D, roots = int(rng.integers(1, 4)), int(rng.integers(2, 4))
+    periodic = tuple(bool(rng.integers(2)) for _ in range(D))
+    forest = Forest((roots,) * D, N=8, periodic=periodic, extents=[(0.0, float(roots))] * D)
+    for _ in range(int(rng.integers(1, 4 if D < 3 else 3))):
+        pick = [k for k in forest.leaves if rng.random() < 0.25]
+        if pick:
+            forest.refine(pick)
+            forest.balance()
+    geo = Geometry(forest)
+    for C in interface_cases(D):
+        for G in (0, 1):
+            fs = FieldSet(forest, 2, G=G, centering=C)
+            host = np.full(tuple(fs.work.shape), np.nan)
+            fill_arbitrary(fs, host, geo)
+            expected = interface_targets(fs, closed_values(fs, host, geo), geo)
+            out = _unified(fs, UnifySchedule(fs), host)
+            targets = set()
+            for (b, I), want in expected.items():
+                sl = tuple(i - 1 for i in reversed(I))
+                assert np.max(np.abs(out[(b, slice(None)) + sl] - want)) <= \
+                    4 * np.finfo(np.float64).eps
+                targets.add((b,) + sl)
+            mask = np.ones(out.shape, bool)
+            for t in targets:
+                mask[(t[0], slice(None)) + t[1:]] = False
+            assert np.array_equal(nanbits(out[mask]), nanbits(host[mask]))
