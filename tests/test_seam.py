@@ -472,9 +472,12 @@ SEAM_CASES = [(2, (1, 2), "none"), (2, (2, 1), "none"), (3, (1, 2), "periodic"),
               (3, (2, 1), "reflect_lo"), (3, (3, 1), "outer")]
 HALF_CASES = [(2, (1, 2), "none"), (2, (2, 1), "none"), (3, (1, 2), "periodic"),
               (3, (3, 2), "reflect_lo")]
+# more planes and faces, checked with the oracle on the CPU
+MORE_SEAM_CASES = [(3, (1, 3), "outer"), (3, (3, 2), "reflect_lo")]
+MORE_HALF_CASES = [(3, (2, 3), "reflect_lo"), (3, (3, 1), "periodic")]
 
 
-@pytest.mark.parametrize("D,plane,other", SEAM_CASES)
+@pytest.mark.parametrize("D,plane,other", SEAM_CASES + MORE_SEAM_CASES)
 def test_a_rotating_quadrant_is_the_turned_full_plane(D, plane, other):
     """``test/rotate_tests.jl:437-456`` and ``:399-435``: every stored point
     of the quadrant after the fill, ghosts included, is the full plane's at
@@ -494,7 +497,7 @@ def test_a_rotating_quadrant_is_the_turned_full_plane(D, plane, other):
     assert not np.isnan(got).any()
 
 
-@pytest.mark.parametrize("D,plane,other", HALF_CASES)
+@pytest.mark.parametrize("D,plane,other", HALF_CASES + MORE_HALF_CASES)
 def test_a_half_plane_is_the_turned_full_plane(D, plane, other):
     """``test/halfturn_tests.jl:349-377``."""
     quad, fs, s, full, ff, image = quadrant_case(D, plane, other, half=True)
@@ -824,7 +827,8 @@ def _dot(a, b):
     return float(np.dot(a.ravel().astype(np.float64), b.ravel().astype(np.float64)))
 
 
-@pytest.mark.parametrize("case", [("q",) + c for c in SEAM_CASES[:4]] +
+@pytest.mark.parametrize("case", [("q",) + c for c in SEAM_CASES[:4] + MORE_SEAM_CASES] +
+                         [("h",) + c for c in MORE_HALF_CASES] +
                          [("h",) + c for c in HALF_CASES[:3]])
 def test_oracle_adjoint_dot_product_across_the_seam(case):
     """``<A x, y> = <x, A^T y>`` to 1e-13 with turned transfers, A the
@@ -892,6 +896,10 @@ def test_gpu_adjoint_of_a_pair_member_is_refused(cuda_lib):
 VERTEX_CASES = [("q", 2, (1, 2), "none"), ("q", 2, (2, 1), "none"),
                 ("q", 3, (1, 2), "periodic"), ("q", 3, (3, 1), "outer"),
                 ("h", 2, (1, 2), "none"), ("h", 3, (1, 2), "periodic")]
+# checked with the oracle on the CPU: a reflecting low face beside the seam
+# puts stage P (an odd and an even variable across the wall) into the fill
+MORE_VERTEX_CASES = [("q", 3, (1, 2), "reflect_lo"), ("h", 3, (3, 2), "reflect_lo"),
+                     ("q", 3, (2, 3), "outer"), ("h", 3, (1, 3), "periodic")]
 
 
 def _centering(D, plane, which):
@@ -902,7 +910,7 @@ def _centering(D, plane, which):
     return tuple("vertex" if d + 1 in plane else "cell" for d in range(D))
 
 
-@pytest.mark.parametrize("case", VERTEX_CASES)
+@pytest.mark.parametrize("case", VERTEX_CASES + MORE_VERTEX_CASES)
 @pytest.mark.parametrize("which", ["vertex", "plane"])
 def test_a_vertex_like_quadrant_is_the_turned_full_plane(case, which):
     """``test/rotate_tests.jl:437-456`` for vertex-like sets: the seam
@@ -978,7 +986,7 @@ def oracle_vertex_adjoint(s, fs, y):
     return oracle.fill_adjoint(s, y, fs.nvars, fs.factors_host, last=-1, rotvars=rv)
 
 
-@pytest.mark.parametrize("case", VERTEX_CASES)
+@pytest.mark.parametrize("case", VERTEX_CASES + MORE_VERTEX_CASES)
 def test_oracle_adjoint_dot_product_across_a_vertex_seam(case):
     """``<A x, y> = <x, A^T y>`` to 1e-13 where the fill holds the axis
     projection between stage P and stage 0, and the projection of the
