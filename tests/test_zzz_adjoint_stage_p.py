@@ -25,13 +25,13 @@ def _dot(a, b):
     return float(np.dot(a.ravel().astype(np.float64), b.ravel().astype(np.float64)))
 
 
-def _plane_case():
-    """2-D, 2 x 2 roots, N = 4, G = 1: periodic along x, a reflecting low and
-    an outflow high face along y; a variable odd in both dimensions and one
-    even in both."""
+def _plane_case(G=1):
+    """2-D, 2 x 2 roots, N = 4: periodic along x, a reflecting low and an
+    outflow high face along y; a variable odd in both dimensions and one even
+    in both."""
     f = Forest((2, 2), N=4, periodic=(True, False), reflecting=((False, False), (True, False)),
                outflow=((False, False), (False, True)), extents=((0.0, 1.0),) * 2)
-    fs = FieldSet(f, 2, G=1, centering=vertexcentered(2),
+    fs = FieldSet(f, 2, G=G, centering=vertexcentered(2),
                   parity=[(OddParity, OddParity), (EvenParity, EvenParity)], T=np.float64)
     return fs, GhostSchedule(fs, Operators(prolongation=2, restriction=2))
 
@@ -60,7 +60,7 @@ def _dense(fs, s, first=oracle.ALL_FIRST, last=oracle.ALL_LAST):
 
 
 def test_stage_p_is_there_with_even_and_odd_variables():
-    for fs, s in (_plane_case(), _walls_case()):
+    for fs, s in (_plane_case(), _plane_case(G=2), _walls_case()):
         assert any(g.stage == -1 for g in s.groups)
 
 
@@ -91,7 +91,7 @@ def test_oracle_dot_product_walls_layout():
 @pytest.mark.parametrize("case", ["plane", "walls"])
 def test_gpu_adjoint_with_stage_p(cuda_lib, case):
     from treeamr.adjoint import fill_ghosts_adjoint
-    fs, s = _plane_case() if case == "plane" else _walls_case()
+    fs, s = _plane_case(G=2) if case == "plane" else _walls_case()
     rng = np.random.default_rng(5)
     x = rng.uniform(-1, 1, size=tuple(fs.work.shape))
     y = rng.uniform(-1, 1, size=tuple(fs.work.shape))
