@@ -567,6 +567,34 @@ class ClockSampler:
         return out
 
 
+def dot_test(work, fill, adjoint, seed: int) -> dict:
+    """<A x, y> = <x, A^T y> with x and y seeded uniform over the whole array:
+    ``fill(work)`` applies A to ``work`` in place and ``adjoint(t)`` applies
+    A^T to ``t`` in place.  Each inner product is summed in float64 chunks,
+    the chunks summed exactly.  ``work`` keeps its contents."""
+    import math
+    import torch
+    keep = work.clone()
+    g = torch.Generator(device=work.device).manual_seed(seed)
+    x = torch.empty_like(work).uniform_(-1.0, 1.0, generator=g)
+    y = torch.empty_like(work).uniform_(-1.0, 1.0, generator=g)
+    work.copy_(x)
+    fill(work)
+    aty = y.clone()
+    adjoint(aty)
+
+    def dot(a, b):
+        a, b = a.reshape(-1), b.reshape(-1)
+        step = 1 << 22
+        return math.fsum(float(torch.dot(a[i:i + step].double(), b[i:i + step].double()))
+                         for i in range(0, a.numel(), step))
+    lhs, rhs = dot(work, y), dot(x, aty)
+    work.copy_(keep)
+    bound = 1e-13 if work.dtype == torch.float64 else 1e-5
+    return {"lhs": lhs, "rhs": rhs,
+            "relative_residual": abs(lhs - rhs) / max(abs(lhs), abs(rhs)), "bound": bound}
+
+
 def run_side(workloads: dict, name: str, world: int, fn, *args):
     """``workloads[name] = fn(*args)``.  On one GPU a side workload that raises
     records its error in the line instead of costing the headline; under
@@ -1097,6 +1125,13 @@ def main():
         adj_stage_ms.setdefault(str(tag), []).append(a.elapsed_time(b))
     adj_stage_ms = {k: statistics.mean(v) for k, v in adj_stage_ms.items()}
     del yadj
+    # and its dot-product test at full size (the field data kept)
+    try:
+        adj_dot = dot_test(fs.work, lambda t: fill_ghosts(fs, sched, method=method),
+                           lambda t: fill_ghosts_adjoint(fs, sched, t), 22)
+    except Exception as e:  # noqa: BLE001
+        adj_dot = {"error": f"{type(e).__name__}: {e}"}
+    torch.cuda.empty_cache()
 
     stage_ms, stage_bytes = stage_times(ds, fs, sched, stream, dev, max(3, args.steps // 2))
     kern_ms = sum(statistics.mean(v) for v in stage_ms.values())
@@ -1165,7 +1200,7 @@ def main():
                       "ms_per_step": ms_plain, "speedup_fused_vs_plain": ms_plain / ms},
             "adjoint": {"value": world * bytes_per_fill / (ms_adj * 1e-3) / 1e9, "unit": UNIT,
                         "ms_per_step": ms_adj, "time_vs_forward": ms_adj / ms,
-                        "stage_ms": adj_stage_ms},
+                        "stage_ms": adj_stage_ms, "dot_test": adj_dot},
             "throughput": throughput,
             "error": error,
             "workloads": workloads,

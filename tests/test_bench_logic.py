@@ -114,3 +114,26 @@ def test_a_failing_side_workload_keeps_the_line():
     with pytest.raises(MemoryError):
         bench.run_side(workloads, "bad2", 2, bad, "it")
     assert "bad2" not in workloads
+
+
+def test_dot_test_helper_on_a_matrix():
+    """The bench's dot-product test on a dense map and its transpose: a
+    residual at rounding, the array's contents kept; a wrong transpose is
+    caught."""
+    import torch
+    import bench
+    n = 64
+    g = torch.Generator().manual_seed(0)
+    A = torch.randn(n, n, dtype=torch.float64, generator=g)
+    work = torch.randn(n, dtype=torch.float64, generator=g)
+    before = work.clone()
+
+    def fill(t):
+        t.copy_(A @ t)
+
+    def adjoint(t):
+        t.copy_(A.T @ t)
+    out = bench.dot_test(work, fill, adjoint, 3)
+    assert out["relative_residual"] < 1e-13 and out["bound"] == 1e-13
+    assert torch.equal(work, before)
+    assert bench.dot_test(work, fill, fill, 3)["relative_residual"] > 1e-6
