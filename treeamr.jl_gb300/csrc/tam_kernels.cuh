@@ -1303,8 +1303,8 @@ cudaError_t launch_both(const Tile *tiles, const PTile *ptiles, const Stage &stg
 }
 
 // A stage: its unit copies and its stencils, two launches with no
-// dependency between them (their targets are disjoint and neither reads a
-// point of the stage's targets).
+// dependency between them (their targets are disjoint, and no transfer reads
+// another's targets: a stage-P copy reads only the point it writes).
 template <typename T>
 cudaError_t fused_dispatch(int D, const Tile *tiles, const PTile *ptiles, const Stage &st,
                            const Args<T> &a, const T *src, T *work, const T *factors, int nvars,
