@@ -305,3 +305,47 @@ def test_gpu_prescribed_wall_bit_exact(cuda_lib, D, T):
             torch.cuda.synchronize()
             assert np.array_equal(nanbits(fs.work.cpu().numpy()), nanbits(expect)), (C, g)
             fs.factors = fs.factors.cpu()
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_polynomial_hook_keeps_random_fills_exact(seed):
+    """Seeded random layouts with outer faces everywhere (1-D to 3-D, cell or
+    vertex sets, orders 2 and 4, one or two levels around two random
+    points): with polynomial data of degree p-1 (at most 2) and the same
+    polynomial as the hook, between phase 1 and the prolongations, the
+    oracle's fill is exact at every point, ghosts past the outer faces
+    included."""
+    from test_pointwise import _near
+    from treeamr import Forest, meshes
+    rng = np.random.default_rng(6100 + seed)
+    D, vertex, p = int(rng.integers(1, 4)), bool(rng.integers(2)), int(rng.choice([2, 4]))
+    f = Forest((3,) * D, N=8, periodic=(False,) * D, extents=((0.0, 1.0),) * D)
+    pts = [tuple(float(x) for x in rng.uniform(0.05, 0.95, size=D)) for _ in range(2)]
+    meshes.refine_where(f, _near(pts), range(int(rng.integers(1, 3))))
+    fs = FieldSet(f, 1, G=2, centering=vertexcentered(D) if vertex else None)
+    s = GhostSchedule(fs, Operators(prolongation=p, restriction=p))
+    assert s.boundaries
+    terms = {(0,) * D: [0.5]}
+    for d in range(D):
+        e = [0] * D
+        e[d] = 1
+        terms[tuple(e)] = [0.25 * (d + 1)]
+    quad = 0.125 if p == 4 else 0.0
+    if quad:
+        e = [0] * D
+        e[0] = 2
+        terms[tuple(e)] = [quad]
+
+    def exact(x):
+        return 0.5 + sum(0.25 * (d + 1) * x[d] for d in range(D)) + quad * x[0] ** 2
+    host = np.zeros(tuple(fs.work.shape))
+    for b in range(fs.nblocks()):
+        grids = np.meshgrid(*fs.positions(b), indexing="ij")
+        host[b, 0] = np.transpose(exact(grids))
+    filled = host.copy()
+    filled[:, :, ghost_mask(fs)] = np.nan
+    out = oracle.fill(s, filled, fs.nvars, fs.factors_host, last=PHASE1_TAG)
+    oracle.cell_boundary(fs, out, s.boundaries, Polynomial(terms))
+    out = oracle.fill(s, out, fs.nvars, fs.factors_host, first=PHASE1_TAG + 1)
+    assert not np.isnan(out).any()
+    assert np.max(np.abs(out - host)) < 1e-10
