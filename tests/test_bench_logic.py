@@ -137,3 +137,46 @@ def test_dot_test_helper_on_a_matrix():
     assert out["relative_residual"] < 1e-13 and out["bound"] == 1e-13
     assert torch.equal(work, before)
     assert bench.dot_test(work, fill, fill, 3)["relative_residual"] > 1e-6
+
+
+def test_written_sector_counts_equal_the_oracles_writes():
+    """The layout's written and partly written sectors, counted by the bench
+    from the schedule, equal a brute-force count of the points each stage of
+    the oracle's fill actually writes (its targets set to NaN after the
+    earlier stages, every one a number afterwards), per variable plane as the
+    bench counts them, in 32- and 64-byte units, on a small walls mesh."""
+    import oracle
+    import bench
+    from treeamr import FieldSet, Operators
+    from treeamr.storage import vertexcentered
+    f = meshes.walls_forest(roots=2, N=8, levels=2)
+    fs = FieldSet(f, 2, G=2, centering=vertexcentered(3), parity=meshes.walls_parities()[:2],
+                  T=np.float64)
+    s = GhostSchedule(fs, Operators(prolongation=4, restriction=4))
+    shape, tags = tuple(fs.work.shape), sorted({g.stage for g in s.groups})
+    for tag in tags:
+        host = np.random.default_rng(0).uniform(1, 2, size=shape)
+        prev = [t for t in tags if t < tag]
+        if prev:
+            host = oracle.fill(s, host, fs.nvars, fs.factors_host, first=prev[0], last=prev[-1])
+        for g in s.groups:
+            if g.stage == tag:
+                sl = tuple(slice(st.targetfirst - 1, st.targetfirst - 1 + st.ntarget)
+                           for st in reversed(g.stencils))
+                for tb in g.targetblocks:
+                    host[(tb - 1, slice(None)) + sl] = np.nan
+        before = np.isnan(host)
+        out = oracle.fill(s, host, fs.nvars, fs.factors_host, first=tag, last=tag)
+        assert not np.isnan(out).any()
+        for unit in (32, 64):
+            m = bench.sector_minimum(s, fs.nvars, 8, tag, stencils=True, unit=unit)
+            written = partial = 0
+            for v in range(fs.nvars):
+                mask = np.zeros(shape, bool)
+                mask[:, v] = before[:, v]
+                sec, cnt = np.unique(np.flatnonzero(mask.ravel()) * 8 // unit,
+                                     return_counts=True)
+                written += sec.size
+                partial += int((cnt < unit // 8).sum())
+            assert m["sectors_written_bytes"] == written * unit, (tag, unit)
+            assert m["partly_written_bytes"] == partial * unit, (tag, unit)
